@@ -1,0 +1,265 @@
+/*
+ * dem_gb300.h — C ABI of libdem_sm100a.so, the GB300 (sm_103a) DEM time step.
+ *
+ * This boundary replaces the device-side half of the reference package DEMPort
+ * (lucifer1004/taichi_dem_julia_port): the `GlobalData` device state
+ * (src/executor.jl:1-29), `initialize!` (src/executor.jl:155-160), `simulate!`
+ * (src/executor.jl:162-172) and the per-scene setup that `solve` performs before
+ * its loop (src/executor.jl:217-340).  A host front end (the Python package
+ * `taichi_dem_julia_port_gb300`, or a Julia `ccall` shim) keeps the reference's
+ * TOML config, p4p/p4c files and step loop and calls these entry points.
+ *
+ * Conventions
+ *  - Every function returns an int status: DEM_OK (0) or a DEM_ERR_* code.
+ *  - The library owns all device memory; the caller owns every host buffer.
+ *  - Host arrays of 3-vectors are interleaved (x0,y0,z0,x1,...), length 3*n.
+ *    Quaternions are (w,x,y,z), length 4*n.
+ *  - Particle indices are 0-based (reference index - 1).  Values that the
+ *    reference computes as 1-based quantities (cell ijk, Morton code,
+ *    hash-table bucket) are returned with the reference's own values.
+ *  - One host thread per handle.  Each handle has its own CUDA stream; calls
+ *    on one handle are ordered on that stream.
+ */
+#ifndef DEM_GB300_H
+#define DEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define DEM_OK 0
+#define DEM_ERR_INVALID 1   /* bad argument or state                          */
+#define DEM_ERR_CUDA 2      /* a CUDA runtime call failed                     */
+#define DEM_ERR_CAPACITY 3  /* a contact / pair buffer would overflow         */
+#define DEM_ERR_TIMEOUT 4   /* a bounded device-side wait gave up             */
+#define DEM_ERR_NO_DEVICE 5 /* no usable sm_103 device                        */
+#define DEM_ERR_RANGE 6     /* a particle left the 10-bit Morton cell range   */
+
+/* ---- precision modes (dem_set_precision) ------------------------------- */
+#define DEM_FP64 0       /* every force in FP64 (the reference's arithmetic)  */
+#define DEM_FP32_FORCE 1 /* Hertz-Mindlin/EBPM force evaluation in FP32; state,
+                            integration, shear history and the bond-breakage
+                            test stay FP64                                     */
+
+/* ---- contact flags ----------------------------------------------------- */
+#define DEM_CONTACT_ACTIVE 1u /* reference BitTable `contact_active`          */
+#define DEM_CONTACT_BONDED 2u /* reference BitTable `contact_bonded`          */
+
+/*
+ * The 32 numeric keys of `DEMConfig` (src/config.jl:3-43), same names and
+ * meaning.  The 33rd key, `init_particles`, is a file name that the host front
+ * end resolves and passes as DemParticlesIn.
+ */
+typedef struct DemConfigC {
+    double domain_min[3];
+    double domain_max[3];
+    double particle_contact_radius_multiplier;
+    double neighboring_search_safety_factor;
+    double particle_elastic_modulus;
+    double particle_poisson_ratio;
+    double wall_normal[3];
+    double wall_distance;
+    double wall_density;
+    double wall_elastic_modulus;
+    double wall_poisson_ratio;
+    double bond_radius_ratio;
+    double bond_elastic_modulus;
+    double bond_poisson_ratio;
+    double bond_compressive_strength;
+    double bond_tensile_strength;
+    double bond_shear_strength;
+    double pp_coefficient_friction;
+    double pp_coefficient_restitution;
+    double pp_coefficient_rolling_resistance; /* declared, unused (as in the reference) */
+    double pw_coefficient_friction;
+    double pw_coefficient_restitution;
+    double pw_coefficient_rolling_resistance; /* declared, unused (as in the reference) */
+    int64_t max_coordinate_number;
+    int64_t collision_pair_init_capacity_factor;
+    double tolerance;
+    int64_t max_particle_count;
+    double gravity[3];
+    double global_damping;
+    double dt;
+    double target_time;
+    double saving_interval_time;
+} DemConfigC;
+
+/* The p4p columns that `solve` reads per grain (src/executor.jl:219-243). */
+typedef struct DemParticlesIn {
+    int64_t n;
+    const int32_t* id;     /* ID column                       */
+    const int32_t* gid;    /* GROUP column                    */
+    const double* volume;  /* VOLUME column (n)               */
+    const double* mass;    /* MASS column (n)                 */
+    const double* pos;     /* PX PY PZ (3n)                   */
+    const double* vel;     /* VX VY VZ (3n)                   */
+} DemParticlesIn;
+
+/* Dynamic particle state (the mutable fields of `Grain`, src/types.jl:46-61,
+ * plus the `forces`/`moments` arrays and the wall shear history of
+ * `GlobalData`).  Any pointer may be NULL to skip that field. */
+typedef struct DemParticleState {
+    int64_t n;
+    double* pos;        /* 3n  𝐤                                         */
+    double* vel;        /* 3n  𝐯                                         */
+    double* omega;      /* 3n  𝛚                                         */
+    double* quat;       /* 4n  𝐪 (w,x,y,z)                               */
+    double* force;      /* 3n  total force of the last step (get only)    */
+    double* moment;     /* 3n  total moment of the last step (get only)   */
+    double* wall_shear; /* 3n  𝐬 of wall_contacts[1, i]                  */
+} DemParticleState;
+
+/* Static per-particle data derived at setup (src/executor.jl:223-242). */
+typedef struct DemParticleStatic {
+    int64_t n;
+    double* radius;   /* r = ∛(V / (4/3 π))      */
+    double* radius0;  /* r₀ = r · multiplier     */
+    double* mass;     /* m                       */
+    double* inertia;  /* 2/5 m r² (diagonal of 𝐈) */
+} DemParticleStatic;
+
+/* Active contacts (the reference's `contacts[1:contact_ptr[1]]` filtered by
+ * the `contact_active` bit, src/utils.jl:53-69).  Arrays hold `cap` entries. */
+typedef struct DemContacts {
+    int32_t* i;        /* owner particle, i < j      */
+    int32_t* j;
+    uint8_t* bonded;   /* 1 = EBPM bond, 0 = Hertz-Mindlin */
+    double* point;     /* 3 per contact, 𝐤 (contact position)   */
+    double* force;     /* 3 per contact, 𝐅ᵢ in the local frame  */
+    double* torque_i;  /* 3 per contact, 𝛕ᵢ                     */
+    double* torque_j;  /* 3 per contact, 𝛕ⱼ                     */
+    double* shear;     /* 3 per contact, 𝐬                      */
+} DemContacts;
+
+/* Values `solve` derives before the loop (src/executor.jl:244-267). */
+typedef struct DemDerived {
+    double cell_size;        /* 4 rₘₐₓ                                  */
+    double r_max;            /* rₘₐₓ                                    */
+    int64_t hash_table_size; /* clamp(∏ ceil((max-min)/cell), 2^20, 2^22) */
+    int64_t total_steps;     /* trunc(target_time / dt)                 */
+    int64_t save_per_steps;  /* trunc(saving_interval_time / dt)        */
+    double material_density; /* m/V of the last grain                   */
+    int64_t contact_capacity;/* n · max_coordinate_number               */
+} DemDerived;
+
+typedef struct DemStats {
+    int64_t n_particles;
+    int64_t steps_done;
+    int64_t contacts;        /* active contacts now (bonded + Hertz)    */
+    int64_t bonded;          /* active bonds now                        */
+    int64_t bonds_broken;    /* cumulative EBPM breakages               */
+    int64_t contacts_ended;  /* cumulative Hertz contacts ended         */
+    int64_t contacts_created;/* cumulative Hertz contacts created       */
+    int64_t warn_gap;        /* "gap > 0" events (src/kernels.jl:243-245)  */
+    int64_t warn_damping;    /* "γ < 0" events (src/kernels.jl:271-279)    */
+    int32_t error;           /* sticky DEM_ERR_* raised on the device   */
+    int32_t precision;       /* DEM_FP64 or DEM_FP32_FORCE              */
+} DemStats;
+
+typedef struct DemHandle DemHandle;
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+/* Makes `device` current for the calling thread; handles created afterwards
+ * live on it.  No counterpart in the reference (one GPU, CUDA.jl default). */
+int dem_set_device(int device);
+
+/* Builds the device state of one scene: the grain setup, derived sizes,
+ * material/surface/wall tables and buffers of `solve`
+ * (src/executor.jl:217-340).  Replaces `cu(grains_cpu)` + `GlobalData(...)`. */
+int dem_create(const DemConfigC* cfg, const DemParticlesIn* particles,
+               DemHandle** out);
+
+/* Frees every device buffer of the handle (the reference relies on GC,
+ * src/executor.jl:176-177). */
+int dem_destroy(DemHandle* h);
+
+/* ---- the step ---------------------------------------------------------- */
+
+/* `initialize!` (src/executor.jl:155-160): broad phase + `init_bonds!`
+ * (src/kernels.jl:60-85). */
+int dem_init_bonds(DemHandle* h);
+
+/* `simulate!` × nsteps (src/executor.jl:162-172): clear_state!, contact!,
+ * resolve_wall!, apply_body_force!, update!, late_clear_state!.  Asynchronous
+ * on the handle's stream; errors raised on the device surface at the next
+ * dem_sync / dem_get_* call. */
+int dem_step(DemHandle* h, int64_t nsteps);
+
+/* Same as dem_step, bracketed by CUDA events on the handle's stream; *ms is
+ * the device time of the nsteps (synchronises). */
+int dem_step_timed(DemHandle* h, int64_t nsteps, float* ms);
+
+/* One step launched phase by phase (no graph) with CUDA events between the
+ * phases on the handle's stream.  phase_ms[0..5] receive the device time of:
+ * broad phase (hash, bucket scan, scatter, canonical order), contact
+ * detection, row scan, contact compaction, contact forces, integration.
+ * No counterpart in the reference: per-kernel timing for roofline reports. */
+int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase);
+
+/* Waits for the handle's stream and reports the sticky device error. */
+int dem_sync(DemHandle* h);
+
+/* Selects the force arithmetic: DEM_FP64 (default, the reference's) or
+ * DEM_FP32_FORCE.  No counterpart in the reference, which is FP64 only. */
+int dem_set_precision(DemHandle* h, int mode);
+
+/* ---- state exchange ---------------------------------------------------- */
+
+/* Reads `grains` (positions, velocities, ...) back to the host, as
+ * `Array(grains)` does in save_single (src/utils.jl:40). */
+int dem_get_particles(DemHandle* h, DemParticleState* out);
+
+/* Overwrites the dynamic particle state from host buffers (fields left NULL
+ * are kept).  Used to start the device from a given state. */
+int dem_set_particles(DemHandle* h, const DemParticleState* in);
+
+int dem_get_static(DemHandle* h, DemParticleStatic* out);
+
+int dem_get_derived(DemHandle* h, DemDerived* out);
+
+/* Active contacts, sorted by (i, j).  *n_out receives the count even when it
+ * exceeds cap (then DEM_ERR_CAPACITY is returned and nothing is written). */
+int dem_get_contacts(DemHandle* h, DemContacts* out, int64_t cap,
+                     int64_t* n_out);
+
+/* Replaces the contact list (active contacts only; sets the active bit, and
+ * the bonded bit where bonded[k] != 0).  Pairs must satisfy i < j and be
+ * unique. */
+int dem_set_contacts(DemHandle* h, const DemContacts* in, int64_t n);
+
+int dem_get_stats(DemHandle* h, DemStats* out);
+
+/* ---- parity / inspection ----------------------------------------------- */
+
+/* Runs only the reference broad phase on the current positions and returns
+ * its intermediate arrays (src/executor.jl:38-78):
+ *   cell[3n]        kid        = cell(𝐤)                (src/utils.jl:1)
+ *   morton[n]       cartesian3morton(kid)               (src/utils.jl:2)
+ *   bucket[n]       hid        = hashcode(kid)  1-based (src/utils.jl:2)
+ *   bucket_count[H] hash_table after count_particles!   (src/kernels.jl:7-13)
+ *   sorted[n]       pid, within-bucket ascending        (src/kernels.jl:15-22)
+ *   cp[2*cp_cap]    cp_list pairs (i,j), i<j            (src/kernels.jl:24-58)
+ * Any output pointer may be NULL.  *cp_n receives the pair count; if it
+ * exceeds cp_cap no pair is written and DEM_ERR_CAPACITY is returned. */
+int dem_debug_broadphase(DemHandle* h, int32_t* cell, uint32_t* morton,
+                         uint32_t* bucket, uint32_t* bucket_count,
+                         uint32_t* sorted, int32_t* cp, int64_t cp_cap,
+                         int64_t* cp_n);
+
+/* ---- misc -------------------------------------------------------------- */
+
+const char* dem_strerror(int code);
+
+/* Library version string, e.g. "dem_gb300 0.1.0 sm_103a". */
+const char* dem_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DEM_GB300_H */

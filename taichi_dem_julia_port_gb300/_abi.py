@@ -1,0 +1,181 @@
+"""ctypes view of include/dem_gb300.h and the loader of libdem_sm100a.so.
+
+The structures here mirror the header field for field; `ENTRY_POINTS` lists
+every function the header declares with its ctypes signature.  The loader never
+falls back to another implementation: a missing library is an error.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+DEM_OK = 0
+DEM_ERR_INVALID = 1
+DEM_ERR_CUDA = 2
+DEM_ERR_CAPACITY = 3
+DEM_ERR_TIMEOUT = 4
+DEM_ERR_NO_DEVICE = 5
+DEM_ERR_RANGE = 6
+
+DEM_FP64 = 0
+DEM_FP32_FORCE = 1
+
+_D3 = C.c_double * 3
+
+
+class DemConfigC(C.Structure):
+    _fields_ = [
+        ("domain_min", _D3),
+        ("domain_max", _D3),
+        ("particle_contact_radius_multiplier", C.c_double),
+        ("neighboring_search_safety_factor", C.c_double),
+        ("particle_elastic_modulus", C.c_double),
+        ("particle_poisson_ratio", C.c_double),
+        ("wall_normal", _D3),
+        ("wall_distance", C.c_double),
+        ("wall_density", C.c_double),
+        ("wall_elastic_modulus", C.c_double),
+        ("wall_poisson_ratio", C.c_double),
+        ("bond_radius_ratio", C.c_double),
+        ("bond_elastic_modulus", C.c_double),
+        ("bond_poisson_ratio", C.c_double),
+        ("bond_compressive_strength", C.c_double),
+        ("bond_tensile_strength", C.c_double),
+        ("bond_shear_strength", C.c_double),
+        ("pp_coefficient_friction", C.c_double),
+        ("pp_coefficient_restitution", C.c_double),
+        ("pp_coefficient_rolling_resistance", C.c_double),
+        ("pw_coefficient_friction", C.c_double),
+        ("pw_coefficient_restitution", C.c_double),
+        ("pw_coefficient_rolling_resistance", C.c_double),
+        ("max_coordinate_number", C.c_int64),
+        ("collision_pair_init_capacity_factor", C.c_int64),
+        ("tolerance", C.c_double),
+        ("max_particle_count", C.c_int64),
+        ("gravity", _D3),
+        ("global_damping", C.c_double),
+        ("dt", C.c_double),
+        ("target_time", C.c_double),
+        ("saving_interval_time", C.c_double),
+    ]
+
+
+_PD = C.POINTER(C.c_double)
+_PI32 = C.POINTER(C.c_int32)
+_PU32 = C.POINTER(C.c_uint32)
+_PU8 = C.POINTER(C.c_uint8)
+
+
+class DemParticlesIn(C.Structure):
+    _fields_ = [("n", C.c_int64), ("id", _PI32), ("gid", _PI32), ("volume", _PD),
+                ("mass", _PD), ("pos", _PD), ("vel", _PD)]
+
+
+class DemParticleState(C.Structure):
+    _fields_ = [("n", C.c_int64), ("pos", _PD), ("vel", _PD), ("omega", _PD), ("quat", _PD),
+                ("force", _PD), ("moment", _PD), ("wall_shear", _PD)]
+
+
+class DemParticleStatic(C.Structure):
+    _fields_ = [("n", C.c_int64), ("radius", _PD), ("radius0", _PD), ("mass", _PD),
+                ("inertia", _PD)]
+
+
+class DemContacts(C.Structure):
+    _fields_ = [("i", _PI32), ("j", _PI32), ("bonded", _PU8), ("point", _PD), ("force", _PD),
+                ("torque_i", _PD), ("torque_j", _PD), ("shear", _PD)]
+
+
+class DemDerived(C.Structure):
+    _fields_ = [("cell_size", C.c_double), ("r_max", C.c_double), ("hash_table_size", C.c_int64),
+                ("total_steps", C.c_int64), ("save_per_steps", C.c_int64),
+                ("material_density", C.c_double), ("contact_capacity", C.c_int64)]
+
+
+class DemStats(C.Structure):
+    _fields_ = [("n_particles", C.c_int64), ("steps_done", C.c_int64), ("contacts", C.c_int64),
+                ("bonded", C.c_int64), ("bonds_broken", C.c_int64), ("contacts_ended", C.c_int64),
+                ("contacts_created", C.c_int64), ("warn_gap", C.c_int64),
+                ("warn_damping", C.c_int64), ("error", C.c_int32), ("precision", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_H = C.c_void_p
+_PH = C.POINTER(C.c_void_p)
+
+# name -> (restype, argtypes); every function of include/dem_gb300.h
+ENTRY_POINTS = {
+    "dem_set_device": (C.c_int, [C.c_int]),
+    "dem_create": (C.c_int, [C.POINTER(DemConfigC), C.POINTER(DemParticlesIn), _PH]),
+    "dem_destroy": (C.c_int, [_H]),
+    "dem_init_bonds": (C.c_int, [_H]),
+    "dem_step": (C.c_int, [_H, C.c_int64]),
+    "dem_step_timed": (C.c_int, [_H, C.c_int64, C.POINTER(C.c_float)]),
+    "dem_step_profiled": (C.c_int, [_H, C.POINTER(C.c_float), C.c_int]),
+    "dem_sync": (C.c_int, [_H]),
+    "dem_set_precision": (C.c_int, [_H, C.c_int]),
+    "dem_get_particles": (C.c_int, [_H, C.POINTER(DemParticleState)]),
+    "dem_set_particles": (C.c_int, [_H, C.POINTER(DemParticleState)]),
+    "dem_get_static": (C.c_int, [_H, C.POINTER(DemParticleStatic)]),
+    "dem_get_derived": (C.c_int, [_H, C.POINTER(DemDerived)]),
+    "dem_get_contacts": (C.c_int, [_H, C.POINTER(DemContacts), C.c_int64, C.POINTER(C.c_int64)]),
+    "dem_set_contacts": (C.c_int, [_H, C.POINTER(DemContacts), C.c_int64]),
+    "dem_get_stats": (C.c_int, [_H, C.POINTER(DemStats)]),
+    "dem_debug_broadphase": (C.c_int, [_H, _PI32, _PU32, _PU32, _PU32, _PU32, _PI32, C.c_int64,
+                                       C.POINTER(C.c_int64)]),
+    "dem_strerror": (C.c_char_p, [C.c_int]),
+    "dem_version": (C.c_char_p, []),
+}
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "libdem_sm100a.so"
+
+
+class DemError(RuntimeError):
+    def __init__(self, code: int, where: str, message: str = ""):
+        self.code = code
+        super().__init__(f"{where}: DEM error {code}: {message}")
+
+
+_lib = None
+
+
+def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Loads libdem_sm100a.so (built in-tree by taichi_dem_julia_port_gb300.build).
+
+    Raises FileNotFoundError when the library has not been built: there is no
+    fallback implementation."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(
+            f"{p} is missing; build it with `python -m taichi_dem_julia_port_gb300.build` "
+            "(the DEM step runs only through this CUDA library)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in ENTRY_POINTS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(lib, rc: int, where: str) -> None:
+    if rc != DEM_OK:
+        raise DemError(rc, where, lib.dem_strerror(rc).decode())
+
+
+def ptr(a: np.ndarray | None, ctype):
+    """Pointer to a contiguous numpy array's data (None -> NULL)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "array must be contiguous"
+    return a.ctypes.data_as(C.POINTER(ctype))

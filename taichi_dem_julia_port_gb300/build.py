@@ -1,0 +1,78 @@
+"""Builds libdem_sm100a.so in-tree (package directory) with nvcc for sm_103a.
+
+Two translation units are compiled in parallel and linked into one shared
+library with the CUDA runtime linked statically, so the library depends only
+on the NVIDIA driver.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB_NAME = "libdem_sm100a.so"
+LIB_PATH = PKG / LIB_NAME
+SOURCES = ["dem_kernels.cu", "dem_api.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc_path() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the DEM library needs the CUDA 13 toolkit to build")
+
+
+def _flags() -> list[str]:
+    return ARCH + [
+        "-O3", "-lineinfo", "-std=c++17",
+        "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+        "-diag-suppress", "1444",
+        f"-I{ROOT / 'include'}", f"-I{CSRC}",
+    ]
+
+
+def _stale(out: Path, deps: list[Path]) -> bool:
+    return not out.exists() or any(d.stat().st_mtime > out.stat().st_mtime for d in deps)
+
+
+def build(verbose: bool = False, force: bool = False) -> Path:
+    """Compile (if needed) and return the path of libdem_sm100a.so."""
+    nvcc = nvcc_path()
+    BUILD.mkdir(exist_ok=True)
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "dem_gb300.h"]
+    objs = []
+    jobs = []
+    for src in SOURCES:
+        obj = BUILD / (Path(src).stem + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [CSRC / src] + headers):
+            cmd = [nvcc, *_flags(), "-c", str(CSRC / src), "-o", str(obj)]
+            jobs.append(cmd)
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"nvcc failed:\n{' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+        return res
+
+    with ThreadPoolExecutor(max_workers=len(jobs) or 1) as ex:
+        list(ex.map(run, jobs))
+    if force or jobs or _stale(LIB_PATH, objs):
+        tmp = LIB_PATH.with_suffix(".so.tmp")
+        run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs)])
+        os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build(verbose=True, force="--force" in sys.argv))

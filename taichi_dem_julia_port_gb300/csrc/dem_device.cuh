@@ -1,0 +1,119 @@
+// dem_device.cuh — device helpers shared by the DEM kernels.
+#pragma once
+
+#include <cuda/atomic>
+#include <math_constants.h>
+
+#include "dem_internal.h"
+
+namespace dem {
+
+// ---- exact (non-contracted) FP64 pieces --------------------------------------
+// The reference compares distances and cell coordinates with plain IEEE
+// arithmetic (Julia does not fuse multiply-adds).  Every quantity that feeds a
+// discrete decision is computed here with explicit round-to-nearest intrinsics
+// so that nvcc cannot contract it into an FMA.
+
+__device__ __forceinline__ int32_t ceil_i32(double t) {
+    double c = ceil(t);
+    if (!(c > -2147483648.0 && c < 2147483647.0)) return 0;  // NaN / overflow
+    return (int32_t)c;
+}
+
+// StaticArrays `norm` (sqrt of ((x²+y²)+z²), rescaled when not in (0, Inf)).
+__device__ __noinline__ double norm_scaled(double x, double y, double z) {
+    if (isnan(x) || isnan(y) || isnan(z)) return CUDART_NAN;
+    double sc = fmax(fabs(x), fmax(fabs(y), fabs(z)));
+    if (sc == 0.0) return 0.0;
+    double a = __ddiv_rn(x, sc), b = __ddiv_rn(y, sc), c = __ddiv_rn(z, sc);
+    return __dmul_rn(sc, __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)),
+                                              __dmul_rn(c, c))));
+}
+__device__ __forceinline__ double norm_rn(double x, double y, double z) {
+    double l = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+    if (l > 0.0 && l < CUDART_INF) return l;
+    return norm_scaled(x, y, z);
+}
+
+// `norm(𝐤ᵢ - 𝐤ⱼ) < rᵢ + rⱼ` exactly as the reference evaluates it
+// (src/kernels.jl:72, 103).
+__device__ __forceinline__ bool touching_rn(double xi, double yi, double zi, double xj, double yj,
+                                            double zj, double ri, double rj) {
+    double l = norm_rn(__dsub_rn(xi, xj), __dsub_rn(yi, yj), __dsub_rn(zi, zj));
+    return l < __dadd_rn(ri, rj);
+}
+
+// Conservative FP32 rejection: returns false only when the FP64 test above is
+// certain to fail.  Inputs are FP32 copies (u = 2^-24 relative rounding) of
+// positions relative to a common origin and of the radii.  The FP32 distance d'
+// differs from the true one by at most 2(M_i + M_j)u + 6u·d' (M = largest
+// coordinate magnitude of a particle) and r_i + r_j <= (r'_i + r'_j)(1 + 3u);
+// the test rejects only when d'(1 - 2^-18) exceeds (r'_i + r'_j) plus
+// (M_i + M_j + r'_i + r'_j)·2^-19, which leaves a factor of 10 on each term.
+__device__ __forceinline__ bool maybe_touching32(float4 a, float4 b) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    float s = dx * dx + dy * dy + dz * dz;
+    float M = fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fabsf(a.z)) +
+              fmaxf(fmaxf(fabsf(b.x), fabsf(b.y)), fabsf(b.z));
+    float rs = a.w + b.w;
+    float B = rs + (M + rs) * 0x1p-19f;
+    return !(s * (1.0f - 0x1p-17f) > B * B);
+}
+
+// ---- Morton / bucket ---------------------------------------------------------
+// Morton.jl `cartesian3morton` for 1-based cells (x in bit 0): the interleave of
+// (ijk - 1) plus one.  Each coordinate keeps its low 10 bits.  The spreading
+// uses the usual shift-and-mask bit interleave.
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+__device__ __forceinline__ uint32_t morton1(int x, int y, int z) {
+    return (spread10((uint32_t)(x - 1)) | (spread10((uint32_t)(y - 1)) << 1) |
+            (spread10((uint32_t)(z - 1)) << 2)) +
+           1u;
+}
+// 0-based bucket: hashcode(ijk) - 1 = cartesian3morton(ijk) % H (src/utils.jl:2)
+__device__ __forceinline__ uint32_t bucket_of(int x, int y, int z, const DemParams& p) {
+    uint32_t m = morton1(x, y, z);
+    return p.H_pow2_mask ? (m & p.H_pow2_mask) : (m % p.H);
+}
+// The 8 octant buckets of `neighbors` (src/utils.jl:4-16), in its order.
+__device__ __forceinline__ void buckets8(int4 ci, const DemParams& p, uint32_t B[8]) {
+    const int dx = (ci.w & 1) ? 1 : -1, dy = (ci.w & 2) ? 1 : -1, dz = (ci.w & 4) ? 1 : -1;
+    B[0] = bucket_of(ci.x, ci.y, ci.z, p);
+    B[1] = bucket_of(ci.x + dx, ci.y, ci.z, p);
+    B[2] = bucket_of(ci.x, ci.y + dy, ci.z, p);
+    B[3] = bucket_of(ci.x, ci.y, ci.z + dz, p);
+    B[4] = bucket_of(ci.x + dx, ci.y + dy, ci.z, p);
+    B[5] = bucket_of(ci.x + dx, ci.y, ci.z + dz, p);
+    B[6] = bucket_of(ci.x, ci.y + dy, ci.z + dz, p);
+    B[7] = bucket_of(ci.x + dx, ci.y + dy, ci.z + dz, p);
+}
+
+// ---- small vector helpers (contractible; used by the force models) ----------
+template <typename T>
+struct Vec3 {
+    T x, y, z;
+};
+template <typename T>
+__device__ __forceinline__ Vec3<T> cross3(Vec3<T> a, Vec3<T> b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+// Julia min / max propagate NaN (fmin / fmax do not).
+__device__ __forceinline__ double jl_min(double a, double b) {
+    return (isnan(a) || isnan(b)) ? CUDART_NAN : (b < a ? b : a);
+}
+__device__ __forceinline__ double jl_max(double a, double b) {
+    return (isnan(a) || isnan(b)) ? CUDART_NAN : (b > a ? b : a);
+}
+__device__ __forceinline__ double jl_sign(double x) { return x < 0.0 ? -1.0 : (x > 0.0 ? 1.0 : x); }
+
+__device__ __forceinline__ void raise_error(DevCounters* c, int bit) { atomicOr(&c->error, bit); }
+
+}  // namespace dem

@@ -1,0 +1,287 @@
+"""Host front end mirroring DEMPort's executor (src/executor.jl).
+
+`GlobalData` owns one scene's device state through libdem_sm100a.so (the
+reference's `GlobalData`, src/executor.jl:1-29); `initialize` and `simulate`
+are `initialize!` / `simulate!` (src/executor.jl:155-172); `solve` is the
+reference's driver (src/executor.jl:174-394): TOML config, p4p input, step
+loop, p4p/p4c output every `saving_interval_time`.
+
+Every step runs on the GPU; there is no CPU path in this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import logging
+import time
+from pathlib import Path
+
+import numpy as np
+
+from . import _abi
+from ._abi import check, ptr
+from .config import DEMConfig
+from .p4io import read_p4p, write_p4c, write_p4p
+from .scenes import ParticleInput
+
+log = logging.getLogger("taichi_dem_julia_port_gb300")
+
+PRECISIONS = {"fp64": _abi.DEM_FP64, "fp32": _abi.DEM_FP32_FORCE,
+              "fp32_force": _abi.DEM_FP32_FORCE}
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a.reshape(shape) if shape is not None else a
+
+
+class GlobalData:
+    """Device state of one scene (particles, broad phase, contacts)."""
+
+    def __init__(self, cfg: DEMConfig, particles: ParticleInput, precision: str = "fp64",
+                 lib=None):
+        self.lib = lib or _abi.load_library()
+        self.cfg = cfg
+        self.n = particles.n
+        self._cfg_c = cfg.to_c()
+        ids = np.ascontiguousarray(particles.id, dtype=np.int32)
+        gid = np.ascontiguousarray(particles.gid, dtype=np.int32)
+        vol = _f64(particles.volume)
+        mass = _f64(particles.mass)
+        pos = _f64(particles.pos, (self.n, 3))
+        vel = _f64(particles.vel, (self.n, 3))
+        self.ids, self.gid, self.volume, self.mass = ids, gid, vol, mass
+        pin = _abi.DemParticlesIn(self.n, ptr(ids, C.c_int32), ptr(gid, C.c_int32),
+                                  ptr(vol, C.c_double), ptr(mass, C.c_double),
+                                  ptr(pos, C.c_double), ptr(vel, C.c_double))
+        h = C.c_void_p()
+        check(self.lib, self.lib.dem_create(C.byref(self._cfg_c), C.byref(pin), C.byref(h)),
+              "dem_create")
+        self.h = h
+        self.set_precision(precision)
+
+    # ---- lifetime -------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.dem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- the step -------------------------------------------------------------
+    def set_precision(self, precision: str) -> None:
+        check(self.lib, self.lib.dem_set_precision(self.h, PRECISIONS[precision]),
+              "dem_set_precision")
+        self.precision = precision
+
+    def initialize(self) -> None:
+        """`initialize!`: broad phase + init_bonds! (bond every cp_list pair
+        closer than r₀ᵢ + r₀ⱼ)."""
+        check(self.lib, self.lib.dem_init_bonds(self.h), "dem_init_bonds")
+
+    def simulate(self, nsteps: int = 1) -> None:
+        """`simulate!` × nsteps (asynchronous; errors surface at sync())."""
+        check(self.lib, self.lib.dem_step(self.h, int(nsteps)), "dem_step")
+
+    def simulate_timed(self, nsteps: int) -> float:
+        """Runs nsteps and returns their device time in milliseconds."""
+        ms = C.c_float()
+        check(self.lib, self.lib.dem_step_timed(self.h, int(nsteps), C.byref(ms)),
+              "dem_step_timed")
+        return float(ms.value)
+
+    PHASES = ("broadphase", "detect", "scan_rows", "compact", "force", "integrate")
+
+    def simulate_profiled(self) -> dict:
+        """One step launched phase by phase; device milliseconds per phase."""
+        ms = (C.c_float * 6)()
+        check(self.lib, self.lib.dem_step_profiled(self.h, ms, 6), "dem_step_profiled")
+        return dict(zip(self.PHASES, [float(x) for x in ms]))
+
+    def sync(self) -> None:
+        check(self.lib, self.lib.dem_sync(self.h), "dem_sync")
+
+    # ---- state ----------------------------------------------------------------
+    def particles(self, forces: bool = True) -> dict:
+        n = self.n
+        out = {k: np.empty((n, 3)) for k in ("pos", "vel", "omega", "wall_shear")}
+        out["quat"] = np.empty((n, 4))
+        if forces:
+            out["force"] = np.empty((n, 3))
+            out["moment"] = np.empty((n, 3))
+        st = _abi.DemParticleState(n, *(ptr(out.get(k), C.c_double) for k in
+                                        ("pos", "vel", "omega", "quat", "force", "moment",
+                                         "wall_shear")))
+        check(self.lib, self.lib.dem_get_particles(self.h, C.byref(st)), "dem_get_particles")
+        return out
+
+    def set_particles(self, pos=None, vel=None, omega=None, quat=None, wall_shear=None) -> None:
+        n = self.n
+        arrs = {"pos": pos, "vel": vel, "omega": omega, "wall_shear": wall_shear}
+        arrs = {k: (_f64(v, (n, 3)) if v is not None else None) for k, v in arrs.items()}
+        q = _f64(quat, (n, 4)) if quat is not None else None
+        st = _abi.DemParticleState(n, ptr(arrs["pos"], C.c_double), ptr(arrs["vel"], C.c_double),
+                                   ptr(arrs["omega"], C.c_double), ptr(q, C.c_double), None, None,
+                                   ptr(arrs["wall_shear"], C.c_double))
+        check(self.lib, self.lib.dem_set_particles(self.h, C.byref(st)), "dem_set_particles")
+
+    def static(self) -> dict:
+        n = self.n
+        out = {k: np.empty(n) for k in ("radius", "radius0", "mass", "inertia")}
+        st = _abi.DemParticleStatic(n, *(ptr(out[k], C.c_double) for k in
+                                         ("radius", "radius0", "mass", "inertia")))
+        check(self.lib, self.lib.dem_get_static(self.h, C.byref(st)), "dem_get_static")
+        return out
+
+    def derived(self) -> dict:
+        d = _abi.DemDerived()
+        check(self.lib, self.lib.dem_get_derived(self.h, C.byref(d)), "dem_get_derived")
+        return {k: getattr(d, k) for k, _ in d._fields_}
+
+    def contacts(self) -> dict:
+        """Active contacts sorted by (i, j) (0-based indices)."""
+        cnt = C.c_int64()
+        check(self.lib, self.lib.dem_get_contacts(self.h, None, 0, C.byref(cnt)),
+              "dem_get_contacts")
+        m = cnt.value
+        out = {"i": np.empty(m, np.int32), "j": np.empty(m, np.int32),
+               "bonded": np.empty(m, np.uint8)}
+        for k in ("point", "force", "torque_i", "torque_j", "shear"):
+            out[k] = np.empty((m, 3))
+        cs = _abi.DemContacts(ptr(out["i"], C.c_int32), ptr(out["j"], C.c_int32),
+                              ptr(out["bonded"], C.c_uint8),
+                              *(ptr(out[k], C.c_double) for k in
+                                ("point", "force", "torque_i", "torque_j", "shear")))
+        check(self.lib, self.lib.dem_get_contacts(self.h, C.byref(cs), m, C.byref(cnt)),
+              "dem_get_contacts")
+        return out
+
+    def set_contacts(self, c: dict) -> None:
+        m = len(c["i"])
+        arr = {"i": np.ascontiguousarray(c["i"], np.int32),
+               "j": np.ascontiguousarray(c["j"], np.int32),
+               "bonded": np.ascontiguousarray(c.get("bonded", np.zeros(m)), np.uint8)}
+        for k in ("point", "force", "torque_i", "torque_j", "shear"):
+            arr[k] = _f64(c[k], (m, 3)) if k in c else np.zeros((m, 3))
+        cs = _abi.DemContacts(ptr(arr["i"], C.c_int32), ptr(arr["j"], C.c_int32),
+                              ptr(arr["bonded"], C.c_uint8),
+                              *(ptr(arr[k], C.c_double) for k in
+                                ("point", "force", "torque_i", "torque_j", "shear")))
+        check(self.lib, self.lib.dem_set_contacts(self.h, C.byref(cs), m), "dem_set_contacts")
+
+    def stats(self) -> dict:
+        s = _abi.DemStats()
+        check(self.lib, self.lib.dem_get_stats(self.h, C.byref(s)), "dem_get_stats")
+        return s.as_dict()
+
+    def debug_broadphase(self, with_pairs: bool = True) -> dict:
+        """The reference broad phase on the current positions: cell ijk, Morton
+        code, 1-based bucket (hashcode), bucket counts, sorted particle order
+        and the cp_list pairs (0-based)."""
+        n = self.n
+        H = self.derived()["hash_table_size"]
+        out = {"cell": np.empty((n, 3), np.int32), "morton": np.empty(n, np.uint32),
+               "bucket": np.empty(n, np.uint32), "bucket_count": np.empty(H, np.uint32),
+               "sorted": np.empty(n, np.uint32)}
+        cnt = C.c_int64()
+        args = [ptr(out["cell"], C.c_int32), ptr(out["morton"], C.c_uint32),
+                ptr(out["bucket"], C.c_uint32), ptr(out["bucket_count"], C.c_uint32),
+                ptr(out["sorted"], C.c_uint32)]
+        check(self.lib, self.lib.dem_debug_broadphase(self.h, *args, None, 0, C.byref(cnt)),
+              "dem_debug_broadphase")
+        if with_pairs:
+            cp = np.empty((max(cnt.value, 1), 2), np.int32)
+            check(self.lib, self.lib.dem_debug_broadphase(self.h, *args, ptr(cp, C.c_int32),
+                                                          cnt.value, C.byref(cnt)),
+                  "dem_debug_broadphase")
+            out["cp"] = cp[:cnt.value]
+        out["cp_count"] = cnt.value
+        return out
+
+
+def initialize(g: GlobalData) -> None:
+    """`initialize!(global_data, ...)` (src/executor.jl:155-160)."""
+    g.initialize()
+
+
+def simulate(g: GlobalData, nsteps: int = 1) -> None:
+    """`simulate!(global_data, ...)` (src/executor.jl:162-172)."""
+    g.simulate(nsteps)
+
+
+def load_particles(p4p_path: str | Path) -> ParticleInput:
+    """The grains of the first record of a p4p file, in file order
+    (src/executor.jl:217-243)."""
+    lines = Path(p4p_path).read_text().split("\n")
+    n = int(lines[1].split()[1])
+    rows = np.array([[float(x) for x in lines[3 + k].split()[:10]] for k in range(n)],
+                    dtype=np.float64).reshape(n, 10)
+    return ParticleInput(id=rows[:, 0].astype(np.int32), gid=rows[:, 1].astype(np.int32),
+                         volume=rows[:, 2].copy(), mass=rows[:, 3].copy(),
+                         pos=rows[:, 4:7].copy(), vel=rows[:, 7:10].copy())
+
+
+def save_single(g: GlobalData, p4p, p4c, t: float) -> int:
+    """`save_single` (src/utils.jl:30-78): appends one record to each file and
+    returns the number of active contacts written."""
+    st = g.particles(forces=False)
+    write_p4p(p4p, t, g.ids, g.gid, g.volume, g.mass, st["pos"], st["vel"])
+    c = g.contacts()
+    write_p4c(p4c, t, c["i"], c["j"], c["point"], c["force"], c["bonded"])
+    return len(c["i"])
+
+
+def solve(cfg_filename: str | Path, no_bond: bool = False, save_snapshot: bool = False,
+          save_information: bool = True, output_dir: str | Path = ".",
+          precision: str = "fp64", particles: ParticleInput | None = None,
+          cfg: DEMConfig | None = None) -> GlobalData:
+    """The reference driver `solve` (src/executor.jl:174-394).
+
+    `save_snapshot` needs an OpenGL stack (GLMakie) and is unavailable here;
+    passing True raises.  `particles`/`cfg` may be given directly instead of
+    reading `init_particles` relative to the config file."""
+    if save_snapshot:
+        raise NotImplementedError("snapshots need a graphics stack (GLMakie); unavailable")
+    t0 = time.perf_counter()
+    if cfg is None:
+        cfg = DEMConfig.from_toml(cfg_filename)
+    if particles is None:
+        particles = load_particles(Path(cfg_filename).parent / cfg.init_particles)
+    g = GlobalData(cfg, particles, precision=precision)
+    d = g.derived()
+    log.info("Setting: hash_table_size=%d cell_size=%g", d["hash_table_size"], d["cell_size"])
+    if not no_bond:
+        g.initialize()
+    total_steps, save_per = cfg.total_steps, max(cfg.save_per_steps, 1)
+    out = Path(output_dir)
+    p4p = p4c = None
+    if save_information:
+        p4p = open(out / "output.p4p", "w")
+        p4c = open(out / "output.p4c", "w")
+        save_single(g, p4p, p4c, 0.0)
+    step = 0
+    try:
+        while step < total_steps:
+            t1 = time.perf_counter()
+            k = save_per  # the reference runs whole save intervals (src/executor.jl:365-370)
+            g.simulate(k)
+            g.sync()
+            step += k
+            log.info("Solving... step=%d dt=%.3fs", step, time.perf_counter() - t1)
+            if save_information:
+                save_single(g, p4p, p4c, step * cfg.dt)
+    finally:
+        if p4p:
+            p4p.close()
+            p4c.close()
+    log.info("Total time: %.3f s", time.perf_counter() - t0)
+    return g

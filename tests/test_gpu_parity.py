@@ -1,0 +1,268 @@
+"""GPU parity: the CUDA DEM step (through the C ABI) against the CPU oracle.
+
+Bit-exact: cell ijk, Morton codes, buckets, bucket counts, sorted order, the
+cp_list multiset, contact sets and bond sets.  Within tolerance: forces,
+positions and velocities (FP64: rtol 1e-9 for one step from an identical
+state, 1e-5 over a short horizon; FP32 force mode: 1e-3)."""
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleScene
+from taichi_dem_julia_port_gb300 import GlobalData, scenes
+from taichi_dem_julia_port_gb300._abi import DEM_ERR_CAPACITY, DemError
+from taichi_dem_julia_port_gb300.config import DEMConfig
+from taichi_dem_julia_port_gb300.scenes import ParticleInput
+from tests.conftest import assert_rows_close
+
+pytestmark = pytest.mark.gpu
+
+RTOL_STEP = 1e-9      # one step from an identical state (FP64)
+RTOL_HORIZON = 1e-5   # short horizon (FP64), the spec force bound
+RTOL_FP32 = 1e-3      # FP32 force mode vs the FP64 oracle
+
+
+def pair_set(c):
+    return set(zip(c["i"].tolist(), c["j"].tolist()))
+
+
+def bonded_set(c):
+    b = c["bonded"].astype(bool)
+    return set(zip(c["i"][b].tolist(), c["j"][b].tolist()))
+
+
+def random_cloud(n, box, rmin, rmax, seed, v=0.0, cfg_kw=None):
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(rmin, rmax, n)
+    pos = rng.uniform(0, 1, (n, 3)) * np.asarray(box)
+    vel = rng.normal(0, v, (n, 3)) if v else np.zeros((n, 3))
+    kw = dict(domain_min=[-0.02] * 3, domain_max=(np.asarray(box) + 0.02).tolist(),
+              max_coordinate_number=64, wall_distance=0.0, gravity=[0.0, 0.0, -9.81],
+              dt=1e-6, particle_elastic_modulus=1e8, bond_elastic_modulus=1e8,
+              bond_tensile_strength=1e6, bond_shear_strength=1e6)
+    kw.update(cfg_kw or {})
+    return DEMConfig(**kw), ParticleInput.from_arrays(r, pos, vel, 2500.0)
+
+
+def both(cfg, p, precision="fp64"):
+    return GlobalData(cfg, p, precision=precision), OracleScene(cfg, p)
+
+
+def compare_broadphase(g, o):
+    a, b = g.debug_broadphase(), o.debug_broadphase()
+    for k in ("cell", "morton", "bucket", "bucket_count", "sorted"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    assert a["cp_count"] == b["cp_count"]
+    ca = a["cp"][np.lexsort((a["cp"][:, 1], a["cp"][:, 0]))]
+    cb = b["cp"][np.lexsort((b["cp"][:, 1], b["cp"][:, 0]))]
+    np.testing.assert_array_equal(ca, cb)
+    return a
+
+
+def compare_state(g, o, rtol, what=""):
+    cg, co = g.contacts(), o.contacts()
+    assert pair_set(cg) == pair_set(co), f"{what}: contact sets differ"
+    assert bonded_set(cg) == bonded_set(co), f"{what}: bond sets differ"
+    pg, po = g.particles(), o.particles()
+    assert_rows_close(pg["pos"], po["pos"], rtol, f"{what} pos")
+    assert_rows_close(pg["vel"], po["vel"], rtol, f"{what} vel")
+    assert_rows_close(pg["force"], po["force"], rtol, f"{what} force", atol_frac=rtol)
+    assert_rows_close(pg["moment"], po["moment"], rtol, f"{what} moment", atol_frac=rtol)
+    assert_rows_close(cg["force"], co["force"], rtol, f"{what} contact force", atol_frac=rtol)
+    assert_rows_close(cg["shear"], co["shear"], rtol, f"{what} shear", atol_frac=rtol)
+    assert_rows_close(cg["point"], co["point"], rtol, f"{what} point")
+    return cg
+
+
+# ---- broad phase ---------------------------------------------------------------------
+
+@pytest.mark.parametrize("side", [3, 10, 26])
+def test_broadphase_lattice_bitexact(gpu, side):
+    sc = scenes.bonded_cube(side, steps=0)
+    g, o = both(sc.cfg, sc.particles)
+    a = compare_broadphase(g, o)
+    assert a["cp_count"] > 0
+
+
+def test_broadphase_hash_collisions_bitexact(gpu):
+    """A wide domain so Morton codes exceed H and buckets collide (non-power
+    of two H, so neighbour buckets may coincide too)."""
+    cfg, p = random_cloud(4000, (3.9, 3.9, 3.9), 0.004, 0.006, seed=3,
+                          cfg_kw=dict(domain_max=[4.0, 4.0, 4.0]))
+    g, o = both(cfg, p)
+    H = g.derived()["hash_table_size"]
+    assert H & (H - 1) != 0, "want a non power-of-two table"
+    a = compare_broadphase(g, o)
+    assert a["morton"].max() > H
+
+
+def test_broadphase_outside_domain_bitexact(gpu):
+    """Particles below domain_min (cells <= 0) and on exact cell boundaries."""
+    cfg, p = random_cloud(500, (0.2, 0.2, 0.2), 0.005, 0.01, seed=9)
+    g0, _ = both(cfg, p)
+    cs = g0.derived()["cell_size"]
+    g0.close()
+    pos = p.pos.copy()
+    pos[:50] -= 0.5
+    pos[50:100] = np.asarray(cfg.domain_min) + np.round(pos[50:100] / cs) * cs
+    q = ParticleInput.from_arrays(np.cbrt(p.volume / (4 / 3 * np.pi)), pos, p.vel, 2500.0)
+    g, o = both(cfg, q)
+    compare_broadphase(g, o)
+
+
+# ---- contacts --------------------------------------------------------------------------
+
+@pytest.mark.parametrize("side", [3, 10, 26])
+def test_init_bonds_bitexact(gpu, side):
+    sc = scenes.bonded_cube(side, steps=0)
+    g, o = both(sc.cfg, sc.particles)
+    g.initialize()
+    o.initialize()
+    cg, co = g.contacts(), o.contacts()
+    assert pair_set(cg) == pair_set(co)
+    assert bonded_set(cg) == bonded_set(co)
+    assert len(cg["i"]) == 3 * side * side * (side - 1)
+
+
+def test_one_step_from_identical_state_cube(gpu):
+    """Run the oracle into the impact, copy its state to the GPU, step both."""
+    sc = scenes.bonded_cube(8, speed=10.0, steps=0, seed=4)
+    g, o = both(sc.cfg, sc.particles)
+    o.initialize()
+    o.simulate(160)  # past first wall contact at ~100 steps
+    for _ in range(3):
+        p, c = o.particles(), o.contacts()
+        g.set_particles(pos=p["pos"], vel=p["vel"], omega=p["omega"], quat=p["quat"],
+                        wall_shear=p["wall_shear"])
+        g.set_contacts(c)
+        g.simulate(1)
+        o.simulate(1)
+        compare_state(g, o, RTOL_STEP, "cube one step")
+        o.simulate(40)
+
+
+def test_one_step_from_identical_state_granular(gpu):
+    """Overlapping random cloud: Hertz contacts created, ended and sliding."""
+    cfg, p = random_cloud(3000, (0.05, 0.05, 0.05), 0.0008, 0.0015, seed=5, v=0.5,
+                          cfg_kw=dict(pp_coefficient_friction=0.3))
+    g, o = both(cfg, p)
+    o.simulate(5)
+    for _ in range(3):
+        pp, c = o.particles(), o.contacts()
+        g.set_particles(pos=pp["pos"], vel=pp["vel"], omega=pp["omega"], quat=pp["quat"],
+                        wall_shear=pp["wall_shear"])
+        g.set_contacts(c)
+        g.simulate(1)
+        o.simulate(1)
+        cg = compare_state(g, o, RTOL_STEP, "granular one step")
+        assert len(cg["i"]) > 100
+        o.simulate(10)
+    s = o.stats()
+    assert s["contacts_created"] > 0 and s["contacts_ended"] > 0
+
+
+def test_short_horizon_cube(gpu):
+    sc = scenes.bonded_cube(10, speed=10.0, steps=0, seed=1)
+    g, o = both(sc.cfg, sc.particles)
+    g.initialize()
+    o.initialize()
+    for _ in range(4):
+        g.simulate(50)
+        o.simulate(50)
+        compare_state(g, o, RTOL_HORIZON, "cube horizon")
+    assert g.stats()["error"] == 0
+
+
+def test_short_horizon_fast_impact_breaks_bonds(gpu):
+    """A fast impact that breaks bonds: broken-bond counts and bond sets match."""
+    sc = scenes.bonded_cube(6, speed=60.0, steps=0, seed=2)
+    g, o = both(sc.cfg, sc.particles)
+    g.initialize()
+    o.initialize()
+    for _ in range(6):
+        g.simulate(50)
+        o.simulate(50)
+        compare_state(g, o, RTOL_HORIZON, "fast impact")
+    assert o.stats()["bonds_broken"] > 0
+    assert g.stats()["bonds_broken"] == o.stats()["bonds_broken"]
+
+
+def test_deterministic_rerun(gpu):
+    cfg, p = random_cloud(2000, (0.04, 0.04, 0.04), 0.0008, 0.0015, seed=8, v=0.3)
+    outs = []
+    for _ in range(2):
+        g = GlobalData(cfg, p)
+        g.simulate(100)
+        outs.append((g.particles(), g.contacts()))
+        g.close()
+    for k in outs[0][0]:
+        np.testing.assert_array_equal(outs[0][0][k], outs[1][0][k])
+    for k in outs[0][1]:
+        np.testing.assert_array_equal(outs[0][1][k], outs[1][1][k])
+
+
+def test_fp32_force_mode_error(gpu):
+    cfg, p = random_cloud(3000, (0.05, 0.05, 0.05), 0.0008, 0.0015, seed=5, v=0.5)
+    g, o = both(cfg, p, precision="fp32")
+    o.simulate(5)
+    pp, c = o.particles(), o.contacts()
+    g.set_particles(pos=pp["pos"], vel=pp["vel"], omega=pp["omega"], quat=pp["quat"],
+                    wall_shear=pp["wall_shear"])
+    g.set_contacts(c)
+    g.simulate(1)
+    o.simulate(1)
+    cg, co = g.contacts(), o.contacts()
+    assert pair_set(cg) == pair_set(co)
+    assert_rows_close(cg["force"], co["force"], RTOL_FP32, "fp32 contact force", atol_frac=RTOL_FP32)
+    pg, po = g.particles(), o.particles()
+    assert_rows_close(pg["force"], po["force"], RTOL_FP32, "fp32 force", atol_frac=RTOL_FP32)
+
+
+def test_fp32_force_mode_bonded(gpu):
+    sc = scenes.bonded_cube(8, speed=10.0, steps=0, seed=4)
+    g, o = both(sc.cfg, sc.particles, precision="fp32")
+    g.initialize()
+    o.initialize()
+    g.simulate(200)
+    o.simulate(200)
+    cg, co = g.contacts(), o.contacts()
+    assert bonded_set(cg) == bonded_set(co)
+    pg, po = g.particles(), o.particles()
+    assert_rows_close(pg["pos"], po["pos"], 1e-6, "fp32 pos")
+    assert_rows_close(pg["force"], po["force"], RTOL_FP32, "fp32 force", atol_frac=RTOL_FP32)
+
+
+# ---- edge cases ----------------------------------------------------------------------------
+
+def test_single_particle_on_wall(gpu):
+    cfg = DEMConfig(domain_min=[-1, -1, -1], domain_max=[1, 1, 1], wall_distance=0.0,
+                    dt=1e-6, max_coordinate_number=4)
+    p = ParticleInput.from_arrays(np.array([0.01]), np.array([[0.0, 0.0, 0.0095]]),
+                                  np.array([[0.1, 0.0, -0.5]]), 2500.0)
+    g, o = both(cfg, p)
+    for _ in range(5):
+        g.simulate(20)
+        o.simulate(20)
+        pg, po = g.particles(), o.particles()
+        assert_rows_close(pg["pos"], po["pos"], RTOL_HORIZON, "pos")
+        assert_rows_close(pg["vel"], po["vel"], RTOL_HORIZON, "vel")
+        assert_rows_close(pg["wall_shear"], po["wall_shear"], RTOL_HORIZON, "wall shear",
+                          atol_frac=RTOL_HORIZON)
+
+
+def test_empty_scene(gpu):
+    cfg = DEMConfig(domain_min=[-1, -1, -1], domain_max=[1, 1, 1])
+    p = ParticleInput.from_arrays(np.zeros(0), np.zeros((0, 3)), np.zeros((0, 3)), 2500.0)
+    g = GlobalData(cfg, p)
+    g.initialize()
+    g.simulate(3)
+    g.sync()
+    assert len(g.contacts()["i"]) == 0
+
+
+def test_capacity_overflow_reports_error(gpu):
+    sc = scenes.bonded_cube(5, steps=0)
+    cfg = sc.cfg.replace(max_coordinate_number=1)
+    g = GlobalData(cfg, sc.particles)
+    with pytest.raises(DemError) as e:
+        g.initialize()
+    assert e.value.code == DEM_ERR_CAPACITY

@@ -1,0 +1,130 @@
+"""CPU tests of the host side: config, p4p/p4c files, scenes and the C ABI
+surface of libdem_sm100a.so (loaded, no GPU call)."""
+import ctypes
+import io
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from taichi_dem_julia_port_gb300 import _abi, p4io, scenes
+from taichi_dem_julia_port_gb300.config import DEMConfig
+
+ROOT = Path(__file__).resolve().parents[1]
+REF_CFG = Path("/root/reference/cfg")
+
+
+def header_functions():
+    src = (ROOT / "include" / "dem_gb300.h").read_text()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(dem_\w+)\s*\(", src, flags=re.M)))
+
+
+def test_library_exports_every_header_function(dem_lib_path):
+    lib = ctypes.CDLL(str(dem_lib_path))
+    names = header_functions()
+    assert len(names) >= 19
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(names) == set(_abi.ENTRY_POINTS), set(names) ^ set(_abi.ENTRY_POINTS)
+    assert _abi.load_library().dem_version().decode().startswith("dem_gb300")
+
+
+def test_config_struct_matches_header():
+    src = (ROOT / "include" / "dem_gb300.h").read_text()
+    body = src[src.index("typedef struct DemConfigC {"):src.index("} DemConfigC;")]
+    fields = re.findall(r"(?:double|int64_t)\s+(\w+)", body)
+    assert fields == [f for f, _ in _abi.DemConfigC._fields_]
+    assert len(fields) == 32  # + init_particles = the 33 keys of DEMConfig
+
+
+def test_config_defaults_and_roundtrip(tmp_path):
+    c = DEMConfig()
+    assert c.dt == 2.63e-5 and c.max_coordinate_number == 64 and c.tolerance == 1e-12
+    assert c.total_steps == int(0.5 / 2.63e-5)
+    t = tmp_path / "c.toml"
+    t.write_text(c.replace(dt=1e-6, domain_min=[1.0, 2.0, 3.0]).to_toml())
+    d = DEMConfig.from_toml(t)
+    assert d.dt == 1e-6 and d.domain_min == [1.0, 2.0, 3.0]
+    cc = d.to_c()
+    assert cc.dt == 1e-6 and list(cc.domain_min) == [1.0, 2.0, 3.0]
+    with pytest.raises(ValueError):
+        DEMConfig.from_dict({"no_such_key": 1})
+
+
+@pytest.mark.skipif(not REF_CFG.exists(), reason="reference checkout not present")
+def test_reference_config_files_parse():
+    for f in sorted(REF_CFG.glob("*.toml")):
+        c = DEMConfig.from_toml(f)
+        assert c.dt > 0 and len(c.domain_min) == 3
+
+
+def test_jl_float_format():
+    assert p4io.jl_float(0.5) == "0.5"
+    assert p4io.jl_float(1e-5) == "1.0e-5"
+    assert p4io.jl_float(2.0) == "2.0"
+    assert p4io.jl_float(1e6) == "1.0e6"
+    assert p4io.jl_float(123456.0) == "123456.0"
+    for x in (0.1, 1 / 3, -2.5e-7, 6.02e23, 3.0):
+        assert float(p4io.jl_float(x)) == x
+
+
+def test_p4p_p4c_roundtrip_and_compare(tmp_path):
+    rng = np.random.default_rng(0)
+    n = 20
+    ids = np.arange(1, n + 1)
+    pos, vel = rng.standard_normal((n, 3)), rng.standard_normal((n, 3))
+    vol, mass = rng.uniform(1, 2, n), rng.uniform(1, 2, n)
+    f1, f2 = tmp_path / "a.p4p", tmp_path / "b.p4p"
+    for f, p in ((f1, pos), (f2, pos * (1 + 1e-12))):
+        with open(f, "w") as fh:
+            p4io.write_p4p(fh, 0.0, ids, np.zeros(n), vol, mass, p, vel)
+            p4io.write_p4p(fh, 1e-3, ids, np.zeros(n), vol, mass, p, vel)
+    recs = p4io.read_p4p(f1)
+    assert len(recs) == 2 and np.array_equal(recs[0].pos, pos)
+    p4io.compare_p4p(f1, f2)
+    with open(f2, "w") as fh:
+        p4io.write_p4p(fh, 0.0, ids, np.zeros(n), vol, mass, pos * 1.001, vel)
+        p4io.write_p4p(fh, 1e-3, ids, np.zeros(n), vol, mass, pos, vel)
+    with pytest.raises(AssertionError):
+        p4io.compare_p4p(f1, f2)
+    ci, cj = np.array([0, 2, 1]), np.array([1, 5, 3])
+    pt, fo = rng.standard_normal((3, 3)), rng.standard_normal((3, 3))
+    c1, c2 = tmp_path / "a.p4c", tmp_path / "b.p4c"
+    with open(c1, "w") as fh:
+        p4io.write_p4c(fh, 0.0, ci, cj, pt, fo, [1, 0, 1])
+    order = [2, 0, 1]
+    with open(c2, "w") as fh:
+        p4io.write_p4c(fh, 0.0, ci[order], cj[order], pt[order], fo[order], np.array([1, 0, 1])[order])
+    p4io.compare_p4c(c1, c2)  # compared as sorted pairs
+    r = p4io.read_p4c(c1)[0]
+    assert list(zip(r.i, r.j)) == [(1, 2), (2, 4), (3, 6)]
+    with pytest.raises(RuntimeError):
+        p4io.write_p4c(io.StringIO(), 0.0, [0, 0], [1, 1], pt[:2], fo[:2], [0, 0])
+
+
+def test_bonded_cube_scene():
+    sc = scenes.bonded_cube(4, steps=0)
+    assert sc.n == 64
+    r = np.cbrt(sc.particles.volume / (4 / 3 * np.pi))
+    assert np.all((r > 0.0095 - 1e-12) & (r < 0.0105 + 1e-12))
+    wall_z = -sc.cfg.wall_distance
+    assert np.isclose(np.min(sc.particles.pos[:, 2] - r) - wall_z, 1e-3)
+    assert np.all(sc.particles.vel[:, 2] == -10.0)
+
+
+def test_granular_pour_no_overlap():
+    sc = scenes.granular_pour(8000, box=(0.1, 0.1, 0.1), seed=1)
+    from scipy.spatial import cKDTree
+    p = sc.particles.pos
+    r = np.cbrt(sc.particles.volume / (4 / 3 * np.pi))
+    pairs = cKDTree(p).query_pairs(2 * r.max())
+    for i, j in pairs:
+        assert np.linalg.norm(p[i] - p[j]) >= r[i] + r[j]
+    assert np.all(p > 0) and np.all(p < 0.1)
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(FileNotFoundError):
+        _abi.load_library(tmp_path / "libdem_sm100a.so")
