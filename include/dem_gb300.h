@@ -251,6 +251,33 @@ int dem_debug_broadphase(DemHandle* h, int32_t* cell, uint32_t* morton,
                          uint32_t* sorted, int32_t* cp, int64_t cp_cap,
                          int64_t* cp_n);
 
+/* Bucket sort of the reference broad phase (cell, hashcode, counting sort:
+ * src/utils.jl:1-2, src/kernels.jl:7-22) that allocates nothing.  No
+ * counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory: a host that reserves all
+ * of its GPU buffers up front and forbids allocation afterwards, a process
+ * whose device allocator belongs to another framework, or code running while
+ * allocation is blocked.  The caller passes device pointers: positions
+ * px/py/pz (n each), and the outputs bucket[n] (the reference's 1-based
+ * hashcode) and sorted[n] (particle indices grouped by bucket, ascending
+ * inside a bucket; the same as dem_debug_broadphase's `sorted`).  Work is
+ * queued on `stream` (a cudaStream_t, NULL for the default stream); results
+ * are ready when that stream is synchronised.
+ *
+ * The temporary memory is one 12.6 MB array inside the library, reserved on
+ * every GPU that loads it until the process exits, so n and hash_table_size
+ * are each limited to 1,048,576 (larger values return DEM_ERR_CAPACITY
+ * before any work is queued).  The first call on a device looks up that
+ * array's device address; make that first call before any stream capture on
+ * the device.  Every call reuses the same array: calls whose work overlaps on
+ * the GPU (different streams or threads) race and must be serialised by the
+ * caller. */
+int dem_bucket_sort_noalloc(const double* px, const double* py, const double* pz,
+                            int64_t n, const double* domain_min, double cell_size,
+                            int64_t hash_table_size, uint32_t* bucket,
+                            uint32_t* sorted, void* stream);
+
 /* ---- misc -------------------------------------------------------------- */
 
 const char* dem_strerror(int code);

@@ -128,6 +128,9 @@ ENTRY_POINTS = {
     "dem_get_stats": (C.c_int, [_H, C.POINTER(DemStats)]),
     "dem_debug_broadphase": (C.c_int, [_H, _PI32, _PU32, _PU32, _PU32, _PU32, _PI32, C.c_int64,
                                        C.POINTER(C.c_int64)]),
+    "dem_bucket_sort_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                          C.POINTER(C.c_double), C.c_double, C.c_int64,
+                                          C.c_void_p, C.c_void_p, C.c_void_p]),
     "dem_strerror": (C.c_char_p, [C.c_int]),
     "dem_version": (C.c_char_p, []),
 }

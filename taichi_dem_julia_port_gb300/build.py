@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB_NAME = "libdem_sm100a.so"
 LIB_PATH = PKG / LIB_NAME
-SOURCES = ["dem_kernels.cu", "dem_api.cu"]
+SOURCES = ["dem_kernels.cu", "dem_api.cu", "dem_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -21,7 +21,7 @@ __device__ __forceinline__ int32_t ceil_i32(double t) {
 }
 
 // StaticArrays `norm` (sqrt of ((x²+y²)+z²), rescaled when not in (0, Inf)).
-__device__ __noinline__ double norm_scaled(double x, double y, double z) {
+static __device__ __noinline__ double norm_scaled(double x, double y, double z) {
     if (isnan(x) || isnan(y) || isnan(z)) return CUDART_NAN;
     double sc = fmax(fabs(x), fmax(fabs(y), fabs(z)));
     if (sc == 0.0) return 0.0;
