@@ -153,7 +153,7 @@ int allocate(DemHandle* h) {
     const size_t n = (size_t)h->n, cap = (size_t)h->p.cap, H = h->p.H;
     DemDev& d = h->d;
     double** dbl[] = {&d.px, &d.py, &d.pz, &d.vx, &d.vy, &d.vz, &d.wx, &d.wy, &d.wz,
-                      &d.qw, &d.qx, &d.qy, &d.qz, &d.m, &d.r, &d.r0, &d.inv_inertia,
+                      &d.qw, &d.qx, &d.qy, &d.qz, &d.m, &d.inv_m, &d.r, &d.r0, &d.inv_inertia, &d.b_invA, &d.b_rbI,
                       &d.fx, &d.fy, &d.fz, &d.tx, &d.ty, &d.tz, &d.wsx, &d.wsy, &d.wsz};
     for (double** a : dbl) TRY(dalloc(h, a, n));
     TRY(dalloc(h, &d.cellinfo, n));
@@ -201,7 +201,7 @@ void record_step(DemHandle* h, int cur) {
     launch_broadphase(h->d, h->p, h->ntiles_cells, h->stream);
     launch_detect(h->d, h->p, cur, false, h->stream);
     launch_scan_rows(h->d, h->p, nxt, h->stream);
-    launch_compact(h->d, h->p, cur, false, h->stream);
+    launch_compact(h->d, h->p, cur, false, h->force_grid, h->stream);
     launch_force(h->d, h->p, nxt, h->force_grid, h->stream);
     launch_integrate(h->d, h->p, nxt, h->stream);
 }
@@ -302,7 +302,8 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
     h->n = (int)pin->n;
     const int n = h->n;
     // grain setup (src/executor.jl:219-243)
-    std::vector<double> r(n), r0(n), inv_inertia(n), q0(n, 1.0), zeros(n, 0.0);
+    std::vector<double> r(n), r0(n), inv_inertia(n), inv_m(n), q0(n, 1.0), zeros(n, 0.0);
+    std::vector<double> b_invA(n), b_rbI(n);
     std::vector<double> pos[3], vel[3];
     double rmax_r = -INFINITY;
     for (int c = 0; c < 3; ++c) {
@@ -314,6 +315,12 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
         r[i] = std::cbrt(V / (4.0 / 3.0 * kPi));
         r0[i] = r[i] * cfg->particle_contact_radius_multiplier;
         inv_inertia[i] = 1.0 / (2.0 / 5.0 * m * (r[i] * r[i]));
+        inv_m[i] = 1.0 / m;
+        // bond section of src/kernels.jl:178-184 for rb = ρ·rᵢ: 1/A and rb/I
+        const double rb = cfg->bond_radius_ratio * r[i];
+        const double Ab = rb * rb * kPi, Ib = rb * rb * (rb * rb) * (kPi / 4.0);
+        b_invA[i] = 1.0 / Ab;
+        b_rbI[i] = rb / Ib;
         rmax_r = std::max(rmax_r, r[i]);
         for (int c = 0; c < 3; ++c) {
             pos[c][i] = pin->pos[3 * i + c];
@@ -408,7 +415,7 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
     if (rc != DEM_OK) return fail(rc);
     h->ntiles_cells = scan_tiles((int64_t)p.H);
     h->force_grid = (int)std::max<int64_t>(
-        1, std::min<int64_t>(((int64_t)p.cap + 255) / 256, (int64_t)h->sm_count * 8));
+        1, std::min<int64_t>(((int64_t)p.cap + 255) / 256, (int64_t)h->sm_count * 16));
     auto up = [&](double* dst, const std::vector<double>& src) {
         return n ? cudaMemcpyAsync(dst, src.data(), n * sizeof(double), cudaMemcpyHostToDevice,
                                    h->stream)
@@ -424,6 +431,9 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
     }
     if (e == cudaSuccess) e = up(h->d.qw, q0);
     if (e == cudaSuccess) e = up(h->d.m, mass);
+    if (e == cudaSuccess) e = up(h->d.inv_m, inv_m);
+    if (e == cudaSuccess) e = up(h->d.b_invA, b_invA);
+    if (e == cudaSuccess) e = up(h->d.b_rbI, b_rbI);
     if (e == cudaSuccess) e = up(h->d.r, r);
     if (e == cudaSuccess) e = up(h->d.r0, r0);
     if (e == cudaSuccess) e = up(h->d.inv_inertia, inv_inertia);
@@ -457,7 +467,7 @@ int dem_init_bonds(DemHandle* h) {
     launch_broadphase(h->d, h->p, h->ntiles_cells, h->stream);
     launch_detect(h->d, h->p, cur, true, h->stream);
     launch_scan_rows(h->d, h->p, nxt, h->stream);
-    launch_compact(h->d, h->p, cur, true, h->stream);
+    launch_compact(h->d, h->p, cur, true, h->force_grid, h->stream);
     CU(cudaGetLastError());
     h->cur = nxt;
     return device_error(h);
@@ -505,7 +515,7 @@ int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
     cudaEventRecord(ev[2], h->stream);
     launch_scan_rows(h->d, h->p, nxt, h->stream);
     cudaEventRecord(ev[3], h->stream);
-    launch_compact(h->d, h->p, cur, false, h->stream);
+    launch_compact(h->d, h->p, cur, false, h->force_grid, h->stream);
     cudaEventRecord(ev[4], h->stream);
     launch_force(h->d, h->p, nxt, h->force_grid, h->stream);
     cudaEventRecord(ev[5], h->stream);
@@ -814,8 +824,12 @@ int dem_debug_broadphase(DemHandle* h, int32_t* cell, uint32_t* morton, uint32_t
         }
         if (bucket) bucket[i] = bk[i] + 1u;
     }
+    DevCounters ctr;
+    if (cudaMemcpy(&ctr, h->d.ctr, sizeof(ctr), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return DEM_ERR_CUDA;
     if (bucket_count)
-        for (uint32_t b = 0; b < h->p.H; ++b) bucket_count[b] = start[b + 1] - start[b];
+        for (uint32_t b = 0; b < h->p.H; ++b)
+            bucket_count[b] = b < ctr.cell_limit ? start[b + 1] - start[b] : 0u;
     int err = device_error(h);
     return err != DEM_OK ? err : rc;
 }

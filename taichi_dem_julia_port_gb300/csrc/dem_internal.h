@@ -37,7 +37,9 @@ enum ContactField { CK = 0, CF = 3, CTI = 6, CTJ = 9, CS = 12 };
 
 struct DevCounters {
     int error;
-    int pad;
+    unsigned int bmax;        // largest bucket id of this step (k_hash), reset by the cell scan
+    unsigned int cell_limit;  // buckets [0, cell_limit) have valid starts this step
+    unsigned int pad;
     unsigned long long broken, ended, created, warn_gap, warn_damp;
     unsigned long long scan_tiles;  // tile counter of the decoupled look-back scan
     unsigned long long scan_done;
@@ -48,7 +50,8 @@ struct DemDev {
     // particles, caller order
     double *px, *py, *pz, *vx, *vy, *vz, *wx, *wy, *wz;
     double *qw, *qx, *qy, *qz;
-    double *m, *r, *r0, *inv_inertia;
+    double *m, *inv_m, *r, *r0, *inv_inertia;
+    double *b_invA, *b_rbI;  // bond section constants for rb = ρ·r (1/A, rb/I)
     double *fx, *fy, *fz, *tx, *ty, *tz;  // totals of the last step
     double *wsx, *wsy, *wsz;              // wall shear history (one wall)
     // broad phase
@@ -108,7 +111,8 @@ void launch_broadphase(const DemDev& d, const DemParams& p, int n_scan_tiles_cel
                        cudaStream_t s);
 void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, cudaStream_t s);
 void launch_scan_rows(const DemDev& d, const DemParams& p, int nxt, cudaStream_t s);
-void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, cudaStream_t s);
+void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, int grid,
+                    cudaStream_t s);
 void launch_force(const DemDev& d, const DemParams& p, int nxt, int grid, cudaStream_t s);
 void launch_integrate(const DemDev& d, const DemParams& p, int nxt, cudaStream_t s);
 

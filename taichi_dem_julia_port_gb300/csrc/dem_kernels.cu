@@ -25,7 +25,7 @@ namespace dem {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kScanBlock = 256;
+constexpr int kScanBlock = 1024;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanBlock * kScanItems;
 constexpr unsigned long long kSpinLimit = 1ull << 24;
@@ -48,7 +48,10 @@ __device__ __forceinline__ int row_at(const int32_t* rp, int i, int cap) {
 // every wait is bounded and raises kErrTimeout when the bound is hit.  The
 // last tile to finish resets the tile states and counters for the next launch.
 // out has count+1 entries; out[count] is the total.
-template <typename T>
+// LIMITED: the bucket-count scan covers only [0, bmax] (bmax = largest bucket
+// this step, from k_hash); tiles past it exit at once, cell_limit records the
+// covered range and bmax is reset for the next step.
+template <typename T, bool LIMITED>
 __global__ void __launch_bounds__(kScanBlock)
     k_scan_excl(const T* __restrict__ in, T* __restrict__ out, long long count, int ntiles,
                 unsigned long long* state, DevCounters* ctr) {
@@ -56,81 +59,96 @@ __global__ void __launch_bounds__(kScanBlock)
     __shared__ int s_last;
     __shared__ unsigned long long s_warp[kScanBlock / 32];
     __shared__ unsigned long long s_prefix;
+    if (LIMITED) {
+        const long long lim = (long long)ctr->bmax + 1;
+        count = lim < count ? lim : count;
+    }
+    const int ntiles_eff = (int)((count + kScanTile - 1) / kScanTile);
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(&ctr->scan_tiles, 1ull);
     __syncthreads();
     const int tile = s_tile;
-    const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
-    unsigned long long v[kScanItems];
-    unsigned long long sum = 0;
+    if (tile < ntiles_eff) {
+        const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
+        T v[kScanItems];
+        unsigned long long sum = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        long long idx = base + k;
-        v[k] = idx < count ? (unsigned long long)in[idx] : 0ull;
-        sum += v[k];
-    }
-    unsigned long long x = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane_id() >= (unsigned)o) x += y;
-    }
-    const int warp = threadIdx.x >> 5;
-    if (lane_id() == 31) s_warp[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        unsigned long long w = lane_id() < kScanBlock / 32 ? s_warp[lane_id()] : 0ull;
+        for (int k = 0; k < kScanItems; ++k) {
+            long long idx = base + k;
+            v[k] = idx < count ? in[idx] : (T)0;
+            sum += (unsigned long long)v[k];
+        }
+        unsigned long long x = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane_id() >= (unsigned)o) w += y;
+            unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane_id() >= (unsigned)o) x += y;
         }
-        if (lane_id() < kScanBlock / 32) s_warp[lane_id()] = w;
-    }
-    __syncthreads();
-    const unsigned long long agg = s_warp[kScanBlock / 32 - 1];
-    const unsigned long long texcl = (warp ? s_warp[warp - 1] : 0ull) + x - sum;
-    if (threadIdx.x == 0) {
-        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> me(state[tile]);
-        unsigned long long prefix = 0;
-        if (tile == 0) {
-            me.store(kFlagIncl | (agg & kValMask), cuda::memory_order_release);
-        } else {
-            me.store(kFlagAgg | (agg & kValMask), cuda::memory_order_release);
-            for (int q = tile - 1; q >= 0; --q) {
-                cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> pr(state[q]);
-                unsigned long long st = 0;
-                for (unsigned long long it = 0;; ++it) {
-                    st = pr.load(cuda::memory_order_acquire);
-                    if (st >> 62) break;
-                    if (it > kSpinLimit) {
-                        raise_error(ctr, kErrTimeout);
-                        st = kFlagIncl;
-                        break;
-                    }
-                    __nanosleep(64);
-                }
-                prefix += st & kValMask;
-                if ((st & ~kValMask) == kFlagIncl) break;
+        const int warp = threadIdx.x >> 5;
+        if (lane_id() == 31) s_warp[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long w = lane_id() < kScanBlock / 32 ? s_warp[lane_id()] : 0ull;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane_id() >= (unsigned)o) w += y;
             }
-            me.store(kFlagIncl | ((prefix + agg) & kValMask), cuda::memory_order_release);
+            if (lane_id() < kScanBlock / 32) s_warp[lane_id()] = w;
         }
-        s_prefix = prefix;
-        if (tile == ntiles - 1) out[count] = (T)(prefix + agg);
+        __syncthreads();
+        const unsigned long long agg = s_warp[kScanBlock / 32 - 1];
+        const unsigned long long texcl = (warp ? s_warp[warp - 1] : 0ull) + x - sum;
+        if (threadIdx.x == 0) {
+            cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> me(state[tile]);
+            unsigned long long prefix = 0;
+            if (tile == 0) {
+                me.store(kFlagIncl | (agg & kValMask), cuda::memory_order_release);
+            } else {
+                me.store(kFlagAgg | (agg & kValMask), cuda::memory_order_release);
+                for (int q = tile - 1; q >= 0; --q) {
+                    cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> pr(state[q]);
+                    unsigned long long st = 0;
+                    for (unsigned long long it = 0;; ++it) {
+                        st = pr.load(cuda::memory_order_acquire);
+                        if (st >> 62) break;
+                        if (it > kSpinLimit) {
+                            raise_error(ctr, kErrTimeout);
+                            st = kFlagIncl;
+                            break;
+                        }
+                        __nanosleep(64);
+                    }
+                    prefix += st & kValMask;
+                    if ((st & ~kValMask) == kFlagIncl) break;
+                }
+                me.store(kFlagIncl | ((prefix + agg) & kValMask), cuda::memory_order_release);
+            }
+            s_prefix = prefix;
+            if (tile == ntiles_eff - 1) out[count] = (T)(prefix + agg);
+        }
+        __syncthreads();
+        unsigned long long run = s_prefix + texcl;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            long long idx = base + k;
+            if (idx < count) out[idx] = (T)run;
+            run += (unsigned long long)v[k];
+        }
+    }
+    if (threadIdx.x == 0) {
         __threadfence();
         unsigned long long done = atomicAdd(&ctr->scan_done, 1ull);
         s_last = (done == (unsigned long long)ntiles - 1) ? 1 : 0;
     }
     __syncthreads();
-    unsigned long long run = s_prefix + texcl;
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        long long idx = base + k;
-        if (idx < count) out[idx] = (T)run;
-        run += v[k];
-    }
     if (s_last) {
-        for (int t = threadIdx.x; t < ntiles; t += kScanBlock) state[t] = 0ull;
+        for (int t = threadIdx.x; t < ntiles_eff; t += kScanBlock) state[t] = 0ull;
         if (threadIdx.x == 0) {
+            if (count == 0) out[0] = (T)0;
+            if (LIMITED) {
+                ctr->cell_limit = (unsigned int)count;
+                ctr->bmax = 0u;
+            }
             ctr->scan_tiles = 0ull;
             ctr->scan_done = 0ull;
         }
@@ -163,6 +181,8 @@ __global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p) {
     if (act) {
         const unsigned peers = __match_any_sync(mask, b);
         if (lane_id() == (unsigned)(__ffs(peers) - 1)) atomicAdd(&d.cell_count[b], __popc(peers));
+        const unsigned wmax = __reduce_max_sync(mask, b);
+        if (lane_id() == (unsigned)(__ffs(mask) - 1)) atomicMax(&d.ctr->bmax, wmax);
     }
 }
 
@@ -203,33 +223,62 @@ __global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p) {
 
 // ---------------------------------------------------------------------------
 // cp_list enumeration fused with `update_contacts!` (src/kernels.jl:87-120) or
-// `init_bonds!` (src/kernels.jl:60-85).  One thread per particle i, in bucket
-// order.  Pairs (i, j) with j > i in one of i's 8 octant buckets are the
-// reference's cp_list.
+// `init_bonds!` (src/kernels.jl:60-85).  Eight lanes per particle i (in
+// bucket order), lane t taking the t-th of i's octant buckets in the order of
+// `neighbors` (src/utils.jl:4-16); pairs (i, j) with j > i in those buckets are
+// the reference's cp_list.  A bucket that repeats an earlier lane's bucket is
+// skipped, so a pair listed twice in cp_list is handled once.
 //  * existing Hertz contact (i, j): ends iff the pair is in cp_list and no
 //    longer touching; bonded contacts survive (breakage is decided by the
 //    force kernel); contacts broken last step are dropped.
-//  * new contact: touching, not yet in row i; appended once even when the
-//    pair appears twice in cp_list.
+//  * new contact: touching and not in row i.  Row membership is checked
+//    before the FP64 distance test, so bonded neighbours cost no FP64 work.
+constexpr int kLanes = 8;
+__device__ __forceinline__ void bucket_range(const DemDev& d, uint32_t b, uint32_t lim,
+                                             uint32_t* s, uint32_t* e) {
+    if (b < lim) {
+        *s = d.cell_start[b];
+        *e = d.cell_start[b + 1];
+    } else {
+        *s = *e = 0u;
+    }
+}
+
 template <bool INIT>
 __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int cur) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ int s_new[kThreads / kLanes];
+    const int lane = threadIdx.x & (kLanes - 1);
+    const int g = threadIdx.x / kLanes;
+    const int k = blockIdx.x * (kThreads / kLanes) + g;
+    if (lane == 0) s_new[g] = 0;
+    __syncwarp();
     if (k >= p.n) return;
+    const unsigned gmask = 0xffu << (lane_id() & ~7u);
     const int i = (int)d.sorted[k];
     const double4_32a P = d.spos[k];
     const float4 P32 = d.spos32[k];
     const int4 ci = d.cellinfo[i];
+    const int dx = (ci.w & 1) ? 1 : -1, dy = (ci.w & 2) ? 1 : -1, dz = (ci.w & 4) ? 1 : -1;
+    const int ox = (lane == 1 || lane == 4 || lane == 5 || lane == 7) ? dx : 0;
+    const int oy = (lane == 2 || lane == 4 || lane == 6 || lane == 7) ? dy : 0;
+    const int oz = (lane == 3 || lane == 5 || lane == 6 || lane == 7) ? dz : 0;
+    const uint32_t myB = bucket_of(ci.x + ox, ci.y + oy, ci.z + oz, p);
     uint32_t B[8];
-    buckets8(ci, p, B);
+    bool dup = false;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        B[u] = __shfl_sync(gmask, myB, u, kLanes);
+        dup |= (u < lane) && (B[u] == myB);
+    }
     const double ri = INIT ? d.r0[i] : P.w;
 
     const ContactSoA o = d.c[cur];
     const int e0 = row_at(d.row_ptr[cur], i, p.cap), e1 = row_at(d.row_ptr[cur], i + 1, p.cap);
     int nkeep = 0;
-    unsigned long long ended = 0;
-    for (int e = e0; e < e1; ++e) {
+    int ended = 0;
+    for (int e = e0 + lane; e < e1; e += kLanes) {
         const uint32_t fl = o.fl[e];
-        uint8_t keep;
+        int keep;
         if (!(fl & kActive)) {
             keep = 0;
         } else if (INIT || (fl & kBonded)) {
@@ -242,103 +291,115 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
 #pragma unroll
             for (int t = 0; t < 8; ++t) in_cp |= (B[t] == bj);
             keep = (valid || !in_cp) ? 1 : 0;
-            ended += keep ? 0ull : 1ull;
+            ended += 1 - keep;
         }
-        d.keep[e] = keep;
+        d.keep[e] = (uint8_t)keep;
         nkeep += keep;
     }
+    nkeep = __reduce_add_sync(gmask, nkeep);
+    ended = __reduce_add_sync(gmask, ended);
 
-    int nnew = 0;
     int32_t* stash = d.stash + (size_t)i * p.kstash;
-    for (int t = 0; t < 8; ++t) {
-        const uint32_t b = B[t];
-        const uint32_t s = d.cell_start[b], e = d.cell_start[b + 1];
-        for (uint32_t q = s; q < e; ++q) {
-            const int j = (int)d.sorted[q];
-            if (j <= i) continue;
-            if (!INIT && !maybe_touching32(P32, d.spos32[q])) continue;
-            const double4_32a Q = d.spos[q];
-            const double rj = INIT ? d.r0[j] : Q.w;
-            if (!touching_rn(P.x, P.y, P.z, Q.x, Q.y, Q.z, ri, rj)) continue;
-            bool found = false;
-            for (int e2 = e0; e2 < e1 && !found; ++e2)
-                found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
-            if (found) continue;
-            const int lim = nnew < p.kstash ? nnew : p.kstash;
-            for (int u = 0; u < lim && !found; ++u) found = stash[u] == j;
-            if (found) continue;
-            if (nnew < p.kstash) stash[nnew] = j;
-            ++nnew;
+    uint32_t s, e;
+    bucket_range(d, myB, d.ctr->cell_limit, &s, &e);
+    if (dup) e = s;
+    for (uint32_t q = s; q < e; ++q) {
+        const int j = (int)d.sorted[q];
+        const float4 Q32 = d.spos32[q];
+        if (j <= i) continue;
+        if (!INIT && !maybe_touching32(P32, Q32)) continue;
+        bool found = false;
+        for (int e2 = e0; e2 < e1 && !found; ++e2) found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
+        if (found) continue;
+        const double4_32a Q = d.spos[q];
+        const double rj = INIT ? d.r0[j] : Q.w;
+        if (!touching_rn(P.x, P.y, P.z, Q.x, Q.y, Q.z, ri, rj)) continue;
+        const int slot = atomicAdd(&s_new[g], 1);
+        if (slot < p.kstash) stash[slot] = j;
+    }
+    __syncwarp(gmask);
+    if (lane == 0) {
+        int nnew = s_new[g];
+        if (nnew > p.kstash) {
+            raise_error(d.ctr, kErrCapacity);
+            nnew = p.kstash;
         }
+        for (int a2 = 1; a2 < nnew; ++a2) {  // new partners ascending
+            const int v = stash[a2];
+            int b2 = a2 - 1;
+            while (b2 >= 0 && stash[b2] > v) {
+                stash[b2 + 1] = stash[b2];
+                --b2;
+            }
+            stash[b2 + 1] = v;
+        }
+        d.nnew[i] = nnew;
+        d.cnt[i] = nkeep + nnew;
+        if (ended) atomicAdd(&d.ctr->ended, (unsigned long long)ended);
+        if (!INIT && nnew) atomicAdd(&d.ctr->created, (unsigned long long)nnew);
     }
-    if (nnew > p.kstash) {
-        raise_error(d.ctr, kErrCapacity);
-        nnew = p.kstash;
-    }
-    d.nnew[i] = nnew;
-    d.cnt[i] = nkeep + nnew;
-    if (ended) atomicAdd(&d.ctr->ended, ended);
-    if (!INIT && nnew) atomicAdd(&d.ctr->created, (unsigned long long)nnew);
 }
 
 // Rolling-array rebuild (the reference's remove_inactive_contact! + swap,
 // src/kernels.jl:487-506, src/executor.jl:140-153): row i of buffer cur^1 is
-// the merge, by j, of the surviving entries of row i and the new partners.
+// the merge, by j, of the surviving entries of row i and the sorted new
+// partners.  One thread per old contact (coalesced copies) and one per
+// particle for its new contacts; each computes its final slot directly.
 template <bool INIT>
 __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int cur) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
     const int nxt = cur ^ 1;
     const int total = d.row_ptr[nxt][p.n];
     if (total > p.cap) {
-        if (i == 0) raise_error(d.ctr, kErrCapacity);
+        if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(d.ctr, kErrCapacity);
         return;
     }
+    const int* rpo = d.row_ptr[cur];
+    const int* rpn = d.row_ptr[nxt];
+    const int cold = row_at(rpo, p.n, p.cap);
     const ContactSoA o = d.c[cur];
     const ContactSoA w = d.c[nxt];
-    const int e0 = row_at(d.row_ptr[cur], i, p.cap), e1 = row_at(d.row_ptr[cur], i + 1, p.cap);
-    int dst = d.row_ptr[nxt][i];
-    const int nn = d.nnew[i];
-    int32_t* st = d.stash + (size_t)i * p.kstash;
-    for (int a = 1; a < nn; ++a) {  // insertion sort of the new partners
-        const int v = st[a];
-        int b = a - 1;
-        while (b >= 0 && st[b] > v) {
-            st[b + 1] = st[b];
-            --b;
-        }
-        st[b + 1] = v;
-    }
-    int e = e0, u = 0;
-    while (true) {
-        while (e < e1 && !d.keep[e]) ++e;
-        const bool has_old = e < e1, has_new = u < nn;
-        if (!has_old && !has_new) break;
-        const bool take_old = has_old && (!has_new || o.cj[e] < st[u]);
-        int j;
-        if (take_old) {
-            j = o.cj[e];
-            w.ci[dst] = i;
-            w.cj[dst] = j;
-            w.fl[dst] = o.fl[e];
+    const int stride = gridDim.x * blockDim.x;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cold + p.n; t += stride) {
+        if (t < cold) {
+            if (!d.keep[t]) continue;
+            const int i = o.ci[t], j = o.cj[t];
+            int pos = rpn[i];
+            for (int q = row_at(rpo, i, p.cap); q < t; ++q) pos += d.keep[q];
+            const int nn = d.nnew[i];
+            const int32_t* st = d.stash + (size_t)i * p.kstash;
+            for (int u = 0; u < nn; ++u) pos += st[u] < j ? 1 : 0;
+            w.ci[pos] = i;
+            w.cj[pos] = j;
+            w.fl[pos] = o.fl[t];
 #pragma unroll
-            for (int f = 0; f < 15; ++f) w.f[f][dst] = o.f[f][e];
-            ++e;
+            for (int f = 0; f < 15; ++f) w.f[f][pos] = o.f[f][t];
+            if (!INIT) {
+                const int slot = atomicAdd(&d.in_cnt[j], 1);
+                if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = pos;
+                else raise_error(d.ctr, kErrCapacity);
+            }
         } else {
-            j = st[u];
-            w.ci[dst] = i;
-            w.cj[dst] = j;
-            w.fl[dst] = INIT ? (kActive | kBonded) : kActive;
+            const int i = t - cold;
+            const int nn = d.nnew[i];
+            if (!nn) continue;
+            const int e0 = row_at(rpo, i, p.cap), e1 = row_at(rpo, i + 1, p.cap);
+            const int32_t* st = d.stash + (size_t)i * p.kstash;
+            for (int u = 0; u < nn; ++u) {
+                const int j = st[u];
+                int pos = rpn[i] + u;
+                for (int q = e0; q < e1; ++q) pos += (d.keep[q] && o.cj[q] < j) ? 1 : 0;
+                w.ci[pos] = i;
+                w.cj[pos] = j;
+                w.fl[pos] = INIT ? (kActive | kBonded) : kActive;
 #pragma unroll
-            for (int f = 0; f < 15; ++f) w.f[f][dst] = 0.0;
-            ++u;
+                for (int f = 0; f < 15; ++f) w.f[f][pos] = 0.0;
+                if (!INIT) {
+                    const int slot = atomicAdd(&d.in_cnt[j], 1);
+                    if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = pos;
+                    else raise_error(d.ctr, kErrCapacity);
+                }
+            }
         }
-        if (!INIT) {
-            const int slot = atomicAdd(&d.in_cnt[j], 1);
-            if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = dst;
-            else raise_error(d.ctr, kErrCapacity);
-        }
-        ++dst;
     }
 }
 
@@ -401,6 +462,51 @@ __device__ __forceinline__ Vec3<T> from_d(Vec3<double> v) {
     return {(T)v.x, (T)v.y, (T)v.z};
 }
 
+// The frame with the normal a already computed approximately (rsqrt).  Far
+// from the degenerate case (s = |a × x̂| >= 2·tolerance) both branches of the
+// reference are decided the same way and the general formula is used; near
+// it, a and s are recomputed exactly as the reference does (normalize and norm
+// without contraction) so the branch matches the reference bit for bit.
+__device__ __forceinline__ Frame contact_frame_fast(double dx, double dy, double dz, double ax,
+                                                    double ay, double az, double tol) {
+    const double s2 = ay * ay + az * az;
+    if (s2 < 4.0 * tol * tol) {
+        const double L = norm_rn(dx, dy, dz);
+        const double il = __ddiv_rn(1.0, L);
+        return contact_frame(__dmul_rn(il, dx), __dmul_rn(il, dy), __dmul_rn(il, dz), tol);
+    }
+    Frame F;
+    const double f = (1.0 - ax) / s2;
+    F.r[0][0] = ax; F.r[0][1] = ay; F.r[0][2] = az;
+    F.r[1][0] = -ay; F.r[1][1] = 1.0 - ay * ay * f; F.r[1][2] = -ay * az * f;
+    F.r[2][0] = -az; F.r[2][1] = -ay * az * f; F.r[2][2] = 1.0 - az * az * f;
+    return F;
+}
+
+// EBPM failure (src/kernels.jl:208-219):
+//   σcᵢ = -Fₓ/A - (r/I)·sqrt(τᵢ₂²+τᵢ₃²), σc = -min(σcᵢ, σcⱼ), σt = max(σcᵢ, σcⱼ),
+//   σs = |τᵢ₁|·r/2/I + 4/3/A·sqrt(F₂²+F₃²);  breaks if σc >= σc₀ or σt >= σt₀ or
+//   σs >= σs₀.
+// Each comparison is evaluated without its square root: sqrt(a)·k >= R is
+// R <= 0 or a·k² >= R², and sqrt(a)·k <= R is R >= 0 and a·k² <= R² (k > 0).
+// A NaN operand makes a comparison false, as in the reference.
+__device__ __forceinline__ bool bond_breaks(const Vec3<double>& F, const Vec3<double>& ti,
+                                            const Vec3<double>& tj, double invA, double rbI,
+                                            const DemParams& p) {
+    const double ai = ti.y * ti.y + ti.z * ti.z, aj = tj.y * tj.y + tj.z * tj.z;
+    const double amax = jl_max(ai, aj), amin = jl_min(ai, aj);
+    const double fa = F.x * invA, k2 = rbI * rbI;
+    const double Rc = p.b_sc - fa;     // σc >= σc₀  <=>  rbI·sqrt(amax) >= Rc
+    const double Rt = -(p.b_st + fa);  // σt >= σt₀  <=>  rbI·sqrt(amin) <= Rt
+    const double Rs = p.b_ss - fabs(ti.x) * (0.5 * rbI);  // σs >= σs₀ <=> 4/3·invA·sqrt(b) >= Rs
+    const double b = F.y * F.y + F.z * F.z;
+    const double ks = (4.0 / 3.0) * invA;
+    const bool comp = !isnan(amax) && (Rc <= 0.0 || amax * k2 >= Rc * Rc);
+    const bool tens = !isnan(amin) && Rt >= 0.0 && amin * k2 <= Rt * Rt;
+    const bool shear = !isnan(b) && !isnan(Rs) && (Rs <= 0.0 || b * (ks * ks) >= Rs * Rs);
+    return comp || tens || shear;
+}
+
 // `resolve_collision!` for one active contact (src/kernels.jl:136-313).  T is
 // the arithmetic type of the force model: double (DEM_FP64) or float
 // (DEM_FP32_FORCE).  Relative quantities (overlap, relative displacement and
@@ -426,13 +532,13 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
         const int i = w.ci[c], j = w.cj[c];
         const Vec3<double> ki{d.px[i], d.py[i], d.pz[i]}, kj{d.px[j], d.py[j], d.pz[j]};
         const double ri = d.r[i], rj = d.r[j];
-        // normal, exactly as normalize(𝐤ⱼ - 𝐤ᵢ) and norm(𝐤ⱼ - 𝐤ᵢ)
-        const double dx = __dsub_rn(kj.x, ki.x), dy = __dsub_rn(kj.y, ki.y),
-                     dz = __dsub_rn(kj.z, ki.z);
-        const double L = norm_rn(dx, dy, dz);
-        const double invL = __ddiv_rn(1.0, L);
-        const double ax = __dmul_rn(invL, dx), ay = __dmul_rn(invL, dy), az = __dmul_rn(invL, dz);
-        const Frame R = contact_frame(ax, ay, az, p.tol);
+        // normal and length; the frame's branch is decided on the exact
+        // reference values when the normal is within 2·tolerance of ±x̂
+        const double dx = kj.x - ki.x, dy = kj.y - ki.y, dz = kj.z - ki.z;
+        const double invL = rsqrt(dx * dx + dy * dy + dz * dz);
+        const double L = (dx * dx + dy * dy + dz * dz) * invL;
+        const double ax = dx * invL, ay = dy * invL, az = dz * invL;
+        const Frame R = contact_frame_fast(dx, dy, dz, ax, ay, az, p.tol);
         const Vec3<double> vi{d.vx[i], d.vy[i], d.vz[i]}, vj{d.vx[j], d.vy[j], d.vz[j]};
         const Vec3<double> wi{d.wx[i], d.wy[i], d.wz[i]}, wj{d.wx[j], d.wy[j], d.wz[j]};
         Vec3<T> fig, mi, mj;
@@ -464,15 +570,9 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
             Fi = {Fi.x + (double)dFx, Fi.y + (double)dFy, Fi.z + (double)dFz};
             ti = {ti.x + (double)dtix, ti.y + (double)dtiy, ti.z + (double)dtiz};
             tj = {tj.x + (double)dtjx, tj.y + (double)dtjy, tj.z + (double)dtjz};
-            // breakage test, FP64 (src/kernels.jl:208-222)
-            const double invA = 1.0 / Ab;
-            const double rbI = rb / Ib;
-            const double sci = -Fi.x * invA - rbI * sqrt(ti.y * ti.y + ti.z * ti.z);
-            const double scj = -Fi.x * invA - rbI * sqrt(tj.y * tj.y + tj.z * tj.z);
-            const double sc = -jl_min(sci, scj);
-            const double stt = jl_max(sci, scj);
-            const double ss = fabs(ti.x) * (0.5 * rbI) + (4.0 / 3.0) * invA * sqrt(Fi.y * Fi.y + Fi.z * Fi.z);
-            if (sc >= p.b_sc || stt >= p.b_st || ss >= p.b_ss) {
+            // breakage test, FP64 (src/kernels.jl:208-222), see bond_breaks()
+            const int small = ri <= rj ? i : j;  // rb = ρ·min(rᵢ, rⱼ)
+            if (bond_breaks(Fi, ti, tj, d.b_invA[small], d.b_rbI[small], p)) {
                 w.fl[c] = 0u;  // contact_active and contact_bonded bits cleared
                 ++nbroken;
                 fig = {(T)0, (T)0, (T)0};
@@ -560,6 +660,7 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
 // inv(𝐑)·inv(𝐈)·(𝐑𝛕 - 𝐑𝛚 × 𝐈𝐑𝛚) is 𝛕 / I exactly in real arithmetic and the
 // quaternion only evolves as state.
 constexpr int kMaxIncoming = 64;
+constexpr int kRegIncoming = 16;
 __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, int nxt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -578,23 +679,50 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     d.in_cnt[i] = 0;
     nin = nin < p.kin ? nin : p.kin;
     nin = nin < kMaxIncoming ? nin : kMaxIncoming;
-    int inc[kMaxIncoming];
     const int* il = d.in_list + (size_t)i * p.kin;
-    for (int t = 0; t < nin; ++t) {
-        const int v = il[t];
-        int b = t - 1;
-        while (b >= 0 && inc[b] > v) {
-            inc[b + 1] = inc[b];
-            --b;
-        }
-        inc[b + 1] = v;
-    }
-    for (int t = 0; t < nin; ++t) {
-        const int c = inc[t];
+    if (nin <= kRegIncoming) {
+        // ascending contact index, sorted in registers (odd-even transposition)
+        int v[kRegIncoming];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            F[q] += -d.contrib[q * cap + c];
-            M[q] += d.contrib[(6 + q) * cap + c];
+        for (int t = 0; t < kRegIncoming; ++t) v[t] = t < nin ? il[t] : 0x7fffffff;
+#pragma unroll
+        for (int r = 0; r < kRegIncoming; ++r) {
+#pragma unroll
+            for (int t = r & 1; t + 1 < kRegIncoming; t += 2) {
+                const int lo = min(v[t], v[t + 1]), hi = max(v[t], v[t + 1]);
+                v[t] = lo;
+                v[t + 1] = hi;
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < kRegIncoming; ++t) {
+            if (t < nin) {
+                const int c = v[t];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    F[q] += -d.contrib[q * cap + c];
+                    M[q] += d.contrib[(6 + q) * cap + c];
+                }
+            }
+        }
+    } else {
+        int inc[kMaxIncoming];
+        for (int t = 0; t < nin; ++t) {
+            const int v = il[t];
+            int b = t - 1;
+            while (b >= 0 && inc[b] > v) {
+                inc[b + 1] = inc[b];
+                --b;
+            }
+            inc[b + 1] = v;
+        }
+        for (int t = 0; t < nin; ++t) {
+            const int c = inc[t];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                F[q] += -d.contrib[q * cap + c];
+                M[q] += d.contrib[(6 + q) * cap + c];
+            }
         }
     }
     const double x = d.px[i], y = d.py[i], z = d.pz[i];
@@ -679,7 +807,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
         }
     }
     // update!
-    const double invm = 1.0 / m;
+    const double invm = d.inv_m[i];
     const double ax = F[0] * invm, ay = F[1] * invm, az = F[2] * invm;
     const double hdt2 = 0.5 * (dt * dt);
     d.px[i] = x + vx * dt + ax * hdt2;
@@ -694,7 +822,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     const double dq2 = 0.5 * (qw * wy + qx * wz + qz * wx);
     const double dq3 = 0.5 * (qw * wz + qx * wy - qy * wx);
     const double nw = qw + dq0, nx = qx + dq1, ny = qy + dq2, nz = qz + dq3;
-    const double inq = 1.0 / sqrt(nw * nw + nx * nx + ny * ny + nz * nz);
+    const double inq = rsqrt(nw * nw + nx * nx + ny * ny + nz * nz);
     d.qw[i] = nw * inq;
     d.qx[i] = nx * inq;
     d.qy[i] = ny * inq;
@@ -724,10 +852,13 @@ __global__ void k_cp_count(DemDev d, DemParams p, int32_t* cnt) {
     if (i >= p.n) return;
     uint32_t B[8];
     buckets8(d.cellinfo[i], p, B);
+    const uint32_t lim = d.ctr->cell_limit;
     int c = 0;
-    for (int t = 0; t < 8; ++t)
-        for (uint32_t q = d.cell_start[B[t]]; q < d.cell_start[B[t] + 1]; ++q)
-            c += (int)d.sorted[q] > i ? 1 : 0;
+    for (int t = 0; t < 8; ++t) {
+        uint32_t s, e;
+        bucket_range(d, B[t], lim, &s, &e);
+        for (uint32_t q = s; q < e; ++q) c += (int)d.sorted[q] > i ? 1 : 0;
+    }
     cnt[i] = c;
 }
 // update_cp_list! (src/kernels.jl:39-58)
@@ -736,9 +867,12 @@ __global__ void k_cp_fill(DemDev d, DemParams p, const int32_t* off, int32_t* cp
     if (i >= p.n) return;
     uint32_t B[8];
     buckets8(d.cellinfo[i], p, B);
+    const uint32_t lim = d.ctr->cell_limit;
     int o = off[i];
-    for (int t = 0; t < 8; ++t)
-        for (uint32_t q = d.cell_start[B[t]]; q < d.cell_start[B[t] + 1]; ++q) {
+    for (int t = 0; t < 8; ++t) {
+        uint32_t s, e;
+        bucket_range(d, B[t], lim, &s, &e);
+        for (uint32_t q = s; q < e; ++q) {
             const int j = (int)d.sorted[q];
             if (j > i) {
                 cp[2 * o] = i;
@@ -746,6 +880,7 @@ __global__ void k_cp_fill(DemDev d, DemParams p, const int32_t* off, int32_t* cp
                 ++o;
             }
         }
+    }
 }
 
 inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
@@ -760,14 +895,14 @@ void launch_scan_i32(const int32_t* in, int32_t* out, int64_t n, const DemDev& d
         cudaMemsetAsync(out, 0, sizeof(int32_t), s);
         return;
     }
-    k_scan_excl<int32_t><<<nt, kScanBlock, 0, s>>>(in, out, n, nt, d.scan_state, d.ctr);
+    k_scan_excl<int32_t, false><<<nt, kScanBlock, 0, s>>>(in, out, n, nt, d.scan_state, d.ctr);
 }
 
 void launch_broadphase(const DemDev& d, const DemParams& p, int ntiles_cells, cudaStream_t s) {
     if (p.n == 0) return;
     const int nb = blocks_for(p.n, kThreads);
     k_hash<<<nb, kThreads, 0, s>>>(d, p);
-    k_scan_excl<uint32_t><<<ntiles_cells, kScanBlock, 0, s>>>(d.cell_count, d.cell_start,
+    k_scan_excl<uint32_t, true><<<ntiles_cells, kScanBlock, 0, s>>>(d.cell_count, d.cell_start,
                                                                (long long)p.H, ntiles_cells,
                                                                d.scan_state, d.ctr);
     k_scatter<<<nb, kThreads, 0, s>>>(d, p);
@@ -776,7 +911,7 @@ void launch_broadphase(const DemDev& d, const DemParams& p, int ntiles_cells, cu
 
 void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, cudaStream_t s) {
     if (p.n == 0) return;
-    const int nb = blocks_for(p.n, kThreads);
+    const int nb = blocks_for((long long)p.n * kLanes, kThreads);
     if (init) k_detect<true><<<nb, kThreads, 0, s>>>(d, p, cur);
     else k_detect<false><<<nb, kThreads, 0, s>>>(d, p, cur);
 }
@@ -785,9 +920,10 @@ void launch_scan_rows(const DemDev& d, const DemParams& p, int nxt, cudaStream_t
     launch_scan_i32(d.cnt, d.row_ptr[nxt], p.n, d, s);
 }
 
-void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, cudaStream_t s) {
+void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, int grid,
+                    cudaStream_t s) {
     if (p.n == 0) return;
-    const int nb = blocks_for(p.n, kThreads);
+    const int nb = min(blocks_for((long long)p.cap + p.n, kThreads), grid);
     if (init) k_compact<true><<<nb, kThreads, 0, s>>>(d, p, cur);
     else k_compact<false><<<nb, kThreads, 0, s>>>(d, p, cur);
 }
