@@ -49,7 +49,7 @@ FORCE_BYTES_HERTZ = 12 + 176 + 24 + 72 + 72
 # Algorithmic bytes of the other phases per particle / per contact
 BROADPHASE_BYTES_PER_PARTICLE = 24 + 16 + 4 + 4 + 4 + 8 + 24 + 8 + 32 + 16  # hash..canon
 INTEGRATE_BYTES_PER_PARTICLE = 13 * 8 * 2 + 4 * 8 + 6 * 8 + 3 * 8 * 2 + 8 + 4  # state r/w
-KERNELS_PER_STEP = 9  # hash, scan, scatter, canon, detect, scan, compact, force, integrate
+KERNELS_PER_STEP = 8  # hash, scan, scatter, canon, detect, compact, force, integrate
 L2_FLUSH_BYTES = 256 << 20
 
 

@@ -195,9 +195,10 @@ int dem_step(DemHandle* h, int64_t nsteps);
 int dem_step_timed(DemHandle* h, int64_t nsteps, float* ms);
 
 /* One step launched phase by phase (no graph) with CUDA events between the
- * phases on the handle's stream.  phase_ms[0..5] receive the device time of:
+ * phases on the handle's stream.  phase_ms[0..4] receive the device time of:
  * broad phase (hash, bucket scan, scatter, canonical order), contact
- * detection, row scan, contact compaction, contact forces, integration.
+ * detection (with row allocation), contact compaction, contact forces,
+ * integration.
  * No counterpart in the reference: per-kernel timing for roofline reports. */
 int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase);
 

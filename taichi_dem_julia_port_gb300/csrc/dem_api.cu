@@ -154,6 +154,7 @@ int allocate(DemHandle* h) {
     DemDev& d = h->d;
     double** dbl[] = {&d.px, &d.py, &d.pz, &d.vx, &d.vy, &d.vz, &d.wx, &d.wy, &d.wz,
                       &d.qw, &d.qx, &d.qy, &d.qz, &d.m, &d.inv_m, &d.r, &d.r0, &d.inv_inertia, &d.b_invA, &d.b_rbI,
+                      &d.b_EA, &d.b_EI, &d.b_phic,
                       &d.fx, &d.fy, &d.fz, &d.tx, &d.ty, &d.tz, &d.wsx, &d.wsy, &d.wsz};
     for (double** a : dbl) TRY(dalloc(h, a, n));
     TRY(dalloc(h, &d.cellinfo, n));
@@ -169,17 +170,17 @@ int allocate(DemHandle* h) {
         TRY(dalloc(h, &d.c[b].cj, cap));
         TRY(dalloc(h, &d.c[b].fl, cap));
         for (int f = 0; f < 15; ++f) TRY(dalloc(h, &d.c[b].f[f], cap));
-        TRY(dalloc(h, &d.row_ptr[b], n + 1));
+        TRY(dalloc(h, &d.row_start[b], n));
+        TRY(dalloc(h, &d.row_len[b], n));
     }
-    TRY(dalloc(h, &d.cnt, n));
     TRY(dalloc(h, &d.nnew, n));
     TRY(dalloc(h, &d.stash, n * (size_t)h->p.kstash));
     TRY(dalloc(h, &d.keep, cap));
     TRY(dalloc(h, &d.in_cnt, n));
     TRY(dalloc(h, &d.in_list, n * (size_t)h->p.kin));
     TRY(dalloc(h, &d.contrib, 9 * cap));
-    const int tiles = std::max(scan_tiles((int64_t)H), scan_tiles((int64_t)n + 1));
-    TRY(dalloc(h, &d.scan_state, (size_t)tiles));
+    TRY(dalloc(h, &d.scan_state[kScanCells], (size_t)scan_tiles((int64_t)H)));
+    TRY(dalloc(h, &d.scan_state[kScanDebug], (size_t)scan_tiles((int64_t)n)));
     TRY(dalloc(h, &d.ctr, 1));
     return DEM_OK;
 }
@@ -200,10 +201,9 @@ void record_step(DemHandle* h, int cur) {
     const int nxt = cur ^ 1;
     launch_broadphase(h->d, h->p, h->ntiles_cells, h->stream);
     launch_detect(h->d, h->p, cur, false, h->stream);
-    launch_scan_rows(h->d, h->p, nxt, h->stream);
     launch_compact(h->d, h->p, cur, false, h->force_grid, h->stream);
     launch_force(h->d, h->p, nxt, h->force_grid, h->stream);
-    launch_integrate(h->d, h->p, nxt, h->stream);
+    launch_integrate(h->d, h->p, cur, h->stream);
 }
 
 int build_graphs(DemHandle* h) {
@@ -240,10 +240,12 @@ int device_error(DemHandle* h) {
     return DEM_OK;
 }
 
-int download_row_ptr_total(DemHandle* h, int buf, int32_t* total) {
-    CU(cudaMemcpyAsync(total, h->d.row_ptr[buf] + h->n, sizeof(int32_t), cudaMemcpyDeviceToHost,
+int contact_count(DemHandle* h, int buf, int32_t* total) {
+    unsigned int v = 0;
+    CU(cudaMemcpyAsync(&v, &h->d.ctr->row_alloc[buf], sizeof(v), cudaMemcpyDeviceToHost,
                        h->stream));
     CU(cudaStreamSynchronize(h->stream));
+    *total = (int32_t)v;
     return DEM_OK;
 }
 
@@ -303,7 +305,7 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
     const int n = h->n;
     // grain setup (src/executor.jl:219-243)
     std::vector<double> r(n), r0(n), inv_inertia(n), inv_m(n), q0(n, 1.0), zeros(n, 0.0);
-    std::vector<double> b_invA(n), b_rbI(n);
+    std::vector<double> b_invA(n), b_rbI(n), b_EA(n), b_EI(n), b_phic(n);
     std::vector<double> pos[3], vel[3];
     double rmax_r = -INFINITY;
     for (int c = 0; c < 3; ++c) {
@@ -321,6 +323,9 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
         const double Ab = rb * rb * kPi, Ib = rb * rb * (rb * rb) * (kPi / 4.0);
         b_invA[i] = 1.0 / Ab;
         b_rbI[i] = rb / Ib;
+        b_EA[i] = cfg->bond_elastic_modulus * Ab;
+        b_EI[i] = cfg->bond_elastic_modulus * Ib;
+        b_phic[i] = 20.0 / 3.0 * (1.0 + cfg->bond_poisson_ratio) * (rb * rb);
         rmax_r = std::max(rmax_r, r[i]);
         for (int c = 0; c < 3; ++c) {
             pos[c][i] = pin->pos[3 * i + c];
@@ -365,6 +370,7 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
         p.wn[c] = cfg->wall_normal[c];
     }
     p.cell = D.cell_size;
+    p.inv_cell = 1.0 / D.cell_size;
     p.dt = cfg->dt;
     p.tol = cfg->tolerance;
     p.damping = cfg->global_damping;
@@ -434,6 +440,9 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
     if (e == cudaSuccess) e = up(h->d.inv_m, inv_m);
     if (e == cudaSuccess) e = up(h->d.b_invA, b_invA);
     if (e == cudaSuccess) e = up(h->d.b_rbI, b_rbI);
+    if (e == cudaSuccess) e = up(h->d.b_EA, b_EA);
+    if (e == cudaSuccess) e = up(h->d.b_EI, b_EI);
+    if (e == cudaSuccess) e = up(h->d.b_phic, b_phic);
     if (e == cudaSuccess) e = up(h->d.r, r);
     if (e == cudaSuccess) e = up(h->d.r0, r0);
     if (e == cudaSuccess) e = up(h->d.inv_inertia, inv_inertia);
@@ -466,8 +475,9 @@ int dem_init_bonds(DemHandle* h) {
     const int cur = h->cur, nxt = cur ^ 1;
     launch_broadphase(h->d, h->p, h->ntiles_cells, h->stream);
     launch_detect(h->d, h->p, cur, true, h->stream);
-    launch_scan_rows(h->d, h->p, nxt, h->stream);
     launch_compact(h->d, h->p, cur, true, h->force_grid, h->stream);
+    // the old buffer becomes the next step's target: its allocator starts at 0
+    CU(cudaMemsetAsync(&h->d.ctr->row_alloc[cur], 0, sizeof(unsigned int), h->stream));
     CU(cudaGetLastError());
     h->cur = nxt;
     return device_error(h);
@@ -500,30 +510,28 @@ int dem_step_timed(DemHandle* h, int64_t nsteps, float* ms) {
 }
 
 int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
-    if (!h || !phase_ms || nphase < 6) return DEM_ERR_INVALID;
+    if (!h || !phase_ms || nphase < 5) return DEM_ERR_INVALID;
     if (h->n == 0) {
-        for (int k = 0; k < 6; ++k) phase_ms[k] = 0.f;
+        for (int k = 0; k < 5; ++k) phase_ms[k] = 0.f;
         return DEM_OK;
     }
-    cudaEvent_t ev[7];
-    for (int k = 0; k < 7; ++k) CU(cudaEventCreate(&ev[k]));
+    cudaEvent_t ev[6];
+    for (int k = 0; k < 6; ++k) CU(cudaEventCreate(&ev[k]));
     const int cur = h->cur, nxt = cur ^ 1;
     cudaEventRecord(ev[0], h->stream);
     launch_broadphase(h->d, h->p, h->ntiles_cells, h->stream);
     cudaEventRecord(ev[1], h->stream);
     launch_detect(h->d, h->p, cur, false, h->stream);
     cudaEventRecord(ev[2], h->stream);
-    launch_scan_rows(h->d, h->p, nxt, h->stream);
-    cudaEventRecord(ev[3], h->stream);
     launch_compact(h->d, h->p, cur, false, h->force_grid, h->stream);
-    cudaEventRecord(ev[4], h->stream);
+    cudaEventRecord(ev[3], h->stream);
     launch_force(h->d, h->p, nxt, h->force_grid, h->stream);
+    cudaEventRecord(ev[4], h->stream);
+    launch_integrate(h->d, h->p, cur, h->stream);
     cudaEventRecord(ev[5], h->stream);
-    launch_integrate(h->d, h->p, nxt, h->stream);
-    cudaEventRecord(ev[6], h->stream);
-    cudaError_t e = cudaEventSynchronize(ev[6]);
-    for (int k = 0; k < 6 && e == cudaSuccess; ++k) e = cudaEventElapsedTime(&phase_ms[k], ev[k], ev[k + 1]);
-    for (int k = 0; k < 7; ++k) cudaEventDestroy(ev[k]);
+    cudaError_t e = cudaEventSynchronize(ev[5]);
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = cudaEventElapsedTime(&phase_ms[k], ev[k], ev[k + 1]);
+    for (int k = 0; k < 6; ++k) cudaEventDestroy(ev[k]);
     CU(e);
     h->cur = nxt;
     h->steps += 1;
@@ -643,7 +651,7 @@ int dem_get_contacts(DemHandle* h, DemContacts* out, int64_t cap, int64_t* n_out
     if (!h || !n_out) return DEM_ERR_INVALID;
     TRY(device_error(h));
     int32_t C = 0;
-    if (h->n) TRY(download_row_ptr_total(h, h->cur, &C));
+    if (h->n) TRY(contact_count(h, h->cur, &C));
     C = std::min(C, h->p.cap);
     const ContactSoA& s = h->d.c[h->cur];
     std::vector<int32_t> ci(C), cj(C);
@@ -656,14 +664,19 @@ int dem_get_contacts(DemHandle* h, DemContacts* out, int64_t cap, int64_t* n_out
         for (int q = 0; q < 15; ++q) TRY(get_dev(f[q], s.f[q], (size_t)C, h->stream));
         CU(cudaStreamSynchronize(h->stream));
     }
-    int64_t na = 0;
-    for (int32_t c = 0; c < C; ++c) na += (fl[c] & kActive) ? 1 : 0;
+    std::vector<int32_t> act;  // active contacts, sorted by (i, j)
+    act.reserve(C);
+    for (int32_t c = 0; c < C; ++c)
+        if (fl[c] & kActive) act.push_back(c);
+    std::sort(act.begin(), act.end(), [&](int32_t a, int32_t b) {
+        return ci[a] != ci[b] ? ci[a] < ci[b] : cj[a] < cj[b];
+    });
+    const int64_t na = (int64_t)act.size();
     *n_out = na;
     if (!out) return DEM_OK;
     if (na > cap) return DEM_ERR_CAPACITY;
-    int64_t t = 0;
-    for (int32_t c = 0; c < C; ++c) {
-        if (!(fl[c] & kActive)) continue;
+    for (int64_t t = 0; t < na; ++t) {
+        const int32_t c = act[t];
         if (out->i) out->i[t] = ci[c];
         if (out->j) out->j[t] = cj[c];
         if (out->bonded) out->bonded[t] = (fl[c] & kBonded) ? 1 : 0;
@@ -674,7 +687,6 @@ int dem_get_contacts(DemHandle* h, DemContacts* out, int64_t cap, int64_t* n_out
             if (out->torque_j) out->torque_j[3 * t + q] = f[CTJ + q][c];
             if (out->shear) out->shear[3 * t + q] = f[CS + q][c];
         }
-        ++t;
     }
     return DEM_OK;
 }
@@ -693,7 +705,7 @@ int dem_set_contacts(DemHandle* h, const DemContacts* in, int64_t nc) {
     for (int64_t t = 1; t < nc; ++t)
         if (in->i[order[t]] == in->i[order[t - 1]] && in->j[order[t]] == in->j[order[t - 1]])
             return DEM_ERR_INVALID;
-    std::vector<int32_t> rp(n + 1, 0), ci(nc), cj(nc);
+    std::vector<int32_t> rs(n, 0), rl(n, 0), ci(nc), cj(nc);
     std::vector<uint32_t> fl(nc);
     std::vector<double> f[15];
     for (int q = 0; q < 15; ++q) f[q].assign(nc, 0.0);
@@ -702,13 +714,13 @@ int dem_set_contacts(DemHandle* h, const DemContacts* in, int64_t nc) {
         ci[t] = in->i[s];
         cj[t] = in->j[s];
         fl[t] = kActive | ((in->bonded && in->bonded[s]) ? kBonded : 0u);
-        rp[ci[t] + 1]++;
+        rl[ci[t]]++;
         const double* src[5] = {in->point, in->force, in->torque_i, in->torque_j, in->shear};
         for (int g = 0; g < 5; ++g)
             if (src[g])
                 for (int q = 0; q < 3; ++q) f[3 * g + q][t] = src[g][3 * s + q];
     }
-    for (int i = 0; i < n; ++i) rp[i + 1] += rp[i];
+    for (int i = 1; i < n; ++i) rs[i] = rs[i - 1] + rl[i - 1];
     const ContactSoA& s = h->d.c[h->cur];
     if (nc) {
         CU(cudaMemcpyAsync(s.ci, ci.data(), nc * 4, cudaMemcpyHostToDevice, h->stream));
@@ -717,7 +729,14 @@ int dem_set_contacts(DemHandle* h, const DemContacts* in, int64_t nc) {
         for (int q = 0; q < 15; ++q)
             CU(cudaMemcpyAsync(s.f[q], f[q].data(), nc * 8, cudaMemcpyHostToDevice, h->stream));
     }
-    CU(cudaMemcpyAsync(h->d.row_ptr[h->cur], rp.data(), (n + 1) * 4, cudaMemcpyHostToDevice,
+    if (n) {
+        CU(cudaMemcpyAsync(h->d.row_start[h->cur], rs.data(), n * 4, cudaMemcpyHostToDevice,
+                           h->stream));
+        CU(cudaMemcpyAsync(h->d.row_len[h->cur], rl.data(), n * 4, cudaMemcpyHostToDevice,
+                           h->stream));
+    }
+    const unsigned int alloc[2] = {h->cur == 0 ? (unsigned)nc : 0u, h->cur == 1 ? (unsigned)nc : 0u};
+    CU(cudaMemcpyAsync(h->d.ctr->row_alloc, alloc, sizeof(alloc), cudaMemcpyHostToDevice,
                        h->stream));
     CU(cudaStreamSynchronize(h->stream));
     return DEM_OK;
@@ -728,7 +747,7 @@ int dem_get_stats(DemHandle* h, DemStats* out) {
     DevCounters c;
     TRY(read_counters(h, &c));
     int32_t C = 0;
-    if (h->n) TRY(download_row_ptr_total(h, h->cur, &C));
+    if (h->n) TRY(contact_count(h, h->cur, &C));
     C = std::min(C, h->p.cap);
     std::vector<uint32_t> fl(C);
     if (C) CU(cudaMemcpy(fl.data(), h->d.c[h->cur].fl, C * 4, cudaMemcpyDeviceToHost));
@@ -781,7 +800,7 @@ int dem_debug_broadphase(DemHandle* h, int32_t* cell, uint32_t* morton, uint32_t
     }
     launch_morton(h->d, h->p, dmorton, h->stream);
     launch_cplist_count(h->d, h->p, dcnt, h->stream);
-    launch_scan_i32(dcnt, doff, n, h->d, h->stream);
+    launch_scan_i32(dcnt, doff, n, h->d, kScanDebug, h->stream);
     int32_t total = 0;
     cudaMemcpyAsync(&total, doff + n, 4, cudaMemcpyDeviceToHost, h->stream);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) {

@@ -7,8 +7,9 @@
 //    hash_table), and particle copies in bucket-sorted order (double4 x,y,z,r
 //    and a float4 copy relative to domain_min for the distance pre-filter);
 //  * contacts: two buffers (the reference's contacts / contacts_temp rolling
-//    pair), each a structure of arrays in CSR form — row i holds the contacts
-//    (i, j) with j > i, sorted by j; row_ptr has n+1 entries;
+//    pair), each a structure of arrays of rows — row i holds the contacts
+//    (i, j) with j > i, sorted by j, at [row_start[i], row_start[i]+row_len[i]);
+//    rows are placed by an atomic allocator, so the buffers need no scan;
 //  * per-contact force contributions (9 FP64 values) and a per-particle list
 //    of incoming contacts (those where the particle is j) used to sum forces
 //    per particle in a fixed order, without floating-point atomics.
@@ -37,13 +38,17 @@ enum ContactField { CK = 0, CF = 3, CTI = 6, CTJ = 9, CS = 12 };
 
 struct DevCounters {
     int error;
-    unsigned int bmax;        // largest bucket id of this step (k_hash), reset by the cell scan
+    unsigned int bmax;        // largest bucket id of this step (k_hash), reset by k_canon
     unsigned int cell_limit;  // buckets [0, cell_limit) have valid starts this step
     unsigned int pad;
+    unsigned int row_alloc[2];  // contacts allocated in each contact buffer
     unsigned long long broken, ended, created, warn_gap, warn_damp;
-    unsigned long long scan_tiles;  // tile counter of the decoupled look-back scan
-    unsigned long long scan_done;
+    unsigned long long tickets[2];  // tile tickets of the scan sites (never reset)
 };
+
+// scan sites: each has its own ticket counter and tile-state array
+constexpr int kScanCells = 0;
+constexpr int kScanDebug = 1;
 
 // Device pointers of one scene (passed by value to every kernel).
 struct DemDev {
@@ -52,6 +57,7 @@ struct DemDev {
     double *qw, *qx, *qy, *qz;
     double *m, *inv_m, *r, *r0, *inv_inertia;
     double *b_invA, *b_rbI;  // bond section constants for rb = ρ·r (1/A, rb/I)
+    double *b_EA, *b_EI, *b_phic;  // E·A, E·I and 20/3·(1+ν)·rb² for rb = ρ·r
     double *fx, *fy, *fz, *tx, *ty, *tz;  // totals of the last step
     double *wsx, *wsy, *wsz;              // wall shear history (one wall)
     // broad phase
@@ -65,16 +71,16 @@ struct DemDev {
     float4* spos32;        // n, (x-ox, y-oy, z-oz, r) in FP32, sorted order
     // contacts
     ContactSoA c[2];
-    int32_t* row_ptr[2];  // n + 1
-    int32_t* cnt;         // n (row sizes, scan input)
-    int32_t* nnew;        // n
+    int32_t* row_start[2];  // n, first slot of each particle's row
+    int32_t* row_len[2];    // n, entries in the row
+    int32_t* nnew;          // n
     int32_t* stash;       // n * kstash new partners of this step
     uint8_t* keep;        // cap, survival flags of the current buffer
     int32_t* in_cnt;      // n, zero between steps
-    int32_t* in_list;     // n * kin
+    int2* in_list;        // n * kin: (contact slot, owner i) of contacts where the particle is j
     double* contrib;      // 9 * cap, [field][contact]
-    // scan scratch
-    unsigned long long* scan_state;  // tiles
+    // scan scratch: tile states of each scan site
+    unsigned long long* scan_state[2];
     DevCounters* ctr;
 };
 
@@ -89,7 +95,7 @@ struct DemParams {
     int has_wall;
     int precision;  // 0 = FP64, 1 = FP32 force
     double dmin[3];
-    double cell;
+    double cell, inv_cell;
     double dt, tol;
     double grav[3];
     double damping;
@@ -110,11 +116,10 @@ struct DemParams {
 void launch_broadphase(const DemDev& d, const DemParams& p, int n_scan_tiles_cells,
                        cudaStream_t s);
 void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, cudaStream_t s);
-void launch_scan_rows(const DemDev& d, const DemParams& p, int nxt, cudaStream_t s);
 void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, int grid,
                     cudaStream_t s);
 void launch_force(const DemDev& d, const DemParams& p, int nxt, int grid, cudaStream_t s);
-void launch_integrate(const DemDev& d, const DemParams& p, int nxt, cudaStream_t s);
+void launch_integrate(const DemDev& d, const DemParams& p, int cur, cudaStream_t s);
 
 // debug: cp_list materialisation on the current bucket arrays
 void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cudaStream_t s);
@@ -122,7 +127,7 @@ void launch_cplist_fill(const DemDev& d, const DemParams& p, const int32_t* off,
                         cudaStream_t s);
 void launch_morton(const DemDev& d, const DemParams& p, uint32_t* morton, cudaStream_t s);
 // exclusive scan of n int32 values into out[0..n] (out[n] = total)
-void launch_scan_i32(const int32_t* in, int32_t* out, int64_t n, const DemDev& d,
+void launch_scan_i32(const int32_t* in, int32_t* out, int64_t n, const DemDev& d, int site,
                      cudaStream_t s);
 
 int scan_tiles(int64_t n);

@@ -2,23 +2,21 @@
 //
 // One step (the reference's `simulate!`, src/executor.jl:162-172) is
 //   k_hash       cell, Morton bucket, octant; warp-aggregated bucket counts
-//   k_scan       exclusive scan of the H bucket counts (single pass, decoupled
-//                look-back)                                   -> bucket starts
+//   k_scan       exclusive scan of the occupied bucket range (single pass,
+//                decoupled look-back)                          -> bucket starts
 //   k_scatter    counting-sort scatter (warp-aggregated atomics; the counts
 //                return to zero, so the table needs no clearing)
 //   k_canon      ascending index inside each bucket + bucket-sorted copies of
 //                the positions (FP64 and an FP32 copy for the pre-filter)
 //   k_detect     cp_list enumeration fused with update_contacts!: existing
-//                contacts decide survival, new touching pairs are stashed
-//   k_scan       exclusive scan of the new row sizes          -> row_ptr
+//                contacts decide survival, new touching pairs are stashed,
+//                each particle's new row is allocated (block-aggregated atomic)
 //   k_compact    rolling-array rebuild: surviving + new contacts, rows sorted
 //                by j; incoming-contact lists for the force gather
 //   k_force      resolve_collision! per contact (EBPM or Hertz-Mindlin)
 //   k_integrate  per particle: contact force gather in a fixed order,
 //                resolve_wall!, apply_body_force!, update!
 // All of it is captured once in a CUDA graph per contact-buffer parity.
-#include <cstdio>
-
 #include "dem_device.cuh"
 
 namespace dem {
@@ -29,34 +27,34 @@ constexpr int kScanBlock = 1024;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanBlock * kScanItems;
 constexpr unsigned long long kSpinLimit = 1ull << 24;
-constexpr unsigned long long kFlagAgg = 1ull << 62;
-constexpr unsigned long long kFlagIncl = 2ull << 62;
-constexpr unsigned long long kValMask = (1ull << 62) - 1;
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
-// Row bound clamped to the buffer capacity: after a capacity overflow (which
-// raises kErrCapacity) no kernel reads or writes past the contact buffers.
-__device__ __forceinline__ int row_at(const int32_t* rp, int i, int cap) {
-    const int v = rp[i];
-    return v < 0 ? 0 : (v < cap ? v : cap);
-}
 
 // ---------------------------------------------------------------------------
-// Exclusive scan, single pass with decoupled look-back.  Tiles are taken in
-// launch order from a counter, so a tile only waits for tiles already running;
-// every wait is bounded and raises kErrTimeout when the bound is hit.  The
-// last tile to finish resets the tile states and counters for the next launch.
+// Exclusive scan, single pass with decoupled look-back.  Every CTA draws a
+// ticket from its scan site's counter; a launch draws exactly `ntiles`
+// tickets, so tile = ticket mod ntiles and the launch's epoch = ticket div
+// ntiles + 1.  Tiles are processed in ticket order, so a tile only waits for
+// tiles that are already running; each wait is bounded and raises
+// kErrTimeout when the bound is hit.  Tile states carry the epoch, so nothing
+// has to be reset between launches.
+//   state word: epoch (30 bits) | flag (2 bits: 1 aggregate, 2 inclusive) | value (32 bits)
 // out has count+1 entries; out[count] is the total.
 // LIMITED: the bucket-count scan covers only [0, bmax] (bmax = largest bucket
-// this step, from k_hash); tiles past it exit at once, cell_limit records the
-// covered range and bmax is reset for the next step.
+// this step, from k_hash); tiles past it exit at once and cell_limit records
+// the covered range.
+constexpr unsigned long long kEpochMask = (1ull << 30) - 1;
+__device__ __forceinline__ unsigned long long scan_word(unsigned long long epoch, unsigned flag,
+                                                        unsigned long long v) {
+    return ((epoch & kEpochMask) << 34) | ((unsigned long long)flag << 32) | (v & 0xffffffffull);
+}
+
 template <typename T, bool LIMITED>
 __global__ void __launch_bounds__(kScanBlock)
     k_scan_excl(const T* __restrict__ in, T* __restrict__ out, long long count, int ntiles,
-                unsigned long long* state, DevCounters* ctr) {
-    __shared__ int s_tile;
-    __shared__ int s_last;
+                unsigned long long* state, unsigned long long* tickets, DevCounters* ctr) {
+    __shared__ unsigned long long s_ticket;
     __shared__ unsigned long long s_warp[kScanBlock / 32];
     __shared__ unsigned long long s_prefix;
     if (LIMITED) {
@@ -64,98 +62,100 @@ __global__ void __launch_bounds__(kScanBlock)
         count = lim < count ? lim : count;
     }
     const int ntiles_eff = (int)((count + kScanTile - 1) / kScanTile);
-    if (threadIdx.x == 0) s_tile = (int)atomicAdd(&ctr->scan_tiles, 1ull);
+    if (threadIdx.x == 0) s_ticket = atomicAdd(tickets, 1ull);
     __syncthreads();
-    const int tile = s_tile;
-    if (tile < ntiles_eff) {
-        const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
-        T v[kScanItems];
-        unsigned long long sum = 0;
+    const int tile = (int)(s_ticket % (unsigned long long)ntiles);
+    const unsigned long long epoch = (s_ticket / (unsigned long long)ntiles + 1ull) & kEpochMask;
+    if (tile == 0 && threadIdx.x == 0) {
+        if (LIMITED) ctr->cell_limit = (unsigned int)count;
+        if (count == 0) out[0] = (T)0;
+    }
+    if (tile >= ntiles_eff) return;
+    const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
+    T v[kScanItems];
+    unsigned long long sum = 0;
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            long long idx = base + k;
-            v[k] = idx < count ? in[idx] : (T)0;
-            sum += (unsigned long long)v[k];
-        }
-        unsigned long long x = sum;
+    for (int k = 0; k < kScanItems; ++k) {
+        const long long idx = base + k;
+        v[k] = idx < count ? in[idx] : (T)0;
+        sum += (unsigned long long)v[k];
+    }
+    unsigned long long x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane_id() >= (unsigned)o) x += y;
+    }
+    const int warp = threadIdx.x >> 5;
+    if (lane_id() == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long w = s_warp[lane_id()];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane_id() >= (unsigned)o) x += y;
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane_id() >= (unsigned)o) w += y;
         }
-        const int warp = threadIdx.x >> 5;
-        if (lane_id() == 31) s_warp[warp] = x;
-        __syncthreads();
-        if (warp == 0) {
-            unsigned long long w = lane_id() < kScanBlock / 32 ? s_warp[lane_id()] : 0ull;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane_id() >= (unsigned)o) w += y;
-            }
-            if (lane_id() < kScanBlock / 32) s_warp[lane_id()] = w;
-        }
-        __syncthreads();
-        const unsigned long long agg = s_warp[kScanBlock / 32 - 1];
-        const unsigned long long texcl = (warp ? s_warp[warp - 1] : 0ull) + x - sum;
-        if (threadIdx.x == 0) {
-            cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> me(state[tile]);
-            unsigned long long prefix = 0;
-            if (tile == 0) {
-                me.store(kFlagIncl | (agg & kValMask), cuda::memory_order_release);
-            } else {
-                me.store(kFlagAgg | (agg & kValMask), cuda::memory_order_release);
-                for (int q = tile - 1; q >= 0; --q) {
-                    cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> pr(state[q]);
-                    unsigned long long st = 0;
-                    for (unsigned long long it = 0;; ++it) {
-                        st = pr.load(cuda::memory_order_acquire);
-                        if (st >> 62) break;
-                        if (it > kSpinLimit) {
-                            raise_error(ctr, kErrTimeout);
-                            st = kFlagIncl;
-                            break;
-                        }
-                        __nanosleep(64);
-                    }
-                    prefix += st & kValMask;
-                    if ((st & ~kValMask) == kFlagIncl) break;
-                }
-                me.store(kFlagIncl | ((prefix + agg) & kValMask), cuda::memory_order_release);
-            }
-            s_prefix = prefix;
-            if (tile == ntiles_eff - 1) out[count] = (T)(prefix + agg);
-        }
-        __syncthreads();
-        unsigned long long run = s_prefix + texcl;
-#pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            long long idx = base + k;
-            if (idx < count) out[idx] = (T)run;
-            run += (unsigned long long)v[k];
-        }
-    }
-    if (threadIdx.x == 0) {
-        __threadfence();
-        unsigned long long done = atomicAdd(&ctr->scan_done, 1ull);
-        s_last = (done == (unsigned long long)ntiles - 1) ? 1 : 0;
+        s_warp[lane_id()] = w;
     }
     __syncthreads();
-    if (s_last) {
-        for (int t = threadIdx.x; t < ntiles_eff; t += kScanBlock) state[t] = 0ull;
-        if (threadIdx.x == 0) {
-            if (count == 0) out[0] = (T)0;
-            if (LIMITED) {
-                ctr->cell_limit = (unsigned int)count;
-                ctr->bmax = 0u;
+    const unsigned long long agg = s_warp[kScanBlock / 32 - 1];
+    const unsigned long long texcl = (warp ? s_warp[warp - 1] : 0ull) + x - sum;
+    if (threadIdx.x == 0) {
+        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> me(state[tile]);
+        unsigned long long prefix = 0;
+        if (tile == 0) {
+            me.store(scan_word(epoch, 2u, agg), cuda::memory_order_release);
+        } else {
+            me.store(scan_word(epoch, 1u, agg), cuda::memory_order_release);
+            for (int q = tile - 1; q >= 0; --q) {
+                cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> pr(state[q]);
+                unsigned long long st = 0;
+                unsigned flag = 0;
+                for (unsigned long long it = 0;; ++it) {
+                    st = pr.load(cuda::memory_order_acquire);
+                    flag = (unsigned)(st >> 32) & 3u;
+                    if ((st >> 34) == epoch && flag) break;
+                    if (it > kSpinLimit) {
+                        raise_error(ctr, kErrTimeout);
+                        flag = 2u;
+                        st = 0;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+                prefix += st & 0xffffffffull;
+                if (flag == 2u) break;
             }
-            ctr->scan_tiles = 0ull;
-            ctr->scan_done = 0ull;
+            me.store(scan_word(epoch, 2u, prefix + agg), cuda::memory_order_release);
         }
+        s_prefix = prefix;
+        if (tile == ntiles_eff - 1) out[count] = (T)(prefix + agg);
+    }
+    __syncthreads();
+    unsigned long long run = s_prefix + texcl;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const long long idx = base + k;
+        if (idx < count) out[idx] = (T)run;
+        run += (unsigned long long)v[k];
     }
 }
 
 // ---------------------------------------------------------------------------
+// ceil(num / cell) with num / cell rounded as IEEE division (src/utils.jl:1).
+// q = num·(1/cell) is within 2^-51·|q| of the rounded quotient; when no
+// integer lies within 2^-49·|q| of q, both have the same ceiling.  Otherwise
+// (rare: q must sit within ~10^-15 relative of an integer) the quotient is
+// computed by the correctly rounded division.
+__device__ __forceinline__ int32_t cell_index(double num, const DemParams& p) {
+    const double q = num * p.inv_cell;
+    const double d = fabs(q) * 0x1p-49;
+    const double lo = ceil(q - d), hi = ceil(q + d);
+    if (lo == hi && lo > -2147483648.0 && lo < 2147483647.0) return (int32_t)lo;
+    return ceil_i32(__ddiv_rn(num, p.cell));
+}
+
 // `cell`, `hashcode`, `center`, `neighbors` (src/utils.jl:1-16) and
 // `count_particles!` (src/kernels.jl:7-13).
 __global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p) {
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p) {
         int oct = 0;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            ijk[c] = ceil_i32(__ddiv_rn(__dsub_rn(pos[c], p.dmin[c]), p.cell));
+            ijk[c] = cell_index(__dsub_rn(pos[c], p.dmin[c]), p);
             const double ctr =
                 __dadd_rn(p.dmin[c], __dmul_rn(__dsub_rn((double)ijk[c], 0.5), p.cell));
             if (pos[c] > ctr) oct |= 1 << c;
@@ -204,9 +204,11 @@ __global__ void __launch_bounds__(kThreads) k_scatter(DemDev d, DemParams p) {
 }
 
 // Canonical order inside a bucket (ascending particle index) and the sorted
-// position copies used by the pair search.
+// position copies used by the pair search.  Also clears this step's bucket
+// maximum (all its readers have finished).
 __global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) d.ctr->bmax = 0u;
     if (k >= p.n) return;
     const uint32_t i = d.unsorted[k];
     const uint32_t b = d.bucket[i];
@@ -231,9 +233,12 @@ __global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p) {
 //  * existing Hertz contact (i, j): ends iff the pair is in cp_list and no
 //    longer touching; bonded contacts survive (breakage is decided by the
 //    force kernel); contacts broken last step are dropped.
-//  * new contact: touching and not in row i.  Row membership is checked
-//    before the FP64 distance test, so bonded neighbours cost no FP64 work.
+//  * new contact: touching and not in row i.  Row membership (from a shared
+//    memory copy of row i) is checked before the FP64 distance test, so
+//    bonded neighbours cost no FP64 work.
 constexpr int kLanes = 8;
+constexpr int kRowCache = 24;
+constexpr int kBatch = 4;
 __device__ __forceinline__ void bucket_range(const DemDev& d, uint32_t b, uint32_t lim,
                                              uint32_t* s, uint32_t* e) {
     if (b < lim) {
@@ -247,96 +252,152 @@ __device__ __forceinline__ void bucket_range(const DemDev& d, uint32_t b, uint32
 template <bool INIT>
 __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int cur) {
     __shared__ int s_new[kThreads / kLanes];
+    __shared__ int s_row[kThreads / kLanes][kRowCache];
+    __shared__ int s_tot[kThreads / kLanes];
+    __shared__ int s_base;
     const int lane = threadIdx.x & (kLanes - 1);
     const int g = threadIdx.x / kLanes;
     const int k = blockIdx.x * (kThreads / kLanes) + g;
-    if (lane == 0) s_new[g] = 0;
-    __syncwarp();
-    if (k >= p.n) return;
-    const unsigned gmask = 0xffu << (lane_id() & ~7u);
-    const int i = (int)d.sorted[k];
-    const double4_32a P = d.spos[k];
-    const float4 P32 = d.spos32[k];
-    const int4 ci = d.cellinfo[i];
-    const int dx = (ci.w & 1) ? 1 : -1, dy = (ci.w & 2) ? 1 : -1, dz = (ci.w & 4) ? 1 : -1;
-    const int ox = (lane == 1 || lane == 4 || lane == 5 || lane == 7) ? dx : 0;
-    const int oy = (lane == 2 || lane == 4 || lane == 6 || lane == 7) ? dy : 0;
-    const int oz = (lane == 3 || lane == 5 || lane == 6 || lane == 7) ? dz : 0;
-    const uint32_t myB = bucket_of(ci.x + ox, ci.y + oy, ci.z + oz, p);
-    uint32_t B[8];
-    bool dup = false;
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-        B[u] = __shfl_sync(gmask, myB, u, kLanes);
-        dup |= (u < lane) && (B[u] == myB);
-    }
-    const double ri = INIT ? d.r0[i] : P.w;
-
-    const ContactSoA o = d.c[cur];
-    const int e0 = row_at(d.row_ptr[cur], i, p.cap), e1 = row_at(d.row_ptr[cur], i + 1, p.cap);
-    int nkeep = 0;
-    int ended = 0;
-    for (int e = e0 + lane; e < e1; e += kLanes) {
-        const uint32_t fl = o.fl[e];
-        int keep;
-        if (!(fl & kActive)) {
-            keep = 0;
-        } else if (INIT || (fl & kBonded)) {
-            keep = 1;
-        } else {
-            const int j = o.cj[e];
-            const bool valid = touching_rn(P.x, P.y, P.z, d.px[j], d.py[j], d.pz[j], P.w, d.r[j]);
-            const uint32_t bj = d.bucket[j];
-            bool in_cp = false;
-#pragma unroll
-            for (int t = 0; t < 8; ++t) in_cp |= (B[t] == bj);
-            keep = (valid || !in_cp) ? 1 : 0;
-            ended += 1 - keep;
-        }
-        d.keep[e] = (uint8_t)keep;
-        nkeep += keep;
-    }
-    nkeep = __reduce_add_sync(gmask, nkeep);
-    ended = __reduce_add_sync(gmask, ended);
-
-    int32_t* stash = d.stash + (size_t)i * p.kstash;
-    uint32_t s, e;
-    bucket_range(d, myB, d.ctr->cell_limit, &s, &e);
-    if (dup) e = s;
-    for (uint32_t q = s; q < e; ++q) {
-        const int j = (int)d.sorted[q];
-        const float4 Q32 = d.spos32[q];
-        if (j <= i) continue;
-        if (!INIT && !maybe_touching32(P32, Q32)) continue;
-        bool found = false;
-        for (int e2 = e0; e2 < e1 && !found; ++e2) found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
-        if (found) continue;
-        const double4_32a Q = d.spos[q];
-        const double rj = INIT ? d.r0[j] : Q.w;
-        if (!touching_rn(P.x, P.y, P.z, Q.x, Q.y, Q.z, ri, rj)) continue;
-        const int slot = atomicAdd(&s_new[g], 1);
-        if (slot < p.kstash) stash[slot] = j;
-    }
-    __syncwarp(gmask);
+    const int nxt = cur ^ 1;
     if (lane == 0) {
-        int nnew = s_new[g];
-        if (nnew > p.kstash) {
-            raise_error(d.ctr, kErrCapacity);
-            nnew = p.kstash;
+        s_new[g] = 0;
+        s_tot[g] = 0;
+    }
+    __syncwarp();
+    const bool act = k < p.n;
+    int i = 0, nkeep = 0, ended = 0;
+    if (act) {
+        const unsigned gmask = 0xffu << (lane_id() & ~7u);
+        i = (int)d.sorted[k];
+        const double4_32a P = d.spos[k];
+        const float4 P32 = d.spos32[k];
+        const int4 ci = d.cellinfo[i];
+        const int dx = (ci.w & 1) ? 1 : -1, dy = (ci.w & 2) ? 1 : -1, dz = (ci.w & 4) ? 1 : -1;
+        const int ox = (lane == 1 || lane == 4 || lane == 5 || lane == 7) ? dx : 0;
+        const int oy = (lane == 2 || lane == 4 || lane == 6 || lane == 7) ? dy : 0;
+        const int oz = (lane == 3 || lane == 5 || lane == 6 || lane == 7) ? dz : 0;
+        const uint32_t myB = bucket_of(ci.x + ox, ci.y + oy, ci.z + oz, p);
+        uint32_t B[8];
+        bool dup = false;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            B[u] = __shfl_sync(gmask, myB, u, kLanes);
+            dup |= (u < lane) && (B[u] == myB);
         }
-        for (int a2 = 1; a2 < nnew; ++a2) {  // new partners ascending
-            const int v = stash[a2];
-            int b2 = a2 - 1;
-            while (b2 >= 0 && stash[b2] > v) {
-                stash[b2 + 1] = stash[b2];
-                --b2;
+        uint32_t s, e;
+        bucket_range(d, myB, d.ctr->cell_limit, &s, &e);
+        if (dup) e = s;
+        const double ri = INIT ? d.r0[i] : P.w;
+
+        const ContactSoA o = d.c[cur];
+        const int e0 = d.row_start[cur][i];
+        const int e1 = e0 + d.row_len[cur][i];
+        const bool cached = e1 - e0 <= kRowCache;
+        for (int e2 = e0 + lane; e2 < e1; e2 += kLanes) {
+            const uint32_t fl = o.fl[e2];
+            const int j = o.cj[e2];
+            if (cached) s_row[g][e2 - e0] = (fl & kActive) ? j : -1;
+            int keep;
+            if (!(fl & kActive)) {
+                keep = 0;
+            } else if (INIT || (fl & kBonded)) {
+                keep = 1;
+            } else {
+                const bool valid =
+                    touching_rn(P.x, P.y, P.z, d.px[j], d.py[j], d.pz[j], P.w, d.r[j]);
+                const uint32_t bj = d.bucket[j];
+                bool in_cp = false;
+#pragma unroll
+                for (int t = 0; t < 8; ++t) in_cp |= (B[t] == bj);
+                keep = (valid || !in_cp) ? 1 : 0;
+                ended += 1 - keep;
             }
-            stash[b2 + 1] = v;
+            d.keep[e2] = (uint8_t)keep;
+            nkeep += keep;
         }
-        d.nnew[i] = nnew;
-        d.cnt[i] = nkeep + nnew;
-        if (ended) atomicAdd(&d.ctr->ended, (unsigned long long)ended);
-        if (!INIT && nnew) atomicAdd(&d.ctr->created, (unsigned long long)nnew);
+        nkeep = __reduce_add_sync(gmask, nkeep);
+        ended = __reduce_add_sync(gmask, ended);
+        __syncwarp(gmask);
+
+        int32_t* stash = d.stash + (size_t)i * p.kstash;
+        for (uint32_t q0 = s; q0 < e; q0 += kBatch) {
+            int jj[kBatch];
+            float4 qq[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                const uint32_t q = q0 + u;
+                jj[u] = q < e ? (int)d.sorted[q] : -1;
+                qq[u] = q < e ? d.spos32[q] : P32;
+            }
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                const int j = jj[u];
+                if (j <= i) continue;
+                if (!INIT && !maybe_touching32(P32, qq[u])) continue;
+                bool found = false;
+                if (cached) {
+                    for (int t = 0; t < e1 - e0 && !found; ++t) found = s_row[g][t] == j;
+                } else {
+                    for (int e2 = e0; e2 < e1 && !found; ++e2)
+                        found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
+                }
+                if (found) continue;
+                const double4_32a Q = d.spos[q0 + u];
+                const double rj = INIT ? d.r0[j] : Q.w;
+                if (!touching_rn(P.x, P.y, P.z, Q.x, Q.y, Q.z, ri, rj)) continue;
+                const int slot = atomicAdd(&s_new[g], 1);
+                if (slot < p.kstash) stash[slot] = j;
+            }
+        }
+        __syncwarp(gmask);
+        if (lane == 0) {
+            int nnew = s_new[g];
+            if (nnew > p.kstash) {
+                raise_error(d.ctr, kErrCapacity);
+                nnew = p.kstash;
+            }
+            for (int a2 = 1; a2 < nnew; ++a2) {  // new partners ascending
+                const int v = stash[a2];
+                int b2 = a2 - 1;
+                while (b2 >= 0 && stash[b2] > v) {
+                    stash[b2 + 1] = stash[b2];
+                    --b2;
+                }
+                stash[b2 + 1] = v;
+            }
+            d.nnew[i] = nnew;
+            s_new[g] = nnew;
+            s_tot[g] = nkeep + nnew;
+            if (ended) atomicAdd(&d.ctr->ended, (unsigned long long)ended);
+            if (!INIT && nnew) atomicAdd(&d.ctr->created, (unsigned long long)nnew);
+        }
+    }
+    // rows of this block allocated with one atomic (the atomic-compacted
+    // contact list of src/kernels.jl:74, 109): particle g gets base + Σ s_tot[<g]
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int v = s_tot[threadIdx.x];
+        int x = v;
+#pragma unroll
+        for (int o2 = 1; o2 < 32; o2 <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o2);
+            if (lane_id() >= (unsigned)o2) x += y;
+        }
+        s_tot[threadIdx.x] = x - v;  // exclusive
+        if (threadIdx.x == 31) s_base = (int)atomicAdd(&d.ctr->row_alloc[nxt], (unsigned)x);
+    }
+    __syncthreads();
+    if (act && lane == 0) {
+        const int len = nkeep + s_new[g];
+        int start = s_base + s_tot[g];
+        int rl = len;
+        if ((long long)start + len > (long long)p.cap) {
+            raise_error(d.ctr, kErrCapacity);
+            start = 0;
+            rl = 0;
+        }
+        d.row_start[nxt][i] = start;
+        d.row_len[nxt][i] = rl;
     }
 }
 
@@ -348,45 +409,46 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
 template <bool INIT>
 __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int cur) {
     const int nxt = cur ^ 1;
-    const int total = d.row_ptr[nxt][p.n];
-    if (total > p.cap) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(d.ctr, kErrCapacity);
-        return;
-    }
-    const int* rpo = d.row_ptr[cur];
-    const int* rpn = d.row_ptr[nxt];
-    const int cold = row_at(rpo, p.n, p.cap);
+    const int cold = min((int)d.ctr->row_alloc[cur], p.cap);
     const ContactSoA o = d.c[cur];
     const ContactSoA w = d.c[nxt];
     const int stride = gridDim.x * blockDim.x;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cold + p.n; t += stride) {
         if (t < cold) {
-            if (!d.keep[t]) continue;
+            const uint8_t kp = d.keep[t];
             const int i = o.ci[t], j = o.cj[t];
-            int pos = rpn[i];
-            for (int q = row_at(rpo, i, p.cap); q < t; ++q) pos += d.keep[q];
+            const uint32_t fl = o.fl[t];
+            double v[15];
+#pragma unroll
+            for (int f = 0; f < 15; ++f) v[f] = o.f[f][t];
+            if (!kp) continue;
+            const int rl = d.row_len[nxt][i];
+            if (rl == 0) continue;  // row dropped after a capacity overflow
+            int pos = d.row_start[nxt][i];
+            for (int q = d.row_start[cur][i]; q < t; ++q) pos += d.keep[q];
             const int nn = d.nnew[i];
             const int32_t* st = d.stash + (size_t)i * p.kstash;
             for (int u = 0; u < nn; ++u) pos += st[u] < j ? 1 : 0;
             w.ci[pos] = i;
             w.cj[pos] = j;
-            w.fl[pos] = o.fl[t];
+            w.fl[pos] = fl;
 #pragma unroll
-            for (int f = 0; f < 15; ++f) w.f[f][pos] = o.f[f][t];
+            for (int f = 0; f < 15; ++f) w.f[f][pos] = v[f];
             if (!INIT) {
                 const int slot = atomicAdd(&d.in_cnt[j], 1);
-                if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = pos;
+                if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = make_int2(pos, i);
                 else raise_error(d.ctr, kErrCapacity);
             }
         } else {
             const int i = t - cold;
             const int nn = d.nnew[i];
-            if (!nn) continue;
-            const int e0 = row_at(rpo, i, p.cap), e1 = row_at(rpo, i + 1, p.cap);
+            if (!nn || d.row_len[nxt][i] == 0) continue;
+            const int e0 = d.row_start[cur][i], e1 = e0 + d.row_len[cur][i];
             const int32_t* st = d.stash + (size_t)i * p.kstash;
+            const int base = d.row_start[nxt][i];
             for (int u = 0; u < nn; ++u) {
                 const int j = st[u];
-                int pos = rpn[i] + u;
+                int pos = base + u;
                 for (int q = e0; q < e1; ++q) pos += (d.keep[q] && o.cj[q] < j) ? 1 : 0;
                 w.ci[pos] = i;
                 w.cj[pos] = j;
@@ -395,7 +457,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int
                 for (int f = 0; f < 15; ++f) w.f[f][pos] = 0.0;
                 if (!INIT) {
                     const int slot = atomicAdd(&d.in_cnt[j], 1);
-                    if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = pos;
+                    if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = make_int2(pos, i);
                     else raise_error(d.ctr, kErrCapacity);
                 }
             }
@@ -404,45 +466,72 @@ __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int
 }
 
 // ---------------------------------------------------------------------------
-// Contact frame of src/kernels.jl:145-165: the rotation taking the unit normal
-// a = normalize(𝐤ⱼ - 𝐤ᵢ) to the local x axis.  For b = x̂ the reference's
-// I + [v]ₓ + [v]ₓ² (1-c)/s² reduces to the rows
-//   ( c, a₂, a₃ ), ( -a₂, 1 - a₂² f, -a₂a₃ f ), ( -a₃, -a₂a₃ f, 1 - a₃² f ),
-// f = (1 - c)/s².  The branch s < tolerance is decided on exactly the
-// reference's s and c (normalize and norm without contraction).  The matrix is
-// orthonormal, so its inverse (src/kernels.jl:224, 298) is its transpose.
+// Contact frame of src/kernels.jl:145-165: the rotation 𝐑 taking the unit
+// normal a = normalize(𝐤ⱼ - 𝐤ᵢ) to the local x axis.  For b = x̂ the
+// reference's I + [v]ₓ + [v]ₓ² (1-c)/s² has the rows
+//   ( a₁, a₂, a₃ ), ( -a₂, 1 - a₂² f, -a₂a₃ f ), ( -a₃, -a₂a₃ f, 1 - a₃² f ),
+// f = (1 - a₁)/s², s² = a₂² + a₃²; its degenerate branch (s < tolerance) is
+// diag(±1, 1, ±1).  Both are kept as (a₁, a₂, a₃, f, neg3):
+//   𝐑v  = ( a₁v₁ + w,  v₂ - a₂ t,  ±(v₃ - a₃ t) ),  w = a₂v₂ + a₃v₃, t = v₁ + f w
+//   𝐑ᵀv = ( a₁v₁ - w,  v₂ + a₂ u,  ±(v₃ + a₃ u) ),  u = v₁ - f w
+// (6 FP64 operations instead of 9).  𝐑 is orthonormal, so its inverse
+// (src/kernels.jl:224, 298) is its transpose.  The branch is decided on the
+// exact reference values of a and s when a is within 2·tolerance of ±x̂.
 struct Frame {
-    double r[3][3];
+    double a1, a2, a3, f;
+    bool neg3;
 };
-__device__ __forceinline__ Frame contact_frame(double ax, double ay, double az, double tol) {
-    Frame F;
+__device__ __forceinline__ Frame frame_exact(double ax, double ay, double az, double tol) {
     // v = a × x̂ = (±0, a₃, -a₂); s = norm(v) evaluated as sqrt((0 + a₃²) + a₂²)
     const double s = norm_rn(0.0, az, -ay);
-    const double c = ax;
+    Frame F;
     if (s < tol) {
-        const double sg = c > 0.0 ? 1.0 : -1.0;
-        F.r[0][0] = sg; F.r[0][1] = 0.0; F.r[0][2] = 0.0;
-        F.r[1][0] = 0.0; F.r[1][1] = 1.0; F.r[1][2] = 0.0;
-        F.r[2][0] = 0.0; F.r[2][1] = 0.0; F.r[2][2] = sg;
+        const double sg = ax > 0.0 ? 1.0 : -1.0;
+        F.a1 = sg;
+        F.a2 = 0.0;
+        F.a3 = 0.0;
+        F.f = 0.0;
+        F.neg3 = sg < 0.0;
     } else {
-        const double f = (1.0 - c) / (s * s);
-        F.r[0][0] = c; F.r[0][1] = ay; F.r[0][2] = az;
-        F.r[1][0] = -ay; F.r[1][1] = 1.0 - ay * ay * f; F.r[1][2] = -ay * az * f;
-        F.r[2][0] = -az; F.r[2][1] = -ay * az * f; F.r[2][2] = 1.0 - az * az * f;
+        F.a1 = ax;
+        F.a2 = ay;
+        F.a3 = az;
+        F.f = (1.0 - ax) / (s * s);
+        F.neg3 = false;
     }
     return F;
 }
-template <typename T>
-__device__ __forceinline__ Vec3<T> rot(const Frame& F, Vec3<T> v) {  // R v
-    return {(T)F.r[0][0] * v.x + (T)F.r[0][1] * v.y + (T)F.r[0][2] * v.z,
-            (T)F.r[1][0] * v.x + (T)F.r[1][1] * v.y + (T)F.r[1][2] * v.z,
-            (T)F.r[2][0] * v.x + (T)F.r[2][1] * v.y + (T)F.r[2][2] * v.z};
+__device__ __forceinline__ Frame contact_frame(double dx, double dy, double dz, double ax,
+                                               double ay, double az, double tol) {
+    const double s2 = ay * ay + az * az;
+    if (s2 < 4.0 * tol * tol) {
+        const double L = norm_rn(dx, dy, dz);
+        const double il = __ddiv_rn(1.0, L);
+        return frame_exact(__dmul_rn(il, dx), __dmul_rn(il, dy), __dmul_rn(il, dz), tol);
+    }
+    Frame F;
+    F.a1 = ax;
+    F.a2 = ay;
+    F.a3 = az;
+    F.f = (1.0 - ax) / s2;
+    F.neg3 = false;
+    return F;
 }
 template <typename T>
-__device__ __forceinline__ Vec3<T> rot_t(const Frame& F, Vec3<T> v) {  // Rᵀ v
-    return {(T)F.r[0][0] * v.x + (T)F.r[1][0] * v.y + (T)F.r[2][0] * v.z,
-            (T)F.r[0][1] * v.x + (T)F.r[1][1] * v.y + (T)F.r[2][1] * v.z,
-            (T)F.r[0][2] * v.x + (T)F.r[1][2] * v.y + (T)F.r[2][2] * v.z};
+__device__ __forceinline__ Vec3<T> rot(const Frame& R, Vec3<T> v) {  // 𝐑 v
+    const T a1 = (T)R.a1, a2 = (T)R.a2, a3 = (T)R.a3, f = (T)R.f;
+    const T w = a2 * v.y + a3 * v.z;
+    const T t = v.x + f * w;
+    const T z = v.z - a3 * t;
+    return {a1 * v.x + w, v.y - a2 * t, R.neg3 ? -z : z};
+}
+template <typename T>
+__device__ __forceinline__ Vec3<T> rot_t(const Frame& R, Vec3<T> v) {  // 𝐑ᵀ v
+    const T a1 = (T)R.a1, a2 = (T)R.a2, a3 = (T)R.a3, f = (T)R.f;
+    const T w = a2 * v.y + a3 * v.z;
+    const T u = v.x - f * w;
+    const T z = v.z + a3 * u;
+    return {a1 * v.x - w, v.y + a2 * u, R.neg3 ? -z : z};
 }
 
 __device__ __forceinline__ Vec3<double> ld3(const double* const* f, int base, int c) {
@@ -454,33 +543,8 @@ __device__ __forceinline__ void st3(double* const* f, int base, int c, Vec3<doub
     f[base + 2][c] = v.z;
 }
 template <typename T>
-__device__ __forceinline__ Vec3<double> to_d(Vec3<T> v) {
-    return {(double)v.x, (double)v.y, (double)v.z};
-}
-template <typename T>
 __device__ __forceinline__ Vec3<T> from_d(Vec3<double> v) {
     return {(T)v.x, (T)v.y, (T)v.z};
-}
-
-// The frame with the normal a already computed approximately (rsqrt).  Far
-// from the degenerate case (s = |a × x̂| >= 2·tolerance) both branches of the
-// reference are decided the same way and the general formula is used; near
-// it, a and s are recomputed exactly as the reference does (normalize and norm
-// without contraction) so the branch matches the reference bit for bit.
-__device__ __forceinline__ Frame contact_frame_fast(double dx, double dy, double dz, double ax,
-                                                    double ay, double az, double tol) {
-    const double s2 = ay * ay + az * az;
-    if (s2 < 4.0 * tol * tol) {
-        const double L = norm_rn(dx, dy, dz);
-        const double il = __ddiv_rn(1.0, L);
-        return contact_frame(__dmul_rn(il, dx), __dmul_rn(il, dy), __dmul_rn(il, dz), tol);
-    }
-    Frame F;
-    const double f = (1.0 - ax) / s2;
-    F.r[0][0] = ax; F.r[0][1] = ay; F.r[0][2] = az;
-    F.r[1][0] = -ay; F.r[1][1] = 1.0 - ay * ay * f; F.r[1][2] = -ay * az * f;
-    F.r[2][0] = -az; F.r[2][1] = -ay * az * f; F.r[2][2] = 1.0 - az * az * f;
-    return F;
 }
 
 // EBPM failure (src/kernels.jl:208-219):
@@ -494,15 +558,16 @@ __device__ __forceinline__ bool bond_breaks(const Vec3<double>& F, const Vec3<do
                                             const Vec3<double>& tj, double invA, double rbI,
                                             const DemParams& p) {
     const double ai = ti.y * ti.y + ti.z * ti.z, aj = tj.y * tj.y + tj.z * tj.z;
-    const double amax = jl_max(ai, aj), amin = jl_min(ai, aj);
+    const bool nan_a = isnan(ai) || isnan(aj);
+    const double amax = fmax(ai, aj), amin = fmin(ai, aj);
     const double fa = F.x * invA, k2 = rbI * rbI;
     const double Rc = p.b_sc - fa;     // σc >= σc₀  <=>  rbI·sqrt(amax) >= Rc
     const double Rt = -(p.b_st + fa);  // σt >= σt₀  <=>  rbI·sqrt(amin) <= Rt
     const double Rs = p.b_ss - fabs(ti.x) * (0.5 * rbI);  // σs >= σs₀ <=> 4/3·invA·sqrt(b) >= Rs
     const double b = F.y * F.y + F.z * F.z;
     const double ks = (4.0 / 3.0) * invA;
-    const bool comp = !isnan(amax) && (Rc <= 0.0 || amax * k2 >= Rc * Rc);
-    const bool tens = !isnan(amin) && Rt >= 0.0 && amin * k2 <= Rt * Rt;
+    const bool comp = !nan_a && (Rc <= 0.0 || amax * k2 >= Rc * Rc);
+    const bool tens = !nan_a && Rt >= 0.0 && amin * k2 <= Rt * Rt;
     const bool shear = !isnan(b) && !isnan(Rs) && (Rs <= 0.0 || b * (ks * ks) >= Rs * Rs);
     return comp || tens || shear;
 }
@@ -517,11 +582,10 @@ __device__ __forceinline__ bool bond_breaks(const Vec3<double>& F, const Vec3<do
 // EBPM in sum/difference form: with 𝚫 = 𝐝ᵢ - 𝐝ⱼ = 𝐑(𝐯ᵢ - 𝐯ⱼ)dt,
 // 𝛉ₛ = 𝐑(𝛚ᵢ + 𝛚ⱼ)dt and 𝛉_d = 𝐑(𝛚ᵢ - 𝛚ⱼ)dt, the reference's increments
 // k₅𝛉ᵢ + k₆𝛉ⱼ and k₆𝛉ᵢ + k₅𝛉ⱼ are k₊𝛉ₛ ± k₋𝛉_d with k₊ = (k₅+k₆)/2 =
-// 3EI/L/(1+ϕ) and k₋ = (k₅-k₆)/2 = EI/L.
+// 3EI/L/(1+ϕ) and k₋ = (k₅-k₆)/2 = EI/L; dt is folded into the stiffnesses.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int nxt) {
-    int C = d.row_ptr[nxt][p.n];
-    C = C < p.cap ? C : p.cap;
+    const int C = min((int)d.ctr->row_alloc[nxt], p.cap);
     const ContactSoA w = d.c[nxt];
     const int stride = gridDim.x * blockDim.x;
     const double dt = p.dt;
@@ -532,36 +596,32 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
         const int i = w.ci[c], j = w.cj[c];
         const Vec3<double> ki{d.px[i], d.py[i], d.pz[i]}, kj{d.px[j], d.py[j], d.pz[j]};
         const double ri = d.r[i], rj = d.r[j];
-        // normal and length; the frame's branch is decided on the exact
-        // reference values when the normal is within 2·tolerance of ±x̂
-        const double dx = kj.x - ki.x, dy = kj.y - ki.y, dz = kj.z - ki.z;
-        const double invL = rsqrt(dx * dx + dy * dy + dz * dz);
-        const double L = (dx * dx + dy * dy + dz * dz) * invL;
-        const double ax = dx * invL, ay = dy * invL, az = dz * invL;
-        const Frame R = contact_frame_fast(dx, dy, dz, ax, ay, az, p.tol);
         const Vec3<double> vi{d.vx[i], d.vy[i], d.vz[i]}, vj{d.vx[j], d.vy[j], d.vz[j]};
         const Vec3<double> wi{d.wx[i], d.wy[i], d.wz[i]}, wj{d.wx[j], d.wy[j], d.wz[j]};
+        const double dx = kj.x - ki.x, dy = kj.y - ki.y, dz = kj.z - ki.z;
+        const double L2 = dx * dx + dy * dy + dz * dz;
+        const double invL = rsqrt(L2);
+        const double L = L2 * invL;
+        const double ax = dx * invL, ay = dy * invL, az = dz * invL;
+        const Frame R = contact_frame(dx, dy, dz, ax, ay, az, p.tol);
         Vec3<T> fig, mi, mj;
         if (fl & kBonded) {
             // EBPM (src/kernels.jl:170-239)
-            const Vec3<double> Dd = rot<double>(R, {(vi.x - vj.x) * dt, (vi.y - vj.y) * dt, (vi.z - vj.z) * dt});
-            const Vec3<double> Ts = rot<double>(R, {(wi.x + wj.x) * dt, (wi.y + wj.y) * dt, (wi.z + wj.z) * dt});
-            const Vec3<double> Td = rot<double>(R, {(wi.x - wj.x) * dt, (wi.y - wj.y) * dt, (wi.z - wj.z) * dt});
+            const Vec3<double> Dd = rot<double>(R, {vi.x - vj.x, vi.y - vj.y, vi.z - vj.z});
+            const Vec3<double> Ts = rot<double>(R, {wi.x + wj.x, wi.y + wj.y, wi.z + wj.z});
+            const Vec3<double> Td = rot<double>(R, {wi.x - wj.x, wi.y - wj.y, wi.z - wj.z});
             const Vec3<T> D = from_d<T>(Dd), S = from_d<T>(Ts), Q = from_d<T>(Td);
-            const double rb = p.b_rho * jl_min(ri, rj);
-            const double rb2 = rb * rb;
-            const double Ib = rb2 * rb2 * (CUDART_PI / 4.0);
-            const double Ab = rb2 * CUDART_PI;
-            const T tinvL = (T)invL;
-            const T phi = (T)(20.0 / 3.0 * (1.0 + p.b_nu) * rb2) * tinvL * tinvL;
+            const int small = ri <= rj ? i : j;  // rb = ρ·min(rᵢ, rⱼ)
+            const T tinvL = (T)invL, tdt = (T)dt;
+            const T phi = (T)d.b_phic[small] * tinvL * tinvL;
             const T iphi = (T)1.0 / ((T)1.0 + phi);
-            const T EIL = (T)(p.b_E * Ib) * tinvL;  // EI/L
-            const T k1 = (T)(p.b_E * Ab) * tinvL;
-            const T k3 = (T)6.0 * EIL * tinvL * iphi;
+            const T EILdt = (T)d.b_EI[small] * tinvL * tdt;  // EI/L·dt
+            const T k1 = (T)d.b_EA[small] * tinvL * tdt;
+            const T k3 = (T)6.0 * EILdt * tinvL * iphi;
             const T k2 = (T)2.0 * k3 * tinvL;
-            const T k4 = EIL * (T)p.b_inv1pnu;
-            const T kp = (T)3.0 * EIL * iphi;
-            const T km = EIL;
+            const T k4 = EILdt * (T)p.b_inv1pnu;
+            const T kp = (T)3.0 * EILdt * iphi;
+            const T km = EILdt;
             const T dFx = k1 * D.x, dFy = k2 * D.y + k3 * S.z, dFz = k2 * D.z - k3 * S.y;
             const T ay_ = -k3 * D.z + kp * S.y, az_ = k3 * D.y + kp * S.z;
             const T dtix = k4 * Q.x, dtiy = ay_ + km * Q.y, dtiz = az_ + km * Q.z;
@@ -570,8 +630,7 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
             Fi = {Fi.x + (double)dFx, Fi.y + (double)dFy, Fi.z + (double)dFz};
             ti = {ti.x + (double)dtix, ti.y + (double)dtiy, ti.z + (double)dtiz};
             tj = {tj.x + (double)dtjx, tj.y + (double)dtjy, tj.z + (double)dtjz};
-            // breakage test, FP64 (src/kernels.jl:208-222), see bond_breaks()
-            const int small = ri <= rj ? i : j;  // rb = ρ·min(rᵢ, rⱼ)
+            // breakage test, FP64 (src/kernels.jl:208-222)
             if (bond_breaks(Fi, ti, tj, d.b_invA[small], d.b_rbI[small], p)) {
                 w.fl[c] = 0u;  // contact_active and contact_bonded bits cleared
                 ++nbroken;
@@ -579,12 +638,9 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
                 mi = fig;
                 mj = fig;
             } else {
-                const Vec3<double> fg = rot_t<double>(R, {-Fi.x, -Fi.y, -Fi.z});
-                const Vec3<double> mg_i = rot_t<double>(R, {-ti.x, -ti.y, -ti.z});
-                const Vec3<double> mg_j = rot_t<double>(R, {-tj.x, -tj.y, -tj.z});
-                fig = from_d<T>(fg);
-                mi = from_d<T>(mg_i);
-                mj = from_d<T>(mg_j);
+                fig = from_d<T>(rot_t<double>(R, {-Fi.x, -Fi.y, -Fi.z}));
+                mi = from_d<T>(rot_t<double>(R, {-ti.x, -ti.y, -ti.z}));
+                mj = from_d<T>(rot_t<double>(R, {-tj.x, -tj.y, -tj.z}));
                 st3(w.f, CK, c, {(ki.x + kj.x) * 0.5, (ki.y + kj.y) * 0.5, (ki.z + kj.z) * 0.5});
                 st3(w.f, CF, c, Fi);
                 st3(w.f, CTI, c, ti);
@@ -653,22 +709,92 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
     if (ngamma) atomicAdd(&d.ctr->warn_damp, ngamma);
 }
 
-// Per particle: contact force gather in a fixed order (own row by j, then
-// incoming contacts by contact index), `resolve_wall!` (src/kernels.jl:317-426),
+// ---------------------------------------------------------------------------
+// Per particle: contact force gather, `resolve_wall!` (src/kernels.jl:317-426),
 // `apply_body_force!` (src/kernels.jl:428-443) and `update!`
-// (src/kernels.jl:445-485).  For spheres 𝐈 = (2/5 m r²) I₃, so
-// inv(𝐑)·inv(𝐈)·(𝐑𝛕 - 𝐑𝛚 × 𝐈𝐑𝛚) is 𝛕 / I exactly in real arithmetic and the
-// quaternion only evolves as state.
+// (src/kernels.jl:445-485).  One thread per particle, so every FP64
+// instruction runs on full warps.  Contributions are added in a fixed order:
+// the particle's own row (ordered by j), then its incoming contacts ordered by
+// owner index i.  The order depends only on the contact set, not on where the
+// contacts sit in the buffers, so results are reproducible.
+// For spheres 𝐈 = (2/5 m r²) I₃, so inv(𝐑)·inv(𝐈)·(𝐑𝛕 - 𝐑𝛚 × 𝐈𝐑𝛚) is 𝛕/I
+// exactly in real arithmetic; the quaternion only evolves as state.
 constexpr int kMaxIncoming = 64;
-constexpr int kRegIncoming = 16;
-__global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, int nxt) {
+
+// ascending .y, an odd-even transposition network on N register slots
+template <int N>
+__device__ __forceinline__ void sort_by_owner(int2 (&v)[N]) {
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+#pragma unroll
+        for (int u = r & 1; u + 1 < N; u += 2) {
+            const bool sw = v[u].y > v[u + 1].y;
+            const int2 a = v[u], b = v[u + 1];
+            v[u] = sw ? b : a;
+            v[u + 1] = sw ? a : b;
+        }
+    }
+}
+template <int N>
+__device__ __forceinline__ void add_incoming(const DemDev& d, size_t cap, const int2* il, int nin,
+                                             double* F, double* M) {
+    int2 v[N];
+#pragma unroll
+    for (int u = 0; u < N; ++u) v[u] = u < nin ? il[u] : make_int2(0, 0x7fffffff);
+    sort_by_owner<N>(v);
+    double g[N][6];
+#pragma unroll
+    for (int u = 0; u < N; ++u) {
+        if (u < nin) {
+            const int c = v[u].x;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                g[u][q] = d.contrib[q * cap + c];
+                g[u][3 + q] = d.contrib[(6 + q) * cap + c];
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < N; ++u) {
+        if (u < nin) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                F[q] += -g[u][q];
+                M[q] += g[u][3 + q];
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nxt = cur ^ 1;
+    if (i == 0) d.ctr->row_alloc[cur] = 0u;  // the free buffer is next step's target
     if (i >= p.n) return;
     const size_t cap = (size_t)p.cap;
-    const int* rp = d.row_ptr[nxt];
     double F[3] = {0.0, 0.0, 0.0}, M[3] = {0.0, 0.0, 0.0};
-    const int c0 = row_at(rp, i, p.cap), c1 = row_at(rp, i + 1, p.cap);
-    for (int c = c0; c < c1; ++c) {
+    const int c0 = d.row_start[nxt][i];
+    const int c1 = min(c0 + d.row_len[nxt][i], p.cap);
+    int c = c0;
+    for (; c + 1 < c1; c += 2) {
+        double a[6], b[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            a[q] = d.contrib[q * cap + c];
+            b[q] = d.contrib[q * cap + c + 1];
+        }
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            F[q] += a[q];
+            M[q] += a[3 + q];
+        }
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            F[q] += b[q];
+            M[q] += b[3 + q];
+        }
+    }
+    if (c < c1) {
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             F[q] += d.contrib[q * cap + c];
@@ -676,55 +802,34 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
         }
     }
     int nin = d.in_cnt[i];
-    d.in_cnt[i] = 0;
     nin = nin < p.kin ? nin : p.kin;
     nin = nin < kMaxIncoming ? nin : kMaxIncoming;
-    const int* il = d.in_list + (size_t)i * p.kin;
-    if (nin <= kRegIncoming) {
-        // ascending contact index, sorted in registers (odd-even transposition)
-        int v[kRegIncoming];
-#pragma unroll
-        for (int t = 0; t < kRegIncoming; ++t) v[t] = t < nin ? il[t] : 0x7fffffff;
-#pragma unroll
-        for (int r = 0; r < kRegIncoming; ++r) {
-#pragma unroll
-            for (int t = r & 1; t + 1 < kRegIncoming; t += 2) {
-                const int lo = min(v[t], v[t + 1]), hi = max(v[t], v[t + 1]);
-                v[t] = lo;
-                v[t + 1] = hi;
-            }
-        }
-#pragma unroll
-        for (int t = 0; t < kRegIncoming; ++t) {
-            if (t < nin) {
-                const int c = v[t];
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    F[q] += -d.contrib[q * cap + c];
-                    M[q] += d.contrib[(6 + q) * cap + c];
-                }
-            }
-        }
+    const int2* il = d.in_list + (size_t)i * p.kin;
+    if (nin <= 4) {
+        add_incoming<4>(d, cap, il, nin, F, M);
+    } else if (nin <= 8) {
+        add_incoming<8>(d, cap, il, nin, F, M);
     } else {
-        int inc[kMaxIncoming];
-        for (int t = 0; t < nin; ++t) {
-            const int v = il[t];
-            int b = t - 1;
-            while (b >= 0 && inc[b] > v) {
+        int2 inc[kMaxIncoming];
+        for (int u = 0; u < nin; ++u) {
+            const int2 v = il[u];
+            int b = u - 1;
+            while (b >= 0 && inc[b].y > v.y) {
                 inc[b + 1] = inc[b];
                 --b;
             }
             inc[b + 1] = v;
         }
-        for (int t = 0; t < nin; ++t) {
-            const int c = inc[t];
+        for (int u = 0; u < nin; ++u) {
+            const int cc = inc[u].x;
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
-                F[q] += -d.contrib[q * cap + c];
-                M[q] += d.contrib[(6 + q) * cap + c];
+                F[q] += -d.contrib[q * cap + cc];
+                M[q] += d.contrib[(6 + q) * cap + cc];
             }
         }
     }
+    d.in_cnt[i] = 0;
     const double x = d.px[i], y = d.py[i], z = d.pz[i];
     const double vx = d.vx[i], vy = d.vy[i], vz = d.vz[i];
     const double wx = d.wx[i], wy = d.wy[i], wz = d.wz[i];
@@ -889,22 +994,24 @@ inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
 
 int scan_tiles(int64_t n) { return (int)((n + kScanTile - 1) / kScanTile); }
 
-void launch_scan_i32(const int32_t* in, int32_t* out, int64_t n, const DemDev& d, cudaStream_t s) {
+void launch_scan_i32(const int32_t* in, int32_t* out, int64_t n, const DemDev& d, int site,
+                     cudaStream_t s) {
     const int nt = scan_tiles(n);
     if (nt == 0) {
         cudaMemsetAsync(out, 0, sizeof(int32_t), s);
         return;
     }
-    k_scan_excl<int32_t, false><<<nt, kScanBlock, 0, s>>>(in, out, n, nt, d.scan_state, d.ctr);
+    k_scan_excl<int32_t, false><<<nt, kScanBlock, 0, s>>>(in, out, n, nt, d.scan_state[site],
+                                                          &d.ctr->tickets[site], d.ctr);
 }
 
 void launch_broadphase(const DemDev& d, const DemParams& p, int ntiles_cells, cudaStream_t s) {
     if (p.n == 0) return;
     const int nb = blocks_for(p.n, kThreads);
     k_hash<<<nb, kThreads, 0, s>>>(d, p);
-    k_scan_excl<uint32_t, true><<<ntiles_cells, kScanBlock, 0, s>>>(d.cell_count, d.cell_start,
-                                                               (long long)p.H, ntiles_cells,
-                                                               d.scan_state, d.ctr);
+    k_scan_excl<uint32_t, true><<<ntiles_cells, kScanBlock, 0, s>>>(
+        d.cell_count, d.cell_start, (long long)p.H, ntiles_cells, d.scan_state[kScanCells],
+        &d.ctr->tickets[kScanCells], d.ctr);
     k_scatter<<<nb, kThreads, 0, s>>>(d, p);
     k_canon<<<nb, kThreads, 0, s>>>(d, p);
 }
@@ -914,10 +1021,6 @@ void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, cuda
     const int nb = blocks_for((long long)p.n * kLanes, kThreads);
     if (init) k_detect<true><<<nb, kThreads, 0, s>>>(d, p, cur);
     else k_detect<false><<<nb, kThreads, 0, s>>>(d, p, cur);
-}
-
-void launch_scan_rows(const DemDev& d, const DemParams& p, int nxt, cudaStream_t s) {
-    launch_scan_i32(d.cnt, d.row_ptr[nxt], p.n, d, s);
 }
 
 void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, int grid,
@@ -934,9 +1037,9 @@ void launch_force(const DemDev& d, const DemParams& p, int nxt, int grid, cudaSt
     else k_force<double><<<grid, kThreads, 0, s>>>(d, p, nxt);
 }
 
-void launch_integrate(const DemDev& d, const DemParams& p, int nxt, cudaStream_t s) {
+void launch_integrate(const DemDev& d, const DemParams& p, int cur, cudaStream_t s) {
     if (p.n == 0) return;
-    k_integrate<<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, nxt);
+    k_integrate<<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, cur);
 }
 
 void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cudaStream_t s) {

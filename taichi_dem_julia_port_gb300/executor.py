@@ -99,12 +99,12 @@ class GlobalData:
               "dem_step_timed")
         return float(ms.value)
 
-    PHASES = ("broadphase", "detect", "scan_rows", "compact", "force", "integrate")
+    PHASES = ("broadphase", "detect", "compact", "force", "integrate")
 
     def simulate_profiled(self) -> dict:
         """One step launched phase by phase; device milliseconds per phase."""
-        ms = (C.c_float * 6)()
-        check(self.lib, self.lib.dem_step_profiled(self.h, ms, 6), "dem_step_profiled")
+        ms = (C.c_float * 5)()
+        check(self.lib, self.lib.dem_step_profiled(self.h, ms, 5), "dem_step_profiled")
         return dict(zip(self.PHASES, [float(x) for x in ms]))
 
     def sync(self) -> None:
