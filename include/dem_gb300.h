@@ -235,6 +235,67 @@ int dem_set_contacts(DemHandle* h, const DemContacts* in, int64_t n);
 
 int dem_get_stats(DemHandle* h, DemStats* out);
 
+/* ---- arenas: many independent scenes stepped together ------------------- */
+/*
+ * No counterpart in the reference, which steps one scene per process.  An
+ * arena is a handle whose particle slots, contact buffers and bucket table are
+ * shared by independent scenes; every dem_step advances all scenes in Step
+ * mode by one `simulate!` each, in the same kernels.  Scenes can be added and
+ * removed between steps (the device step graph never changes), which is what
+ * the batched and served modes build on.  Each scene's results are the same,
+ * bit for bit, as when it is stepped alone in its own arena.
+ */
+typedef struct DemArenaConfig {
+    int64_t max_particles;   /* particle slots shared by all scenes          */
+    int64_t max_contacts;    /* contact capacity shared by all scenes        */
+    int64_t max_buckets;     /* bucket-table entries shared by all scenes    */
+    int32_t max_scenes;
+    int32_t max_coordinate_number; /* new partners / incoming contacts per
+                                      particle and step (at most 64)         */
+    int32_t precision;       /* DEM_FP64 or DEM_FP32_FORCE                   */
+    int32_t pad;
+    double cell_factor;      /* search cell = cell_factor · 4 rₘₐₓ; 0 = 1.  Values
+                                down to the minimum that still finds every
+                                touching pair (cell >= 4·max r) are accepted. */
+} DemArenaConfig;
+
+#define DEM_SCENE_FREE 0
+#define DEM_SCENE_FROZEN 1 /* state kept, not stepped (e.g. step target reached) */
+#define DEM_SCENE_STEP 2
+#define DEM_SCENE_INIT 3   /* bonds are created on the next dem_step         */
+
+typedef struct DemSceneInfo {
+    int32_t mode;            /* DEM_SCENE_*                                   */
+    int32_t pad;
+    int64_t n;               /* particles                                     */
+    int64_t first_slot;      /* particle slot of the scene's particle 0      */
+    int64_t steps_done;
+    int64_t steps_target;    /* the scene freezes when steps_done reaches it (0 = never) */
+    int64_t buckets;         /* bucket-table entries of the scene            */
+} DemSceneInfo;
+
+int dem_arena_create(const DemArenaConfig* cfg, DemHandle** out);
+
+/* Adds a scene (the set-up of `solve`, src/executor.jl:217-315) to free slots.
+ * init_bonds != 0 runs `initialize!` (src/kernels.jl:60-85) on the next
+ * dem_step before the scene starts stepping; steps_target > 0 freezes the
+ * scene after that many steps.  Returns DEM_ERR_CAPACITY when the arena has no
+ * room (particles, buckets or scene records). */
+int dem_arena_add(DemHandle* h, const DemConfigC* cfg, const DemParticlesIn* particles,
+                  int init_bonds, int64_t steps_target, int32_t* scene);
+
+/* Releases a scene's slots and contacts. */
+int dem_arena_remove(DemHandle* h, int32_t scene);
+
+int dem_arena_scene_info(DemHandle* h, int32_t scene, DemSceneInfo* out);
+
+/* Per-scene state exchange; indices are scene-local (0-based). */
+int dem_scene_get_particles(DemHandle* h, int32_t scene, DemParticleState* out);
+int dem_scene_get_contacts(DemHandle* h, int32_t scene, DemContacts* out, int64_t cap,
+                           int64_t* n_out);
+int dem_scene_get_stats(DemHandle* h, int32_t scene, DemStats* out);
+int dem_scene_get_derived(DemHandle* h, int32_t scene, DemDerived* out);
+
 /* ---- parity / inspection ----------------------------------------------- */
 
 /* Runs only the reference broad phase on the current positions and returns

@@ -105,6 +105,28 @@ class DemStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+DEM_SCENE_FREE = 0
+DEM_SCENE_FROZEN = 1
+DEM_SCENE_STEP = 2
+DEM_SCENE_INIT = 3
+
+
+class DemArenaConfig(C.Structure):
+    _fields_ = [("max_particles", C.c_int64), ("max_contacts", C.c_int64),
+                ("max_buckets", C.c_int64), ("max_scenes", C.c_int32),
+                ("max_coordinate_number", C.c_int32), ("precision", C.c_int32),
+                ("pad", C.c_int32), ("cell_factor", C.c_double)]
+
+
+class DemSceneInfo(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("pad", C.c_int32), ("n", C.c_int64),
+                ("first_slot", C.c_int64), ("steps_done", C.c_int64),
+                ("steps_target", C.c_int64), ("buckets", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
 _H = C.c_void_p
 _PH = C.POINTER(C.c_void_p)
 
@@ -128,6 +150,16 @@ ENTRY_POINTS = {
     "dem_get_stats": (C.c_int, [_H, C.POINTER(DemStats)]),
     "dem_debug_broadphase": (C.c_int, [_H, _PI32, _PU32, _PU32, _PU32, _PU32, _PI32, C.c_int64,
                                        C.POINTER(C.c_int64)]),
+    "dem_arena_create": (C.c_int, [C.POINTER(DemArenaConfig), _PH]),
+    "dem_arena_add": (C.c_int, [_H, C.POINTER(DemConfigC), C.POINTER(DemParticlesIn), C.c_int,
+                                C.c_int64, C.POINTER(C.c_int32)]),
+    "dem_arena_remove": (C.c_int, [_H, C.c_int32]),
+    "dem_arena_scene_info": (C.c_int, [_H, C.c_int32, C.POINTER(DemSceneInfo)]),
+    "dem_scene_get_particles": (C.c_int, [_H, C.c_int32, C.POINTER(DemParticleState)]),
+    "dem_scene_get_contacts": (C.c_int, [_H, C.c_int32, C.POINTER(DemContacts), C.c_int64,
+                                         C.POINTER(C.c_int64)]),
+    "dem_scene_get_stats": (C.c_int, [_H, C.c_int32, C.POINTER(DemStats)]),
+    "dem_scene_get_derived": (C.c_int, [_H, C.c_int32, C.POINTER(DemDerived)]),
     "dem_bucket_sort_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                           C.POINTER(C.c_double), C.c_double, C.c_int64,
                                           C.c_void_p, C.c_void_p, C.c_void_p]),

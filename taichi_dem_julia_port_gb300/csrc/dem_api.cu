@@ -2,11 +2,12 @@
 //
 // Host responsibilities: the per-scene setup that `solve` performs before its
 // loop (src/executor.jl:217-315), device buffers, the CUDA-graph step
-// (`simulate!`, src/executor.jl:162-172) and host<->device state exchange.
+// (`simulate!`, src/executor.jl:162-172), host<->device state exchange, and the
+// arena of independent scenes (slot and bucket-range allocation, scene modes).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <algorithm>
 #include <numeric>
 #include <vector>
 
@@ -99,16 +100,198 @@ Hertz hertz_constants(double Ei, double nui, double Ej, double nuj, double e) {
 
 thread_local char g_msg[512];
 
+// First-fit allocator of [start, start + len) ranges inside [0, cap).
+struct FreeList {
+    std::vector<std::pair<int64_t, int64_t>> free;  // (start, len), sorted by start
+    void init(int64_t cap) {
+        free.clear();
+        if (cap > 0) free.push_back({0, cap});
+    }
+    bool take(int64_t len, int64_t* start) {
+        if (len == 0) {
+            *start = 0;
+            return true;
+        }
+        for (size_t k = 0; k < free.size(); ++k) {
+            if (free[k].second >= len) {
+                *start = free[k].first;
+                free[k].first += len;
+                free[k].second -= len;
+                if (free[k].second == 0) free.erase(free.begin() + (long)k);
+                return true;
+            }
+        }
+        return false;
+    }
+    void give(int64_t start, int64_t len) {
+        if (len == 0) return;
+        auto it = std::lower_bound(free.begin(), free.end(), std::make_pair(start, (int64_t)0));
+        it = free.insert(it, {start, len});
+        size_t k = (size_t)(it - free.begin());
+        if (k + 1 < free.size() && free[k].first + free[k].second == free[k + 1].first) {
+            free[k].second += free[k + 1].second;
+            free.erase(free.begin() + (long)k + 1);
+        }
+        if (k > 0 && free[k - 1].first + free[k - 1].second == free[k].first) {
+            free[k - 1].second += free[k].second;
+            free.erase(free.begin() + (long)k);
+        }
+    }
+};
+
+struct SceneHost {
+    int mode = kModeFree;
+    DemConfigC cfg{};
+    DemDerived der{};
+    SceneParams sp{};
+    int64_t steps = 0, target = 0;
+};
+
+// Per-particle arrays of one scene, derived on the host.
+struct SceneArrays {
+    std::vector<double> pos[3], vel[3];
+    std::vector<double> m, inv_m, r, r0, inv_inertia, b_invA, b_rbI, b_EA, b_EI, b_phic;
+};
+
+uint32_t pow2_mask(uint32_t H) { return (H & (H - 1)) == 0 ? H - 1 : 0u; }
+
+// The grain set-up and derived values of `solve` (src/executor.jl:217-315).
+int prepare_scene(const DemConfigC* cfg, const DemParticlesIn* pin, double cell_factor,
+                  SceneHost& S, SceneArrays& A) {
+    if (!cfg || !pin || pin->n < 0 || pin->n > 0x3fffffff) return DEM_ERR_INVALID;
+    if (pin->n > 0 && (!pin->volume || !pin->mass || !pin->pos || !pin->vel)) return DEM_ERR_INVALID;
+    if (!(cfg->dt > 0) || cfg->max_coordinate_number <= 0) return DEM_ERR_INVALID;
+    const int n = (int)pin->n;
+    S.cfg = *cfg;
+    for (auto* v : {&A.m, &A.inv_m, &A.r, &A.r0, &A.inv_inertia, &A.b_invA, &A.b_rbI, &A.b_EA,
+                    &A.b_EI, &A.b_phic})
+        v->resize(n);
+    for (int c = 0; c < 3; ++c) {
+        A.pos[c].resize(n);
+        A.vel[c].resize(n);
+    }
+    double rmax_r = -INFINITY;
+    for (int i = 0; i < n; ++i) {
+        const double V = pin->volume[i], m = pin->mass[i];
+        A.m[i] = m;
+        A.r[i] = std::cbrt(V / (4.0 / 3.0 * kPi));
+        A.r0[i] = A.r[i] * cfg->particle_contact_radius_multiplier;
+        A.inv_inertia[i] = 1.0 / (2.0 / 5.0 * m * (A.r[i] * A.r[i]));
+        A.inv_m[i] = 1.0 / m;
+        // bond section of src/kernels.jl:178-184 for rb = ρ·rᵢ
+        const double rb = cfg->bond_radius_ratio * A.r[i];
+        const double Ab = rb * rb * kPi, Ib = rb * rb * (rb * rb) * (kPi / 4.0);
+        A.b_invA[i] = 1.0 / Ab;
+        A.b_rbI[i] = rb / Ib;
+        A.b_EA[i] = cfg->bond_elastic_modulus * Ab;
+        A.b_EI[i] = cfg->bond_elastic_modulus * Ib;
+        A.b_phic[i] = 20.0 / 3.0 * (1.0 + cfg->bond_poisson_ratio) * (rb * rb);
+        rmax_r = std::max(rmax_r, A.r[i]);
+        for (int c = 0; c < 3; ++c) {
+            A.pos[c][i] = pin->pos[3 * i + c];
+            A.vel[c][i] = pin->vel[3 * i + c];
+        }
+    }
+    // derived sizes (src/executor.jl:244-267)
+    DemDerived& D = S.der;
+    D.material_density = n ? pin->mass[n - 1] / pin->volume[n - 1] : 0.0;
+    D.r_max = rmax_r * cfg->particle_contact_radius_multiplier *
+              (1.0 + cfg->bond_tensile_strength / cfg->bond_elastic_modulus) *
+              cfg->neighboring_search_safety_factor;
+    D.cell_size = 4.0 * D.r_max;
+    int64_t prod = 1;
+    for (int c = 0; c < 3; ++c)
+        prod *= (int64_t)std::ceil((cfg->domain_max[c] - cfg->domain_min[c]) / D.cell_size);
+    D.hash_table_size = std::min<int64_t>(std::max<int64_t>(prod, 1 << 20), 1 << 22);
+    D.total_steps = (int64_t)std::trunc(cfg->target_time / cfg->dt);
+    D.save_per_steps = (int64_t)std::trunc(cfg->saving_interval_time / cfg->dt);
+    D.contact_capacity = (int64_t)n * cfg->max_coordinate_number;
+    if (n > 0 && !(D.cell_size > 0 && std::isfinite(D.cell_size))) return DEM_ERR_INVALID;
+    // device constants (materials / surfaces / wall of src/executor.jl:282-315)
+    SceneParams& p = S.sp;
+    std::memset(&p, 0, sizeof(p));
+    p.n = n;
+    p.Href = (uint32_t)D.hash_table_size;
+    p.Href_mask = pow2_mask(p.Href);
+    p.has_wall = 1;
+    for (int c = 0; c < 3; ++c) {
+        p.dmin[c] = cfg->domain_min[c];
+        p.grav[c] = cfg->gravity[c];
+        p.wn[c] = cfg->wall_normal[c];
+    }
+    p.cell_ref = D.cell_size;
+    p.inv_cell_ref = 1.0 / D.cell_size;
+    // Search cells.  A smaller cell still finds every touching pair with the
+    // octant search as long as cell >= 2(rᵢ + rⱼ) for the radii in use, i.e.
+    // 4·max r (stepping) and 4·max r₀ (bond initialisation).
+    const double f = cell_factor > 0 ? cell_factor : 1.0;
+    const double floor_cell =
+        4.0 * rmax_r * std::max(1.0, cfg->particle_contact_radius_multiplier) * (1.0 + 1e-9);
+    p.cell = n ? std::min(D.cell_size, std::max(f * D.cell_size, floor_cell)) : D.cell_size;
+    p.inv_cell = 1.0 / p.cell;
+    p.same_grid = p.cell == p.cell_ref ? 1 : 0;
+    p.dt = cfg->dt;
+    p.tol = cfg->tolerance;
+    p.damping = cfg->global_damping;
+    const Hertz pp = hertz_constants(cfg->particle_elastic_modulus, cfg->particle_poisson_ratio,
+                                     cfg->particle_elastic_modulus, cfg->particle_poisson_ratio,
+                                     cfg->pp_coefficient_restitution);
+    p.pp_mu = cfg->pp_coefficient_friction;
+    p.pp_Ys = pp.Ys;
+    p.pp_Gs = pp.Gs;
+    p.pp_cgn = pp.cgn;
+    p.pp_cgt = pp.cgt;
+    p.b_inv1pnu = 1.0 / (1.0 + cfg->bond_poisson_ratio);
+    p.b_sc = cfg->bond_compressive_strength;
+    p.b_st = cfg->bond_tensile_strength;
+    p.b_ss = cfg->bond_shear_strength;
+    p.wd = cfg->wall_distance;
+    const M3 WR = wall_frame(cfg->wall_normal, cfg->tolerance);
+    const M3 WRi = inverse3(WR);
+    for (int r_ = 0; r_ < 3; ++r_)
+        for (int c = 0; c < 3; ++c) {
+            p.wR[3 * r_ + c] = WR.a[r_][c];
+            p.wRinv[3 * r_ + c] = WRi.a[r_][c];
+        }
+    const Hertz pw = hertz_constants(cfg->particle_elastic_modulus, cfg->particle_poisson_ratio,
+                                     cfg->wall_elastic_modulus, cfg->wall_poisson_ratio,
+                                     cfg->pw_coefficient_restitution);
+    p.pw_mu = cfg->pw_coefficient_friction;
+    p.pw_Ys = pw.Ys;
+    p.pw_Gs = pw.Gs;
+    p.pw_cgn = pw.cgn;
+    p.pw_cgt = pw.cgt;
+    return DEM_OK;
+}
+
+// Mode changes of up to 64 scenes, applied on the device in stream order.
+struct ModeUpdates {
+    int count;
+    int idx[64];
+    int mode[64];
+};
+__global__ void k_set_modes(SceneParams* sp, ModeUpdates u) {
+    const int t = threadIdx.x;
+    if (t < u.count) sp[u.idx[t]].mode = u.mode[t];
+}
+__global__ void k_fill_i32(int32_t* a, int64_t n, int32_t v) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
 }  // namespace
 
 struct DemHandle {
-    DemConfigC cfg{};
-    DemDerived der{};
+    bool multi = false;
+    int device = 0;
+    int sm_count = 0;
+    int n_cap = 0, c_cap = 0, s_cap = 0;
+    uint32_t t_cap = 0;
+    double cell_factor = 1.0;
     DemParams p{};
     DemDev d{};
-    int device = 0;
-    int n = 0;
-    int sm_count = 0;
+    std::vector<SceneHost> scenes;
+    FreeList pfree, tfree;
     int cur = 0;  // contact buffer holding the current state
     int64_t steps = 0;
     int ntiles_cells = 0;
@@ -119,15 +302,22 @@ struct DemHandle {
     std::vector<void*> allocs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double* pinned = nullptr;  // host staging for particle state exchange
+    int64_t pinned_n = 0;
 };
 
-#define CU(expr)                                                                   \
-    do {                                                                           \
-        cudaError_t _e = (expr);                                                   \
-        if (_e != cudaSuccess) {                                                   \
-            std::snprintf(g_msg, sizeof(g_msg), "%s: %s", #expr, cudaGetErrorString(_e)); \
-            return DEM_ERR_CUDA;                                                   \
-        }                                                                          \
+#define CU(expr)                                                                            \
+    do {                                                                                    \
+        cudaError_t _e = (expr);                                                            \
+        if (_e != cudaSuccess) {                                                            \
+            std::snprintf(g_msg, sizeof(g_msg), "%s: %s", #expr, cudaGetErrorString(_e));   \
+            return DEM_ERR_CUDA;                                                            \
+        }                                                                                   \
+    } while (0)
+
+#define TRY(expr)                      \
+    do {                               \
+        int _rc = (expr);              \
+        if (_rc != DEM_OK) return _rc; \
     } while (0)
 
 namespace {
@@ -137,30 +327,40 @@ int dalloc(DemHandle* h, T** ptr, size_t count) {
     void* p = nullptr;
     size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
     CU(cudaMalloc(&p, bytes));
-    CU(cudaMemsetAsync(p, 0, bytes, h->stream));
     h->allocs.push_back(p);
+    CU(cudaMemsetAsync(p, 0, bytes, h->stream));
     *ptr = static_cast<T*>(p);
     return DEM_OK;
 }
 
-#define TRY(expr)                      \
-    do {                               \
-        int _rc = (expr);              \
-        if (_rc != DEM_OK) return _rc; \
-    } while (0)
+int check_device(int* dev, int* sms) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DEM_ERR_NO_DEVICE;
+    CU(cudaGetDevice(dev));
+    cudaDeviceProp prop;
+    CU(cudaGetDeviceProperties(&prop, *dev));
+    if (prop.major != 10 || prop.minor != 3) {
+        std::snprintf(g_msg, sizeof(g_msg), "device %d is sm_%d%d; this library is built for sm_103a",
+                      *dev, prop.major, prop.minor);
+        return DEM_ERR_NO_DEVICE;
+    }
+    *sms = prop.multiProcessorCount;
+    return DEM_OK;
+}
 
+// Device buffers for n_cap particle slots, c_cap contacts, t_cap buckets.
 int allocate(DemHandle* h) {
-    const size_t n = (size_t)h->n, cap = (size_t)h->p.cap, H = h->p.H;
+    const size_t n = (size_t)h->n_cap, cap = (size_t)h->c_cap, T = h->t_cap;
     DemDev& d = h->d;
     double** dbl[] = {&d.px, &d.py, &d.pz, &d.vx, &d.vy, &d.vz, &d.wx, &d.wy, &d.wz,
-                      &d.qw, &d.qx, &d.qy, &d.qz, &d.m, &d.inv_m, &d.r, &d.r0, &d.inv_inertia, &d.b_invA, &d.b_rbI,
-                      &d.b_EA, &d.b_EI, &d.b_phic,
+                      &d.qw, &d.qx, &d.qy, &d.qz, &d.m, &d.inv_m, &d.r, &d.r0, &d.inv_inertia,
+                      &d.b_invA, &d.b_rbI, &d.b_EA, &d.b_EI, &d.b_phic,
                       &d.fx, &d.fy, &d.fz, &d.tx, &d.ty, &d.tz, &d.wsx, &d.wsy, &d.wsz};
     for (double** a : dbl) TRY(dalloc(h, a, n));
     TRY(dalloc(h, &d.cellinfo, n));
     TRY(dalloc(h, &d.bucket, n));
-    TRY(dalloc(h, &d.cell_count, H));
-    TRY(dalloc(h, &d.cell_start, H + 1));
+    TRY(dalloc(h, &d.cell_count, T));
+    TRY(dalloc(h, &d.cell_start, T + 1));
     TRY(dalloc(h, &d.unsorted, n));
     TRY(dalloc(h, &d.sorted, n));
     TRY(dalloc(h, &d.spos, n));
@@ -179,9 +379,16 @@ int allocate(DemHandle* h) {
     TRY(dalloc(h, &d.in_cnt, n));
     TRY(dalloc(h, &d.in_list, n * (size_t)h->p.kin));
     TRY(dalloc(h, &d.contrib, 9 * cap));
-    TRY(dalloc(h, &d.scan_state[kScanCells], (size_t)scan_tiles((int64_t)H)));
+    TRY(dalloc(h, &d.scan_state[kScanCells], (size_t)scan_tiles((int64_t)T)));
     TRY(dalloc(h, &d.scan_state[kScanDebug], (size_t)scan_tiles((int64_t)n)));
     TRY(dalloc(h, &d.ctr, 1));
+    TRY(dalloc(h, &d.sctr, (size_t)std::max(h->s_cap, 1)));
+    if (h->multi) {
+        TRY(dalloc(h, &d.scene_of, n));
+        TRY(dalloc(h, &d.sp, (size_t)h->s_cap));
+        TRY(dalloc(h, &d.refcell, n));
+        CU(cudaMemsetAsync(d.scene_of, 0xff, sizeof(int32_t) * std::max<size_t>(n, 1), h->stream));
+    }
     return DEM_OK;
 }
 
@@ -197,13 +404,62 @@ void free_all(DemHandle* h) {
     h->pinned = nullptr;
 }
 
+int init_handle(DemHandle* h) {
+    CU(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CU(cudaEventCreate(&h->ev0));
+    CU(cudaEventCreate(&h->ev1));
+    TRY(allocate(h));
+    h->ntiles_cells = std::max(1, scan_tiles((int64_t)h->t_cap));
+    h->force_grid = (int)std::max<int64_t>(
+        1, std::min<int64_t>(((int64_t)h->c_cap + 255) / 256, (int64_t)h->sm_count * 16));
+    return DEM_OK;
+}
+
+// Uploads a scene's particle arrays into slots [p0, p0 + n) and resets their
+// dynamic state (ω = 0, q = 1, wall shear = 0, last forces = 0).
+int upload_scene(DemHandle* h, const SceneArrays& A, int64_t p0) {
+    const size_t n = A.r.size();
+    if (!n) return DEM_OK;
+    auto up = [&](double* dst, const std::vector<double>& src) {
+        return cudaMemcpyAsync(dst + p0, src.data(), n * sizeof(double), cudaMemcpyHostToDevice,
+                               h->stream);
+    };
+    DemDev& d = h->d;
+    double* pd[3] = {d.px, d.py, d.pz};
+    double* vd[3] = {d.vx, d.vy, d.vz};
+    for (int c = 0; c < 3; ++c) {
+        CU(up(pd[c], A.pos[c]));
+        CU(up(vd[c], A.vel[c]));
+    }
+    const std::pair<double*, const std::vector<double>*> cols[] = {
+        {d.m, &A.m},
+        {d.inv_m, &A.inv_m},
+        {d.r, &A.r},
+        {d.r0, &A.r0},
+        {d.inv_inertia, &A.inv_inertia},
+        {d.b_invA, &A.b_invA},
+        {d.b_rbI, &A.b_rbI},
+        {d.b_EA, &A.b_EA},
+        {d.b_EI, &A.b_EI},
+        {d.b_phic, &A.b_phic}};
+    for (const auto& c : cols) CU(up(c.first, *c.second));
+    std::vector<double> one(n, 1.0);
+    CU(up(d.qw, one));
+    for (double* z : {d.wx, d.wy, d.wz, d.qx, d.qy, d.qz, d.wsx, d.wsy, d.wsz, d.fx, d.fy, d.fz,
+                      d.tx, d.ty, d.tz})
+        CU(cudaMemsetAsync(z + p0, 0, n * sizeof(double), h->stream));
+    // the host vectors above must outlive the copies
+    CU(cudaStreamSynchronize(h->stream));
+    return DEM_OK;
+}
+
 void record_step(DemHandle* h, int cur) {
     const int nxt = cur ^ 1;
-    launch_broadphase(h->d, h->p, h->ntiles_cells, h->stream);
-    launch_detect(h->d, h->p, cur, false, h->stream);
-    launch_compact(h->d, h->p, cur, false, h->force_grid, h->stream);
-    launch_force(h->d, h->p, nxt, h->force_grid, h->stream);
-    launch_integrate(h->d, h->p, cur, h->stream);
+    launch_broadphase(h->d, h->p, cur, h->multi, h->ntiles_cells, h->stream);
+    launch_detect(h->d, h->p, cur, false, h->multi, h->stream);
+    launch_compact(h->d, h->p, cur, false, h->multi, h->force_grid, h->stream);
+    launch_force(h->d, h->p, nxt, h->multi, h->force_grid, h->stream);
+    launch_integrate(h->d, h->p, cur, h->multi, h->stream);
 }
 
 int build_graphs(DemHandle* h) {
@@ -231,13 +487,17 @@ int read_counters(DemHandle* h, DevCounters* out) {
     return DEM_OK;
 }
 
+int error_code(int bits) {
+    if (bits & kErrCapacity) return DEM_ERR_CAPACITY;
+    if (bits & kErrTimeout) return DEM_ERR_TIMEOUT;
+    if (bits & kErrRange) return DEM_ERR_RANGE;
+    return DEM_OK;
+}
+
 int device_error(DemHandle* h) {
     DevCounters c;
     TRY(read_counters(h, &c));
-    if (c.error & kErrCapacity) return DEM_ERR_CAPACITY;
-    if (c.error & kErrTimeout) return DEM_ERR_TIMEOUT;
-    if (c.error & kErrRange) return DEM_ERR_RANGE;
-    return DEM_OK;
+    return error_code(c.error);
 }
 
 int contact_count(DemHandle* h, int buf, int32_t* total) {
@@ -245,7 +505,7 @@ int contact_count(DemHandle* h, int buf, int32_t* total) {
     CU(cudaMemcpyAsync(&v, &h->d.ctr->row_alloc[buf], sizeof(v), cudaMemcpyDeviceToHost,
                        h->stream));
     CU(cudaStreamSynchronize(h->stream));
-    *total = (int32_t)v;
+    *total = (int32_t)std::min<int64_t>((int64_t)v, (int64_t)h->c_cap);
     return DEM_OK;
 }
 
@@ -255,20 +515,195 @@ int get_dev(std::vector<double>& host, const double* dev, size_t n, cudaStream_t
     return DEM_OK;
 }
 
+// Particle state exchange goes through one pinned staging buffer per handle
+// (22 FP64 columns), so each call is one batch of asynchronous copies and one
+// synchronisation.
+int staging(DemHandle* h, int64_t n, double** out) {
+    if (!h->pinned || h->pinned_n < n) {
+        if (h->pinned) cudaFreeHost(h->pinned);
+        h->pinned = nullptr;
+        h->pinned_n = 0;
+        const int64_t m = std::max<int64_t>(n, 1);
+        CU(cudaMallocHost(&h->pinned, sizeof(double) * 22 * (size_t)m));
+        h->pinned_n = m;
+    }
+    *out = h->pinned;
+    return DEM_OK;
+}
+
+const SceneHost* scene_at(DemHandle* h, int32_t s) {
+    if (!h || s < 0 || s >= (int32_t)h->scenes.size()) return nullptr;
+    const SceneHost& S = h->scenes[s];
+    return S.mode == kModeFree ? nullptr : &S;
+}
+
+int apply_modes(DemHandle* h, const std::vector<std::pair<int, int>>& upd) {
+    for (size_t k = 0; k < upd.size(); k += 64) {
+        ModeUpdates u{};
+        u.count = (int)std::min<size_t>(64, upd.size() - k);
+        for (int t = 0; t < u.count; ++t) {
+            u.idx[t] = upd[k + t].first;
+            u.mode[t] = upd[k + t].second;
+        }
+        k_set_modes<<<1, 64, 0, h->stream>>>(h->d.sp, u);
+        CU(cudaGetLastError());
+    }
+    return DEM_OK;
+}
+
+// Particle state of slots [p0, p0 + n) to host arrays (scene-local order).
+int get_particles_range(DemHandle* h, int64_t p0, int64_t n, DemParticleState* out) {
+    struct F {
+        double* dst;
+        int stride;
+        double* src[4];
+        int k;
+    };
+    const DemDev& d = h->d;
+    const F fields[] = {{out->pos, 3, {d.px, d.py, d.pz}, 3},
+                        {out->vel, 3, {d.vx, d.vy, d.vz}, 3},
+                        {out->omega, 3, {d.wx, d.wy, d.wz}, 3},
+                        {out->quat, 4, {d.qw, d.qx, d.qy, d.qz}, 4},
+                        {out->force, 3, {d.fx, d.fy, d.fz}, 3},
+                        {out->moment, 3, {d.tx, d.ty, d.tz}, 3},
+                        {out->wall_shear, 3, {d.wsx, d.wsy, d.wsz}, 3}};
+    double* st = nullptr;
+    TRY(staging(h, n, &st));
+    if (n) {
+        size_t col = 0;
+        for (const F& f : fields) {
+            if (!f.dst) continue;
+            for (int c = 0; c < f.k; ++c, ++col)
+                CU(cudaMemcpyAsync(st + col * n, f.src[c] + p0, n * sizeof(double),
+                                   cudaMemcpyDeviceToHost, h->stream));
+        }
+        CU(cudaStreamSynchronize(h->stream));
+        col = 0;
+        for (const F& f : fields) {
+            if (!f.dst) continue;
+            for (int c = 0; c < f.k; ++c, ++col) {
+                const double* src = st + col * n;
+                for (int64_t i = 0; i < n; ++i) f.dst[f.stride * i + c] = src[i];
+            }
+        }
+    }
+    return device_error(h);
+}
+
+// Contact entries of the current buffer whose owner lies in slots
+// [p0, p0 + n): the rows of those slots, and the active entries among them.
+struct RangeContacts {
+    std::vector<int32_t> ci, cj, act;
+    std::vector<uint32_t> fl;
+    int32_t C = 0;
+};
+int range_contacts(DemHandle* h, int64_t p0, int64_t n, RangeContacts& R) {
+    if (h->n_cap) TRY(contact_count(h, h->cur, &R.C));
+    const int32_t C = R.C;
+    const ContactSoA& s = h->d.c[h->cur];
+    R.ci.resize(C);
+    R.cj.resize(C);
+    R.fl.resize(C);
+    std::vector<int32_t> rs(n), rl(n);
+    if (C) {
+        CU(cudaMemcpyAsync(R.ci.data(), s.ci, (size_t)C * 4, cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaMemcpyAsync(R.cj.data(), s.cj, (size_t)C * 4, cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaMemcpyAsync(R.fl.data(), s.fl, (size_t)C * 4, cudaMemcpyDeviceToHost, h->stream));
+    }
+    if (n) {
+        CU(cudaMemcpyAsync(rs.data(), h->d.row_start[h->cur] + p0, (size_t)n * 4,
+                           cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaMemcpyAsync(rl.data(), h->d.row_len[h->cur] + p0, (size_t)n * 4,
+                           cudaMemcpyDeviceToHost, h->stream));
+    }
+    CU(cudaStreamSynchronize(h->stream));
+    R.act.clear();
+    for (int64_t i = 0; i < n; ++i)
+        for (int32_t c = std::max(rs[i], 0); c < std::min(rs[i] + rl[i], C); ++c)
+            if ((R.fl[c] & kActive) && R.ci[c] == p0 + i) R.act.push_back(c);
+    return DEM_OK;
+}
+
+// Active contacts whose owner lies in slots [p0, p0 + n), with scene-local
+// indices, sorted by (i, j).
+int get_contacts_range(DemHandle* h, int64_t p0, int64_t n, DemContacts* out, int64_t cap,
+                       int64_t* n_out) {
+    TRY(device_error(h));
+    RangeContacts R;
+    TRY(range_contacts(h, p0, n, R));
+    const int32_t C = R.C;
+    const ContactSoA& s = h->d.c[h->cur];
+    const std::vector<int32_t>&ci = R.ci, &cj = R.cj;
+    const std::vector<uint32_t>& fl = R.fl;
+    std::vector<int32_t>& act = R.act;
+    std::sort(act.begin(), act.end(), [&](int32_t a, int32_t b) {
+        return ci[a] != ci[b] ? ci[a] < ci[b] : cj[a] < cj[b];
+    });
+    const int64_t na = (int64_t)act.size();
+    *n_out = na;
+    if (!out) return DEM_OK;
+    if (na > cap) return DEM_ERR_CAPACITY;
+    std::vector<double> f[15];
+    if (na) {
+        for (int q = 0; q < 15; ++q) TRY(get_dev(f[q], s.f[q], (size_t)C, h->stream));
+        CU(cudaStreamSynchronize(h->stream));
+    }
+    for (int64_t t = 0; t < na; ++t) {
+        const int32_t c = act[t];
+        if (out->i) out->i[t] = (int32_t)(ci[c] - p0);
+        if (out->j) out->j[t] = (int32_t)(cj[c] - p0);
+        if (out->bonded) out->bonded[t] = (fl[c] & kBonded) ? 1 : 0;
+        for (int q = 0; q < 3; ++q) {
+            if (out->point) out->point[3 * t + q] = f[CK + q][c];
+            if (out->force) out->force[3 * t + q] = f[CF + q][c];
+            if (out->torque_i) out->torque_i[3 * t + q] = f[CTI + q][c];
+            if (out->torque_j) out->torque_j[3 * t + q] = f[CTJ + q][c];
+            if (out->shear) out->shear[3 * t + q] = f[CS + q][c];
+        }
+    }
+    return DEM_OK;
+}
+
+int stats_of(DemHandle* h, int32_t s, const SceneHost& S, DemStats* out) {
+    DevCounters c;
+    TRY(read_counters(h, &c));
+    SceneCounters sc{};
+    CU(cudaMemcpy(&sc, h->d.sctr + s, sizeof(sc), cudaMemcpyDeviceToHost));
+    RangeContacts R;
+    TRY(range_contacts(h, S.sp.p0, S.sp.n, R));
+    const int64_t act = (int64_t)R.act.size();
+    int64_t bnd = 0;
+    for (int32_t k : R.act) bnd += (R.fl[k] & kBonded) ? 1 : 0;
+    std::memset(out, 0, sizeof(*out));
+    out->n_particles = S.sp.n;
+    out->steps_done = h->multi ? S.steps : h->steps;
+    out->contacts = act;
+    out->bonded = bnd;
+    out->bonds_broken = (int64_t)sc.broken;
+    out->contacts_ended = (int64_t)sc.ended;
+    out->contacts_created = (int64_t)sc.created;
+    out->warn_gap = (int64_t)sc.warn_gap;
+    out->warn_damping = (int64_t)sc.warn_damp;
+    out->error = error_code(c.error);
+    out->precision = h->p.precision;
+    return DEM_OK;
+}
+
 }  // namespace
 
 extern "C" {
 
-const char* dem_version(void) { return "dem_gb300 0.1.0 sm_103a"; }
+const char* dem_version(void) { return "dem_gb300 0.2.0 sm_103a"; }
 
 const char* dem_strerror(int code) {
     switch (code) {
         case DEM_OK: return "ok";
         case DEM_ERR_INVALID: return "invalid argument or state";
         case DEM_ERR_CUDA: return g_msg[0] ? g_msg : "CUDA runtime error";
-        case DEM_ERR_CAPACITY: return "contact buffer capacity exceeded (raise max_coordinate_number)";
+        case DEM_ERR_CAPACITY:
+            return "capacity exceeded (contacts per particle, arena slots, buckets or scenes)";
         case DEM_ERR_TIMEOUT: return "a bounded device-side wait gave up";
-        case DEM_ERR_NO_DEVICE: return "no sm_103 (GB300) CUDA device available";
+        case DEM_ERR_NO_DEVICE: return g_msg[0] ? g_msg : "no sm_103 (GB300) CUDA device available";
         case DEM_ERR_RANGE: return "particle outside the representable cell range";
         default: return "unknown error";
     }
@@ -283,175 +718,166 @@ int dem_set_device(int device) {
 }
 
 int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out) {
-    if (!cfg || !pin || !out || pin->n < 0 || pin->n > 0x3fffffff) return DEM_ERR_INVALID;
-    if (pin->n > 0 && (!pin->volume || !pin->mass || !pin->pos || !pin->vel)) return DEM_ERR_INVALID;
-    if (!(cfg->dt > 0) || cfg->max_coordinate_number <= 0) return DEM_ERR_INVALID;
+    if (!out) return DEM_ERR_INVALID;
     *out = nullptr;
-    int dev = 0, ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DEM_ERR_NO_DEVICE;
-    CU(cudaGetDevice(&dev));
-    cudaDeviceProp prop;
-    CU(cudaGetDeviceProperties(&prop, dev));
-    if (prop.major != 10 || prop.minor != 3) {
-        std::snprintf(g_msg, sizeof(g_msg), "device %d is sm_%d%d; this library is built for sm_103a",
-                      dev, prop.major, prop.minor);
-        return DEM_ERR_NO_DEVICE;
-    }
+    SceneHost S;
+    SceneArrays A;
+    TRY(prepare_scene(cfg, pin, 1.0, S, A));
+    if (S.der.contact_capacity > 0x7fffffff) return DEM_ERR_CAPACITY;
+    int dev = 0, sms = 0;
+    TRY(check_device(&dev, &sms));
     DemHandle* h = new DemHandle();
-    h->cfg = *cfg;
     h->device = dev;
-    h->sm_count = prop.multiProcessorCount;
-    h->n = (int)pin->n;
-    const int n = h->n;
-    // grain setup (src/executor.jl:219-243)
-    std::vector<double> r(n), r0(n), inv_inertia(n), inv_m(n), q0(n, 1.0), zeros(n, 0.0);
-    std::vector<double> b_invA(n), b_rbI(n), b_EA(n), b_EI(n), b_phic(n);
-    std::vector<double> pos[3], vel[3];
-    double rmax_r = -INFINITY;
-    for (int c = 0; c < 3; ++c) {
-        pos[c].resize(n);
-        vel[c].resize(n);
-    }
-    for (int i = 0; i < n; ++i) {
-        const double V = pin->volume[i], m = pin->mass[i];
-        r[i] = std::cbrt(V / (4.0 / 3.0 * kPi));
-        r0[i] = r[i] * cfg->particle_contact_radius_multiplier;
-        inv_inertia[i] = 1.0 / (2.0 / 5.0 * m * (r[i] * r[i]));
-        inv_m[i] = 1.0 / m;
-        // bond section of src/kernels.jl:178-184 for rb = ρ·rᵢ: 1/A and rb/I
-        const double rb = cfg->bond_radius_ratio * r[i];
-        const double Ab = rb * rb * kPi, Ib = rb * rb * (rb * rb) * (kPi / 4.0);
-        b_invA[i] = 1.0 / Ab;
-        b_rbI[i] = rb / Ib;
-        b_EA[i] = cfg->bond_elastic_modulus * Ab;
-        b_EI[i] = cfg->bond_elastic_modulus * Ib;
-        b_phic[i] = 20.0 / 3.0 * (1.0 + cfg->bond_poisson_ratio) * (rb * rb);
-        rmax_r = std::max(rmax_r, r[i]);
-        for (int c = 0; c < 3; ++c) {
-            pos[c][i] = pin->pos[3 * i + c];
-            vel[c][i] = pin->vel[3 * i + c];
-        }
-    }
-    // derived sizes (src/executor.jl:244-267)
-    DemDerived& D = h->der;
-    D.material_density = n ? pin->mass[n - 1] / pin->volume[n - 1] : 0.0;
-    D.r_max = rmax_r * cfg->particle_contact_radius_multiplier *
-              (1.0 + cfg->bond_tensile_strength / cfg->bond_elastic_modulus) *
-              cfg->neighboring_search_safety_factor;
-    D.cell_size = 4.0 * D.r_max;
-    int64_t prod = 1;
-    for (int c = 0; c < 3; ++c)
-        prod *= (int64_t)std::ceil((cfg->domain_max[c] - cfg->domain_min[c]) / D.cell_size);
-    D.hash_table_size = std::min<int64_t>(std::max<int64_t>(prod, 1 << 20), 1 << 22);
-    D.total_steps = (int64_t)std::trunc(cfg->target_time / cfg->dt);
-    D.save_per_steps = (int64_t)std::trunc(cfg->saving_interval_time / cfg->dt);
-    D.contact_capacity = (int64_t)n * cfg->max_coordinate_number;
-    if (n > 0 && !(D.cell_size > 0 && std::isfinite(D.cell_size))) {
-        delete h;
-        return DEM_ERR_INVALID;
-    }
-    if (D.contact_capacity > 0x7fffffff) {
-        delete h;
-        return DEM_ERR_CAPACITY;
-    }
-    // device constants (materials / surfaces / wall of src/executor.jl:282-315)
-    DemParams& p = h->p;
-    p.n = n;
-    p.cap = (int)D.contact_capacity;
-    p.kstash = (int)std::min<int64_t>(cfg->max_coordinate_number, 64);
-    p.kin = p.kstash;
-    p.H = (uint32_t)D.hash_table_size;
-    p.H_pow2_mask = (p.H & (p.H - 1)) == 0 ? p.H - 1 : 0;
-    p.has_wall = 1;
-    p.precision = DEM_FP64;
-    for (int c = 0; c < 3; ++c) {
-        p.dmin[c] = cfg->domain_min[c];
-        p.grav[c] = cfg->gravity[c];
-        p.wn[c] = cfg->wall_normal[c];
-    }
-    p.cell = D.cell_size;
-    p.inv_cell = 1.0 / D.cell_size;
-    p.dt = cfg->dt;
-    p.tol = cfg->tolerance;
-    p.damping = cfg->global_damping;
-    const Hertz pp = hertz_constants(cfg->particle_elastic_modulus, cfg->particle_poisson_ratio,
-                                     cfg->particle_elastic_modulus, cfg->particle_poisson_ratio,
-                                     cfg->pp_coefficient_restitution);
-    p.pp_mu = cfg->pp_coefficient_friction;
-    p.pp_beta = pp.beta;
-    p.pp_Ys = pp.Ys;
-    p.pp_Gs = pp.Gs;
-    p.pp_cgn = pp.cgn;
-    p.pp_cgt = pp.cgt;
-    p.b_rho = cfg->bond_radius_ratio;
-    p.b_E = cfg->bond_elastic_modulus;
-    p.b_nu = cfg->bond_poisson_ratio;
-    p.b_inv1pnu = 1.0 / (1.0 + cfg->bond_poisson_ratio);
-    p.b_sc = cfg->bond_compressive_strength;
-    p.b_st = cfg->bond_tensile_strength;
-    p.b_ss = cfg->bond_shear_strength;
-    p.wd = cfg->wall_distance;
-    const M3 WR = wall_frame(cfg->wall_normal, cfg->tolerance);
-    const M3 WRi = inverse3(WR);
-    for (int r_ = 0; r_ < 3; ++r_)
-        for (int c = 0; c < 3; ++c) {
-            p.wR[3 * r_ + c] = WR.a[r_][c];
-            p.wRinv[3 * r_ + c] = WRi.a[r_][c];
-        }
-    const Hertz pw = hertz_constants(cfg->particle_elastic_modulus, cfg->particle_poisson_ratio,
-                                     cfg->wall_elastic_modulus, cfg->wall_poisson_ratio,
-                                     cfg->pw_coefficient_restitution);
-    p.pw_mu = cfg->pw_coefficient_friction;
-    p.pw_beta = pw.beta;
-    p.pw_Ys = pw.Ys;
-    p.pw_Gs = pw.Gs;
-    p.pw_cgn = pw.cgn;
-    p.pw_cgt = pw.cgt;
-
-    auto fail = [&](int rc) {
+    h->sm_count = sms;
+    h->multi = false;
+    h->n_cap = (int)pin->n;
+    h->c_cap = (int)S.der.contact_capacity;
+    h->t_cap = (uint32_t)S.der.hash_table_size;
+    h->s_cap = 1;
+    h->p.n = h->n_cap;
+    h->p.cap = h->c_cap;
+    h->p.kstash = (int)std::min<int64_t>(cfg->max_coordinate_number, 64);
+    h->p.kin = h->p.kstash;
+    h->p.T = h->t_cap;
+    h->p.precision = DEM_FP64;
+    S.sp.mode = kModeStep;
+    S.sp.p0 = 0;
+    S.sp.t0 = 0;
+    S.sp.H = S.sp.Href;
+    S.sp.Hmask = S.sp.Href_mask;
+    S.mode = kModeStep;
+    h->p.s0 = S.sp;
+    h->scenes.push_back(S);
+    int rc = init_handle(h);
+    if (rc == DEM_OK) rc = upload_scene(h, A, 0);
+    if (rc != DEM_OK) {
         free_all(h);
         delete h;
         return rc;
-    };
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
-        return fail(DEM_ERR_CUDA);
-    if (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
-        return fail(DEM_ERR_CUDA);
-    int rc = allocate(h);
-    if (rc != DEM_OK) return fail(rc);
-    h->ntiles_cells = scan_tiles((int64_t)p.H);
-    h->force_grid = (int)std::max<int64_t>(
-        1, std::min<int64_t>(((int64_t)p.cap + 255) / 256, (int64_t)h->sm_count * 16));
-    auto up = [&](double* dst, const std::vector<double>& src) {
-        return n ? cudaMemcpyAsync(dst, src.data(), n * sizeof(double), cudaMemcpyHostToDevice,
-                                   h->stream)
-                 : cudaSuccess;
-    };
-    std::vector<double> mass(pin->mass, pin->mass + n);
-    cudaError_t e = cudaSuccess;
-    double* pd[3] = {h->d.px, h->d.py, h->d.pz};
-    double* vd[3] = {h->d.vx, h->d.vy, h->d.vz};
-    for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
-        e = up(pd[c], pos[c]);
-        if (e == cudaSuccess) e = up(vd[c], vel[c]);
-    }
-    if (e == cudaSuccess) e = up(h->d.qw, q0);
-    if (e == cudaSuccess) e = up(h->d.m, mass);
-    if (e == cudaSuccess) e = up(h->d.inv_m, inv_m);
-    if (e == cudaSuccess) e = up(h->d.b_invA, b_invA);
-    if (e == cudaSuccess) e = up(h->d.b_rbI, b_rbI);
-    if (e == cudaSuccess) e = up(h->d.b_EA, b_EA);
-    if (e == cudaSuccess) e = up(h->d.b_EI, b_EI);
-    if (e == cudaSuccess) e = up(h->d.b_phic, b_phic);
-    if (e == cudaSuccess) e = up(h->d.r, r);
-    if (e == cudaSuccess) e = up(h->d.r0, r0);
-    if (e == cudaSuccess) e = up(h->d.inv_inertia, inv_inertia);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    if (e != cudaSuccess) {
-        std::snprintf(g_msg, sizeof(g_msg), "dem_create upload: %s", cudaGetErrorString(e));
-        return fail(DEM_ERR_CUDA);
     }
     *out = h;
+    return DEM_OK;
+}
+
+int dem_arena_create(const DemArenaConfig* cfg, DemHandle** out) {
+    if (!cfg || !out || cfg->max_particles <= 0 || cfg->max_particles > 0x3fffffff ||
+        cfg->max_contacts <= 0 || cfg->max_contacts > 0x7fffffff || cfg->max_buckets <= 0 ||
+        cfg->max_buckets > 0x7fffffff || cfg->max_scenes <= 0 || cfg->max_coordinate_number <= 0 ||
+        (cfg->precision != DEM_FP64 && cfg->precision != DEM_FP32_FORCE) ||
+        !(cfg->cell_factor >= 0) || cfg->cell_factor > 1)
+        return DEM_ERR_INVALID;
+    *out = nullptr;
+    int dev = 0, sms = 0;
+    TRY(check_device(&dev, &sms));
+    DemHandle* h = new DemHandle();
+    h->device = dev;
+    h->sm_count = sms;
+    h->multi = true;
+    h->n_cap = (int)cfg->max_particles;
+    h->c_cap = (int)cfg->max_contacts;
+    h->t_cap = (uint32_t)cfg->max_buckets;
+    h->s_cap = cfg->max_scenes;
+    h->cell_factor = cfg->cell_factor > 0 ? cfg->cell_factor : 1.0;
+    h->p.n = h->n_cap;
+    h->p.cap = h->c_cap;
+    h->p.kstash = std::min(cfg->max_coordinate_number, 64);
+    h->p.kin = h->p.kstash;
+    h->p.T = h->t_cap;
+    h->p.precision = cfg->precision;
+    h->scenes.resize(h->s_cap);
+    h->pfree.init(h->n_cap);
+    h->tfree.init(h->t_cap);
+    int rc = init_handle(h);
+    if (rc == DEM_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = DEM_ERR_CUDA;
+    if (rc != DEM_OK) {
+        free_all(h);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return DEM_OK;
+}
+
+int dem_arena_add(DemHandle* h, const DemConfigC* cfg, const DemParticlesIn* pin, int init_bonds,
+                  int64_t steps_target, int32_t* scene) {
+    if (!h || !h->multi || !scene || steps_target < 0) return DEM_ERR_INVALID;
+    SceneHost S;
+    SceneArrays A;
+    TRY(prepare_scene(cfg, pin, h->cell_factor, S, A));
+    int idx = -1;
+    for (int s = 0; s < h->s_cap; ++s)
+        if (h->scenes[s].mode == kModeFree) {
+            idx = s;
+            break;
+        }
+    if (idx < 0) return DEM_ERR_CAPACITY;
+    const int64_t n = pin->n;
+    // search table of the scene: a power of two of at least 4 entries per particle
+    uint32_t H = 1024;
+    while ((int64_t)H < 4 * n && H < (1u << 30)) H <<= 1;
+    int64_t p0 = 0, t0 = 0;
+    if (!h->pfree.take(n, &p0)) return DEM_ERR_CAPACITY;
+    if (!h->tfree.take(H, &t0)) {
+        h->pfree.give(p0, n);
+        return DEM_ERR_CAPACITY;
+    }
+    S.sp.p0 = (int)p0;
+    S.sp.t0 = (uint32_t)t0;
+    S.sp.H = H;
+    S.sp.Hmask = H - 1;
+    S.sp.mode = init_bonds ? kModeInit : kModeStep;
+    S.mode = S.sp.mode;
+    S.steps = 0;
+    S.target = steps_target;
+    int rc = upload_scene(h, A, p0);
+    // the slots start with empty contact rows in both buffers
+    for (int b = 0; b < 2 && rc == DEM_OK && n; ++b)
+        if (cudaMemsetAsync(h->d.row_len[b] + p0, 0, (size_t)n * 4, h->stream) != cudaSuccess ||
+            cudaMemsetAsync(h->d.row_start[b] + p0, 0, (size_t)n * 4, h->stream) != cudaSuccess)
+            rc = DEM_ERR_CUDA;
+    if (rc == DEM_OK && n) {
+        const int nb = (int)((n + 255) / 256);
+        k_fill_i32<<<nb, 256, 0, h->stream>>>(h->d.scene_of + p0, n, idx);
+        if (cudaGetLastError() != cudaSuccess) rc = DEM_ERR_CUDA;
+    }
+    if (rc == DEM_OK &&
+        (cudaMemcpyAsync(h->d.sp + idx, &S.sp, sizeof(SceneParams), cudaMemcpyHostToDevice,
+                         h->stream) != cudaSuccess ||
+         cudaMemsetAsync(h->d.sctr + idx, 0, sizeof(SceneCounters), h->stream) != cudaSuccess ||
+         cudaStreamSynchronize(h->stream) != cudaSuccess))
+        rc = DEM_ERR_CUDA;
+    if (rc != DEM_OK) {
+        h->pfree.give(p0, n);
+        h->tfree.give(t0, H);
+        return rc;
+    }
+    h->scenes[idx] = S;
+    *scene = idx;
+    return DEM_OK;
+}
+
+int dem_arena_remove(DemHandle* h, int32_t s) {
+    if (!h || !h->multi || !scene_at(h, s)) return DEM_ERR_INVALID;
+    SceneHost& S = h->scenes[s];
+    const int64_t p0 = S.sp.p0, n = S.sp.n;
+    TRY(apply_modes(h, {{s, kModeFree}}));
+    if (n) CU(cudaMemsetAsync(h->d.scene_of + p0, 0xff, (size_t)n * sizeof(int32_t), h->stream));
+    h->pfree.give(p0, n);
+    h->tfree.give(S.sp.t0, S.sp.H);
+    S = SceneHost();
+    return DEM_OK;
+}
+
+int dem_arena_scene_info(DemHandle* h, int32_t s, DemSceneInfo* out) {
+    const SceneHost* S = scene_at(h, s);
+    if (!S || !out) return DEM_ERR_INVALID;
+    std::memset(out, 0, sizeof(*out));
+    out->mode = S->mode;
+    out->n = S->sp.n;
+    out->first_slot = S->sp.p0;
+    out->steps_done = h->multi ? S->steps : h->steps;
+    out->steps_target = S->target;
+    out->buckets = S->sp.H;
     return DEM_OK;
 }
 
@@ -470,12 +896,12 @@ int dem_set_precision(DemHandle* h, int mode) {
 }
 
 int dem_init_bonds(DemHandle* h) {
-    if (!h) return DEM_ERR_INVALID;
-    if (h->n == 0) return DEM_OK;
+    if (!h || h->multi) return DEM_ERR_INVALID;
+    if (h->n_cap == 0) return DEM_OK;
     const int cur = h->cur, nxt = cur ^ 1;
-    launch_broadphase(h->d, h->p, h->ntiles_cells, h->stream);
-    launch_detect(h->d, h->p, cur, true, h->stream);
-    launch_compact(h->d, h->p, cur, true, h->force_grid, h->stream);
+    launch_broadphase(h->d, h->p, cur, false, h->ntiles_cells, h->stream);
+    launch_detect(h->d, h->p, cur, true, false, h->stream);
+    launch_compact(h->d, h->p, cur, true, false, h->force_grid, h->stream);
     // the old buffer becomes the next step's target: its allocator starts at 0
     CU(cudaMemsetAsync(&h->d.ctr->row_alloc[cur], 0, sizeof(unsigned int), h->stream));
     CU(cudaGetLastError());
@@ -485,14 +911,51 @@ int dem_init_bonds(DemHandle* h) {
 
 int dem_step(DemHandle* h, int64_t nsteps) {
     if (!h || nsteps < 0) return DEM_ERR_INVALID;
-    if (h->n == 0 || nsteps == 0) {
+    if (h->n_cap == 0 || nsteps == 0) {
         h->steps += nsteps;
         return DEM_OK;
     }
     TRY(build_graphs(h));
+    std::vector<std::pair<int, int>> upd;
+    if (h->multi) {
+        // `initialize!` of newly added scenes: one launch in which they run in
+        // Init mode and every stepping scene is held (Frozen carries its state
+        // and contacts over unchanged), so it costs them no step
+        std::vector<std::pair<int, int>> back;
+        for (int k = 0; k < h->s_cap; ++k) {
+            SceneHost& S = h->scenes[k];
+            if (S.mode == kModeStep) {
+                upd.push_back({k, kModeFrozen});
+                back.push_back({k, kModeStep});
+            } else if (S.mode == kModeInit) {
+                S.mode = kModeStep;
+                back.push_back({k, kModeStep});
+            }
+        }
+        if (back.size() > upd.size()) {
+            TRY(apply_modes(h, upd));
+            CU(cudaGraphLaunch(h->exec[h->cur], h->stream));
+            h->cur ^= 1;
+            TRY(apply_modes(h, back));
+        }
+    }
     for (int64_t s = 0; s < nsteps; ++s) {
         CU(cudaGraphLaunch(h->exec[h->cur], h->stream));
         h->cur ^= 1;
+        if (!h->multi) continue;
+        // scene bookkeeping between launches (stream-ordered, no host sync)
+        upd.clear();
+        for (int k = 0; k < h->s_cap; ++k) {
+            SceneHost& S = h->scenes[k];
+            if (S.mode == kModeStep) {
+                ++S.steps;
+                if (S.target > 0 && S.steps >= S.target) {
+                    S.mode = kModeFrozen;
+                    upd.push_back({k, kModeFrozen});
+                }
+            }
+        }
+        if (!upd.empty()) TRY(apply_modes(h, upd));
     }
     h->steps += nsteps;
     return DEM_OK;
@@ -510,8 +973,8 @@ int dem_step_timed(DemHandle* h, int64_t nsteps, float* ms) {
 }
 
 int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
-    if (!h || !phase_ms || nphase < 5) return DEM_ERR_INVALID;
-    if (h->n == 0) {
+    if (!h || !phase_ms || nphase < 5 || h->multi) return DEM_ERR_INVALID;
+    if (h->n_cap == 0) {
         for (int k = 0; k < 5; ++k) phase_ms[k] = 0.f;
         return DEM_OK;
     }
@@ -519,18 +982,19 @@ int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
     for (int k = 0; k < 6; ++k) CU(cudaEventCreate(&ev[k]));
     const int cur = h->cur, nxt = cur ^ 1;
     cudaEventRecord(ev[0], h->stream);
-    launch_broadphase(h->d, h->p, h->ntiles_cells, h->stream);
+    launch_broadphase(h->d, h->p, cur, false, h->ntiles_cells, h->stream);
     cudaEventRecord(ev[1], h->stream);
-    launch_detect(h->d, h->p, cur, false, h->stream);
+    launch_detect(h->d, h->p, cur, false, false, h->stream);
     cudaEventRecord(ev[2], h->stream);
-    launch_compact(h->d, h->p, cur, false, h->force_grid, h->stream);
+    launch_compact(h->d, h->p, cur, false, false, h->force_grid, h->stream);
     cudaEventRecord(ev[3], h->stream);
-    launch_force(h->d, h->p, nxt, h->force_grid, h->stream);
+    launch_force(h->d, h->p, nxt, false, h->force_grid, h->stream);
     cudaEventRecord(ev[4], h->stream);
-    launch_integrate(h->d, h->p, cur, h->stream);
+    launch_integrate(h->d, h->p, cur, false, h->stream);
     cudaEventRecord(ev[5], h->stream);
     cudaError_t e = cudaEventSynchronize(ev[5]);
-    for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = cudaEventElapsedTime(&phase_ms[k], ev[k], ev[k + 1]);
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k)
+        e = cudaEventElapsedTime(&phase_ms[k], ev[k], ev[k + 1]);
     for (int k = 0; k < 6; ++k) cudaEventDestroy(ev[k]);
     CU(e);
     h->cur = nxt;
@@ -543,20 +1007,24 @@ int dem_sync(DemHandle* h) {
     return device_error(h);
 }
 
-int dem_get_derived(DemHandle* h, DemDerived* out) {
-    if (!h || !out) return DEM_ERR_INVALID;
-    *out = h->der;
+int dem_scene_get_derived(DemHandle* h, int32_t s, DemDerived* out) {
+    const SceneHost* S = scene_at(h, s);
+    if (!S || !out) return DEM_ERR_INVALID;
+    *out = S->der;
     return DEM_OK;
 }
 
+int dem_get_derived(DemHandle* h, DemDerived* out) { return dem_scene_get_derived(h, 0, out); }
+
 int dem_get_static(DemHandle* h, DemParticleStatic* out) {
-    if (!h || !out) return DEM_ERR_INVALID;
-    const size_t n = (size_t)h->n;
+    const SceneHost* S = scene_at(h, 0);
+    if (!S || !out) return DEM_ERR_INVALID;
+    const size_t n = (size_t)S->sp.n, p0 = (size_t)S->sp.p0;
     std::vector<double> r, r0, m, ii;
-    TRY(get_dev(r, h->d.r, n, h->stream));
-    TRY(get_dev(r0, h->d.r0, n, h->stream));
-    TRY(get_dev(m, h->d.m, n, h->stream));
-    TRY(get_dev(ii, h->d.inv_inertia, n, h->stream));
+    TRY(get_dev(r, h->d.r + p0, n, h->stream));
+    TRY(get_dev(r0, h->d.r0 + p0, n, h->stream));
+    TRY(get_dev(m, h->d.m + p0, n, h->stream));
+    TRY(get_dev(ii, h->d.inv_inertia + p0, n, h->stream));
     CU(cudaStreamSynchronize(h->stream));
     for (size_t i = 0; i < n; ++i) {
         if (out->radius) out->radius[i] = r[i];
@@ -567,72 +1035,36 @@ int dem_get_static(DemHandle* h, DemParticleStatic* out) {
     return DEM_OK;
 }
 
-// Particle state exchange goes through one pinned staging buffer per handle
-// (22 FP64 columns), so each call is one batch of asynchronous copies and one
-// synchronisation.
-static int staging(DemHandle* h, double** out) {
-    if (!h->pinned) CU(cudaMallocHost(&h->pinned, sizeof(double) * 22 * std::max(h->n, 1)));
-    *out = h->pinned;
-    return DEM_OK;
+int dem_scene_get_particles(DemHandle* h, int32_t s, DemParticleState* out) {
+    const SceneHost* S = scene_at(h, s);
+    if (!S || !out) return DEM_ERR_INVALID;
+    return get_particles_range(h, S->sp.p0, S->sp.n, out);
 }
 
 int dem_get_particles(DemHandle* h, DemParticleState* out) {
-    if (!h || !out) return DEM_ERR_INVALID;
-    const size_t n = (size_t)h->n;
-    struct F {
-        double* dst;
-        int stride;
-        double* src[4];
-        int k;
-    };
-    const F fields[] = {{out->pos, 3, {h->d.px, h->d.py, h->d.pz}, 3},
-                        {out->vel, 3, {h->d.vx, h->d.vy, h->d.vz}, 3},
-                        {out->omega, 3, {h->d.wx, h->d.wy, h->d.wz}, 3},
-                        {out->quat, 4, {h->d.qw, h->d.qx, h->d.qy, h->d.qz}, 4},
-                        {out->force, 3, {h->d.fx, h->d.fy, h->d.fz}, 3},
-                        {out->moment, 3, {h->d.tx, h->d.ty, h->d.tz}, 3},
-                        {out->wall_shear, 3, {h->d.wsx, h->d.wsy, h->d.wsz}, 3}};
-    double* st = nullptr;
-    TRY(staging(h, &st));
-    if (n) {
-        size_t col = 0;
-        for (const F& f : fields) {
-            if (!f.dst) continue;
-            for (int c = 0; c < f.k; ++c, ++col)
-                CU(cudaMemcpyAsync(st + col * n, f.src[c], n * sizeof(double),
-                                   cudaMemcpyDeviceToHost, h->stream));
-        }
-        CU(cudaStreamSynchronize(h->stream));
-        col = 0;
-        for (const F& f : fields) {
-            if (!f.dst) continue;
-            for (int c = 0; c < f.k; ++c, ++col) {
-                const double* src = st + col * n;
-                for (size_t i = 0; i < n; ++i) f.dst[f.stride * i + c] = src[i];
-            }
-        }
-    }
-    return device_error(h);
+    return dem_scene_get_particles(h, 0, out);
 }
 
 int dem_set_particles(DemHandle* h, const DemParticleState* in) {
-    if (!h || !in) return DEM_ERR_INVALID;
-    const size_t n = (size_t)h->n;
+    const SceneHost* S = scene_at(h, 0);
+    if (!S || !in || h->multi) return DEM_ERR_INVALID;
+    const size_t n = (size_t)S->sp.n;
     struct F {
         const double* src;
         int stride;
         double* dst[4];
         int k;
     };
-    const F fields[] = {{in->pos, 3, {h->d.px, h->d.py, h->d.pz}, 3},
-                        {in->vel, 3, {h->d.vx, h->d.vy, h->d.vz}, 3},
-                        {in->omega, 3, {h->d.wx, h->d.wy, h->d.wz}, 3},
-                        {in->quat, 4, {h->d.qw, h->d.qx, h->d.qy, h->d.qz}, 4},
-                        {in->wall_shear, 3, {h->d.wsx, h->d.wsy, h->d.wsz}, 3}};
-    double* st = nullptr;
-    TRY(staging(h, &st));
+    const DemDev& d = h->d;
+    const F fields[] = {{in->pos, 3, {d.px, d.py, d.pz}, 3},
+                        {in->vel, 3, {d.vx, d.vy, d.vz}, 3},
+                        {in->omega, 3, {d.wx, d.wy, d.wz}, 3},
+                        {in->quat, 4, {d.qw, d.qx, d.qy, d.qz}, 4},
+                        {in->wall_shear, 3, {d.wsx, d.wsy, d.wsz}, 3}};
     if (!n) return DEM_OK;
     CU(cudaStreamSynchronize(h->stream));  // the staging buffer may still be in use
+    double* st = nullptr;
+    TRY(staging(h, (int64_t)n, &st));
     size_t col = 0;
     for (const F& f : fields) {
         if (!f.src) continue;
@@ -647,54 +1079,21 @@ int dem_set_particles(DemHandle* h, const DemParticleState* in) {
     return DEM_OK;
 }
 
+int dem_scene_get_contacts(DemHandle* h, int32_t s, DemContacts* out, int64_t cap,
+                           int64_t* n_out) {
+    const SceneHost* S = scene_at(h, s);
+    if (!S || !n_out) return DEM_ERR_INVALID;
+    return get_contacts_range(h, S->sp.p0, S->sp.n, out, cap, n_out);
+}
+
 int dem_get_contacts(DemHandle* h, DemContacts* out, int64_t cap, int64_t* n_out) {
-    if (!h || !n_out) return DEM_ERR_INVALID;
-    TRY(device_error(h));
-    int32_t C = 0;
-    if (h->n) TRY(contact_count(h, h->cur, &C));
-    C = std::min(C, h->p.cap);
-    const ContactSoA& s = h->d.c[h->cur];
-    std::vector<int32_t> ci(C), cj(C);
-    std::vector<uint32_t> fl(C);
-    std::vector<double> f[15];
-    if (C) {
-        CU(cudaMemcpyAsync(ci.data(), s.ci, C * 4, cudaMemcpyDeviceToHost, h->stream));
-        CU(cudaMemcpyAsync(cj.data(), s.cj, C * 4, cudaMemcpyDeviceToHost, h->stream));
-        CU(cudaMemcpyAsync(fl.data(), s.fl, C * 4, cudaMemcpyDeviceToHost, h->stream));
-        for (int q = 0; q < 15; ++q) TRY(get_dev(f[q], s.f[q], (size_t)C, h->stream));
-        CU(cudaStreamSynchronize(h->stream));
-    }
-    std::vector<int32_t> act;  // active contacts, sorted by (i, j)
-    act.reserve(C);
-    for (int32_t c = 0; c < C; ++c)
-        if (fl[c] & kActive) act.push_back(c);
-    std::sort(act.begin(), act.end(), [&](int32_t a, int32_t b) {
-        return ci[a] != ci[b] ? ci[a] < ci[b] : cj[a] < cj[b];
-    });
-    const int64_t na = (int64_t)act.size();
-    *n_out = na;
-    if (!out) return DEM_OK;
-    if (na > cap) return DEM_ERR_CAPACITY;
-    for (int64_t t = 0; t < na; ++t) {
-        const int32_t c = act[t];
-        if (out->i) out->i[t] = ci[c];
-        if (out->j) out->j[t] = cj[c];
-        if (out->bonded) out->bonded[t] = (fl[c] & kBonded) ? 1 : 0;
-        for (int q = 0; q < 3; ++q) {
-            if (out->point) out->point[3 * t + q] = f[CK + q][c];
-            if (out->force) out->force[3 * t + q] = f[CF + q][c];
-            if (out->torque_i) out->torque_i[3 * t + q] = f[CTI + q][c];
-            if (out->torque_j) out->torque_j[3 * t + q] = f[CTJ + q][c];
-            if (out->shear) out->shear[3 * t + q] = f[CS + q][c];
-        }
-    }
-    return DEM_OK;
+    return dem_scene_get_contacts(h, 0, out, cap, n_out);
 }
 
 int dem_set_contacts(DemHandle* h, const DemContacts* in, int64_t nc) {
-    if (!h || !in || nc < 0 || (nc > 0 && (!in->i || !in->j))) return DEM_ERR_INVALID;
+    if (!h || h->multi || !in || nc < 0 || (nc > 0 && (!in->i || !in->j))) return DEM_ERR_INVALID;
     if (nc > h->p.cap) return DEM_ERR_CAPACITY;
-    const int n = h->n;
+    const int n = h->n_cap;
     std::vector<int64_t> order(nc);
     std::iota(order.begin(), order.end(), 0);
     for (int64_t t = 0; t < nc; ++t)
@@ -730,10 +1129,10 @@ int dem_set_contacts(DemHandle* h, const DemContacts* in, int64_t nc) {
             CU(cudaMemcpyAsync(s.f[q], f[q].data(), nc * 8, cudaMemcpyHostToDevice, h->stream));
     }
     if (n) {
-        CU(cudaMemcpyAsync(h->d.row_start[h->cur], rs.data(), n * 4, cudaMemcpyHostToDevice,
-                           h->stream));
-        CU(cudaMemcpyAsync(h->d.row_len[h->cur], rl.data(), n * 4, cudaMemcpyHostToDevice,
-                           h->stream));
+        CU(cudaMemcpyAsync(h->d.row_start[h->cur], rs.data(), (size_t)n * 4,
+                           cudaMemcpyHostToDevice, h->stream));
+        CU(cudaMemcpyAsync(h->d.row_len[h->cur], rl.data(), (size_t)n * 4,
+                           cudaMemcpyHostToDevice, h->stream));
     }
     const unsigned int alloc[2] = {h->cur == 0 ? (unsigned)nc : 0u, h->cur == 1 ? (unsigned)nc : 0u};
     CU(cudaMemcpyAsync(h->d.ctr->row_alloc, alloc, sizeof(alloc), cudaMemcpyHostToDevice,
@@ -742,49 +1141,25 @@ int dem_set_contacts(DemHandle* h, const DemContacts* in, int64_t nc) {
     return DEM_OK;
 }
 
-int dem_get_stats(DemHandle* h, DemStats* out) {
-    if (!h || !out) return DEM_ERR_INVALID;
-    DevCounters c;
-    TRY(read_counters(h, &c));
-    int32_t C = 0;
-    if (h->n) TRY(contact_count(h, h->cur, &C));
-    C = std::min(C, h->p.cap);
-    std::vector<uint32_t> fl(C);
-    if (C) CU(cudaMemcpy(fl.data(), h->d.c[h->cur].fl, C * 4, cudaMemcpyDeviceToHost));
-    int64_t act = 0, bnd = 0;
-    for (uint32_t f : fl) {
-        act += (f & kActive) ? 1 : 0;
-        bnd += ((f & kActive) && (f & kBonded)) ? 1 : 0;
-    }
-    std::memset(out, 0, sizeof(*out));
-    out->n_particles = h->n;
-    out->steps_done = h->steps;
-    out->contacts = act;
-    out->bonded = bnd;
-    out->bonds_broken = (int64_t)c.broken;
-    out->contacts_ended = (int64_t)c.ended;
-    out->contacts_created = (int64_t)c.created;
-    out->warn_gap = (int64_t)c.warn_gap;
-    out->warn_damping = (int64_t)c.warn_damp;
-    out->error = (c.error & kErrCapacity) ? DEM_ERR_CAPACITY
-                 : (c.error & kErrTimeout) ? DEM_ERR_TIMEOUT
-                 : (c.error & kErrRange)   ? DEM_ERR_RANGE
-                                           : DEM_OK;
-    out->precision = h->p.precision;
-    return DEM_OK;
+int dem_scene_get_stats(DemHandle* h, int32_t s, DemStats* out) {
+    const SceneHost* S = scene_at(h, s);
+    if (!S || !out) return DEM_ERR_INVALID;
+    return stats_of(h, s, *S, out);
 }
+
+int dem_get_stats(DemHandle* h, DemStats* out) { return dem_scene_get_stats(h, 0, out); }
 
 int dem_debug_broadphase(DemHandle* h, int32_t* cell, uint32_t* morton, uint32_t* bucket,
                          uint32_t* bucket_count, uint32_t* sorted, int32_t* cp, int64_t cp_cap,
                          int64_t* cp_n) {
-    if (!h || !cp_n) return DEM_ERR_INVALID;
-    const int n = h->n;
+    if (!h || !cp_n || h->multi) return DEM_ERR_INVALID;
+    const int n = h->n_cap;
     *cp_n = 0;
     if (n == 0) {
-        if (bucket_count) std::memset(bucket_count, 0, sizeof(uint32_t) * h->p.H);
+        if (bucket_count) std::memset(bucket_count, 0, sizeof(uint32_t) * h->t_cap);
         return DEM_OK;
     }
-    launch_broadphase(h->d, h->p, h->ntiles_cells, h->stream);
+    launch_broadphase(h->d, h->p, h->cur, false, h->ntiles_cells, h->stream);
     uint32_t* dmorton = nullptr;
     int32_t *dcnt = nullptr, *doff = nullptr, *dcp = nullptr;
     auto cleanup = [&]() {
@@ -793,8 +1168,9 @@ int dem_debug_broadphase(DemHandle* h, int32_t* cell, uint32_t* morton, uint32_t
         cudaFree(doff);
         cudaFree(dcp);
     };
-    if (cudaMalloc(&dmorton, n * 4) != cudaSuccess || cudaMalloc(&dcnt, n * 4) != cudaSuccess ||
-        cudaMalloc(&doff, (n + 1) * 4) != cudaSuccess) {
+    if (cudaMalloc(&dmorton, (size_t)n * 4) != cudaSuccess ||
+        cudaMalloc(&dcnt, (size_t)n * 4) != cudaSuccess ||
+        cudaMalloc(&doff, ((size_t)n + 1) * 4) != cudaSuccess) {
         cleanup();
         return DEM_ERR_CUDA;
     }
@@ -820,12 +1196,13 @@ int dem_debug_broadphase(DemHandle* h, int32_t* cell, uint32_t* morton, uint32_t
     }
     std::vector<int4> ci(n);
     std::vector<uint32_t> bk(n), start;
-    cudaMemcpyAsync(ci.data(), h->d.cellinfo, n * sizeof(int4), cudaMemcpyDeviceToHost, h->stream);
-    cudaMemcpyAsync(bk.data(), h->d.bucket, n * 4, cudaMemcpyDeviceToHost, h->stream);
-    if (morton) cudaMemcpyAsync(morton, dmorton, n * 4, cudaMemcpyDeviceToHost, h->stream);
-    if (sorted) cudaMemcpyAsync(sorted, h->d.sorted, n * 4, cudaMemcpyDeviceToHost, h->stream);
+    cudaMemcpyAsync(ci.data(), h->d.cellinfo, (size_t)n * sizeof(int4), cudaMemcpyDeviceToHost,
+                    h->stream);
+    cudaMemcpyAsync(bk.data(), h->d.bucket, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream);
+    if (morton) cudaMemcpyAsync(morton, dmorton, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream);
+    if (sorted) cudaMemcpyAsync(sorted, h->d.sorted, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream);
     if (bucket_count) {
-        start.resize((size_t)h->p.H + 1);
+        start.resize((size_t)h->t_cap + 1);
         cudaMemcpyAsync(start.data(), h->d.cell_start, start.size() * 4, cudaMemcpyDeviceToHost,
                         h->stream);
     }
@@ -847,7 +1224,7 @@ int dem_debug_broadphase(DemHandle* h, int32_t* cell, uint32_t* morton, uint32_t
     if (cudaMemcpy(&ctr, h->d.ctr, sizeof(ctr), cudaMemcpyDeviceToHost) != cudaSuccess)
         return DEM_ERR_CUDA;
     if (bucket_count)
-        for (uint32_t b = 0; b < h->p.H; ++b)
+        for (uint32_t b = 0; b < h->t_cap; ++b)
             bucket_count[b] = b < ctr.cell_limit ? start[b + 1] - start[b] : 0u;
     int err = device_error(h);
     return err != DEM_OK ? err : rc;

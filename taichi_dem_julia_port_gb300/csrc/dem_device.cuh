@@ -77,22 +77,29 @@ __device__ __forceinline__ uint32_t morton1(int x, int y, int z) {
             (spread10((uint32_t)(z - 1)) << 2)) +
            1u;
 }
-// 0-based bucket: hashcode(ijk) - 1 = cartesian3morton(ijk) % H (src/utils.jl:2)
-__device__ __forceinline__ uint32_t bucket_of(int x, int y, int z, const DemParams& p) {
-    uint32_t m = morton1(x, y, z);
-    return p.H_pow2_mask ? (m & p.H_pow2_mask) : (m % p.H);
+// Search bucket of a cell: the scene's table range [t0, t0 + H) indexed by
+// cartesian3morton % H.  For a single-scene handle t0 = 0 and H is the
+// reference's table size, so this is hashcode(ijk) - 1 (src/utils.jl:2).
+__device__ __forceinline__ uint32_t bucket_of(int x, int y, int z, const SceneParams& S) {
+    const uint32_t m = morton1(x, y, z);
+    return S.t0 + (S.Hmask ? (m & S.Hmask) : (m % S.H));
+}
+// The reference's 0-based bucket, hashcode(ijk) - 1 with its own table size.
+__device__ __forceinline__ uint32_t ref_bucket_of(int x, int y, int z, const SceneParams& S) {
+    const uint32_t m = morton1(x, y, z);
+    return S.Href_mask ? (m & S.Href_mask) : (m % S.Href);
 }
 // The 8 octant buckets of `neighbors` (src/utils.jl:4-16), in its order.
-__device__ __forceinline__ void buckets8(int4 ci, const DemParams& p, uint32_t B[8]) {
+__device__ __forceinline__ void buckets8(int4 ci, const SceneParams& S, uint32_t B[8]) {
     const int dx = (ci.w & 1) ? 1 : -1, dy = (ci.w & 2) ? 1 : -1, dz = (ci.w & 4) ? 1 : -1;
-    B[0] = bucket_of(ci.x, ci.y, ci.z, p);
-    B[1] = bucket_of(ci.x + dx, ci.y, ci.z, p);
-    B[2] = bucket_of(ci.x, ci.y + dy, ci.z, p);
-    B[3] = bucket_of(ci.x, ci.y, ci.z + dz, p);
-    B[4] = bucket_of(ci.x + dx, ci.y + dy, ci.z, p);
-    B[5] = bucket_of(ci.x + dx, ci.y, ci.z + dz, p);
-    B[6] = bucket_of(ci.x, ci.y + dy, ci.z + dz, p);
-    B[7] = bucket_of(ci.x + dx, ci.y + dy, ci.z + dz, p);
+    B[0] = bucket_of(ci.x, ci.y, ci.z, S);
+    B[1] = bucket_of(ci.x + dx, ci.y, ci.z, S);
+    B[2] = bucket_of(ci.x, ci.y + dy, ci.z, S);
+    B[3] = bucket_of(ci.x, ci.y, ci.z + dz, S);
+    B[4] = bucket_of(ci.x + dx, ci.y + dy, ci.z, S);
+    B[5] = bucket_of(ci.x + dx, ci.y, ci.z + dz, S);
+    B[6] = bucket_of(ci.x, ci.y + dy, ci.z + dz, S);
+    B[7] = bucket_of(ci.x + dx, ci.y + dy, ci.z + dz, S);
 }
 
 // ---- small vector helpers (contractible; used by the force models) ----------

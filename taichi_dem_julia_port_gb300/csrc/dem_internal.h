@@ -1,11 +1,16 @@
 // dem_internal.h — device data layout and kernel launchers of libdem_sm100a.so.
 //
-// Layout in HBM (one scene, n particles, contact capacity cap = n·max_coord):
-//  * particles: structure of arrays in the caller's particle order, FP64;
+// Layout in HBM.  A handle is an arena of particle slots holding one or more
+// independent scenes (a single scene for dem_create; many for the batched and
+// served modes).  Each scene owns a contiguous range of particle slots and a
+// contiguous range of bucket-table entries; its constants live in a
+// SceneParams record.
+//  * particles: structure of arrays over all slots, FP64;
 //  * broad phase: per-particle cell record (int4: ijk + octant bits), bucket
-//    id, a dense bucket table of H counts / H+1 starts (the reference's
-//    hash_table), and particle copies in bucket-sorted order (double4 x,y,z,r
-//    and a float4 copy relative to domain_min for the distance pre-filter);
+//    id, a bucket table of counts / starts (the reference's hash_table, one
+//    range per scene), and particle copies in bucket-sorted order (double4
+//    x,y,z,r and a float4 copy relative to the scene's domain_min for the
+//    distance pre-filter);
 //  * contacts: two buffers (the reference's contacts / contacts_temp rolling
 //    pair), each a structure of arrays of rows — row i holds the contacts
 //    (i, j) with j > i, sorted by j, at [row_start[i], row_start[i]+row_len[i]);
@@ -28,6 +33,14 @@ constexpr int kErrCapacity = 1;
 constexpr int kErrTimeout = 2;
 constexpr int kErrRange = 4;
 
+// scene modes (SceneParams::mode)
+constexpr int kModeFree = 0;    // slot range not in use: particles ignored, no contacts
+constexpr int kModeFrozen = 1;  // state kept (contacts carried), no stepping
+constexpr int kModeStep = 2;    // `simulate!`
+constexpr int kModeInit = 3;    // `initialize!` (bonds from r₀), no integration
+
+constexpr uint32_t kNoBucket = 0xffffffffu;
+
 struct ContactSoA {
     int32_t* ci;
     int32_t* cj;
@@ -36,13 +49,42 @@ struct ContactSoA {
 };
 enum ContactField { CK = 0, CF = 3, CTI = 6, CTJ = 9, CS = 12 };
 
+// Constants of one scene (host-derived).  For a single-scene handle the record
+// travels in the kernel parameters; for an arena it is an array in HBM.
+struct SceneParams {
+    int mode;
+    int p0, n;                // particle slots [p0, p0 + n)
+    uint32_t t0, H, Hmask;    // search buckets [t0, t0 + H); Hmask = H-1 if H is a power of 2
+    uint32_t Href, Href_mask; // the reference's hash-table size (src/executor.jl:266-267)
+    int has_wall;
+    int same_grid;            // search cells are the reference's cells (cell == cell_ref)
+    double dmin[3];
+    double cell, inv_cell;           // search cell size
+    double cell_ref, inv_cell_ref;   // the reference's cell size 4 rₘₐₓ (src/executor.jl:265)
+    double dt, tol;
+    double grav[3];
+    double damping;
+    // particle-particle Hertz-Mindlin constants (surface [1,1], materials 1,1)
+    // cgn = -2β·sqrt(5/3·Y*), cgt = -2β·sqrt(20/3·G*): γₙ = cgn·sqrt(m*·sqrt(R*Δn))
+    double pp_mu, pp_Ys, pp_Gs, pp_cgn, pp_cgt;
+    // EBPM bond constants (surface [1,1])
+    double b_inv1pnu, b_sc, b_st, b_ss;
+    // wall (wall_normal, wall_distance) and particle-wall constants
+    double wn[3], wd;
+    double wR[9], wRinv[9];  // contact frame of the wall and its inverse
+    double pw_mu, pw_Ys, pw_Gs, pw_cgn, pw_cgt;
+};
+
+struct SceneCounters {
+    unsigned long long broken, ended, created, warn_gap, warn_damp;
+};
+
 struct DevCounters {
     int error;
     unsigned int bmax;        // largest bucket id of this step (k_hash), reset by k_canon
     unsigned int cell_limit;  // buckets [0, cell_limit) have valid starts this step
     unsigned int pad;
-    unsigned int row_alloc[2];  // contacts allocated in each contact buffer
-    unsigned long long broken, ended, created, warn_gap, warn_damp;
+    unsigned int row_alloc[2];      // contacts allocated in each contact buffer
     unsigned long long tickets[2];  // tile tickets of the scan sites (never reset)
 };
 
@@ -50,33 +92,37 @@ struct DevCounters {
 constexpr int kScanCells = 0;
 constexpr int kScanDebug = 1;
 
-// Device pointers of one scene (passed by value to every kernel).
+// Device pointers of one arena (passed by value to every kernel).
 struct DemDev {
-    // particles, caller order
+    // particles
     double *px, *py, *pz, *vx, *vy, *vz, *wx, *wy, *wz;
     double *qw, *qx, *qy, *qz;
     double *m, *inv_m, *r, *r0, *inv_inertia;
-    double *b_invA, *b_rbI;  // bond section constants for rb = ρ·r (1/A, rb/I)
+    double *b_invA, *b_rbI;        // bond section constants for rb = ρ·r (1/A, rb/I)
     double *b_EA, *b_EI, *b_phic;  // E·A, E·I and 20/3·(1+ν)·rb² for rb = ρ·r
     double *fx, *fy, *fz, *tx, *ty, *tz;  // totals of the last step
     double *wsx, *wsy, *wsz;              // wall shear history (one wall)
+    int32_t* scene_of;                    // arena: scene of each slot (-1 free); null otherwise
+    SceneParams* sp;                      // arena: scene records; null otherwise
+    SceneCounters* sctr;                  // per-scene event counters
     // broad phase
-    int4* cellinfo;
-    uint32_t* bucket;      // 0-based bucket of each particle
-    uint32_t* cell_count;  // H, zero between steps
-    uint32_t* cell_start;  // H + 1
-    uint32_t* unsorted;    // n, bucket-grouped, arbitrary order inside a bucket
-    uint32_t* sorted;      // n, bucket-grouped, ascending index inside a bucket
-    double4_32a* spos;        // n, (x, y, z, r) in sorted order
-    float4* spos32;        // n, (x-ox, y-oy, z-oz, r) in FP32, sorted order
+    int4* cellinfo;        // search cell ijk + octant bits
+    int4* refcell;         // arena: the reference's cell ijk + octant (when grids differ)
+    uint32_t* bucket;      // bucket of each particle (kNoBucket when not hashed)
+    uint32_t* cell_count;  // table entries, zero between steps
+    uint32_t* cell_start;  // table entries + 1
+    uint32_t* unsorted;    // bucket-grouped, arbitrary order inside a bucket
+    uint32_t* sorted;      // bucket-grouped, ascending index inside a bucket
+    double4_32a* spos;     // (x, y, z, r) in sorted order
+    float4* spos32;        // (x-ox, y-oy, z-oz, r) in FP32, sorted order
     // contacts
     ContactSoA c[2];
-    int32_t* row_start[2];  // n, first slot of each particle's row
-    int32_t* row_len[2];    // n, entries in the row
-    int32_t* nnew;          // n
+    int32_t* row_start[2];  // first slot of each particle's row
+    int32_t* row_len[2];    // entries in the row
+    int32_t* nnew;
     int32_t* stash;       // n * kstash new partners of this step
     uint8_t* keep;        // cap, survival flags of the current buffer
-    int32_t* in_cnt;      // n, zero between steps
+    int32_t* in_cnt;      // zero between steps
     int2* in_list;        // n * kin: (contact slot, owner i) of contacts where the particle is j
     double* contrib;      // 9 * cap, [field][contact]
     // scan scratch: tile states of each scan site
@@ -84,44 +130,32 @@ struct DemDev {
     DevCounters* ctr;
 };
 
-// Scene constants (host-derived, passed by value).
+// Arena-wide constants (passed by value).
 struct DemParams {
-    int n;
+    int n;          // particle slots
     int cap;        // contact capacity
     int kstash;     // new partners per particle per step
     int kin;        // incoming contacts per particle
-    uint32_t H;     // hash table size
-    uint32_t H_pow2_mask;  // H-1 when H is a power of two, else 0
-    int has_wall;
+    uint32_t T;     // bucket-table entries
     int precision;  // 0 = FP64, 1 = FP32 force
-    double dmin[3];
-    double cell, inv_cell;
-    double dt, tol;
-    double grav[3];
-    double damping;
-    // particle-particle Hertz-Mindlin constants (surface [1,1], materials 1,1)
-    // cgn = -2β·sqrt(5/3·Y*), cgt = -2β·sqrt(20/3·G*): γₙ = cgn·sqrt(m*·sqrt(R*Δn))
-    double pp_mu, pp_beta, pp_Ys, pp_Gs, pp_cgn, pp_cgt;
-    // EBPM bond constants (surface [1,1])
-    double b_rho, b_E, b_nu, b_inv1pnu, b_sc, b_st, b_ss;
-    // wall (wall_normal, wall_distance) and particle-wall constants
-    double wn[3], wd;
-    double wR[9], wRinv[9];  // contact frame of the wall and its inverse
-    double pw_mu, pw_beta, pw_Ys, pw_Gs, pw_cgn, pw_cgt;
+    SceneParams s0; // the scene of a single-scene handle
 };
 
 // ---- launchers (dem_kernels.cu) --------------------------------------------
 // All launches go to `s`.  `cur` selects the contact buffer that holds the
-// state at the start of the step; the step writes buffer cur^1.
-void launch_broadphase(const DemDev& d, const DemParams& p, int n_scan_tiles_cells,
-                       cudaStream_t s);
-void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, cudaStream_t s);
-void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, int grid,
-                    cudaStream_t s);
-void launch_force(const DemDev& d, const DemParams& p, int nxt, int grid, cudaStream_t s);
-void launch_integrate(const DemDev& d, const DemParams& p, int cur, cudaStream_t s);
+// state at the start of the step; the step writes buffer cur^1.  `multi`
+// selects the arena kernels (per-slot scene records) over the single-scene ones.
+void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi,
+                       int n_scan_tiles_cells, cudaStream_t s);
+void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+                   cudaStream_t s);
+void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+                    int grid, cudaStream_t s);
+void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, int grid,
+                  cudaStream_t s);
+void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi, cudaStream_t s);
 
-// debug: cp_list materialisation on the current bucket arrays
+// debug: cp_list materialisation on the current bucket arrays (single scene)
 void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cudaStream_t s);
 void launch_cplist_fill(const DemDev& d, const DemParams& p, const int32_t* off, int32_t* cp,
                         cudaStream_t s);

@@ -31,6 +31,22 @@ constexpr unsigned long long kSpinLimit = 1ull << 24;
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
 
+// Scene of a particle slot and its record: the kernel-parameter record for a
+// single-scene handle, the HBM array for an arena (MULTI).
+template <bool MULTI>
+__device__ __forceinline__ int slot_scene(const DemDev& d, int i) {
+    return MULTI ? d.scene_of[i] : 0;
+}
+template <bool MULTI>
+__device__ __forceinline__ const SceneParams& scene_rec(const DemDev& d, const DemParams& p, int s) {
+    if (MULTI) return d.sp[s];
+    return p.s0;
+}
+// particles placed in the bucket-sorted arrays this step
+__device__ __forceinline__ int sorted_count(const DemDev& d) {
+    return (int)d.cell_start[d.ctr->cell_limit];
+}
+
 // ---------------------------------------------------------------------------
 // Exclusive scan, single pass with decoupled look-back.  Every CTA draws a
 // ticket from its scan site's counter; a launch draws exactly `ntiles`
@@ -148,34 +164,52 @@ __global__ void __launch_bounds__(kScanBlock)
 // integer lies within 2^-49·|q| of q, both have the same ceiling.  Otherwise
 // (rare: q must sit within ~10^-15 relative of an integer) the quotient is
 // computed by the correctly rounded division.
-__device__ __forceinline__ int32_t cell_index(double num, const DemParams& p) {
-    const double q = num * p.inv_cell;
+__device__ __forceinline__ int32_t cell_index(double num, double cell, double inv_cell) {
+    const double q = num * inv_cell;
     const double d = fabs(q) * 0x1p-49;
     const double lo = ceil(q - d), hi = ceil(q + d);
     if (lo == hi && lo > -2147483648.0 && lo < 2147483647.0) return (int32_t)lo;
-    return ceil_i32(__ddiv_rn(num, p.cell));
+    return ceil_i32(__ddiv_rn(num, cell));
+}
+// cell ijk (1-based) and octant bits of a position for a given cell size
+// (`cell` and the center comparison of `neighbors`, src/utils.jl:1-16)
+__device__ __forceinline__ int4 cell_of(const double pos[3], const double dmin[3], double cell,
+                                        double inv_cell) {
+    int ijk[3];
+    int oct = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        ijk[c] = cell_index(__dsub_rn(pos[c], dmin[c]), cell, inv_cell);
+        const double ctr = __dadd_rn(dmin[c], __dmul_rn(__dsub_rn((double)ijk[c], 0.5), cell));
+        if (pos[c] > ctr) oct |= 1 << c;
+    }
+    return make_int4(ijk[0], ijk[1], ijk[2], oct);
 }
 
 // `cell`, `hashcode`, `center`, `neighbors` (src/utils.jl:1-16) and
 // `count_particles!` (src/kernels.jl:7-13).
-__global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p) {
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool act = i < p.n;
+    bool act = i < p.n;
     uint32_t b = 0;
     if (act) {
-        const double pos[3] = {d.px[i], d.py[i], d.pz[i]};
-        int ijk[3];
-        int oct = 0;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            ijk[c] = cell_index(__dsub_rn(pos[c], p.dmin[c]), p);
-            const double ctr =
-                __dadd_rn(p.dmin[c], __dmul_rn(__dsub_rn((double)ijk[c], 0.5), p.cell));
-            if (pos[c] > ctr) oct |= 1 << c;
+        const int sc = slot_scene<MULTI>(d, i);
+        if (MULTI && (sc < 0 || d.sp[sc].mode == kModeFree)) {
+            // free slot: not hashed, and no contact row in the next buffer
+            d.bucket[i] = kNoBucket;
+            d.row_len[cur ^ 1][i] = 0;
+            d.row_start[cur ^ 1][i] = 0;
+            act = false;
+        } else {
+            const SceneParams& S = scene_rec<MULTI>(d, p, sc);
+            const double pos[3] = {d.px[i], d.py[i], d.pz[i]};
+            const int4 ci = cell_of(pos, S.dmin, S.cell, S.inv_cell);
+            b = bucket_of(ci.x, ci.y, ci.z, S);
+            d.cellinfo[i] = ci;
+            d.bucket[i] = b;
+            if (MULTI && !S.same_grid) d.refcell[i] = cell_of(pos, S.dmin, S.cell_ref, S.inv_cell_ref);
         }
-        b = bucket_of(ijk[0], ijk[1], ijk[2], p);
-        d.cellinfo[i] = make_int4(ijk[0], ijk[1], ijk[2], oct);
-        d.bucket[i] = b;
     }
     const unsigned mask = __ballot_sync(0xffffffffu, act);
     if (act) {
@@ -190,10 +224,10 @@ __global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p) {
 // atomic decrements bring every count back to zero.
 __global__ void __launch_bounds__(kThreads) k_scatter(DemDev d, DemParams p) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool act = i < p.n;
+    const uint32_t b = i < p.n ? d.bucket[i] : kNoBucket;
+    const bool act = b != kNoBucket;
     const unsigned mask = __ballot_sync(0xffffffffu, act);
     if (!act) return;
-    const uint32_t b = d.bucket[i];
     const unsigned peers = __match_any_sync(mask, b);
     const int leader = __ffs(peers) - 1;
     uint32_t old = 0;
@@ -206,10 +240,11 @@ __global__ void __launch_bounds__(kThreads) k_scatter(DemDev d, DemParams p) {
 // Canonical order inside a bucket (ascending particle index) and the sorted
 // position copies used by the pair search.  Also clears this step's bucket
 // maximum (all its readers have finished).
+template <bool MULTI>
 __global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0) d.ctr->bmax = 0u;
-    if (k >= p.n) return;
+    if (k >= sorted_count(d)) return;
     const uint32_t i = d.unsorted[k];
     const uint32_t b = d.bucket[i];
     const uint32_t s = d.cell_start[b], e = d.cell_start[b + 1];
@@ -218,9 +253,10 @@ __global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p) {
     const uint32_t pos = s + rank;
     d.sorted[pos] = i;
     const double x = d.px[i], y = d.py[i], z = d.pz[i], r = d.r[i];
+    const SceneParams& S = scene_rec<MULTI>(d, p, slot_scene<MULTI>(d, (int)i));
     d.spos[pos] = make_double4_32a(x, y, z, r);
-    d.spos32[pos] = make_float4((float)(x - p.dmin[0]), (float)(y - p.dmin[1]),
-                                (float)(z - p.dmin[2]), (float)r);
+    d.spos32[pos] = make_float4((float)(x - S.dmin[0]), (float)(y - S.dmin[1]),
+                                (float)(z - S.dmin[2]), (float)r);
 }
 
 // ---------------------------------------------------------------------------
@@ -249,7 +285,7 @@ __device__ __forceinline__ void bucket_range(const DemDev& d, uint32_t b, uint32
     }
 }
 
-template <bool INIT>
+template <bool INIT, bool MULTI>
 __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int cur) {
     __shared__ int s_new[kThreads / kLanes];
     __shared__ int s_row[kThreads / kLanes][kRowCache];
@@ -264,11 +300,15 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
         s_tot[g] = 0;
     }
     __syncwarp();
-    const bool act = k < p.n;
-    int i = 0, nkeep = 0, ended = 0;
+    const bool act = k < sorted_count(d);
+    int i = 0, nkeep = 0, ended = 0, sc = 0;
     if (act) {
         const unsigned gmask = 0xffu << (lane_id() & ~7u);
         i = (int)d.sorted[k];
+        sc = slot_scene<MULTI>(d, i);
+        const SceneParams& S = scene_rec<MULTI>(d, p, sc);
+        const bool init = INIT || (MULTI && S.mode == kModeInit);
+        const bool frozen = MULTI && S.mode == kModeFrozen;
         const double4_32a P = d.spos[k];
         const float4 P32 = d.spos32[k];
         const int4 ci = d.cellinfo[i];
@@ -276,18 +316,27 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
         const int ox = (lane == 1 || lane == 4 || lane == 5 || lane == 7) ? dx : 0;
         const int oy = (lane == 2 || lane == 4 || lane == 6 || lane == 7) ? dy : 0;
         const int oz = (lane == 3 || lane == 5 || lane == 6 || lane == 7) ? dz : 0;
-        const uint32_t myB = bucket_of(ci.x + ox, ci.y + oy, ci.z + oz, p);
-        uint32_t B[8];
+        const uint32_t myB = bucket_of(ci.x + ox, ci.y + oy, ci.z + oz, S);
+        // the reference's buckets decide cp_list membership (equal to the
+        // search buckets for a single-scene handle)
+        uint32_t myR = myB;
+        if (MULTI) {
+            const int4 rc = S.same_grid ? ci : d.refcell[i];
+            const int rx = (rc.w & 1) ? 1 : -1, ry = (rc.w & 2) ? 1 : -1, rz = (rc.w & 4) ? 1 : -1;
+            myR = ref_bucket_of(rc.x + (ox ? rx : 0), rc.y + (oy ? ry : 0), rc.z + (oz ? rz : 0), S);
+        }
+        uint32_t B[8], RB[8];
         bool dup = false;
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             B[u] = __shfl_sync(gmask, myB, u, kLanes);
+            RB[u] = MULTI ? __shfl_sync(gmask, myR, u, kLanes) : B[u];
             dup |= (u < lane) && (B[u] == myB);
         }
         uint32_t s, e;
         bucket_range(d, myB, d.ctr->cell_limit, &s, &e);
-        if (dup) e = s;
-        const double ri = INIT ? d.r0[i] : P.w;
+        if (dup || frozen) e = s;
+        const double ri = init ? d.r0[i] : P.w;
 
         const ContactSoA o = d.c[cur];
         const int e0 = d.row_start[cur][i];
@@ -300,15 +349,21 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
             int keep;
             if (!(fl & kActive)) {
                 keep = 0;
-            } else if (INIT || (fl & kBonded)) {
+            } else if (init || frozen || (fl & kBonded)) {
                 keep = 1;
             } else {
                 const bool valid =
                     touching_rn(P.x, P.y, P.z, d.px[j], d.py[j], d.pz[j], P.w, d.r[j]);
-                const uint32_t bj = d.bucket[j];
+                uint32_t bj;
+                if (MULTI) {
+                    const int4 cj4 = S.same_grid ? d.cellinfo[j] : d.refcell[j];
+                    bj = ref_bucket_of(cj4.x, cj4.y, cj4.z, S);
+                } else {
+                    bj = d.bucket[j];
+                }
                 bool in_cp = false;
 #pragma unroll
-                for (int t = 0; t < 8; ++t) in_cp |= (B[t] == bj);
+                for (int t = 0; t < 8; ++t) in_cp |= (RB[t] == bj);
                 keep = (valid || !in_cp) ? 1 : 0;
                 ended += 1 - keep;
             }
@@ -333,7 +388,7 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
             for (int u = 0; u < kBatch; ++u) {
                 const int j = jj[u];
                 if (j <= i) continue;
-                if (!INIT && !maybe_touching32(P32, qq[u])) continue;
+                if (!init && !maybe_touching32(P32, qq[u])) continue;
                 bool found = false;
                 if (cached) {
                     for (int t = 0; t < e1 - e0 && !found; ++t) found = s_row[g][t] == j;
@@ -343,7 +398,7 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
                 }
                 if (found) continue;
                 const double4_32a Q = d.spos[q0 + u];
-                const double rj = INIT ? d.r0[j] : Q.w;
+                const double rj = init ? d.r0[j] : Q.w;
                 if (!touching_rn(P.x, P.y, P.z, Q.x, Q.y, Q.z, ri, rj)) continue;
                 const int slot = atomicAdd(&s_new[g], 1);
                 if (slot < p.kstash) stash[slot] = j;
@@ -368,8 +423,8 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
             d.nnew[i] = nnew;
             s_new[g] = nnew;
             s_tot[g] = nkeep + nnew;
-            if (ended) atomicAdd(&d.ctr->ended, (unsigned long long)ended);
-            if (!INIT && nnew) atomicAdd(&d.ctr->created, (unsigned long long)nnew);
+            if (ended) atomicAdd(&d.sctr[sc].ended, (unsigned long long)ended);
+            if (!init && nnew) atomicAdd(&d.sctr[sc].created, (unsigned long long)nnew);
         }
     }
     // rows of this block allocated with one atomic (the atomic-compacted
@@ -406,7 +461,7 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
 // the merge, by j, of the surviving entries of row i and the sorted new
 // partners.  One thread per old contact (coalesced copies) and one per
 // particle for its new contacts; each computes its final slot directly.
-template <bool INIT>
+template <bool INIT, bool MULTI>
 __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int cur) {
     const int nxt = cur ^ 1;
     const int cold = min((int)d.ctr->row_alloc[cur], p.cap);
@@ -422,10 +477,15 @@ __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int
 #pragma unroll
             for (int f = 0; f < 15; ++f) v[f] = o.f[f][t];
             if (!kp) continue;
+            // entries outside the owner's current row are left-overs of a
+            // removed scene (arena) and are dropped
+            const int r0 = d.row_start[cur][i];
+            if (t < r0 || t >= r0 + d.row_len[cur][i]) continue;
             const int rl = d.row_len[nxt][i];
-            if (rl == 0) continue;  // row dropped after a capacity overflow
+            if (rl == 0) continue;  // row dropped after a capacity overflow, or a free slot
+            const int mode = MULTI ? d.sp[d.scene_of[i]].mode : (INIT ? kModeInit : kModeStep);
             int pos = d.row_start[nxt][i];
-            for (int q = d.row_start[cur][i]; q < t; ++q) pos += d.keep[q];
+            for (int q = r0; q < t; ++q) pos += d.keep[q];
             const int nn = d.nnew[i];
             const int32_t* st = d.stash + (size_t)i * p.kstash;
             for (int u = 0; u < nn; ++u) pos += st[u] < j ? 1 : 0;
@@ -434,7 +494,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int
             w.fl[pos] = fl;
 #pragma unroll
             for (int f = 0; f < 15; ++f) w.f[f][pos] = v[f];
-            if (!INIT) {
+            if (mode == kModeStep) {
                 const int slot = atomicAdd(&d.in_cnt[j], 1);
                 if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = make_int2(pos, i);
                 else raise_error(d.ctr, kErrCapacity);
@@ -443,6 +503,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int
             const int i = t - cold;
             const int nn = d.nnew[i];
             if (!nn || d.row_len[nxt][i] == 0) continue;
+            const int mode = MULTI ? d.sp[d.scene_of[i]].mode : (INIT ? kModeInit : kModeStep);
             const int e0 = d.row_start[cur][i], e1 = e0 + d.row_len[cur][i];
             const int32_t* st = d.stash + (size_t)i * p.kstash;
             const int base = d.row_start[nxt][i];
@@ -452,10 +513,10 @@ __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int
                 for (int q = e0; q < e1; ++q) pos += (d.keep[q] && o.cj[q] < j) ? 1 : 0;
                 w.ci[pos] = i;
                 w.cj[pos] = j;
-                w.fl[pos] = INIT ? (kActive | kBonded) : kActive;
+                w.fl[pos] = mode == kModeInit ? (kActive | kBonded) : kActive;
 #pragma unroll
                 for (int f = 0; f < 15; ++f) w.f[f][pos] = 0.0;
-                if (!INIT) {
+                if (mode == kModeStep) {
                     const int slot = atomicAdd(&d.in_cnt[j], 1);
                     if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = make_int2(pos, i);
                     else raise_error(d.ctr, kErrCapacity);
@@ -556,7 +617,7 @@ __device__ __forceinline__ Vec3<T> from_d(Vec3<double> v) {
 // A NaN operand makes a comparison false, as in the reference.
 __device__ __forceinline__ bool bond_breaks(const Vec3<double>& F, const Vec3<double>& ti,
                                             const Vec3<double>& tj, double invA, double rbI,
-                                            const DemParams& p) {
+                                            const SceneParams& p) {
     const double ai = ti.y * ti.y + ti.z * ti.z, aj = tj.y * tj.y + tj.z * tj.z;
     const bool nan_a = isnan(ai) || isnan(aj);
     const double amax = fmax(ai, aj), amin = fmin(ai, aj);
@@ -583,17 +644,19 @@ __device__ __forceinline__ bool bond_breaks(const Vec3<double>& F, const Vec3<do
 // 𝛉ₛ = 𝐑(𝛚ᵢ + 𝛚ⱼ)dt and 𝛉_d = 𝐑(𝛚ᵢ - 𝛚ⱼ)dt, the reference's increments
 // k₅𝛉ᵢ + k₆𝛉ⱼ and k₆𝛉ᵢ + k₅𝛉ⱼ are k₊𝛉ₛ ± k₋𝛉_d with k₊ = (k₅+k₆)/2 =
 // 3EI/L/(1+ϕ) and k₋ = (k₅-k₆)/2 = EI/L; dt is folded into the stiffnesses.
-template <typename T>
+template <typename T, bool MULTI>
 __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int nxt) {
     const int C = min((int)d.ctr->row_alloc[nxt], p.cap);
     const ContactSoA w = d.c[nxt];
     const int stride = gridDim.x * blockDim.x;
-    const double dt = p.dt;
     const size_t cap = (size_t)p.cap;
-    unsigned long long nbroken = 0, ngap = 0, ngamma = 0;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += stride) {
         const uint32_t fl = w.fl[c];
         const int i = w.ci[c], j = w.cj[c];
+        const int sc = slot_scene<MULTI>(d, i);
+        if (MULTI && (sc < 0 || d.sp[sc].mode != kModeStep)) continue;
+        const SceneParams& SP = scene_rec<MULTI>(d, p, sc);
+        const double dt = SP.dt;
         const Vec3<double> ki{d.px[i], d.py[i], d.pz[i]}, kj{d.px[j], d.py[j], d.pz[j]};
         const double ri = d.r[i], rj = d.r[j];
         const Vec3<double> vi{d.vx[i], d.vy[i], d.vz[i]}, vj{d.vx[j], d.vy[j], d.vz[j]};
@@ -603,14 +666,14 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
         const double invL = rsqrt(L2);
         const double L = L2 * invL;
         const double ax = dx * invL, ay = dy * invL, az = dz * invL;
-        const Frame R = contact_frame(dx, dy, dz, ax, ay, az, p.tol);
+        const Frame R = contact_frame(dx, dy, dz, ax, ay, az, SP.tol);
         Vec3<T> fig, mi, mj;
         if (fl & kBonded) {
             // EBPM (src/kernels.jl:170-239)
             const Vec3<double> Dd = rot<double>(R, {vi.x - vj.x, vi.y - vj.y, vi.z - vj.z});
             const Vec3<double> Ts = rot<double>(R, {wi.x + wj.x, wi.y + wj.y, wi.z + wj.z});
             const Vec3<double> Td = rot<double>(R, {wi.x - wj.x, wi.y - wj.y, wi.z - wj.z});
-            const Vec3<T> D = from_d<T>(Dd), S = from_d<T>(Ts), Q = from_d<T>(Td);
+            const Vec3<T> D = from_d<T>(Dd), Sv = from_d<T>(Ts), Q = from_d<T>(Td);
             const int small = ri <= rj ? i : j;  // rb = ρ·min(rᵢ, rⱼ)
             const T tinvL = (T)invL, tdt = (T)dt;
             const T phi = (T)d.b_phic[small] * tinvL * tinvL;
@@ -619,11 +682,11 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
             const T k1 = (T)d.b_EA[small] * tinvL * tdt;
             const T k3 = (T)6.0 * EILdt * tinvL * iphi;
             const T k2 = (T)2.0 * k3 * tinvL;
-            const T k4 = EILdt * (T)p.b_inv1pnu;
+            const T k4 = EILdt * (T)SP.b_inv1pnu;
             const T kp = (T)3.0 * EILdt * iphi;
             const T km = EILdt;
-            const T dFx = k1 * D.x, dFy = k2 * D.y + k3 * S.z, dFz = k2 * D.z - k3 * S.y;
-            const T ay_ = -k3 * D.z + kp * S.y, az_ = k3 * D.y + kp * S.z;
+            const T dFx = k1 * D.x, dFy = k2 * D.y + k3 * Sv.z, dFz = k2 * D.z - k3 * Sv.y;
+            const T ay_ = -k3 * D.z + kp * Sv.y, az_ = k3 * D.y + kp * Sv.z;
             const T dtix = k4 * Q.x, dtiy = ay_ + km * Q.y, dtiz = az_ + km * Q.z;
             const T dtjx = -k4 * Q.x, dtjy = ay_ - km * Q.y, dtjz = az_ - km * Q.z;
             Vec3<double> Fi = ld3(w.f, CF, c), ti = ld3(w.f, CTI, c), tj = ld3(w.f, CTJ, c);
@@ -631,9 +694,9 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
             ti = {ti.x + (double)dtix, ti.y + (double)dtiy, ti.z + (double)dtiz};
             tj = {tj.x + (double)dtjx, tj.y + (double)dtjy, tj.z + (double)dtjz};
             // breakage test, FP64 (src/kernels.jl:208-222)
-            if (bond_breaks(Fi, ti, tj, d.b_invA[small], d.b_rbI[small], p)) {
+            if (bond_breaks(Fi, ti, tj, d.b_invA[small], d.b_rbI[small], SP)) {
                 w.fl[c] = 0u;  // contact_active and contact_bonded bits cleared
-                ++nbroken;
+                atomicAdd(&d.sctr[sc].broken, 1ull);
                 fig = {(T)0, (T)0, (T)0};
                 mi = fig;
                 mj = fig;
@@ -650,7 +713,7 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
         } else {
             // Hertz-Mindlin (src/kernels.jl:240-313)
             const double gap = L - ri - rj;
-            if (gap > 0) ++ngap;
+            if (gap > 0) atomicAdd(&d.sctr[sc].warn_gap, 1ull);
             const double ext = ri - fabs(gap);
             st3(w.f, CK, c, {ki.x + ax * ext, ki.y + ay * ext, ki.z + az * ext});
             const Vec3<T> kri{(T)(ax * ext), (T)(ay * ext), (T)(az * ext)};
@@ -665,19 +728,19 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
             const T ms = tmi * tmj / (tmi + tmj);
             const T tgap = (T)gap;
             const T sq = sqrt(Rs * (T)fabs(gap));
-            const T kn = (T)(4.0 / 3.0 * p.pp_Ys) * sq;
-            const T kt = (T)(8.0 * p.pp_Gs) * sq;
+            const T kn = (T)(4.0 / 3.0 * SP.pp_Ys) * sq;
+            const T kt = (T)(8.0 * SP.pp_Gs) * sq;
             const T root = sqrt(ms * sq);
-            const T gn = (T)p.pp_cgn * root;
-            const T gt = (T)p.pp_cgt * root;
-            if (gn < (T)0) ++ngamma;
-            if (gt < (T)0) ++ngamma;
+            const T gn = (T)SP.pp_cgn * root;
+            const T gt = (T)SP.pp_cgt * root;
+            if (gn < (T)0 || gt < (T)0)
+                atomicAdd(&d.sctr[sc].warn_damp, (unsigned long long)((gn < (T)0) + (gt < (T)0)));
             Vec3<double> s = ld3(w.f, CS, c);
             s = {s.x + (double)vc.x * 0.0, s.y + (double)vc.y * dt, s.z + (double)vc.z * dt};
             const T F1 = -kn * tgap - gn * vc.x;
             const Vec3<T> Ft{-kt * (T)s.x, -kt * (T)s.y, -kt * (T)s.z};
             const T nFt = sqrt(Ft.x * Ft.x + Ft.y * Ft.y + Ft.z * Ft.z);
-            const T muF1 = (T)p.pp_mu * F1;
+            const T muF1 = (T)SP.pp_mu * F1;
             T F2, F3;
             if (nFt >= muF1) {
                 const T ratio = muF1 / nFt;
@@ -704,9 +767,6 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
         d.contrib[7 * cap + c] = (double)mj.y;
         d.contrib[8 * cap + c] = (double)mj.z;
     }
-    if (nbroken) atomicAdd(&d.ctr->broken, nbroken);
-    if (ngap) atomicAdd(&d.ctr->warn_gap, ngap);
-    if (ngamma) atomicAdd(&d.ctr->warn_damp, ngamma);
 }
 
 // ---------------------------------------------------------------------------
@@ -766,11 +826,18 @@ __device__ __forceinline__ void add_incoming(const DemDev& d, size_t cap, const 
     }
 }
 
+template <bool MULTI>
 __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nxt = cur ^ 1;
     if (i == 0) d.ctr->row_alloc[cur] = 0u;  // the free buffer is next step's target
     if (i >= p.n) return;
+    const int sc = slot_scene<MULTI>(d, i);
+    if (MULTI && (sc < 0 || d.sp[sc].mode != kModeStep)) {
+        d.in_cnt[i] = 0;
+        return;
+    }
+    const SceneParams& S = scene_rec<MULTI>(d, p, sc);
     const size_t cap = (size_t)p.cap;
     double F[3] = {0.0, 0.0, 0.0}, M[3] = {0.0, 0.0, 0.0};
     const int c0 = d.row_start[nxt][i];
@@ -834,38 +901,38 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     const double vx = d.vx[i], vy = d.vy[i], vz = d.vz[i];
     const double wx = d.wx[i], wy = d.wy[i], wz = d.wz[i];
     const double r = d.r[i], m = d.m[i];
-    const double dt = p.dt;
+    const double dt = S.dt;
     // resolve_wall!, one wall
-    if (p.has_wall) {
-        const double dotkn = __dadd_rn(__dadd_rn(__dmul_rn(x, p.wn[0]), __dmul_rn(y, p.wn[1])),
-                                       __dmul_rn(z, p.wn[2]));
-        const double L = __dsub_rn(dotkn, p.wd);
+    if (S.has_wall) {
+        const double dotkn = __dadd_rn(__dadd_rn(__dmul_rn(x, S.wn[0]), __dmul_rn(y, S.wn[1])),
+                                       __dmul_rn(z, S.wn[2]));
+        const double L = __dsub_rn(dotkn, S.wd);
         if (fabs(L) < r) {
             const double gap = fabs(L) - r;
             const double dn = fabs(gap);
-            const double sc = (fabs(L) + dn / 2.0) / fabs(L);
-            const double kix = -L * p.wn[0] * sc, kiy = -L * p.wn[1] * sc, kiz = -L * p.wn[2] * sc;
+            const double lsc = (fabs(L) + dn / 2.0) / fabs(L);
+            const double kix = -L * S.wn[0] * lsc, kiy = -L * S.wn[1] * lsc, kiz = -L * S.wn[2] * lsc;
             const double vcix = wy * kiz - wz * kiy + vx, vciy = wz * kix - wx * kiz + vy,
                          vciz = wx * kiy - wy * kix + vz;
-            const double* Rw = p.wR;
+            const double* Rw = S.wR;
             const double vcx = -(Rw[0] * vcix + Rw[1] * vciy + Rw[2] * vciz);
             const double vcy = -(Rw[3] * vcix + Rw[4] * vciy + Rw[5] * vciz);
             const double vcz = -(Rw[6] * vcix + Rw[7] * vciy + Rw[8] * vciz);
             const double sq = sqrt(r * dn);
-            const double kn = 4.0 / 3.0 * p.pw_Ys * sq;
-            const double kt = 8.0 * p.pw_Gs * sq;
+            const double kn = 4.0 / 3.0 * S.pw_Ys * sq;
+            const double kt = 8.0 * S.pw_Gs * sq;
             const double root = sqrt(m * sq);
-            const double gn = p.pw_cgn * root;
-            const double gt = p.pw_cgt * root;
-            if (gn < 0) atomicAdd(&d.ctr->warn_damp, 1ull);
-            if (gt < 0) atomicAdd(&d.ctr->warn_damp, 1ull);
+            const double gn = S.pw_cgn * root;
+            const double gt = S.pw_cgt * root;
+            if (gn < 0) atomicAdd(&d.sctr[sc].warn_damp, 1ull);
+            if (gt < 0) atomicAdd(&d.sctr[sc].warn_damp, 1ull);
             double sx = d.wsx[i] + vcx * 0.0, sy = d.wsy[i] + vcy * dt, sz = d.wsz[i] + vcz * dt;
             const double F1 = -kn * gap - gn * vcx;
             const double Ftx = -kt * sx, Fty = -kt * sy, Ftz = -kt * sz;
             const double nFt = sqrt(Ftx * Ftx + Fty * Fty + Ftz * Ftz);
             double F2, F3;
-            if (nFt >= p.pw_mu * F1) {
-                const double ratio = p.pw_mu * F1 / nFt;
+            if (nFt >= S.pw_mu * F1) {
+                const double ratio = S.pw_mu * F1 / nFt;
                 F2 = ratio * Fty;
                 F3 = ratio * Ftz;
                 sy = F2 / kt;
@@ -874,7 +941,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
                 F2 = Fty - gt * vcy;
                 F3 = Ftz - gt * vcz;
             }
-            const double* Ri = p.wRinv;
+            const double* Ri = S.wRinv;
             const double gx = -(Ri[0] * F1 + Ri[1] * F2 + Ri[2] * F3);
             const double gy = -(Ri[3] * F1 + Ri[4] * F2 + Ri[5] * F3);
             const double gz = -(Ri[6] * F1 + Ri[7] * F2 + Ri[8] * F3);
@@ -894,16 +961,16 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
         }
     }
     // apply_body_force!
-    F[0] += p.grav[0] * m;
-    F[1] += p.grav[1] * m;
-    F[2] += p.grav[2] * m;
-    if (p.damping != 0.0) {
+    F[0] += S.grav[0] * m;
+    F[1] += S.grav[1] * m;
+    F[2] += S.grav[2] * m;
+    if (S.damping != 0.0) {
         const double v3[3] = {vx, vy, vz}, w3[3] = {wx, wy, wz};
         double dF[3], dM[3];
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            dF[q] = -p.damping * fabs(F[q]) * jl_sign(v3[q]);
-            dM[q] = -p.damping * fabs(M[q]) * jl_sign(w3[q]);
+            dF[q] = -S.damping * fabs(F[q]) * jl_sign(v3[q]);
+            dM[q] = -S.damping * fabs(M[q]) * jl_sign(w3[q]);
         }
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
@@ -956,7 +1023,7 @@ __global__ void k_cp_count(DemDev d, DemParams p, int32_t* cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     uint32_t B[8];
-    buckets8(d.cellinfo[i], p, B);
+    buckets8(d.cellinfo[i], p.s0, B);
     const uint32_t lim = d.ctr->cell_limit;
     int c = 0;
     for (int t = 0; t < 8; ++t) {
@@ -971,7 +1038,7 @@ __global__ void k_cp_fill(DemDev d, DemParams p, const int32_t* off, int32_t* cp
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     uint32_t B[8];
-    buckets8(d.cellinfo[i], p, B);
+    buckets8(d.cellinfo[i], p.s0, B);
     const uint32_t lim = d.ctr->cell_limit;
     int o = off[i];
     for (int t = 0; t < 8; ++t) {
@@ -1005,41 +1072,54 @@ void launch_scan_i32(const int32_t* in, int32_t* out, int64_t n, const DemDev& d
                                                           &d.ctr->tickets[site], d.ctr);
 }
 
-void launch_broadphase(const DemDev& d, const DemParams& p, int ntiles_cells, cudaStream_t s) {
+void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi, int ntiles_cells,
+                       cudaStream_t s) {
     if (p.n == 0) return;
     const int nb = blocks_for(p.n, kThreads);
-    k_hash<<<nb, kThreads, 0, s>>>(d, p);
+    if (multi) k_hash<true><<<nb, kThreads, 0, s>>>(d, p, cur);
+    else k_hash<false><<<nb, kThreads, 0, s>>>(d, p, cur);
     k_scan_excl<uint32_t, true><<<ntiles_cells, kScanBlock, 0, s>>>(
-        d.cell_count, d.cell_start, (long long)p.H, ntiles_cells, d.scan_state[kScanCells],
+        d.cell_count, d.cell_start, (long long)p.T, ntiles_cells, d.scan_state[kScanCells],
         &d.ctr->tickets[kScanCells], d.ctr);
     k_scatter<<<nb, kThreads, 0, s>>>(d, p);
-    k_canon<<<nb, kThreads, 0, s>>>(d, p);
+    if (multi) k_canon<true><<<nb, kThreads, 0, s>>>(d, p);
+    else k_canon<false><<<nb, kThreads, 0, s>>>(d, p);
 }
 
-void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, cudaStream_t s) {
+void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+                   cudaStream_t s) {
     if (p.n == 0) return;
     const int nb = blocks_for((long long)p.n * kLanes, kThreads);
-    if (init) k_detect<true><<<nb, kThreads, 0, s>>>(d, p, cur);
-    else k_detect<false><<<nb, kThreads, 0, s>>>(d, p, cur);
+    if (multi) k_detect<false, true><<<nb, kThreads, 0, s>>>(d, p, cur);
+    else if (init) k_detect<true, false><<<nb, kThreads, 0, s>>>(d, p, cur);
+    else k_detect<false, false><<<nb, kThreads, 0, s>>>(d, p, cur);
 }
 
-void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, int grid,
+void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi, int grid,
                     cudaStream_t s) {
     if (p.n == 0) return;
     const int nb = min(blocks_for((long long)p.cap + p.n, kThreads), grid);
-    if (init) k_compact<true><<<nb, kThreads, 0, s>>>(d, p, cur);
-    else k_compact<false><<<nb, kThreads, 0, s>>>(d, p, cur);
+    if (multi) k_compact<false, true><<<nb, kThreads, 0, s>>>(d, p, cur);
+    else if (init) k_compact<true, false><<<nb, kThreads, 0, s>>>(d, p, cur);
+    else k_compact<false, false><<<nb, kThreads, 0, s>>>(d, p, cur);
 }
 
-void launch_force(const DemDev& d, const DemParams& p, int nxt, int grid, cudaStream_t s) {
+void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, int grid,
+                  cudaStream_t s) {
     if (p.n == 0 || p.cap == 0) return;
-    if (p.precision == 1) k_force<float><<<grid, kThreads, 0, s>>>(d, p, nxt);
-    else k_force<double><<<grid, kThreads, 0, s>>>(d, p, nxt);
+    if (p.precision == 1) {
+        if (multi) k_force<float, true><<<grid, kThreads, 0, s>>>(d, p, nxt);
+        else k_force<float, false><<<grid, kThreads, 0, s>>>(d, p, nxt);
+    } else {
+        if (multi) k_force<double, true><<<grid, kThreads, 0, s>>>(d, p, nxt);
+        else k_force<double, false><<<grid, kThreads, 0, s>>>(d, p, nxt);
+    }
 }
 
-void launch_integrate(const DemDev& d, const DemParams& p, int cur, cudaStream_t s) {
+void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi, cudaStream_t s) {
     if (p.n == 0) return;
-    k_integrate<<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, cur);
+    if (multi) k_integrate<true><<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, cur);
+    else k_integrate<false><<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, cur);
 }
 
 void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cudaStream_t s) {

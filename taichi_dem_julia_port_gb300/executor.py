@@ -34,6 +34,40 @@ def _f64(a, shape=None):
     return a.reshape(shape) if shape is not None else a
 
 
+def read_particles(lib, call, n: int, forces: bool, where: str) -> dict:
+    """Particle state through a dem_*get_particles call taking a DemParticleState*."""
+    out = {k: np.empty((n, 3)) for k in ("pos", "vel", "omega", "wall_shear")}
+    out["quat"] = np.empty((n, 4))
+    if forces:
+        out["force"] = np.empty((n, 3))
+        out["moment"] = np.empty((n, 3))
+    st = _abi.DemParticleState(n, *(ptr(out.get(k), C.c_double) for k in
+                                    ("pos", "vel", "omega", "quat", "force", "moment",
+                                     "wall_shear")))
+    check(lib, call(C.byref(st)), where)
+    return out
+
+
+_CONTACT_VECS = ("point", "force", "torque_i", "torque_j", "shear")
+
+
+def read_contacts(lib, call, where: str) -> dict:
+    """Active contacts sorted by (i, j) through a dem_*get_contacts call taking
+    (DemContacts*, cap, int64_t* count)."""
+    cnt = C.c_int64()
+    check(lib, call(None, 0, C.byref(cnt)), where)
+    m = cnt.value
+    out = {"i": np.empty(m, np.int32), "j": np.empty(m, np.int32),
+           "bonded": np.empty(m, np.uint8)}
+    for k in _CONTACT_VECS:
+        out[k] = np.empty((m, 3))
+    cs = _abi.DemContacts(ptr(out["i"], C.c_int32), ptr(out["j"], C.c_int32),
+                          ptr(out["bonded"], C.c_uint8),
+                          *(ptr(out[k], C.c_double) for k in _CONTACT_VECS))
+    check(lib, call(C.byref(cs), m, C.byref(cnt)), where)
+    return out
+
+
 class GlobalData:
     """Device state of one scene (particles, broad phase, contacts)."""
 
@@ -112,17 +146,8 @@ class GlobalData:
 
     # ---- state ----------------------------------------------------------------
     def particles(self, forces: bool = True) -> dict:
-        n = self.n
-        out = {k: np.empty((n, 3)) for k in ("pos", "vel", "omega", "wall_shear")}
-        out["quat"] = np.empty((n, 4))
-        if forces:
-            out["force"] = np.empty((n, 3))
-            out["moment"] = np.empty((n, 3))
-        st = _abi.DemParticleState(n, *(ptr(out.get(k), C.c_double) for k in
-                                        ("pos", "vel", "omega", "quat", "force", "moment",
-                                         "wall_shear")))
-        check(self.lib, self.lib.dem_get_particles(self.h, C.byref(st)), "dem_get_particles")
-        return out
+        return read_particles(self.lib, lambda st: self.lib.dem_get_particles(self.h, st),
+                              self.n, forces, "dem_get_particles")
 
     def set_particles(self, pos=None, vel=None, omega=None, quat=None, wall_shear=None) -> None:
         n = self.n
@@ -149,21 +174,9 @@ class GlobalData:
 
     def contacts(self) -> dict:
         """Active contacts sorted by (i, j) (0-based indices)."""
-        cnt = C.c_int64()
-        check(self.lib, self.lib.dem_get_contacts(self.h, None, 0, C.byref(cnt)),
-              "dem_get_contacts")
-        m = cnt.value
-        out = {"i": np.empty(m, np.int32), "j": np.empty(m, np.int32),
-               "bonded": np.empty(m, np.uint8)}
-        for k in ("point", "force", "torque_i", "torque_j", "shear"):
-            out[k] = np.empty((m, 3))
-        cs = _abi.DemContacts(ptr(out["i"], C.c_int32), ptr(out["j"], C.c_int32),
-                              ptr(out["bonded"], C.c_uint8),
-                              *(ptr(out[k], C.c_double) for k in
-                                ("point", "force", "torque_i", "torque_j", "shear")))
-        check(self.lib, self.lib.dem_get_contacts(self.h, C.byref(cs), m, C.byref(cnt)),
-              "dem_get_contacts")
-        return out
+        return read_contacts(
+            self.lib, lambda cs, cap, cnt: self.lib.dem_get_contacts(self.h, cs, cap, cnt),
+            "dem_get_contacts")
 
     def set_contacts(self, c: dict) -> None:
         m = len(c["i"])

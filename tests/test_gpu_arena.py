@@ -1,0 +1,176 @@
+"""GPU: scenes in a shared arena give the results they give alone.
+
+A scene stepped inside an arena (with other scenes, added or removed while it
+runs, with a smaller search grid) must produce, bit for bit, the particle
+state and contact list that a single-scene handle (dem_create) produces for
+it; the single-scene handle is itself checked against the oracle in
+test_gpu_parity.py, and one arena scene is checked against the oracle here."""
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleScene
+from taichi_dem_julia_port_gb300 import Arena, GlobalData, scenes
+from taichi_dem_julia_port_gb300._abi import DEM_ERR_CAPACITY, DemError
+from tests.conftest import assert_rows_close
+
+pytestmark = pytest.mark.gpu
+
+PARTICLE_KEYS = ("pos", "vel", "omega", "quat", "force", "moment", "wall_shear")
+CONTACT_KEYS = ("i", "j", "bonded", "point", "force", "torque_i", "torque_j", "shear")
+
+
+def small_cube(side=5, speed=20.0, seed=1, **kw):
+    sc = scenes.bonded_cube(side, speed=speed, steps=0, seed=seed, **kw)
+    # strong impact on the wall right away: bonds stressed, Hertz contacts form
+    sc.cfg = sc.cfg.replace(bond_tensile_strength=3e5, bond_shear_strength=3e5)
+    return sc
+
+
+def small_pour(n=600, seed=5, **kw):
+    """Unbonded spheres with narrow gaps and 5 m/s random velocities: Hertz
+    contacts form and end within tens of steps."""
+    sc = scenes.granular_pour(n, box=(0.03, 0.03, 0.04), seed=seed, steps=0, rmin=0.8e-3,
+                              rmax=1.2e-3, **kw)
+    sc.cfg = sc.cfg.replace(dt=1e-6)
+    pv = sc.particles.copy()
+    rng = np.random.default_rng(seed)
+    pv.vel = rng.normal(0, 5.0, pv.vel.shape)
+    sc.particles = pv
+    return sc
+
+
+def alone(sc, steps, init=True, precision="fp64"):
+    g = GlobalData(sc.cfg, sc.particles, precision=precision)
+    if init:
+        g.initialize()
+    g.simulate(steps)
+    out = (g.particles(), g.contacts(), g.stats())
+    g.close()
+    return out
+
+
+def assert_same(arena, sid, ref, what):
+    p, c = arena.particles(sid), arena.contacts(sid)
+    rp, rc, _ = ref
+    for k in PARTICLE_KEYS:
+        np.testing.assert_array_equal(p[k], rp[k], err_msg=f"{what}: particles.{k}")
+    assert len(c["i"]) == len(rc["i"]), f"{what}: contact count {len(c['i'])} vs {len(rc['i'])}"
+    for k in CONTACT_KEYS:
+        np.testing.assert_array_equal(c[k], rc[k], err_msg=f"{what}: contacts.{k}")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_single_scene_arena_equals_alone(gpu, precision):
+    sc = small_cube()
+    ref = alone(sc, 60, precision=precision)
+    with Arena(4096, max_scenes=4, precision=precision) as a:
+        s = a.add(sc.cfg, sc.particles)
+        a.step(60)
+        assert a.info(s)["steps_done"] == 60
+        assert_same(a, s, ref, f"arena {precision}")
+        st = a.stats(s)
+        assert st["bonded"] == ref[2]["bonded"] and st["contacts"] == ref[2]["contacts"]
+        assert st["bonds_broken"] == ref[2]["bonds_broken"]
+
+
+def test_mixed_scenes_each_equal_alone(gpu):
+    cube_a = small_cube(5, seed=1)
+    cube_b = small_cube(6, speed=25.0, seed=2, E=5e8, friction=0.3)
+    pour = small_pour(600, seed=7)
+    steps = 80
+    refs = [alone(cube_a, steps), alone(cube_b, steps), alone(pour, steps, init=False)]
+    with Arena(8192, max_scenes=8) as a:
+        ids = [a.add(cube_a.cfg, cube_a.particles), a.add(cube_b.cfg, cube_b.particles),
+               a.add(pour.cfg, pour.particles, init_bonds=False)]
+        a.step(steps)
+        for sid, ref, name in zip(ids, refs, ("cube_a", "cube_b", "pour")):
+            assert_same(a, sid, ref, name)
+    # something happened: bonds in the cubes, Hertz contacts made and ended in the pour
+    assert refs[0][2]["bonded"] > 0
+    assert refs[2][2]["contacts"] > 0 and refs[2][2]["contacts_ended"] > 0
+
+
+def test_scenes_join_and_leave_while_running(gpu):
+    """Continuous batching: A runs; B joins after 30 steps; A leaves; C takes
+    A's freed slots (C is no larger than A).  B and C match their alone runs."""
+    A, B, C = small_cube(5, seed=11), small_cube(5, speed=15.0, seed=12), small_pour(120, seed=13)
+    ref_b = alone(B, 70)
+    ref_c = alone(C, 40, init=False)
+    with Arena(4096, max_scenes=4) as a:
+        sa = a.add(A.cfg, A.particles)
+        a.step(30)
+        sb = a.add(B.cfg, B.particles)
+        a.step(30)
+        first_a = a.info(sa)["first_slot"]
+        a.remove(sa)
+        sc_ = a.add(C.cfg, C.particles, init_bonds=False)
+        assert a.info(sc_)["first_slot"] == first_a, "C should reuse A's slots"
+        a.step(40)
+        assert_same(a, sb, ref_b, "B")
+        assert_same(a, sc_, ref_c, "C")
+
+
+def test_step_target_freezes_scene(gpu):
+    sc = small_cube(5, seed=21)
+    ref = alone(sc, 25)
+    with Arena(2048, max_scenes=2) as a:
+        s = a.add(sc.cfg, sc.particles, steps=25)
+        a.step(40)
+        info = a.info(s)
+        assert info["mode"] == "frozen" and info["steps_done"] == 25
+        assert_same(a, s, ref, "frozen at target")
+
+
+def test_smaller_search_cells_same_results(gpu):
+    """cell_factor < 1: a finer search grid, the reference's cp_list rules
+    still decide contact ends, so every result is unchanged."""
+    cube, pour = small_cube(6, seed=31), small_pour(800, seed=32)
+    steps = 60
+    refs = [alone(cube, steps), alone(pour, steps, init=False)]
+    with Arena(4096, max_scenes=4, cell_factor=0.3) as a:
+        ids = [a.add(cube.cfg, cube.particles), a.add(pour.cfg, pour.particles, init_bonds=False)]
+        a.step(steps)
+        for sid, ref, name in zip(ids, refs, ("cube", "pour")):
+            assert_same(a, sid, ref, f"fine grid {name}")
+
+
+def test_arena_scene_against_oracle(gpu):
+    sc = small_cube(5, seed=41)
+    o = OracleScene(sc.cfg, sc.particles)
+    o.initialize()
+    o.simulate(40)
+    with Arena(2048, max_scenes=2, cell_factor=0.5) as a:
+        s = a.add(sc.cfg, sc.particles)
+        a.step(40)
+        cg, co = a.contacts(s), o.contacts()
+        assert set(zip(cg["i"].tolist(), cg["j"].tolist())) == \
+            set(zip(co["i"].tolist(), co["j"].tolist()))
+        pg, po = a.particles(s), o.particles()
+        assert_rows_close(pg["pos"], po["pos"], 1e-9, "pos")
+        assert_rows_close(pg["force"], po["force"], 1e-5, "force", atol_frac=1e-5)
+
+
+def test_arena_capacity_errors(gpu):
+    sc = small_cube(5)  # 125 particles
+    with Arena(130, max_scenes=4) as a:
+        a.add(sc.cfg, sc.particles)
+        with pytest.raises(DemError) as e:
+            a.add(sc.cfg, sc.particles)  # no particle slots left
+        assert e.value.code == DEM_ERR_CAPACITY
+    with Arena(1000, max_scenes=1) as a:
+        a.add(sc.cfg, sc.particles)
+        with pytest.raises(DemError) as e:
+            a.add(sc.cfg, sc.particles)  # no scene record left
+        assert e.value.code == DEM_ERR_CAPACITY
+
+
+def test_arena_empty_steps(gpu):
+    pour = small_pour(100, seed=3)
+    ref = alone(pour, 3, init=False)
+    with Arena(1024, max_scenes=2) as a:
+        a.step(5)  # nothing to step
+        a.sync()
+        s = a.add(pour.cfg, pour.particles, init_bonds=False)
+        a.step(3)
+        assert a.info(s)["steps_done"] == 3
+        assert_same(a, s, ref, "after empty steps")
