@@ -209,6 +209,22 @@ int dem_sync(DemHandle* h);
  * DEM_FP32_FORCE.  No counterpart in the reference, which is FP64 only. */
 int dem_set_precision(DemHandle* h, int mode);
 
+/* Launch shape of the grid-stride kernels (contact compaction, contact
+ * forces, integration): block sizes (multiples of 32, at most 256) and grid
+ * upper bounds.  Results are the same for every shape; the shape only changes
+ * speed (the autotuner's knob).  No counterpart in the reference. */
+typedef struct DemLaunchShape {
+    int32_t force_block;
+    int32_t force_grid;
+    int32_t compact_block;
+    int32_t compact_grid;
+    int32_t integrate_block;
+    int32_t pad;
+} DemLaunchShape;
+
+int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* shape);
+int dem_get_launch_shape(DemHandle* h, DemLaunchShape* out);
+
 /* ---- state exchange ---------------------------------------------------- */
 
 /* Reads `grains` (positions, velocities, ...) back to the host, as
@@ -286,6 +302,12 @@ int dem_arena_add(DemHandle* h, const DemConfigC* cfg, const DemParticlesIn* par
 
 /* Releases a scene's slots and contacts. */
 int dem_arena_remove(DemHandle* h, int32_t scene);
+
+/* Search-cell factor of one scene (scene >= 0) or of every scene (scene < 0),
+ * as DemArenaConfig.cell_factor.  Takes effect at the next step and leaves
+ * every result unchanged (contact ends still follow the reference's cells);
+ * only the pair-search work changes (the autotuner's knob). */
+int dem_arena_set_cell_factor(DemHandle* h, int32_t scene, double cell_factor);
 
 int dem_arena_scene_info(DemHandle* h, int32_t scene, DemSceneInfo* out);
 

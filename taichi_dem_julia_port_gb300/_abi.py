@@ -105,6 +105,15 @@ class DemStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class DemLaunchShape(C.Structure):
+    _fields_ = [("force_block", C.c_int32), ("force_grid", C.c_int32),
+                ("compact_block", C.c_int32), ("compact_grid", C.c_int32),
+                ("integrate_block", C.c_int32), ("pad", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
 DEM_SCENE_FREE = 0
 DEM_SCENE_FROZEN = 1
 DEM_SCENE_STEP = 2
@@ -141,6 +150,8 @@ ENTRY_POINTS = {
     "dem_step_profiled": (C.c_int, [_H, C.POINTER(C.c_float), C.c_int]),
     "dem_sync": (C.c_int, [_H]),
     "dem_set_precision": (C.c_int, [_H, C.c_int]),
+    "dem_set_launch_shape": (C.c_int, [_H, C.POINTER(DemLaunchShape)]),
+    "dem_get_launch_shape": (C.c_int, [_H, C.POINTER(DemLaunchShape)]),
     "dem_get_particles": (C.c_int, [_H, C.POINTER(DemParticleState)]),
     "dem_set_particles": (C.c_int, [_H, C.POINTER(DemParticleState)]),
     "dem_get_static": (C.c_int, [_H, C.POINTER(DemParticleStatic)]),
@@ -154,6 +165,7 @@ ENTRY_POINTS = {
     "dem_arena_add": (C.c_int, [_H, C.POINTER(DemConfigC), C.POINTER(DemParticlesIn), C.c_int,
                                 C.c_int64, C.POINTER(C.c_int32)]),
     "dem_arena_remove": (C.c_int, [_H, C.c_int32]),
+    "dem_arena_set_cell_factor": (C.c_int, [_H, C.c_int32, C.c_double]),
     "dem_arena_scene_info": (C.c_int, [_H, C.c_int32, C.POINTER(DemSceneInfo)]),
     "dem_scene_get_particles": (C.c_int, [_H, C.c_int32, C.POINTER(DemParticleState)]),
     "dem_scene_get_contacts": (C.c_int, [_H, C.c_int32, C.POINTER(DemContacts), C.c_int64,

@@ -19,7 +19,8 @@ import numpy as np
 from . import _abi
 from ._abi import check, ptr
 from .config import DEMConfig
-from .executor import PRECISIONS, _f64, read_contacts, read_particles
+from .executor import (PRECISIONS, _f64, get_launch_shape, read_contacts, read_particles,
+                       set_launch_shape)
 from .scenes import ParticleInput
 
 MODES = {_abi.DEM_SCENE_FREE: "free", _abi.DEM_SCENE_FROZEN: "frozen",
@@ -28,9 +29,9 @@ MODES = {_abi.DEM_SCENE_FREE: "free", _abi.DEM_SCENE_FROZEN: "frozen",
 
 def buckets_for(n: int) -> int:
     """Bucket-table entries a scene of n particles takes: the power of two of
-    at least 4n, and at least 1024 (mirrors dem_arena_add)."""
+    at least 2n, and at least 1024 (mirrors dem_arena_add)."""
     H = 1024
-    while H < 4 * n:
+    while H < 2 * n:
         H <<= 1
     return H
 
@@ -53,7 +54,7 @@ class Arena:
         if max_contacts is None:
             max_contacts = max_particles * max_coordinate_number
         if max_buckets is None:
-            max_buckets = 8 * max_particles + 1024 * max_scenes
+            max_buckets = 4 * max_particles + 1024 * max_scenes
         self.max_particles, self.max_scenes = int(max_particles), int(max_scenes)
         self.max_contacts, self.max_buckets = int(max_contacts), int(max_buckets)
         self.precision = precision
@@ -120,6 +121,18 @@ class Arena:
         d["mode"] = MODES[d["mode"]]
         return d
 
+    def set_cell_factor(self, cell_factor: float, scene: int = -1) -> None:
+        """Search-cell factor of one scene or all (-1); results do not change."""
+        check(self.lib, self.lib.dem_arena_set_cell_factor(self.h, int(scene),
+                                                           float(cell_factor)),
+              "dem_arena_set_cell_factor")
+
+    def launch_shape(self) -> dict:
+        return get_launch_shape(self.lib, self.h)
+
+    def set_launch_shape(self, **shape) -> None:
+        set_launch_shape(self.lib, self.h, shape)
+
     # ---- the step -------------------------------------------------------------
     def step(self, nsteps: int = 1) -> None:
         """`simulate!` × nsteps for every scene in Step mode (asynchronous)."""
@@ -130,6 +143,13 @@ class Arena:
         check(self.lib, self.lib.dem_step_timed(self.h, int(nsteps), C.byref(ms)),
               "dem_step_timed")
         return float(ms.value)
+
+    def step_profiled(self) -> dict:
+        """One step launched phase by phase; device milliseconds per phase."""
+        ms = (C.c_float * 5)()
+        check(self.lib, self.lib.dem_step_profiled(self.h, ms, 5), "dem_step_profiled")
+        return dict(zip(("broadphase", "detect", "compact", "force", "integrate"),
+                        [float(x) for x in ms]))
 
     def sync(self) -> None:
         check(self.lib, self.lib.dem_sync(self.h), "dem_sync")

@@ -1,0 +1,86 @@
+"""Autotuner for a stepping handle (an `Arena` or a `GlobalData`).
+
+Picks the search-cell factor (arenas) and the launch shape of the grid-stride
+kernels (contact compaction, contact forces, integration) by timing real steps
+on the live workload with CUDA events.  None of these knobs changes a result:
+the search grid only changes which buckets the pair search visits (contact
+ends follow the reference's cells), and every kernel computes the same values
+for any launch shape; the arena tests check both bit for bit.  The steps taken
+while tuning are ordinary simulation steps.
+
+The search is coordinate descent: cell factor first, then the force kernel's
+block and grid, then the compaction grid, then the integration block; each
+candidate is timed over `steps` steps after one untimed step.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+CELL_FACTORS = (1.0, 0.8, 0.6, 0.45, 0.35)
+BLOCKS = (128, 256)
+GRIDS_PER_SM = (4, 8, 16, 32)
+INTEGRATE_BLOCKS = (128, 256)
+
+
+@dataclass
+class TuneResult:
+    cell_factor: float | None
+    shape: dict
+    ms_per_step: float
+    trials: list = field(default_factory=list)
+
+    def as_dict(self) -> dict:
+        return {"cell_factor": self.cell_factor, "shape": self.shape,
+                "ms_per_step": self.ms_per_step, "trials": len(self.trials)}
+
+
+def _time(target, steps: int) -> float:
+    target.step(1) if hasattr(target, "step") else target.simulate(1)
+    t = target.step_timed(steps) if hasattr(target, "step_timed") else \
+        target.simulate_timed(steps)
+    return t / steps
+
+
+def autotune(target, sm_count: int = 152, steps: int = 10, cell_factors=CELL_FACTORS,
+             blocks=BLOCKS, grids_per_sm=GRIDS_PER_SM,
+             integrate_blocks=INTEGRATE_BLOCKS) -> TuneResult:
+    """Tunes `target` in place and returns the chosen settings."""
+    trials = []
+    is_arena = hasattr(target, "set_cell_factor")
+    best_cf = None
+    best = _time(target, steps)
+    trials.append(({"baseline": True}, best))
+    if is_arena:
+        best_cf = 1.0
+        for cf in cell_factors:
+            target.set_cell_factor(cf)
+            t = _time(target, steps)
+            trials.append(({"cell_factor": cf}, t))
+            if t < best:
+                best, best_cf = t, cf
+        target.set_cell_factor(best_cf)
+    shape = target.launch_shape()
+    for fb in blocks:
+        for g in grids_per_sm:
+            cand = dict(shape, force_block=fb, force_grid=g * sm_count)
+            target.set_launch_shape(**cand)
+            t = _time(target, steps)
+            trials.append((cand, t))
+            if t < best:
+                best, shape = t, cand
+    for g in grids_per_sm:
+        cand = dict(shape, compact_grid=g * sm_count)
+        target.set_launch_shape(**cand)
+        t = _time(target, steps)
+        trials.append((cand, t))
+        if t < best:
+            best, shape = t, cand
+    for ib in integrate_blocks:
+        cand = dict(shape, integrate_block=ib)
+        target.set_launch_shape(**cand)
+        t = _time(target, steps)
+        trials.append((cand, t))
+        if t < best:
+            best, shape = t, cand
+    target.set_launch_shape(**shape)
+    return TuneResult(best_cf, shape, best, trials)

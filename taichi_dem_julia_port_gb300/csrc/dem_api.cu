@@ -144,8 +144,18 @@ struct SceneHost {
     DemConfigC cfg{};
     DemDerived der{};
     SceneParams sp{};
+    double min_cell = 0.0;  // smallest search cell that finds every touching pair
     int64_t steps = 0, target = 0;
 };
+
+// Search cells of a scene for a cell factor f: f·(the reference's cell),
+// clamped to [min_cell, the reference's cell].
+void set_search_cell(SceneParams& p, double f, double min_cell, bool empty) {
+    f = f > 0 ? f : 1.0;
+    p.cell = empty ? p.cell_ref : std::min(p.cell_ref, std::max(f * p.cell_ref, min_cell));
+    p.inv_cell = 1.0 / p.cell;
+    p.same_grid = p.cell == p.cell_ref ? 1 : 0;
+}
 
 // Per-particle arrays of one scene, derived on the host.
 struct SceneArrays {
@@ -224,12 +234,9 @@ int prepare_scene(const DemConfigC* cfg, const DemParticlesIn* pin, double cell_
     // Search cells.  A smaller cell still finds every touching pair with the
     // octant search as long as cell >= 2(rᵢ + rⱼ) for the radii in use, i.e.
     // 4·max r (stepping) and 4·max r₀ (bond initialisation).
-    const double f = cell_factor > 0 ? cell_factor : 1.0;
-    const double floor_cell =
+    S.min_cell =
         4.0 * rmax_r * std::max(1.0, cfg->particle_contact_radius_multiplier) * (1.0 + 1e-9);
-    p.cell = n ? std::min(D.cell_size, std::max(f * D.cell_size, floor_cell)) : D.cell_size;
-    p.inv_cell = 1.0 / p.cell;
-    p.same_grid = p.cell == p.cell_ref ? 1 : 0;
+    set_search_cell(p, cell_factor, S.min_cell, n == 0);
     p.dt = cfg->dt;
     p.tol = cfg->tolerance;
     p.damping = cfg->global_damping;
@@ -295,7 +302,7 @@ struct DemHandle {
     int cur = 0;  // contact buffer holding the current state
     int64_t steps = 0;
     int ntiles_cells = 0;
-    int force_grid = 1;
+    LaunchShape shape{};
     cudaStream_t stream = nullptr;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     int graph_precision = -1;
@@ -358,6 +365,8 @@ int allocate(DemHandle* h) {
                       &d.fx, &d.fy, &d.fz, &d.tx, &d.ty, &d.tz, &d.wsx, &d.wsy, &d.wsz};
     for (double** a : dbl) TRY(dalloc(h, a, n));
     TRY(dalloc(h, &d.cellinfo, n));
+    TRY(dalloc(h, &d.scell, n));
+    TRY(dalloc(h, &d.srow, n));
     TRY(dalloc(h, &d.bucket, n));
     TRY(dalloc(h, &d.cell_count, T));
     TRY(dalloc(h, &d.cell_start, T + 1));
@@ -409,9 +418,8 @@ int init_handle(DemHandle* h) {
     CU(cudaEventCreate(&h->ev0));
     CU(cudaEventCreate(&h->ev1));
     TRY(allocate(h));
-    h->ntiles_cells = std::max(1, scan_tiles((int64_t)h->t_cap));
-    h->force_grid = (int)std::max<int64_t>(
-        1, std::min<int64_t>(((int64_t)h->c_cap + 255) / 256, (int64_t)h->sm_count * 16));
+    h->ntiles_cells = std::max(1, scan_tiles((int64_t)h->p.T));
+    h->shape = LaunchShape{256, h->sm_count * 16, 256, h->sm_count * 16, 256};
     return DEM_OK;
 }
 
@@ -457,9 +465,47 @@ void record_step(DemHandle* h, int cur) {
     const int nxt = cur ^ 1;
     launch_broadphase(h->d, h->p, cur, h->multi, h->ntiles_cells, h->stream);
     launch_detect(h->d, h->p, cur, false, h->multi, h->stream);
-    launch_compact(h->d, h->p, cur, false, h->multi, h->force_grid, h->stream);
-    launch_force(h->d, h->p, nxt, h->multi, h->force_grid, h->stream);
-    launch_integrate(h->d, h->p, cur, h->multi, h->stream);
+    launch_compact(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
+    launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
+    launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
+}
+
+void drop_graphs(DemHandle* h) {
+    for (int b = 0; b < 2; ++b) {
+        if (h->exec[b]) cudaGraphExecDestroy(h->exec[b]);
+        h->exec[b] = nullptr;
+    }
+}
+
+// Slots and buckets a step processes: up to the end of the highest range in
+// use, rounded up, so the step's launches shrink with the arena's occupancy.
+// The bucket scan's tickets and tile states restart when its tile count
+// changes (its tile and epoch arithmetic assume a fixed count).
+int update_bounds(DemHandle* h) {
+    auto hi = [](const FreeList& fl, int64_t cap, int64_t grain) {
+        int64_t top = cap;
+        if (!fl.free.empty() && fl.free.back().first + fl.free.back().second == cap)
+            top = fl.free.back().first;
+        top = (top + grain - 1) / grain * grain;
+        return std::min(std::max(top, grain), cap);
+    };
+    const int n = (int)hi(h->pfree, h->n_cap, 32768);
+    const uint32_t T = (uint32_t)hi(h->tfree, h->t_cap, 65536);
+    if (n == h->p.n && T == h->p.T) return DEM_OK;
+    CU(cudaStreamSynchronize(h->stream));
+    h->p.n = n;
+    h->p.T = T;
+    const int nt = std::max(1, scan_tiles((int64_t)T));
+    if (nt != h->ntiles_cells) {
+        h->ntiles_cells = nt;
+        CU(cudaMemsetAsync(&h->d.ctr->tickets[kScanCells], 0, sizeof(unsigned long long),
+                           h->stream));
+        CU(cudaMemsetAsync(h->d.scan_state[kScanCells], 0,
+                           sizeof(unsigned long long) * (size_t)scan_tiles((int64_t)h->t_cap),
+                           h->stream));
+    }
+    drop_graphs(h);
+    return DEM_OK;
 }
 
 int build_graphs(DemHandle* h) {
@@ -549,6 +595,46 @@ int apply_modes(DemHandle* h, const std::vector<std::pair<int, int>>& upd) {
         CU(cudaGetLastError());
     }
     return DEM_OK;
+}
+
+// `initialize!` of newly added arena scenes: one launch in which they run in
+// Init mode and every stepping scene is held (Frozen carries its state and
+// contacts over unchanged), so it costs them no step.  Needs the graphs.
+int launch_inits(DemHandle* h) {
+    if (!h->multi) return DEM_OK;
+    std::vector<std::pair<int, int>> hold, back;
+    for (int k = 0; k < h->s_cap; ++k) {
+        SceneHost& S = h->scenes[k];
+        if (S.mode == kModeStep) {
+            hold.push_back({k, kModeFrozen});
+            back.push_back({k, kModeStep});
+        } else if (S.mode == kModeInit) {
+            back.push_back({k, kModeStep});
+        }
+    }
+    if (back.size() == hold.size()) return DEM_OK;  // no scene to initialise
+    for (auto& kv : back) h->scenes[kv.first].mode = kModeStep;
+    TRY(apply_modes(h, hold));
+    CU(cudaGraphLaunch(h->exec[h->cur], h->stream));
+    h->cur ^= 1;
+    return apply_modes(h, back);
+}
+
+// Scene bookkeeping after a step launch (stream-ordered, no host sync): step
+// counts, and scenes that reached their target freeze.
+int after_launch(DemHandle* h) {
+    if (!h->multi) return DEM_OK;
+    std::vector<std::pair<int, int>> upd;
+    for (int k = 0; k < h->s_cap; ++k) {
+        SceneHost& S = h->scenes[k];
+        if (S.mode != kModeStep) continue;
+        ++S.steps;
+        if (S.target > 0 && S.steps >= S.target) {
+            S.mode = kModeFrozen;
+            upd.push_back({k, kModeFrozen});
+        }
+    }
+    return upd.empty() ? DEM_OK : apply_modes(h, upd);
 }
 
 // Particle state of slots [p0, p0 + n) to host arrays (scene-local order).
@@ -787,6 +873,8 @@ int dem_arena_create(const DemArenaConfig* cfg, DemHandle** out) {
     h->scenes.resize(h->s_cap);
     h->pfree.init(h->n_cap);
     h->tfree.init(h->t_cap);
+    h->p.n = std::min(h->n_cap, 32768);
+    h->p.T = std::min<uint32_t>(h->t_cap, 65536u);
     int rc = init_handle(h);
     if (rc == DEM_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = DEM_ERR_CUDA;
     if (rc != DEM_OK) {
@@ -812,9 +900,9 @@ int dem_arena_add(DemHandle* h, const DemConfigC* cfg, const DemParticlesIn* pin
         }
     if (idx < 0) return DEM_ERR_CAPACITY;
     const int64_t n = pin->n;
-    // search table of the scene: a power of two of at least 4 entries per particle
+    // search table of the scene: a power of two of at least 2 entries per particle
     uint32_t H = 1024;
-    while ((int64_t)H < 4 * n && H < (1u << 30)) H <<= 1;
+    while ((int64_t)H < 2 * n && H < (1u << 30)) H <<= 1;
     int64_t p0 = 0, t0 = 0;
     if (!h->pfree.take(n, &p0)) return DEM_ERR_CAPACITY;
     if (!h->tfree.take(H, &t0)) {
@@ -853,7 +941,7 @@ int dem_arena_add(DemHandle* h, const DemConfigC* cfg, const DemParticlesIn* pin
     }
     h->scenes[idx] = S;
     *scene = idx;
-    return DEM_OK;
+    return update_bounds(h);
 }
 
 int dem_arena_remove(DemHandle* h, int32_t s) {
@@ -861,10 +949,52 @@ int dem_arena_remove(DemHandle* h, int32_t s) {
     SceneHost& S = h->scenes[s];
     const int64_t p0 = S.sp.p0, n = S.sp.n;
     TRY(apply_modes(h, {{s, kModeFree}}));
-    if (n) CU(cudaMemsetAsync(h->d.scene_of + p0, 0xff, (size_t)n * sizeof(int32_t), h->stream));
+    if (n) {
+        CU(cudaMemsetAsync(h->d.scene_of + p0, 0xff, (size_t)n * sizeof(int32_t), h->stream));
+        // the scene's rows are emptied, so its contacts are not carried over
+        for (int b = 0; b < 2; ++b)
+            CU(cudaMemsetAsync(h->d.row_len[b] + p0, 0, (size_t)n * 4, h->stream));
+    }
     h->pfree.give(p0, n);
     h->tfree.give(S.sp.t0, S.sp.H);
     S = SceneHost();
+    return update_bounds(h);
+}
+
+int dem_arena_set_cell_factor(DemHandle* h, int32_t s, double f) {
+    if (!h || !h->multi || !(f >= 0) || f > 1) return DEM_ERR_INVALID;
+    if (s >= 0 && !scene_at(h, s)) return DEM_ERR_INVALID;
+    for (int k = 0; k < h->s_cap; ++k) {
+        if ((s >= 0 && k != s) || h->scenes[k].mode == kModeFree) continue;
+        SceneHost& S = h->scenes[k];
+        set_search_cell(S.sp, f, S.min_cell, S.sp.n == 0);
+        // the record's mode on the device may differ from the host copy for
+        // the length of dem_step only, so the host record is current here
+        S.sp.mode = S.mode;
+        CU(cudaMemcpyAsync(h->d.sp + k, &S.sp, sizeof(SceneParams), cudaMemcpyHostToDevice,
+                           h->stream));
+    }
+    if (s < 0) h->cell_factor = f > 0 ? f : 1.0;
+    CU(cudaStreamSynchronize(h->stream));
+    return DEM_OK;
+}
+
+int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* sh) {
+    if (!h || !sh || sh->force_block < 32 || sh->force_block > 256 || sh->force_block % 32 ||
+        sh->compact_block < 32 || sh->compact_block > 256 || sh->compact_block % 32 ||
+        sh->integrate_block < 32 || sh->integrate_block > 256 || sh->integrate_block % 32 ||
+        sh->force_grid < 1 || sh->compact_grid < 1)
+        return DEM_ERR_INVALID;
+    h->shape = LaunchShape{sh->force_block, sh->force_grid, sh->compact_block, sh->compact_grid,
+                           sh->integrate_block};
+    drop_graphs(h);
+    return DEM_OK;
+}
+
+int dem_get_launch_shape(DemHandle* h, DemLaunchShape* out) {
+    if (!h || !out) return DEM_ERR_INVALID;
+    *out = DemLaunchShape{h->shape.force_block, h->shape.force_grid, h->shape.compact_block,
+                          h->shape.compact_grid, h->shape.integrate_block, 0};
     return DEM_OK;
 }
 
@@ -901,7 +1031,7 @@ int dem_init_bonds(DemHandle* h) {
     const int cur = h->cur, nxt = cur ^ 1;
     launch_broadphase(h->d, h->p, cur, false, h->ntiles_cells, h->stream);
     launch_detect(h->d, h->p, cur, true, false, h->stream);
-    launch_compact(h->d, h->p, cur, true, false, h->force_grid, h->stream);
+    launch_compact(h->d, h->p, cur, true, false, h->shape, h->stream);
     // the old buffer becomes the next step's target: its allocator starts at 0
     CU(cudaMemsetAsync(&h->d.ctr->row_alloc[cur], 0, sizeof(unsigned int), h->stream));
     CU(cudaGetLastError());
@@ -916,46 +1046,11 @@ int dem_step(DemHandle* h, int64_t nsteps) {
         return DEM_OK;
     }
     TRY(build_graphs(h));
-    std::vector<std::pair<int, int>> upd;
-    if (h->multi) {
-        // `initialize!` of newly added scenes: one launch in which they run in
-        // Init mode and every stepping scene is held (Frozen carries its state
-        // and contacts over unchanged), so it costs them no step
-        std::vector<std::pair<int, int>> back;
-        for (int k = 0; k < h->s_cap; ++k) {
-            SceneHost& S = h->scenes[k];
-            if (S.mode == kModeStep) {
-                upd.push_back({k, kModeFrozen});
-                back.push_back({k, kModeStep});
-            } else if (S.mode == kModeInit) {
-                S.mode = kModeStep;
-                back.push_back({k, kModeStep});
-            }
-        }
-        if (back.size() > upd.size()) {
-            TRY(apply_modes(h, upd));
-            CU(cudaGraphLaunch(h->exec[h->cur], h->stream));
-            h->cur ^= 1;
-            TRY(apply_modes(h, back));
-        }
-    }
+    TRY(launch_inits(h));
     for (int64_t s = 0; s < nsteps; ++s) {
         CU(cudaGraphLaunch(h->exec[h->cur], h->stream));
         h->cur ^= 1;
-        if (!h->multi) continue;
-        // scene bookkeeping between launches (stream-ordered, no host sync)
-        upd.clear();
-        for (int k = 0; k < h->s_cap; ++k) {
-            SceneHost& S = h->scenes[k];
-            if (S.mode == kModeStep) {
-                ++S.steps;
-                if (S.target > 0 && S.steps >= S.target) {
-                    S.mode = kModeFrozen;
-                    upd.push_back({k, kModeFrozen});
-                }
-            }
-        }
-        if (!upd.empty()) TRY(apply_modes(h, upd));
+        TRY(after_launch(h));
     }
     h->steps += nsteps;
     return DEM_OK;
@@ -973,24 +1068,28 @@ int dem_step_timed(DemHandle* h, int64_t nsteps, float* ms) {
 }
 
 int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
-    if (!h || !phase_ms || nphase < 5 || h->multi) return DEM_ERR_INVALID;
+    if (!h || !phase_ms || nphase < 5) return DEM_ERR_INVALID;
     if (h->n_cap == 0) {
         for (int k = 0; k < 5; ++k) phase_ms[k] = 0.f;
         return DEM_OK;
+    }
+    if (h->multi) {
+        TRY(build_graphs(h));
+        TRY(launch_inits(h));
     }
     cudaEvent_t ev[6];
     for (int k = 0; k < 6; ++k) CU(cudaEventCreate(&ev[k]));
     const int cur = h->cur, nxt = cur ^ 1;
     cudaEventRecord(ev[0], h->stream);
-    launch_broadphase(h->d, h->p, cur, false, h->ntiles_cells, h->stream);
+    launch_broadphase(h->d, h->p, cur, h->multi, h->ntiles_cells, h->stream);
     cudaEventRecord(ev[1], h->stream);
-    launch_detect(h->d, h->p, cur, false, false, h->stream);
+    launch_detect(h->d, h->p, cur, false, h->multi, h->stream);
     cudaEventRecord(ev[2], h->stream);
-    launch_compact(h->d, h->p, cur, false, false, h->force_grid, h->stream);
+    launch_compact(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
     cudaEventRecord(ev[3], h->stream);
-    launch_force(h->d, h->p, nxt, false, h->force_grid, h->stream);
+    launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
     cudaEventRecord(ev[4], h->stream);
-    launch_integrate(h->d, h->p, cur, false, h->stream);
+    launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
     cudaEventRecord(ev[5], h->stream);
     cudaError_t e = cudaEventSynchronize(ev[5]);
     for (int k = 0; k < 5 && e == cudaSuccess; ++k)
@@ -999,6 +1098,7 @@ int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
     CU(e);
     h->cur = nxt;
     h->steps += 1;
+    TRY(after_launch(h));
     return device_error(h);
 }
 

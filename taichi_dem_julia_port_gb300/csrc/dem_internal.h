@@ -106,7 +106,9 @@ struct DemDev {
     SceneParams* sp;                      // arena: scene records; null otherwise
     SceneCounters* sctr;                  // per-scene event counters
     // broad phase
-    int4* cellinfo;        // search cell ijk + octant bits
+    int4* cellinfo;        // search cell ijk; .w = octant bits | scene index << 3
+    int4* scell;           // cellinfo in sorted order
+    int2* srow;            // (row_start, row_len) of the current buffer, sorted order
     int4* refcell;         // arena: the reference's cell ijk + octant (when grids differ)
     uint32_t* bucket;      // bucket of each particle (kNoBucket when not hashed)
     uint32_t* cell_count;  // table entries, zero between steps
@@ -132,13 +134,22 @@ struct DemDev {
 
 // Arena-wide constants (passed by value).
 struct DemParams {
-    int n;          // particle slots
+    int n;          // particle slots processed by a step (all in use lie below)
     int cap;        // contact capacity
     int kstash;     // new partners per particle per step
     int kin;        // incoming contacts per particle
-    uint32_t T;     // bucket-table entries
+    uint32_t T;     // bucket-table entries processed by a step (all in use lie below)
     int precision;  // 0 = FP64, 1 = FP32 force
     SceneParams s0; // the scene of a single-scene handle
+};
+
+// Launch shape of the grid-stride kernels (block sizes are multiples of 32 up
+// to 256; grids are upper bounds).  Results do not depend on it: every kernel
+// computes the same values for any shape.
+struct LaunchShape {
+    int force_block, force_grid;
+    int compact_block, compact_grid;
+    int integrate_block;
 };
 
 // ---- launchers (dem_kernels.cu) --------------------------------------------
@@ -150,10 +161,11 @@ void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi,
 void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
                    cudaStream_t s);
 void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
-                    int grid, cudaStream_t s);
-void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, int grid,
+                    const LaunchShape& sh, cudaStream_t s);
+void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, const LaunchShape& sh,
                   cudaStream_t s);
-void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi, cudaStream_t s);
+void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
+                      const LaunchShape& sh, cudaStream_t s);
 
 // debug: cp_list materialisation on the current bucket arrays (single scene)
 void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cudaStream_t s);

@@ -17,6 +17,8 @@
 //   k_integrate  per particle: contact force gather in a fixed order,
 //                resolve_wall!, apply_body_force!, update!
 // All of it is captured once in a CUDA graph per contact-buffer parity.
+#include <type_traits>
+
 #include "dem_device.cuh"
 
 namespace dem {
@@ -204,8 +206,9 @@ __global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p, int cu
         } else {
             const SceneParams& S = scene_rec<MULTI>(d, p, sc);
             const double pos[3] = {d.px[i], d.py[i], d.pz[i]};
-            const int4 ci = cell_of(pos, S.dmin, S.cell, S.inv_cell);
+            int4 ci = cell_of(pos, S.dmin, S.cell, S.inv_cell);
             b = bucket_of(ci.x, ci.y, ci.z, S);
+            if (MULTI) ci.w |= sc << 3;
             d.cellinfo[i] = ci;
             d.bucket[i] = b;
             if (MULTI && !S.same_grid) d.refcell[i] = cell_of(pos, S.dmin, S.cell_ref, S.inv_cell_ref);
@@ -238,10 +241,12 @@ __global__ void __launch_bounds__(kThreads) k_scatter(DemDev d, DemParams p) {
 }
 
 // Canonical order inside a bucket (ascending particle index) and the sorted
-// position copies used by the pair search.  Also clears this step's bucket
-// maximum (all its readers have finished).
+// copies the pair search reads at its own index (positions, the cell record,
+// the current contact row), so its first loads do not wait on the particle
+// index.  Also clears this step's bucket maximum (all its readers have
+// finished).
 template <bool MULTI>
-__global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p) {
+__global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p, int cur) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0) d.ctr->bmax = 0u;
     if (k >= sorted_count(d)) return;
@@ -257,6 +262,8 @@ __global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p) {
     d.spos[pos] = make_double4_32a(x, y, z, r);
     d.spos32[pos] = make_float4((float)(x - S.dmin[0]), (float)(y - S.dmin[1]),
                                 (float)(z - S.dmin[2]), (float)r);
+    d.scell[pos] = d.cellinfo[i];
+    d.srow[pos] = make_int2(d.row_start[cur][i], d.row_len[cur][i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -286,10 +293,11 @@ __device__ __forceinline__ void bucket_range(const DemDev& d, uint32_t b, uint32
 }
 
 template <bool INIT, bool MULTI>
-__global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int cur) {
+__global__ void __launch_bounds__(kThreads, 4) k_detect(DemDev d, DemParams p, int cur) {
     __shared__ int s_new[kThreads / kLanes];
     __shared__ int s_row[kThreads / kLanes][kRowCache];
     __shared__ int s_tot[kThreads / kLanes];
+    __shared__ uint32_t s_rb[kThreads / kLanes][kLanes];  // the reference's 8 octant buckets
     __shared__ int s_base;
     const int lane = threadIdx.x & (kLanes - 1);
     const int g = threadIdx.x / kLanes;
@@ -305,13 +313,13 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
     if (act) {
         const unsigned gmask = 0xffu << (lane_id() & ~7u);
         i = (int)d.sorted[k];
-        sc = slot_scene<MULTI>(d, i);
+        const int4 ci = d.scell[k];
+        const float4 P32 = d.spos32[k];
+        const int2 row = d.srow[k];
+        sc = MULTI ? (ci.w >> 3) : 0;
         const SceneParams& S = scene_rec<MULTI>(d, p, sc);
         const bool init = INIT || (MULTI && S.mode == kModeInit);
         const bool frozen = MULTI && S.mode == kModeFrozen;
-        const double4_32a P = d.spos[k];
-        const float4 P32 = d.spos32[k];
-        const int4 ci = d.cellinfo[i];
         const int dx = (ci.w & 1) ? 1 : -1, dy = (ci.w & 2) ? 1 : -1, dz = (ci.w & 4) ? 1 : -1;
         const int ox = (lane == 1 || lane == 4 || lane == 5 || lane == 7) ? dx : 0;
         const int oy = (lane == 2 || lane == 4 || lane == 6 || lane == 7) ? dy : 0;
@@ -325,22 +333,21 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
             const int rx = (rc.w & 1) ? 1 : -1, ry = (rc.w & 2) ? 1 : -1, rz = (rc.w & 4) ? 1 : -1;
             myR = ref_bucket_of(rc.x + (ox ? rx : 0), rc.y + (oy ? ry : 0), rc.z + (oz ? rz : 0), S);
         }
-        uint32_t B[8], RB[8];
+        s_rb[g][lane] = myR;
         bool dup = false;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            B[u] = __shfl_sync(gmask, myB, u, kLanes);
-            RB[u] = MULTI ? __shfl_sync(gmask, myR, u, kLanes) : B[u];
-            dup |= (u < lane) && (B[u] == myB);
+        for (int u = 0; u < 7; ++u) {
+            const uint32_t bu = __shfl_sync(gmask, myB, u, kLanes);  // every lane of the group
+            dup |= (u < lane) && (bu == myB);
         }
+        __syncwarp(gmask);
         uint32_t s, e;
         bucket_range(d, myB, d.ctr->cell_limit, &s, &e);
         if (dup || frozen) e = s;
-        const double ri = init ? d.r0[i] : P.w;
 
         const ContactSoA o = d.c[cur];
-        const int e0 = d.row_start[cur][i];
-        const int e1 = e0 + d.row_len[cur][i];
+        const int e0 = row.x;
+        const int e1 = e0 + row.y;
         const bool cached = e1 - e0 <= kRowCache;
         for (int e2 = e0 + lane; e2 < e1; e2 += kLanes) {
             const uint32_t fl = o.fl[e2];
@@ -352,6 +359,8 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
             } else if (init || frozen || (fl & kBonded)) {
                 keep = 1;
             } else {
+                // FP64 position of i reloaded where needed (keeps registers free)
+                const double4_32a P = d.spos[k];
                 const bool valid =
                     touching_rn(P.x, P.y, P.z, d.px[j], d.py[j], d.pz[j], P.w, d.r[j]);
                 uint32_t bj;
@@ -363,7 +372,7 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
                 }
                 bool in_cp = false;
 #pragma unroll
-                for (int t = 0; t < 8; ++t) in_cp |= (RB[t] == bj);
+                for (int t = 0; t < 8; ++t) in_cp |= (s_rb[g][t] == bj);
                 keep = (valid || !in_cp) ? 1 : 0;
                 ended += 1 - keep;
             }
@@ -397,7 +406,9 @@ __global__ void __launch_bounds__(kThreads) k_detect(DemDev d, DemParams p, int 
                         found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
                 }
                 if (found) continue;
+                const double4_32a P = d.spos[k];
                 const double4_32a Q = d.spos[q0 + u];
+                const double ri = init ? d.r0[i] : P.w;
                 const double rj = init ? d.r0[j] : Q.w;
                 if (!touching_rn(P.x, P.y, P.z, Q.x, Q.y, Q.z, ri, rj)) continue;
                 const int slot = atomicAdd(&s_new[g], 1);
@@ -476,7 +487,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int
             double v[15];
 #pragma unroll
             for (int f = 0; f < 15; ++f) v[f] = o.f[f][t];
-            if (!kp) continue;
+            if (!kp || i >= p.n) continue;
             // entries outside the owner's current row are left-overs of a
             // removed scene (arena) and are dropped
             const int r0 = d.row_start[cur][i];
@@ -633,6 +644,189 @@ __device__ __forceinline__ bool bond_breaks(const Vec3<double>& F, const Vec3<do
     return comp || tens || shear;
 }
 
+// Breakage decision of bond_breaks behind an FP32 screen.  The three stresses
+// σc = fa + rb/I·sqrt(amax), σt = -fa - rb/I·sqrt(amin) and
+// σs = |τᵢ₁|·rb/2/I + 4/3/A·sqrt(F₂²+F₃²) are evaluated in FP32 from the FP64
+// values; each FP32 result lies within 2^-20 (|terms| + |threshold|) of the
+// exact one, so when every stress is below its threshold by 2^-16 of that
+// scale the bond cannot break and the FP64 test is skipped.  Otherwise (and for
+// NaN or out-of-range values, which fail every comparison) the FP64 test
+// decides, so the outcome is always that of bond_breaks.
+__device__ __forceinline__ bool bond_breaks_screened(const Vec3<double>& F, const Vec3<double>& ti,
+                                                     const Vec3<double>& tj, double invA,
+                                                     double rbI, const SceneParams& p) {
+    const float tiy = (float)ti.y, tiz = (float)ti.z, tjy = (float)tj.y, tjz = (float)tj.z;
+    const float ai = tiy * tiy + tiz * tiz, aj = tjy * tjy + tjz * tjz;
+    const float rb = (float)rbI, iA = (float)invA;
+    const float fa = (float)F.x * iA;
+    const float smax = rb * sqrtf(fmaxf(ai, aj)), smin = rb * sqrtf(fminf(ai, aj));
+    const float fy = (float)F.y, fz = (float)F.z;
+    const float s1 = fabsf((float)ti.x) * 0.5f * rb, s2 = (4.0f / 3.0f) * iA * sqrtf(fy * fy + fz * fz);
+    const float sc = (float)p.b_sc, st = (float)p.b_st, ss = (float)p.b_ss;
+    const float afa = fabsf(fa);
+    const bool clear = (fa + smax + (afa + smax + fabsf(sc)) * 0x1p-16f < sc) &&
+                       (-fa - smin + (afa + smin + fabsf(st)) * 0x1p-16f < st) &&
+                       (s1 + s2 + (s1 + s2 + fabsf(ss)) * 0x1p-16f < ss);
+    if (clear) return false;
+    return bond_breaks(F, ti, tj, invA, rbI, p);
+}
+
+// FP32 contact frame (same rows as Frame), from the FP32 unit normal; the
+// degenerate branch is decided as in contact_frame, on FP64 values.
+struct Frame32 {
+    float a1, a2, a3, f;
+    bool neg3;
+};
+__device__ __forceinline__ Frame32 contact_frame32(float ax, float ay, float az, double dx,
+                                                   double dy, double dz, const SceneParams& S) {
+    const float s2 = ay * ay + az * az;
+    if (s2 < 4.0f * (float)S.tol * (float)S.tol) {
+        const double L = norm_rn(dx, dy, dz);
+        const double il = __ddiv_rn(1.0, L);
+        const Frame F = frame_exact(__dmul_rn(il, dx), __dmul_rn(il, dy), __dmul_rn(il, dz), S.tol);
+        return {(float)F.a1, (float)F.a2, (float)F.a3, (float)F.f, F.neg3};
+    }
+    return {ax, ay, az, (1.0f - ax) / s2, false};
+}
+__device__ __forceinline__ Vec3<float> rot32(const Frame32& R, Vec3<float> v) {
+    const float w = R.a2 * v.y + R.a3 * v.z;
+    const float t = v.x + R.f * w;
+    const float z = v.z - R.a3 * t;
+    return {R.a1 * v.x + w, v.y - R.a2 * t, R.neg3 ? -z : z};
+}
+__device__ __forceinline__ Vec3<float> rot_t32(const Frame32& R, Vec3<float> v) {
+    const float w = R.a2 * v.y + R.a3 * v.z;
+    const float u = v.x - R.f * w;
+    const float z = v.z + R.a3 * u;
+    return {R.a1 * v.x - w, v.y + R.a2 * u, R.neg3 ? -z : z};
+}
+
+// `resolve_collision!` in the FP32 force mode (DEM_FP32_FORCE).  Differences
+// of positions and velocities are formed in FP64 and then cast; the contact
+// frame, stiffnesses, damping and friction run in FP32.  FP64 stays for the
+// accumulated bond force and torques, the shear displacement 𝐬, the contact
+// point and the bond-breakage decision.  The Hertz overlap is
+// (L² - (rᵢ+rⱼ)²)/(L + rᵢ + rⱼ) with the numerator in FP64, which keeps the
+// overlap's relative error at FP32 rounding even though L is FP32.
+__device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
+                                        const ContactSoA& w, int c, uint32_t fl, int i, int j,
+                                        int sc, size_t cap) {
+    const double kix = d.px[i], kiy = d.py[i], kiz = d.pz[i];
+    const double dxd = d.px[j] - kix, dyd = d.py[j] - kiy, dzd = d.pz[j] - kiz;
+    const float dx = (float)dxd, dy = (float)dyd, dz = (float)dzd;
+    const float L2 = dx * dx + dy * dy + dz * dz;
+    const float invL = rsqrtf(L2);
+    const float ax = dx * invL, ay = dy * invL, az = dz * invL;
+    const Frame32 R = contact_frame32(ax, ay, az, dxd, dyd, dzd, SP);
+    const double ri = d.r[i], rj = d.r[j];
+    Vec3<float> fig, mi, mj;
+    if (fl & kBonded) {
+        // EBPM (src/kernels.jl:170-239), increments in FP32
+        const double wix = d.wx[i], wiy = d.wy[i], wiz = d.wz[i];
+        const double wjx = d.wx[j], wjy = d.wy[j], wjz = d.wz[j];
+        const Vec3<float> D = rot32(R, {(float)(d.vx[i] - d.vx[j]), (float)(d.vy[i] - d.vy[j]),
+                                        (float)(d.vz[i] - d.vz[j])});
+        const Vec3<float> Sv =
+            rot32(R, {(float)(wix + wjx), (float)(wiy + wjy), (float)(wiz + wjz)});
+        const Vec3<float> Q = rot32(R, {(float)(wix - wjx), (float)(wiy - wjy), (float)(wiz - wjz)});
+        const int small = ri <= rj ? i : j;  // rb = ρ·min(rᵢ, rⱼ)
+        const float tdt = (float)SP.dt;
+        const float phi = (float)d.b_phic[small] * invL * invL;
+        const float iphi = 1.0f / (1.0f + phi);
+        const float EILdt = (float)d.b_EI[small] * invL * tdt;
+        const float k1 = (float)d.b_EA[small] * invL * tdt;
+        const float k3 = 6.0f * EILdt * invL * iphi;
+        const float k2 = 2.0f * k3 * invL;
+        const float k4 = EILdt * (float)SP.b_inv1pnu;
+        const float kp = 3.0f * EILdt * iphi;
+        const float km = EILdt;
+        const float dFx = k1 * D.x, dFy = k2 * D.y + k3 * Sv.z, dFz = k2 * D.z - k3 * Sv.y;
+        const float ay_ = -k3 * D.z + kp * Sv.y, az_ = k3 * D.y + kp * Sv.z;
+        const float dtix = k4 * Q.x, dtiy = ay_ + km * Q.y, dtiz = az_ + km * Q.z;
+        const float dtjx = -k4 * Q.x, dtjy = ay_ - km * Q.y, dtjz = az_ - km * Q.z;
+        Vec3<double> Fi = ld3(w.f, CF, c), ti = ld3(w.f, CTI, c), tj = ld3(w.f, CTJ, c);
+        Fi = {Fi.x + (double)dFx, Fi.y + (double)dFy, Fi.z + (double)dFz};
+        ti = {ti.x + (double)dtix, ti.y + (double)dtiy, ti.z + (double)dtiz};
+        tj = {tj.x + (double)dtjx, tj.y + (double)dtjy, tj.z + (double)dtjz};
+        if (bond_breaks_screened(Fi, ti, tj, d.b_invA[small], d.b_rbI[small], SP)) {
+            w.fl[c] = 0u;
+            atomicAdd(&d.sctr[sc].broken, 1ull);
+            fig = {0.0f, 0.0f, 0.0f};
+            mi = fig;
+            mj = fig;
+        } else {
+            fig = rot_t32(R, {-(float)Fi.x, -(float)Fi.y, -(float)Fi.z});
+            mi = rot_t32(R, {-(float)ti.x, -(float)ti.y, -(float)ti.z});
+            mj = rot_t32(R, {-(float)tj.x, -(float)tj.y, -(float)tj.z});
+            st3(w.f, CK, c, {kix + 0.5 * dxd, kiy + 0.5 * dyd, kiz + 0.5 * dzd});
+            st3(w.f, CF, c, Fi);
+            st3(w.f, CTI, c, ti);
+            st3(w.f, CTJ, c, tj);
+            st3(w.f, CS, c, {0.0, 0.0, 0.0});
+        }
+    } else {
+        // Hertz-Mindlin (src/kernels.jl:240-313)
+        const double Rsum = ri + rj;
+        const double num = (dxd * dxd + dyd * dyd + dzd * dzd) - Rsum * Rsum;
+        const float L = L2 * invL;
+        const float gap = (float)num / (L + (float)Rsum);
+        if (num > 0.0) atomicAdd(&d.sctr[sc].warn_gap, 1ull);
+        const float ext = (float)ri - fabsf(gap);
+        const Vec3<float> kri{ax * ext, ay * ext, az * ext};
+        st3(w.f, CK, c, {kix + (double)kri.x, kiy + (double)kri.y, kiz + (double)kri.z});
+        const Vec3<float> krj{kri.x - dx, kri.y - dy, kri.z - dz};
+        const Vec3<float> wi{(float)d.wx[i], (float)d.wy[i], (float)d.wz[i]};
+        const Vec3<float> wj{(float)d.wx[j], (float)d.wy[j], (float)d.wz[j]};
+        const Vec3<float> wci = cross3<float>(wi, kri), wcj = cross3<float>(wj, krj);
+        const Vec3<float> dv{(float)(d.vx[j] - d.vx[i]) + (wcj.x - wci.x),
+                             (float)(d.vy[j] - d.vy[i]) + (wcj.y - wci.y),
+                             (float)(d.vz[j] - d.vz[i]) + (wcj.z - wci.z)};
+        const Vec3<float> vc = rot32(R, dv);
+        const float fri = (float)ri, frj = (float)rj, tmi = (float)d.m[i], tmj = (float)d.m[j];
+        const float Rs = fri * frj / (fri + frj);
+        const float ms = tmi * tmj / (tmi + tmj);
+        const float sq = sqrtf(Rs * fabsf(gap));
+        const float kn = (float)(4.0 / 3.0 * SP.pp_Ys) * sq;
+        const float kt = (float)(8.0 * SP.pp_Gs) * sq;
+        const float root = sqrtf(ms * sq);
+        const float gn = (float)SP.pp_cgn * root;
+        const float gt = (float)SP.pp_cgt * root;
+        if (gn < 0.0f || gt < 0.0f)
+            atomicAdd(&d.sctr[sc].warn_damp, (unsigned long long)((gn < 0.0f) + (gt < 0.0f)));
+        const double dt = SP.dt;
+        Vec3<double> s = ld3(w.f, CS, c);
+        s = {s.x + (double)vc.x * 0.0, s.y + (double)vc.y * dt, s.z + (double)vc.z * dt};
+        const float F1 = -kn * gap - gn * vc.x;
+        const Vec3<float> Ft{-kt * (float)s.x, -kt * (float)s.y, -kt * (float)s.z};
+        const float nFt = sqrtf(Ft.x * Ft.x + Ft.y * Ft.y + Ft.z * Ft.z);
+        const float muF1 = (float)SP.pp_mu * F1;
+        float F2, F3;
+        if (nFt >= muF1) {
+            const float ratio = muF1 / nFt;
+            F2 = ratio * Ft.y;
+            F3 = ratio * Ft.z;
+            s = {s.x, (double)(F2 / kt), (double)(F3 / kt)};
+        } else {
+            F2 = Ft.y - gt * vc.y;
+            F3 = Ft.z - gt * vc.z;
+        }
+        fig = rot_t32(R, {-F1, -F2, -F3});
+        mi = cross3<float>(kri, fig);
+        mj = cross3<float>(krj, {-fig.x, -fig.y, -fig.z});
+        st3(w.f, CF, c, {(double)F1, (double)F2, (double)F3});
+        st3(w.f, CS, c, s);
+    }
+    d.contrib[0 * cap + c] = (double)fig.x;
+    d.contrib[1 * cap + c] = (double)fig.y;
+    d.contrib[2 * cap + c] = (double)fig.z;
+    d.contrib[3 * cap + c] = (double)mi.x;
+    d.contrib[4 * cap + c] = (double)mi.y;
+    d.contrib[5 * cap + c] = (double)mi.z;
+    d.contrib[6 * cap + c] = (double)mj.x;
+    d.contrib[7 * cap + c] = (double)mj.y;
+    d.contrib[8 * cap + c] = (double)mj.z;
+}
+
 // `resolve_collision!` for one active contact (src/kernels.jl:136-313).  T is
 // the arithmetic type of the force model: double (DEM_FP64) or float
 // (DEM_FP32_FORCE).  Relative quantities (overlap, relative displacement and
@@ -656,6 +850,10 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
         const int sc = slot_scene<MULTI>(d, i);
         if (MULTI && (sc < 0 || d.sp[sc].mode != kModeStep)) continue;
         const SceneParams& SP = scene_rec<MULTI>(d, p, sc);
+        if constexpr (std::is_same<T, float>::value) {
+            force32(d, SP, w, c, fl, i, j, sc, cap);
+            continue;
+        }
         const double dt = SP.dt;
         const Vec3<double> ki{d.px[i], d.py[i], d.pz[i]}, kj{d.px[j], d.py[j], d.pz[j]};
         const double ri = d.r[i], rj = d.r[j];
@@ -1056,6 +1254,8 @@ __global__ void k_cp_fill(DemDev d, DemParams p, const int32_t* off, int32_t* cp
 }
 
 inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
+// block sizes of the grid-stride kernels: a multiple of 32 in [32, kThreads]
+inline int clamp_block(int b) { return b < 32 ? 32 : (b > kThreads ? kThreads : (b / 32) * 32); }
 
 }  // namespace
 
@@ -1082,8 +1282,8 @@ void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi,
         d.cell_count, d.cell_start, (long long)p.T, ntiles_cells, d.scan_state[kScanCells],
         &d.ctr->tickets[kScanCells], d.ctr);
     k_scatter<<<nb, kThreads, 0, s>>>(d, p);
-    if (multi) k_canon<true><<<nb, kThreads, 0, s>>>(d, p);
-    else k_canon<false><<<nb, kThreads, 0, s>>>(d, p);
+    if (multi) k_canon<true><<<nb, kThreads, 0, s>>>(d, p, cur);
+    else k_canon<false><<<nb, kThreads, 0, s>>>(d, p, cur);
 }
 
 void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
@@ -1095,31 +1295,36 @@ void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool
     else k_detect<false, false><<<nb, kThreads, 0, s>>>(d, p, cur);
 }
 
-void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi, int grid,
-                    cudaStream_t s) {
+void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+                    const LaunchShape& sh, cudaStream_t s) {
     if (p.n == 0) return;
-    const int nb = min(blocks_for((long long)p.cap + p.n, kThreads), grid);
-    if (multi) k_compact<false, true><<<nb, kThreads, 0, s>>>(d, p, cur);
-    else if (init) k_compact<true, false><<<nb, kThreads, 0, s>>>(d, p, cur);
-    else k_compact<false, false><<<nb, kThreads, 0, s>>>(d, p, cur);
+    const int block = clamp_block(sh.compact_block);
+    const int nb = min(blocks_for((long long)p.cap + p.n, block), max(sh.compact_grid, 1));
+    if (multi) k_compact<false, true><<<nb, block, 0, s>>>(d, p, cur);
+    else if (init) k_compact<true, false><<<nb, block, 0, s>>>(d, p, cur);
+    else k_compact<false, false><<<nb, block, 0, s>>>(d, p, cur);
 }
 
-void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, int grid,
+void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, const LaunchShape& sh,
                   cudaStream_t s) {
     if (p.n == 0 || p.cap == 0) return;
+    const int block = clamp_block(sh.force_block);
+    const int grid = min(blocks_for(p.cap, block), max(sh.force_grid, 1));
     if (p.precision == 1) {
-        if (multi) k_force<float, true><<<grid, kThreads, 0, s>>>(d, p, nxt);
-        else k_force<float, false><<<grid, kThreads, 0, s>>>(d, p, nxt);
+        if (multi) k_force<float, true><<<grid, block, 0, s>>>(d, p, nxt);
+        else k_force<float, false><<<grid, block, 0, s>>>(d, p, nxt);
     } else {
-        if (multi) k_force<double, true><<<grid, kThreads, 0, s>>>(d, p, nxt);
-        else k_force<double, false><<<grid, kThreads, 0, s>>>(d, p, nxt);
+        if (multi) k_force<double, true><<<grid, block, 0, s>>>(d, p, nxt);
+        else k_force<double, false><<<grid, block, 0, s>>>(d, p, nxt);
     }
 }
 
-void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi, cudaStream_t s) {
+void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
+                      const LaunchShape& sh, cudaStream_t s) {
     if (p.n == 0) return;
-    if (multi) k_integrate<true><<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, cur);
-    else k_integrate<false><<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, cur);
+    const int block = clamp_block(sh.integrate_block);
+    if (multi) k_integrate<true><<<blocks_for(p.n, block), block, 0, s>>>(d, p, cur);
+    else k_integrate<false><<<blocks_for(p.n, block), block, 0, s>>>(d, p, cur);
 }
 
 void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cudaStream_t s) {

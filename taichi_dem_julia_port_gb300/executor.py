@@ -68,6 +68,20 @@ def read_contacts(lib, call, where: str) -> dict:
     return out
 
 
+def get_launch_shape(lib, h) -> dict:
+    sh = _abi.DemLaunchShape()
+    check(lib, lib.dem_get_launch_shape(h, C.byref(sh)), "dem_get_launch_shape")
+    return sh.as_dict()
+
+
+def set_launch_shape(lib, h, shape: dict) -> None:
+    """Updates the given fields of the launch shape (results do not change)."""
+    cur = get_launch_shape(lib, h)
+    cur.update(shape)
+    sh = _abi.DemLaunchShape(**cur)
+    check(lib, lib.dem_set_launch_shape(h, C.byref(sh)), "dem_set_launch_shape")
+
+
 class GlobalData:
     """Device state of one scene (particles, broad phase, contacts)."""
 
@@ -116,6 +130,12 @@ class GlobalData:
         check(self.lib, self.lib.dem_set_precision(self.h, PRECISIONS[precision]),
               "dem_set_precision")
         self.precision = precision
+
+    def launch_shape(self) -> dict:
+        return get_launch_shape(self.lib, self.h)
+
+    def set_launch_shape(self, **shape) -> None:
+        set_launch_shape(self.lib, self.h, shape)
 
     def initialize(self) -> None:
         """`initialize!`: broad phase + init_bonds! (bond every cp_list pair

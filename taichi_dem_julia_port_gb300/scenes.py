@@ -8,6 +8,8 @@ definitions:
   bonded_cube(10, ...)  1,000-sphere bonded cube impact (10x10x10 lattice)
   bonded_cube(26, ...)  17,576-sphere bonded cube impact (26x26x26 lattice)
   granular_pour(n)      unbonded polydisperse pour, lognormal radii
+  mixed_batch(256)      256 independent scenes of 500-20,000 spheres, half
+                        cubes and half pours, per-scene materials
 """
 from __future__ import annotations
 
@@ -137,6 +139,38 @@ def granular_pour(n: int = 2_000_000, box=(0.4, 0.4, 1.2), seed: int = 3, median
         saving_interval_time=1000 * dt, gravity=[0.0, 0.0, -9.81],
     )
     return Scene(f"granular_pour_{n}", cfg, p, steps, False)
+
+
+def mixed_batch(count: int = 256, seed: int = 4, nmin: int = 500, nmax: int = 20_000,
+                steps: int = 10_000) -> list[Scene]:
+    """Independent scenes for batched stepping: sizes log-uniform in
+    [nmin, nmax]; even entries are bonded lattice cubes (the 1,000-sphere cube
+    impact's rules: radius 0.01 m ±5%, 10 m/s onto a plane 1 mm below,
+    dt 1e-6 s; side = round(∛n), so n becomes side³), odd entries unbonded
+    polydisperse pours (the 2,000,000-sphere pour's rules: lognormal radii,
+    median 1 mm, σ 0.25, clipped to [0.5, 2] mm, at rest in a box of the same
+    shape scaled to hold n spheres at the same density, dt 2e-7 s).  Each scene
+    draws its particle elastic modulus from U(1e7, 1e9) Pa and its friction
+    coefficient from U(0.2, 0.8)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(math.log(nmin), math.log(nmax), count))
+    E = rng.uniform(1e7, 1e9, count)
+    mu = rng.uniform(0.2, 0.8, count)
+    out = []
+    for k in range(count):
+        sub = int(rng.integers(0, 2**31 - 1))
+        if k % 2 == 0:
+            side = max(2, int(round(sizes[k] ** (1.0 / 3.0))))
+            sc = bonded_cube(side, speed=10.0, steps=steps, seed=sub, E=float(E[k]),
+                             friction=float(mu[k]))
+        else:
+            n = int(round(sizes[k]))
+            f = (n / 2_000_000) ** (1.0 / 3.0) * 1.05
+            sc = granular_pour(n, box=(0.4 * f, 0.4 * f, 1.2 * f), seed=sub, E=float(E[k]),
+                               friction=float(mu[k]), steps=steps)
+        sc.name = f"{sc.name}#{k}"
+        out.append(sc)
+    return out
 
 
 def c1(seed: int = 1) -> Scene:

@@ -174,3 +174,31 @@ def test_arena_empty_steps(gpu):
         a.step(3)
         assert a.info(s)["steps_done"] == 3
         assert_same(a, s, ref, "after empty steps")
+
+
+def test_tuning_knobs_keep_results(gpu):
+    """Launch shape and search-cell changes in the middle of a run (what the
+    autotuner does) leave every result unchanged."""
+    cube, pour = small_cube(5, seed=51), small_pour(400, seed=52)
+    refs = [alone(cube, 40), alone(pour, 40, init=False)]
+    with Arena(4096, max_scenes=4) as a:
+        ids = [a.add(cube.cfg, cube.particles), a.add(pour.cfg, pour.particles, init_bonds=False)]
+        a.step(15)
+        a.set_launch_shape(force_block=128, force_grid=152 * 4, compact_block=64,
+                           compact_grid=152 * 2, integrate_block=128)
+        a.set_cell_factor(0.4)
+        a.step(15)
+        a.set_cell_factor(0.7, scene=ids[0])
+        a.set_launch_shape(force_block=256, force_grid=152 * 32, integrate_block=256)
+        a.step(10)
+        for sid, ref, name in zip(ids, refs, ("cube", "pour")):
+            assert_same(a, sid, ref, f"retuned {name}")
+    g = GlobalData(cube.cfg, cube.particles)
+    g.initialize()
+    g.simulate(20)
+    g.set_launch_shape(force_block=96, force_grid=100, compact_grid=50, integrate_block=64)
+    g.simulate(20)
+    p, c = g.particles(), g.contacts()
+    for k in PARTICLE_KEYS:
+        np.testing.assert_array_equal(p[k], refs[0][0][k], err_msg=f"single retuned {k}")
+    np.testing.assert_array_equal(c["force"], refs[0][1]["force"])

@@ -232,6 +232,34 @@ def test_fp32_force_mode_bonded(gpu):
     assert_rows_close(pg["force"], po["force"], RTOL_FP32, "fp32 force", atol_frac=RTOL_FP32)
 
 
+def kinetic_energy(st, mass):
+    return 0.5 * float(np.sum(mass * np.sum(st["vel"] ** 2, axis=1)))
+
+
+def test_fp32_force_mode_impact_errors(gpu):
+    """FP32 force mode on a fast impact that breaks bonds, against the FP64
+    oracle: per-result errors stated in the assertions (force 1e-3 relative,
+    kinetic energy 1e-4 relative, broken-bond count within 1% of the bonds;
+    the breakage decision itself is the FP64 test)."""
+    sc = scenes.bonded_cube(6, speed=30.0, steps=0, seed=2)
+    cfg = sc.cfg.replace(bond_tensile_strength=2e5, bond_shear_strength=2e5)
+    g, o = both(cfg, sc.particles, precision="fp32")
+    g.initialize()
+    o.initialize()
+    nb0 = o.stats()["bonded"]
+    for _ in range(4):
+        g.simulate(50)
+        o.simulate(50)
+    pg, po = g.particles(), o.particles()
+    m = sc.particles.mass
+    ke_g, ke_o = kinetic_energy(pg, m), kinetic_energy(po, m)
+    assert abs(ke_g - ke_o) <= 1e-4 * ke_o, (ke_g, ke_o)
+    bg, bo = g.stats()["bonds_broken"], o.stats()["bonds_broken"]
+    assert bo > 0
+    assert abs(bg - bo) <= max(1, 0.01 * nb0), (bg, bo)
+    assert_rows_close(pg["pos"], po["pos"], 1e-6, "fp32 impact pos")
+
+
 # ---- edge cases ----------------------------------------------------------------------------
 
 def test_single_particle_on_wall(gpu):
