@@ -16,6 +16,14 @@ and reads it back (dem_get_particles).  `roofline` reports the dominant kernel
 from per-phase CUDA events (dem_step_profiled).  `cpu_baseline` times the CPU
 oracle (OpenMP, all host threads) on a bounded sample of the same workload.
 
+--workload c4 steps 256 independent scenes (500-20,000 spheres each, half
+bonded cubes, half pours, FP32 force / FP64 state) together in one arena,
+after the autotuner picks the search-cell factor and launch shape, and reports
+the same metric for the plain FP64 path run scene by scene.  The default run
+appends this comparison as `batched` (50 timed steps).  --workload c5 runs the
+served request stream (Poisson arrivals, continuous batching within an HBM
+budget) and reports aggregate particle-steps/s with p50/p99 completion latency.
+
 --impl reference times the CPU restatement of the reference step on all host
 threads (the reference's own GPU path, Julia + CUDA.jl, cannot run here).
 With N > 1 (torchrun) every rank steps an independent replica (the path does
@@ -126,6 +134,194 @@ def make_scene(name: str):
     raise ValueError(name)
 
 
+def batched_scenes(count: int):
+    from taichi_dem_julia_port_gb300 import scenes
+    batch = scenes.mixed_batch(count)
+    n = sum(s.n for s in batch)
+    desc = (f"{count} independent scenes, 500-20,000 spheres log-uniform ({n:,} total), half "
+            "bonded cubes / half unbonded pours, per-scene E U(1e7,1e9) friction U(0.2,0.8), "
+            "FP32 force / FP64 state, one arena, CUDA graph per step")
+    return batch, n, desc
+
+
+def oracle_sample(scene_list, seconds: float) -> dict:
+    """CPU oracle (all host threads) over the given scenes in turn, a few
+    steps each, for about `seconds`."""
+    from oracle.oracle import OracleScene, host_threads
+    threads = host_threads()
+    work, el, used = 0, 0.0, 0
+    per = max(seconds / max(len(scene_list), 1), 0.5)
+    for sc in scene_list:
+        o = OracleScene(sc.cfg, sc.particles, threads=threads)
+        if sc.bonded:
+            o.initialize()
+        o.simulate(1)
+        steps, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < per and steps < 2000:
+            o.simulate(1)
+            steps += 1
+        el += time.perf_counter() - t0
+        work += sc.n * steps
+        used += 1
+        if el >= seconds:
+            break
+    return {"value": work / el, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{used} scenes of the workload, {work:,} particle-steps in {el:.1f} s "
+                      "on the CPU oracle"}
+
+
+def run_batched(args, lib, quick: bool = False) -> dict:
+    """The batched workload on one arena: returns the JSON fields."""
+    import torch
+    from taichi_dem_julia_port_gb300 import Arena, GlobalData
+    from taichi_dem_julia_port_gb300.autotune import autotune
+
+    batch, n_total, desc = batched_scenes(args.scenes)
+    precision = args.precision or "fp32"
+    arena = Arena(n_total, max_scenes=len(batch), precision=precision, lib=lib)
+    for sc in batch:
+        arena.add(sc.cfg, sc.particles, init_bonds=sc.bonded)
+    arena.step(max(args.warmup, 3))
+    tune = autotune(arena, sm_count=torch.cuda.get_device_properties(0).multi_processor_count,
+                    steps=5 if quick else 10)
+    steps = min(args.steps, 50) if quick else args.steps
+    clocks = ClockSampler(torch.cuda.current_device())
+    torch.cuda.synchronize()
+    clocks.start()
+    ms = arena.step_timed(steps)  # CUDA events on the arena's stream
+    clk = clocks.stop()
+    ms_per_step = ms / steps
+    ph = arena.step_profiled()
+    stats = [arena.stats(k) for k in arena.scenes()]
+    contacts = sum(x["contacts"] for x in stats)
+    bonded = sum(x["bonded"] for x in stats)
+    errors = sorted({x["error"] for x in stats})
+    arena.close()
+    value = n_total * steps / (ms * 1e-3)
+    # the plain FP64 path, scene by scene on single-scene handles
+    plain_ms = 0.0
+    for sc in batch:
+        g = GlobalData(sc.cfg, sc.particles, precision="fp64", lib=lib)
+        if sc.bonded:
+            g.initialize()
+        g.simulate(3)
+        plain_ms += g.simulate_timed(10) / 10
+        g.close()
+    plain = n_total / (plain_ms * 1e-3)
+    peaks = load_peaks()
+    force_bytes = bonded * FORCE_BYTES_BOND + (contacts - bonded) * FORCE_BYTES_HERTZ
+    alg = {"force": force_bytes, "broadphase": n_total * BROADPHASE_BYTES_PER_PARTICLE,
+           "integrate": n_total * INTEGRATE_BYTES_PER_PARTICLE}
+    dom = max(ph, key=ph.get)
+    roof = {"bound": "hbm", "kernel": dom, "unit": "GB/s", "peak": peaks["hbm_gbs"],
+            "peak_source": peaks["source"], "traffic": None, "phase_ms": ph}
+    if dom in alg:
+        ach = alg[dom] / (ph[dom] * 1e-3) / 1e9
+        roof.update({"achieved": ach, "frac": ach / peaks["hbm_gbs"], "algorithmic_bytes": alg[dom]})
+    return {"value": value, "ms_per_step": ms_per_step, "steps": steps, "desc": desc,
+            "n_particles": n_total, "scenes": len(batch), "contacts": contacts,
+            "contact_steps_per_s": contacts * steps / (ms * 1e-3), "precision": precision,
+            "plain_fp64_scene_by_scene": plain, "speedup_vs_plain": value / plain,
+            "tune": tune.as_dict(), "roofline": roof, "clocks": clk, "errors": errors,
+            "batch": batch}
+
+
+def run_batched_e2e(args, lib, batch, steps: int) -> dict:
+    """The batched job end to end through the public API: scenes uploaded from
+    host arrays (dem_arena_add), `steps` steps, every scene's state read back."""
+    from taichi_dem_julia_port_gb300 import Arena
+    n_total = sum(s.n for s in batch)
+    h2d = sum(s.particles.volume.nbytes + s.particles.mass.nbytes + s.particles.pos.nbytes +
+              s.particles.vel.nbytes for s in batch)
+    t0 = time.perf_counter()
+    arena = Arena(n_total, max_scenes=len(batch), precision=args.precision or "fp32", lib=lib)
+    ids = [arena.add(sc.cfg, sc.particles, init_bonds=sc.bonded) for sc in batch]
+    arena.step(steps)
+    d2h = 0
+    for sid in ids:
+        st = arena.particles(sid, forces=False)
+        d2h += st["pos"].nbytes + st["vel"].nbytes
+    el = time.perf_counter() - t0
+    arena.close()
+    return {"value": n_total * steps / el, "unit": "particle-steps/s",
+            "h2d_bytes_per_step": int(h2d / steps), "d2h_bytes_per_step": int(d2h / steps),
+            "steps": steps, "note": "whole job: arena set-up and upload, steps, read-back"}
+
+
+def main_batched(args, lib, ws, rank) -> None:
+    import torch
+    r = run_batched(args, lib)
+    e2e = run_batched_e2e(args, lib, r["batch"], args.e2e_steps * 4)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = oracle_sample(r["batch"][:16], args.cpu_seconds)
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": ws * r["value"], "unit": "particle-steps/s",
+            "n_gpus": ws, "steps": r["steps"], "warmup": args.warmup,
+            "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-force/f64-state" if r["precision"] == "fp32" else "f64",
+            "data": "synthetic (seeded scenes)",
+            "config": {"workload": r["desc"], "n_particles": r["n_particles"],
+                       "scenes": r["scenes"], "contacts": r["contacts"],
+                       "contact_steps_per_s": ws * r["contact_steps_per_s"],
+                       "plain_fp64_scene_by_scene": r["plain_fp64_scene_by_scene"],
+                       "speedup_vs_plain": r["speedup_vs_plain"], "autotune": r["tune"],
+                       "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "one arena"},
+            "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": e2e, "clocks": r["clocks"],
+            "gpu_launches": KERNELS_PER_STEP * r["steps"],
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main_served(args, lib, ws, rank) -> None:
+    import torch
+    from taichi_dem_julia_port_gb300.serving import (ArenaSizing, Server, poisson_requests,
+                                                     sequential_plain)
+    reqs = poisson_requests(args.requests, rate=50.0, seed=5)
+    sizing = ArenaSizing.from_budget(args.hbm_budget_gb * 1e9)
+    clocks = ClockSampler(torch.cuda.current_device())
+    with Server(sizing, precision=args.precision or "fp32", chunk_steps=200, lib=lib,
+                keep_state=False) as srv:
+        clocks.start()
+        rep = srv.run(reqs, realtime=True)
+        clk = clocks.stop()
+    pct = rep.latency_percentiles()
+    plain = sequential_plain(reqs, lib=lib)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = oracle_sample([r.make_scene() for r in reqs[:4]], args.cpu_seconds)
+    h2d = sum(r.n * 8 * 8 for r in rep.results)  # V, m, pos, vel per particle
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": ws * rep.throughput, "unit": "particle-steps/s",
+            "n_gpus": ws, "steps": rep.launches, "warmup": 0,
+            "ms_per_step": 1e3 * rep.makespan_s / max(rep.launches, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32-force/f64-state",
+            "data": "synthetic (seeded Poisson request stream)",
+            "config": {"workload": (f"served: {len(reqs)} requests, Poisson 50/s, 1e3-1e6 spheres "
+                                    "log-uniform, 1e3-5e4 steps, mixed bonded/unbonded, "
+                                    f"{args.hbm_budget_gb:g} GB HBM budget, continuous batching"),
+                       "requests": len(reqs), "latency_p50_s": pct.get("p50"),
+                       "latency_p99_s": pct.get("p99"), "makespan_s": rep.makespan_s,
+                       "particle_steps": rep.particle_steps,
+                       "admissions_deferred": rep.admissions_deferred,
+                       "arena_slots": sizing.max_particles,
+                       "plain_fp64_scene_by_scene": plain,
+                       "speedup_vs_plain": rep.throughput / plain["particle_steps_per_s"],
+                       "l2": "inputs larger than L2 (no flush)", "parallelism": "one arena"},
+            "roofline": None, "cpu_baseline": cpu,
+            "e2e": {"value": ws * rep.throughput, "unit": "particle-steps/s",
+                    "h2d_bytes_per_step": int(h2d / max(rep.launches, 1)),
+                    "d2h_bytes_per_step": 0,
+                    "note": "the served loop is end to end: uploads at admission, device-side "
+                            "completion, host bookkeeping; results are step counts and stats"},
+            "clocks": clk, "gpu_launches": KERNELS_PER_STEP * rep.launches,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -138,6 +334,31 @@ def run_reference(args) -> None:
     if rank != 0:
         return
     from oracle.oracle import OracleScene, host_threads
+    if args.workload in ("c4", "c5"):
+        if args.workload == "c4":
+            scs, _, desc = batched_scenes(args.scenes)
+        else:
+            from taichi_dem_julia_port_gb300.serving import poisson_requests
+            scs = [r.make_scene() for r in poisson_requests(args.requests, seed=5)[:4]]
+            desc = f"served request stream ({args.requests} requests), first 4 scenes"
+        t_all = time.perf_counter()
+        cpu = oracle_sample(scs, max(10.0, 0.5 * args.steps))
+        value = cpu["value"]
+        line = {
+            "impl": "reference", "metric": "particle-steps/s", "value": value,
+            "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded scenes)",
+            "config": {"workload": desc, "parallelism": "cpu-openmp, scenes in turn",
+                       "wall_s": time.perf_counter() - t_all},
+            "cpu_baseline": cpu,
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "CPU restatement of the reference step on a bounded sample of the scenes",
+        }
+        print(json.dumps(line), flush=True)
+        return
     sc, desc = make_scene(args.workload)
     threads = host_threads()
     o = OracleScene(sc.cfg, sc.particles, threads=threads)
@@ -191,7 +412,12 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--scenes", type=int, default=256, help="c4: number of scenes")
+    ap.add_argument("--requests", type=int, default=12, help="c5: number of requests")
+    ap.add_argument("--hbm-budget-gb", type=float, default=160.0, help="c5: arena budget")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="default workload: skip the batched summary")
     ap.add_argument("--precision", default=None, choices=["fp64", "fp32"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--e2e-steps", type=int, default=50)
@@ -216,6 +442,16 @@ def main() -> None:
 
     lib = _abi.load_library()
     _abi.check(lib, lib.dem_set_device(local), "dem_set_device")
+    if args.workload == "c4":
+        main_batched(args, lib, ws, rank)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload == "c5":
+        main_served(args, lib, ws, rank)
+        if dist:
+            dist.destroy_process_group()
+        return
     sc, desc = make_scene(args.workload)
     precision = args.precision or ("fp32" if args.workload == "c3" else "fp64")
     g = GlobalData(sc.cfg, sc.particles, precision=precision)
@@ -304,6 +540,15 @@ def main() -> None:
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, args.cpu_seconds)
+    batched = None
+    if args.workload == "c2" and not args.no_batched:
+        g.close()
+        r = run_batched(args, lib, quick=True)
+        batched = {k: r[k] for k in ("desc", "value", "ms_per_step", "steps", "n_particles",
+                                     "contact_steps_per_s", "plain_fp64_scene_by_scene",
+                                     "speedup_vs_plain", "precision", "tune")}
+        batched["phase_ms"] = r["roofline"]["phase_ms"]
+        batched["metric"] = "particle-steps/s"
     if rank == 0:
         line = {
             "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
@@ -319,6 +564,8 @@ def main() -> None:
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": KERNELS_PER_STEP * args.steps,
         }
+        if batched:
+            line["batched"] = batched
         print(json.dumps(line), flush=True)
     g.close()
     if dist:

@@ -128,3 +128,18 @@ def test_granular_pour_no_overlap():
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(FileNotFoundError):
         _abi.load_library(tmp_path / "libdem_sm100a.so")
+
+
+def test_serving_sizing_and_requests():
+    from taichi_dem_julia_port_gb300.serving import ArenaSizing, poisson_requests
+    s = ArenaSizing.from_budget(160e9)
+    assert 160e9 * 0.95 < s.bytes <= 160e9
+    assert s.max_contacts == s.max_particles * s.contacts_per_particle
+    a, b = poisson_requests(50, seed=9), poisson_requests(50, seed=9)
+    assert [(r.arrival_s, r.steps, r.n_hint) for r in a] == [(r.arrival_s, r.steps, r.n_hint) for r in b]
+    gaps = np.diff([0.0] + [r.arrival_s for r in a])
+    assert 0.005 < gaps.mean() < 0.05  # mean 1/50 s
+    assert all(1_000 <= r.steps <= 50_000 for r in a)
+    assert all(900 <= r.n_hint <= 1_000_000 for r in a)
+    sc = a[1].scene()
+    assert not sc.bonded and abs(sc.n - a[1].n_hint) == 0
