@@ -182,8 +182,10 @@ def run_batched(args, lib, quick: bool = False) -> dict:
     for sc in batch:
         arena.add(sc.cfg, sc.particles, init_bonds=sc.bonded)
     arena.step(max(args.warmup, 3))
-    tune = autotune(arena, sm_count=torch.cuda.get_device_properties(0).multi_processor_count,
-                    steps=5 if quick else 10)
+    tune = None
+    if not getattr(args, "no_tune", False):
+        tune = autotune(arena, sm_count=torch.cuda.get_device_properties(0).multi_processor_count,
+                        steps=5 if quick else 10)
     steps = min(args.steps, 50) if quick else args.steps
     clocks = ClockSampler(torch.cuda.current_device())
     torch.cuda.synchronize()
@@ -200,14 +202,14 @@ def run_batched(args, lib, quick: bool = False) -> dict:
     value = n_total * steps / (ms * 1e-3)
     # the plain FP64 path, scene by scene on single-scene handles
     plain_ms = 0.0
-    for sc in batch:
+    for sc in ([] if getattr(args, "no_plain", False) else batch):
         g = GlobalData(sc.cfg, sc.particles, precision="fp64", lib=lib)
         if sc.bonded:
             g.initialize()
         g.simulate(3)
         plain_ms += g.simulate_timed(10) / 10
         g.close()
-    plain = n_total / (plain_ms * 1e-3)
+    plain = n_total / (plain_ms * 1e-3) if plain_ms > 0 else None
     peaks = load_peaks()
     force_bytes = bonded * FORCE_BYTES_BOND + (contacts - bonded) * FORCE_BYTES_HERTZ
     alg = {"force": force_bytes, "broadphase": n_total * BROADPHASE_BYTES_PER_PARTICLE,
@@ -221,8 +223,9 @@ def run_batched(args, lib, quick: bool = False) -> dict:
     return {"value": value, "ms_per_step": ms_per_step, "steps": steps, "desc": desc,
             "n_particles": n_total, "scenes": len(batch), "contacts": contacts,
             "contact_steps_per_s": contacts * steps / (ms * 1e-3), "precision": precision,
-            "plain_fp64_scene_by_scene": plain, "speedup_vs_plain": value / plain,
-            "tune": tune.as_dict(), "roofline": roof, "clocks": clk, "errors": errors,
+            "plain_fp64_scene_by_scene": plain,
+            "speedup_vs_plain": value / plain if plain else None,
+            "tune": tune.as_dict() if tune else None, "roofline": roof, "clocks": clk, "errors": errors,
             "batch": batch}
 
 
@@ -418,6 +421,9 @@ def main() -> None:
     ap.add_argument("--hbm-budget-gb", type=float, default=160.0, help="c5: arena budget")
     ap.add_argument("--no-batched", action="store_true",
                     help="default workload: skip the batched summary")
+    ap.add_argument("--no-tune", action="store_true", help="c4: keep the default launch shape")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="c4: skip the scene-by-scene plain-path comparison")
     ap.add_argument("--precision", default=None, choices=["fp64", "fp32"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--e2e-steps", type=int, default=50)

@@ -219,7 +219,7 @@ typedef struct DemLaunchShape {
     int32_t compact_block;
     int32_t compact_grid;
     int32_t integrate_block;
-    int32_t pad;
+    int32_t detect_blocks_per_sm; /* register budget of the pair search: 3 or 4 (0 = 4) */
 } DemLaunchShape;
 
 int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* shape);

@@ -9,7 +9,8 @@ for any launch shape; the arena tests check both bit for bit.  The steps taken
 while tuning are ordinary simulation steps.
 
 The search is coordinate descent: cell factor first, then the force kernel's
-block and grid, then the compaction grid, then the integration block; each
+block and grid, then the compaction grid, the integration block and the
+pair search's register budget; each
 candidate is timed over `steps` steps after one untimed step.
 """
 from __future__ import annotations
@@ -20,6 +21,7 @@ CELL_FACTORS = (1.0, 0.8, 0.6, 0.45, 0.35)
 BLOCKS = (128, 256)
 GRIDS_PER_SM = (4, 8, 16, 32)
 INTEGRATE_BLOCKS = (128, 256)
+DETECT_BLOCKS = (3, 4)  # pair-search register budget (blocks per SM)
 
 
 @dataclass
@@ -43,7 +45,7 @@ def _time(target, steps: int) -> float:
 
 def autotune(target, sm_count: int = 152, steps: int = 10, cell_factors=CELL_FACTORS,
              blocks=BLOCKS, grids_per_sm=GRIDS_PER_SM,
-             integrate_blocks=INTEGRATE_BLOCKS) -> TuneResult:
+             integrate_blocks=INTEGRATE_BLOCKS, detect_blocks=DETECT_BLOCKS) -> TuneResult:
     """Tunes `target` in place and returns the chosen settings."""
     trials = []
     is_arena = hasattr(target, "set_cell_factor")
@@ -77,6 +79,13 @@ def autotune(target, sm_count: int = 152, steps: int = 10, cell_factors=CELL_FAC
             best, shape = t, cand
     for ib in integrate_blocks:
         cand = dict(shape, integrate_block=ib)
+        target.set_launch_shape(**cand)
+        t = _time(target, steps)
+        trials.append((cand, t))
+        if t < best:
+            best, shape = t, cand
+    for db in detect_blocks:
+        cand = dict(shape, detect_blocks_per_sm=db)
         target.set_launch_shape(**cand)
         t = _time(target, steps)
         trials.append((cand, t))

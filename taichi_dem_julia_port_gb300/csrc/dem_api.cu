@@ -268,6 +268,17 @@ int prepare_scene(const DemConfigC* cfg, const DemParticlesIn* pin, double cell_
     p.pw_Gs = pw.Gs;
     p.pw_cgn = pw.cgn;
     p.pw_cgt = pw.cgt;
+    p.f_dt = (float)p.dt;
+    p.f_inv1pnu = (float)p.b_inv1pnu;
+    p.f_sc = (float)p.b_sc;
+    p.f_st = (float)p.b_st;
+    p.f_ss = (float)p.b_ss;
+    p.f_mu = (float)p.pp_mu;
+    p.f_kn = (float)(4.0 / 3.0 * p.pp_Ys);
+    p.f_kt = (float)(8.0 * p.pp_Gs);
+    p.f_cgn = (float)p.pp_cgn;
+    p.f_cgt = (float)p.pp_cgt;
+    p.f_tol4 = (float)(4.0 * p.tol * p.tol);
     return DEM_OK;
 }
 
@@ -388,6 +399,9 @@ int allocate(DemHandle* h) {
     TRY(dalloc(h, &d.in_cnt, n));
     TRY(dalloc(h, &d.in_list, n * (size_t)h->p.kin));
     TRY(dalloc(h, &d.contrib, 9 * cap));
+    TRY(dalloc(h, &d.contrib32, 9 * cap));
+    TRY(dalloc(h, &d.bk32, n));
+    TRY(dalloc(h, &d.rm32, n));
     TRY(dalloc(h, &d.scan_state[kScanCells], (size_t)scan_tiles((int64_t)T)));
     TRY(dalloc(h, &d.scan_state[kScanDebug], (size_t)scan_tiles((int64_t)n)));
     TRY(dalloc(h, &d.ctr, 1));
@@ -419,7 +433,7 @@ int init_handle(DemHandle* h) {
     CU(cudaEventCreate(&h->ev1));
     TRY(allocate(h));
     h->ntiles_cells = std::max(1, scan_tiles((int64_t)h->p.T));
-    h->shape = LaunchShape{256, h->sm_count * 16, 256, h->sm_count * 16, 256};
+    h->shape = LaunchShape{256, h->sm_count * 16, 256, h->sm_count * 16, 256, 4};
     return DEM_OK;
 }
 
@@ -453,6 +467,17 @@ int upload_scene(DemHandle* h, const SceneArrays& A, int64_t p0) {
     for (const auto& c : cols) CU(up(c.first, *c.second));
     std::vector<double> one(n, 1.0);
     CU(up(d.qw, one));
+    std::vector<float4> bk(n);
+    std::vector<float2> rm(n);
+    for (size_t i = 0; i < n; ++i) {
+        bk[i] = make_float4((float)A.b_phic[i], (float)A.b_EI[i], (float)A.b_EA[i],
+                            (float)A.b_invA[i]);
+        rm[i] = make_float2((float)A.b_rbI[i], (float)A.m[i]);
+    }
+    CU(cudaMemcpyAsync(d.bk32 + p0, bk.data(), n * sizeof(float4), cudaMemcpyHostToDevice,
+                       h->stream));
+    CU(cudaMemcpyAsync(d.rm32 + p0, rm.data(), n * sizeof(float2), cudaMemcpyHostToDevice,
+                       h->stream));
     for (double* z : {d.wx, d.wy, d.wz, d.qx, d.qy, d.qz, d.wsx, d.wsy, d.wsz, d.fx, d.fy, d.fz,
                       d.tx, d.ty, d.tz})
         CU(cudaMemsetAsync(z + p0, 0, n * sizeof(double), h->stream));
@@ -464,7 +489,7 @@ int upload_scene(DemHandle* h, const SceneArrays& A, int64_t p0) {
 void record_step(DemHandle* h, int cur) {
     const int nxt = cur ^ 1;
     launch_broadphase(h->d, h->p, cur, h->multi, h->ntiles_cells, h->stream);
-    launch_detect(h->d, h->p, cur, false, h->multi, h->stream);
+    launch_detect(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
     launch_compact(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
     launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
     launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
@@ -981,12 +1006,15 @@ int dem_arena_set_cell_factor(DemHandle* h, int32_t s, double f) {
 
 int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* sh) {
     if (!h || !sh || sh->force_block < 32 || sh->force_block > 256 || sh->force_block % 32 ||
+        (sh->detect_blocks_per_sm != 0 && sh->detect_blocks_per_sm != 3 &&
+         sh->detect_blocks_per_sm != 4) ||
         sh->compact_block < 32 || sh->compact_block > 256 || sh->compact_block % 32 ||
         sh->integrate_block < 32 || sh->integrate_block > 256 || sh->integrate_block % 32 ||
         sh->force_grid < 1 || sh->compact_grid < 1)
         return DEM_ERR_INVALID;
     h->shape = LaunchShape{sh->force_block, sh->force_grid, sh->compact_block, sh->compact_grid,
-                           sh->integrate_block};
+                           sh->integrate_block,
+                           sh->detect_blocks_per_sm ? sh->detect_blocks_per_sm : 4};
     drop_graphs(h);
     return DEM_OK;
 }
@@ -994,7 +1022,8 @@ int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* sh) {
 int dem_get_launch_shape(DemHandle* h, DemLaunchShape* out) {
     if (!h || !out) return DEM_ERR_INVALID;
     *out = DemLaunchShape{h->shape.force_block, h->shape.force_grid, h->shape.compact_block,
-                          h->shape.compact_grid, h->shape.integrate_block, 0};
+                          h->shape.compact_grid, h->shape.integrate_block,
+                          h->shape.detect_blocks_per_sm};
     return DEM_OK;
 }
 
@@ -1030,7 +1059,7 @@ int dem_init_bonds(DemHandle* h) {
     if (h->n_cap == 0) return DEM_OK;
     const int cur = h->cur, nxt = cur ^ 1;
     launch_broadphase(h->d, h->p, cur, false, h->ntiles_cells, h->stream);
-    launch_detect(h->d, h->p, cur, true, false, h->stream);
+    launch_detect(h->d, h->p, cur, true, false, h->shape, h->stream);
     launch_compact(h->d, h->p, cur, true, false, h->shape, h->stream);
     // the old buffer becomes the next step's target: its allocator starts at 0
     CU(cudaMemsetAsync(&h->d.ctr->row_alloc[cur], 0, sizeof(unsigned int), h->stream));
@@ -1083,7 +1112,7 @@ int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
     cudaEventRecord(ev[0], h->stream);
     launch_broadphase(h->d, h->p, cur, h->multi, h->ntiles_cells, h->stream);
     cudaEventRecord(ev[1], h->stream);
-    launch_detect(h->d, h->p, cur, false, h->multi, h->stream);
+    launch_detect(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
     cudaEventRecord(ev[2], h->stream);
     launch_compact(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
     cudaEventRecord(ev[3], h->stream);

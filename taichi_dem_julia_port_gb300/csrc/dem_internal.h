@@ -73,6 +73,10 @@ struct SceneParams {
     double wn[3], wd;
     double wR[9], wRinv[9];  // contact frame of the wall and its inverse
     double pw_mu, pw_Ys, pw_Gs, pw_cgn, pw_cgt;
+    // FP32 copies for the FP32 force mode (no conversions in the force kernel)
+    float f_dt, f_inv1pnu, f_sc, f_st, f_ss;
+    float f_mu, f_kn, f_kt, f_cgn, f_cgt;  // μ, 4/3·Y*, 8·G*, cgn, cgt (particle-particle)
+    float f_tol4;                          // 4·tolerance² (degenerate frame test)
 };
 
 struct SceneCounters {
@@ -100,6 +104,8 @@ struct DemDev {
     double *m, *inv_m, *r, *r0, *inv_inertia;
     double *b_invA, *b_rbI;        // bond section constants for rb = ρ·r (1/A, rb/I)
     double *b_EA, *b_EI, *b_phic;  // E·A, E·I and 20/3·(1+ν)·rb² for rb = ρ·r
+    float4* bk32;                  // FP32 (b_phic, b_EI, b_EA, b_invA)
+    float2* rm32;                  // FP32 (b_rbI, m)
     double *fx, *fy, *fz, *tx, *ty, *tz;  // totals of the last step
     double *wsx, *wsy, *wsz;              // wall shear history (one wall)
     int32_t* scene_of;                    // arena: scene of each slot (-1 free); null otherwise
@@ -127,6 +133,7 @@ struct DemDev {
     int32_t* in_cnt;      // zero between steps
     int2* in_list;        // n * kin: (contact slot, owner i) of contacts where the particle is j
     double* contrib;      // 9 * cap, [field][contact]
+    float* contrib32;     // 9 * cap, the FP32 force mode's contributions
     // scan scratch: tile states of each scan site
     unsigned long long* scan_state[2];
     DevCounters* ctr;
@@ -150,6 +157,7 @@ struct LaunchShape {
     int force_block, force_grid;
     int compact_block, compact_grid;
     int integrate_block;
+    int detect_blocks_per_sm;  // register budget of the pair search: 3 or 4 blocks per SM
 };
 
 // ---- launchers (dem_kernels.cu) --------------------------------------------
@@ -159,7 +167,7 @@ struct LaunchShape {
 void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi,
                        int n_scan_tiles_cells, cudaStream_t s);
 void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
-                   cudaStream_t s);
+                   const LaunchShape& sh, cudaStream_t s);
 void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
                     const LaunchShape& sh, cudaStream_t s);
 void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, const LaunchShape& sh,

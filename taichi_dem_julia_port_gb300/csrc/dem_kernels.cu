@@ -292,179 +292,193 @@ __device__ __forceinline__ void bucket_range(const DemDev& d, uint32_t b, uint32
     }
 }
 
-template <bool INIT, bool MULTI>
-__global__ void __launch_bounds__(kThreads, 4) k_detect(DemDev d, DemParams p, int cur) {
+template <bool INIT, bool MULTI, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p, int cur) {
     __shared__ int s_new[kThreads / kLanes];
     __shared__ int s_row[kThreads / kLanes][kRowCache];
-    __shared__ int s_tot[kThreads / kLanes];
     __shared__ uint32_t s_rb[kThreads / kLanes][kLanes];  // the reference's 8 octant buckets
-    __shared__ int s_base;
+    __shared__ int2 s_seg[kThreads / kLanes][kLanes];     // (first sorted slot, prefix) per bucket
     const int lane = threadIdx.x & (kLanes - 1);
     const int g = threadIdx.x / kLanes;
     const int k = blockIdx.x * (kThreads / kLanes) + g;
     const int nxt = cur ^ 1;
-    if (lane == 0) {
-        s_new[g] = 0;
-        s_tot[g] = 0;
+    if (k >= sorted_count(d)) return;  // whole 8-lane groups leave together
+    const unsigned gmask = 0xffu << (lane_id() & ~7u);
+    if (lane == 0) s_new[g] = 0;
+    const int i = (int)d.sorted[k];
+    const int4 ci = d.scell[k];
+    const float4 P32 = d.spos32[k];
+    const int2 row = d.srow[k];
+    const int sc = MULTI ? (ci.w >> 3) : 0;
+    const SceneParams& S = scene_rec<MULTI>(d, p, sc);
+    const bool init = INIT || (MULTI && S.mode == kModeInit);
+    const bool frozen = MULTI && S.mode == kModeFrozen;
+    const int dx = (ci.w & 1) ? 1 : -1, dy = (ci.w & 2) ? 1 : -1, dz = (ci.w & 4) ? 1 : -1;
+    const int ox = (lane == 1 || lane == 4 || lane == 5 || lane == 7) ? dx : 0;
+    const int oy = (lane == 2 || lane == 4 || lane == 6 || lane == 7) ? dy : 0;
+    const int oz = (lane == 3 || lane == 5 || lane == 6 || lane == 7) ? dz : 0;
+    const uint32_t myB = bucket_of(ci.x + ox, ci.y + oy, ci.z + oz, S);
+    // the reference's buckets decide cp_list membership (equal to the search
+    // buckets for a single-scene handle)
+    uint32_t myR = myB;
+    if (MULTI) {
+        const int4 rc = S.same_grid ? ci : d.refcell[i];
+        const int rx = (rc.w & 1) ? 1 : -1, ry = (rc.w & 2) ? 1 : -1, rz = (rc.w & 4) ? 1 : -1;
+        myR = ref_bucket_of(rc.x + (ox ? rx : 0), rc.y + (oy ? ry : 0), rc.z + (oz ? rz : 0), S);
     }
-    __syncwarp();
-    const bool act = k < sorted_count(d);
-    int i = 0, nkeep = 0, ended = 0, sc = 0;
-    if (act) {
-        const unsigned gmask = 0xffu << (lane_id() & ~7u);
-        i = (int)d.sorted[k];
-        const int4 ci = d.scell[k];
-        const float4 P32 = d.spos32[k];
-        const int2 row = d.srow[k];
-        sc = MULTI ? (ci.w >> 3) : 0;
-        const SceneParams& S = scene_rec<MULTI>(d, p, sc);
-        const bool init = INIT || (MULTI && S.mode == kModeInit);
-        const bool frozen = MULTI && S.mode == kModeFrozen;
-        const int dx = (ci.w & 1) ? 1 : -1, dy = (ci.w & 2) ? 1 : -1, dz = (ci.w & 4) ? 1 : -1;
-        const int ox = (lane == 1 || lane == 4 || lane == 5 || lane == 7) ? dx : 0;
-        const int oy = (lane == 2 || lane == 4 || lane == 6 || lane == 7) ? dy : 0;
-        const int oz = (lane == 3 || lane == 5 || lane == 6 || lane == 7) ? dz : 0;
-        const uint32_t myB = bucket_of(ci.x + ox, ci.y + oy, ci.z + oz, S);
-        // the reference's buckets decide cp_list membership (equal to the
-        // search buckets for a single-scene handle)
-        uint32_t myR = myB;
-        if (MULTI) {
-            const int4 rc = S.same_grid ? ci : d.refcell[i];
-            const int rx = (rc.w & 1) ? 1 : -1, ry = (rc.w & 2) ? 1 : -1, rz = (rc.w & 4) ? 1 : -1;
-            myR = ref_bucket_of(rc.x + (ox ? rx : 0), rc.y + (oy ? ry : 0), rc.z + (oz ? rz : 0), S);
-        }
-        s_rb[g][lane] = myR;
-        bool dup = false;
+    bool dup = false;
 #pragma unroll
-        for (int u = 0; u < 7; ++u) {
-            const uint32_t bu = __shfl_sync(gmask, myB, u, kLanes);  // every lane of the group
-            dup |= (u < lane) && (bu == myB);
-        }
-        __syncwarp(gmask);
-        uint32_t s, e;
-        bucket_range(d, myB, d.ctr->cell_limit, &s, &e);
-        if (dup || frozen) e = s;
+    for (int u = 0; u < 7; ++u) {
+        const uint32_t bu = __shfl_sync(gmask, myB, u, kLanes);  // every lane of the group
+        dup |= (u < lane) && (bu == myB);
+    }
+    uint32_t s, e;
+    bucket_range(d, myB, d.ctr->cell_limit, &s, &e);
+    if (dup || frozen) e = s;
+    // the group's candidates: the concatenation of its 8 bucket ranges
+    const int cnt = (int)(e - s);
+    int incl = cnt;
+#pragma unroll
+    for (int o2 = 1; o2 < kLanes; o2 <<= 1) {
+        const int y = __shfl_up_sync(gmask, incl, o2, kLanes);
+        if (lane >= o2) incl += y;
+    }
+    const int total = __shfl_sync(gmask, incl, kLanes - 1, kLanes);
+    s_rb[g][lane] = myR;
+    s_seg[g][lane] = make_int2((int)s, incl - cnt);
+    __syncwarp(gmask);
 
-        const ContactSoA o = d.c[cur];
-        const int e0 = row.x;
-        const int e1 = e0 + row.y;
-        const bool cached = e1 - e0 <= kRowCache;
-        for (int e2 = e0 + lane; e2 < e1; e2 += kLanes) {
-            const uint32_t fl = o.fl[e2];
-            const int j = o.cj[e2];
-            if (cached) s_row[g][e2 - e0] = (fl & kActive) ? j : -1;
-            int keep;
-            if (!(fl & kActive)) {
-                keep = 0;
-            } else if (init || frozen || (fl & kBonded)) {
-                keep = 1;
+    // existing row: survival (update_contacts!, src/kernels.jl:87-101)
+    const ContactSoA o = d.c[cur];
+    const int e0 = row.x;
+    const int e1 = e0 + row.y;
+    const bool cached = e1 - e0 <= kRowCache;
+    int nkeep = 0, ended = 0;
+    for (int e2 = e0 + lane; e2 < e1; e2 += kLanes) {
+        const uint32_t fl = o.fl[e2];
+        const int j = o.cj[e2];
+        if (cached) s_row[g][e2 - e0] = (fl & kActive) ? j : -1;
+        int keep;
+        if (!(fl & kActive)) {
+            keep = 0;
+        } else if (init || frozen || (fl & kBonded)) {
+            keep = 1;
+        } else {
+            // FP64 position of i reloaded where needed (keeps registers free)
+            const double4_32a P = d.spos[k];
+            const bool valid = touching_rn(P.x, P.y, P.z, d.px[j], d.py[j], d.pz[j], P.w, d.r[j]);
+            uint32_t bj;
+            if (MULTI) {
+                const int4 cj4 = S.same_grid ? d.cellinfo[j] : d.refcell[j];
+                bj = ref_bucket_of(cj4.x, cj4.y, cj4.z, S);
             } else {
-                // FP64 position of i reloaded where needed (keeps registers free)
-                const double4_32a P = d.spos[k];
-                const bool valid =
-                    touching_rn(P.x, P.y, P.z, d.px[j], d.py[j], d.pz[j], P.w, d.r[j]);
-                uint32_t bj;
-                if (MULTI) {
-                    const int4 cj4 = S.same_grid ? d.cellinfo[j] : d.refcell[j];
-                    bj = ref_bucket_of(cj4.x, cj4.y, cj4.z, S);
-                } else {
-                    bj = d.bucket[j];
-                }
-                bool in_cp = false;
-#pragma unroll
-                for (int t = 0; t < 8; ++t) in_cp |= (s_rb[g][t] == bj);
-                keep = (valid || !in_cp) ? 1 : 0;
-                ended += 1 - keep;
+                bj = d.bucket[j];
             }
-            d.keep[e2] = (uint8_t)keep;
-            nkeep += keep;
+            bool in_cp = false;
+#pragma unroll
+            for (int t = 0; t < 8; ++t) in_cp |= (s_rb[g][t] == bj);
+            keep = (valid || !in_cp) ? 1 : 0;
+            ended += 1 - keep;
         }
-        nkeep = __reduce_add_sync(gmask, nkeep);
-        ended = __reduce_add_sync(gmask, ended);
-        __syncwarp(gmask);
+        d.keep[e2] = (uint8_t)keep;
+        nkeep += keep;
+    }
+    nkeep = __reduce_add_sync(gmask, nkeep);
+    ended = __reduce_add_sync(gmask, ended);
+    __syncwarp(gmask);
 
-        int32_t* stash = d.stash + (size_t)i * p.kstash;
-        for (uint32_t q0 = s; q0 < e; q0 += kBatch) {
-            int jj[kBatch];
-            float4 qq[kBatch];
+    // new contacts: lane t takes candidates t, t+8, ... of the concatenation,
+    // so the group's lanes share the work evenly and read consecutive slots
+    int32_t* stash = d.stash + (size_t)i * p.kstash;
+    int seg = 0;
+    for (int c0 = 0; c0 < total; c0 += kLanes * kBatch) {
+        int jj[kBatch], qi[kBatch];
+        float4 qq[kBatch];
 #pragma unroll
-            for (int u = 0; u < kBatch; ++u) {
-                const uint32_t q = q0 + u;
-                jj[u] = q < e ? (int)d.sorted[q] : -1;
-                qq[u] = q < e ? d.spos32[q] : P32;
-            }
-#pragma unroll
-            for (int u = 0; u < kBatch; ++u) {
-                const int j = jj[u];
-                if (j <= i) continue;
-                if (!init && !maybe_touching32(P32, qq[u])) continue;
-                bool found = false;
-                if (cached) {
-                    for (int t = 0; t < e1 - e0 && !found; ++t) found = s_row[g][t] == j;
-                } else {
-                    for (int e2 = e0; e2 < e1 && !found; ++e2)
-                        found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
-                }
-                if (found) continue;
-                const double4_32a P = d.spos[k];
-                const double4_32a Q = d.spos[q0 + u];
-                const double ri = init ? d.r0[i] : P.w;
-                const double rj = init ? d.r0[j] : Q.w;
-                if (!touching_rn(P.x, P.y, P.z, Q.x, Q.y, Q.z, ri, rj)) continue;
-                const int slot = atomicAdd(&s_new[g], 1);
-                if (slot < p.kstash) stash[slot] = j;
+        for (int u = 0; u < kBatch; ++u) {
+            const int c = c0 + u * kLanes + lane;
+            jj[u] = -1;
+            qi[u] = 0;
+            qq[u] = P32;
+            if (c < total) {
+                while (seg + 1 < kLanes && s_seg[g][seg + 1].y <= c) ++seg;
+                const int q = s_seg[g][seg].x + (c - s_seg[g][seg].y);
+                qi[u] = q;
+                jj[u] = (int)d.sorted[q];
+                qq[u] = d.spos32[q];
             }
         }
-        __syncwarp(gmask);
-        if (lane == 0) {
-            int nnew = s_new[g];
-            if (nnew > p.kstash) {
-                raise_error(d.ctr, kErrCapacity);
-                nnew = p.kstash;
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+            const int j = jj[u];
+            if (j <= i) continue;
+            if (!init && !maybe_touching32(P32, qq[u])) continue;
+            bool found = false;
+            if (cached) {
+                for (int t = 0; t < e1 - e0 && !found; ++t) found = s_row[g][t] == j;
+            } else {
+                for (int e2 = e0; e2 < e1 && !found; ++e2)
+                    found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
             }
-            for (int a2 = 1; a2 < nnew; ++a2) {  // new partners ascending
-                const int v = stash[a2];
-                int b2 = a2 - 1;
-                while (b2 >= 0 && stash[b2] > v) {
-                    stash[b2 + 1] = stash[b2];
-                    --b2;
-                }
-                stash[b2 + 1] = v;
-            }
-            d.nnew[i] = nnew;
-            s_new[g] = nnew;
-            s_tot[g] = nkeep + nnew;
-            if (ended) atomicAdd(&d.sctr[sc].ended, (unsigned long long)ended);
-            if (!init && nnew) atomicAdd(&d.sctr[sc].created, (unsigned long long)nnew);
+            if (found) continue;
+            const double4_32a P = d.spos[k];
+            const double4_32a Q = d.spos[qi[u]];
+            const double ri = init ? d.r0[i] : P.w;
+            const double rj = init ? d.r0[j] : Q.w;
+            if (!touching_rn(P.x, P.y, P.z, Q.x, Q.y, Q.z, ri, rj)) continue;
+            const int slot = atomicAdd(&s_new[g], 1);
+            if (slot < p.kstash) stash[slot] = j;
         }
     }
-    // rows of this block allocated with one atomic (the atomic-compacted
-    // contact list of src/kernels.jl:74, 109): particle g gets base + Σ s_tot[<g]
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        const int v = s_tot[threadIdx.x];
-        int x = v;
-#pragma unroll
-        for (int o2 = 1; o2 < 32; o2 <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, x, o2);
-            if (lane_id() >= (unsigned)o2) x += y;
-        }
-        s_tot[threadIdx.x] = x - v;  // exclusive
-        if (threadIdx.x == 31) s_base = (int)atomicAdd(&d.ctr->row_alloc[nxt], (unsigned)x);
-    }
-    __syncthreads();
-    if (act && lane == 0) {
-        const int len = nkeep + s_new[g];
-        int start = s_base + s_tot[g];
-        int rl = len;
-        if ((long long)start + len > (long long)p.cap) {
+    __syncwarp(gmask);
+    if (lane == 0) {
+        int nnew = s_new[g];
+        if (nnew > p.kstash) {
             raise_error(d.ctr, kErrCapacity);
-            start = 0;
-            rl = 0;
+            nnew = p.kstash;
         }
-        d.row_start[nxt][i] = start;
-        d.row_len[nxt][i] = rl;
+        for (int a2 = 1; a2 < nnew; ++a2) {  // new partners ascending
+            const int v = stash[a2];
+            int b2 = a2 - 1;
+            while (b2 >= 0 && stash[b2] > v) {
+                stash[b2 + 1] = stash[b2];
+                --b2;
+            }
+            stash[b2 + 1] = v;
+        }
+        d.nnew[i] = nnew;
+        d.row_len[nxt][i] = nkeep + nnew;  // placed by k_rows
+        if (ended) atomicAdd(&d.sctr[sc].ended, (unsigned long long)ended);
+        if (!init && nnew) atomicAdd(&d.sctr[sc].created, (unsigned long long)nnew);
     }
+}
+
+// Row placement in the next contact buffer (the atomic-compacted contact list
+// of src/kernels.jl:74, 109): one warp-aggregated atomic per 32 slots.  Free
+// arena slots have length 0.  A row that would cross the capacity raises
+// kErrCapacity and is dropped (length 0).
+__global__ void __launch_bounds__(kThreads) k_rows(DemDev d, DemParams p, int nxt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int len = i < p.n ? d.row_len[nxt][i] : 0;
+    int incl = len;
+#pragma unroll
+    for (int o2 = 1; o2 < 32; o2 <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o2);
+        if (lane_id() >= (unsigned)o2) incl += y;
+    }
+    int base = 0;
+    if (lane_id() == 31 && incl) base = (int)atomicAdd(&d.ctr->row_alloc[nxt], (unsigned)incl);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    if (i >= p.n) return;
+    int start = base + incl - len;
+    int rl = len;
+    if ((long long)start + len > (long long)p.cap) {
+        raise_error(d.ctr, kErrCapacity);
+        start = 0;
+        rl = 0;
+    }
+    d.row_start[nxt][i] = start;
+    d.row_len[nxt][i] = rl;
 }
 
 // Rolling-array rebuild (the reference's remove_inactive_contact! + swap,
@@ -653,22 +667,22 @@ __device__ __forceinline__ bool bond_breaks(const Vec3<double>& F, const Vec3<do
 // NaN or out-of-range values, which fail every comparison) the FP64 test
 // decides, so the outcome is always that of bond_breaks.
 __device__ __forceinline__ bool bond_breaks_screened(const Vec3<double>& F, const Vec3<double>& ti,
-                                                     const Vec3<double>& tj, double invA,
-                                                     double rbI, const SceneParams& p) {
-    const float tiy = (float)ti.y, tiz = (float)ti.z, tjy = (float)tj.y, tjz = (float)tj.z;
-    const float ai = tiy * tiy + tiz * tiz, aj = tjy * tjy + tjz * tjz;
-    const float rb = (float)rbI, iA = (float)invA;
-    const float fa = (float)F.x * iA;
+                                                     const Vec3<double>& tj, const Vec3<float>& Ff,
+                                                     const Vec3<float>& tif, const Vec3<float>& tjf,
+                                                     float iA, float rb, const DemDev& d, int small,
+                                                     const SceneParams& p) {
+    const float ai = tif.y * tif.y + tif.z * tif.z, aj = tjf.y * tjf.y + tjf.z * tjf.z;
+    const float fa = Ff.x * iA;
     const float smax = rb * sqrtf(fmaxf(ai, aj)), smin = rb * sqrtf(fminf(ai, aj));
-    const float fy = (float)F.y, fz = (float)F.z;
-    const float s1 = fabsf((float)ti.x) * 0.5f * rb, s2 = (4.0f / 3.0f) * iA * sqrtf(fy * fy + fz * fz);
-    const float sc = (float)p.b_sc, st = (float)p.b_st, ss = (float)p.b_ss;
+    const float s1 = fabsf(tif.x) * 0.5f * rb;
+    const float s2 = (4.0f / 3.0f) * iA * sqrtf(Ff.y * Ff.y + Ff.z * Ff.z);
+    const float sc = p.f_sc, st = p.f_st, ss = p.f_ss;
     const float afa = fabsf(fa);
     const bool clear = (fa + smax + (afa + smax + fabsf(sc)) * 0x1p-16f < sc) &&
                        (-fa - smin + (afa + smin + fabsf(st)) * 0x1p-16f < st) &&
                        (s1 + s2 + (s1 + s2 + fabsf(ss)) * 0x1p-16f < ss);
     if (clear) return false;
-    return bond_breaks(F, ti, tj, invA, rbI, p);
+    return bond_breaks(F, ti, tj, d.b_invA[small], d.b_rbI[small], p);
 }
 
 // FP32 contact frame (same rows as Frame), from the FP32 unit normal; the
@@ -680,7 +694,7 @@ struct Frame32 {
 __device__ __forceinline__ Frame32 contact_frame32(float ax, float ay, float az, double dx,
                                                    double dy, double dz, const SceneParams& S) {
     const float s2 = ay * ay + az * az;
-    if (s2 < 4.0f * (float)S.tol * (float)S.tol) {
+    if (s2 < S.f_tol4) {
         const double L = norm_rn(dx, dy, dz);
         const double il = __ddiv_rn(1.0, L);
         const Frame F = frame_exact(__dmul_rn(il, dx), __dmul_rn(il, dy), __dmul_rn(il, dz), S.tol);
@@ -730,14 +744,15 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
             rot32(R, {(float)(wix + wjx), (float)(wiy + wjy), (float)(wiz + wjz)});
         const Vec3<float> Q = rot32(R, {(float)(wix - wjx), (float)(wiy - wjy), (float)(wiz - wjz)});
         const int small = ri <= rj ? i : j;  // rb = ρ·min(rᵢ, rⱼ)
-        const float tdt = (float)SP.dt;
-        const float phi = (float)d.b_phic[small] * invL * invL;
+        const float4 bk = d.bk32[small];     // (ϕ coefficient, E·I, E·A, 1/A)
+        const float tdt = SP.f_dt;
+        const float phi = bk.x * invL * invL;
         const float iphi = 1.0f / (1.0f + phi);
-        const float EILdt = (float)d.b_EI[small] * invL * tdt;
-        const float k1 = (float)d.b_EA[small] * invL * tdt;
+        const float EILdt = bk.y * invL * tdt;
+        const float k1 = bk.z * invL * tdt;
         const float k3 = 6.0f * EILdt * invL * iphi;
         const float k2 = 2.0f * k3 * invL;
-        const float k4 = EILdt * (float)SP.b_inv1pnu;
+        const float k4 = EILdt * SP.f_inv1pnu;
         const float kp = 3.0f * EILdt * iphi;
         const float km = EILdt;
         const float dFx = k1 * D.x, dFy = k2 * D.y + k3 * Sv.z, dFz = k2 * D.z - k3 * Sv.y;
@@ -748,16 +763,19 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
         Fi = {Fi.x + (double)dFx, Fi.y + (double)dFy, Fi.z + (double)dFz};
         ti = {ti.x + (double)dtix, ti.y + (double)dtiy, ti.z + (double)dtiz};
         tj = {tj.x + (double)dtjx, tj.y + (double)dtjy, tj.z + (double)dtjz};
-        if (bond_breaks_screened(Fi, ti, tj, d.b_invA[small], d.b_rbI[small], SP)) {
+        const Vec3<float> Ff{(float)Fi.x, (float)Fi.y, (float)Fi.z};
+        const Vec3<float> tif{(float)ti.x, (float)ti.y, (float)ti.z};
+        const Vec3<float> tjf{(float)tj.x, (float)tj.y, (float)tj.z};
+        if (bond_breaks_screened(Fi, ti, tj, Ff, tif, tjf, bk.w, d.rm32[small].x, d, small, SP)) {
             w.fl[c] = 0u;
             atomicAdd(&d.sctr[sc].broken, 1ull);
             fig = {0.0f, 0.0f, 0.0f};
             mi = fig;
             mj = fig;
         } else {
-            fig = rot_t32(R, {-(float)Fi.x, -(float)Fi.y, -(float)Fi.z});
-            mi = rot_t32(R, {-(float)ti.x, -(float)ti.y, -(float)ti.z});
-            mj = rot_t32(R, {-(float)tj.x, -(float)tj.y, -(float)tj.z});
+            fig = rot_t32(R, {-Ff.x, -Ff.y, -Ff.z});
+            mi = rot_t32(R, {-tif.x, -tif.y, -tif.z});
+            mj = rot_t32(R, {-tjf.x, -tjf.y, -tjf.z});
             st3(w.f, CK, c, {kix + 0.5 * dxd, kiy + 0.5 * dyd, kiz + 0.5 * dzd});
             st3(w.f, CF, c, Fi);
             st3(w.f, CTI, c, ti);
@@ -782,24 +800,24 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
                              (float)(d.vy[j] - d.vy[i]) + (wcj.y - wci.y),
                              (float)(d.vz[j] - d.vz[i]) + (wcj.z - wci.z)};
         const Vec3<float> vc = rot32(R, dv);
-        const float fri = (float)ri, frj = (float)rj, tmi = (float)d.m[i], tmj = (float)d.m[j];
+        const float fri = (float)ri, frj = (float)rj, tmi = d.rm32[i].y, tmj = d.rm32[j].y;
         const float Rs = fri * frj / (fri + frj);
         const float ms = tmi * tmj / (tmi + tmj);
         const float sq = sqrtf(Rs * fabsf(gap));
-        const float kn = (float)(4.0 / 3.0 * SP.pp_Ys) * sq;
-        const float kt = (float)(8.0 * SP.pp_Gs) * sq;
+        const float kn = SP.f_kn * sq;
+        const float kt = SP.f_kt * sq;
         const float root = sqrtf(ms * sq);
-        const float gn = (float)SP.pp_cgn * root;
-        const float gt = (float)SP.pp_cgt * root;
+        const float gn = SP.f_cgn * root;
+        const float gt = SP.f_cgt * root;
         if (gn < 0.0f || gt < 0.0f)
             atomicAdd(&d.sctr[sc].warn_damp, (unsigned long long)((gn < 0.0f) + (gt < 0.0f)));
-        const double dt = SP.dt;
+        // 𝐬 += (0, vc₂, vc₃)·dt in FP64 (the normal component stays)
         Vec3<double> s = ld3(w.f, CS, c);
-        s = {s.x + (double)vc.x * 0.0, s.y + (double)vc.y * dt, s.z + (double)vc.z * dt};
+        s = {s.x, s.y + (double)(vc.y * SP.f_dt), s.z + (double)(vc.z * SP.f_dt)};
         const float F1 = -kn * gap - gn * vc.x;
         const Vec3<float> Ft{-kt * (float)s.x, -kt * (float)s.y, -kt * (float)s.z};
         const float nFt = sqrtf(Ft.x * Ft.x + Ft.y * Ft.y + Ft.z * Ft.z);
-        const float muF1 = (float)SP.pp_mu * F1;
+        const float muF1 = SP.f_mu * F1;
         float F2, F3;
         if (nFt >= muF1) {
             const float ratio = muF1 / nFt;
@@ -816,15 +834,16 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
         st3(w.f, CF, c, {(double)F1, (double)F2, (double)F3});
         st3(w.f, CS, c, s);
     }
-    d.contrib[0 * cap + c] = (double)fig.x;
-    d.contrib[1 * cap + c] = (double)fig.y;
-    d.contrib[2 * cap + c] = (double)fig.z;
-    d.contrib[3 * cap + c] = (double)mi.x;
-    d.contrib[4 * cap + c] = (double)mi.y;
-    d.contrib[5 * cap + c] = (double)mi.z;
-    d.contrib[6 * cap + c] = (double)mj.x;
-    d.contrib[7 * cap + c] = (double)mj.y;
-    d.contrib[8 * cap + c] = (double)mj.z;
+    float* cb = d.contrib32;
+    cb[0 * cap + c] = fig.x;
+    cb[1 * cap + c] = fig.y;
+    cb[2 * cap + c] = fig.z;
+    cb[3 * cap + c] = mi.x;
+    cb[4 * cap + c] = mi.y;
+    cb[5 * cap + c] = mi.z;
+    cb[6 * cap + c] = mj.x;
+    cb[7 * cap + c] = mj.y;
+    cb[8 * cap + c] = mj.z;
 }
 
 // `resolve_collision!` for one active contact (src/kernels.jl:136-313).  T is
@@ -993,22 +1012,28 @@ __device__ __forceinline__ void sort_by_owner(int2 (&v)[N]) {
         }
     }
 }
-template <int N>
+template <typename T>
+__device__ __forceinline__ const T* contrib_of(const DemDev& d) {
+    if constexpr (std::is_same<T, float>::value) return d.contrib32;
+    else return d.contrib;
+}
+template <typename T, int N>
 __device__ __forceinline__ void add_incoming(const DemDev& d, size_t cap, const int2* il, int nin,
-                                             double* F, double* M) {
+                                             T* F, T* M) {
+    const T* cb = contrib_of<T>(d);
     int2 v[N];
 #pragma unroll
     for (int u = 0; u < N; ++u) v[u] = u < nin ? il[u] : make_int2(0, 0x7fffffff);
     sort_by_owner<N>(v);
-    double g[N][6];
+    T g[N][6];
 #pragma unroll
     for (int u = 0; u < N; ++u) {
         if (u < nin) {
             const int c = v[u].x;
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
-                g[u][q] = d.contrib[q * cap + c];
-                g[u][3 + q] = d.contrib[(6 + q) * cap + c];
+                g[u][q] = cb[q * cap + c];
+                g[u][3 + q] = cb[(6 + q) * cap + c];
             }
         }
     }
@@ -1024,29 +1049,23 @@ __device__ __forceinline__ void add_incoming(const DemDev& d, size_t cap, const 
     }
 }
 
-template <bool MULTI>
-__global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, int cur) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nxt = cur ^ 1;
-    if (i == 0) d.ctr->row_alloc[cur] = 0u;  // the free buffer is next step's target
-    if (i >= p.n) return;
-    const int sc = slot_scene<MULTI>(d, i);
-    if (MULTI && (sc < 0 || d.sp[sc].mode != kModeStep)) {
-        d.in_cnt[i] = 0;
-        return;
-    }
-    const SceneParams& S = scene_rec<MULTI>(d, p, sc);
+// Sum of the contact contributions on particle i in the fixed order: its own
+// row (by j), then its incoming contacts by owner index.  T = double for the
+// FP64 force mode, float for the FP32 force mode (its contributions are FP32).
+template <typename T>
+__device__ __forceinline__ void gather(const DemDev& d, const DemParams& p, int i, int nxt, T* F,
+                                       T* M) {
     const size_t cap = (size_t)p.cap;
-    double F[3] = {0.0, 0.0, 0.0}, M[3] = {0.0, 0.0, 0.0};
+    const T* cb = contrib_of<T>(d);
     const int c0 = d.row_start[nxt][i];
     const int c1 = min(c0 + d.row_len[nxt][i], p.cap);
     int c = c0;
     for (; c + 1 < c1; c += 2) {
-        double a[6], b[6];
+        T a[6], b[6];
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
-            a[q] = d.contrib[q * cap + c];
-            b[q] = d.contrib[q * cap + c + 1];
+            a[q] = cb[q * cap + c];
+            b[q] = cb[q * cap + c + 1];
         }
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
@@ -1062,8 +1081,8 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     if (c < c1) {
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            F[q] += d.contrib[q * cap + c];
-            M[q] += d.contrib[(3 + q) * cap + c];
+            F[q] += cb[q * cap + c];
+            M[q] += cb[(3 + q) * cap + c];
         }
     }
     int nin = d.in_cnt[i];
@@ -1071,9 +1090,9 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     nin = nin < kMaxIncoming ? nin : kMaxIncoming;
     const int2* il = d.in_list + (size_t)i * p.kin;
     if (nin <= 4) {
-        add_incoming<4>(d, cap, il, nin, F, M);
+        add_incoming<T, 4>(d, cap, il, nin, F, M);
     } else if (nin <= 8) {
-        add_incoming<8>(d, cap, il, nin, F, M);
+        add_incoming<T, 8>(d, cap, il, nin, F, M);
     } else {
         int2 inc[kMaxIncoming];
         for (int u = 0; u < nin; ++u) {
@@ -1089,10 +1108,36 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
             const int cc = inc[u].x;
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
-                F[q] += -d.contrib[q * cap + cc];
-                M[q] += d.contrib[(6 + q) * cap + cc];
+                F[q] += -cb[q * cap + cc];
+                M[q] += cb[(6 + q) * cap + cc];
             }
         }
+    }
+}
+
+template <bool MULTI, bool F32>
+__global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, int cur) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nxt = cur ^ 1;
+    if (i == 0) d.ctr->row_alloc[cur] = 0u;  // the free buffer is next step's target
+    if (i >= p.n) return;
+    const int sc = slot_scene<MULTI>(d, i);
+    if (MULTI && (sc < 0 || d.sp[sc].mode != kModeStep)) {
+        d.in_cnt[i] = 0;
+        return;
+    }
+    const SceneParams& S = scene_rec<MULTI>(d, p, sc);
+    double F[3] = {0.0, 0.0, 0.0}, M[3] = {0.0, 0.0, 0.0};
+    if constexpr (F32) {
+        float Ff[3] = {0.0f, 0.0f, 0.0f}, Mf[3] = {0.0f, 0.0f, 0.0f};
+        gather<float>(d, p, i, nxt, Ff, Mf);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            F[q] = (double)Ff[q];
+            M[q] = (double)Mf[q];
+        }
+    } else {
+        gather<double>(d, p, i, nxt, F, M);
     }
     d.in_cnt[i] = 0;
     const double x = d.px[i], y = d.py[i], z = d.pz[i];
@@ -1286,13 +1331,21 @@ void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi,
     else k_canon<false><<<nb, kThreads, 0, s>>>(d, p, cur);
 }
 
+template <int MINB>
+void launch_detect_b(const DemDev& d, const DemParams& p, int cur, bool init, bool multi, int nb,
+                     cudaStream_t s) {
+    if (multi) k_detect<false, true, MINB><<<nb, kThreads, 0, s>>>(d, p, cur);
+    else if (init) k_detect<true, false, MINB><<<nb, kThreads, 0, s>>>(d, p, cur);
+    else k_detect<false, false, MINB><<<nb, kThreads, 0, s>>>(d, p, cur);
+}
+
 void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
-                   cudaStream_t s) {
+                   const LaunchShape& sh, cudaStream_t s) {
     if (p.n == 0) return;
     const int nb = blocks_for((long long)p.n * kLanes, kThreads);
-    if (multi) k_detect<false, true><<<nb, kThreads, 0, s>>>(d, p, cur);
-    else if (init) k_detect<true, false><<<nb, kThreads, 0, s>>>(d, p, cur);
-    else k_detect<false, false><<<nb, kThreads, 0, s>>>(d, p, cur);
+    if (sh.detect_blocks_per_sm == 3) launch_detect_b<3>(d, p, cur, init, multi, nb, s);
+    else launch_detect_b<4>(d, p, cur, init, multi, nb, s);
+    k_rows<<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, cur ^ 1);
 }
 
 void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
@@ -1323,8 +1376,14 @@ void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
                       const LaunchShape& sh, cudaStream_t s) {
     if (p.n == 0) return;
     const int block = clamp_block(sh.integrate_block);
-    if (multi) k_integrate<true><<<blocks_for(p.n, block), block, 0, s>>>(d, p, cur);
-    else k_integrate<false><<<blocks_for(p.n, block), block, 0, s>>>(d, p, cur);
+    const int nb = blocks_for(p.n, block);
+    if (p.precision == 1) {
+        if (multi) k_integrate<true, true><<<nb, block, 0, s>>>(d, p, cur);
+        else k_integrate<false, true><<<nb, block, 0, s>>>(d, p, cur);
+    } else {
+        if (multi) k_integrate<true, false><<<nb, block, 0, s>>>(d, p, cur);
+        else k_integrate<false, false><<<nb, block, 0, s>>>(d, p, cur);
+    }
 }
 
 void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cudaStream_t s) {
