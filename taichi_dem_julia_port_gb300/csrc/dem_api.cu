@@ -155,6 +155,12 @@ void set_search_cell(SceneParams& p, double f, double min_cell, bool empty) {
     p.cell = empty ? p.cell_ref : std::min(p.cell_ref, std::max(f * p.cell_ref, min_cell));
     p.inv_cell = 1.0 / p.cell;
     p.same_grid = p.cell == p.cell_ref ? 1 : 0;
+    // the FP32 cell screen: 1/cell and max|dmin|/cell rounded up a little
+    const double dm = std::max(std::fabs(p.dmin[0]), std::max(std::fabs(p.dmin[1]), std::fabs(p.dmin[2])));
+    p.f_inv_cell = (float)p.inv_cell;
+    p.f_inv_cell_ref = (float)p.inv_cell_ref;
+    p.f_dmin_cells = (float)(dm * p.inv_cell * 1.001);
+    p.f_dmin_cells_ref = (float)(dm * p.inv_cell_ref * 1.001);
 }
 
 // Per-particle arrays of one scene, derived on the host.
@@ -317,6 +323,7 @@ struct DemHandle {
     cudaStream_t stream = nullptr;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     int graph_precision = -1;
+    int enc = DEM_FP64;  // encoding of 𝐅ᵢ, 𝛕ᵢ, 𝛕ⱼ in the current contact buffer
     std::vector<void*> allocs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double* pinned = nullptr;  // host staging for particle state exchange
@@ -468,15 +475,15 @@ int upload_scene(DemHandle* h, const SceneArrays& A, int64_t p0) {
     std::vector<double> one(n, 1.0);
     CU(up(d.qw, one));
     std::vector<float4> bk(n);
-    std::vector<float2> rm(n);
+    std::vector<float4> rm(n);
     for (size_t i = 0; i < n; ++i) {
         bk[i] = make_float4((float)A.b_phic[i], (float)A.b_EI[i], (float)A.b_EA[i],
                             (float)A.b_invA[i]);
-        rm[i] = make_float2((float)A.b_rbI[i], (float)A.m[i]);
+        rm[i] = make_float4((float)A.b_rbI[i], (float)A.m[i], (float)A.r[i], 0.0f);
     }
     CU(cudaMemcpyAsync(d.bk32 + p0, bk.data(), n * sizeof(float4), cudaMemcpyHostToDevice,
                        h->stream));
-    CU(cudaMemcpyAsync(d.rm32 + p0, rm.data(), n * sizeof(float2), cudaMemcpyHostToDevice,
+    CU(cudaMemcpyAsync(d.rm32 + p0, rm.data(), n * sizeof(float4), cudaMemcpyHostToDevice,
                        h->stream));
     for (double* z : {d.wx, d.wy, d.wz, d.qx, d.qy, d.qz, d.wsx, d.wsy, d.wsz, d.fx, d.fy, d.fz,
                       d.tx, d.ty, d.tz})
@@ -578,6 +585,32 @@ int contact_count(DemHandle* h, int buf, int32_t* total) {
     CU(cudaStreamSynchronize(h->stream));
     *total = (int32_t)std::min<int64_t>((int64_t)v, (int64_t)h->c_cap);
     return DEM_OK;
+}
+
+// The FP32 force mode keeps 𝐅ᵢ, 𝛕ᵢ, 𝛕ⱼ as FP32 hi/lo pairs; re-encode the
+// current buffer's contacts when the handle's precision changed.
+int ensure_encoding(DemHandle* h) {
+    if (h->enc == h->p.precision) return DEM_OK;
+    int32_t C = 0;
+    if (h->n_cap) TRY(contact_count(h, h->cur, &C));
+    launch_recode(h->d, h->cur, C, h->p.precision == DEM_FP32_FORCE, h->stream);
+    CU(cudaGetLastError());
+    h->enc = h->p.precision;
+    return DEM_OK;
+}
+
+// host side of the same encoding
+inline double pair_decode(double slot) {
+    float v[2];
+    std::memcpy(v, &slot, sizeof(v));
+    return (double)v[0] + (double)v[1];
+}
+inline double pair_encode(double x) {
+    const float hi = (float)x;
+    const float v[2] = {hi, (float)(x - (double)hi)};
+    double slot;
+    std::memcpy(&slot, v, sizeof(slot));
+    return slot;
 }
 
 int get_dev(std::vector<double>& host, const double* dev, size_t n, cudaStream_t s) {
@@ -758,6 +791,9 @@ int get_contacts_range(DemHandle* h, int64_t p0, int64_t n, DemContacts* out, in
     if (na) {
         for (int q = 0; q < 15; ++q) TRY(get_dev(f[q], s.f[q], (size_t)C, h->stream));
         CU(cudaStreamSynchronize(h->stream));
+        if (h->enc == DEM_FP32_FORCE)
+            for (int q = CF; q < CS; ++q)
+                for (int32_t c : act) f[q][c] = pair_decode(f[q][c]);
     }
     for (int64_t t = 0; t < na; ++t) {
         const int32_t c = act[t];
@@ -1057,6 +1093,7 @@ int dem_set_precision(DemHandle* h, int mode) {
 int dem_init_bonds(DemHandle* h) {
     if (!h || h->multi) return DEM_ERR_INVALID;
     if (h->n_cap == 0) return DEM_OK;
+    TRY(ensure_encoding(h));
     const int cur = h->cur, nxt = cur ^ 1;
     launch_broadphase(h->d, h->p, cur, false, h->ntiles_cells, h->stream);
     launch_detect(h->d, h->p, cur, true, false, h->shape, h->stream);
@@ -1074,6 +1111,7 @@ int dem_step(DemHandle* h, int64_t nsteps) {
         h->steps += nsteps;
         return DEM_OK;
     }
+    TRY(ensure_encoding(h));
     TRY(build_graphs(h));
     TRY(launch_inits(h));
     for (int64_t s = 0; s < nsteps; ++s) {
@@ -1102,6 +1140,7 @@ int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
         for (int k = 0; k < 5; ++k) phase_ms[k] = 0.f;
         return DEM_OK;
     }
+    TRY(ensure_encoding(h));
     if (h->multi) {
         TRY(build_graphs(h));
         TRY(launch_inits(h));
@@ -1247,6 +1286,8 @@ int dem_set_contacts(DemHandle* h, const DemContacts* in, int64_t nc) {
         for (int g = 0; g < 5; ++g)
             if (src[g])
                 for (int q = 0; q < 3; ++q) f[3 * g + q][t] = src[g][3 * s + q];
+        if (h->enc == DEM_FP32_FORCE)
+            for (int q = CF; q < CS; ++q) f[q][t] = pair_encode(f[q][t]);
     }
     for (int i = 1; i < n; ++i) rs[i] = rs[i - 1] + rl[i - 1];
     const ContactSoA& s = h->d.c[h->cur];

@@ -45,18 +45,20 @@ __device__ __forceinline__ bool touching_rn(double xi, double yi, double zi, dou
 
 // Conservative FP32 rejection: returns false only when the FP64 test above is
 // certain to fail.  Inputs are FP32 copies (u = 2^-24 relative rounding) of
-// positions relative to a common origin and of the radii.  The FP32 distance d'
-// differs from the true one by at most 2(M_i + M_j)u + 6u·d' (M = largest
-// coordinate magnitude of a particle) and r_i + r_j <= (r'_i + r'_j)(1 + 3u);
-// the test rejects only when d'(1 - 2^-18) exceeds (r'_i + r'_j) plus
-// (M_i + M_j + r'_i + r'_j)·2^-19, which leaves a factor of 10 on each term.
+// positions relative to a common origin; .w holds the particle's reach
+// w = r'(1 + 2^-19) + M·2^-19 (r' its FP32 radius, M its largest coordinate
+// magnitude), see reach32.  The FP32 distance d' differs from the true one by
+// at most 2(M_i + M_j)u + 6u·d', and r_i + r_j <= (r'_i + r'_j)(1 + 3u); the
+// test rejects only when d'(1 - 2^-18) exceeds w_i + w_j, which leaves a
+// factor of 10 on each error term.
+__device__ __forceinline__ float reach32(float x, float y, float z, float r) {
+    const float M = fmaxf(fmaxf(fabsf(x), fabsf(y)), fabsf(z));
+    return (r * (1.0f + 0x1p-19f) + M * 0x1p-19f) * (1.0f + 0x1p-21f);
+}
 __device__ __forceinline__ bool maybe_touching32(float4 a, float4 b) {
-    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
-    float s = dx * dx + dy * dy + dz * dz;
-    float M = fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fabsf(a.z)) +
-              fmaxf(fmaxf(fabsf(b.x), fabsf(b.y)), fabsf(b.z));
-    float rs = a.w + b.w;
-    float B = rs + (M + rs) * 0x1p-19f;
+    const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    const float s = dx * dx + dy * dy + dz * dz;
+    const float B = a.w + b.w;
     return !(s * (1.0f - 0x1p-17f) > B * B);
 }
 

@@ -77,6 +77,8 @@ struct SceneParams {
     float f_dt, f_inv1pnu, f_sc, f_st, f_ss;
     float f_mu, f_kn, f_kt, f_cgn, f_cgt;  // μ, 4/3·Y*, 8·G*, cgn, cgt (particle-particle)
     float f_tol4;                          // 4·tolerance² (degenerate frame test)
+    // FP32 screen of the cell computation: 1/cell and max|dmin|/cell
+    float f_inv_cell, f_dmin_cells, f_inv_cell_ref, f_dmin_cells_ref;
 };
 
 struct SceneCounters {
@@ -105,7 +107,7 @@ struct DemDev {
     double *b_invA, *b_rbI;        // bond section constants for rb = ρ·r (1/A, rb/I)
     double *b_EA, *b_EI, *b_phic;  // E·A, E·I and 20/3·(1+ν)·rb² for rb = ρ·r
     float4* bk32;                  // FP32 (b_phic, b_EI, b_EA, b_invA)
-    float2* rm32;                  // FP32 (b_rbI, m)
+    float4* rm32;                  // FP32 (b_rbI, m, r, 0)
     double *fx, *fy, *fz, *tx, *ty, *tz;  // totals of the last step
     double *wsx, *wsy, *wsz;              // wall shear history (one wall)
     int32_t* scene_of;                    // arena: scene of each slot (-1 free); null otherwise
@@ -132,6 +134,8 @@ struct DemDev {
     uint8_t* keep;        // cap, survival flags of the current buffer
     int32_t* in_cnt;      // zero between steps
     int2* in_list;        // n * kin: (contact slot, owner i) of contacts where the particle is j
+    // Contact columns 𝐅ᵢ, 𝛕ᵢ, 𝛕ⱼ hold FP64 values in the FP64 force mode and
+    // FP32 (hi, lo) pairs in the FP32 force mode.
     double* contrib;      // 9 * cap, [field][contact]
     float* contrib32;     // 9 * cap, the FP32 force mode's contributions
     // scan scratch: tile states of each scan site
@@ -180,6 +184,8 @@ void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cuda
 void launch_cplist_fill(const DemDev& d, const DemParams& p, const int32_t* off, int32_t* cp,
                         cudaStream_t s);
 void launch_morton(const DemDev& d, const DemParams& p, uint32_t* morton, cudaStream_t s);
+// re-encodes 𝐅ᵢ, 𝛕ᵢ, 𝛕ⱼ of contacts [0, n) of buffer `buf`: FP64 <-> FP32 hi/lo pairs
+void launch_recode(const DemDev& d, int buf, int n, bool to_pairs, cudaStream_t s);
 // exclusive scan of n int32 values into out[0..n] (out[n] = total)
 void launch_scan_i32(const int32_t* in, int32_t* out, int64_t n, const DemDev& d, int site,
                      cudaStream_t s);

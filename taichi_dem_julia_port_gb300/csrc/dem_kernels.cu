@@ -188,6 +188,38 @@ __device__ __forceinline__ int4 cell_of(const double pos[3], const double dmin[3
     return make_int4(ijk[0], ijk[1], ijk[2], oct);
 }
 
+// cell_of with an FP32 screen.  num = pos - dmin is formed exactly as the
+// reference forms it; q' = fl32(num)·fl32(1/cell) lies within 4·2^-24·|q| of
+// the exact quotient q = num/cell, and the reference's center
+// dmin + (ijk - 1/2)·cell within 2^-51·(|dmin|/cell + |q| + 1) of its exact
+// value (in cell units).  When the fraction of q' keeps a distance of
+// m = 2^-20·(|q'| + |dmin|/cell + 1) from 0, 1/2 and 1, the exact ceiling and
+// the exact octant side follow from q' alone; otherwise (and for NaN or huge
+// values, which fail the test) the exact FP64 computation decides.
+__device__ __forceinline__ int4 cell_of_screened(const double pos[3], const double dmin[3],
+                                                 double cell, double inv_cell, float inv_cell32,
+                                                 float dmin_cells) {
+    int ijk[3];
+    int oct = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const double num = __dsub_rn(pos[c], dmin[c]);
+        const float q = (float)num * inv_cell32;
+        const float fl = floorf(q);
+        const float frac = q - fl;
+        const float m = (fabsf(q) + dmin_cells + 1.0f) * 0x1p-20f;
+        if (frac > m && frac < 1.0f - m && fabsf(frac - 0.5f) > m) {
+            ijk[c] = (int)fl + 1;
+            if (frac > 0.5f) oct |= 1 << c;
+        } else {
+            ijk[c] = cell_index(num, cell, inv_cell);
+            const double ctr = __dadd_rn(dmin[c], __dmul_rn(__dsub_rn((double)ijk[c], 0.5), cell));
+            if (pos[c] > ctr) oct |= 1 << c;
+        }
+    }
+    return make_int4(ijk[0], ijk[1], ijk[2], oct);
+}
+
 // `cell`, `hashcode`, `center`, `neighbors` (src/utils.jl:1-16) and
 // `count_particles!` (src/kernels.jl:7-13).
 template <bool MULTI>
@@ -206,12 +238,14 @@ __global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p, int cu
         } else {
             const SceneParams& S = scene_rec<MULTI>(d, p, sc);
             const double pos[3] = {d.px[i], d.py[i], d.pz[i]};
-            int4 ci = cell_of(pos, S.dmin, S.cell, S.inv_cell);
+            int4 ci = cell_of_screened(pos, S.dmin, S.cell, S.inv_cell, S.f_inv_cell, S.f_dmin_cells);
             b = bucket_of(ci.x, ci.y, ci.z, S);
             if (MULTI) ci.w |= sc << 3;
             d.cellinfo[i] = ci;
             d.bucket[i] = b;
-            if (MULTI && !S.same_grid) d.refcell[i] = cell_of(pos, S.dmin, S.cell_ref, S.inv_cell_ref);
+            if (MULTI && !S.same_grid)
+                d.refcell[i] = cell_of_screened(pos, S.dmin, S.cell_ref, S.inv_cell_ref,
+                                                S.f_inv_cell_ref, S.f_dmin_cells_ref);
         }
     }
     const unsigned mask = __ballot_sync(0xffffffffu, act);
@@ -260,8 +294,9 @@ __global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p, int c
     const double x = d.px[i], y = d.py[i], z = d.pz[i], r = d.r[i];
     const SceneParams& S = scene_rec<MULTI>(d, p, slot_scene<MULTI>(d, (int)i));
     d.spos[pos] = make_double4_32a(x, y, z, r);
-    d.spos32[pos] = make_float4((float)(x - S.dmin[0]), (float)(y - S.dmin[1]),
-                                (float)(z - S.dmin[2]), (float)r);
+    const float fx = (float)(x - S.dmin[0]), fy = (float)(y - S.dmin[1]),
+                fz = (float)(z - S.dmin[2]);
+    d.spos32[pos] = make_float4(fx, fy, fz, reach32(fx, fy, fz, (float)r));
     d.scell[pos] = d.cellinfo[i];
     d.srow[pos] = make_int2(d.row_start[cur][i], d.row_len[cur][i]);
 }
@@ -335,6 +370,17 @@ __global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p
     uint32_t s, e;
     bucket_range(d, myB, d.ctr->cell_limit, &s, &e);
     if (dup || frozen) e = s;
+    // a bucket lists its particles by ascending index: keep those above i
+    // (cp_list holds the pairs i < j)
+    {
+        uint32_t lo = s, hi = e;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if ((int)d.sorted[mid] > i) hi = mid;
+            else lo = mid + 1;
+        }
+        s = lo;
+    }
     // the group's candidates: the concatenation of its 8 bucket ranges
     const int cnt = (int)(e - s);
     int incl = cnt;
@@ -390,7 +436,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p
     // new contacts: lane t takes candidates t, t+8, ... of the concatenation,
     // so the group's lanes share the work evenly and read consecutive slots
     int32_t* stash = d.stash + (size_t)i * p.kstash;
-    int seg = 0;
+    // current segment: its offset (first slot - prefix) and the next prefix
+    int seg = 0, segoff = s_seg[g][0].x, nextb = s_seg[g][1].y;
     for (int c0 = 0; c0 < total; c0 += kLanes * kBatch) {
         int jj[kBatch], qi[kBatch];
         float4 qq[kBatch];
@@ -401,8 +448,13 @@ __global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p
             qi[u] = 0;
             qq[u] = P32;
             if (c < total) {
-                while (seg + 1 < kLanes && s_seg[g][seg + 1].y <= c) ++seg;
-                const int q = s_seg[g][seg].x + (c - s_seg[g][seg].y);
+                while (nextb <= c) {  // nextb of the last segment is total, > c
+                    ++seg;
+                    const int2 sg = s_seg[g][seg];
+                    segoff = sg.x - sg.y;
+                    nextb = seg + 1 < kLanes ? s_seg[g][seg + 1].y : total;
+                }
+                const int q = segoff + c;
                 qi[u] = q;
                 jj[u] = (int)d.sorted[q];
                 qq[u] = d.spos32[q];
@@ -666,8 +718,10 @@ __device__ __forceinline__ bool bond_breaks(const Vec3<double>& F, const Vec3<do
 // scale the bond cannot break and the FP64 test is skipped.  Otherwise (and for
 // NaN or out-of-range values, which fail every comparison) the FP64 test
 // decides, so the outcome is always that of bond_breaks.
-__device__ __forceinline__ bool bond_breaks_screened(const Vec3<double>& F, const Vec3<double>& ti,
-                                                     const Vec3<double>& tj, const Vec3<float>& Ff,
+__device__ __forceinline__ double pair_value(float2 v) { return (double)v.x + (double)v.y; }
+
+__device__ __forceinline__ bool bond_breaks_screened(const float2 (&F)[3], const float2 (&ti)[3],
+                                                     const float2 (&tj)[3], const Vec3<float>& Ff,
                                                      const Vec3<float>& tif, const Vec3<float>& tjf,
                                                      float iA, float rb, const DemDev& d, int small,
                                                      const SceneParams& p) {
@@ -682,7 +736,23 @@ __device__ __forceinline__ bool bond_breaks_screened(const Vec3<double>& F, cons
                        (-fa - smin + (afa + smin + fabsf(st)) * 0x1p-16f < st) &&
                        (s1 + s2 + (s1 + s2 + fabsf(ss)) * 0x1p-16f < ss);
     if (clear) return false;
-    return bond_breaks(F, ti, tj, d.b_invA[small], d.b_rbI[small], p);
+    const Vec3<double> Fd{pair_value(F[0]), pair_value(F[1]), pair_value(F[2])};
+    const Vec3<double> tid{pair_value(ti[0]), pair_value(ti[1]), pair_value(ti[2])};
+    const Vec3<double> tjd{pair_value(tj[0]), pair_value(tj[1]), pair_value(tj[2])};
+    return bond_breaks(Fd, tid, tjd, d.b_invA[small], d.b_rbI[small], p);
+}
+
+// FP32 hi/lo pair accumulator (hi + lo carries about 48 bits): (hi, lo) + x
+// by Knuth's two-sum and a fast renormalisation, all in FP32.
+__device__ __forceinline__ float2 pair_add(float2 a, float x) {
+    const float s = a.x + x;
+    const float bp = s - a.x;
+    const float e = (a.x - (s - bp)) + (x - bp) + a.y;
+    const float h = s + e;
+    return make_float2(h, e - (h - s));
+}
+__device__ __forceinline__ float2* pair_col(const ContactSoA& w, int f) {
+    return reinterpret_cast<float2*>(w.f[f]);
 }
 
 // FP32 contact frame (same rows as Frame), from the FP32 unit normal; the
@@ -717,9 +787,14 @@ __device__ __forceinline__ Vec3<float> rot_t32(const Frame32& R, Vec3<float> v) 
 
 // `resolve_collision!` in the FP32 force mode (DEM_FP32_FORCE).  Differences
 // of positions and velocities are formed in FP64 and then cast; the contact
-// frame, stiffnesses, damping and friction run in FP32.  FP64 stays for the
-// accumulated bond force and torques, the shear displacement 𝐬, the contact
-// point and the bond-breakage decision.  The Hertz overlap is
+// frame, stiffnesses, damping and friction run in FP32.  The shear
+// displacement 𝐬 and the contact point stay FP64; the accumulated bond force
+// and torques are FP32 hi/lo pairs (compensated sums, about 48 significant
+// bits) stored in their FP64 slots, and the bond-breakage decision is the
+// FP64 test's.  Contact forces are stored as (F, 0) pairs in this mode; the
+// host decodes them, and a precision switch re-encodes the stored contacts
+// (k_recode).  FP64↔FP32 conversions run on the FP64 pipe, so the path keeps
+// them to the differences it must form in FP64.  The Hertz overlap is
 // (L² - (rᵢ+rⱼ)²)/(L + rᵢ + rⱼ) with the numerator in FP64, which keeps the
 // overlap's relative error at FP32 rounding even though L is FP32.
 __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
@@ -743,7 +818,9 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
         const Vec3<float> Sv =
             rot32(R, {(float)(wix + wjx), (float)(wiy + wjy), (float)(wiz + wjz)});
         const Vec3<float> Q = rot32(R, {(float)(wix - wjx), (float)(wiy - wjy), (float)(wiz - wjz)});
-        const int small = ri <= rj ? i : j;  // rb = ρ·min(rᵢ, rⱼ)
+        const float4 rmi = d.rm32[i], rmj = d.rm32[j];
+        const bool i_small = rmi.z <= rmj.z;
+        const int small = i_small ? i : j;   // rb = ρ·min(rᵢ, rⱼ)
         const float4 bk = d.bk32[small];     // (ϕ coefficient, E·I, E·A, 1/A)
         const float tdt = SP.f_dt;
         const float phi = bk.x * invL * invL;
@@ -759,14 +836,21 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
         const float ay_ = -k3 * D.z + kp * Sv.y, az_ = k3 * D.y + kp * Sv.z;
         const float dtix = k4 * Q.x, dtiy = ay_ + km * Q.y, dtiz = az_ + km * Q.z;
         const float dtjx = -k4 * Q.x, dtjy = ay_ - km * Q.y, dtjz = az_ - km * Q.z;
-        Vec3<double> Fi = ld3(w.f, CF, c), ti = ld3(w.f, CTI, c), tj = ld3(w.f, CTJ, c);
-        Fi = {Fi.x + (double)dFx, Fi.y + (double)dFy, Fi.z + (double)dFz};
-        ti = {ti.x + (double)dtix, ti.y + (double)dtiy, ti.z + (double)dtiz};
-        tj = {tj.x + (double)dtjx, tj.y + (double)dtjy, tj.z + (double)dtjz};
-        const Vec3<float> Ff{(float)Fi.x, (float)Fi.y, (float)Fi.z};
-        const Vec3<float> tif{(float)ti.x, (float)ti.y, (float)ti.z};
-        const Vec3<float> tjf{(float)tj.x, (float)tj.y, (float)tj.z};
-        if (bond_breaks_screened(Fi, ti, tj, Ff, tif, tjf, bk.w, d.rm32[small].x, d, small, SP)) {
+        // accumulated bond force and torques: FP32 hi/lo pairs in the FP64 slots
+        float2 Fp[3], tip[3], tjp[3];
+        const float dF[3] = {dFx, dFy, dFz}, dti[3] = {dtix, dtiy, dtiz};
+        const float dtj[3] = {dtjx, dtjy, dtjz};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            Fp[q] = pair_add(pair_col(w, CF + q)[c], dF[q]);
+            tip[q] = pair_add(pair_col(w, CTI + q)[c], dti[q]);
+            tjp[q] = pair_add(pair_col(w, CTJ + q)[c], dtj[q]);
+        }
+        const Vec3<float> Ff{Fp[0].x, Fp[1].x, Fp[2].x};
+        const Vec3<float> tif{tip[0].x, tip[1].x, tip[2].x};
+        const Vec3<float> tjf{tjp[0].x, tjp[1].x, tjp[2].x};
+        if (bond_breaks_screened(Fp, tip, tjp, Ff, tif, tjf, bk.w, (i_small ? rmi : rmj).x, d,
+                                 small, SP)) {
             w.fl[c] = 0u;
             atomicAdd(&d.sctr[sc].broken, 1ull);
             fig = {0.0f, 0.0f, 0.0f};
@@ -777,19 +861,23 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
             mi = rot_t32(R, {-tif.x, -tif.y, -tif.z});
             mj = rot_t32(R, {-tjf.x, -tjf.y, -tjf.z});
             st3(w.f, CK, c, {kix + 0.5 * dxd, kiy + 0.5 * dyd, kiz + 0.5 * dzd});
-            st3(w.f, CF, c, Fi);
-            st3(w.f, CTI, c, ti);
-            st3(w.f, CTJ, c, tj);
-            st3(w.f, CS, c, {0.0, 0.0, 0.0});
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                pair_col(w, CF + q)[c] = Fp[q];
+                pair_col(w, CTI + q)[c] = tip[q];
+                pair_col(w, CTJ + q)[c] = tjp[q];
+            }
+            // 𝐬 of a bond is zero from its creation on and is not stored again
         }
     } else {
         // Hertz-Mindlin (src/kernels.jl:240-313)
+        const float4 rmi = d.rm32[i], rmj = d.rm32[j];  // (rb/I, m, r, 0)
         const double Rsum = ri + rj;
         const double num = (dxd * dxd + dyd * dyd + dzd * dzd) - Rsum * Rsum;
         const float L = L2 * invL;
         const float gap = (float)num / (L + (float)Rsum);
         if (num > 0.0) atomicAdd(&d.sctr[sc].warn_gap, 1ull);
-        const float ext = (float)ri - fabsf(gap);
+        const float ext = rmi.z - fabsf(gap);
         const Vec3<float> kri{ax * ext, ay * ext, az * ext};
         st3(w.f, CK, c, {kix + (double)kri.x, kiy + (double)kri.y, kiz + (double)kri.z});
         const Vec3<float> krj{kri.x - dx, kri.y - dy, kri.z - dz};
@@ -800,7 +888,7 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
                              (float)(d.vy[j] - d.vy[i]) + (wcj.y - wci.y),
                              (float)(d.vz[j] - d.vz[i]) + (wcj.z - wci.z)};
         const Vec3<float> vc = rot32(R, dv);
-        const float fri = (float)ri, frj = (float)rj, tmi = d.rm32[i].y, tmj = d.rm32[j].y;
+        const float fri = rmi.z, frj = rmj.z, tmi = rmi.y, tmj = rmj.y;
         const float Rs = fri * frj / (fri + frj);
         const float ms = tmi * tmj / (tmi + tmj);
         const float sq = sqrtf(Rs * fabsf(gap));
@@ -831,7 +919,9 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
         fig = rot_t32(R, {-F1, -F2, -F3});
         mi = cross3<float>(kri, fig);
         mj = cross3<float>(krj, {-fig.x, -fig.y, -fig.z});
-        st3(w.f, CF, c, {(double)F1, (double)F2, (double)F3});
+        pair_col(w, CF + 0)[c] = make_float2(F1, 0.0f);
+        pair_col(w, CF + 1)[c] = make_float2(F2, 0.0f);
+        pair_col(w, CF + 2)[c] = make_float2(F3, 0.0f);
         st3(w.f, CS, c, s);
     }
     float* cb = d.contrib32;
@@ -1299,6 +1389,24 @@ __global__ void k_cp_fill(DemDev d, DemParams p, const int32_t* off, int32_t* cp
 }
 
 inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
+
+// Re-encodes the force and torque columns (𝐅ᵢ, 𝛕ᵢ, 𝛕ⱼ) of the first n
+// entries of a contact buffer between FP64 values and FP32 hi/lo pairs.
+__global__ void __launch_bounds__(kThreads) k_recode(ContactSoA w, int n, int to_pairs) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+#pragma unroll
+    for (int f = CF; f < CS; ++f) {
+        if (to_pairs) {
+            const double v = w.f[f][c];
+            const float hi = (float)v;
+            reinterpret_cast<float2*>(w.f[f])[c] = make_float2(hi, (float)(v - (double)hi));
+        } else {
+            const float2 v = reinterpret_cast<const float2*>(w.f[f])[c];
+            w.f[f][c] = (double)v.x + (double)v.y;
+        }
+    }
+}
 // block sizes of the grid-stride kernels: a multiple of 32 in [32, kThreads]
 inline int clamp_block(int b) { return b < 32 ? 32 : (b > kThreads ? kThreads : (b / 32) * 32); }
 
@@ -1394,6 +1502,10 @@ void launch_cplist_fill(const DemDev& d, const DemParams& p, const int32_t* off,
                         cudaStream_t s) {
     if (p.n == 0) return;
     k_cp_fill<<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, off, cp);
+}
+void launch_recode(const DemDev& d, int buf, int n, bool to_pairs, cudaStream_t s) {
+    if (n <= 0) return;
+    k_recode<<<blocks_for(n, kThreads), kThreads, 0, s>>>(d.c[buf], n, to_pairs ? 1 : 0);
 }
 void launch_morton(const DemDev& d, const DemParams& p, uint32_t* morton, cudaStream_t s) {
     if (p.n == 0) return;

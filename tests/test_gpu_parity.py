@@ -260,6 +260,28 @@ def test_fp32_force_mode_impact_errors(gpu):
     assert_rows_close(pg["pos"], po["pos"], 1e-6, "fp32 impact pos")
 
 
+def test_precision_switch_midrun(gpu):
+    """FP64 -> FP32 -> FP64 force modes in one run: the stored bond forces are
+    re-encoded at each switch (FP32 mode keeps them as FP32 hi/lo pairs), so
+    the run stays within the FP32 tolerance of the FP64 oracle throughout."""
+    sc = scenes.bonded_cube(6, speed=30.0, steps=0, seed=7)
+    g, o = both(sc.cfg, sc.particles)
+    g.initialize()
+    o.initialize()
+    for prec in ("fp64", "fp32", "fp64", "fp32"):
+        g.set_precision(prec)
+        g.simulate(40)
+        o.simulate(40)
+        cg, co = g.contacts(), o.contacts()
+        assert bonded_set(cg) == bonded_set(co), prec
+        assert_rows_close(cg["force"], co["force"], RTOL_FP32, f"{prec} contact force",
+                          atol_frac=RTOL_FP32)
+        assert_rows_close(cg["torque_i"], co["torque_i"], RTOL_FP32, f"{prec} torque",
+                          atol_frac=RTOL_FP32)
+        pg, po = g.particles(), o.particles()
+        assert_rows_close(pg["pos"], po["pos"], 1e-6, f"{prec} pos")
+
+
 # ---- edge cases ----------------------------------------------------------------------------
 
 def test_single_particle_on_wall(gpu):
