@@ -57,7 +57,8 @@ FORCE_BYTES_HERTZ = 12 + 176 + 24 + 72 + 72
 # Algorithmic bytes of the other phases per particle / per contact
 BROADPHASE_BYTES_PER_PARTICLE = 24 + 16 + 4 + 4 + 4 + 8 + 24 + 8 + 32 + 16  # hash..canon
 INTEGRATE_BYTES_PER_PARTICLE = 13 * 8 * 2 + 4 * 8 + 6 * 8 + 3 * 8 * 2 + 8 + 4  # state r/w
-KERNELS_PER_STEP = 8  # hash, scan, scatter, canon, detect, compact, force, integrate
+# hash, scan, scatter, canon, detect, list detect, rows, compact, force, integrate, flags
+KERNELS_PER_STEP = 11
 L2_FLUSH_BYTES = 256 << 20
 
 

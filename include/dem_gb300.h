@@ -158,6 +158,8 @@ typedef struct DemStats {
     int64_t warn_damping;    /* "γ < 0" events (src/kernels.jl:271-279)    */
     int32_t error;           /* sticky DEM_ERR_* raised on the device   */
     int32_t precision;       /* DEM_FP64 or DEM_FP32_FORCE              */
+    int64_t full_searches;   /* steps that ran the full pair search (the
+                                others tested the neighbour lists)      */
 } DemStats;
 
 typedef struct DemHandle DemHandle;
@@ -223,6 +225,15 @@ typedef struct DemLaunchShape {
 } DemLaunchShape;
 
 int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* shape);
+
+/* Neighbour-list skin of one scene (scene >= 0; 0 for a single-scene handle)
+ * or of every scene (scene < 0), as a fraction in [0, 1] of the largest skin
+ * the octant search allows (cell/2 - 2·max r).  Default 0.9.  A scene runs the
+ * full pair search (the reference's cp_list) when one of its particles has
+ * moved by skin/2 since its last full search, and otherwise tests only its
+ * lists; contact sets are the same either way.  0 searches in full every
+ * step.  No counterpart in the reference (it searches every step). */
+int dem_set_skin_factor(DemHandle* h, int32_t scene, double skin_factor);
 int dem_get_launch_shape(DemHandle* h, DemLaunchShape* out);
 
 /* ---- state exchange ---------------------------------------------------- */

@@ -99,7 +99,8 @@ class DemStats(C.Structure):
     _fields_ = [("n_particles", C.c_int64), ("steps_done", C.c_int64), ("contacts", C.c_int64),
                 ("bonded", C.c_int64), ("bonds_broken", C.c_int64), ("contacts_ended", C.c_int64),
                 ("contacts_created", C.c_int64), ("warn_gap", C.c_int64),
-                ("warn_damping", C.c_int64), ("error", C.c_int32), ("precision", C.c_int32)]
+                ("warn_damping", C.c_int64), ("error", C.c_int32), ("precision", C.c_int32),
+                ("full_searches", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -152,6 +153,7 @@ ENTRY_POINTS = {
     "dem_set_precision": (C.c_int, [_H, C.c_int]),
     "dem_set_launch_shape": (C.c_int, [_H, C.POINTER(DemLaunchShape)]),
     "dem_get_launch_shape": (C.c_int, [_H, C.POINTER(DemLaunchShape)]),
+    "dem_set_skin_factor": (C.c_int, [_H, C.c_int32, C.c_double]),
     "dem_get_particles": (C.c_int, [_H, C.POINTER(DemParticleState)]),
     "dem_set_particles": (C.c_int, [_H, C.POINTER(DemParticleState)]),
     "dem_get_static": (C.c_int, [_H, C.POINTER(DemParticleStatic)]),

@@ -133,6 +133,13 @@ class Arena:
     def set_launch_shape(self, **shape) -> None:
         set_launch_shape(self.lib, self.h, shape)
 
+    def set_skin_factor(self, skin_factor: float, scene: int = -1) -> None:
+        """Neighbour-list skin of one scene or all (-1), as a fraction of the
+        largest the search allows (0 = full pair search every step); results do
+        not change."""
+        check(self.lib, self.lib.dem_set_skin_factor(self.h, int(scene), float(skin_factor)),
+              "dem_set_skin_factor")
+
     # ---- the step -------------------------------------------------------------
     def step(self, nsteps: int = 1) -> None:
         """`simulate!` × nsteps for every scene in Step mode (asynchronous)."""

@@ -19,6 +19,7 @@ using namespace dem;
 namespace {
 
 constexpr double kPi = 3.141592653589793;
+constexpr int kListCapacity = 16;  // neighbour-list partners per particle
 
 struct M3 {
     double a[3][3];
@@ -145,16 +146,27 @@ struct SceneHost {
     DemDerived der{};
     SceneParams sp{};
     double min_cell = 0.0;  // smallest search cell that finds every touching pair
+    double rmax = 0.0;      // largest radius
+    double cell_factor = 1.0;
+    double skin_factor = 0.9;
     int64_t steps = 0, target = 0;
 };
 
 // Search cells of a scene for a cell factor f: f·(the reference's cell),
-// clamped to [min_cell, the reference's cell].
-void set_search_cell(SceneParams& p, double f, double min_cell, bool empty) {
+// clamped to [min_cell, the reference's cell].  The neighbour-list skin is
+// skin_factor times the slack the octant search leaves for it: a pair found
+// from i's octant buckets lies within cell/2, so the lists hold every pair
+// within rᵢ + rⱼ + skin when skin <= cell/2 - 2·max r.
+void set_search_cell(SceneParams& p, double f, double min_cell, bool empty, double rmax,
+                     double skin_factor) {
     f = f > 0 ? f : 1.0;
     p.cell = empty ? p.cell_ref : std::min(p.cell_ref, std::max(f * p.cell_ref, min_cell));
     p.inv_cell = 1.0 / p.cell;
     p.same_grid = p.cell == p.cell_ref ? 1 : 0;
+    const double slack = 0.5 * p.cell - 2.0 * rmax * (1.0 + 1e-6);
+    p.skin = (!empty && slack > 0.0 && skin_factor > 0.0) ? std::min(skin_factor, 1.0) * slack : 0.0;
+    p.f_skin = (float)(p.skin * (1.0 + 0x1p-20));
+    p.f_half_skin = (float)(0.5 * p.skin * (1.0 - 0x1p-20));
     // the FP32 cell screen: 1/cell and max|dmin|/cell rounded up a little
     const double dm = std::max(std::fabs(p.dmin[0]), std::max(std::fabs(p.dmin[1]), std::fabs(p.dmin[2])));
     p.f_inv_cell = (float)p.inv_cell;
@@ -242,7 +254,9 @@ int prepare_scene(const DemConfigC* cfg, const DemParticlesIn* pin, double cell_
     // 4·max r (stepping) and 4·max r₀ (bond initialisation).
     S.min_cell =
         4.0 * rmax_r * std::max(1.0, cfg->particle_contact_radius_multiplier) * (1.0 + 1e-9);
-    set_search_cell(p, cell_factor, S.min_cell, n == 0);
+    S.rmax = n ? rmax_r : 0.0;
+    S.cell_factor = cell_factor > 0 ? cell_factor : 1.0;
+    set_search_cell(p, S.cell_factor, S.min_cell, n == 0, S.rmax, S.skin_factor);
     p.dt = cfg->dt;
     p.tol = cfg->tolerance;
     p.damping = cfg->global_damping;
@@ -413,6 +427,11 @@ int allocate(DemHandle* h) {
     TRY(dalloc(h, &d.scan_state[kScanDebug], (size_t)scan_tiles((int64_t)n)));
     TRY(dalloc(h, &d.ctr, 1));
     TRY(dalloc(h, &d.sctr, (size_t)std::max(h->s_cap, 1)));
+    TRY(dalloc(h, &d.vl, n * (size_t)h->p.kvl));
+    TRY(dalloc(h, &d.vl_len, n));
+    TRY(dalloc(h, &d.xref, n));
+    TRY(dalloc(h, &d.pos32, n));
+    for (int b = 0; b < 2; ++b) TRY(dalloc(h, &d.sflags[b], (size_t)std::max(h->s_cap, 1)));
     if (h->multi) {
         TRY(dalloc(h, &d.scene_of, n));
         TRY(dalloc(h, &d.sp, (size_t)h->s_cap));
@@ -493,13 +512,21 @@ int upload_scene(DemHandle* h, const SceneArrays& A, int64_t p0) {
     return DEM_OK;
 }
 
+// Marks scene s (every buffer parity) for a full pair search at its next step.
+int flag_search(DemHandle* h, int s) {
+    for (int b = 0; b < 2; ++b)
+        CU(cudaMemsetAsync(h->d.sflags[b] + s, 1, sizeof(uint32_t), h->stream));
+    return DEM_OK;
+}
+
 void record_step(DemHandle* h, int cur) {
     const int nxt = cur ^ 1;
-    launch_broadphase(h->d, h->p, cur, h->multi, h->ntiles_cells, h->stream);
+    launch_broadphase(h->d, h->p, cur, h->multi, false, h->ntiles_cells, h->stream);
     launch_detect(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
     launch_compact(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
     launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
     launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
+    launch_scene_flags(h->d, h->p, cur, h->multi, h->stream);
 }
 
 void drop_graphs(DemHandle* h) {
@@ -831,6 +858,7 @@ int stats_of(DemHandle* h, int32_t s, const SceneHost& S, DemStats* out) {
     out->contacts_created = (int64_t)sc.created;
     out->warn_gap = (int64_t)sc.warn_gap;
     out->warn_damping = (int64_t)sc.warn_damp;
+    out->full_searches = (int64_t)sc.searches;
     out->error = error_code(c.error);
     out->precision = h->p.precision;
     return DEM_OK;
@@ -885,6 +913,9 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
     h->p.cap = h->c_cap;
     h->p.kstash = (int)std::min<int64_t>(cfg->max_coordinate_number, 64);
     h->p.kin = h->p.kstash;
+    h->p.kvl = kListCapacity;
+    h->p.ns = 1;
+    h->p.sms = sms;
     h->p.T = h->t_cap;
     h->p.precision = DEM_FP64;
     S.sp.mode = kModeStep;
@@ -897,6 +928,7 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
     h->scenes.push_back(S);
     int rc = init_handle(h);
     if (rc == DEM_OK) rc = upload_scene(h, A, 0);
+    if (rc == DEM_OK) rc = flag_search(h, 0);
     if (rc != DEM_OK) {
         free_all(h);
         delete h;
@@ -929,6 +961,9 @@ int dem_arena_create(const DemArenaConfig* cfg, DemHandle** out) {
     h->p.cap = h->c_cap;
     h->p.kstash = std::min(cfg->max_coordinate_number, 64);
     h->p.kin = h->p.kstash;
+    h->p.kvl = kListCapacity;
+    h->p.ns = h->s_cap;
+    h->p.sms = sms;
     h->p.T = h->t_cap;
     h->p.precision = cfg->precision;
     h->scenes.resize(h->s_cap);
@@ -989,6 +1024,7 @@ int dem_arena_add(DemHandle* h, const DemConfigC* cfg, const DemParticlesIn* pin
         k_fill_i32<<<nb, 256, 0, h->stream>>>(h->d.scene_of + p0, n, idx);
         if (cudaGetLastError() != cudaSuccess) rc = DEM_ERR_CUDA;
     }
+    if (rc == DEM_OK) rc = flag_search(h, idx);
     if (rc == DEM_OK &&
         (cudaMemcpyAsync(h->d.sp + idx, &S.sp, sizeof(SceneParams), cudaMemcpyHostToDevice,
                          h->stream) != cudaSuccess ||
@@ -1028,7 +1064,8 @@ int dem_arena_set_cell_factor(DemHandle* h, int32_t s, double f) {
     for (int k = 0; k < h->s_cap; ++k) {
         if ((s >= 0 && k != s) || h->scenes[k].mode == kModeFree) continue;
         SceneHost& S = h->scenes[k];
-        set_search_cell(S.sp, f, S.min_cell, S.sp.n == 0);
+        S.cell_factor = f > 0 ? f : 1.0;
+        set_search_cell(S.sp, S.cell_factor, S.min_cell, S.sp.n == 0, S.rmax, S.skin_factor);
         // the record's mode on the device may differ from the host copy for
         // the length of dem_step only, so the host record is current here
         S.sp.mode = S.mode;
@@ -1036,6 +1073,28 @@ int dem_arena_set_cell_factor(DemHandle* h, int32_t s, double f) {
                            h->stream));
     }
     if (s < 0) h->cell_factor = f > 0 ? f : 1.0;
+    CU(cudaStreamSynchronize(h->stream));
+    return DEM_OK;
+}
+
+int dem_set_skin_factor(DemHandle* h, int32_t s, double f) {
+    if (!h || !(f >= 0) || f > 1) return DEM_ERR_INVALID;
+    if (s >= 0 && !scene_at(h, s)) return DEM_ERR_INVALID;
+    for (int k = 0; k < (int)h->scenes.size(); ++k) {
+        if ((s >= 0 && k != s) || h->scenes[k].mode == kModeFree) continue;
+        SceneHost& S = h->scenes[k];
+        S.skin_factor = f;
+        set_search_cell(S.sp, S.cell_factor, S.min_cell, S.sp.n == 0, S.rmax, f);
+        if (h->multi) {
+            S.sp.mode = S.mode;
+            CU(cudaMemcpyAsync(h->d.sp + k, &S.sp, sizeof(SceneParams), cudaMemcpyHostToDevice,
+                               h->stream));
+        } else {
+            h->p.s0 = S.sp;  // kernel parameters: the step graphs are recaptured
+            drop_graphs(h);
+        }
+        TRY(flag_search(h, k));
+    }
     CU(cudaStreamSynchronize(h->stream));
     return DEM_OK;
 }
@@ -1095,7 +1154,7 @@ int dem_init_bonds(DemHandle* h) {
     if (h->n_cap == 0) return DEM_OK;
     TRY(ensure_encoding(h));
     const int cur = h->cur, nxt = cur ^ 1;
-    launch_broadphase(h->d, h->p, cur, false, h->ntiles_cells, h->stream);
+    launch_broadphase(h->d, h->p, cur, false, true, h->ntiles_cells, h->stream);
     launch_detect(h->d, h->p, cur, true, false, h->shape, h->stream);
     launch_compact(h->d, h->p, cur, true, false, h->shape, h->stream);
     // the old buffer becomes the next step's target: its allocator starts at 0
@@ -1149,7 +1208,7 @@ int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
     for (int k = 0; k < 6; ++k) CU(cudaEventCreate(&ev[k]));
     const int cur = h->cur, nxt = cur ^ 1;
     cudaEventRecord(ev[0], h->stream);
-    launch_broadphase(h->d, h->p, cur, h->multi, h->ntiles_cells, h->stream);
+    launch_broadphase(h->d, h->p, cur, h->multi, false, h->ntiles_cells, h->stream);
     cudaEventRecord(ev[1], h->stream);
     launch_detect(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
     cudaEventRecord(ev[2], h->stream);
@@ -1158,6 +1217,7 @@ int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
     launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
     cudaEventRecord(ev[4], h->stream);
     launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
+    launch_scene_flags(h->d, h->p, cur, h->multi, h->stream);
     cudaEventRecord(ev[5], h->stream);
     cudaError_t e = cudaEventSynchronize(ev[5]);
     for (int k = 0; k < 5 && e == cudaSuccess; ++k)
@@ -1243,6 +1303,7 @@ int dem_set_particles(DemHandle* h, const DemParticleState* in) {
                                h->stream));
         }
     }
+    TRY(flag_search(h, 0));  // positions changed: the neighbour lists are rebuilt
     CU(cudaStreamSynchronize(h->stream));
     return DEM_OK;
 }
@@ -1329,7 +1390,7 @@ int dem_debug_broadphase(DemHandle* h, int32_t* cell, uint32_t* morton, uint32_t
         if (bucket_count) std::memset(bucket_count, 0, sizeof(uint32_t) * h->t_cap);
         return DEM_OK;
     }
-    launch_broadphase(h->d, h->p, h->cur, false, h->ntiles_cells, h->stream);
+    launch_broadphase(h->d, h->p, h->cur, false, true, h->ntiles_cells, h->stream);
     uint32_t* dmorton = nullptr;
     int32_t *dcnt = nullptr, *doff = nullptr, *dcp = nullptr;
     auto cleanup = [&]() {

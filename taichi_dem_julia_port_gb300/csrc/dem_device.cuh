@@ -55,10 +55,10 @@ __device__ __forceinline__ float reach32(float x, float y, float z, float r) {
     const float M = fmaxf(fmaxf(fabsf(x), fabsf(y)), fabsf(z));
     return (r * (1.0f + 0x1p-19f) + M * 0x1p-19f) * (1.0f + 0x1p-21f);
 }
-__device__ __forceinline__ bool maybe_touching32(float4 a, float4 b) {
+__device__ __forceinline__ bool maybe_touching32(float4 a, float4 b, float extra = 0.0f) {
     const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
     const float s = dx * dx + dy * dy + dz * dz;
-    const float B = a.w + b.w;
+    const float B = a.w + b.w + extra;  // extra: the neighbour-list skin
     return !(s * (1.0f - 0x1p-17f) > B * B);
 }
 

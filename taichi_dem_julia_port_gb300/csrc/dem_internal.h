@@ -41,6 +41,14 @@ constexpr int kModeInit = 3;    // `initialize!` (bonds from r₀), no integrati
 
 constexpr uint32_t kNoBucket = 0xffffffffu;
 
+// Neighbour lists.  A full pair search (the reference's cp_list over the
+// octant buckets) runs only for scenes whose rebuild flag is set; it also
+// records, per particle, the partners j > i within rᵢ + rⱼ + skin (the
+// neighbour list) and the particle's position.  Until any particle of the
+// scene has moved by skin/2 from that position, every pair that can touch is
+// on the list, so the other steps test only the list.  Contact ends still
+// follow the reference's cells (computed from the current positions).
+
 struct ContactSoA {
     int32_t* ci;
     int32_t* cj;
@@ -79,10 +87,14 @@ struct SceneParams {
     float f_tol4;                          // 4·tolerance² (degenerate frame test)
     // FP32 screen of the cell computation: 1/cell and max|dmin|/cell
     float f_inv_cell, f_dmin_cells, f_inv_cell_ref, f_dmin_cells_ref;
+    // neighbour-list skin (0: a full search every step) and half of it in FP32
+    double skin;
+    float f_skin, f_half_skin;
 };
 
 struct SceneCounters {
     unsigned long long broken, ended, created, warn_gap, warn_damp;
+    unsigned long long searches;  // steps that ran the full pair search
 };
 
 struct DevCounters {
@@ -111,6 +123,14 @@ struct DemDev {
     double *fx, *fy, *fz, *tx, *ty, *tz;  // totals of the last step
     double *wsx, *wsy, *wsz;              // wall shear history (one wall)
     int32_t* scene_of;                    // arena: scene of each slot (-1 free); null otherwise
+    // neighbour lists: kvl partners per slot, their count, the position at the
+    // last full search and the current position (FP32, relative to the
+    // scene's domain_min, .w = reach32); rebuild flags per scene and buffer
+    int32_t* vl;
+    int32_t* vl_len;
+    float4* xref;
+    float4* pos32;
+    uint32_t* sflags[2];
     SceneParams* sp;                      // arena: scene records; null otherwise
     SceneCounters* sctr;                  // per-scene event counters
     // broad phase
@@ -151,6 +171,9 @@ struct DemParams {
     int kin;        // incoming contacts per particle
     uint32_t T;     // bucket-table entries processed by a step (all in use lie below)
     int precision;  // 0 = FP64, 1 = FP32 force
+    int kvl;        // neighbour-list capacity per particle
+    int ns;         // scene records
+    int sms;        // streaming multiprocessors (grid-stride launch sizes)
     SceneParams s0; // the scene of a single-scene handle
 };
 
@@ -168,8 +191,11 @@ struct LaunchShape {
 // All launches go to `s`.  `cur` selects the contact buffer that holds the
 // state at the start of the step; the step writes buffer cur^1.  `multi`
 // selects the arena kernels (per-slot scene records) over the single-scene ones.
-void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi,
+// `all`: hash every particle (otherwise only the scenes that search this step)
+void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi, bool all,
                        int n_scan_tiles_cells, cudaStream_t s);
+// end of a step: rebuild flags carried over or cleared
+void launch_scene_flags(const DemDev& d, const DemParams& p, int cur, bool multi, cudaStream_t s);
 void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
                    const LaunchShape& sh, cudaStream_t s);
 void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,

@@ -44,6 +44,12 @@ __device__ __forceinline__ const SceneParams& scene_rec(const DemDev& d, const D
     if (MULTI) return d.sp[s];
     return p.s0;
 }
+// Does scene sc run the full pair search this step?  (Its rebuild flag is set,
+// or it initialises bonds, or the caller hashes everything.)
+__device__ __forceinline__ bool full_search(const DemDev& d, int cur, int sc, int mode, int all) {
+    return all || mode == kModeInit || d.sflags[cur][sc] != 0u;
+}
+
 // particles placed in the bucket-sorted arrays this step
 __device__ __forceinline__ int sorted_count(const DemDev& d) {
     return (int)d.cell_start[d.ctr->cell_limit];
@@ -223,17 +229,21 @@ __device__ __forceinline__ int4 cell_of_screened(const double pos[3], const doub
 // `cell`, `hashcode`, `center`, `neighbors` (src/utils.jl:1-16) and
 // `count_particles!` (src/kernels.jl:7-13).
 template <bool MULTI>
-__global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p, int cur) {
+__global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p, int cur, int all) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool act = i < p.n;
     uint32_t b = 0;
     if (act) {
         const int sc = slot_scene<MULTI>(d, i);
-        if (MULTI && (sc < 0 || d.sp[sc].mode == kModeFree)) {
+        const int mode = MULTI ? (sc < 0 ? kModeFree : d.sp[sc].mode) : kModeStep;
+        if (mode == kModeFree) {
             // free slot: not hashed, and no contact row in the next buffer
             d.bucket[i] = kNoBucket;
             d.row_len[cur ^ 1][i] = 0;
             d.row_start[cur ^ 1][i] = 0;
+            act = false;
+        } else if (!full_search(d, cur, sc, mode, all)) {
+            d.bucket[i] = kNoBucket;  // this scene tests its neighbour lists
             act = false;
         } else {
             const SceneParams& S = scene_rec<MULTI>(d, p, sc);
@@ -327,19 +337,24 @@ __device__ __forceinline__ void bucket_range(const DemDev& d, uint32_t b, uint32
     }
 }
 
-template <bool INIT, bool MULTI, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p, int cur) {
-    __shared__ int s_new[kThreads / kLanes];
-    __shared__ int s_row[kThreads / kLanes][kRowCache];
-    __shared__ uint32_t s_rb[kThreads / kLanes][kLanes];  // the reference's 8 octant buckets
-    __shared__ int2 s_seg[kThreads / kLanes][kLanes];     // (first sorted slot, prefix) per bucket
-    const int lane = threadIdx.x & (kLanes - 1);
-    const int g = threadIdx.x / kLanes;
-    const int k = blockIdx.x * (kThreads / kLanes) + g;
+// Shared memory of one 8-lane group of k_detect.
+struct DetectShared {
+    int nnew;
+    int nvl;                  // neighbour-list entries found
+    int row[kRowCache];       // cached current row (partner or -1)
+    uint32_t rb[kLanes];      // the reference's 8 octant buckets
+    int2 seg[kLanes];         // (first sorted slot, prefix) per bucket
+};
+
+// The full pair search for the particle at sorted position k (one 8-lane group).
+template <bool INIT, bool MULTI>
+__device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p, int cur, int k,
+                                             int lane, unsigned gmask, DetectShared& sh) {
     const int nxt = cur ^ 1;
-    if (k >= sorted_count(d)) return;  // whole 8-lane groups leave together
-    const unsigned gmask = 0xffu << (lane_id() & ~7u);
-    if (lane == 0) s_new[g] = 0;
+    if (lane == 0) {
+        sh.nnew = 0;
+        sh.nvl = 0;
+    }
     const int i = (int)d.sorted[k];
     const int4 ci = d.scell[k];
     const float4 P32 = d.spos32[k];
@@ -390,8 +405,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p
         if (lane >= o2) incl += y;
     }
     const int total = __shfl_sync(gmask, incl, kLanes - 1, kLanes);
-    s_rb[g][lane] = myR;
-    s_seg[g][lane] = make_int2((int)s, incl - cnt);
+    sh.rb[lane] = myR;
+    sh.seg[lane] = make_int2((int)s, incl - cnt);
     __syncwarp(gmask);
 
     // existing row: survival (update_contacts!, src/kernels.jl:87-101)
@@ -403,7 +418,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p
     for (int e2 = e0 + lane; e2 < e1; e2 += kLanes) {
         const uint32_t fl = o.fl[e2];
         const int j = o.cj[e2];
-        if (cached) s_row[g][e2 - e0] = (fl & kActive) ? j : -1;
+        if (cached) sh.row[e2 - e0] = (fl & kActive) ? j : -1;
         int keep;
         if (!(fl & kActive)) {
             keep = 0;
@@ -422,7 +437,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p
             }
             bool in_cp = false;
 #pragma unroll
-            for (int t = 0; t < 8; ++t) in_cp |= (s_rb[g][t] == bj);
+            for (int t = 0; t < 8; ++t) in_cp |= (sh.rb[t] == bj);
             keep = (valid || !in_cp) ? 1 : 0;
             ended += 1 - keep;
         }
@@ -437,7 +452,11 @@ __global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p
     // so the group's lanes share the work evenly and read consecutive slots
     int32_t* stash = d.stash + (size_t)i * p.kstash;
     // current segment: its offset (first slot - prefix) and the next prefix
-    int seg = 0, segoff = s_seg[g][0].x, nextb = s_seg[g][1].y;
+    int seg = 0, segoff = sh.seg[0].x, nextb = sh.seg[1].y;
+    // the neighbour list is rebuilt with this search (not for held scenes)
+    const bool build = !frozen;
+    int32_t* vl = d.vl + (size_t)i * p.kvl;
+    const float skin = S.f_skin;
     for (int c0 = 0; c0 < total; c0 += kLanes * kBatch) {
         int jj[kBatch], qi[kBatch];
         float4 qq[kBatch];
@@ -450,9 +469,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p
             if (c < total) {
                 while (nextb <= c) {  // nextb of the last segment is total, > c
                     ++seg;
-                    const int2 sg = s_seg[g][seg];
+                    const int2 sg = sh.seg[seg];
                     segoff = sg.x - sg.y;
-                    nextb = seg + 1 < kLanes ? s_seg[g][seg + 1].y : total;
+                    nextb = seg + 1 < kLanes ? sh.seg[seg + 1].y : total;
                 }
                 const int q = segoff + c;
                 qi[u] = q;
@@ -464,10 +483,18 @@ __global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p
         for (int u = 0; u < kBatch; ++u) {
             const int j = jj[u];
             if (j <= i) continue;
-            if (!init && !maybe_touching32(P32, qq[u])) continue;
+            // partners within rᵢ + rⱼ + skin join the neighbour list
+            const bool near = maybe_touching32(P32, qq[u], skin);
+            if (build && near) {
+                const int vs = atomicAdd(&sh.nvl, 1);
+                if (vs < p.kvl) vl[vs] = j;
+            }
+            // bond initialisation tests r₀ (no FP32 pre-filter); otherwise a
+            // touching pair is near and passes the pre-filter
+            if (!init && (!near || !maybe_touching32(P32, qq[u]))) continue;
             bool found = false;
             if (cached) {
-                for (int t = 0; t < e1 - e0 && !found; ++t) found = s_row[g][t] == j;
+                for (int t = 0; t < e1 - e0 && !found; ++t) found = sh.row[t] == j;
             } else {
                 for (int e2 = e0; e2 < e1 && !found; ++e2)
                     found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
@@ -478,13 +505,19 @@ __global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p
             const double ri = init ? d.r0[i] : P.w;
             const double rj = init ? d.r0[j] : Q.w;
             if (!touching_rn(P.x, P.y, P.z, Q.x, Q.y, Q.z, ri, rj)) continue;
-            const int slot = atomicAdd(&s_new[g], 1);
+            const int slot = atomicAdd(&sh.nnew, 1);
             if (slot < p.kstash) stash[slot] = j;
         }
     }
     __syncwarp(gmask);
     if (lane == 0) {
-        int nnew = s_new[g];
+        if (build) {
+            const int nv = sh.nvl;
+            d.vl_len[i] = nv < p.kvl ? nv : p.kvl;
+            d.xref[i] = P32;
+            if (nv > p.kvl) atomicOr(&d.sflags[nxt][sc], 1u);  // list overflow: search again
+        }
+        int nnew = sh.nnew;
         if (nnew > p.kstash) {
             raise_error(d.ctr, kErrCapacity);
             nnew = p.kstash;
@@ -503,6 +536,162 @@ __global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p
         if (ended) atomicAdd(&d.sctr[sc].ended, (unsigned long long)ended);
         if (!init && nnew) atomicAdd(&d.sctr[sc].created, (unsigned long long)nnew);
     }
+}
+
+template <bool INIT, bool MULTI, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p, int cur) {
+    __shared__ DetectShared sh[kThreads / kLanes];
+    const int lane = threadIdx.x & (kLanes - 1);
+    const int g = threadIdx.x / kLanes;
+    const unsigned gmask = 0xffu << (lane_id() & ~7u);
+    const int count = sorted_count(d);
+    // grid-stride over sorted positions; whole 8-lane groups move together
+    for (int k = blockIdx.x * (kThreads / kLanes) + g; k < count; k += gridDim.x * (kThreads / kLanes)) {
+        detect_group<INIT, MULTI>(d, p, cur, k, lane, gmask, sh[g]);
+        __syncwarp(gmask);
+    }
+}
+
+// cp_list membership of the pair (i, j), i < j, from the current positions:
+// j's bucket among i's 8 octant buckets, in the reference's cells and table.
+template <bool MULTI>
+__device__ __noinline__ bool in_cp_list(const DemDev& d, const SceneParams& S, int i, int j) {
+    const double pi[3] = {d.px[i], d.py[i], d.pz[i]}, pj[3] = {d.px[j], d.py[j], d.pz[j]};
+    const int4 ci = cell_of_screened(pi, S.dmin, S.cell_ref, S.inv_cell_ref, S.f_inv_cell_ref,
+                                     S.f_dmin_cells_ref);
+    const int4 cj = cell_of_screened(pj, S.dmin, S.cell_ref, S.inv_cell_ref, S.f_inv_cell_ref,
+                                     S.f_dmin_cells_ref);
+    const uint32_t bj = ref_bucket_of(cj.x, cj.y, cj.z, S);
+    const int dx = (ci.w & 1) ? 1 : -1, dy = (ci.w & 2) ? 1 : -1, dz = (ci.w & 4) ? 1 : -1;
+    bool in = false;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int ox = (t == 1 || t == 4 || t == 5 || t == 7) ? dx : 0;
+        const int oy = (t == 2 || t == 4 || t == 6 || t == 7) ? dy : 0;
+        const int oz = (t == 3 || t == 5 || t == 6 || t == 7) ? dz : 0;
+        in |= ref_bucket_of(ci.x + ox, ci.y + oy, ci.z + oz, S) == bj;
+    }
+    return in;
+}
+
+// `update_contacts!` from the neighbour lists, for the particles of scenes
+// that do not run the full search this step (four lanes per particle,
+// grid-stride over slots).  Survival of the current row is decided as in
+// k_detect; new contacts are the touching list partners that are not in the
+// row.
+constexpr int kVLanes = 4;
+struct ListShared {
+    int nnew;
+    int row[kRowCache];
+};
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_vdetect(DemDev d, DemParams p, int cur) {
+    __shared__ ListShared sh[kThreads / kVLanes];
+    const int lane = threadIdx.x & (kVLanes - 1);
+    const int g = threadIdx.x / kVLanes;
+    const unsigned gmask = 0xfu << (lane_id() & ~3u);
+    const int nxt = cur ^ 1;
+    const ContactSoA o = d.c[cur];
+    for (int i = blockIdx.x * (kThreads / kVLanes) + g; i < p.n;
+         i += gridDim.x * (kThreads / kVLanes)) {
+        const int sc = slot_scene<MULTI>(d, i);
+        const int mode = MULTI ? (sc < 0 ? kModeFree : d.sp[sc].mode) : kModeStep;
+        if (mode == kModeFree || full_search(d, cur, sc, mode, 0)) continue;
+        const SceneParams& S = scene_rec<MULTI>(d, p, sc);
+        const bool frozen = mode == kModeFrozen;
+        if (lane == 0) sh[g].nnew = 0;
+        const int e0 = d.row_start[cur][i];
+        const int e1 = e0 + d.row_len[cur][i];
+        const bool cached = e1 - e0 <= kRowCache;
+        int nkeep = 0, ended = 0;
+        for (int e2 = e0 + lane; e2 < e1; e2 += kVLanes) {
+            const uint32_t fl = o.fl[e2];
+            const int j = o.cj[e2];
+            if (cached) sh[g].row[e2 - e0] = (fl & kActive) ? j : -1;
+            int keep;
+            if (!(fl & kActive)) {
+                keep = 0;
+            } else if (frozen || (fl & kBonded)) {
+                keep = 1;
+            } else {
+                const bool valid = touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j],
+                                               d.pz[j], d.r[i], d.r[j]);
+                keep = (valid || !in_cp_list<MULTI>(d, S, i, j)) ? 1 : 0;
+                ended += 1 - keep;
+            }
+            d.keep[e2] = (uint8_t)keep;
+            nkeep += keep;
+        }
+        nkeep = __reduce_add_sync(gmask, nkeep);
+        ended = __reduce_add_sync(gmask, ended);
+        __syncwarp(gmask);
+        int32_t* stash = d.stash + (size_t)i * p.kstash;
+        if (!frozen) {
+            const float4 Pi = d.pos32[i];
+            const int nv = d.vl_len[i];
+            const int32_t* vl = d.vl + (size_t)i * p.kvl;
+            for (int v = lane; v < nv; v += kVLanes) {
+                const int j = vl[v];
+                if (!maybe_touching32(Pi, d.pos32[j])) continue;
+                bool found = false;
+                if (cached) {
+                    for (int t = 0; t < e1 - e0 && !found; ++t) found = sh[g].row[t] == j;
+                } else {
+                    for (int e2 = e0; e2 < e1 && !found; ++e2)
+                        found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
+                }
+                if (found) continue;
+                if (!touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j], d.pz[j], d.r[i],
+                                 d.r[j]))
+                    continue;
+                const int slot = atomicAdd(&sh[g].nnew, 1);
+                if (slot < p.kstash) stash[slot] = j;
+            }
+        }
+        __syncwarp(gmask);
+        if (lane == 0) {
+            int nnew = sh[g].nnew;
+            if (nnew > p.kstash) {
+                raise_error(d.ctr, kErrCapacity);
+                nnew = p.kstash;
+            }
+            for (int a2 = 1; a2 < nnew; ++a2) {  // new partners ascending
+                const int v = stash[a2];
+                int b2 = a2 - 1;
+                while (b2 >= 0 && stash[b2] > v) {
+                    stash[b2 + 1] = stash[b2];
+                    --b2;
+                }
+                stash[b2 + 1] = v;
+            }
+            d.nnew[i] = nnew;
+            d.row_len[nxt][i] = nkeep + nnew;
+            if (ended) atomicAdd(&d.sctr[sc].ended, (unsigned long long)ended);
+            if (nnew) atomicAdd(&d.sctr[sc].created, (unsigned long long)nnew);
+        }
+        __syncwarp(gmask);
+    }
+}
+
+// End of a step: the rebuild flags of this step are cleared; scenes that did
+// not step keep theirs for their next step; scenes without a skin search in
+// full every step.
+template <bool MULTI>
+__global__ void k_scene_flags(DemDev d, DemParams p, int cur) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= p.ns) return;
+    const SceneParams& S = scene_rec<MULTI>(d, p, s);
+    const int mode = MULTI ? S.mode : kModeStep;
+    const int nxt = cur ^ 1;
+    if (mode == kModeFree) {
+        d.sflags[cur][s] = 0u;
+        return;
+    }
+    if (mode == kModeStep && d.sflags[cur][s] != 0u) d.sctr[s].searches += 1ull;
+    uint32_t carry = mode != kModeStep ? d.sflags[cur][s] : 0u;
+    if (mode == kModeStep && !(S.f_half_skin > 0.0f)) carry = 1u;
+    if (carry) atomicOr(&d.sflags[nxt][s], carry);
+    d.sflags[cur][s] = 0u;
 }
 
 // Row placement in the next contact buffer (the atomic-compacted contact list
@@ -1315,9 +1504,33 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     const double invm = d.inv_m[i];
     const double ax = F[0] * invm, ay = F[1] * invm, az = F[2] * invm;
     const double hdt2 = 0.5 * (dt * dt);
-    d.px[i] = x + vx * dt + ax * hdt2;
-    d.py[i] = y + vy * dt + ay * hdt2;
-    d.pz[i] = z + vz * dt + az * hdt2;
+    const double px1 = x + vx * dt + ax * hdt2, py1 = y + vy * dt + ay * hdt2,
+                 pz1 = z + vz * dt + az * hdt2;
+    d.px[i] = px1;
+    d.py[i] = py1;
+    d.pz[i] = pz1;
+    // FP32 position for the neighbour-list search, and the skin test: the
+    // scene searches in full next step once a particle has moved by skin/2
+    // from where its list was built (FP32 rounding of both positions is
+    // taken off the allowance)
+    {
+        const float fx = (float)(px1 - S.dmin[0]), fy = (float)(py1 - S.dmin[1]),
+                    fz = (float)(pz1 - S.dmin[2]);
+        d.pos32[i] = make_float4(fx, fy, fz, reach32(fx, fy, fz, d.rm32[i].z));
+        bool moved = false;
+        if (S.f_half_skin > 0.0f) {
+            const float4 xr = d.xref[i];
+            const float ex = fx - xr.x, ey = fy - xr.y, ez = fz - xr.z;
+            const float M = fmaxf(fmaxf(fabsf(fx), fabsf(fy)), fabsf(fz)) +
+                            fmaxf(fmaxf(fabsf(xr.x), fabsf(xr.y)), fabsf(xr.z));
+            const float lim = S.f_half_skin - M * 0x1p-21f;
+            moved = !(lim > 0.0f) || !(ex * ex + ey * ey + ez * ez <= lim * lim);
+        }
+        const unsigned am = __activemask();
+        const unsigned peers = __match_any_sync(am, moved ? sc : -1);
+        if (moved && lane_id() == (unsigned)(__ffs(peers) - 1) && d.sflags[nxt][sc] == 0u)
+            atomicOr(&d.sflags[nxt][sc], 1u);
+    }
     d.vx[i] = vx + ax * dt;
     d.vy[i] = vy + ay * dt;
     d.vz[i] = vz + az * dt;
@@ -1425,12 +1638,12 @@ void launch_scan_i32(const int32_t* in, int32_t* out, int64_t n, const DemDev& d
                                                           &d.ctr->tickets[site], d.ctr);
 }
 
-void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi, int ntiles_cells,
-                       cudaStream_t s) {
+void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi, bool all,
+                       int ntiles_cells, cudaStream_t s) {
     if (p.n == 0) return;
     const int nb = blocks_for(p.n, kThreads);
-    if (multi) k_hash<true><<<nb, kThreads, 0, s>>>(d, p, cur);
-    else k_hash<false><<<nb, kThreads, 0, s>>>(d, p, cur);
+    if (multi) k_hash<true><<<nb, kThreads, 0, s>>>(d, p, cur, all ? 1 : 0);
+    else k_hash<false><<<nb, kThreads, 0, s>>>(d, p, cur, all ? 1 : 0);
     k_scan_excl<uint32_t, true><<<ntiles_cells, kScanBlock, 0, s>>>(
         d.cell_count, d.cell_start, (long long)p.T, ntiles_cells, d.scan_state[kScanCells],
         &d.ctr->tickets[kScanCells], d.ctr);
@@ -1440,8 +1653,10 @@ void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi,
 }
 
 template <int MINB>
-void launch_detect_b(const DemDev& d, const DemParams& p, int cur, bool init, bool multi, int nb,
+void launch_detect_b(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
                      cudaStream_t s) {
+    // grid-stride: one wave of resident blocks at most
+    const int nb = max(1, min(blocks_for((long long)p.n * kLanes, kThreads), p.sms * MINB));
     if (multi) k_detect<false, true, MINB><<<nb, kThreads, 0, s>>>(d, p, cur);
     else if (init) k_detect<true, false, MINB><<<nb, kThreads, 0, s>>>(d, p, cur);
     else k_detect<false, false, MINB><<<nb, kThreads, 0, s>>>(d, p, cur);
@@ -1450,9 +1665,13 @@ void launch_detect_b(const DemDev& d, const DemParams& p, int cur, bool init, bo
 void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
                    const LaunchShape& sh, cudaStream_t s) {
     if (p.n == 0) return;
-    const int nb = blocks_for((long long)p.n * kLanes, kThreads);
-    if (sh.detect_blocks_per_sm == 3) launch_detect_b<3>(d, p, cur, init, multi, nb, s);
-    else launch_detect_b<4>(d, p, cur, init, multi, nb, s);
+    if (sh.detect_blocks_per_sm == 3) launch_detect_b<3>(d, p, cur, init, multi, s);
+    else launch_detect_b<4>(d, p, cur, init, multi, s);
+    if (!init) {  // the scenes that test their neighbour lists
+        const int nv = max(1, min(blocks_for((long long)p.n * kVLanes, kThreads), p.sms * 8));
+        if (multi) k_vdetect<true><<<nv, kThreads, 0, s>>>(d, p, cur);
+        else k_vdetect<false><<<nv, kThreads, 0, s>>>(d, p, cur);
+    }
     k_rows<<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, cur ^ 1);
 }
 
@@ -1503,6 +1722,12 @@ void launch_cplist_fill(const DemDev& d, const DemParams& p, const int32_t* off,
     if (p.n == 0) return;
     k_cp_fill<<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, off, cp);
 }
+void launch_scene_flags(const DemDev& d, const DemParams& p, int cur, bool multi, cudaStream_t s) {
+    if (p.n == 0 || p.ns <= 0) return;
+    if (multi) k_scene_flags<true><<<blocks_for(p.ns, 128), 128, 0, s>>>(d, p, cur);
+    else k_scene_flags<false><<<blocks_for(p.ns, 128), 128, 0, s>>>(d, p, cur);
+}
+
 void launch_recode(const DemDev& d, int buf, int n, bool to_pairs, cudaStream_t s) {
     if (n <= 0) return;
     k_recode<<<blocks_for(n, kThreads), kThreads, 0, s>>>(d.c[buf], n, to_pairs ? 1 : 0);

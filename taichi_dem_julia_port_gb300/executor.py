@@ -137,6 +137,12 @@ class GlobalData:
     def set_launch_shape(self, **shape) -> None:
         set_launch_shape(self.lib, self.h, shape)
 
+    def set_skin_factor(self, skin_factor: float) -> None:
+        """Neighbour-list skin as a fraction of the largest the search allows
+        (0 = full pair search every step); results do not change."""
+        check(self.lib, self.lib.dem_set_skin_factor(self.h, 0, float(skin_factor)),
+              "dem_set_skin_factor")
+
     def initialize(self) -> None:
         """`initialize!`: broad phase + init_bonds! (bond every cp_list pair
         closer than r₀ᵢ + r₀ⱼ)."""

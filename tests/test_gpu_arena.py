@@ -202,3 +202,42 @@ def test_tuning_knobs_keep_results(gpu):
     for k in PARTICLE_KEYS:
         np.testing.assert_array_equal(p[k], refs[0][0][k], err_msg=f"single retuned {k}")
     np.testing.assert_array_equal(c["force"], refs[0][1]["force"])
+
+
+def test_neighbour_lists_equal_full_search(gpu):
+    """Steps that test neighbour lists give the results of a full pair search
+    every step (skin factor 0), bit for bit, while the scenes move enough to
+    rebuild their lists several times."""
+    cube = small_cube(6, speed=40.0, seed=61)
+    pour = small_pour(600, seed=62)
+    steps = 150
+
+    def run(skin):
+        out = []
+        for sc, init in ((cube, True), (pour, False)):
+            g = GlobalData(sc.cfg, sc.particles)
+            g.set_skin_factor(skin)
+            if init:
+                g.initialize()
+            g.simulate(steps)
+            out.append((g.particles(), g.contacts(), g.stats()))
+            g.close()
+        return out
+
+    full, lists = run(0.0), run(0.9)
+    for (pf, cf, sf), (pl, cl, sl), name in zip(full, lists, ("cube", "pour")):
+        for k in PARTICLE_KEYS:
+            np.testing.assert_array_equal(pl[k], pf[k], err_msg=f"{name} {k}")
+        for k in CONTACT_KEYS:
+            np.testing.assert_array_equal(cl[k], cf[k], err_msg=f"{name} contacts {k}")
+        assert sf["full_searches"] == steps, (name, sf["full_searches"])
+        assert 1 <= sl["full_searches"] < steps, (name, sl["full_searches"])
+        assert sl["contacts_ended"] == sf["contacts_ended"]
+    assert full[1][2]["contacts_created"] > 0 and full[1][2]["contacts_ended"] > 0
+    # the same inside an arena, with per-scene skins
+    with Arena(4096, max_scenes=4) as a:
+        ids = [a.add(cube.cfg, cube.particles), a.add(pour.cfg, pour.particles, init_bonds=False)]
+        a.set_skin_factor(0.5, scene=ids[1])
+        a.step(steps)
+        for sid, ref, name in zip(ids, full, ("cube", "pour")):
+            assert_same(a, sid, ref, f"arena lists {name}")
