@@ -177,6 +177,7 @@ ENTRY_POINTS = {
     "dem_bucket_sort_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                           C.POINTER(C.c_double), C.c_double, C.c_int64,
                                           C.c_void_p, C.c_void_p, C.c_void_p]),
+    "dem_selftest_conversions": (C.c_int, [C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
     "dem_strerror": (C.c_char_p, [C.c_int]),
     "dem_version": (C.c_char_p, []),
 }

@@ -299,6 +299,14 @@ int prepare_scene(const DemConfigC* cfg, const DemParticlesIn* pin, double cell_
     p.f_cgn = (float)p.pp_cgn;
     p.f_cgt = (float)p.pp_cgt;
     p.f_tol4 = (float)(4.0 * p.tol * p.tol);
+    p.f_tol1 = (float)(p.tol * p.tol * (1.0 - 0x1p-10));
+    p.hdt2 = 0.5 * (p.dt * p.dt);
+    double c0 = -p.wd;
+    for (int c = 0; c < 3; ++c) {
+        p.f_wn[c] = (float)p.wn[c];
+        c0 += p.wn[c] * p.dmin[c];
+    }
+    p.f_wc0 = (float)c0;
     return DEM_OK;
 }
 
@@ -884,6 +892,26 @@ const char* dem_strerror(int code) {
     }
 }
 
+int dem_selftest_conversions(int64_t n, uint64_t seed, int64_t* mismatches) {
+    if (n < 0 || !mismatches) return DEM_ERR_INVALID;
+    int dev = 0, sms = 0;
+    TRY(check_device(&dev, &sms));
+    unsigned long long* bad = nullptr;
+    CU(cudaMalloc(&bad, 2 * sizeof(unsigned long long)));
+    unsigned long long hb[2] = {0, 0};
+    cudaError_t e = cudaMemset(bad, 0, sizeof(hb));
+    if (e == cudaSuccess) {
+        launch_selftest_conv((long long)n, (unsigned long long)seed, bad, 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(hb, bad, sizeof(hb), cudaMemcpyDeviceToHost);
+    cudaFree(bad);
+    CU(e);
+    mismatches[0] = (int64_t)hb[0];
+    mismatches[1] = (int64_t)hb[1];
+    return DEM_OK;
+}
+
 int dem_set_device(int device) {
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DEM_ERR_NO_DEVICE;
@@ -929,6 +957,10 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
     int rc = init_handle(h);
     if (rc == DEM_OK) rc = upload_scene(h, A, 0);
     if (rc == DEM_OK) rc = flag_search(h, 0);
+    if (rc == DEM_OK) {
+        launch_refresh_pos32(h->d, h->p, false, 0, h->n_cap, h->stream);
+        if (cudaGetLastError() != cudaSuccess) rc = DEM_ERR_CUDA;
+    }
     if (rc != DEM_OK) {
         free_all(h);
         delete h;
@@ -1031,6 +1063,11 @@ int dem_arena_add(DemHandle* h, const DemConfigC* cfg, const DemParticlesIn* pin
          cudaMemsetAsync(h->d.sctr + idx, 0, sizeof(SceneCounters), h->stream) != cudaSuccess ||
          cudaStreamSynchronize(h->stream) != cudaSuccess))
         rc = DEM_ERR_CUDA;
+    if (rc == DEM_OK && n) {
+        launch_refresh_pos32(h->d, h->p, true, (int)p0, (int)n, h->stream);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess)
+            rc = DEM_ERR_CUDA;
+    }
     if (rc != DEM_OK) {
         h->pfree.give(p0, n);
         h->tfree.give(t0, H);
@@ -1304,6 +1341,8 @@ int dem_set_particles(DemHandle* h, const DemParticleState* in) {
         }
     }
     TRY(flag_search(h, 0));  // positions changed: the neighbour lists are rebuilt
+    launch_refresh_pos32(h->d, h->p, false, 0, (int)n, h->stream);
+    CU(cudaGetLastError());
     CU(cudaStreamSynchronize(h->stream));
     return DEM_OK;
 }

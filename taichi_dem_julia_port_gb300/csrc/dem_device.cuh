@@ -62,6 +62,42 @@ __device__ __forceinline__ bool maybe_touching32(float4 a, float4 b, float extra
     return !(s * (1.0f - 0x1p-17f) > B * B);
 }
 
+// ---- FP64 <-> FP32 conversions on the integer pipe -----------------------------
+// GB300 runs conversions involving FP64 on its narrow FP64 pipe.  These do the
+// same conversions with integer instructions, from the IEEE 754 binary64 and
+// binary32 layouts: narrowing rounds to nearest, ties to even (a carry out of
+// the significand moves into the exponent, up to infinity as the rounding
+// requires); widening is exact.  Inputs whose result is zero, subnormal or
+// not finite take the hardware conversion.
+// The rare cases are out-of-line calls, so the compiler cannot evaluate them
+// unconditionally (on the FP64 pipe) and select.
+static __device__ __noinline__ float d2f_hw(double x) { return __double2float_rn(x); }
+static __device__ __noinline__ double f2d_hw(float f) { return (double)f; }
+__device__ __forceinline__ float d2f(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int e = (int)((hi >> 20) & 0x7ffu) - (1023 - 127);  // binary32 exponent field
+    if ((unsigned)(e - 1) >= 254u) {
+        if (((hi << 1) | lo) == 0u) return __uint_as_float(hi);  // ±0
+        return d2f_hw(x);
+    }
+    const unsigned sig = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 significand bits
+    const unsigned rest = lo & 0x1fffffffu;                    // the 29 bits rounded off
+    unsigned r = (hi & 0x80000000u) | ((unsigned)e << 23) | sig;
+    r += (rest > 0x10000000u || (rest == 0x10000000u && (sig & 1u))) ? 1u : 0u;
+    return __uint_as_float(r);
+}
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) {
+        if ((u << 1) == 0u) return __hiloint2double((int)u, 0);  // ±0
+        return f2d_hw(f);
+    }
+    const unsigned hi = (u & 0x80000000u) | ((e + (1023 - 127)) << 20) | ((u & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
 // ---- Morton / bucket ---------------------------------------------------------
 // Morton.jl `cartesian3morton` for 1-based cells (x in bit 0): the interleave of
 // (ijk - 1) plus one.  Each coordinate keeps its low 10 bits.  The spreading

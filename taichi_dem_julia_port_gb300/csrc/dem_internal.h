@@ -85,11 +85,14 @@ struct SceneParams {
     float f_dt, f_inv1pnu, f_sc, f_st, f_ss;
     float f_mu, f_kn, f_kt, f_cgn, f_cgt;  // μ, 4/3·Y*, 8·G*, cgn, cgt (particle-particle)
     float f_tol4;                          // 4·tolerance² (degenerate frame test)
+    float f_tol1;                          // tolerance²·(1 - 2^-10), rounded down
     // FP32 screen of the cell computation: 1/cell and max|dmin|/cell
     float f_inv_cell, f_dmin_cells, f_inv_cell_ref, f_dmin_cells_ref;
     // neighbour-list skin (0: a full search every step) and half of it in FP32
     double skin;
     float f_skin, f_half_skin;
+    double hdt2;            // dt²/2
+    float f_wn[3], f_wc0;   // FP32 wall normal and n·domain_min - wall_distance (wall screen)
 };
 
 struct SceneCounters {
@@ -210,11 +213,19 @@ void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cuda
 void launch_cplist_fill(const DemDev& d, const DemParams& p, const int32_t* off, int32_t* cp,
                         cudaStream_t s);
 void launch_morton(const DemDev& d, const DemParams& p, uint32_t* morton, cudaStream_t s);
+// FP32 positions (pos32) of slots [first, first + n) from the FP64 positions
+void launch_refresh_pos32(const DemDev& d, const DemParams& p, bool multi, int first, int n,
+                          cudaStream_t s);
 // re-encodes 𝐅ᵢ, 𝛕ᵢ, 𝛕ⱼ of contacts [0, n) of buffer `buf`: FP64 <-> FP32 hi/lo pairs
 void launch_recode(const DemDev& d, int buf, int n, bool to_pairs, cudaStream_t s);
 // exclusive scan of n int32 values into out[0..n] (out[n] = total)
 void launch_scan_i32(const int32_t* in, int32_t* out, int64_t n, const DemDev& d, int site,
                      cudaStream_t s);
+
+// self-test of the integer-pipe FP64<->FP32 conversions (bad[0]: narrowing,
+// bad[1]: widening mismatches against the hardware)
+void launch_selftest_conv(long long n, unsigned long long seed, unsigned long long* bad,
+                          cudaStream_t s);
 
 int scan_tiles(int64_t n);
 

@@ -210,7 +210,7 @@ __device__ __forceinline__ int4 cell_of_screened(const double pos[3], const doub
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const double num = __dsub_rn(pos[c], dmin[c]);
-        const float q = (float)num * inv_cell32;
+        const float q = d2f(num) * inv_cell32;
         const float fl = floorf(q);
         const float frac = q - fl;
         const float m = (fabsf(q) + dmin_cells + 1.0f) * 0x1p-20f;
@@ -304,9 +304,8 @@ __global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p, int c
     const double x = d.px[i], y = d.py[i], z = d.pz[i], r = d.r[i];
     const SceneParams& S = scene_rec<MULTI>(d, p, slot_scene<MULTI>(d, (int)i));
     d.spos[pos] = make_double4_32a(x, y, z, r);
-    const float fx = (float)(x - S.dmin[0]), fy = (float)(y - S.dmin[1]),
-                fz = (float)(z - S.dmin[2]);
-    d.spos32[pos] = make_float4(fx, fy, fz, reach32(fx, fy, fz, (float)r));
+    const float fx = d2f(x - S.dmin[0]), fy = d2f(y - S.dmin[1]), fz = d2f(z - S.dmin[2]);
+    d.spos32[pos] = make_float4(fx, fy, fz, reach32(fx, fy, fz, d2f(r)));
     d.scell[pos] = d.cellinfo[i];
     d.srow[pos] = make_int2(d.row_start[cur][i], d.row_len[cur][i]);
 }
@@ -828,9 +827,23 @@ __device__ __forceinline__ Frame frame_exact(double ax, double ay, double az, do
     }
     return F;
 }
+// The degenerate branch without the exact recomputation: s² below tol² by a
+// relative 2^-30 (far beyond the 1e-15 relative error of the fast normal)
+// decides s < tol for the reference's exactly normalised a as well.
+__device__ __forceinline__ Frame frame_degenerate(double ax) {
+    const double sg = ax > 0.0 ? 1.0 : -1.0;
+    Frame F;
+    F.a1 = sg;
+    F.a2 = 0.0;
+    F.a3 = 0.0;
+    F.f = 0.0;
+    F.neg3 = sg < 0.0;
+    return F;
+}
 __device__ __forceinline__ Frame contact_frame(double dx, double dy, double dz, double ax,
                                                double ay, double az, double tol) {
     const double s2 = ay * ay + az * az;
+    if (s2 < tol * tol * (1.0 - 0x1p-30)) return frame_degenerate(ax);
     if (s2 < 4.0 * tol * tol) {
         const double L = norm_rn(dx, dy, dz);
         const double il = __ddiv_rn(1.0, L);
@@ -909,6 +922,17 @@ __device__ __forceinline__ bool bond_breaks(const Vec3<double>& F, const Vec3<do
 // decides, so the outcome is always that of bond_breaks.
 __device__ __forceinline__ double pair_value(float2 v) { return (double)v.x + (double)v.y; }
 
+// bond_breaks on FP32 hi/lo pairs (out of line: the FP32 screen settles
+// almost every bond without it)
+static __device__ __noinline__ bool bond_breaks_pairs(const float2 (&F)[3], const float2 (&ti)[3],
+                                                      const float2 (&tj)[3], double invA,
+                                                      double rbI, const SceneParams& p) {
+    const Vec3<double> Fd{pair_value(F[0]), pair_value(F[1]), pair_value(F[2])};
+    const Vec3<double> tid{pair_value(ti[0]), pair_value(ti[1]), pair_value(ti[2])};
+    const Vec3<double> tjd{pair_value(tj[0]), pair_value(tj[1]), pair_value(tj[2])};
+    return bond_breaks(Fd, tid, tjd, invA, rbI, p);
+}
+
 __device__ __forceinline__ bool bond_breaks_screened(const float2 (&F)[3], const float2 (&ti)[3],
                                                      const float2 (&tj)[3], const Vec3<float>& Ff,
                                                      const Vec3<float>& tif, const Vec3<float>& tjf,
@@ -925,10 +949,7 @@ __device__ __forceinline__ bool bond_breaks_screened(const float2 (&F)[3], const
                        (-fa - smin + (afa + smin + fabsf(st)) * 0x1p-16f < st) &&
                        (s1 + s2 + (s1 + s2 + fabsf(ss)) * 0x1p-16f < ss);
     if (clear) return false;
-    const Vec3<double> Fd{pair_value(F[0]), pair_value(F[1]), pair_value(F[2])};
-    const Vec3<double> tid{pair_value(ti[0]), pair_value(ti[1]), pair_value(ti[2])};
-    const Vec3<double> tjd{pair_value(tj[0]), pair_value(tj[1]), pair_value(tj[2])};
-    return bond_breaks(Fd, tid, tjd, d.b_invA[small], d.b_rbI[small], p);
+    return bond_breaks_pairs(F, ti, tj, d.b_invA[small], d.b_rbI[small], p);
 }
 
 // FP32 hi/lo pair accumulator (hi + lo carries about 48 bits): (hi, lo) + x
@@ -950,15 +971,22 @@ struct Frame32 {
     float a1, a2, a3, f;
     bool neg3;
 };
+static __device__ __noinline__ Frame32 frame32_exact(double dx, double dy, double dz, double tol) {
+    const double L = norm_rn(dx, dy, dz);
+    const double il = __ddiv_rn(1.0, L);
+    const Frame F = frame_exact(__dmul_rn(il, dx), __dmul_rn(il, dy), __dmul_rn(il, dz), tol);
+    return {(float)F.a1, (float)F.a2, (float)F.a3, (float)F.f, F.neg3};
+}
 __device__ __forceinline__ Frame32 contact_frame32(float ax, float ay, float az, double dx,
                                                    double dy, double dz, const SceneParams& S) {
     const float s2 = ay * ay + az * az;
-    if (s2 < S.f_tol4) {
-        const double L = norm_rn(dx, dy, dz);
-        const double il = __ddiv_rn(1.0, L);
-        const Frame F = frame_exact(__dmul_rn(il, dx), __dmul_rn(il, dy), __dmul_rn(il, dz), S.tol);
-        return {(float)F.a1, (float)F.a2, (float)F.a3, (float)F.f, F.neg3};
+    // s² below tol² by a relative 2^-10 (the FP32 normal is within 1e-6):
+    // the reference's degenerate branch, decided without FP64
+    if (s2 < S.f_tol1) {
+        const float sg = ax > 0.0f ? 1.0f : -1.0f;
+        return {sg, 0.0f, 0.0f, 0.0f, sg < 0.0f};
     }
+    if (s2 < S.f_tol4) return frame32_exact(dx, dy, dz, S.tol);
     return {ax, ay, az, (1.0f - ax) / s2, false};
 }
 __device__ __forceinline__ Vec3<float> rot32(const Frame32& R, Vec3<float> v) {
@@ -982,8 +1010,9 @@ __device__ __forceinline__ Vec3<float> rot_t32(const Frame32& R, Vec3<float> v) 
 // bits) stored in their FP64 slots, and the bond-breakage decision is the
 // FP64 test's.  Contact forces are stored as (F, 0) pairs in this mode; the
 // host decodes them, and a precision switch re-encodes the stored contacts
-// (k_recode).  FP64↔FP32 conversions run on the FP64 pipe, so the path keeps
-// them to the differences it must form in FP64.  The Hertz overlap is
+// (k_recode).  The FP64 differences are narrowed with d2f (integer pipe), so
+// the FP64 pipe only forms the differences and the contact point.  The Hertz
+// overlap is
 // (L² - (rᵢ+rⱼ)²)/(L + rᵢ + rⱼ) with the numerator in FP64, which keeps the
 // overlap's relative error at FP32 rounding even though L is FP32.
 __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
@@ -991,7 +1020,7 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
                                         int sc, size_t cap) {
     const double kix = d.px[i], kiy = d.py[i], kiz = d.pz[i];
     const double dxd = d.px[j] - kix, dyd = d.py[j] - kiy, dzd = d.pz[j] - kiz;
-    const float dx = (float)dxd, dy = (float)dyd, dz = (float)dzd;
+    const float dx = d2f(dxd), dy = d2f(dyd), dz = d2f(dzd);
     const float L2 = dx * dx + dy * dy + dz * dz;
     const float invL = rsqrtf(L2);
     const float ax = dx * invL, ay = dy * invL, az = dz * invL;
@@ -1002,11 +1031,11 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
         // EBPM (src/kernels.jl:170-239), increments in FP32
         const double wix = d.wx[i], wiy = d.wy[i], wiz = d.wz[i];
         const double wjx = d.wx[j], wjy = d.wy[j], wjz = d.wz[j];
-        const Vec3<float> D = rot32(R, {(float)(d.vx[i] - d.vx[j]), (float)(d.vy[i] - d.vy[j]),
-                                        (float)(d.vz[i] - d.vz[j])});
+        const Vec3<float> D = rot32(R, {d2f(d.vx[i] - d.vx[j]), d2f(d.vy[i] - d.vy[j]),
+                                        d2f(d.vz[i] - d.vz[j])});
         const Vec3<float> Sv =
-            rot32(R, {(float)(wix + wjx), (float)(wiy + wjy), (float)(wiz + wjz)});
-        const Vec3<float> Q = rot32(R, {(float)(wix - wjx), (float)(wiy - wjy), (float)(wiz - wjz)});
+            rot32(R, {d2f(wix + wjx), d2f(wiy + wjy), d2f(wiz + wjz)});
+        const Vec3<float> Q = rot32(R, {d2f(wix - wjx), d2f(wiy - wjy), d2f(wiz - wjz)});
         const float4 rmi = d.rm32[i], rmj = d.rm32[j];
         const bool i_small = rmi.z <= rmj.z;
         const int small = i_small ? i : j;   // rb = ρ·min(rᵢ, rⱼ)
@@ -1064,18 +1093,18 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
         const double Rsum = ri + rj;
         const double num = (dxd * dxd + dyd * dyd + dzd * dzd) - Rsum * Rsum;
         const float L = L2 * invL;
-        const float gap = (float)num / (L + (float)Rsum);
+        const float gap = d2f(num) / (L + d2f(Rsum));
         if (num > 0.0) atomicAdd(&d.sctr[sc].warn_gap, 1ull);
         const float ext = rmi.z - fabsf(gap);
         const Vec3<float> kri{ax * ext, ay * ext, az * ext};
-        st3(w.f, CK, c, {kix + (double)kri.x, kiy + (double)kri.y, kiz + (double)kri.z});
+        st3(w.f, CK, c, {kix + f2d(kri.x), kiy + f2d(kri.y), kiz + f2d(kri.z)});
         const Vec3<float> krj{kri.x - dx, kri.y - dy, kri.z - dz};
-        const Vec3<float> wi{(float)d.wx[i], (float)d.wy[i], (float)d.wz[i]};
-        const Vec3<float> wj{(float)d.wx[j], (float)d.wy[j], (float)d.wz[j]};
+        const Vec3<float> wi{d2f(d.wx[i]), d2f(d.wy[i]), d2f(d.wz[i])};
+        const Vec3<float> wj{d2f(d.wx[j]), d2f(d.wy[j]), d2f(d.wz[j])};
         const Vec3<float> wci = cross3<float>(wi, kri), wcj = cross3<float>(wj, krj);
-        const Vec3<float> dv{(float)(d.vx[j] - d.vx[i]) + (wcj.x - wci.x),
-                             (float)(d.vy[j] - d.vy[i]) + (wcj.y - wci.y),
-                             (float)(d.vz[j] - d.vz[i]) + (wcj.z - wci.z)};
+        const Vec3<float> dv{d2f(d.vx[j] - d.vx[i]) + (wcj.x - wci.x),
+                             d2f(d.vy[j] - d.vy[i]) + (wcj.y - wci.y),
+                             d2f(d.vz[j] - d.vz[i]) + (wcj.z - wci.z)};
         const Vec3<float> vc = rot32(R, dv);
         const float fri = rmi.z, frj = rmj.z, tmi = rmi.y, tmj = rmj.y;
         const float Rs = fri * frj / (fri + frj);
@@ -1090,9 +1119,9 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
             atomicAdd(&d.sctr[sc].warn_damp, (unsigned long long)((gn < 0.0f) + (gt < 0.0f)));
         // 𝐬 += (0, vc₂, vc₃)·dt in FP64 (the normal component stays)
         Vec3<double> s = ld3(w.f, CS, c);
-        s = {s.x, s.y + (double)(vc.y * SP.f_dt), s.z + (double)(vc.z * SP.f_dt)};
+        s = {s.x, s.y + f2d(vc.y * SP.f_dt), s.z + f2d(vc.z * SP.f_dt)};
         const float F1 = -kn * gap - gn * vc.x;
-        const Vec3<float> Ft{-kt * (float)s.x, -kt * (float)s.y, -kt * (float)s.z};
+        const Vec3<float> Ft{-kt * d2f(s.x), -kt * d2f(s.y), -kt * d2f(s.z)};
         const float nFt = sqrtf(Ft.x * Ft.x + Ft.y * Ft.y + Ft.z * Ft.z);
         const float muF1 = SP.f_mu * F1;
         float F2, F3;
@@ -1100,7 +1129,7 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
             const float ratio = muF1 / nFt;
             F2 = ratio * Ft.y;
             F3 = ratio * Ft.z;
-            s = {s.x, (double)(F2 / kt), (double)(F3 / kt)};
+            s = {s.x, f2d(F2 / kt), f2d(F3 / kt)};
         } else {
             F2 = Ft.y - gt * vc.y;
             F3 = Ft.z - gt * vc.z;
@@ -1412,8 +1441,8 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
         gather<float>(d, p, i, nxt, Ff, Mf);
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            F[q] = (double)Ff[q];
-            M[q] = (double)Mf[q];
+            F[q] = f2d(Ff[q]);
+            M[q] = f2d(Mf[q]);
         }
     } else {
         gather<double>(d, p, i, nxt, F, M);
@@ -1424,8 +1453,22 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     const double wx = d.wx[i], wy = d.wy[i], wz = d.wz[i];
     const double r = d.r[i], m = d.m[i];
     const double dt = S.dt;
-    // resolve_wall!, one wall
+    // resolve_wall!, one wall.  An FP32 screen on the step's starting position
+    // (pos32, within 2^-24 of the FP64 one per coordinate) skips the exact
+    // test when |n·x - d| exceeds r by a margin that covers its rounding.
+    bool wall_near = true;
     if (S.has_wall) {
+        const float4 q = d.pos32[i];
+        const float Lf = q.x * S.f_wn[0] + q.y * S.f_wn[1] + q.z * S.f_wn[2] + S.f_wc0;
+        const float rf = d.rm32[i].z;
+        const float mg = (fabsf(q.x) + fabsf(q.y) + fabsf(q.z) + fabsf(S.f_wc0) + rf) * 0x1p-20f;
+        wall_near = !(fabsf(Lf) > rf + mg);
+    }
+    if (S.has_wall && !wall_near) {
+        d.wsx[i] = 0.0;
+        d.wsy[i] = 0.0;
+        d.wsz[i] = 0.0;
+    } else if (S.has_wall) {
         const double dotkn = __dadd_rn(__dadd_rn(__dmul_rn(x, S.wn[0]), __dmul_rn(y, S.wn[1])),
                                        __dmul_rn(z, S.wn[2]));
         const double L = __dsub_rn(dotkn, S.wd);
@@ -1503,7 +1546,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     // update!
     const double invm = d.inv_m[i];
     const double ax = F[0] * invm, ay = F[1] * invm, az = F[2] * invm;
-    const double hdt2 = 0.5 * (dt * dt);
+    const double hdt2 = S.hdt2;  // 0.5·(dt·dt)
     const double px1 = x + vx * dt + ax * hdt2, py1 = y + vy * dt + ay * hdt2,
                  pz1 = z + vz * dt + az * hdt2;
     d.px[i] = px1;
@@ -1514,8 +1557,8 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     // from where its list was built (FP32 rounding of both positions is
     // taken off the allowance)
     {
-        const float fx = (float)(px1 - S.dmin[0]), fy = (float)(py1 - S.dmin[1]),
-                    fz = (float)(pz1 - S.dmin[2]);
+        const float fx = d2f(px1 - S.dmin[0]), fy = d2f(py1 - S.dmin[1]),
+                    fz = d2f(pz1 - S.dmin[2]);
         d.pos32[i] = make_float4(fx, fy, fz, reach32(fx, fy, fz, d.rm32[i].z));
         bool moved = false;
         if (S.f_half_skin > 0.0f) {
@@ -1722,10 +1765,65 @@ void launch_cplist_fill(const DemDev& d, const DemParams& p, const int32_t* off,
     if (p.n == 0) return;
     k_cp_fill<<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, off, cp);
 }
+// Self-test of d2f / f2d against the hardware conversions: thread t draws a
+// binary64 value (random significand, exponents spread over and beyond the
+// binary32 range, every 8th one a rounding tie) and a binary32 value, and
+// counts results whose bits differ.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+__global__ void k_selftest_conv(long long n, unsigned long long seed, unsigned long long* bad) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const unsigned long long r1 = mix64(seed ^ (unsigned long long)t);
+    const unsigned long long r2 = mix64(r1);
+    // exponent field within [1023-160, 1023+160]: subnormal, normal and overflowing results
+    const unsigned long long ex = 1023ull - 160ull + (r2 % 321ull);
+    unsigned long long sig = r1 & 0xfffffffffffffull;
+    if ((t & 7) == 0) sig = (sig & ~0x3fffffffull) | 0x10000000ull;  // exact tie
+    unsigned long long bits = ((r2 >> 63) << 63) | (ex << 52) | sig;
+    if ((t & 15) == 1) bits &= 0x8000000000000000ull;  // ±0
+    const double x = __longlong_as_double((long long)bits);
+    const unsigned a = __float_as_uint(d2f(x)), b = __float_as_uint(__double2float_rn(x));
+    const float f = __uint_as_float((t & 15) == 2 ? ((unsigned)r2 & 0x80000000u) : (unsigned)r2);
+    const unsigned long long c = (unsigned long long)__double_as_longlong(f2d(f));
+    const unsigned long long e = (unsigned long long)__double_as_longlong((double)f);
+    if (a != b) atomicAdd(bad, 1ull);
+    if (c != e && !isnan(f)) atomicAdd(bad + 1, 1ull);
+}
+
+void launch_selftest_conv(long long n, unsigned long long seed, unsigned long long* bad,
+                          cudaStream_t s) {
+    if (n <= 0) return;
+    k_selftest_conv<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, seed, bad);
+}
+
 void launch_scene_flags(const DemDev& d, const DemParams& p, int cur, bool multi, cudaStream_t s) {
     if (p.n == 0 || p.ns <= 0) return;
     if (multi) k_scene_flags<true><<<blocks_for(p.ns, 128), 128, 0, s>>>(d, p, cur);
     else k_scene_flags<false><<<blocks_for(p.ns, 128), 128, 0, s>>>(d, p, cur);
+}
+
+template <bool MULTI>
+__global__ void k_refresh_pos32(DemDev d, DemParams p, int first, int n) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int i = first + t;
+    const int sc = slot_scene<MULTI>(d, i);
+    if (MULTI && sc < 0) return;
+    const SceneParams& S = scene_rec<MULTI>(d, p, sc);
+    const float fx = d2f(d.px[i] - S.dmin[0]), fy = d2f(d.py[i] - S.dmin[1]),
+                fz = d2f(d.pz[i] - S.dmin[2]);
+    d.pos32[i] = make_float4(fx, fy, fz, reach32(fx, fy, fz, d.rm32[i].z));
+}
+void launch_refresh_pos32(const DemDev& d, const DemParams& p, bool multi, int first, int n,
+                          cudaStream_t s) {
+    if (n <= 0) return;
+    if (multi) k_refresh_pos32<true><<<blocks_for(n, kThreads), kThreads, 0, s>>>(d, p, first, n);
+    else k_refresh_pos32<false><<<blocks_for(n, kThreads), kThreads, 0, s>>>(d, p, first, n);
 }
 
 void launch_recode(const DemDev& d, int buf, int n, bool to_pairs, cudaStream_t s) {

@@ -317,3 +317,14 @@ def test_capacity_overflow_reports_error(gpu):
     with pytest.raises(DemError) as e:
         g.initialize()
     assert e.value.code == DEM_ERR_CAPACITY
+
+
+def test_integer_pipe_conversions_match_hardware(gpu):
+    """The FP64<->FP32 conversions done with integer instructions round
+    exactly as the hardware conversions (ties, range edges, subnormal and
+    overflowing results included)."""
+    import ctypes
+    bad = (ctypes.c_int64 * 2)()
+    for seed in (1, 2, 3):
+        assert gpu.dem_selftest_conversions(1 << 22, seed, bad) == 0
+        assert (bad[0], bad[1]) == (0, 0), (seed, bad[0], bad[1])
