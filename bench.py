@@ -54,12 +54,38 @@ import numpy as np  # noqa: E402
 # force contributions (9 × 8 B).
 FORCE_BYTES_BOND = 12 + 176 + 72 + 120 + 72
 FORCE_BYTES_HERTZ = 12 + 176 + 24 + 72 + 72
+# Compaction per surviving contact: ids + flags read and written (2 × 12 B),
+# the carried state read and written (bond 𝐅, 𝛕ᵢ, 𝛕ⱼ: 2 × 72 B; Hertz 𝐬:
+# 2 × 24 B) and the incoming-list entry (8 B).
+COMPACT_BYTES_BOND = 24 + 144 + 8
+COMPACT_BYTES_HERTZ = 24 + 48 + 8
 # Algorithmic bytes of the other phases per particle / per contact
 BROADPHASE_BYTES_PER_PARTICLE = 24 + 16 + 4 + 4 + 4 + 8 + 24 + 8 + 32 + 16  # hash..canon
 INTEGRATE_BYTES_PER_PARTICLE = 13 * 8 * 2 + 4 * 8 + 6 * 8 + 3 * 8 * 2 + 8 + 4  # state r/w
+# neighbour-list step per particle: path byte, current row bounds, list length,
+# FP32 position, row length written, 4 list partners (index + FP32 position)
+DETECT_BYTES_PER_PARTICLE = 1 + 8 + 4 + 16 + 8 + 4 * (4 + 16)
 # hash, scan, scatter, canon, detect, list detect, rows, compact, force, integrate, flags
 KERNELS_PER_STEP = 11
 L2_FLUSH_BYTES = 256 << 20
+
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
+# of each dominant kernel, from one ncu capture each (the summaries under
+# profiles/), with the particles that launch processed.  The batched captures
+# ran on the first 64 scenes of the batch (431,416 spheres); their traffic is
+# scaled to a launch by particles processed.
+NCU_TRAFFIC = {
+    ("c2", "force"): (6.419456e6, 17576),          # k_force<double>
+    ("c4", "force"): (145.409024e6, 431416),       # k_force<float>
+    ("c4", "integrate"): (186.321408e6, 431416),   # k_integrate (FP32 gather)
+    ("c4", "compact"): (113.883648e6, 431416),     # k_compact
+    ("c4", "detect"): (33.391104e6, 431416),       # k_vdetect (list steps)
+}
+
+
+def ncu_traffic(workload: str, kernel: str, n: int):
+    t = NCU_TRAFFIC.get((workload, kernel))
+    return None if t is None else t[0] * n / t[1]
 
 
 def load_peaks() -> dict:
@@ -214,10 +240,13 @@ def run_batched(args, lib, quick: bool = False) -> dict:
     peaks = load_peaks()
     force_bytes = bonded * FORCE_BYTES_BOND + (contacts - bonded) * FORCE_BYTES_HERTZ
     alg = {"force": force_bytes, "broadphase": n_total * BROADPHASE_BYTES_PER_PARTICLE,
-           "integrate": n_total * INTEGRATE_BYTES_PER_PARTICLE}
+           "integrate": n_total * INTEGRATE_BYTES_PER_PARTICLE,
+           "detect": n_total * DETECT_BYTES_PER_PARTICLE,
+           "compact": bonded * COMPACT_BYTES_BOND + (contacts - bonded) * COMPACT_BYTES_HERTZ}
     dom = max(ph, key=ph.get)
     roof = {"bound": "hbm", "kernel": dom, "unit": "GB/s", "peak": peaks["hbm_gbs"],
-            "peak_source": peaks["source"], "traffic": None, "phase_ms": ph}
+            "peak_source": peaks["source"], "traffic": ncu_traffic("c4", dom, n_total),
+            "phase_ms": ph}
     if dom in alg:
         ach = alg[dom] / (ph[dom] * 1e-3) / 1e9
         roof.update({"achieved": ach, "frac": ach / peaks["hbm_gbs"], "algorithmic_bytes": alg[dom]})
@@ -509,13 +538,15 @@ def main() -> None:
     force_bytes = n_bond * FORCE_BYTES_BOND + (c_now - n_bond) * FORCE_BYTES_HERTZ
     alg = {"force": force_bytes,
            "broadphase": sc.n * BROADPHASE_BYTES_PER_PARTICLE,
-           "integrate": sc.n * INTEGRATE_BYTES_PER_PARTICLE}
+           "integrate": sc.n * INTEGRATE_BYTES_PER_PARTICLE,
+           "detect": sc.n * DETECT_BYTES_PER_PARTICLE,
+           "compact": n_bond * COMPACT_BYTES_BOND + (c_now - n_bond) * COMPACT_BYTES_HERTZ}
     dom = max(ph, key=ph.get)
     dom_bytes = alg.get(dom)
     peaks = load_peaks()
     roofline = {"bound": "hbm", "kernel": dom, "unit": "GB/s",
                 "peak": peaks["hbm_gbs"], "peak_source": peaks["source"],
-                "traffic": None, "phase_ms": ph}
+                "traffic": ncu_traffic(args.workload, dom, sc.n), "phase_ms": ph}
     if dom_bytes is not None:
         ach = dom_bytes / (ph[dom] * 1e-3) / 1e9
         roofline.update({"achieved": ach, "frac": ach / peaks["hbm_gbs"],

@@ -222,6 +222,8 @@ typedef struct DemLaunchShape {
     int32_t compact_grid;
     int32_t integrate_block;
     int32_t detect_blocks_per_sm; /* register budget of the pair search: 3 or 4 (0 = 4) */
+    int32_t force_blocks_per_sm;  /* FP32 force kernel: 0 (compiler's choice) or 4     */
+    int32_t pad;
 } DemLaunchShape;
 
 int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* shape);

@@ -22,6 +22,7 @@ BLOCKS = (128, 256)
 GRIDS_PER_SM = (4, 8, 16, 32)
 INTEGRATE_BLOCKS = (128, 256)
 DETECT_BLOCKS = (3, 4)  # pair-search register budget (blocks per SM)
+FORCE_BLOCKS = (0, 4)   # FP32 force kernel register budget (0: compiler's choice)
 
 
 @dataclass
@@ -45,7 +46,8 @@ def _time(target, steps: int) -> float:
 
 def autotune(target, sm_count: int = 152, steps: int = 10, cell_factors=CELL_FACTORS,
              blocks=BLOCKS, grids_per_sm=GRIDS_PER_SM,
-             integrate_blocks=INTEGRATE_BLOCKS, detect_blocks=DETECT_BLOCKS) -> TuneResult:
+             integrate_blocks=INTEGRATE_BLOCKS, detect_blocks=DETECT_BLOCKS,
+             force_blocks=FORCE_BLOCKS) -> TuneResult:
     """Tunes `target` in place and returns the chosen settings."""
     trials = []
     is_arena = hasattr(target, "set_cell_factor")
@@ -79,6 +81,13 @@ def autotune(target, sm_count: int = 152, steps: int = 10, cell_factors=CELL_FAC
             best, shape = t, cand
     for ib in integrate_blocks:
         cand = dict(shape, integrate_block=ib)
+        target.set_launch_shape(**cand)
+        t = _time(target, steps)
+        trials.append((cand, t))
+        if t < best:
+            best, shape = t, cand
+    for fb in force_blocks:
+        cand = dict(shape, force_blocks_per_sm=fb)
         target.set_launch_shape(**cand)
         t = _time(target, steps)
         trials.append((cand, t))

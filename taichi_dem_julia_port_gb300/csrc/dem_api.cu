@@ -439,6 +439,7 @@ int allocate(DemHandle* h) {
     TRY(dalloc(h, &d.vl_len, n));
     TRY(dalloc(h, &d.xref, n));
     TRY(dalloc(h, &d.pos32, n));
+    TRY(dalloc(h, &d.path, n));
     for (int b = 0; b < 2; ++b) TRY(dalloc(h, &d.sflags[b], (size_t)std::max(h->s_cap, 1)));
     if (h->multi) {
         TRY(dalloc(h, &d.scene_of, n));
@@ -467,7 +468,7 @@ int init_handle(DemHandle* h) {
     CU(cudaEventCreate(&h->ev1));
     TRY(allocate(h));
     h->ntiles_cells = std::max(1, scan_tiles((int64_t)h->p.T));
-    h->shape = LaunchShape{256, h->sm_count * 16, 256, h->sm_count * 16, 256, 4};
+    h->shape = LaunchShape{256, h->sm_count * 16, 256, h->sm_count * 16, 256, 4, 0};
     return DEM_OK;
 }
 
@@ -834,13 +835,15 @@ int get_contacts_range(DemHandle* h, int64_t p0, int64_t n, DemContacts* out, in
         const int32_t c = act[t];
         if (out->i) out->i[t] = (int32_t)(ci[c] - p0);
         if (out->j) out->j[t] = (int32_t)(cj[c] - p0);
-        if (out->bonded) out->bonded[t] = (fl[c] & kBonded) ? 1 : 0;
+        const bool bonded = (fl[c] & kBonded) != 0;
+        if (out->bonded) out->bonded[t] = bonded ? 1 : 0;
+        // a bond's 𝐬 and a Hertz contact's torques are zero (not stored)
         for (int q = 0; q < 3; ++q) {
             if (out->point) out->point[3 * t + q] = f[CK + q][c];
             if (out->force) out->force[3 * t + q] = f[CF + q][c];
-            if (out->torque_i) out->torque_i[3 * t + q] = f[CTI + q][c];
-            if (out->torque_j) out->torque_j[3 * t + q] = f[CTJ + q][c];
-            if (out->shear) out->shear[3 * t + q] = f[CS + q][c];
+            if (out->torque_i) out->torque_i[3 * t + q] = bonded ? f[CTI + q][c] : 0.0;
+            if (out->torque_j) out->torque_j[3 * t + q] = bonded ? f[CTJ + q][c] : 0.0;
+            if (out->shear) out->shear[3 * t + q] = bonded ? 0.0 : f[CS + q][c];
         }
     }
     return DEM_OK;
@@ -1140,22 +1143,25 @@ int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* sh) {
     if (!h || !sh || sh->force_block < 32 || sh->force_block > 256 || sh->force_block % 32 ||
         (sh->detect_blocks_per_sm != 0 && sh->detect_blocks_per_sm != 3 &&
          sh->detect_blocks_per_sm != 4) ||
+        (sh->force_blocks_per_sm != 0 && sh->force_blocks_per_sm != 4) ||
         sh->compact_block < 32 || sh->compact_block > 256 || sh->compact_block % 32 ||
         sh->integrate_block < 32 || sh->integrate_block > 256 || sh->integrate_block % 32 ||
         sh->force_grid < 1 || sh->compact_grid < 1)
         return DEM_ERR_INVALID;
     h->shape = LaunchShape{sh->force_block, sh->force_grid, sh->compact_block, sh->compact_grid,
                            sh->integrate_block,
-                           sh->detect_blocks_per_sm ? sh->detect_blocks_per_sm : 4};
+                           sh->detect_blocks_per_sm ? sh->detect_blocks_per_sm : 4,
+                           sh->force_blocks_per_sm};
     drop_graphs(h);
     return DEM_OK;
 }
 
 int dem_get_launch_shape(DemHandle* h, DemLaunchShape* out) {
     if (!h || !out) return DEM_ERR_INVALID;
-    *out = DemLaunchShape{h->shape.force_block, h->shape.force_grid, h->shape.compact_block,
-                          h->shape.compact_grid, h->shape.integrate_block,
-                          h->shape.detect_blocks_per_sm};
+    *out = DemLaunchShape{h->shape.force_block,         h->shape.force_grid,
+                          h->shape.compact_block,       h->shape.compact_grid,
+                          h->shape.integrate_block,     h->shape.detect_blocks_per_sm,
+                          h->shape.force_blocks_per_sm, 0};
     return DEM_OK;
 }
 

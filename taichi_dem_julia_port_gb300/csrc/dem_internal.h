@@ -134,6 +134,7 @@ struct DemDev {
     float4* xref;
     float4* pos32;
     uint32_t* sflags[2];
+    uint8_t* path;  // this step: 0 free slot, 1 full search, 2 list (stepping), 3 list (held)
     SceneParams* sp;                      // arena: scene records; null otherwise
     SceneCounters* sctr;                  // per-scene event counters
     // broad phase
@@ -188,6 +189,7 @@ struct LaunchShape {
     int compact_block, compact_grid;
     int integrate_block;
     int detect_blocks_per_sm;  // register budget of the pair search: 3 or 4 blocks per SM
+    int force_blocks_per_sm;   // register budget of the FP32 force kernel: 0 (none) or 4
 };
 
 // ---- launchers (dem_kernels.cu) --------------------------------------------

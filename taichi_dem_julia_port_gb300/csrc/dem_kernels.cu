@@ -241,11 +241,14 @@ __global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p, int cu
             d.bucket[i] = kNoBucket;
             d.row_len[cur ^ 1][i] = 0;
             d.row_start[cur ^ 1][i] = 0;
+            d.path[i] = 0;
             act = false;
         } else if (!full_search(d, cur, sc, mode, all)) {
             d.bucket[i] = kNoBucket;  // this scene tests its neighbour lists
+            d.path[i] = mode == kModeFrozen ? 3 : 2;
             act = false;
         } else {
+            d.path[i] = 1;
             const SceneParams& S = scene_rec<MULTI>(d, p, sc);
             const double pos[3] = {d.px[i], d.py[i], d.pz[i]};
             int4 ci = cell_of_screened(pos, S.dmin, S.cell, S.inv_cell, S.f_inv_cell, S.f_dmin_cells);
@@ -593,11 +596,9 @@ __global__ void __launch_bounds__(kThreads) k_vdetect(DemDev d, DemParams p, int
     const ContactSoA o = d.c[cur];
     for (int i = blockIdx.x * (kThreads / kVLanes) + g; i < p.n;
          i += gridDim.x * (kThreads / kVLanes)) {
-        const int sc = slot_scene<MULTI>(d, i);
-        const int mode = MULTI ? (sc < 0 ? kModeFree : d.sp[sc].mode) : kModeStep;
-        if (mode == kModeFree || full_search(d, cur, sc, mode, 0)) continue;
-        const SceneParams& S = scene_rec<MULTI>(d, p, sc);
-        const bool frozen = mode == kModeFrozen;
+        const uint8_t path = d.path[i];  // set by k_hash this step
+        if (path < 2) continue;
+        const bool frozen = path == 3;
         if (lane == 0) sh[g].nnew = 0;
         const int e0 = d.row_start[cur][i];
         const int e1 = e0 + d.row_len[cur][i];
@@ -615,7 +616,10 @@ __global__ void __launch_bounds__(kThreads) k_vdetect(DemDev d, DemParams p, int
             } else {
                 const bool valid = touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j],
                                                d.pz[j], d.r[i], d.r[j]);
-                keep = (valid || !in_cp_list<MULTI>(d, S, i, j)) ? 1 : 0;
+                keep = (valid || !in_cp_list<MULTI>(d, scene_rec<MULTI>(d, p, slot_scene<MULTI>(d, i)),
+                                                     i, j))
+                           ? 1
+                           : 0;
                 ended += 1 - keep;
             }
             d.keep[e2] = (uint8_t)keep;
@@ -665,8 +669,11 @@ __global__ void __launch_bounds__(kThreads) k_vdetect(DemDev d, DemParams p, int
             }
             d.nnew[i] = nnew;
             d.row_len[nxt][i] = nkeep + nnew;
-            if (ended) atomicAdd(&d.sctr[sc].ended, (unsigned long long)ended);
-            if (nnew) atomicAdd(&d.sctr[sc].created, (unsigned long long)nnew);
+            if (ended || nnew) {
+                const int sc = slot_scene<MULTI>(d, i);
+                if (ended) atomicAdd(&d.sctr[sc].ended, (unsigned long long)ended);
+                if (nnew) atomicAdd(&d.sctr[sc].created, (unsigned long long)nnew);
+            }
         }
         __syncwarp(gmask);
     }
@@ -735,20 +742,37 @@ __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int
     const int stride = gridDim.x * blockDim.x;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cold + p.n; t += stride) {
         if (t < cold) {
-            const uint8_t kp = d.keep[t];
-            const int i = o.ci[t], j = o.cj[t];
-            const uint32_t fl = o.fl[t];
-            double v[15];
-#pragma unroll
-            for (int f = 0; f < 15; ++f) v[f] = o.f[f][t];
-            if (!kp || i >= p.n) continue;
+            if (!d.keep[t]) continue;
+            const int i = o.ci[t];
+            if (i >= p.n) continue;
             // entries outside the owner's current row are left-overs of a
             // removed scene (arena) and are dropped
             const int r0 = d.row_start[cur][i];
             if (t < r0 || t >= r0 + d.row_len[cur][i]) continue;
             const int rl = d.row_len[nxt][i];
             if (rl == 0) continue;  // row dropped after a capacity overflow, or a free slot
+            const int j = o.cj[t];
+            const uint32_t fl = o.fl[t];
             const int mode = MULTI ? d.sp[d.scene_of[i]].mode : (INIT ? kModeInit : kModeStep);
+            // A stepping contact carries only the state the next force pass
+            // reads: a bond its accumulated 𝐅, 𝛕ᵢ, 𝛕ⱼ, a Hertz contact its 𝐬 (the
+            // force pass rewrites 𝐤 and 𝐅; a bond's 𝐬 and a Hertz contact's
+            // torques are zero, reported as such by the host).  Contacts of
+            // scenes that do not step keep every field.  The loads are issued
+            // before the slot is computed (unrolled: the column pointers stay
+            // in registers).
+            const int kind = mode != kModeStep ? 0 : ((fl & kBonded) ? 1 : 2);
+            double v[15];
+            if (kind == 0) {
+#pragma unroll
+                for (int f = 0; f < 15; ++f) v[f] = o.f[f][t];
+            } else if (kind == 1) {
+#pragma unroll
+                for (int f = CF; f < CS; ++f) v[f] = o.f[f][t];
+            } else {
+#pragma unroll
+                for (int f = CS; f < CS + 3; ++f) v[f] = o.f[f][t];
+            }
             int pos = d.row_start[nxt][i];
             for (int q = r0; q < t; ++q) pos += d.keep[q];
             const int nn = d.nnew[i];
@@ -757,8 +781,16 @@ __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int
             w.ci[pos] = i;
             w.cj[pos] = j;
             w.fl[pos] = fl;
+            if (kind == 0) {
 #pragma unroll
-            for (int f = 0; f < 15; ++f) w.f[f][pos] = v[f];
+                for (int f = 0; f < 15; ++f) w.f[f][pos] = v[f];
+            } else if (kind == 1) {
+#pragma unroll
+                for (int f = CF; f < CS; ++f) w.f[f][pos] = v[f];
+            } else {
+#pragma unroll
+                for (int f = CS; f < CS + 3; ++f) w.f[f][pos] = v[f];
+            }
             if (mode == kModeStep) {
                 const int slot = atomicAdd(&d.in_cnt[j], 1);
                 if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = make_int2(pos, i);
@@ -1166,7 +1198,7 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
 // k₅𝛉ᵢ + k₆𝛉ⱼ and k₆𝛉ᵢ + k₅𝛉ⱼ are k₊𝛉ₛ ± k₋𝛉_d with k₊ = (k₅+k₆)/2 =
 // 3EI/L/(1+ϕ) and k₋ = (k₅-k₆)/2 = EI/L; dt is folded into the stiffnesses.
 template <typename T, bool MULTI>
-__global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int nxt) {
+__device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, int nxt) {
     const int C = min((int)d.ctr->row_alloc[nxt], p.cap);
     const ContactSoA w = d.c[nxt];
     const int stride = gridDim.x * blockDim.x;
@@ -1232,8 +1264,7 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
                 st3(w.f, CK, c, {(ki.x + kj.x) * 0.5, (ki.y + kj.y) * 0.5, (ki.z + kj.z) * 0.5});
                 st3(w.f, CF, c, Fi);
                 st3(w.f, CTI, c, ti);
-                st3(w.f, CTJ, c, tj);
-                st3(w.f, CS, c, {0.0, 0.0, 0.0});
+                st3(w.f, CTJ, c, tj);  // a bond's 𝐬 stays zero and is not stored
             }
         } else {
             // Hertz-Mindlin (src/kernels.jl:240-313)
@@ -1292,6 +1323,17 @@ __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int n
         d.contrib[7 * cap + c] = (double)mj.y;
         d.contrib[8 * cap + c] = (double)mj.z;
     }
+}
+
+// The force pass with the compiler's register choice, and with a budget for
+// four 256-thread blocks per SM (an autotuner choice for the FP32 mode).
+template <typename T, bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int nxt) {
+    force_body<T, MULTI>(d, p, nxt);
+}
+template <typename T, bool MULTI>
+__global__ void __launch_bounds__(kThreads, 4) k_force4(DemDev d, DemParams p, int nxt) {
+    force_body<T, MULTI>(d, p, nxt);
 }
 
 // ---------------------------------------------------------------------------
@@ -1734,8 +1776,14 @@ void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, cons
     const int block = clamp_block(sh.force_block);
     const int grid = min(blocks_for(p.cap, block), max(sh.force_grid, 1));
     if (p.precision == 1) {
-        if (multi) k_force<float, true><<<grid, block, 0, s>>>(d, p, nxt);
-        else k_force<float, false><<<grid, block, 0, s>>>(d, p, nxt);
+        // FP32 mode: register budget for 3 (default) or 4 blocks of 256 per SM
+        if (sh.force_blocks_per_sm == 4) {
+            if (multi) k_force4<float, true><<<grid, block, 0, s>>>(d, p, nxt);
+            else k_force4<float, false><<<grid, block, 0, s>>>(d, p, nxt);
+        } else {
+            if (multi) k_force<float, true><<<grid, block, 0, s>>>(d, p, nxt);
+            else k_force<float, false><<<grid, block, 0, s>>>(d, p, nxt);
+        }
     } else {
         if (multi) k_force<double, true><<<grid, block, 0, s>>>(d, p, nxt);
         else k_force<double, false><<<grid, block, 0, s>>>(d, p, nxt);
