@@ -381,9 +381,11 @@ const char* dem_strerror(int code);
 
 /* Self-test: compares the library's integer-pipe FP64->FP32 and FP32->FP64
  * conversions (used by the FP32 force mode and the neighbour lists) with the
- * hardware conversions on n seeded random values; mismatches[0] / [1]
- * receive the narrowing / widening mismatch counts (both 0 when exact).  No
- * counterpart in the reference. */
+ * hardware conversions, and its Newton-Raphson FP64 reciprocal with the
+ * correctly rounded one, on n seeded random values; mismatches[0] / [1] /
+ * [2] receive the narrowing / widening mismatch counts and the reciprocals
+ * more than 2 ulp off (all 0 when correct).  No counterpart in the
+ * reference. */
 int dem_selftest_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
 
 /* Library version string, e.g. "dem_gb300 0.1.0 sm_103a". */

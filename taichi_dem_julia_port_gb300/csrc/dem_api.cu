@@ -301,6 +301,8 @@ int prepare_scene(const DemConfigC* cfg, const DemParticlesIn* pin, double cell_
     p.f_tol4 = (float)(4.0 * p.tol * p.tol);
     p.f_tol1 = (float)(p.tol * p.tol * (1.0 - 0x1p-10));
     p.hdt2 = 0.5 * (p.dt * p.dt);
+    p.tol2_lo = p.tol * p.tol * (1.0 - 0x1p-30);
+    p.tol2_x4 = 4.0 * p.tol * p.tol;
     double c0 = -p.wd;
     for (int c = 0; c < 3; ++c) {
         p.f_wn[c] = (float)p.wn[c];
@@ -900,8 +902,8 @@ int dem_selftest_conversions(int64_t n, uint64_t seed, int64_t* mismatches) {
     int dev = 0, sms = 0;
     TRY(check_device(&dev, &sms));
     unsigned long long* bad = nullptr;
-    CU(cudaMalloc(&bad, 2 * sizeof(unsigned long long)));
-    unsigned long long hb[2] = {0, 0};
+    CU(cudaMalloc(&bad, 3 * sizeof(unsigned long long)));
+    unsigned long long hb[3] = {0, 0, 0};
     cudaError_t e = cudaMemset(bad, 0, sizeof(hb));
     if (e == cudaSuccess) {
         launch_selftest_conv((long long)n, (unsigned long long)seed, bad, 0);
@@ -912,6 +914,7 @@ int dem_selftest_conversions(int64_t n, uint64_t seed, int64_t* mismatches) {
     CU(e);
     mismatches[0] = (int64_t)hb[0];
     mismatches[1] = (int64_t)hb[1];
+    mismatches[2] = (int64_t)hb[2];
     return DEM_OK;
 }
 

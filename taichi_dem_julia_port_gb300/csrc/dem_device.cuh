@@ -98,6 +98,19 @@ __device__ __forceinline__ double f2d(float f) {
     return __hiloint2double((int)hi, (int)(u << 29));
 }
 
+// 1/x for x > 0 in the normal FP32 range: an FP32 reciprocal refined by two
+// Newton–Raphson steps y ← y + y(1 - x·y) in FP64 (quadratic convergence:
+// 2^-23 → 2^-46 → below FP64 rounding), four FP64 operations instead of an
+// FP64 division.  The result is within 2 ulp of the correctly rounded 1/x
+// (checked against it by dem_selftest_conversions).
+__device__ __forceinline__ double rcp_nr(double x) {
+    double y = f2d(__frcp_rn(d2f(x)));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
 // ---- Morton / bucket ---------------------------------------------------------
 // Morton.jl `cartesian3morton` for 1-based cells (x in bit 0): the interleave of
 // (ijk - 1) plus one.  Each coordinate keeps its low 10 bits.  The spreading

@@ -92,6 +92,7 @@ struct SceneParams {
     double skin;
     float f_skin, f_half_skin;
     double hdt2;            // dt²/2
+    double tol2_lo, tol2_x4;  // tolerance²·(1 - 2^-30) and 4·tolerance² (contact frame)
     float f_wn[3], f_wc0;   // FP32 wall normal and n·domain_min - wall_distance (wall screen)
 };
 

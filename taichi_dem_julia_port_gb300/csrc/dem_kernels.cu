@@ -872,20 +872,21 @@ __device__ __forceinline__ Frame frame_degenerate(double ax) {
     F.neg3 = sg < 0.0;
     return F;
 }
+static __device__ __noinline__ Frame frame_exact_from(double dx, double dy, double dz, double tol) {
+    const double L = norm_rn(dx, dy, dz);
+    const double il = __ddiv_rn(1.0, L);
+    return frame_exact(__dmul_rn(il, dx), __dmul_rn(il, dy), __dmul_rn(il, dz), tol);
+}
 __device__ __forceinline__ Frame contact_frame(double dx, double dy, double dz, double ax,
-                                               double ay, double az, double tol) {
+                                               double ay, double az, const SceneParams& S) {
     const double s2 = ay * ay + az * az;
-    if (s2 < tol * tol * (1.0 - 0x1p-30)) return frame_degenerate(ax);
-    if (s2 < 4.0 * tol * tol) {
-        const double L = norm_rn(dx, dy, dz);
-        const double il = __ddiv_rn(1.0, L);
-        return frame_exact(__dmul_rn(il, dx), __dmul_rn(il, dy), __dmul_rn(il, dz), tol);
-    }
+    if (s2 < S.tol2_lo) return frame_degenerate(ax);
+    if (s2 < S.tol2_x4) return frame_exact_from(dx, dy, dz, S.tol);
     Frame F;
     F.a1 = ax;
     F.a2 = ay;
     F.a3 = az;
-    F.f = (1.0 - ax) / s2;
+    F.f = (1.0 - ax) * rcp_nr(s2);  // (1 - a₁)/s²
     F.neg3 = false;
     return F;
 }
@@ -965,11 +966,9 @@ static __device__ __noinline__ bool bond_breaks_pairs(const float2 (&F)[3], cons
     return bond_breaks(Fd, tid, tjd, invA, rbI, p);
 }
 
-__device__ __forceinline__ bool bond_breaks_screened(const float2 (&F)[3], const float2 (&ti)[3],
-                                                     const float2 (&tj)[3], const Vec3<float>& Ff,
-                                                     const Vec3<float>& tif, const Vec3<float>& tjf,
-                                                     float iA, float rb, const DemDev& d, int small,
-                                                     const SceneParams& p) {
+__device__ __forceinline__ bool stress_clear(const Vec3<float>& Ff, const Vec3<float>& tif,
+                                             const Vec3<float>& tjf, float iA, float rb,
+                                             const SceneParams& p) {
     const float ai = tif.y * tif.y + tif.z * tif.z, aj = tjf.y * tjf.y + tjf.z * tjf.z;
     const float fa = Ff.x * iA;
     const float smax = rb * sqrtf(fmaxf(ai, aj)), smin = rb * sqrtf(fminf(ai, aj));
@@ -977,11 +976,32 @@ __device__ __forceinline__ bool bond_breaks_screened(const float2 (&F)[3], const
     const float s2 = (4.0f / 3.0f) * iA * sqrtf(Ff.y * Ff.y + Ff.z * Ff.z);
     const float sc = p.f_sc, st = p.f_st, ss = p.f_ss;
     const float afa = fabsf(fa);
-    const bool clear = (fa + smax + (afa + smax + fabsf(sc)) * 0x1p-16f < sc) &&
-                       (-fa - smin + (afa + smin + fabsf(st)) * 0x1p-16f < st) &&
-                       (s1 + s2 + (s1 + s2 + fabsf(ss)) * 0x1p-16f < ss);
-    if (clear) return false;
+    return (fa + smax + (afa + smax + fabsf(sc)) * 0x1p-16f < sc) &&
+           (-fa - smin + (afa + smin + fabsf(st)) * 0x1p-16f < st) &&
+           (s1 + s2 + (s1 + s2 + fabsf(ss)) * 0x1p-16f < ss);
+}
+__device__ __forceinline__ bool bond_breaks_screened(const float2 (&F)[3], const float2 (&ti)[3],
+                                                     const float2 (&tj)[3], const Vec3<float>& Ff,
+                                                     const Vec3<float>& tif, const Vec3<float>& tjf,
+                                                     float iA, float rb, const DemDev& d, int small,
+                                                     const SceneParams& p) {
+    if (stress_clear(Ff, tif, tjf, iA, rb, p)) return false;
     return bond_breaks_pairs(F, ti, tj, d.b_invA[small], d.b_rbI[small], p);
+}
+// The FP64 force mode's breakage decision behind the same FP32 screen.
+static __device__ __noinline__ bool bond_breaks_d(const Vec3<double>& F, const Vec3<double>& ti,
+                                                  const Vec3<double>& tj, double invA, double rbI,
+                                                  const SceneParams& p) {
+    return bond_breaks(F, ti, tj, invA, rbI, p);
+}
+__device__ __forceinline__ bool bond_breaks_fp64(const Vec3<double>& F, const Vec3<double>& ti,
+                                                 const Vec3<double>& tj, const DemDev& d,
+                                                 int small, const SceneParams& p) {
+    const Vec3<float> Ff{d2f(F.x), d2f(F.y), d2f(F.z)};
+    const Vec3<float> tif{d2f(ti.x), d2f(ti.y), d2f(ti.z)};
+    const Vec3<float> tjf{d2f(tj.x), d2f(tj.y), d2f(tj.z)};
+    if (stress_clear(Ff, tif, tjf, d.bk32[small].w, d.rm32[small].x, p)) return false;
+    return bond_breaks_d(F, ti, tj, d.b_invA[small], d.b_rbI[small], p);
 }
 
 // FP32 hi/lo pair accumulator (hi + lo carries about 48 bits): (hi, lo) + x
@@ -1223,7 +1243,7 @@ __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, 
         const double invL = rsqrt(L2);
         const double L = L2 * invL;
         const double ax = dx * invL, ay = dy * invL, az = dz * invL;
-        const Frame R = contact_frame(dx, dy, dz, ax, ay, az, SP.tol);
+        const Frame R = contact_frame(dx, dy, dz, ax, ay, az, SP);
         Vec3<T> fig, mi, mj;
         if (fl & kBonded) {
             // EBPM (src/kernels.jl:170-239)
@@ -1234,7 +1254,7 @@ __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, 
             const int small = ri <= rj ? i : j;  // rb = ρ·min(rᵢ, rⱼ)
             const T tinvL = (T)invL, tdt = (T)dt;
             const T phi = (T)d.b_phic[small] * tinvL * tinvL;
-            const T iphi = (T)1.0 / ((T)1.0 + phi);
+            const T iphi = rcp_nr((T)1.0 + phi);  // 1/(1 + ϕ)
             const T EILdt = (T)d.b_EI[small] * tinvL * tdt;  // EI/L·dt
             const T k1 = (T)d.b_EA[small] * tinvL * tdt;
             const T k3 = (T)6.0 * EILdt * tinvL * iphi;
@@ -1251,7 +1271,7 @@ __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, 
             ti = {ti.x + (double)dtix, ti.y + (double)dtiy, ti.z + (double)dtiz};
             tj = {tj.x + (double)dtjx, tj.y + (double)dtjy, tj.z + (double)dtjz};
             // breakage test, FP64 (src/kernels.jl:208-222)
-            if (bond_breaks(Fi, ti, tj, d.b_invA[small], d.b_rbI[small], SP)) {
+            if (bond_breaks_fp64(Fi, ti, tj, d, small, SP)) {
                 w.fl[c] = 0u;  // contact_active and contact_bonded bits cleared
                 atomicAdd(&d.sctr[sc].broken, 1ull);
                 fig = {(T)0, (T)0, (T)0};
@@ -1841,6 +1861,13 @@ __global__ void k_selftest_conv(long long n, unsigned long long seed, unsigned l
     const unsigned long long e = (unsigned long long)__double_as_longlong((double)f);
     if (a != b) atomicAdd(bad, 1ull);
     if (c != e && !isnan(f)) atomicAdd(bad + 1, 1ull);
+    // rcp_nr on positive values across the normal FP32 range: within 2 ulp of
+    // the correctly rounded reciprocal
+    const double xr = __longlong_as_double((long long)(((1023ull - 100ull + (r2 % 201ull)) << 52) |
+                                                       (r1 & 0xfffffffffffffull)));
+    const long long u1 = __double_as_longlong(rcp_nr(xr)), u2 = __double_as_longlong(__drcp_rn(xr));
+    const long long du = u1 > u2 ? u1 - u2 : u2 - u1;
+    if (du > 2) atomicAdd(bad + 2, 1ull);
 }
 
 void launch_selftest_conv(long long n, unsigned long long seed, unsigned long long* bad,
