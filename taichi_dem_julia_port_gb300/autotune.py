@@ -18,9 +18,9 @@ from __future__ import annotations
 from dataclasses import dataclass, field
 
 CELL_FACTORS = (1.0, 0.8, 0.6, 0.45, 0.35)
-BLOCKS = (128, 256)
+BLOCKS = (64, 128, 256)
 GRIDS_PER_SM = (4, 8, 16, 32)
-INTEGRATE_BLOCKS = (128, 256)
+INTEGRATE_BLOCKS = (32, 64, 128, 256)
 DETECT_BLOCKS = (3, 4)  # pair-search register budget (blocks per SM)
 FORCE_BLOCKS = (0, 4)   # FP32 force kernel register budget (0: compiler's choice)
 

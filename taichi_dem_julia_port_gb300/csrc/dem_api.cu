@@ -464,13 +464,28 @@ void free_all(DemHandle* h) {
     h->pinned = nullptr;
 }
 
+// Default launch shape: blocks of at most 256 threads, small enough that a
+// single scene's particles (and its expected ~3 contacts per particle) give
+// every SM at least four blocks (a 17,576-sphere scene in 256-thread blocks
+// would leave half the SMs idle).  Arenas start at 256; the autotuner refines.
+LaunchShape default_shape(const DemHandle* h) {
+    auto block_for = [&](int64_t units) {
+        int b = 256;
+        while (b > 32 && units < (int64_t)b * 4 * h->sm_count) b >>= 1;
+        return b;
+    };
+    const int64_t n = h->multi ? INT64_MAX / 8 : h->n_cap;
+    const int ib = block_for(n), fb = block_for(3 * n), cb = block_for(4 * n);
+    return LaunchShape{fb, h->sm_count * 16, cb, h->sm_count * 16, ib, 4, 0};
+}
+
 int init_handle(DemHandle* h) {
     CU(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     CU(cudaEventCreate(&h->ev0));
     CU(cudaEventCreate(&h->ev1));
     TRY(allocate(h));
     h->ntiles_cells = std::max(1, scan_tiles((int64_t)h->p.T));
-    h->shape = LaunchShape{256, h->sm_count * 16, 256, h->sm_count * 16, 256, 4, 0};
+    h->shape = default_shape(h);
     return DEM_OK;
 }
 
