@@ -596,9 +596,16 @@ __global__ void __launch_bounds__(kThreads) k_vdetect(DemDev d, DemParams p, int
     const ContactSoA o = d.c[cur];
     for (int i = blockIdx.x * (kThreads / kVLanes) + g; i < p.n;
          i += gridDim.x * (kThreads / kVLanes)) {
-        const uint8_t path = d.path[i];  // set by k_hash this step
-        if (path < 2) continue;
-        const bool frozen = path == 3;
+        // which particles test their lists: the path byte k_hash wrote (arena);
+        // a single-scene handle decides from its one flag
+        bool frozen = false;
+        if (MULTI) {
+            const uint8_t path = d.path[i];
+            if (path < 2) continue;
+            frozen = path == 3;
+        } else if (d.sflags[cur][0] != 0u) {
+            continue;
+        }
         if (lane == 0) sh[g].nnew = 0;
         const int e0 = d.row_start[cur][i];
         const int e1 = e0 + d.row_len[cur][i];
@@ -1767,11 +1774,17 @@ void launch_detect_b(const DemDev& d, const DemParams& p, int cur, bool init, bo
     else k_detect<false, false, MINB><<<nb, kThreads, 0, s>>>(d, p, cur);
 }
 
-void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
-                   const LaunchShape& sh, cudaStream_t s) {
+void launch_detect_full(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+                        const LaunchShape& sh, cudaStream_t s) {
     if (p.n == 0) return;
     if (sh.detect_blocks_per_sm == 3) launch_detect_b<3>(d, p, cur, init, multi, s);
     else launch_detect_b<4>(d, p, cur, init, multi, s);
+}
+
+void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+                   const LaunchShape& sh, cudaStream_t s) {
+    if (p.n == 0) return;
+    launch_detect_full(d, p, cur, init, multi, sh, s);
     if (!init) {  // the scenes that test their neighbour lists
         const int nv = max(1, min(blocks_for((long long)p.n * kVLanes, kThreads), p.sms * 8));
         if (multi) k_vdetect<true><<<nv, kThreads, 0, s>>>(d, p, cur);
