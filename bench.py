@@ -65,8 +65,8 @@ INTEGRATE_BYTES_PER_PARTICLE = 13 * 8 * 2 + 4 * 8 + 6 * 8 + 3 * 8 * 2 + 8 + 4  #
 # neighbour-list step per particle: path byte, current row bounds, list length,
 # FP32 position, row length written, 4 list partners (index + FP32 position)
 DETECT_BYTES_PER_PARTICLE = 1 + 8 + 4 + 16 + 8 + 4 * (4 + 16)
-# hash, scan, scatter, canon, detect, list detect, rows, compact, force, integrate, flags
-KERNELS_PER_STEP = 11
+# hash, scan, scatter, canon, detect, list detect, rows, compact, force, integrate
+KERNELS_PER_STEP = 10
 L2_FLUSH_BYTES = 256 << 20
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch

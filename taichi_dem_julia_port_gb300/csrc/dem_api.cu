@@ -552,7 +552,6 @@ void record_step(DemHandle* h, int cur) {
     launch_compact(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
     launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
     launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
-    launch_scene_flags(h->d, h->p, cur, h->multi, h->stream);
 }
 
 void drop_graphs(DemHandle* h) {
@@ -1278,7 +1277,6 @@ int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
     launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
     cudaEventRecord(ev[4], h->stream);
     launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
-    launch_scene_flags(h->d, h->p, cur, h->multi, h->stream);
     cudaEventRecord(ev[5], h->stream);
     cudaError_t e = cudaEventSynchronize(ev[5]);
     for (int k = 0; k < 5 && e == cudaSuccess; ++k)

@@ -200,8 +200,7 @@ struct LaunchShape {
 // `all`: hash every particle (otherwise only the scenes that search this step)
 void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi, bool all,
                        int n_scan_tiles_cells, cudaStream_t s);
-// end of a step: rebuild flags carried over or cleared
-void launch_scene_flags(const DemDev& d, const DemParams& p, int cur, bool multi, cudaStream_t s);
+
 void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
                    const LaunchShape& sh, cudaStream_t s);
 void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,

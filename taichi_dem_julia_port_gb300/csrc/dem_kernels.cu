@@ -686,13 +686,11 @@ __global__ void __launch_bounds__(kThreads) k_vdetect(DemDev d, DemParams p, int
     }
 }
 
-// End of a step: the rebuild flags of this step are cleared; scenes that did
-// not step keep theirs for their next step; scenes without a skin search in
-// full every step.
+// End of a step (run by k_integrate): the rebuild flags of this step are
+// cleared; scenes that did not step keep theirs for their next step; scenes
+// without a skin search in full every step.
 template <bool MULTI>
-__global__ void k_scene_flags(DemDev d, DemParams p, int cur) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= p.ns) return;
+__device__ __forceinline__ void scene_flags_one(const DemDev& d, const DemParams& p, int cur, int s) {
     const SceneParams& S = scene_rec<MULTI>(d, p, s);
     const int mode = MULTI ? S.mode : kModeStep;
     const int nxt = cur ^ 1;
@@ -706,6 +704,7 @@ __global__ void k_scene_flags(DemDev d, DemParams p, int cur) {
     if (carry) atomicOr(&d.sflags[nxt][s], carry);
     d.sflags[cur][s] = 0u;
 }
+
 
 // Row placement in the next contact buffer (the atomic-compacted contact list
 // of src/kernels.jl:74, 109): one warp-aggregated atomic per 32 slots.  Free
@@ -1497,6 +1496,9 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nxt = cur ^ 1;
     if (i == 0) d.ctr->row_alloc[cur] = 0u;  // the free buffer is next step's target
+    // the end-of-step rebuild-flag work of every scene (see scene_flags_one):
+    // it only ORs into the next flags, as the particles' skin test does
+    for (int s = i; s < p.ns; s += gridDim.x * blockDim.x) scene_flags_one<MULTI>(d, p, cur, s);
     if (i >= p.n) return;
     const int sc = slot_scene<MULTI>(d, i);
     if (MULTI && (sc < 0 || d.sp[sc].mode != kModeStep)) {
@@ -1889,11 +1891,6 @@ void launch_selftest_conv(long long n, unsigned long long seed, unsigned long lo
     k_selftest_conv<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, seed, bad);
 }
 
-void launch_scene_flags(const DemDev& d, const DemParams& p, int cur, bool multi, cudaStream_t s) {
-    if (p.n == 0 || p.ns <= 0) return;
-    if (multi) k_scene_flags<true><<<blocks_for(p.ns, 128), 128, 0, s>>>(d, p, cur);
-    else k_scene_flags<false><<<blocks_for(p.ns, 128), 128, 0, s>>>(d, p, cur);
-}
 
 template <bool MULTI>
 __global__ void k_refresh_pos32(DemDev d, DemParams p, int first, int n) {
