@@ -11,8 +11,8 @@ Our arm: W untimed steps, then K steps each timed with CUDA events on the
 library's stream, with a 256 MiB write between steps to flush L2 (the scene
 itself fits in L2).  value = particle-steps/s over all ranks (max time over
 ranks).  `e2e` repeats the metric through the C ABI with host buffers: every
-step uploads the particle state from host memory (dem_set_particles), steps,
-and reads it back (dem_get_particles).  `roofline` reports the dominant kernel
+step uploads the particle state from page-locked host arrays
+(dem_set_particles), steps, and reads it back into them (dem_get_particles).  `roofline` reports the dominant kernel
 from per-phase CUDA events (dem_step_profiled).  `cpu_baseline` times the CPU
 oracle (OpenMP, all host threads) on a bounded sample of the same workload.
 
@@ -554,18 +554,19 @@ def main() -> None:
     else:
         roofline.update({"achieved": None, "frac": None})
 
-    # e2e through the C ABI with host buffers
-    st0 = g.particles(forces=False)
+    # e2e through the C ABI with host buffers (page-locked, as a host
+    # application that exchanges state every step would allocate them)
     keys = ("pos", "vel", "omega", "quat", "wall_shear")
-    host = {k: np.ascontiguousarray(st0[k]) for k in keys}
+    host = {k: torch.empty((sc.n, 4 if k == "quat" else 3), dtype=torch.float64,
+                           pin_memory=True).numpy() for k in keys}
+    g.particles(out=host)
     h2d = sum(host[k].nbytes for k in keys)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         g.set_particles(**host)
         g.simulate(1)
-        out = g.particles(forces=False)
-        host = {k: out[k] for k in keys}
+        g.particles(out=host)
     e2e_s = time.perf_counter() - t0
     if dist:
         t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)

@@ -241,11 +241,17 @@ int dem_get_launch_shape(DemHandle* h, DemLaunchShape* out);
 /* ---- state exchange ---------------------------------------------------- */
 
 /* Reads `grains` (positions, velocities, ...) back to the host, as
- * `Array(grains)` does in save_single (src/utils.jl:40). */
+ * `Array(grains)` does in save_single (src/utils.jl:40).  Buffers in
+ * page-locked host memory (cudaHostAlloc, cudaHostRegister) or in device
+ * memory are written in place by one kernel; pageable buffers take one extra
+ * copy through a device staging buffer.  Returns when the data is in place. */
 int dem_get_particles(DemHandle* h, DemParticleState* out);
 
 /* Overwrites the dynamic particle state from host buffers (fields left NULL
- * are kept).  Used to start the device from a given state. */
+ * are kept; buffers as for dem_get_particles).  Used to start the device from
+ * a given state.  The buffers are no longer read once the call returns.  New
+ * positions keep the neighbour lists while every particle stays within half
+ * the skin of where they were built; otherwise the next step searches in full. */
 int dem_set_particles(DemHandle* h, const DemParticleState* in);
 
 int dem_get_static(DemHandle* h, DemParticleStatic* out);

@@ -162,11 +162,12 @@ class Arena:
         check(self.lib, self.lib.dem_sync(self.h), "dem_sync")
 
     # ---- per-scene state ------------------------------------------------------
-    def particles(self, scene: int, forces: bool = True) -> dict:
+    def particles(self, scene: int, forces: bool = True, out: dict | None = None) -> dict:
+        """A scene's particle state; `out` may hold preallocated (e.g. pinned) arrays."""
         n = self._scenes[scene].particles.n
         return read_particles(
             self.lib, lambda st: self.lib.dem_scene_get_particles(self.h, int(scene), st), n,
-            forces, "dem_scene_get_particles")
+            forces, "dem_scene_get_particles", out)
 
     def contacts(self, scene: int) -> dict:
         return read_contacts(

@@ -350,8 +350,8 @@ struct DemHandle {
     int enc = DEM_FP64;  // encoding of 𝐅ᵢ, 𝛕ᵢ, 𝛕ⱼ in the current contact buffer
     std::vector<void*> allocs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    double* pinned = nullptr;  // host staging for particle state exchange
-    int64_t pinned_n = 0;
+    double* xfer = nullptr;    // device staging: particle records in the host's layout
+    int64_t xfer_n = 0;        // doubles
 };
 
 #define CU(expr)                                                                            \
@@ -460,8 +460,8 @@ void free_all(DemHandle* h) {
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->stream) cudaStreamDestroy(h->stream);
-    if (h->pinned) cudaFreeHost(h->pinned);
-    h->pinned = nullptr;
+    if (h->xfer) cudaFree(h->xfer);
+    h->xfer = nullptr;
 }
 
 // Default launch shape: blocks of at most 256 threads, small enough that a
@@ -671,22 +671,6 @@ int get_dev(std::vector<double>& host, const double* dev, size_t n, cudaStream_t
     return DEM_OK;
 }
 
-// Particle state exchange goes through one pinned staging buffer per handle
-// (22 FP64 columns), so each call is one batch of asynchronous copies and one
-// synchronisation.
-int staging(DemHandle* h, int64_t n, double** out) {
-    if (!h->pinned || h->pinned_n < n) {
-        if (h->pinned) cudaFreeHost(h->pinned);
-        h->pinned = nullptr;
-        h->pinned_n = 0;
-        const int64_t m = std::max<int64_t>(n, 1);
-        CU(cudaMallocHost(&h->pinned, sizeof(double) * 22 * (size_t)m));
-        h->pinned_n = m;
-    }
-    *out = h->pinned;
-    return DEM_OK;
-}
-
 const SceneHost* scene_at(DemHandle* h, int32_t s) {
     if (!h || s < 0 || s >= (int32_t)h->scenes.size()) return nullptr;
     const SceneHost& S = h->scenes[s];
@@ -747,42 +731,87 @@ int after_launch(DemHandle* h) {
     return upd.empty() ? DEM_OK : apply_modes(h, upd);
 }
 
+// Device staging for particle records, at least `doubles` long.
+int xfer_buffer(DemHandle* h, int64_t doubles, double** out) {
+    if (!h->xfer || h->xfer_n < doubles) {
+        if (h->xfer) cudaFree(h->xfer);
+        h->xfer = nullptr;
+        h->xfer_n = 0;
+        CU(cudaMalloc(&h->xfer, sizeof(double) * (size_t)std::max<int64_t>(doubles, 1)));
+        h->xfer_n = std::max<int64_t>(doubles, 1);
+    }
+    *out = h->xfer;
+    return DEM_OK;
+}
+
+// The device address of a caller buffer the GPU can access in place
+// (page-locked host memory, or device memory), else nullptr.
+double* device_view(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeDevice)
+        return static_cast<double*>(a.devicePointer);
+    return nullptr;
+}
+
+// One particle state exchange between caller buffers (`host[f]`, k[f] doubles
+// per particle, nullptr = field not exchanged) and the columns `cols[f]` at
+// slots [p0, p0 + n): one kernel over all fields, which reads or writes
+// device-accessible buffers in place; pageable buffers go through the
+// library's staging copy with one cudaMemcpyAsync each.  Synchronises.
+int exchange(DemHandle* h, int64_t p0, int64_t n, const int* k, double* const* host,
+             double* const (*cols)[4], int nfields, bool to_cols) {
+    if (n <= 0) return DEM_OK;
+    XferSet x{};
+    double* staged[kXferFields] = {};
+    const double* src_host[kXferFields] = {};
+    double* xf = nullptr;
+    size_t off = 0;
+    for (int f = 0; f < nfields; ++f) {
+        if (!host[f]) continue;
+        double* dv = device_view(host[f]);
+        if (!dv) {
+            if (!xf) TRY(xfer_buffer(h, 22 * n, &xf));
+            dv = xf + off;
+            off += (size_t)k[f] * n;
+            staged[x.nf] = dv;
+            src_host[x.nf] = host[f];
+        }
+        x.rec[x.nf] = dv;
+        for (int c = 0; c < 4; ++c) x.col[x.nf][c] = cols[f][c];
+        x.k[x.nf] = k[f];
+        ++x.nf;
+    }
+    if (to_cols)
+        for (int f = 0; f < x.nf; ++f)
+            if (staged[f])
+                CU(cudaMemcpyAsync(staged[f], src_host[f], sizeof(double) * x.k[f] * n,
+                                   cudaMemcpyHostToDevice, h->stream));
+    launch_xfer(x, (int)n, (int)p0, to_cols, h->stream);
+    CU(cudaGetLastError());
+    if (!to_cols)
+        for (int f = 0; f < x.nf; ++f)
+            if (staged[f])
+                CU(cudaMemcpyAsync(const_cast<double*>(src_host[f]), staged[f],
+                                   sizeof(double) * x.k[f] * n, cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaStreamSynchronize(h->stream));
+    return DEM_OK;
+}
+
 // Particle state of slots [p0, p0 + n) to host arrays (scene-local order).
 int get_particles_range(DemHandle* h, int64_t p0, int64_t n, DemParticleState* out) {
-    struct F {
-        double* dst;
-        int stride;
-        double* src[4];
-        int k;
-    };
     const DemDev& d = h->d;
-    const F fields[] = {{out->pos, 3, {d.px, d.py, d.pz}, 3},
-                        {out->vel, 3, {d.vx, d.vy, d.vz}, 3},
-                        {out->omega, 3, {d.wx, d.wy, d.wz}, 3},
-                        {out->quat, 4, {d.qw, d.qx, d.qy, d.qz}, 4},
-                        {out->force, 3, {d.fx, d.fy, d.fz}, 3},
-                        {out->moment, 3, {d.tx, d.ty, d.tz}, 3},
-                        {out->wall_shear, 3, {d.wsx, d.wsy, d.wsz}, 3}};
-    double* st = nullptr;
-    TRY(staging(h, n, &st));
-    if (n) {
-        size_t col = 0;
-        for (const F& f : fields) {
-            if (!f.dst) continue;
-            for (int c = 0; c < f.k; ++c, ++col)
-                CU(cudaMemcpyAsync(st + col * n, f.src[c] + p0, n * sizeof(double),
-                                   cudaMemcpyDeviceToHost, h->stream));
-        }
-        CU(cudaStreamSynchronize(h->stream));
-        col = 0;
-        for (const F& f : fields) {
-            if (!f.dst) continue;
-            for (int c = 0; c < f.k; ++c, ++col) {
-                const double* src = st + col * n;
-                for (int64_t i = 0; i < n; ++i) f.dst[f.stride * i + c] = src[i];
-            }
-        }
-    }
+    const int k[] = {3, 3, 3, 4, 3, 3, 3};
+    double* const host[] = {out->pos,   out->vel,    out->omega,     out->quat,
+                            out->force, out->moment, out->wall_shear};
+    double* const cols[][4] = {{d.px, d.py, d.pz},      {d.vx, d.vy, d.vz},
+                               {d.wx, d.wy, d.wz},      {d.qw, d.qx, d.qy, d.qz},
+                               {d.fx, d.fy, d.fz},      {d.tx, d.ty, d.tz},
+                               {d.wsx, d.wsy, d.wsz}};
+    TRY(exchange(h, p0, n, k, host, cols, 7, false));
     return device_error(h);
 }
 
@@ -978,7 +1007,7 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
     if (rc == DEM_OK) rc = upload_scene(h, A, 0);
     if (rc == DEM_OK) rc = flag_search(h, 0);
     if (rc == DEM_OK) {
-        launch_refresh_pos32(h->d, h->p, false, 0, h->n_cap, h->stream);
+        launch_refresh_pos32(h->d, h->p, false, 0, h->n_cap, -1, h->stream);
         if (cudaGetLastError() != cudaSuccess) rc = DEM_ERR_CUDA;
     }
     if (rc != DEM_OK) {
@@ -1084,7 +1113,7 @@ int dem_arena_add(DemHandle* h, const DemConfigC* cfg, const DemParticlesIn* pin
          cudaStreamSynchronize(h->stream) != cudaSuccess))
         rc = DEM_ERR_CUDA;
     if (rc == DEM_OK && n) {
-        launch_refresh_pos32(h->d, h->p, true, (int)p0, (int)n, h->stream);
+        launch_refresh_pos32(h->d, h->p, true, (int)p0, (int)n, -1, h->stream);
         if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess)
             rc = DEM_ERR_CUDA;
     }
@@ -1335,37 +1364,20 @@ int dem_get_particles(DemHandle* h, DemParticleState* out) {
 int dem_set_particles(DemHandle* h, const DemParticleState* in) {
     const SceneHost* S = scene_at(h, 0);
     if (!S || !in || h->multi) return DEM_ERR_INVALID;
-    const size_t n = (size_t)S->sp.n;
-    struct F {
-        const double* src;
-        int stride;
-        double* dst[4];
-        int k;
-    };
-    const DemDev& d = h->d;
-    const F fields[] = {{in->pos, 3, {d.px, d.py, d.pz}, 3},
-                        {in->vel, 3, {d.vx, d.vy, d.vz}, 3},
-                        {in->omega, 3, {d.wx, d.wy, d.wz}, 3},
-                        {in->quat, 4, {d.qw, d.qx, d.qy, d.qz}, 4},
-                        {in->wall_shear, 3, {d.wsx, d.wsy, d.wsz}, 3}};
+    const int64_t n = S->sp.n;
     if (!n) return DEM_OK;
-    CU(cudaStreamSynchronize(h->stream));  // the staging buffer may still be in use
-    double* st = nullptr;
-    TRY(staging(h, (int64_t)n, &st));
-    size_t col = 0;
-    for (const F& f : fields) {
-        if (!f.src) continue;
-        for (int c = 0; c < f.k; ++c, ++col) {
-            double* dst = st + col * n;
-            for (size_t i = 0; i < n; ++i) dst[i] = f.src[f.stride * i + c];
-            CU(cudaMemcpyAsync(f.dst[c], dst, n * sizeof(double), cudaMemcpyHostToDevice,
-                               h->stream));
-        }
-    }
-    TRY(flag_search(h, 0));  // positions changed: the neighbour lists are rebuilt
-    launch_refresh_pos32(h->d, h->p, false, 0, (int)n, h->stream);
+    const DemDev& d = h->d;
+    const int k[] = {3, 3, 3, 4, 3};
+    double* const host[] = {in->pos, in->vel, in->omega, in->quat, in->wall_shear};
+    double* const cols[][4] = {{d.px, d.py, d.pz}, {d.vx, d.vy, d.vz}, {d.wx, d.wy, d.wz},
+                               {d.qw, d.qx, d.qy, d.qz}, {d.wsx, d.wsy, d.wsz}};
+    // the exchange synchronises before the refresh below is queued: the
+    // caller's buffers are free again on return
+    TRY(exchange(h, 0, n, k, host, cols, 5, true));
+    // new positions: the neighbour lists stay valid while every particle lies
+    // within skin/2 of where they were built, else the next step searches in full
+    launch_refresh_pos32(h->d, h->p, false, 0, (int)n, in->pos ? h->cur : -1, h->stream);
     CU(cudaGetLastError());
-    CU(cudaStreamSynchronize(h->stream));
     return DEM_OK;
 }
 

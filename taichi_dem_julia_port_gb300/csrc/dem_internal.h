@@ -135,7 +135,7 @@ struct DemDev {
     float4* xref;
     float4* pos32;
     uint32_t* sflags[2];
-    uint8_t* path;  // this step: 0 free slot, 1 full search, 2 list (stepping), 3 list (held)
+    uint8_t* path;  // this step: kind (0 free, 1 full search, 2 list) | scene mode << 2
     SceneParams* sp;                      // arena: scene records; null otherwise
     SceneCounters* sctr;                  // per-scene event counters
     // broad phase
@@ -215,9 +215,21 @@ void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cuda
 void launch_cplist_fill(const DemDev& d, const DemParams& p, const int32_t* off, int32_t* cp,
                         cudaStream_t s);
 void launch_morton(const DemDev& d, const DemParams& p, uint32_t* morton, cudaStream_t s);
-// FP32 positions (pos32) of slots [first, first + n) from the FP64 positions
+// particle state exchange: per field, k-component records <-> k columns,
+// slots [p0, p0 + n); to_cols: records -> columns
+constexpr int kXferFields = 7;
+struct XferSet {
+    double* rec[kXferFields];
+    double* col[kXferFields][4];
+    int k[kXferFields];
+    int nf;
+};
+void launch_xfer(const XferSet& x, int n, int p0, bool to_cols, cudaStream_t s);
+// FP32 positions (pos32) of slots [first, first + n) from the FP64 positions;
+// with fb 0 or 1, scenes with a particle beyond skin/2 of its list position
+// are flagged for a full search in sflags[fb] (no test for fb < 0)
 void launch_refresh_pos32(const DemDev& d, const DemParams& p, bool multi, int first, int n,
-                          cudaStream_t s);
+                          int fb, cudaStream_t s);
 // re-encodes 𝐅ᵢ, 𝛕ᵢ, 𝛕ⱼ of contacts [0, n) of buffer `buf`: FP64 <-> FP32 hi/lo pairs
 void launch_recode(const DemDev& d, int buf, int n, bool to_pairs, cudaStream_t s);
 // exclusive scan of n int32 values into out[0..n] (out[n] = total)

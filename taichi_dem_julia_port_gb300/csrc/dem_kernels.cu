@@ -241,14 +241,14 @@ __global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p, int cu
             d.bucket[i] = kNoBucket;
             d.row_len[cur ^ 1][i] = 0;
             d.row_start[cur ^ 1][i] = 0;
-            d.path[i] = 0;
+            d.path[i] = 0;  // kind 0 (free), mode Free
             act = false;
         } else if (!full_search(d, cur, sc, mode, all)) {
             d.bucket[i] = kNoBucket;  // this scene tests its neighbour lists
-            d.path[i] = mode == kModeFrozen ? 3 : 2;
+            d.path[i] = (uint8_t)(2 | (mode << 2));  // kind 2 (list)
             act = false;
         } else {
-            d.path[i] = 1;
+            d.path[i] = (uint8_t)(1 | (mode << 2));  // kind 1 (full search)
             const SceneParams& S = scene_rec<MULTI>(d, p, sc);
             const double pos[3] = {d.px[i], d.py[i], d.pz[i]};
             int4 ci = cell_of_screened(pos, S.dmin, S.cell, S.inv_cell, S.f_inv_cell, S.f_dmin_cells);
@@ -601,8 +601,8 @@ __global__ void __launch_bounds__(kThreads) k_vdetect(DemDev d, DemParams p, int
         bool frozen = false;
         if (MULTI) {
             const uint8_t path = d.path[i];
-            if (path < 2) continue;
-            frozen = path == 3;
+            if ((path & 3) != 2) continue;
+            frozen = (path >> 2) == kModeFrozen;
         } else if (d.sflags[cur][0] != 0u) {
             continue;
         }
@@ -748,18 +748,18 @@ __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int
     const int stride = gridDim.x * blockDim.x;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cold + p.n; t += stride) {
         if (t < cold) {
-            if (!d.keep[t]) continue;
-            const int i = o.ci[t];
-            if (i >= p.n) continue;
+            // independent loads first (the chain below is latency-bound)
+            const uint8_t kp = d.keep[t];
+            const int i = o.ci[t], j = o.cj[t];
+            const uint32_t fl = o.fl[t];
+            if (!kp || i >= p.n) continue;
+            const int r0 = d.row_start[cur][i], n0 = d.row_len[cur][i];
+            const int rl = d.row_len[nxt][i];
+            const int mode = MULTI ? (d.path[i] >> 2) : (INIT ? kModeInit : kModeStep);
             // entries outside the owner's current row are left-overs of a
             // removed scene (arena) and are dropped
-            const int r0 = d.row_start[cur][i];
-            if (t < r0 || t >= r0 + d.row_len[cur][i]) continue;
-            const int rl = d.row_len[nxt][i];
+            if (t < r0 || t >= r0 + n0) continue;
             if (rl == 0) continue;  // row dropped after a capacity overflow, or a free slot
-            const int j = o.cj[t];
-            const uint32_t fl = o.fl[t];
-            const int mode = MULTI ? d.sp[d.scene_of[i]].mode : (INIT ? kModeInit : kModeStep);
             // A stepping contact carries only the state the next force pass
             // reads: a bond its accumulated 𝐅, 𝛕ᵢ, 𝛕ⱼ, a Hertz contact its 𝐬 (the
             // force pass rewrites 𝐤 and 𝐅; a bond's 𝐬 and a Hertz contact's
@@ -806,7 +806,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int
             const int i = t - cold;
             const int nn = d.nnew[i];
             if (!nn || d.row_len[nxt][i] == 0) continue;
-            const int mode = MULTI ? d.sp[d.scene_of[i]].mode : (INIT ? kModeInit : kModeStep);
+            const int mode = MULTI ? (d.path[i] >> 2) : (INIT ? kModeInit : kModeStep);
             const int e0 = d.row_start[cur][i], e1 = e0 + d.row_len[cur][i];
             const int32_t* st = d.stash + (size_t)i * p.kstash;
             const int base = d.row_start[nxt][i];
@@ -1491,6 +1491,18 @@ __device__ __forceinline__ void gather(const DemDev& d, const DemParams& p, int 
     }
 }
 
+// Skin test: true once the FP32 position (fx, fy, fz) lies more than skin/2
+// from xr, the position the scene's neighbour lists were built at (FP32
+// rounding of both positions is taken off the allowance).
+__device__ __forceinline__ bool left_skin(const SceneParams& S, float fx, float fy, float fz,
+                                          float4 xr) {
+    const float ex = fx - xr.x, ey = fy - xr.y, ez = fz - xr.z;
+    const float M = fmaxf(fmaxf(fabsf(fx), fabsf(fy)), fabsf(fz)) +
+                    fmaxf(fmaxf(fabsf(xr.x), fabsf(xr.y)), fabsf(xr.z));
+    const float lim = S.f_half_skin - M * 0x1p-21f;
+    return !(lim > 0.0f) || !(ex * ex + ey * ey + ez * ez <= lim * lim);
+}
+
 template <bool MULTI, bool F32>
 __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1631,15 +1643,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
         const float fx = d2f(px1 - S.dmin[0]), fy = d2f(py1 - S.dmin[1]),
                     fz = d2f(pz1 - S.dmin[2]);
         d.pos32[i] = make_float4(fx, fy, fz, reach32(fx, fy, fz, d.rm32[i].z));
-        bool moved = false;
-        if (S.f_half_skin > 0.0f) {
-            const float4 xr = d.xref[i];
-            const float ex = fx - xr.x, ey = fy - xr.y, ez = fz - xr.z;
-            const float M = fmaxf(fmaxf(fabsf(fx), fabsf(fy)), fabsf(fz)) +
-                            fmaxf(fmaxf(fabsf(xr.x), fabsf(xr.y)), fabsf(xr.z));
-            const float lim = S.f_half_skin - M * 0x1p-21f;
-            moved = !(lim > 0.0f) || !(ex * ex + ey * ey + ez * ez <= lim * lim);
-        }
+        const bool moved = S.f_half_skin > 0.0f && left_skin(S, fx, fy, fz, d.xref[i]);
         const unsigned am = __activemask();
         const unsigned peers = __match_any_sync(am, moved ? sc : -1);
         if (moved && lane_id() == (unsigned)(__ffs(peers) - 1) && d.sflags[nxt][sc] == 0u)
@@ -1892,8 +1896,12 @@ void launch_selftest_conv(long long n, unsigned long long seed, unsigned long lo
 }
 
 
+// FP32 positions of slots [first, first + n) from the FP64 ones; with a
+// flag buffer `fb` >= 0 (the one the next step reads), a scene with a particle
+// now beyond skin/2 of its list position is flagged for a full search, as
+// after an integration.
 template <bool MULTI>
-__global__ void k_refresh_pos32(DemDev d, DemParams p, int first, int n) {
+__global__ void k_refresh_pos32(DemDev d, DemParams p, int first, int n, int fb) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int i = first + t;
@@ -1903,12 +1911,39 @@ __global__ void k_refresh_pos32(DemDev d, DemParams p, int first, int n) {
     const float fx = d2f(d.px[i] - S.dmin[0]), fy = d2f(d.py[i] - S.dmin[1]),
                 fz = d2f(d.pz[i] - S.dmin[2]);
     d.pos32[i] = make_float4(fx, fy, fz, reach32(fx, fy, fz, d.rm32[i].z));
+    if (fb >= 0 && (!(S.f_half_skin > 0.0f) || left_skin(S, fx, fy, fz, d.xref[i])) &&
+        d.sflags[fb][sc] == 0u)
+        atomicOr(&d.sflags[fb][sc], 1u);
 }
 void launch_refresh_pos32(const DemDev& d, const DemParams& p, bool multi, int first, int n,
-                          cudaStream_t s) {
+                          int fb, cudaStream_t s) {
     if (n <= 0) return;
-    if (multi) k_refresh_pos32<true><<<blocks_for(n, kThreads), kThreads, 0, s>>>(d, p, first, n);
-    else k_refresh_pos32<false><<<blocks_for(n, kThreads), kThreads, 0, s>>>(d, p, first, n);
+    const int g = blocks_for(n, kThreads);
+    fb = fb == 0 || fb == 1 ? fb : -1;
+    if (multi) k_refresh_pos32<true><<<g, kThreads, 0, s>>>(d, p, first, n, fb);
+    else k_refresh_pos32<false><<<g, kThreads, 0, s>>>(d, p, first, n, fb);
+}
+
+// Particle state exchange: up to kXferFields fields, each a k-component
+// record per particle (the host's layout) <-> k columns of the structure of
+// arrays at slots [p0, p0 + n).  A record array is device-accessible caller
+// memory (page-locked host or device) or the library's staging copy.
+__global__ void k_xfer(XferSet x, int n, int p0, bool to_cols) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    for (int f = 0; f < x.nf; ++f) {
+        const int k = x.k[f];
+        double* const rec = x.rec[f] + (size_t)k * t;
+        if (to_cols) {
+            for (int c = 0; c < k; ++c) x.col[f][c][p0 + t] = rec[c];
+        } else {
+            for (int c = 0; c < k; ++c) rec[c] = x.col[f][c][p0 + t];
+        }
+    }
+}
+void launch_xfer(const XferSet& x, int n, int p0, bool to_cols, cudaStream_t s) {
+    if (n <= 0 || x.nf <= 0) return;
+    k_xfer<<<blocks_for(n, kThreads), kThreads, 0, s>>>(x, n, p0, to_cols);
 }
 
 void launch_recode(const DemDev& d, int buf, int n, bool to_pairs, cudaStream_t s) {

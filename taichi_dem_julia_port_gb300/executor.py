@@ -34,13 +34,26 @@ def _f64(a, shape=None):
     return a.reshape(shape) if shape is not None else a
 
 
-def read_particles(lib, call, n: int, forces: bool, where: str) -> dict:
-    """Particle state through a dem_*get_particles call taking a DemParticleState*."""
-    out = {k: np.empty((n, 3)) for k in ("pos", "vel", "omega", "wall_shear")}
-    out["quat"] = np.empty((n, 4))
-    if forces:
-        out["force"] = np.empty((n, 3))
-        out["moment"] = np.empty((n, 3))
+_PARTICLE_FIELDS = {"pos": 3, "vel": 3, "omega": 3, "quat": 4, "force": 3, "moment": 3,
+                    "wall_shear": 3}
+
+
+def read_particles(lib, call, n: int, forces: bool, where: str, out: dict | None = None) -> dict:
+    """Particle state through a dem_*get_particles call taking a DemParticleState*.
+
+    `out` may hold preallocated C-contiguous float64 (n, k) arrays for any of
+    the fields (page-locked ones are copied into directly by DMA); the fields
+    it holds are the ones read, others are allocated as needed."""
+    if out is None:
+        out = {k: np.empty((n, c)) for k, c in _PARTICLE_FIELDS.items()
+               if forces or k not in ("force", "moment")}
+    else:
+        for k, a in out.items():
+            c = _PARTICLE_FIELDS[k]
+            if (not isinstance(a, np.ndarray) or a.dtype != np.float64 or a.shape != (n, c)
+                    or not a.flags.c_contiguous or not a.flags.writeable):
+                raise ValueError(f"out[{k!r}] must be a writeable C-contiguous float64 "
+                                 f"array of shape ({n}, {c})")
     st = _abi.DemParticleState(n, *(ptr(out.get(k), C.c_double) for k in
                                     ("pos", "vel", "omega", "quat", "force", "moment",
                                      "wall_shear")))
@@ -171,9 +184,10 @@ class GlobalData:
         check(self.lib, self.lib.dem_sync(self.h), "dem_sync")
 
     # ---- state ----------------------------------------------------------------
-    def particles(self, forces: bool = True) -> dict:
+    def particles(self, forces: bool = True, out: dict | None = None) -> dict:
+        """Particle state; `out` may hold preallocated (e.g. pinned) arrays."""
         return read_particles(self.lib, lambda st: self.lib.dem_get_particles(self.h, st),
-                              self.n, forces, "dem_get_particles")
+                              self.n, forces, "dem_get_particles", out)
 
     def set_particles(self, pos=None, vel=None, omega=None, quat=None, wall_shear=None) -> None:
         n = self.n
