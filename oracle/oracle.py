@@ -128,7 +128,7 @@ class OracleScene:
         out = {k: np.empty((n, 3)) for k in ("pos", "vel", "omega", "wall_shear", "force",
                                               "moment")}
         out["quat"] = np.empty((n, 4))
-        st = _abi.DemParticleState(n, *(ptr(out[k], C.c_double) for k in
+        st = _abi.DemParticleState(n, *(out[k].ctypes.data for k in
                                         ("pos", "vel", "omega", "quat", "force", "moment",
                                          "wall_shear")))
         self.lib.oracle_get_particles(self.h, C.byref(st))
@@ -139,7 +139,7 @@ class OracleScene:
         def f(a, k):
             return None if a is None else np.ascontiguousarray(a, np.float64).reshape(n, k)
         arrs = [f(pos, 3), f(vel, 3), f(omega, 3), f(quat, 4), None, None, f(wall_shear, 3)]
-        st = _abi.DemParticleState(n, *(ptr(a, C.c_double) for a in arrs))
+        st = _abi.DemParticleState(n, *(None if a is None else a.ctypes.data for a in arrs))
         self.lib.oracle_set_particles(self.h, C.byref(st))
 
     def contacts(self) -> dict:

@@ -75,8 +75,11 @@ class DemParticlesIn(C.Structure):
 
 
 class DemParticleState(C.Structure):
-    _fields_ = [("n", C.c_int64), ("pos", _PD), ("vel", _PD), ("omega", _PD), ("quat", _PD),
-                ("force", _PD), ("moment", _PD), ("wall_shear", _PD)]
+    # double* fields held as addresses (c_void_p: built from integers, which
+    # keeps the per-step state exchange cheap)
+    _fields_ = [("n", C.c_int64), ("pos", C.c_void_p), ("vel", C.c_void_p),
+                ("omega", C.c_void_p), ("quat", C.c_void_p), ("force", C.c_void_p),
+                ("moment", C.c_void_p), ("wall_shear", C.c_void_p)]
 
 
 class DemParticleStatic(C.Structure):

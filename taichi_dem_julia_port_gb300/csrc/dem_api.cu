@@ -352,6 +352,7 @@ struct DemHandle {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double* xfer = nullptr;    // device staging: particle records in the host's layout
     int64_t xfer_n = 0;        // doubles
+    int* err_host = nullptr;   // page-locked copy of the device error word
 };
 
 #define CU(expr)                                                                            \
@@ -462,6 +463,8 @@ void free_all(DemHandle* h) {
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->xfer) cudaFree(h->xfer);
     h->xfer = nullptr;
+    if (h->err_host) cudaFreeHost(h->err_host);
+    h->err_host = nullptr;
 }
 
 // Default launch shape: blocks of at most 256 threads, small enough that a
@@ -761,10 +764,22 @@ double* device_view(const void* p) {
 // per particle, nullptr = field not exchanged) and the columns `cols[f]` at
 // slots [p0, p0 + n): one kernel over all fields, which reads or writes
 // device-accessible buffers in place; pageable buffers go through the
-// library's staging copy with one cudaMemcpyAsync each.  Synchronises.
+// library's staging copy with one cudaMemcpyAsync each.  Synchronises; with
+// `error`, also returns the device error word as of the exchange.
 int exchange(DemHandle* h, int64_t p0, int64_t n, const int* k, double* const* host,
-             double* const (*cols)[4], int nfields, bool to_cols) {
-    if (n <= 0) return DEM_OK;
+             double* const (*cols)[4], int nfields, bool to_cols, int* error = nullptr) {
+    if (error) {
+        if (!h->err_host) CU(cudaMallocHost(&h->err_host, 64));
+        CU(cudaMemcpyAsync(h->err_host, &h->d.ctr->error, sizeof(int), cudaMemcpyDeviceToHost,
+                           h->stream));
+    }
+    if (n <= 0) {
+        if (error) {
+            CU(cudaStreamSynchronize(h->stream));
+            *error = *h->err_host;
+        }
+        return DEM_OK;
+    }
     XferSet x{};
     double* staged[kXferFields] = {};
     const double* src_host[kXferFields] = {};
@@ -798,6 +813,7 @@ int exchange(DemHandle* h, int64_t p0, int64_t n, const int* k, double* const* h
                 CU(cudaMemcpyAsync(const_cast<double*>(src_host[f]), staged[f],
                                    sizeof(double) * x.k[f] * n, cudaMemcpyDeviceToHost, h->stream));
     CU(cudaStreamSynchronize(h->stream));
+    if (error) *error = *h->err_host;
     return DEM_OK;
 }
 
@@ -811,8 +827,9 @@ int get_particles_range(DemHandle* h, int64_t p0, int64_t n, DemParticleState* o
                                {d.wx, d.wy, d.wz},      {d.qw, d.qx, d.qy, d.qz},
                                {d.fx, d.fy, d.fz},      {d.tx, d.ty, d.tz},
                                {d.wsx, d.wsy, d.wsz}};
-    TRY(exchange(h, p0, n, k, host, cols, 7, false));
-    return device_error(h);
+    int err = 0;
+    TRY(exchange(h, p0, n, k, host, cols, 7, false, &err));
+    return error_code(err);
 }
 
 // Contact entries of the current buffer whose owner lies in slots

@@ -31,7 +31,7 @@ PRECISIONS = {"fp64": _abi.DEM_FP64, "fp32": _abi.DEM_FP32_FORCE,
 
 def _f64(a, shape=None):
     a = np.ascontiguousarray(a, dtype=np.float64)
-    return a.reshape(shape) if shape is not None else a
+    return a.reshape(shape) if shape is not None and a.shape != shape else a
 
 
 _PARTICLE_FIELDS = {"pos": 3, "vel": 3, "omega": 3, "quat": 4, "force": 3, "moment": 3,
@@ -54,9 +54,8 @@ def read_particles(lib, call, n: int, forces: bool, where: str, out: dict | None
                     or not a.flags.c_contiguous or not a.flags.writeable):
                 raise ValueError(f"out[{k!r}] must be a writeable C-contiguous float64 "
                                  f"array of shape ({n}, {c})")
-    st = _abi.DemParticleState(n, *(ptr(out.get(k), C.c_double) for k in
-                                    ("pos", "vel", "omega", "quat", "force", "moment",
-                                     "wall_shear")))
+    st = _abi.DemParticleState(n, *(out[k].ctypes.data if k in out else None for k in
+                                    _PARTICLE_FIELDS))
     check(lib, call(C.byref(st)), where)
     return out
 
@@ -191,12 +190,11 @@ class GlobalData:
 
     def set_particles(self, pos=None, vel=None, omega=None, quat=None, wall_shear=None) -> None:
         n = self.n
-        arrs = {"pos": pos, "vel": vel, "omega": omega, "wall_shear": wall_shear}
-        arrs = {k: (_f64(v, (n, 3)) if v is not None else None) for k, v in arrs.items()}
-        q = _f64(quat, (n, 4)) if quat is not None else None
-        st = _abi.DemParticleState(n, ptr(arrs["pos"], C.c_double), ptr(arrs["vel"], C.c_double),
-                                   ptr(arrs["omega"], C.c_double), ptr(q, C.c_double), None, None,
-                                   ptr(arrs["wall_shear"], C.c_double))
+        # C-contiguous float64 (n, k) copies only where the input is not one already
+        arrs = [None if v is None else _f64(v, (n, k))
+                for v, k in ((pos, 3), (vel, 3), (omega, 3), (quat, 4), (wall_shear, 3))]
+        st = _abi.DemParticleState(n, *(None if a is None else a.ctypes.data for a in arrs[:4]),
+                                   None, None, None if arrs[4] is None else arrs[4].ctypes.data)
         check(self.lib, self.lib.dem_set_particles(self.h, C.byref(st)), "dem_set_particles")
 
     def static(self) -> dict:

@@ -313,7 +313,7 @@ def test_state_exchange_device_buffers(gpu):
     want = g.particles()
     dev = {k: torch.empty((sc.n, 4 if k == "quat" else 3), dtype=torch.float64, device="cuda")
            for k in PARTICLE_KEYS}
-    dptr = {k: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)) for k, t in dev.items()}
+    dptr = {k: t.data_ptr() for k, t in dev.items()}
     st = _abi.DemParticleState(sc.n, *(dptr[k] for k in PARTICLE_KEYS))
     assert g.lib.dem_get_particles(g.h, C.byref(st)) == 0
     torch.cuda.synchronize()
