@@ -24,6 +24,12 @@ appends this comparison as `batched` (50 timed steps).  --workload c5 runs the
 served request stream (Poisson arrivals, continuous batching within an HBM
 budget) and reports aggregate particle-steps/s with p50/p99 completion latency.
 
+For c1/c2 the line adds `reference_gpu_proxy`: the same scene on a plain CUDA
+C++ restatement of the reference's GPU path with its own structure (AoS
+records, BitTables, ~25 launches and 3 device-to-host reads per step;
+baseline/refproxy), timed the same way, standing in for the reference's
+CUDA.jl path, which cannot run on this GPU.
+
 --impl reference times the CPU restatement of the reference step on all host
 threads (the reference's own GPU path, Julia + CUDA.jl, cannot run here).
 With N > 1 (torchrun) every rank steps an independent replica (the path does
@@ -425,6 +431,33 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_proxy(args, sc, flush) -> dict:
+    """The reference-structured GPU proxy (baseline/refproxy: the reference's
+    kernel decomposition, AoS records, BitTables and three host reads per
+    step, in plain CUDA C++) on the same scene, timed the same way: after the
+    same warm-up, one step at a time between L2 flushes, CUDA events."""
+    import torch
+    from baseline.refproxy import RefProxy
+    p = RefProxy(sc.cfg, sc.particles)
+    if sc.bonded:
+        p.initialize()
+    steps = min(args.steps, 500)
+    for _ in range(args.warmup):
+        p.simulate(1)
+    total = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        total += p.simulate_timed(1)
+    p.close()
+    ms = total / steps
+    return {"value": sc.n / (ms * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms,
+            "steps": steps, "warmup": args.warmup,
+            "kind": "reference-structured CUDA C++ proxy for the reference's CUDA.jl path "
+                    "(AoS 272/136-byte records, BitTables, ~25 launches and 3 device-to-host "
+                    "reads per step); the CUDA.jl path itself cannot run on this GPU"}
+
+
 def cpu_baseline(sc, seconds: float) -> dict:
     from oracle.oracle import OracleScene, host_threads
     threads = host_threads()
@@ -464,6 +497,8 @@ def main() -> None:
     ap.add_argument("--e2e-steps", type=int, default=500)
     ap.add_argument("--profile-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-proxy", action="store_true",
+                    help="skip the reference-structured GPU proxy (c1/c2)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -584,6 +619,9 @@ def main() -> None:
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, args.cpu_seconds)
+    proxy = None
+    if rank == 0 and args.workload in ("c1", "c2") and not args.no_proxy:
+        proxy = run_proxy(args, sc, flush)
     batched = None
     if args.workload == "c2" and not args.no_batched:
         g.close()
@@ -608,6 +646,8 @@ def main() -> None:
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": KERNELS_PER_STEP * args.steps,
         }
+        if proxy:
+            line["reference_gpu_proxy"] = proxy
         if batched:
             line["batched"] = batched
         print(json.dumps(line), flush=True)
