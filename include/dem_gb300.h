@@ -223,7 +223,10 @@ typedef struct DemLaunchShape {
     int32_t integrate_block;
     int32_t detect_blocks_per_sm; /* register budget of the pair search: 3 or 4 (0 = 4) */
     int32_t force_blocks_per_sm;  /* FP32 force kernel: 0 (compiler's choice) or 4     */
-    int32_t pad;
+    int32_t dependent_launch;     /* a step's kernels: 0 ordinary launches; 1
+                                   * programmatic dependent launches (each may be
+                                   * scheduled while its predecessor finishes); 2 the
+                                   * same, successor scheduled once all blocks run  */
 } DemLaunchShape;
 
 int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* shape);

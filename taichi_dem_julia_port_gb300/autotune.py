@@ -9,8 +9,9 @@ for any launch shape; the arena tests check both bit for bit.  The steps taken
 while tuning are ordinary simulation steps.
 
 The search is coordinate descent: cell factor first, then the force kernel's
-block and grid, then the compaction grid, the integration block and the
-pair search's register budget; each
+block and grid, then the compaction grid, the integration block, the FP32
+force kernel's register budget, the launch mode (ordinary or programmatic
+dependent launches) and the pair search's register budget; each
 candidate is timed over `steps` steps after one untimed step.
 """
 from __future__ import annotations
@@ -22,6 +23,7 @@ BLOCKS = (64, 128, 256)
 GRIDS_PER_SM = (4, 8, 16, 32)
 INTEGRATE_BLOCKS = (32, 64, 128, 256)
 DETECT_BLOCKS = (3, 4)  # pair-search register budget (blocks per SM)
+DEPENDENT = (0, 1, 2)   # ordinary / programmatic dependent launches (2: early trigger)
 FORCE_BLOCKS = (0, 4)   # FP32 force kernel register budget (0: compiler's choice)
 
 
@@ -47,7 +49,7 @@ def _time(target, steps: int) -> float:
 def autotune(target, sm_count: int = 152, steps: int = 10, cell_factors=CELL_FACTORS,
              blocks=BLOCKS, grids_per_sm=GRIDS_PER_SM,
              integrate_blocks=INTEGRATE_BLOCKS, detect_blocks=DETECT_BLOCKS,
-             force_blocks=FORCE_BLOCKS) -> TuneResult:
+             force_blocks=FORCE_BLOCKS, dependent=DEPENDENT) -> TuneResult:
     """Tunes `target` in place and returns the chosen settings."""
     trials = []
     is_arena = hasattr(target, "set_cell_factor")
@@ -88,6 +90,13 @@ def autotune(target, sm_count: int = 152, steps: int = 10, cell_factors=CELL_FAC
             best, shape = t, cand
     for fb in force_blocks:
         cand = dict(shape, force_blocks_per_sm=fb)
+        target.set_launch_shape(**cand)
+        t = _time(target, steps)
+        trials.append((cand, t))
+        if t < best:
+            best, shape = t, cand
+    for dl in dependent:
+        cand = dict(shape, dependent_launch=dl)
         target.set_launch_shape(**cand)
         t = _time(target, steps)
         trials.append((cand, t))

@@ -479,7 +479,7 @@ LaunchShape default_shape(const DemHandle* h) {
     };
     const int64_t n = h->multi ? INT64_MAX / 8 : h->n_cap;
     const int ib = block_for(n), fb = block_for(3 * n), cb = block_for(4 * n);
-    return LaunchShape{fb, h->sm_count * 16, cb, h->sm_count * 16, ib, 4, 0};
+    return LaunchShape{fb, h->sm_count * 16, cb, h->sm_count * 16, ib, 4, 0, 0};
 }
 
 int init_handle(DemHandle* h) {
@@ -489,6 +489,7 @@ int init_handle(DemHandle* h) {
     TRY(allocate(h));
     h->ntiles_cells = std::max(1, scan_tiles((int64_t)h->p.T));
     h->shape = default_shape(h);
+    h->p.dep = h->shape.dependent_launch;
     return DEM_OK;
 }
 
@@ -1209,12 +1210,14 @@ int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* sh) {
         (sh->force_blocks_per_sm != 0 && sh->force_blocks_per_sm != 4) ||
         sh->compact_block < 32 || sh->compact_block > 256 || sh->compact_block % 32 ||
         sh->integrate_block < 32 || sh->integrate_block > 256 || sh->integrate_block % 32 ||
-        sh->force_grid < 1 || sh->compact_grid < 1)
+        sh->force_grid < 1 || sh->compact_grid < 1 ||
+        sh->dependent_launch < 0 || sh->dependent_launch > 2)
         return DEM_ERR_INVALID;
     h->shape = LaunchShape{sh->force_block, sh->force_grid, sh->compact_block, sh->compact_grid,
                            sh->integrate_block,
                            sh->detect_blocks_per_sm ? sh->detect_blocks_per_sm : 4,
-                           sh->force_blocks_per_sm};
+                           sh->force_blocks_per_sm, sh->dependent_launch};
+    h->p.dep = h->shape.dependent_launch;
     drop_graphs(h);
     return DEM_OK;
 }
@@ -1224,7 +1227,7 @@ int dem_get_launch_shape(DemHandle* h, DemLaunchShape* out) {
     *out = DemLaunchShape{h->shape.force_block,         h->shape.force_grid,
                           h->shape.compact_block,       h->shape.compact_grid,
                           h->shape.integrate_block,     h->shape.detect_blocks_per_sm,
-                          h->shape.force_blocks_per_sm, 0};
+                          h->shape.force_blocks_per_sm, h->shape.dependent_launch};
     return DEM_OK;
 }
 

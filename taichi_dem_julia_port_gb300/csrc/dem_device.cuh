@@ -175,3 +175,15 @@ __device__ __forceinline__ double jl_sign(double x) { return x < 0.0 ? -1.0 : (x
 __device__ __forceinline__ void raise_error(DevCounters* c, int bit) { atomicOr(&c->error, bit); }
 
 }  // namespace dem
+
+// Programmatic dependent launch: a kernel launched with the programmatic
+// stream serialization attribute may be scheduled while its predecessor in
+// the stream is still running.  It first waits here for that grid to complete
+// (its memory operations visible).  With `early`, it then lets its own
+// successor be scheduled (once every block has passed this point); otherwise
+// the successor is scheduled as this grid's blocks exit.  For an ordinary
+// launch both instructions return at once.
+__device__ __forceinline__ void dep_begin(bool early = false) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (early) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}

@@ -179,6 +179,8 @@ struct DemParams {
     int kvl;        // neighbour-list capacity per particle
     int ns;         // scene records
     int sms;        // streaming multiprocessors (grid-stride launch sizes)
+    int dep;        // a step's kernels: 0 ordinary launches, 1 programmatic dependent
+                    // launches, 2 the same with the successor scheduled early
     SceneParams s0; // the scene of a single-scene handle
 };
 
@@ -191,6 +193,7 @@ struct LaunchShape {
     int integrate_block;
     int detect_blocks_per_sm;  // register budget of the pair search: 3 or 4 blocks per SM
     int force_blocks_per_sm;   // register budget of the FP32 force kernel: 0 (none) or 4
+    int dependent_launch;      // 0 ordinary, 1 programmatic dependent, 2 with early trigger
 };
 
 // ---- launchers (dem_kernels.cu) --------------------------------------------

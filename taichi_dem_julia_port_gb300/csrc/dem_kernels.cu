@@ -80,6 +80,7 @@ __global__ void __launch_bounds__(kScanBlock)
                 unsigned long long* state, unsigned long long* tickets, DevCounters* ctr) {
     __shared__ unsigned long long s_ticket;
     __shared__ unsigned long long s_warp[kScanBlock / 32];
+    dep_begin();
     __shared__ unsigned long long s_prefix;
     if (LIMITED) {
         const long long lim = (long long)ctr->bmax + 1;
@@ -230,6 +231,7 @@ __device__ __forceinline__ int4 cell_of_screened(const double pos[3], const doub
 // `count_particles!` (src/kernels.jl:7-13).
 template <bool MULTI>
 __global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p, int cur, int all) {
+    dep_begin(p.dep == 2);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool act = i < p.n;
     uint32_t b = 0;
@@ -273,6 +275,7 @@ __global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p, int cu
 // `get_particle_id!` (src/kernels.jl:15-22): counting-sort scatter.  The
 // atomic decrements bring every count back to zero.
 __global__ void __launch_bounds__(kThreads) k_scatter(DemDev d, DemParams p) {
+    dep_begin(p.dep == 2);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t b = i < p.n ? d.bucket[i] : kNoBucket;
     const bool act = b != kNoBucket;
@@ -294,6 +297,7 @@ __global__ void __launch_bounds__(kThreads) k_scatter(DemDev d, DemParams p) {
 // finished).
 template <bool MULTI>
 __global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p, int cur) {
+    dep_begin(p.dep == 2);
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0) d.ctr->bmax = 0u;
     if (k >= sorted_count(d)) return;
@@ -543,6 +547,7 @@ __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p
 template <bool INIT, bool MULTI, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p, int cur) {
     __shared__ DetectShared sh[kThreads / kLanes];
+    dep_begin(p.dep == 2);
     const int lane = threadIdx.x & (kLanes - 1);
     const int g = threadIdx.x / kLanes;
     const unsigned gmask = 0xffu << (lane_id() & ~7u);
@@ -589,6 +594,7 @@ struct ListShared {
 template <bool MULTI>
 __global__ void __launch_bounds__(kThreads) k_vdetect(DemDev d, DemParams p, int cur) {
     __shared__ ListShared sh[kThreads / kVLanes];
+    dep_begin(p.dep == 2);
     const int lane = threadIdx.x & (kVLanes - 1);
     const int g = threadIdx.x / kVLanes;
     const unsigned gmask = 0xfu << (lane_id() & ~3u);
@@ -711,6 +717,7 @@ __device__ __forceinline__ void scene_flags_one(const DemDev& d, const DemParams
 // arena slots have length 0.  A row that would cross the capacity raises
 // kErrCapacity and is dropped (length 0).
 __global__ void __launch_bounds__(kThreads) k_rows(DemDev d, DemParams p, int nxt) {
+    dep_begin(p.dep == 2);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int len = i < p.n ? d.row_len[nxt][i] : 0;
     int incl = len;
@@ -741,6 +748,7 @@ __global__ void __launch_bounds__(kThreads) k_rows(DemDev d, DemParams p, int nx
 // particle for its new contacts; each computes its final slot directly.
 template <bool INIT, bool MULTI>
 __global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int cur) {
+    dep_begin(p.dep == 2);
     const int nxt = cur ^ 1;
     const int cold = min((int)d.ctr->row_alloc[cur], p.cap);
     const ContactSoA o = d.c[cur];
@@ -1355,10 +1363,12 @@ __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, 
 // four 256-thread blocks per SM (an autotuner choice for the FP32 mode).
 template <typename T, bool MULTI>
 __global__ void __launch_bounds__(kThreads) k_force(DemDev d, DemParams p, int nxt) {
+    dep_begin(p.dep == 2);
     force_body<T, MULTI>(d, p, nxt);
 }
 template <typename T, bool MULTI>
 __global__ void __launch_bounds__(kThreads, 4) k_force4(DemDev d, DemParams p, int nxt) {
+    dep_begin(p.dep == 2);
     force_body<T, MULTI>(d, p, nxt);
 }
 
@@ -1505,6 +1515,7 @@ __device__ __forceinline__ bool left_skin(const SceneParams& S, float fx, float 
 
 template <bool MULTI, bool F32>
 __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, int cur) {
+    dep_begin(p.dep == 2);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nxt = cur ^ 1;
     if (i == 0) d.ctr->row_alloc[cur] = 0u;  // the free buffer is next step's target
@@ -1741,6 +1752,31 @@ __global__ void __launch_bounds__(kThreads) k_recode(ContactSoA w, int n, int to
 // block sizes of the grid-stride kernels: a multiple of 32 in [32, kThreads]
 inline int clamp_block(int b) { return b < 32 ? 32 : (b > kThreads ? kThreads : (b / 32) * 32); }
 
+// Launches a step kernel on `s`.  With `dep` it is a programmatic dependent
+// launch: the grid may be scheduled while the previous kernel in the stream
+// finishes, and every step kernel begins with dep_begin(), which waits for
+// that kernel's completion before touching any state.  Inside a captured
+// graph this becomes a programmatic edge; the order of effects is the same.
+template <typename... KArgs, typename... Args>
+void launch(bool dep, void (*kern)(KArgs...), int grid, int block, cudaStream_t s,
+            Args... args) {
+    if (!dep) {
+        kern<<<grid, block, 0, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 }  // namespace
 
 int scan_tiles(int64_t n) { return (int)((n + kScanTile - 1) / kScanTile); }
@@ -1760,14 +1796,13 @@ void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi,
                        int ntiles_cells, cudaStream_t s) {
     if (p.n == 0) return;
     const int nb = blocks_for(p.n, kThreads);
-    if (multi) k_hash<true><<<nb, kThreads, 0, s>>>(d, p, cur, all ? 1 : 0);
-    else k_hash<false><<<nb, kThreads, 0, s>>>(d, p, cur, all ? 1 : 0);
-    k_scan_excl<uint32_t, true><<<ntiles_cells, kScanBlock, 0, s>>>(
-        d.cell_count, d.cell_start, (long long)p.T, ntiles_cells, d.scan_state[kScanCells],
-        &d.ctr->tickets[kScanCells], d.ctr);
-    k_scatter<<<nb, kThreads, 0, s>>>(d, p);
-    if (multi) k_canon<true><<<nb, kThreads, 0, s>>>(d, p, cur);
-    else k_canon<false><<<nb, kThreads, 0, s>>>(d, p, cur);
+    const bool dep = p.dep != 0;
+    launch(dep, multi ? k_hash<true> : k_hash<false>, nb, kThreads, s, d, p, cur, all ? 1 : 0);
+    launch(dep, k_scan_excl<uint32_t, true>, ntiles_cells, kScanBlock, s,
+           (const uint32_t*)d.cell_count, d.cell_start, (long long)p.T, ntiles_cells,
+           d.scan_state[kScanCells], &d.ctr->tickets[kScanCells], d.ctr);
+    launch(dep, k_scatter, nb, kThreads, s, d, p);
+    launch(dep, multi ? k_canon<true> : k_canon<false>, nb, kThreads, s, d, p, cur);
 }
 
 template <int MINB>
@@ -1775,9 +1810,10 @@ void launch_detect_b(const DemDev& d, const DemParams& p, int cur, bool init, bo
                      cudaStream_t s) {
     // grid-stride: one wave of resident blocks at most
     const int nb = max(1, min(blocks_for((long long)p.n * kLanes, kThreads), p.sms * MINB));
-    if (multi) k_detect<false, true, MINB><<<nb, kThreads, 0, s>>>(d, p, cur);
-    else if (init) k_detect<true, false, MINB><<<nb, kThreads, 0, s>>>(d, p, cur);
-    else k_detect<false, false, MINB><<<nb, kThreads, 0, s>>>(d, p, cur);
+    launch(p.dep != 0,
+           multi ? k_detect<false, true, MINB>
+                 : (init ? k_detect<true, false, MINB> : k_detect<false, false, MINB>),
+           nb, kThreads, s, d, p, cur);
 }
 
 void launch_detect_full(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
@@ -1793,10 +1829,10 @@ void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool
     launch_detect_full(d, p, cur, init, multi, sh, s);
     if (!init) {  // the scenes that test their neighbour lists
         const int nv = max(1, min(blocks_for((long long)p.n * kVLanes, kThreads), p.sms * 8));
-        if (multi) k_vdetect<true><<<nv, kThreads, 0, s>>>(d, p, cur);
-        else k_vdetect<false><<<nv, kThreads, 0, s>>>(d, p, cur);
+        launch(p.dep != 0, multi ? k_vdetect<true> : k_vdetect<false>, nv, kThreads, s, d, p,
+               cur);
     }
-    k_rows<<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, cur ^ 1);
+    launch(p.dep != 0, k_rows, blocks_for(p.n, kThreads), kThreads, s, d, p, cur ^ 1);
 }
 
 void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
@@ -1804,9 +1840,9 @@ void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, boo
     if (p.n == 0) return;
     const int block = clamp_block(sh.compact_block);
     const int nb = min(blocks_for((long long)p.cap + p.n, block), max(sh.compact_grid, 1));
-    if (multi) k_compact<false, true><<<nb, block, 0, s>>>(d, p, cur);
-    else if (init) k_compact<true, false><<<nb, block, 0, s>>>(d, p, cur);
-    else k_compact<false, false><<<nb, block, 0, s>>>(d, p, cur);
+    launch(p.dep != 0,
+           multi ? k_compact<false, true> : (init ? k_compact<true, false> : k_compact<false, false>),
+           nb, block, s, d, p, cur);
 }
 
 void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, const LaunchShape& sh,
@@ -1816,16 +1852,15 @@ void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, cons
     const int grid = min(blocks_for(p.cap, block), max(sh.force_grid, 1));
     if (p.precision == 1) {
         // FP32 mode: register budget for 3 (default) or 4 blocks of 256 per SM
-        if (sh.force_blocks_per_sm == 4) {
-            if (multi) k_force4<float, true><<<grid, block, 0, s>>>(d, p, nxt);
-            else k_force4<float, false><<<grid, block, 0, s>>>(d, p, nxt);
-        } else {
-            if (multi) k_force<float, true><<<grid, block, 0, s>>>(d, p, nxt);
-            else k_force<float, false><<<grid, block, 0, s>>>(d, p, nxt);
-        }
+        if (sh.force_blocks_per_sm == 4)
+            launch(p.dep != 0, multi ? k_force4<float, true> : k_force4<float, false>, grid, block,
+                   s, d, p, nxt);
+        else
+            launch(p.dep != 0, multi ? k_force<float, true> : k_force<float, false>, grid, block, s,
+                   d, p, nxt);
     } else {
-        if (multi) k_force<double, true><<<grid, block, 0, s>>>(d, p, nxt);
-        else k_force<double, false><<<grid, block, 0, s>>>(d, p, nxt);
+        launch(p.dep != 0, multi ? k_force<double, true> : k_force<double, false>, grid, block, s,
+               d, p, nxt);
     }
 }
 
@@ -1834,13 +1869,12 @@ void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
     if (p.n == 0) return;
     const int block = clamp_block(sh.integrate_block);
     const int nb = blocks_for(p.n, block);
-    if (p.precision == 1) {
-        if (multi) k_integrate<true, true><<<nb, block, 0, s>>>(d, p, cur);
-        else k_integrate<false, true><<<nb, block, 0, s>>>(d, p, cur);
-    } else {
-        if (multi) k_integrate<true, false><<<nb, block, 0, s>>>(d, p, cur);
-        else k_integrate<false, false><<<nb, block, 0, s>>>(d, p, cur);
-    }
+    if (p.precision == 1)
+        launch(p.dep != 0, multi ? k_integrate<true, true> : k_integrate<false, true>, nb, block, s,
+               d, p, cur);
+    else
+        launch(p.dep != 0, multi ? k_integrate<true, false> : k_integrate<false, false>, nb, block,
+               s, d, p, cur);
 }
 
 void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cudaStream_t s) {
@@ -1928,17 +1962,30 @@ void launch_refresh_pos32(const DemDev& d, const DemParams& p, bool multi, int f
 // record per particle (the host's layout) <-> k columns of the structure of
 // arrays at slots [p0, p0 + n).  A record array is device-accessible caller
 // memory (page-locked host or device) or the library's staging copy.
-__global__ void k_xfer(XferSet x, int n, int p0, bool to_cols) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
+// A block moves kThreads particles: their k·kThreads record values are one
+// contiguous range, read or written linearly (whole 128-byte lines, which
+// matters most for page-locked host memory across the chip-to-chip link)
+// and transposed through shared memory.
+__global__ void __launch_bounds__(kThreads) k_xfer(XferSet x, int n, int p0, bool to_cols) {
+    __shared__ double tile[4 * kThreads];
+    const int base = blockIdx.x * kThreads;
+    const int m = min(kThreads, n - base);  // particles of this block
+    const int t = threadIdx.x;
     for (int f = 0; f < x.nf; ++f) {
         const int k = x.k[f];
-        double* const rec = x.rec[f] + (size_t)k * t;
+        double* const rec = x.rec[f] + (size_t)k * base;
         if (to_cols) {
-            for (int c = 0; c < k; ++c) x.col[f][c][p0 + t] = rec[c];
+            for (int e = t; e < k * m; e += kThreads) tile[e] = rec[e];
+            __syncthreads();
+            if (t < m)
+                for (int c = 0; c < k; ++c) x.col[f][c][p0 + base + t] = tile[k * t + c];
         } else {
-            for (int c = 0; c < k; ++c) rec[c] = x.col[f][c][p0 + t];
+            if (t < m)
+                for (int c = 0; c < k; ++c) tile[k * t + c] = x.col[f][c][p0 + base + t];
+            __syncthreads();
+            for (int e = t; e < k * m; e += kThreads) rec[e] = tile[e];
         }
+        __syncthreads();  // the tile is reused by the next field
     }
 }
 void launch_xfer(const XferSet& x, int n, int p0, bool to_cols, cudaStream_t s) {

@@ -189,15 +189,19 @@ def test_tuning_knobs_keep_results(gpu):
         a.set_cell_factor(0.4)
         a.step(15)
         a.set_cell_factor(0.7, scene=ids[0])
-        a.set_launch_shape(force_block=256, force_grid=152 * 32, integrate_block=256)
+        a.set_launch_shape(force_block=256, force_grid=152 * 32, integrate_block=256,
+                           dependent_launch=2)
         a.step(10)
         for sid, ref, name in zip(ids, refs, ("cube", "pour")):
             assert_same(a, sid, ref, f"retuned {name}")
     g = GlobalData(cube.cfg, cube.particles)
     g.initialize()
     g.simulate(20)
-    g.set_launch_shape(force_block=96, force_grid=100, compact_grid=50, integrate_block=64)
-    g.simulate(20)
+    g.set_launch_shape(force_block=96, force_grid=100, compact_grid=50, integrate_block=64,
+                       dependent_launch=1)
+    g.simulate(10)
+    g.set_launch_shape(dependent_launch=2)
+    g.simulate(10)
     p, c = g.particles(), g.contacts()
     for k in PARTICLE_KEYS:
         np.testing.assert_array_equal(p[k], refs[0][0][k], err_msg=f"single retuned {k}")
