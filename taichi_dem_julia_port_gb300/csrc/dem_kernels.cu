@@ -1404,12 +1404,9 @@ __device__ __forceinline__ const T* contrib_of(const DemDev& d) {
     else return d.contrib;
 }
 template <typename T, int N>
-__device__ __forceinline__ void add_incoming(const DemDev& d, size_t cap, const int2* il, int nin,
+__device__ __forceinline__ void add_incoming(const DemDev& d, size_t cap, int2 (&v)[N], int nin,
                                              T* F, T* M) {
     const T* cb = contrib_of<T>(d);
-    int2 v[N];
-#pragma unroll
-    for (int u = 0; u < N; ++u) v[u] = u < nin ? il[u] : make_int2(0, 0x7fffffff);
     sort_by_owner<N>(v);
     T g[N][6];
 #pragma unroll
@@ -1438,13 +1435,21 @@ __device__ __forceinline__ void add_incoming(const DemDev& d, size_t cap, const 
 // Sum of the contact contributions on particle i in the fixed order: its own
 // row (by j), then its incoming contacts by owner index.  T = double for the
 // FP64 force mode, float for the FP32 force mode (its contributions are FP32).
+// The caller loads the row (c0, len) and the incoming count with the rest of
+// the particle's state; the first incoming entries are loaded here before the
+// row's contributions, so the two chains of loads overlap.
 template <typename T>
-__device__ __forceinline__ void gather(const DemDev& d, const DemParams& p, int i, int nxt, T* F,
-                                       T* M) {
+__device__ __forceinline__ void gather(const DemDev& d, const DemParams& p, int i, int c0, int len,
+                                       int nin, T* F, T* M) {
     const size_t cap = (size_t)p.cap;
     const T* cb = contrib_of<T>(d);
-    const int c0 = d.row_start[nxt][i];
-    const int c1 = min(c0 + d.row_len[nxt][i], p.cap);
+    nin = nin < p.kin ? nin : p.kin;
+    nin = nin < kMaxIncoming ? nin : kMaxIncoming;
+    const int2* il = d.in_list + (size_t)i * p.kin;
+    int2 v4[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v4[u] = u < nin ? il[u] : make_int2(0, 0x7fffffff);
+    const int c1 = min(c0 + len, p.cap);
     int c = c0;
     for (; c + 1 < c1; c += 2) {
         T a[6], b[6];
@@ -1471,14 +1476,13 @@ __device__ __forceinline__ void gather(const DemDev& d, const DemParams& p, int 
             M[q] += cb[(3 + q) * cap + c];
         }
     }
-    int nin = d.in_cnt[i];
-    nin = nin < p.kin ? nin : p.kin;
-    nin = nin < kMaxIncoming ? nin : kMaxIncoming;
-    const int2* il = d.in_list + (size_t)i * p.kin;
     if (nin <= 4) {
-        add_incoming<T, 4>(d, cap, il, nin, F, M);
+        add_incoming<T, 4>(d, cap, v4, nin, F, M);
     } else if (nin <= 8) {
-        add_incoming<T, 8>(d, cap, il, nin, F, M);
+        int2 v8[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v8[u] = u < 4 ? v4[u] : (u < nin ? il[u] : make_int2(0, 0x7fffffff));
+        add_incoming<T, 8>(d, cap, v8, nin, F, M);
     } else {
         int2 inc[kMaxIncoming];
         for (int u = 0; u < nin; ++u) {
@@ -1529,32 +1533,39 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
         return;
     }
     const SceneParams& S = scene_rec<MULTI>(d, p, sc);
+    // every load of the particle's own state is issued before the gather's
+    // dependent loads (nothing here is stored before the gather completes)
+    const int row0 = d.row_start[nxt][i], rlen = d.row_len[nxt][i], nin = d.in_cnt[i];
+    const double x = d.px[i], y = d.py[i], z = d.pz[i];
+    const double vx = d.vx[i], vy = d.vy[i], vz = d.vz[i];
+    const double wx = d.wx[i], wy = d.wy[i], wz = d.wz[i];
+    const double r = d.r[i], m = d.m[i];
+    const double invm = d.inv_m[i], ii = d.inv_inertia[i];
+    const double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
+    const float4 p32 = d.pos32[i], xr = d.xref[i];
+    const float r32 = d.rm32[i].z;
     double F[3] = {0.0, 0.0, 0.0}, M[3] = {0.0, 0.0, 0.0};
     if constexpr (F32) {
         float Ff[3] = {0.0f, 0.0f, 0.0f}, Mf[3] = {0.0f, 0.0f, 0.0f};
-        gather<float>(d, p, i, nxt, Ff, Mf);
+        gather<float>(d, p, i, row0, rlen, nin, Ff, Mf);
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             F[q] = f2d(Ff[q]);
             M[q] = f2d(Mf[q]);
         }
     } else {
-        gather<double>(d, p, i, nxt, F, M);
+        gather<double>(d, p, i, row0, rlen, nin, F, M);
     }
     d.in_cnt[i] = 0;
-    const double x = d.px[i], y = d.py[i], z = d.pz[i];
-    const double vx = d.vx[i], vy = d.vy[i], vz = d.vz[i];
-    const double wx = d.wx[i], wy = d.wy[i], wz = d.wz[i];
-    const double r = d.r[i], m = d.m[i];
     const double dt = S.dt;
     // resolve_wall!, one wall.  An FP32 screen on the step's starting position
     // (pos32, within 2^-24 of the FP64 one per coordinate) skips the exact
     // test when |n·x - d| exceeds r by a margin that covers its rounding.
     bool wall_near = true;
     if (S.has_wall) {
-        const float4 q = d.pos32[i];
+        const float4 q = p32;
         const float Lf = q.x * S.f_wn[0] + q.y * S.f_wn[1] + q.z * S.f_wn[2] + S.f_wc0;
-        const float rf = d.rm32[i].z;
+        const float rf = r32;
         const float mg = (fabsf(q.x) + fabsf(q.y) + fabsf(q.z) + fabsf(S.f_wc0) + rf) * 0x1p-20f;
         wall_near = !(fabsf(Lf) > rf + mg);
     }
@@ -1638,7 +1649,6 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
         }
     }
     // update!
-    const double invm = d.inv_m[i];
     const double ax = F[0] * invm, ay = F[1] * invm, az = F[2] * invm;
     const double hdt2 = S.hdt2;  // 0.5·(dt·dt)
     const double px1 = x + vx * dt + ax * hdt2, py1 = y + vy * dt + ay * hdt2,
@@ -1653,8 +1663,8 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     {
         const float fx = d2f(px1 - S.dmin[0]), fy = d2f(py1 - S.dmin[1]),
                     fz = d2f(pz1 - S.dmin[2]);
-        d.pos32[i] = make_float4(fx, fy, fz, reach32(fx, fy, fz, d.rm32[i].z));
-        const bool moved = S.f_half_skin > 0.0f && left_skin(S, fx, fy, fz, d.xref[i]);
+        d.pos32[i] = make_float4(fx, fy, fz, reach32(fx, fy, fz, r32));
+        const bool moved = S.f_half_skin > 0.0f && left_skin(S, fx, fy, fz, xr);
         const unsigned am = __activemask();
         const unsigned peers = __match_any_sync(am, moved ? sc : -1);
         if (moved && lane_id() == (unsigned)(__ffs(peers) - 1) && d.sflags[nxt][sc] == 0u)
@@ -1663,7 +1673,6 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     d.vx[i] = vx + ax * dt;
     d.vy[i] = vy + ay * dt;
     d.vz[i] = vz + az * dt;
-    const double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
     const double dq0 = -0.5 * (qx * wx + qy * wy + qz * wz);
     const double dq1 = 0.5 * (qw * wx + qy * wz - qz * wy);
     const double dq2 = 0.5 * (qw * wy + qx * wz + qz * wx);
@@ -1674,7 +1683,6 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     d.qx[i] = nx * inq;
     d.qy[i] = ny * inq;
     d.qz[i] = nz * inq;
-    const double ii = d.inv_inertia[i];
     d.wx[i] = wx + M[0] * ii * dt;
     d.wy[i] = wy + M[1] * ii * dt;
     d.wz[i] = wz + M[2] * ii * dt;
