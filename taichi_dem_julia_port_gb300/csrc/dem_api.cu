@@ -413,6 +413,7 @@ int allocate(DemHandle* h) {
     TRY(dalloc(h, &d.bucket, n));
     TRY(dalloc(h, &d.cell_count, T));
     TRY(dalloc(h, &d.cell_start, T + 1));
+    TRY(dalloc(h, &d.tile_sums, (size_t)scan_tiles((int64_t)T) + 1));
     TRY(dalloc(h, &d.unsorted, n));
     TRY(dalloc(h, &d.sorted, n));
     TRY(dalloc(h, &d.spos, n));
@@ -551,8 +552,8 @@ int flag_search(DemHandle* h, int s) {
 
 void record_step(DemHandle* h, int cur) {
     const int nxt = cur ^ 1;
-    launch_broadphase(h->d, h->p, cur, h->multi, false, h->ntiles_cells, h->stream);
-    launch_detect(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
+    launch_search(h->d, h->p, cur, false, h->multi, false, h->shape, h->stream);
+    launch_lists(h->d, h->p, cur, false, h->multi, h->stream);
     launch_compact(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
     launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
     launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
@@ -1263,8 +1264,8 @@ int dem_init_bonds(DemHandle* h) {
     if (h->n_cap == 0) return DEM_OK;
     TRY(ensure_encoding(h));
     const int cur = h->cur, nxt = cur ^ 1;
-    launch_broadphase(h->d, h->p, cur, false, true, h->ntiles_cells, h->stream);
-    launch_detect(h->d, h->p, cur, true, false, h->shape, h->stream);
+    launch_search(h->d, h->p, cur, true, false, true, h->shape, h->stream);
+    launch_lists(h->d, h->p, cur, true, false, h->stream);
     launch_compact(h->d, h->p, cur, true, false, h->shape, h->stream);
     // the old buffer becomes the next step's target: its allocator starts at 0
     CU(cudaMemsetAsync(&h->d.ctr->row_alloc[cur], 0, sizeof(unsigned int), h->stream));
@@ -1317,9 +1318,9 @@ int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
     for (int k = 0; k < 6; ++k) CU(cudaEventCreate(&ev[k]));
     const int cur = h->cur, nxt = cur ^ 1;
     cudaEventRecord(ev[0], h->stream);
-    launch_broadphase(h->d, h->p, cur, h->multi, false, h->ntiles_cells, h->stream);
+    launch_search(h->d, h->p, cur, false, h->multi, false, h->shape, h->stream);
     cudaEventRecord(ev[1], h->stream);
-    launch_detect(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
+    launch_lists(h->d, h->p, cur, false, h->multi, h->stream);
     cudaEventRecord(ev[2], h->stream);
     launch_compact(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
     cudaEventRecord(ev[3], h->stream);

@@ -108,6 +108,8 @@ struct DevCounters {
     unsigned int pad;
     unsigned int row_alloc[2];      // contacts allocated in each contact buffer
     unsigned long long tickets[2];  // tile tickets of the scan sites (never reset)
+    unsigned int bar_count, bar_gen;  // grid barrier of the fused search (arrivals, generation)
+    unsigned int hashed[2];           // particles hashed by the step reading buffer cur
 };
 
 // scan sites: each has its own ticket counter and tile-state array
@@ -146,6 +148,7 @@ struct DemDev {
     uint32_t* bucket;      // bucket of each particle (kNoBucket when not hashed)
     uint32_t* cell_count;  // table entries, zero between steps
     uint32_t* cell_start;  // table entries + 1
+    uint32_t* tile_sums;   // bucket-count sums per scan tile (fused search)
     uint32_t* unsorted;    // bucket-grouped, arbitrary order inside a bucket
     uint32_t* sorted;      // bucket-grouped, ascending index inside a bucket
     double4_32a* spos;     // (x, y, z, r) in sorted order
@@ -204,8 +207,17 @@ struct LaunchShape {
 void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi, bool all,
                        int n_scan_tiles_cells, cudaStream_t s);
 
-void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+// The full pair search of the scenes that run it this step, fused into one
+// cooperative launch (hash, bucket scan, counting sort, canonical order,
+// cp_list enumeration with update_contacts! / init_bonds!); a step whose
+// scenes all test their neighbour lists ends it at once.  `all`: every
+// particle searches (bond initialisation).
+void launch_search(const DemDev& d, const DemParams& p, int cur, bool init, bool multi, bool all,
                    const LaunchShape& sh, cudaStream_t s);
+// update_contacts! from the neighbour lists (scenes that do not search) and
+// the placement of the next buffer's rows
+void launch_lists(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+                  cudaStream_t s);
 void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
                     const LaunchShape& sh, cudaStream_t s);
 void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, const LaunchShape& sh,

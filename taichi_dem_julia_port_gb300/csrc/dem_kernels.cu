@@ -1,22 +1,29 @@
 // dem_kernels.cu — the DEM step as hand-written CUDA for sm_103a.
 //
 // One step (the reference's `simulate!`, src/executor.jl:162-172) is
-//   k_hash       cell, Morton bucket, octant; warp-aggregated bucket counts
-//   k_scan       exclusive scan of the occupied bucket range (single pass,
-//                decoupled look-back)                          -> bucket starts
-//   k_scatter    counting-sort scatter (warp-aggregated atomics; the counts
-//                return to zero, so the table needs no clearing)
-//   k_canon      ascending index inside each bucket + bucket-sorted copies of
-//                the positions (FP64 and an FP32 copy for the pre-filter)
-//   k_detect     cp_list enumeration fused with update_contacts!: existing
-//                contacts decide survival, new touching pairs are stashed,
-//                each particle's new row is allocated (block-aggregated atomic)
+//   k_search     the full pair search, one cooperative launch whose phases
+//                are separated by grid barriers (and which ends at once when
+//                no scene searches this step):
+//                  hash     cell, Morton bucket, octant; warp-aggregated counts
+//                  scan     exclusive scan of the occupied bucket range
+//                  scatter  counting-sort scatter (the counts return to zero,
+//                           so the table needs no clearing)
+//                  canon    ascending index inside each bucket + bucket-sorted
+//                           copies of the positions (FP64 and FP32)
+//                  detect   cp_list enumeration fused with update_contacts!:
+//                           existing contacts decide survival, new touching
+//                           pairs are stashed, neighbour lists are rebuilt
+//   k_vdetect    update_contacts! from the neighbour lists (scenes that do
+//                not search this step)
+//   k_rows       placement of each particle's next row (warp-aggregated atomics)
 //   k_compact    rolling-array rebuild: surviving + new contacts, rows sorted
 //                by j; incoming-contact lists for the force gather
 //   k_force      resolve_collision! per contact (EBPM or Hertz-Mindlin)
 //   k_integrate  per particle: contact force gather in a fixed order,
 //                resolve_wall!, apply_body_force!, update!
-// All of it is captured once in a CUDA graph per contact-buffer parity.
+// All of it is captured once in a CUDA graph per contact-buffer parity.  The
+// standalone broad-phase kernels (k_hash, k_scan_excl, k_scatter, k_canon)
+// serve the cp_list inspection entry point.
 #include <type_traits>
 
 #include "dem_device.cuh"
@@ -180,22 +187,9 @@ __device__ __forceinline__ int32_t cell_index(double num, double cell, double in
     if (lo == hi && lo > -2147483648.0 && lo < 2147483647.0) return (int32_t)lo;
     return ceil_i32(__ddiv_rn(num, cell));
 }
-// cell ijk (1-based) and octant bits of a position for a given cell size
-// (`cell` and the center comparison of `neighbors`, src/utils.jl:1-16)
-__device__ __forceinline__ int4 cell_of(const double pos[3], const double dmin[3], double cell,
-                                        double inv_cell) {
-    int ijk[3];
-    int oct = 0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        ijk[c] = cell_index(__dsub_rn(pos[c], dmin[c]), cell, inv_cell);
-        const double ctr = __dadd_rn(dmin[c], __dmul_rn(__dsub_rn((double)ijk[c], 0.5), cell));
-        if (pos[c] > ctr) oct |= 1 << c;
-    }
-    return make_int4(ijk[0], ijk[1], ijk[2], oct);
-}
-
-// cell_of with an FP32 screen.  num = pos - dmin is formed exactly as the
+// Cell ijk (1-based) and octant bits of a position for a given cell size
+// (`cell` and the center comparison of `neighbors`, src/utils.jl:1-16), with
+// an FP32 screen.  num = pos - dmin is formed exactly as the
 // reference forms it; q' = fl32(num)·fl32(1/cell) lies within 4·2^-24·|q| of
 // the exact quotient q = num/cell, and the reference's center
 // dmin + (ijk - 1/2)·cell within 2^-51·(|dmin|/cell + |q| + 1) of its exact
@@ -230,53 +224,66 @@ __device__ __forceinline__ int4 cell_of_screened(const double pos[3], const doub
 // `cell`, `hashcode`, `center`, `neighbors` (src/utils.jl:1-16) and
 // `count_particles!` (src/kernels.jl:7-13).
 template <bool MULTI>
-__global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p, int cur, int all) {
-    dep_begin(p.dep == 2);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool act = i < p.n;
-    uint32_t b = 0;
-    if (act) {
-        const int sc = slot_scene<MULTI>(d, i);
-        const int mode = MULTI ? (sc < 0 ? kModeFree : d.sp[sc].mode) : kModeStep;
-        if (mode == kModeFree) {
-            // free slot: not hashed, and no contact row in the next buffer
-            d.bucket[i] = kNoBucket;
-            d.row_len[cur ^ 1][i] = 0;
-            d.row_start[cur ^ 1][i] = 0;
-            d.path[i] = 0;  // kind 0 (free), mode Free
-            act = false;
-        } else if (!full_search(d, cur, sc, mode, all)) {
-            d.bucket[i] = kNoBucket;  // this scene tests its neighbour lists
-            d.path[i] = (uint8_t)(2 | (mode << 2));  // kind 2 (list)
-            act = false;
-        } else {
-            d.path[i] = (uint8_t)(1 | (mode << 2));  // kind 1 (full search)
-            const SceneParams& S = scene_rec<MULTI>(d, p, sc);
-            const double pos[3] = {d.px[i], d.py[i], d.pz[i]};
-            int4 ci = cell_of_screened(pos, S.dmin, S.cell, S.inv_cell, S.f_inv_cell, S.f_dmin_cells);
-            b = bucket_of(ci.x, ci.y, ci.z, S);
-            if (MULTI) ci.w |= sc << 3;
-            d.cellinfo[i] = ci;
-            d.bucket[i] = b;
-            if (MULTI && !S.same_grid)
-                d.refcell[i] = cell_of_screened(pos, S.dmin, S.cell_ref, S.inv_cell_ref,
-                                                S.f_inv_cell_ref, S.f_dmin_cells_ref);
-        }
+__device__ __forceinline__ void hash_particle(const DemDev& d, const DemParams& p, int cur, int all,
+                                              int i, bool& act, uint32_t& b) {
+    act = true;
+    b = 0;
+    const int sc = slot_scene<MULTI>(d, i);
+    const int mode = MULTI ? (sc < 0 ? kModeFree : d.sp[sc].mode) : kModeStep;
+    if (mode == kModeFree) {
+        // free slot: not hashed, and no contact row in the next buffer
+        d.bucket[i] = kNoBucket;
+        d.row_len[cur ^ 1][i] = 0;
+        d.row_start[cur ^ 1][i] = 0;
+        d.path[i] = 0;  // kind 0 (free), mode Free
+        act = false;
+    } else if (!full_search(d, cur, sc, mode, all)) {
+        d.bucket[i] = kNoBucket;  // this scene tests its neighbour lists
+        d.path[i] = (uint8_t)(2 | (mode << 2));  // kind 2 (list)
+        act = false;
+    } else {
+        d.path[i] = (uint8_t)(1 | (mode << 2));  // kind 1 (full search)
+        const SceneParams& S = scene_rec<MULTI>(d, p, sc);
+        const double pos[3] = {d.px[i], d.py[i], d.pz[i]};
+        int4 ci = cell_of_screened(pos, S.dmin, S.cell, S.inv_cell, S.f_inv_cell, S.f_dmin_cells);
+        b = bucket_of(ci.x, ci.y, ci.z, S);
+        if (MULTI) ci.w |= sc << 3;
+        d.cellinfo[i] = ci;
+        d.bucket[i] = b;
+        if (MULTI && !S.same_grid)
+            d.refcell[i] = cell_of_screened(pos, S.dmin, S.cell_ref, S.inv_cell_ref,
+                                            S.f_inv_cell_ref, S.f_dmin_cells_ref);
     }
+}
+// Bucket counts and the bucket maximum of a warp's hashed particles (every
+// lane of the warp calls this); `hashed` (may be null) counts them.
+__device__ __forceinline__ void hash_count(const DemDev& d, bool act, uint32_t b,
+                                           unsigned int* hashed) {
     const unsigned mask = __ballot_sync(0xffffffffu, act);
     if (act) {
         const unsigned peers = __match_any_sync(mask, b);
         if (lane_id() == (unsigned)(__ffs(peers) - 1)) atomicAdd(&d.cell_count[b], __popc(peers));
         const unsigned wmax = __reduce_max_sync(mask, b);
-        if (lane_id() == (unsigned)(__ffs(mask) - 1)) atomicMax(&d.ctr->bmax, wmax);
+        if (lane_id() == (unsigned)(__ffs(mask) - 1)) {
+            atomicMax(&d.ctr->bmax, wmax);
+            if (hashed) atomicAdd(hashed, __popc(mask));
+        }
     }
+}
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_hash(DemDev d, DemParams p, int cur, int all) {
+    dep_begin(p.dep == 2);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool act = false;
+    uint32_t b = 0;
+    if (i < p.n) hash_particle<MULTI>(d, p, cur, all, i, act, b);
+    hash_count(d, act, b, nullptr);
 }
 
 // `get_particle_id!` (src/kernels.jl:15-22): counting-sort scatter.  The
 // atomic decrements bring every count back to zero.
-__global__ void __launch_bounds__(kThreads) k_scatter(DemDev d, DemParams p) {
-    dep_begin(p.dep == 2);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// (every lane of the warp calls scatter_warp; i >= n is inactive)
+__device__ __forceinline__ void scatter_warp(const DemDev& d, const DemParams& p, int i) {
     const uint32_t b = i < p.n ? d.bucket[i] : kNoBucket;
     const bool act = b != kNoBucket;
     const unsigned mask = __ballot_sync(0xffffffffu, act);
@@ -289,6 +296,10 @@ __global__ void __launch_bounds__(kThreads) k_scatter(DemDev d, DemParams p) {
     const uint32_t slot = old - 1u - (uint32_t)__popc(peers & lanemask_lt());
     d.unsorted[d.cell_start[b] + slot] = (uint32_t)i;
 }
+__global__ void __launch_bounds__(kThreads) k_scatter(DemDev d, DemParams p) {
+    dep_begin(p.dep == 2);
+    scatter_warp(d, p, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // Canonical order inside a bucket (ascending particle index) and the sorted
 // copies the pair search reads at its own index (positions, the cell record,
@@ -296,11 +307,7 @@ __global__ void __launch_bounds__(kThreads) k_scatter(DemDev d, DemParams p) {
 // index.  Also clears this step's bucket maximum (all its readers have
 // finished).
 template <bool MULTI>
-__global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p, int cur) {
-    dep_begin(p.dep == 2);
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k == 0) d.ctr->bmax = 0u;
-    if (k >= sorted_count(d)) return;
+__device__ __forceinline__ void canon_slot(const DemDev& d, const DemParams& p, int cur, int k) {
     const uint32_t i = d.unsorted[k];
     const uint32_t b = d.bucket[i];
     const uint32_t s = d.cell_start[b], e = d.cell_start[b + 1];
@@ -315,6 +322,14 @@ __global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p, int c
     d.spos32[pos] = make_float4(fx, fy, fz, reach32(fx, fy, fz, d2f(r)));
     d.scell[pos] = d.cellinfo[i];
     d.srow[pos] = make_int2(d.row_start[cur][i], d.row_len[cur][i]);
+}
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_canon(DemDev d, DemParams p, int cur) {
+    dep_begin(p.dep == 2);
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) d.ctr->bmax = 0u;
+    if (k >= sorted_count(d)) return;
+    canon_slot<MULTI>(d, p, cur, k);
 }
 
 // ---------------------------------------------------------------------------
@@ -352,10 +367,12 @@ struct DetectShared {
     int2 seg[kLanes];         // (first sorted slot, prefix) per bucket
 };
 
-// The full pair search for the particle at sorted position k (one 8-lane group).
+// The full pair search for the particle at sorted position k (one 8-lane group);
+// lim = the buckets with valid starts this step.
 template <bool INIT, bool MULTI>
 __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p, int cur, int k,
-                                             int lane, unsigned gmask, DetectShared& sh) {
+                                             int lane, unsigned gmask, uint32_t lim,
+                                             DetectShared& sh) {
     const int nxt = cur ^ 1;
     if (lane == 0) {
         sh.nnew = 0;
@@ -389,7 +406,7 @@ __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p
         dup |= (u < lane) && (bu == myB);
     }
     uint32_t s, e;
-    bucket_range(d, myB, d.ctr->cell_limit, &s, &e);
+    bucket_range(d, myB, lim, &s, &e);
     if (dup || frozen) e = s;
     // a bucket lists its particles by ascending index: keep those above i
     // (cp_list holds the pairs i < j)
@@ -544,17 +561,147 @@ __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p
     }
 }
 
+// ---------------------------------------------------------------------------
+// The full pair search fused into one cooperative launch.  Its phases are the
+// broad phase kernels above (hash, bucket scan, counting sort, canonical
+// order) and the cp_list enumeration, separated by grid barriers; every block
+// of a cooperative launch is resident, so the barriers cannot wait on a block
+// that has not started.  A step in which no scene searches ends at the first
+// check: a single-scene handle reads its one flag; an arena hashes (which also
+// records each slot's path) and ends when nothing was hashed.
+
+// Grid barrier: arrival counter and generation word; a block waits for the
+// generation to move on, with a bounded wait that raises kErrTimeout.
+__device__ __forceinline__ void grid_sync(DevCounters* c) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* gen = &c->bar_gen;
+        const unsigned int g = *gen;
+        __threadfence();
+        if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1) {
+            atomicExch(&c->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&c->bar_gen, 1u);
+        } else {
+            for (unsigned long long it = 0; *gen == g; ++it) {
+                if (it > kSpinLimit) {
+                    raise_error(c, kErrTimeout);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// Block-wide sum of one value per thread (kThreads threads).
+__device__ __forceinline__ unsigned long long block_sum(unsigned long long v,
+                                                        unsigned long long* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane_id() == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    unsigned long long t = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+    __syncthreads();
+    return t;
+}
+
+// Exclusive scan of cell_count[0, count) into cell_start (count = the
+// buckets up to this step's largest, as the standalone scan), in tiles of
+// kScanTile: tile sums, a barrier, then each tile's prefix from the sums.
+// Ends with a barrier.
+constexpr int kFusedItems = kScanTile / kThreads;
+__device__ void scan_phase(const DemDev& d, const DemParams& p, unsigned long long* red) {
+    // (values written by other blocks earlier in this launch are read past L1)
+    const long long lim = (long long)__ldcg(&d.ctr->bmax) + 1;
+    const long long count = lim < (long long)p.T ? lim : (long long)p.T;
+    const int ntiles = (int)((count + kScanTile - 1) / kScanTile);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const long long base = (long long)t * kScanTile + (long long)threadIdx.x * kFusedItems;
+        unsigned long long v = 0;
+#pragma unroll 8
+        for (int k = 0; k < kFusedItems; ++k)
+            if (base + k < count) v += d.cell_count[base + k];
+        const unsigned long long tot = block_sum(v, red);
+        if (threadIdx.x == 0) d.tile_sums[t] = (uint32_t)tot;
+    }
+    grid_sync(d.ctr);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        unsigned long long pre = 0;
+        for (int u = threadIdx.x; u < t; u += kThreads) pre += __ldcg(&d.tile_sums[u]);
+        pre = block_sum(pre, red);
+        const long long base = (long long)t * kScanTile + (long long)threadIdx.x * kFusedItems;
+        unsigned long long mine = 0;
+#pragma unroll 8
+        for (int k = 0; k < kFusedItems; ++k)
+            if (base + k < count) mine += d.cell_count[base + k];
+        // exclusive prefix of `mine` across the block
+        unsigned long long x = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane_id() >= (unsigned)o) x += y;
+        }
+        if (lane_id() == 31) red[threadIdx.x >> 5] = x;
+        __syncthreads();
+        unsigned long long wpre = 0;
+        for (int w = 0; w < (int)(threadIdx.x >> 5); ++w) wpre += red[w];
+        __syncthreads();
+        unsigned long long run = pre + wpre + x - mine;
+#pragma unroll 8
+        for (int k = 0; k < kFusedItems; ++k) {
+            if (base + k < count) {
+                d.cell_start[base + k] = (uint32_t)run;
+                run += d.cell_count[base + k];
+            }
+        }
+        if (t == ntiles - 1 && threadIdx.x == kThreads - 1) d.cell_start[count] = (uint32_t)run;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.ctr->cell_limit = (unsigned int)count;
+    grid_sync(d.ctr);
+}
+
 template <bool INIT, bool MULTI, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB) k_detect(DemDev d, DemParams p, int cur) {
+__global__ void __launch_bounds__(kThreads, MINB) k_search(DemDev d, DemParams p, int cur, int all) {
     __shared__ DetectShared sh[kThreads / kLanes];
-    dep_begin(p.dep == 2);
+    __shared__ unsigned long long red[kThreads / 32];
+    dep_begin();
+    if (!MULTI && !(all || INIT || d.sflags[cur][0] != 0u)) return;
+    const int stride = gridDim.x * kThreads;
+    const int wbase = blockIdx.x * kThreads + (int)(threadIdx.x & ~31u);
+    if (MULTI && blockIdx.x == 0 && threadIdx.x == 0) d.ctr->hashed[cur ^ 1] = 0u;
+    // hash (`cell`, `hashcode`, `neighbors`, `count_particles!`)
+    for (int i0 = wbase; i0 < p.n; i0 += stride) {
+        const int i = i0 + (int)lane_id();
+        bool act = false;
+        uint32_t b = 0;
+        if (i < p.n) hash_particle<MULTI>(d, p, cur, all, i, act, b);
+        hash_count(d, act, b, MULTI ? &d.ctr->hashed[cur] : nullptr);
+    }
+    grid_sync(d.ctr);
+    if (MULTI && *(volatile unsigned int*)&d.ctr->hashed[cur] == 0u) return;
+    // `accumulate!` of the bucket counts
+    scan_phase(d, p, red);
+    // `get_particle_id!`
+    for (int i0 = wbase; i0 < p.n; i0 += stride) scatter_warp(d, p, i0 + (int)lane_id());
+    grid_sync(d.ctr);
+    // canonical order; this step's bucket maximum is no longer read
+    const uint32_t lim = __ldcg(&d.ctr->cell_limit);
+    const int count = (int)__ldcg(&d.cell_start[lim]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.ctr->bmax = 0u;
+    for (int k = blockIdx.x * kThreads + (int)threadIdx.x; k < count; k += stride)
+        canon_slot<MULTI>(d, p, cur, k);
+    grid_sync(d.ctr);
+    // cp_list enumeration with update_contacts! / init_bonds!
     const int lane = threadIdx.x & (kLanes - 1);
     const int g = threadIdx.x / kLanes;
     const unsigned gmask = 0xffu << (lane_id() & ~7u);
-    const int count = sorted_count(d);
-    // grid-stride over sorted positions; whole 8-lane groups move together
     for (int k = blockIdx.x * (kThreads / kLanes) + g; k < count; k += gridDim.x * (kThreads / kLanes)) {
-        detect_group<INIT, MULTI>(d, p, cur, k, lane, gmask, sh[g]);
+        detect_group<INIT, MULTI>(d, p, cur, k, lane, gmask, lim, sh[g]);
         __syncwarp(gmask);
     }
 }
@@ -1813,28 +1960,57 @@ void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi,
     launch(dep, multi ? k_canon<true> : k_canon<false>, nb, kThreads, s, d, p, cur);
 }
 
+// Largest cooperative grid of one k_search instantiation (resident blocks per
+// SM from the occupancy calculator, times the SMs).
+template <bool INIT, bool MULTI, int MINB>
+int search_grid_limit(int sms) {
+    static int per_sm = -1;
+    if (per_sm < 0) {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_search<INIT, MULTI, MINB>, kThreads,
+                                                          0) != cudaSuccess)
+            nb = 1;
+        per_sm = nb > 0 ? nb : 1;
+    }
+    return per_sm * sms;
+}
+
+template <bool INIT, bool MULTI, int MINB>
+void launch_search_t(const DemDev& d, const DemParams& p, int cur, bool all, cudaStream_t s) {
+    // one 8-lane group per particle, within the resident limit
+    const int want = max(1, blocks_for((long long)p.n * kLanes, kThreads));
+    const int grid = max(1, min(want, search_grid_limit<INIT, MULTI, MINB>(p.sms)));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)kThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_search<INIT, MULTI, MINB>, d, p, cur, all ? 1 : 0);
+}
+
 template <int MINB>
-void launch_detect_b(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+void launch_search_b(const DemDev& d, const DemParams& p, int cur, bool init, bool multi, bool all,
                      cudaStream_t s) {
-    // grid-stride: one wave of resident blocks at most
-    const int nb = max(1, min(blocks_for((long long)p.n * kLanes, kThreads), p.sms * MINB));
-    launch(p.dep != 0,
-           multi ? k_detect<false, true, MINB>
-                 : (init ? k_detect<true, false, MINB> : k_detect<false, false, MINB>),
-           nb, kThreads, s, d, p, cur);
+    if (multi) launch_search_t<false, true, MINB>(d, p, cur, all, s);
+    else if (init) launch_search_t<true, false, MINB>(d, p, cur, all, s);
+    else launch_search_t<false, false, MINB>(d, p, cur, all, s);
 }
 
-void launch_detect_full(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
-                        const LaunchShape& sh, cudaStream_t s) {
-    if (p.n == 0) return;
-    if (sh.detect_blocks_per_sm == 3) launch_detect_b<3>(d, p, cur, init, multi, s);
-    else launch_detect_b<4>(d, p, cur, init, multi, s);
-}
-
-void launch_detect(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+void launch_search(const DemDev& d, const DemParams& p, int cur, bool init, bool multi, bool all,
                    const LaunchShape& sh, cudaStream_t s) {
     if (p.n == 0) return;
-    launch_detect_full(d, p, cur, init, multi, sh, s);
+    if (sh.detect_blocks_per_sm == 3) launch_search_b<3>(d, p, cur, init, multi, all, s);
+    else launch_search_b<4>(d, p, cur, init, multi, all, s);
+}
+
+void launch_lists(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+                  cudaStream_t s) {
+    if (p.n == 0) return;
     if (!init) {  // the scenes that test their neighbour lists
         const int nv = max(1, min(blocks_for((long long)p.n * kVLanes, kThreads), p.sms * 8));
         launch(p.dep != 0, multi ? k_vdetect<true> : k_vdetect<false>, nv, kThreads, s, d, p,
