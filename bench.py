@@ -69,10 +69,11 @@ COMPACT_BYTES_HERTZ = 24 + 48 + 8
 BROADPHASE_BYTES_PER_PARTICLE = 24 + 16 + 4 + 4 + 4 + 8 + 24 + 8 + 32 + 16  # hash..canon
 INTEGRATE_BYTES_PER_PARTICLE = 13 * 8 * 2 + 4 * 8 + 6 * 8 + 3 * 8 * 2 + 8 + 4  # state r/w
 # neighbour-list step per particle: path byte, current row bounds, list length,
-# FP32 position, row length written, 4 list partners (index + FP32 position)
+# FP32 position, next row bounds written, 4 list partners (index + FP32
+# position); the row rebuild adds the compaction bytes per surviving contact
 DETECT_BYTES_PER_PARTICLE = 1 + 8 + 4 + 16 + 8 + 4 * (4 + 16)
-# hash, scan, scatter, canon, detect, list detect, rows, compact, force, integrate
-KERNELS_PER_STEP = 10
+# k_search (fused full search), k_vdetect (lists + rows), k_force, k_integrate
+KERNELS_PER_STEP = 4
 L2_FLUSH_BYTES = 256 << 20
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
@@ -84,8 +85,6 @@ NCU_TRAFFIC = {
     ("c2", "force"): (6.419456e6, 17576),          # k_force<double>
     ("c4", "force"): (145.409024e6, 431416),       # k_force<float>
     ("c4", "integrate"): (186.321408e6, 431416),   # k_integrate (FP32 gather)
-    ("c4", "compact"): (113.883648e6, 431416),     # k_compact
-    ("c4", "detect"): (33.391104e6, 431416),       # k_vdetect (list steps)
 }
 
 
@@ -250,10 +249,10 @@ def run_batched(args, lib, quick: bool = False) -> dict:
     plain = n_total / (plain_ms * 1e-3) if plain_ms > 0 else None
     peaks = load_peaks()
     force_bytes = bonded * FORCE_BYTES_BOND + (contacts - bonded) * FORCE_BYTES_HERTZ
-    alg = {"force": force_bytes, "broadphase": n_total * BROADPHASE_BYTES_PER_PARTICLE,
+    alg = {"force": force_bytes, "search": n_total * BROADPHASE_BYTES_PER_PARTICLE,
            "integrate": n_total * INTEGRATE_BYTES_PER_PARTICLE,
-           "detect": n_total * DETECT_BYTES_PER_PARTICLE,
-           "compact": bonded * COMPACT_BYTES_BOND + (contacts - bonded) * COMPACT_BYTES_HERTZ}
+           "lists": n_total * DETECT_BYTES_PER_PARTICLE
+           + bonded * COMPACT_BYTES_BOND + (contacts - bonded) * COMPACT_BYTES_HERTZ}
     dom = max(ph, key=ph.get)
     roof = {"bound": "hbm", "kernel": dom, "unit": "GB/s", "peak": peaks["hbm_gbs"],
             "peak_source": peaks["source"], "traffic": ncu_traffic("c4", dom, n_total),
@@ -577,10 +576,10 @@ def main() -> None:
     n_bond = st["bonded"]
     force_bytes = n_bond * FORCE_BYTES_BOND + (c_now - n_bond) * FORCE_BYTES_HERTZ
     alg = {"force": force_bytes,
-           "broadphase": sc.n * BROADPHASE_BYTES_PER_PARTICLE,
+           "search": sc.n * BROADPHASE_BYTES_PER_PARTICLE,
            "integrate": sc.n * INTEGRATE_BYTES_PER_PARTICLE,
-           "detect": sc.n * DETECT_BYTES_PER_PARTICLE,
-           "compact": n_bond * COMPACT_BYTES_BOND + (c_now - n_bond) * COMPACT_BYTES_HERTZ}
+           "lists": sc.n * DETECT_BYTES_PER_PARTICLE
+           + n_bond * COMPACT_BYTES_BOND + (c_now - n_bond) * COMPACT_BYTES_HERTZ}
     dom = max(ph, key=ph.get)
     dom_bytes = alg.get(dom)
     peaks = load_peaks()

@@ -197,9 +197,11 @@ int dem_step(DemHandle* h, int64_t nsteps);
 int dem_step_timed(DemHandle* h, int64_t nsteps, float* ms);
 
 /* One step launched phase by phase (no graph) with CUDA events between the
- * phases on the handle's stream.  phase_ms[0..4] receive the device time of:
- * broad phase (hash, bucket scan, scatter, canonical order), contact
- * detection (with row allocation), contact compaction, contact forces,
+ * phases on the handle's stream.  phase_ms[0..3] (nphase >= 4; further
+ * entries are set to 0) receive the device time of: the full pair search
+ * (hash, bucket scan, scatter, canonical order, cp_list enumeration with
+ * update_contacts!, next rows; it ends at once when no scene searches), the
+ * neighbour-list contact update (with next rows), contact forces,
  * integration.
  * No counterpart in the reference: per-kernel timing for roofline reports. */
 int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase);
@@ -211,17 +213,19 @@ int dem_sync(DemHandle* h);
  * DEM_FP32_FORCE.  No counterpart in the reference, which is FP64 only. */
 int dem_set_precision(DemHandle* h, int mode);
 
-/* Launch shape of the grid-stride kernels (contact compaction, contact
- * forces, integration): block sizes (multiples of 32, at most 256) and grid
- * upper bounds.  Results are the same for every shape; the shape only changes
- * speed (the autotuner's knob).  No counterpart in the reference. */
+/* Launch shape of the grid-stride kernels (contact forces, integration):
+ * block sizes (multiples of 32, at most 256) and grid upper bounds.  Results
+ * are the same for every shape; the shape only changes speed (the
+ * autotuner's knob).  No counterpart in the reference. */
 typedef struct DemLaunchShape {
     int32_t force_block;
     int32_t force_grid;
-    int32_t compact_block;
-    int32_t compact_grid;
+    int32_t compact_block;        /* kept for layout; no effect (rows are rebuilt
+                                   * where contacts are decided)                    */
+    int32_t compact_grid;         /* kept for layout; no effect                     */
     int32_t integrate_block;
-    int32_t detect_blocks_per_sm; /* register budget of the pair search: 3 or 4 (0 = 4) */
+    int32_t detect_blocks_per_sm; /* register budget of the pair search and the
+                                   * neighbour-list update: 3 or 4 (0 = 4)          */
     int32_t force_blocks_per_sm;  /* FP32 force kernel: 0 (compiler's choice) or 4     */
     int32_t dependent_launch;     /* a step's kernels: 0 ordinary launches; 1
                                    * programmatic dependent launches (each may be

@@ -153,10 +153,10 @@ class Arena:
 
     def step_profiled(self) -> dict:
         """One step launched phase by phase; device milliseconds per phase."""
-        ms = (C.c_float * 5)()
-        check(self.lib, self.lib.dem_step_profiled(self.h, ms, 5), "dem_step_profiled")
-        return dict(zip(("broadphase", "detect", "compact", "force", "integrate"),
-                        [float(x) for x in ms]))
+        from .executor import GlobalData
+        ms = (C.c_float * len(GlobalData.PHASES))()
+        check(self.lib, self.lib.dem_step_profiled(self.h, ms, len(ms)), "dem_step_profiled")
+        return dict(zip(GlobalData.PHASES, [float(x) for x in ms]))
 
     def sync(self) -> None:
         check(self.lib, self.lib.dem_sync(self.h), "dem_sync")

@@ -1,7 +1,7 @@
 """Autotuner for a stepping handle (an `Arena` or a `GlobalData`).
 
 Picks the search-cell factor (arenas) and the launch shape of the grid-stride
-kernels (contact compaction, contact forces, integration) by timing real steps
+kernels (contact forces, integration) by timing real steps
 on the live workload with CUDA events.  None of these knobs changes a result:
 the search grid only changes which buckets the pair search visits (contact
 ends follow the reference's cells), and every kernel computes the same values
@@ -9,7 +9,7 @@ for any launch shape; the arena tests check both bit for bit.  The steps taken
 while tuning are ordinary simulation steps.
 
 The search is coordinate descent: cell factor first, then the force kernel's
-block and grid, then the compaction grid, the integration block, the FP32
+block and grid, then the integration block, the FP32
 force kernel's register budget, the launch mode (ordinary or programmatic
 dependent launches) and the pair search's register budget; each
 candidate is timed over `steps` steps after one untimed step.
@@ -74,13 +74,6 @@ def autotune(target, sm_count: int = 152, steps: int = 10, cell_factors=CELL_FAC
             trials.append((cand, t))
             if t < best:
                 best, shape = t, cand
-    for g in grids_per_sm:
-        cand = dict(shape, compact_grid=g * sm_count)
-        target.set_launch_shape(**cand)
-        t = _time(target, steps)
-        trials.append((cand, t))
-        if t < best:
-            best, shape = t, cand
     for ib in integrate_blocks:
         cand = dict(shape, integrate_block=ib)
         target.set_launch_shape(**cand)

@@ -426,7 +426,6 @@ int allocate(DemHandle* h) {
         TRY(dalloc(h, &d.row_start[b], n));
         TRY(dalloc(h, &d.row_len[b], n));
     }
-    TRY(dalloc(h, &d.nnew, n));
     TRY(dalloc(h, &d.stash, n * (size_t)h->p.kstash));
     TRY(dalloc(h, &d.keep, cap));
     TRY(dalloc(h, &d.in_cnt, n));
@@ -553,8 +552,7 @@ int flag_search(DemHandle* h, int s) {
 void record_step(DemHandle* h, int cur) {
     const int nxt = cur ^ 1;
     launch_search(h->d, h->p, cur, false, h->multi, false, h->shape, h->stream);
-    launch_lists(h->d, h->p, cur, false, h->multi, h->stream);
-    launch_compact(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
+    launch_lists(h->d, h->p, cur, h->multi, h->shape, h->stream);
     launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
     launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
 }
@@ -1265,8 +1263,6 @@ int dem_init_bonds(DemHandle* h) {
     TRY(ensure_encoding(h));
     const int cur = h->cur, nxt = cur ^ 1;
     launch_search(h->d, h->p, cur, true, false, true, h->shape, h->stream);
-    launch_lists(h->d, h->p, cur, true, false, h->stream);
-    launch_compact(h->d, h->p, cur, true, false, h->shape, h->stream);
     // the old buffer becomes the next step's target: its allocator starts at 0
     CU(cudaMemsetAsync(&h->d.ctr->row_alloc[cur], 0, sizeof(unsigned int), h->stream));
     CU(cudaGetLastError());
@@ -1304,34 +1300,30 @@ int dem_step_timed(DemHandle* h, int64_t nsteps, float* ms) {
 }
 
 int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
-    if (!h || !phase_ms || nphase < 5) return DEM_ERR_INVALID;
-    if (h->n_cap == 0) {
-        for (int k = 0; k < 5; ++k) phase_ms[k] = 0.f;
-        return DEM_OK;
-    }
+    if (!h || !phase_ms || nphase < 4) return DEM_ERR_INVALID;
+    for (int k = 0; k < nphase; ++k) phase_ms[k] = 0.f;
+    if (h->n_cap == 0) return DEM_OK;
     TRY(ensure_encoding(h));
     if (h->multi) {
         TRY(build_graphs(h));
         TRY(launch_inits(h));
     }
-    cudaEvent_t ev[6];
-    for (int k = 0; k < 6; ++k) CU(cudaEventCreate(&ev[k]));
+    cudaEvent_t ev[5];
+    for (int k = 0; k < 5; ++k) CU(cudaEventCreate(&ev[k]));
     const int cur = h->cur, nxt = cur ^ 1;
     cudaEventRecord(ev[0], h->stream);
     launch_search(h->d, h->p, cur, false, h->multi, false, h->shape, h->stream);
     cudaEventRecord(ev[1], h->stream);
-    launch_lists(h->d, h->p, cur, false, h->multi, h->stream);
+    launch_lists(h->d, h->p, cur, h->multi, h->shape, h->stream);
     cudaEventRecord(ev[2], h->stream);
-    launch_compact(h->d, h->p, cur, false, h->multi, h->shape, h->stream);
-    cudaEventRecord(ev[3], h->stream);
     launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
-    cudaEventRecord(ev[4], h->stream);
+    cudaEventRecord(ev[3], h->stream);
     launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
-    cudaEventRecord(ev[5], h->stream);
-    cudaError_t e = cudaEventSynchronize(ev[5]);
-    for (int k = 0; k < 5 && e == cudaSuccess; ++k)
+    cudaEventRecord(ev[4], h->stream);
+    cudaError_t e = cudaEventSynchronize(ev[4]);
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
         e = cudaEventElapsedTime(&phase_ms[k], ev[k], ev[k + 1]);
-    for (int k = 0; k < 6; ++k) cudaEventDestroy(ev[k]);
+    for (int k = 0; k < 5; ++k) cudaEventDestroy(ev[k]);
     CU(e);
     h->cur = nxt;
     h->steps += 1;

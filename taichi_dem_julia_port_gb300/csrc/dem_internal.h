@@ -157,7 +157,6 @@ struct DemDev {
     ContactSoA c[2];
     int32_t* row_start[2];  // first slot of each particle's row
     int32_t* row_len[2];    // entries in the row
-    int32_t* nnew;
     int32_t* stash;       // n * kstash new partners of this step
     uint8_t* keep;        // cap, survival flags of the current buffer
     int32_t* in_cnt;      // zero between steps
@@ -194,7 +193,8 @@ struct LaunchShape {
     int force_block, force_grid;
     int compact_block, compact_grid;
     int integrate_block;
-    int detect_blocks_per_sm;  // register budget of the pair search: 3 or 4 blocks per SM
+    int detect_blocks_per_sm;  // register budget of the pair search and the list update:
+                               // 3 or 4 blocks per SM
     int force_blocks_per_sm;   // register budget of the FP32 force kernel: 0 (none) or 4
     int dependent_launch;      // 0 ordinary, 1 programmatic dependent, 2 with early trigger
 };
@@ -214,12 +214,10 @@ void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi,
 // particle searches (bond initialisation).
 void launch_search(const DemDev& d, const DemParams& p, int cur, bool init, bool multi, bool all,
                    const LaunchShape& sh, cudaStream_t s);
-// update_contacts! from the neighbour lists (scenes that do not search) and
-// the placement of the next buffer's rows
-void launch_lists(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+// update_contacts! from the neighbour lists (scenes that do not search this
+// step), with their next rows
+void launch_lists(const DemDev& d, const DemParams& p, int cur, bool multi, const LaunchShape& sh,
                   cudaStream_t s);
-void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
-                    const LaunchShape& sh, cudaStream_t s);
 void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, const LaunchShape& sh,
                   cudaStream_t s);
 void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,

@@ -12,12 +12,13 @@
 //                           copies of the positions (FP64 and FP32)
 //                  detect   cp_list enumeration fused with update_contacts!:
 //                           existing contacts decide survival, new touching
-//                           pairs are stashed, neighbour lists are rebuilt
+//                           pairs are found, neighbour lists are rebuilt
 //   k_vdetect    update_contacts! from the neighbour lists (scenes that do
 //                not search this step)
-//   k_rows       placement of each particle's next row (warp-aggregated atomics)
-//   k_compact    rolling-array rebuild: surviving + new contacts, rows sorted
-//                by j; incoming-contact lists for the force gather
+//                Both write each particle's next row where its contacts are
+//                decided (the rolling-array rebuild: survivors + new contacts
+//                sorted by j, placed by warp-aggregated atomics) and the
+//                incoming-contact lists for the force gather.
 //   k_force      resolve_collision! per contact (EBPM or Hertz-Mindlin)
 //   k_integrate  per particle: contact force gather in a fixed order,
 //                resolve_wall!, apply_body_force!, update!
@@ -358,6 +359,127 @@ __device__ __forceinline__ void bucket_range(const DemDev& d, uint32_t b, uint32
     }
 }
 
+// ---- next-buffer rows -------------------------------------------------------
+// The rolling-array rebuild (the reference's remove_inactive_contact! + swap,
+// src/kernels.jl:487-506, src/executor.jl:140-153) happens where a
+// particle's contacts are decided: row i of buffer cur^1 is the merge, by j,
+// of the surviving entries of row i (keep flags) and the sorted new partners.
+// A row is placed by a warp-aggregated atomic on the buffer's allocator.
+
+// One particle's decided row, held by every lane of its group.
+struct RowJob {
+    int i, mode;  // particle; its scene's mode (Step, Init or Frozen)
+    int e0, e1;   // current row entries [e0, e1)
+    int nnew;     // new partners (sorted, in the particle's stash)
+    int len;      // next row length (survivors + new), 0 for no row
+};
+
+// Places the rows of a warp's groups (L lanes each) in buffer nxt: every lane
+// of the warp calls it with its group's (group-uniform) `len`; returns the
+// group's row start.  A row that would cross the capacity raises
+// kErrCapacity and gets length 0.
+template <int L>
+__device__ __forceinline__ int place_rows(const DemDev& d, const DemParams& p, int nxt, int& len) {
+    const unsigned lane = lane_id();
+    const int v = (lane % L == 0) ? len : 0;
+    int incl = v;
+#pragma unroll
+    for (int o2 = 1; o2 < 32; o2 <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o2);
+        if (lane >= (unsigned)o2) incl += y;
+    }
+    int base = 0;
+    if (lane == 31 && incl) base = (int)atomicAdd(&d.ctr->row_alloc[nxt], (unsigned)incl);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    int start = __shfl_sync(0xffffffffu, base + incl - v, (int)(lane & ~(unsigned)(L - 1)));
+    if (len > 0 && (long long)start + len > (long long)p.cap) {
+        if (lane % L == 0) raise_error(d.ctr, kErrCapacity);
+        start = 0;
+        len = 0;
+    }
+    return start;
+}
+
+__device__ __forceinline__ void add_incoming_entry(const DemDev& d, const DemParams& p, int j,
+                                                   int pos, int i) {
+    const int slot = atomicAdd(&d.in_cnt[j], 1);
+    if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = make_int2(pos, i);
+    else raise_error(d.ctr, kErrCapacity);
+}
+
+// Writes the row of job `r` at [start, start + r.len) of buffer cur^1 (L
+// lanes share it) and records, for a stepping scene, each contact in its
+// partner's incoming list (the force gather's order).  A stepping contact
+// carries only the state the next force pass reads: a bond its accumulated
+// 𝐅, 𝛕ᵢ, 𝛕ⱼ, a Hertz contact its 𝐬 (the force pass rewrites 𝐤 and 𝐅; a
+// bond's 𝐬 and a Hertz contact's torques are zero, reported as such by the
+// host).  Contacts of scenes that do not step keep every field.
+template <int L>
+__device__ __forceinline__ void finish_row(const DemDev& d, const DemParams& p, int cur,
+                                           const RowJob& r, int start, int lane) {
+    const ContactSoA o = d.c[cur];
+    const ContactSoA w = d.c[cur ^ 1];
+    const int32_t* st = d.stash + (size_t)r.i * p.kstash;
+    for (int e = r.e0 + lane; e < r.e1; e += L) {
+        if (!d.keep[e]) continue;
+        const int j = o.cj[e];
+        const uint32_t fl = o.fl[e];
+        const int kind = r.mode != kModeStep ? 0 : ((fl & kBonded) ? 1 : 2);
+        // a stepping contact's carried state is loaded before its slot is
+        // computed (the loads overlap the rank loops)
+        double v[9];
+        if (kind == 1) {
+#pragma unroll
+            for (int f = 0; f < 9; ++f) v[f] = o.f[CF + f][e];
+        } else if (kind == 2) {
+#pragma unroll
+            for (int f = 0; f < 3; ++f) v[f] = o.f[CS + f][e];
+        }
+        int pos = start;
+        for (int q = r.e0; q < e; ++q) pos += d.keep[q];
+        for (int u = 0; u < r.nnew; ++u) pos += st[u] < j ? 1 : 0;
+        w.ci[pos] = r.i;
+        w.cj[pos] = j;
+        w.fl[pos] = fl;
+        if (kind == 0) {
+            for (int f = 0; f < 15; ++f) w.f[f][pos] = o.f[f][e];
+        } else if (kind == 1) {
+#pragma unroll
+            for (int f = 0; f < 9; ++f) w.f[CF + f][pos] = v[f];
+        } else {
+#pragma unroll
+            for (int f = 0; f < 3; ++f) w.f[CS + f][pos] = v[f];
+        }
+        if (r.mode == kModeStep) add_incoming_entry(d, p, j, pos, r.i);
+    }
+    for (int u = lane; u < r.nnew; u += L) {
+        const int j = st[u];
+        int pos = start + u;
+        for (int q = r.e0; q < r.e1; ++q) pos += (d.keep[q] && o.cj[q] < j) ? 1 : 0;
+        w.ci[pos] = r.i;
+        w.cj[pos] = j;
+        w.fl[pos] = r.mode == kModeInit ? (kActive | kBonded) : kActive;
+#pragma unroll
+        for (int f = 0; f < 15; ++f) w.f[f][pos] = 0.0;
+        if (r.mode == kModeStep) add_incoming_entry(d, p, j, pos, r.i);
+    }
+}
+
+// Places and writes the rows of a warp's groups: every lane of the warp
+// calls it; `active` groups carry a decided job.
+template <int L>
+__device__ __forceinline__ void emit_rows(const DemDev& d, const DemParams& p, int cur, bool active,
+                                          const RowJob& r, int lane) {
+    int len = active ? r.len : 0;
+    const int start = place_rows<L>(d, p, cur ^ 1, len);
+    if (!active) return;
+    if (lane == 0) {
+        d.row_start[cur ^ 1][r.i] = start;
+        d.row_len[cur ^ 1][r.i] = len;
+    }
+    if (len > 0) finish_row<L>(d, p, cur, r, start, lane);
+}
+
 // Shared memory of one 8-lane group of k_detect.
 struct DetectShared {
     int nnew;
@@ -372,7 +494,7 @@ struct DetectShared {
 template <bool INIT, bool MULTI>
 __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p, int cur, int k,
                                              int lane, unsigned gmask, uint32_t lim,
-                                             DetectShared& sh) {
+                                             DetectShared& sh, RowJob& job) {
     const int nxt = cur ^ 1;
     if (lane == 0) {
         sh.nnew = 0;
@@ -554,11 +676,17 @@ __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p
             }
             stash[b2 + 1] = v;
         }
-        d.nnew[i] = nnew;
-        d.row_len[nxt][i] = nkeep + nnew;  // placed by k_rows
+        sh.nnew = nnew;
         if (ended) atomicAdd(&d.sctr[sc].ended, (unsigned long long)ended);
         if (!init && nnew) atomicAdd(&d.sctr[sc].created, (unsigned long long)nnew);
     }
+    __syncwarp(gmask);
+    job.i = i;
+    job.mode = init ? kModeInit : (frozen ? kModeFrozen : kModeStep);
+    job.e0 = e0;
+    job.e1 = e1;
+    job.nnew = sh.nnew;
+    job.len = nkeep + job.nnew;
 }
 
 // ---------------------------------------------------------------------------
@@ -696,13 +824,20 @@ __global__ void __launch_bounds__(kThreads, MINB) k_search(DemDev d, DemParams p
     for (int k = blockIdx.x * kThreads + (int)threadIdx.x; k < count; k += stride)
         canon_slot<MULTI>(d, p, cur, k);
     grid_sync(d.ctr);
-    // cp_list enumeration with update_contacts! / init_bonds!
+    // cp_list enumeration with update_contacts! / init_bonds!, then the next
+    // rows; a warp's four groups move together (the rows are placed per warp)
     const int lane = threadIdx.x & (kLanes - 1);
     const int g = threadIdx.x / kLanes;
     const unsigned gmask = 0xffu << (lane_id() & ~7u);
-    for (int k = blockIdx.x * (kThreads / kLanes) + g; k < count; k += gridDim.x * (kThreads / kLanes)) {
-        detect_group<INIT, MULTI>(d, p, cur, k, lane, gmask, lim, sh[g]);
-        __syncwarp(gmask);
+    const int gwarp = (int)(threadIdx.x >> 5) * (32 / kLanes);  // the warp's first group
+    for (int k0 = blockIdx.x * (kThreads / kLanes) + gwarp; k0 < count;
+         k0 += gridDim.x * (kThreads / kLanes)) {
+        const int k = k0 + (g - gwarp);
+        RowJob job{};
+        const bool active = k < count;
+        if (active) detect_group<INIT, MULTI>(d, p, cur, k, lane, gmask, lim, sh[g], job);
+        emit_rows<kLanes>(d, p, cur, active, job, lane);
+        __syncwarp();
     }
 }
 
@@ -738,104 +873,116 @@ struct ListShared {
     int nnew;
     int row[kRowCache];
 };
-template <bool MULTI>
-__global__ void __launch_bounds__(kThreads) k_vdetect(DemDev d, DemParams p, int cur) {
+template <bool MULTI, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_vdetect(DemDev d, DemParams p, int cur) {
     __shared__ ListShared sh[kThreads / kVLanes];
     dep_begin(p.dep == 2);
     const int lane = threadIdx.x & (kVLanes - 1);
     const int g = threadIdx.x / kVLanes;
     const unsigned gmask = 0xfu << (lane_id() & ~3u);
-    const int nxt = cur ^ 1;
     const ContactSoA o = d.c[cur];
-    for (int i = blockIdx.x * (kThreads / kVLanes) + g; i < p.n;
-         i += gridDim.x * (kThreads / kVLanes)) {
-        // which particles test their lists: the path byte k_hash wrote (arena);
-        // a single-scene handle decides from its one flag
+    // a single-scene handle decides from its one flag
+    if (!MULTI && d.sflags[cur][0] != 0u) return;
+    // a warp's eight groups move together (their rows are placed per warp)
+    const int gwarp = (int)(threadIdx.x >> 5) * (32 / kVLanes);
+    for (int i0 = blockIdx.x * (kThreads / kVLanes) + gwarp; i0 < p.n;
+         i0 += gridDim.x * (kThreads / kVLanes)) {
+        const int i = i0 + (g - gwarp);
+        // which particles test their lists: the path byte the search wrote (arena)
+        bool active = i < p.n;
         bool frozen = false;
-        if (MULTI) {
+        if (MULTI && active) {
             const uint8_t path = d.path[i];
-            if ((path & 3) != 2) continue;
+            active = (path & 3) == 2;
             frozen = (path >> 2) == kModeFrozen;
-        } else if (d.sflags[cur][0] != 0u) {
-            continue;
         }
-        if (lane == 0) sh[g].nnew = 0;
-        const int e0 = d.row_start[cur][i];
-        const int e1 = e0 + d.row_len[cur][i];
-        const bool cached = e1 - e0 <= kRowCache;
-        int nkeep = 0, ended = 0;
-        for (int e2 = e0 + lane; e2 < e1; e2 += kVLanes) {
-            const uint32_t fl = o.fl[e2];
-            const int j = o.cj[e2];
-            if (cached) sh[g].row[e2 - e0] = (fl & kActive) ? j : -1;
-            int keep;
-            if (!(fl & kActive)) {
-                keep = 0;
-            } else if (frozen || (fl & kBonded)) {
-                keep = 1;
-            } else {
-                const bool valid = touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j],
-                                               d.pz[j], d.r[i], d.r[j]);
-                keep = (valid || !in_cp_list<MULTI>(d, scene_rec<MULTI>(d, p, slot_scene<MULTI>(d, i)),
-                                                     i, j))
-                           ? 1
-                           : 0;
-                ended += 1 - keep;
-            }
-            d.keep[e2] = (uint8_t)keep;
-            nkeep += keep;
-        }
-        nkeep = __reduce_add_sync(gmask, nkeep);
-        ended = __reduce_add_sync(gmask, ended);
-        __syncwarp(gmask);
-        int32_t* stash = d.stash + (size_t)i * p.kstash;
-        if (!frozen) {
-            const float4 Pi = d.pos32[i];
-            const int nv = d.vl_len[i];
-            const int32_t* vl = d.vl + (size_t)i * p.kvl;
-            for (int v = lane; v < nv; v += kVLanes) {
-                const int j = vl[v];
-                if (!maybe_touching32(Pi, d.pos32[j])) continue;
-                bool found = false;
-                if (cached) {
-                    for (int t = 0; t < e1 - e0 && !found; ++t) found = sh[g].row[t] == j;
+        RowJob job{};
+        if (active) {
+            if (lane == 0) sh[g].nnew = 0;
+            const int e0 = d.row_start[cur][i];
+            const int e1 = e0 + d.row_len[cur][i];
+            const bool cached = e1 - e0 <= kRowCache;
+            int nkeep = 0, ended = 0;
+            for (int e2 = e0 + lane; e2 < e1; e2 += kVLanes) {
+                const uint32_t fl = o.fl[e2];
+                const int j = o.cj[e2];
+                if (cached) sh[g].row[e2 - e0] = (fl & kActive) ? j : -1;
+                int keep;
+                if (!(fl & kActive)) {
+                    keep = 0;
+                } else if (frozen || (fl & kBonded)) {
+                    keep = 1;
                 } else {
-                    for (int e2 = e0; e2 < e1 && !found; ++e2)
-                        found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
+                    const bool valid = touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j],
+                                                   d.pz[j], d.r[i], d.r[j]);
+                    keep = (valid ||
+                            !in_cp_list<MULTI>(d, scene_rec<MULTI>(d, p, slot_scene<MULTI>(d, i)), i, j))
+                               ? 1
+                               : 0;
+                    ended += 1 - keep;
                 }
-                if (found) continue;
-                if (!touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j], d.pz[j], d.r[i],
-                                 d.r[j]))
-                    continue;
-                const int slot = atomicAdd(&sh[g].nnew, 1);
-                if (slot < p.kstash) stash[slot] = j;
+                d.keep[e2] = (uint8_t)keep;
+                nkeep += keep;
             }
-        }
-        __syncwarp(gmask);
-        if (lane == 0) {
-            int nnew = sh[g].nnew;
-            if (nnew > p.kstash) {
-                raise_error(d.ctr, kErrCapacity);
-                nnew = p.kstash;
-            }
-            for (int a2 = 1; a2 < nnew; ++a2) {  // new partners ascending
-                const int v = stash[a2];
-                int b2 = a2 - 1;
-                while (b2 >= 0 && stash[b2] > v) {
-                    stash[b2 + 1] = stash[b2];
-                    --b2;
+            nkeep = __reduce_add_sync(gmask, nkeep);
+            ended = __reduce_add_sync(gmask, ended);
+            __syncwarp(gmask);
+            int32_t* stash = d.stash + (size_t)i * p.kstash;
+            if (!frozen) {
+                const float4 Pi = d.pos32[i];
+                const int nv = d.vl_len[i];
+                const int32_t* vl = d.vl + (size_t)i * p.kvl;
+                for (int v = lane; v < nv; v += kVLanes) {
+                    const int j = vl[v];
+                    if (!maybe_touching32(Pi, d.pos32[j])) continue;
+                    bool found = false;
+                    if (cached) {
+                        for (int t = 0; t < e1 - e0 && !found; ++t) found = sh[g].row[t] == j;
+                    } else {
+                        for (int e2 = e0; e2 < e1 && !found; ++e2)
+                            found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
+                    }
+                    if (found) continue;
+                    if (!touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j], d.pz[j], d.r[i],
+                                     d.r[j]))
+                        continue;
+                    const int slot = atomicAdd(&sh[g].nnew, 1);
+                    if (slot < p.kstash) stash[slot] = j;
                 }
-                stash[b2 + 1] = v;
             }
-            d.nnew[i] = nnew;
-            d.row_len[nxt][i] = nkeep + nnew;
-            if (ended || nnew) {
-                const int sc = slot_scene<MULTI>(d, i);
-                if (ended) atomicAdd(&d.sctr[sc].ended, (unsigned long long)ended);
-                if (nnew) atomicAdd(&d.sctr[sc].created, (unsigned long long)nnew);
+            __syncwarp(gmask);
+            if (lane == 0) {
+                int nnew = sh[g].nnew;
+                if (nnew > p.kstash) {
+                    raise_error(d.ctr, kErrCapacity);
+                    nnew = p.kstash;
+                }
+                for (int a2 = 1; a2 < nnew; ++a2) {  // new partners ascending
+                    const int v = stash[a2];
+                    int b2 = a2 - 1;
+                    while (b2 >= 0 && stash[b2] > v) {
+                        stash[b2 + 1] = stash[b2];
+                        --b2;
+                    }
+                    stash[b2 + 1] = v;
+                }
+                sh[g].nnew = nnew;
+                if (ended || nnew) {
+                    const int sc = slot_scene<MULTI>(d, i);
+                    if (ended) atomicAdd(&d.sctr[sc].ended, (unsigned long long)ended);
+                    if (nnew) atomicAdd(&d.sctr[sc].created, (unsigned long long)nnew);
+                }
             }
+            __syncwarp(gmask);
+            job.i = i;
+            job.mode = frozen ? kModeFrozen : kModeStep;
+            job.e0 = e0;
+            job.e1 = e1;
+            job.nnew = sh[g].nnew;
+            job.len = nkeep + job.nnew;
         }
-        __syncwarp(gmask);
+        emit_rows<kVLanes>(d, p, cur, active, job, lane);
+        __syncwarp();
     }
 }
 
@@ -858,131 +1005,6 @@ __device__ __forceinline__ void scene_flags_one(const DemDev& d, const DemParams
     d.sflags[cur][s] = 0u;
 }
 
-
-// Row placement in the next contact buffer (the atomic-compacted contact list
-// of src/kernels.jl:74, 109): one warp-aggregated atomic per 32 slots.  Free
-// arena slots have length 0.  A row that would cross the capacity raises
-// kErrCapacity and is dropped (length 0).
-__global__ void __launch_bounds__(kThreads) k_rows(DemDev d, DemParams p, int nxt) {
-    dep_begin(p.dep == 2);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int len = i < p.n ? d.row_len[nxt][i] : 0;
-    int incl = len;
-#pragma unroll
-    for (int o2 = 1; o2 < 32; o2 <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, o2);
-        if (lane_id() >= (unsigned)o2) incl += y;
-    }
-    int base = 0;
-    if (lane_id() == 31 && incl) base = (int)atomicAdd(&d.ctr->row_alloc[nxt], (unsigned)incl);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    if (i >= p.n) return;
-    int start = base + incl - len;
-    int rl = len;
-    if ((long long)start + len > (long long)p.cap) {
-        raise_error(d.ctr, kErrCapacity);
-        start = 0;
-        rl = 0;
-    }
-    d.row_start[nxt][i] = start;
-    d.row_len[nxt][i] = rl;
-}
-
-// Rolling-array rebuild (the reference's remove_inactive_contact! + swap,
-// src/kernels.jl:487-506, src/executor.jl:140-153): row i of buffer cur^1 is
-// the merge, by j, of the surviving entries of row i and the sorted new
-// partners.  One thread per old contact (coalesced copies) and one per
-// particle for its new contacts; each computes its final slot directly.
-template <bool INIT, bool MULTI>
-__global__ void __launch_bounds__(kThreads) k_compact(DemDev d, DemParams p, int cur) {
-    dep_begin(p.dep == 2);
-    const int nxt = cur ^ 1;
-    const int cold = min((int)d.ctr->row_alloc[cur], p.cap);
-    const ContactSoA o = d.c[cur];
-    const ContactSoA w = d.c[nxt];
-    const int stride = gridDim.x * blockDim.x;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cold + p.n; t += stride) {
-        if (t < cold) {
-            // independent loads first (the chain below is latency-bound)
-            const uint8_t kp = d.keep[t];
-            const int i = o.ci[t], j = o.cj[t];
-            const uint32_t fl = o.fl[t];
-            if (!kp || i >= p.n) continue;
-            const int r0 = d.row_start[cur][i], n0 = d.row_len[cur][i];
-            const int rl = d.row_len[nxt][i];
-            const int mode = MULTI ? (d.path[i] >> 2) : (INIT ? kModeInit : kModeStep);
-            // entries outside the owner's current row are left-overs of a
-            // removed scene (arena) and are dropped
-            if (t < r0 || t >= r0 + n0) continue;
-            if (rl == 0) continue;  // row dropped after a capacity overflow, or a free slot
-            // A stepping contact carries only the state the next force pass
-            // reads: a bond its accumulated 𝐅, 𝛕ᵢ, 𝛕ⱼ, a Hertz contact its 𝐬 (the
-            // force pass rewrites 𝐤 and 𝐅; a bond's 𝐬 and a Hertz contact's
-            // torques are zero, reported as such by the host).  Contacts of
-            // scenes that do not step keep every field.  The loads are issued
-            // before the slot is computed (unrolled: the column pointers stay
-            // in registers).
-            const int kind = mode != kModeStep ? 0 : ((fl & kBonded) ? 1 : 2);
-            double v[15];
-            if (kind == 0) {
-#pragma unroll
-                for (int f = 0; f < 15; ++f) v[f] = o.f[f][t];
-            } else if (kind == 1) {
-#pragma unroll
-                for (int f = CF; f < CS; ++f) v[f] = o.f[f][t];
-            } else {
-#pragma unroll
-                for (int f = CS; f < CS + 3; ++f) v[f] = o.f[f][t];
-            }
-            int pos = d.row_start[nxt][i];
-            for (int q = r0; q < t; ++q) pos += d.keep[q];
-            const int nn = d.nnew[i];
-            const int32_t* st = d.stash + (size_t)i * p.kstash;
-            for (int u = 0; u < nn; ++u) pos += st[u] < j ? 1 : 0;
-            w.ci[pos] = i;
-            w.cj[pos] = j;
-            w.fl[pos] = fl;
-            if (kind == 0) {
-#pragma unroll
-                for (int f = 0; f < 15; ++f) w.f[f][pos] = v[f];
-            } else if (kind == 1) {
-#pragma unroll
-                for (int f = CF; f < CS; ++f) w.f[f][pos] = v[f];
-            } else {
-#pragma unroll
-                for (int f = CS; f < CS + 3; ++f) w.f[f][pos] = v[f];
-            }
-            if (mode == kModeStep) {
-                const int slot = atomicAdd(&d.in_cnt[j], 1);
-                if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = make_int2(pos, i);
-                else raise_error(d.ctr, kErrCapacity);
-            }
-        } else {
-            const int i = t - cold;
-            const int nn = d.nnew[i];
-            if (!nn || d.row_len[nxt][i] == 0) continue;
-            const int mode = MULTI ? (d.path[i] >> 2) : (INIT ? kModeInit : kModeStep);
-            const int e0 = d.row_start[cur][i], e1 = e0 + d.row_len[cur][i];
-            const int32_t* st = d.stash + (size_t)i * p.kstash;
-            const int base = d.row_start[nxt][i];
-            for (int u = 0; u < nn; ++u) {
-                const int j = st[u];
-                int pos = base + u;
-                for (int q = e0; q < e1; ++q) pos += (d.keep[q] && o.cj[q] < j) ? 1 : 0;
-                w.ci[pos] = i;
-                w.cj[pos] = j;
-                w.fl[pos] = mode == kModeInit ? (kActive | kBonded) : kActive;
-#pragma unroll
-                for (int f = 0; f < 15; ++f) w.f[f][pos] = 0.0;
-                if (mode == kModeStep) {
-                    const int slot = atomicAdd(&d.in_cnt[j], 1);
-                    if (slot < p.kin) d.in_list[(size_t)j * p.kin + slot] = make_int2(pos, i);
-                    else raise_error(d.ctr, kErrCapacity);
-                }
-            }
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------
 // Contact frame of src/kernels.jl:145-165: the rotation 𝐑 taking the unit
@@ -2008,25 +2030,16 @@ void launch_search(const DemDev& d, const DemParams& p, int cur, bool init, bool
     else launch_search_b<4>(d, p, cur, init, multi, all, s);
 }
 
-void launch_lists(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
+void launch_lists(const DemDev& d, const DemParams& p, int cur, bool multi, const LaunchShape& sh,
                   cudaStream_t s) {
     if (p.n == 0) return;
-    if (!init) {  // the scenes that test their neighbour lists
-        const int nv = max(1, min(blocks_for((long long)p.n * kVLanes, kThreads), p.sms * 8));
-        launch(p.dep != 0, multi ? k_vdetect<true> : k_vdetect<false>, nv, kThreads, s, d, p,
+    const int nv = max(1, min(blocks_for((long long)p.n * kVLanes, kThreads), p.sms * 8));
+    if (sh.detect_blocks_per_sm == 3)
+        launch(p.dep != 0, multi ? k_vdetect<true, 3> : k_vdetect<false, 3>, nv, kThreads, s, d, p,
                cur);
-    }
-    launch(p.dep != 0, k_rows, blocks_for(p.n, kThreads), kThreads, s, d, p, cur ^ 1);
-}
-
-void launch_compact(const DemDev& d, const DemParams& p, int cur, bool init, bool multi,
-                    const LaunchShape& sh, cudaStream_t s) {
-    if (p.n == 0) return;
-    const int block = clamp_block(sh.compact_block);
-    const int nb = min(blocks_for((long long)p.cap + p.n, block), max(sh.compact_grid, 1));
-    launch(p.dep != 0,
-           multi ? k_compact<false, true> : (init ? k_compact<true, false> : k_compact<false, false>),
-           nb, block, s, d, p, cur);
+    else
+        launch(p.dep != 0, multi ? k_vdetect<true, 4> : k_vdetect<false, 4>, nv, kThreads, s, d, p,
+               cur);
 }
 
 void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, const LaunchShape& sh,

@@ -171,12 +171,12 @@ class GlobalData:
               "dem_step_timed")
         return float(ms.value)
 
-    PHASES = ("broadphase", "detect", "compact", "force", "integrate")
+    PHASES = ("search", "lists", "force", "integrate")
 
     def simulate_profiled(self) -> dict:
         """One step launched phase by phase; device milliseconds per phase."""
-        ms = (C.c_float * 5)()
-        check(self.lib, self.lib.dem_step_profiled(self.h, ms, 5), "dem_step_profiled")
+        ms = (C.c_float * len(self.PHASES))()
+        check(self.lib, self.lib.dem_step_profiled(self.h, ms, len(ms)), "dem_step_profiled")
         return dict(zip(self.PHASES, [float(x) for x in ms]))
 
     def sync(self) -> None:
