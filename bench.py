@@ -12,7 +12,8 @@ library's stream, with a 256 MiB write between steps to flush L2 (the scene
 itself fits in L2).  value = particle-steps/s over all ranks (max time over
 ranks).  `e2e` repeats the metric through the C ABI with host buffers: every
 step uploads the particle state from page-locked host arrays
-(dem_set_particles), steps, and reads it back into them (dem_get_particles).  `roofline` reports the dominant kernel
+(dem_set_particles_async), steps, and reads it back into them
+(dem_get_particles), through GlobalData.state_buffers.  `roofline` reports the dominant kernel
 from per-phase CUDA events (dem_step_profiled).  `cpu_baseline` times the CPU
 oracle (OpenMP, all host threads) on a bounded sample of the same workload.
 
@@ -74,6 +75,12 @@ INTEGRATE_BYTES_PER_PARTICLE = 13 * 8 * 2 + 4 * 8 + 6 * 8 + 3 * 8 * 2 + 8 + 4  #
 DETECT_BYTES_PER_PARTICLE = 1 + 8 + 4 + 16 + 8 + 4 * (4 + 16)
 # k_search (fused full search), k_vdetect (lists + rows), k_force, k_integrate
 KERNELS_PER_STEP = 4
+# FP64 force kernel: FP64 thread instructions per bond (ncu
+# sm__thread_inst_executed_pipe_fp64_pred_on.sum over 50,700 bonds, in
+# profiles/k_force_fp64_bonded_cube_17576.md); GB300's FP64 pipe width
+FP64_INST_PER_BOND = 118.0
+FP64_LANES_PER_SM = 2
+SM_COUNT = 152
 L2_FLUSH_BYTES = 256 << 20
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
@@ -97,7 +104,8 @@ def load_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured",
+                "sm_max_mhz": d.get("sm_max_mhz")}
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
@@ -592,21 +600,33 @@ def main() -> None:
                          "algorithmic_bytes": dom_bytes})
     else:
         roofline.update({"achieved": None, "frac": None})
+    if precision == "fp64" and dom == "force" and n_bond > 0:
+        # the FP64 force kernel is bound by GB300's FP64 pipe (2 lanes per SM
+        # per cycle), not by HBM: its FP64 instructions per bond (ncu count)
+        # over its live per-phase time, against that pipe's peak at the
+        # sampled SM clock
+        sm_mhz = (clk.get("sm_mhz") or peaks.get("sm_max_mhz") or 2070.0)
+        peak = FP64_LANES_PER_SM * SM_COUNT * sm_mhz * 1e6 / 1e9
+        ach = FP64_INST_PER_BOND * n_bond / (ph[dom] * 1e-3) / 1e9
+        roofline["fp64_pipe"] = {
+            "unit": "G FP64 thread-instructions/s", "achieved": ach, "peak": peak,
+            "frac": ach / peak, "inst_per_bond": FP64_INST_PER_BOND,
+            "peak_source": f"nominal: {FP64_LANES_PER_SM} FP64 lanes per SM per cycle x "
+                           f"{SM_COUNT} SMs at the sampled {sm_mhz:.0f} MHz"}
 
-    # e2e through the C ABI with host buffers (page-locked, as a host
-    # application that exchanges state every step would allocate them)
-    keys = ("pos", "vel", "omega", "quat", "wall_shear")
-    host = {k: torch.empty((sc.n, 4 if k == "quat" else 3), dtype=torch.float64,
-                           pin_memory=True).numpy() for k in keys}
-    g.particles(out=host)
-    h2d = sum(host[k].nbytes for k in keys)
+    # e2e through the public API with host buffers: page-locked state arrays
+    # bound to the handle (GlobalData.state_buffers), written to the device,
+    # stepped and read back every step
+    buf = g.state_buffers()
+    h2d = sum(a.nbytes for a in buf.arrays.values())
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        g.set_particles(**host)
+        buf.upload()
         g.simulate(1)
-        g.particles(out=host)
+        buf.download()
     e2e_s = time.perf_counter() - t0
+    buf.close()
     if dist:
         t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)

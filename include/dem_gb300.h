@@ -261,6 +261,18 @@ int dem_get_particles(DemHandle* h, DemParticleState* out);
  * the skin of where they were built; otherwise the next step searches in full. */
 int dem_set_particles(DemHandle* h, const DemParticleState* in);
 
+/* dem_set_particles ordered on the handle's stream without waiting for it:
+ * page-locked or device buffers are read by a kernel later in the stream and
+ * must stay unchanged until the next synchronising call (dem_sync,
+ * dem_get_*, dem_step_timed); pageable buffers are free on return.  For a
+ * host loop that writes the state, steps and reads it back every step. */
+int dem_set_particles_async(DemHandle* h, const DemParticleState* in);
+
+/* Page-locked host memory for state buffers (cudaMallocHost / cudaFreeHost),
+ * for callers without a CUDA runtime of their own. */
+int dem_host_alloc(int64_t bytes, void** out);
+int dem_host_free(void* p);
+
 int dem_get_static(DemHandle* h, DemParticleStatic* out);
 
 int dem_get_derived(DemHandle* h, DemDerived* out);

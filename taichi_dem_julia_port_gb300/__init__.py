@@ -8,14 +8,16 @@ include/dem_gb300.h); this package is its host front end.
 """
 from .arena import Arena
 from .config import DEMConfig
-from .executor import GlobalData, initialize, load_particles, save_single, simulate, solve
+from .executor import (GlobalData, StateBuffers, initialize, load_particles, save_single, simulate,
+                       solve)
 from .p4io import compare_p4c, compare_p4p, read_p4c, read_p4p
 from .scenes import ParticleInput, bonded_cube, granular_pour
 
 DEMConfigDefault = DEMConfig
 
 __all__ = [
-    "Arena", "DEMConfig", "DEMConfigDefault", "GlobalData", "initialize", "simulate", "solve",
+    "Arena", "DEMConfig", "DEMConfigDefault", "GlobalData", "StateBuffers", "initialize",
+    "simulate", "solve",
     "load_particles", "save_single", "read_p4p", "read_p4c", "compare_p4p", "compare_p4c",
     "ParticleInput", "bonded_cube", "granular_pour",
 ]

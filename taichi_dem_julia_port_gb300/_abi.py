@@ -160,6 +160,9 @@ ENTRY_POINTS = {
     "dem_set_skin_factor": (C.c_int, [_H, C.c_int32, C.c_double]),
     "dem_get_particles": (C.c_int, [_H, C.POINTER(DemParticleState)]),
     "dem_set_particles": (C.c_int, [_H, C.POINTER(DemParticleState)]),
+    "dem_set_particles_async": (C.c_int, [_H, C.POINTER(DemParticleState)]),
+    "dem_host_alloc": (C.c_int, [C.c_int64, C.POINTER(C.c_void_p)]),
+    "dem_host_free": (C.c_int, [C.c_void_p]),
     "dem_get_static": (C.c_int, [_H, C.POINTER(DemParticleStatic)]),
     "dem_get_derived": (C.c_int, [_H, C.POINTER(DemDerived)]),
     "dem_get_contacts": (C.c_int, [_H, C.POINTER(DemContacts), C.c_int64, C.POINTER(C.c_int64)]),

@@ -764,10 +764,13 @@ double* device_view(const void* p) {
 // per particle, nullptr = field not exchanged) and the columns `cols[f]` at
 // slots [p0, p0 + n): one kernel over all fields, which reads or writes
 // device-accessible buffers in place; pageable buffers go through the
-// library's staging copy with one cudaMemcpyAsync each.  Synchronises; with
-// `error`, also returns the device error word as of the exchange.
+// library's staging copy with one cudaMemcpyAsync each.  Synchronises unless
+// `sync` is false (uploads only: a pageable buffer is free once its copy call
+// returns, a device-accessible one once the stream has passed the kernel);
+// with `error`, also returns the device error word as of the exchange.
 int exchange(DemHandle* h, int64_t p0, int64_t n, const int* k, double* const* host,
-             double* const (*cols)[4], int nfields, bool to_cols, int* error = nullptr) {
+             double* const (*cols)[4], int nfields, bool to_cols, int* error = nullptr,
+             bool sync = true) {
     if (error) {
         if (!h->err_host) CU(cudaMallocHost(&h->err_host, 64));
         CU(cudaMemcpyAsync(h->err_host, &h->d.ctr->error, sizeof(int), cudaMemcpyDeviceToHost,
@@ -812,6 +815,7 @@ int exchange(DemHandle* h, int64_t p0, int64_t n, const int* k, double* const* h
             if (staged[f])
                 CU(cudaMemcpyAsync(const_cast<double*>(src_host[f]), staged[f],
                                    sizeof(double) * x.k[f] * n, cudaMemcpyDeviceToHost, h->stream));
+    if (!sync && to_cols && !error) return DEM_OK;
     CU(cudaStreamSynchronize(h->stream));
     if (error) *error = *h->err_host;
     return DEM_OK;
@@ -1374,7 +1378,7 @@ int dem_get_particles(DemHandle* h, DemParticleState* out) {
     return dem_scene_get_particles(h, 0, out);
 }
 
-int dem_set_particles(DemHandle* h, const DemParticleState* in) {
+int set_particles(DemHandle* h, const DemParticleState* in, bool sync) {
     const SceneHost* S = scene_at(h, 0);
     if (!S || !in || h->multi) return DEM_ERR_INVALID;
     const int64_t n = S->sp.n;
@@ -1384,13 +1388,31 @@ int dem_set_particles(DemHandle* h, const DemParticleState* in) {
     double* const host[] = {in->pos, in->vel, in->omega, in->quat, in->wall_shear};
     double* const cols[][4] = {{d.px, d.py, d.pz}, {d.vx, d.vy, d.vz}, {d.wx, d.wy, d.wz},
                                {d.qw, d.qx, d.qy, d.qz}, {d.wsx, d.wsy, d.wsz}};
-    // the exchange synchronises before the refresh below is queued: the
-    // caller's buffers are free again on return
-    TRY(exchange(h, 0, n, k, host, cols, 5, true));
+    TRY(exchange(h, 0, n, k, host, cols, 5, true, nullptr, sync));
     // new positions: the neighbour lists stay valid while every particle lies
     // within skin/2 of where they were built, else the next step searches in full
     launch_refresh_pos32(h->d, h->p, false, 0, (int)n, in->pos ? h->cur : -1, h->stream);
     CU(cudaGetLastError());
+    return DEM_OK;
+}
+
+int dem_set_particles(DemHandle* h, const DemParticleState* in) {
+    return set_particles(h, in, true);  // the caller's buffers are free again on return
+}
+
+int dem_set_particles_async(DemHandle* h, const DemParticleState* in) {
+    return set_particles(h, in, false);
+}
+
+int dem_host_alloc(int64_t bytes, void** out) {
+    if (!out || bytes < 0) return DEM_ERR_INVALID;
+    *out = nullptr;
+    CU(cudaMallocHost(out, (size_t)std::max<int64_t>(bytes, 1)));
+    return DEM_OK;
+}
+
+int dem_host_free(void* p) {
+    if (p) CU(cudaFreeHost(p));
     return DEM_OK;
 }
 

@@ -94,6 +94,70 @@ def set_launch_shape(lib, h, shape: dict) -> None:
     check(lib, lib.dem_set_launch_shape(h, C.byref(sh)), "dem_set_launch_shape")
 
 
+class StateBuffers:
+    """Page-locked particle state arrays bound to one handle, for a host loop
+    that writes the state, steps and reads it back every step.  The arrays
+    (`pos`, `vel`, `omega`, `quat`, `wall_shear`, and with forces=True
+    `force`, `moment`) are numpy views of page-locked memory that the
+    library's exchange kernel reads and writes in place; `upload()` is
+    asynchronous (the arrays must stay unchanged until the next `download()`
+    or other synchronising call), `download()` returns when the arrays hold
+    the device state."""
+
+    def __init__(self, g: "GlobalData", forces: bool = False):
+        self._g = g
+        self._lib = g.lib
+        n = g.n
+        names = [k for k in _PARTICLE_FIELDS if forces or k not in ("force", "moment")]
+        total = sum(n * _PARTICLE_FIELDS[k] for k in names)
+        base = C.c_void_p()
+        check(self._lib, self._lib.dem_host_alloc(8 * max(total, 1), C.byref(base)),
+              "dem_host_alloc")
+        self._base = base
+        flat = np.ctypeslib.as_array(C.cast(base, C.POINTER(C.c_double)), shape=(max(total, 1),))
+        self.arrays = {}
+        off = 0
+        for k in names:
+            c = _PARTICLE_FIELDS[k]
+            self.arrays[k] = flat[off:off + n * c].reshape(n, c)
+            off += n * c
+        addr = {k: a.ctypes.data for k, a in self.arrays.items()}
+        self._in = _abi.DemParticleState(n, addr["pos"], addr["vel"], addr["omega"], addr["quat"],
+                                         None, None, addr["wall_shear"])
+        self._out = _abi.DemParticleState(n, *(addr.get(k) for k in _PARTICLE_FIELDS))
+        self.download()
+
+    def __getattr__(self, name):
+        arrays = self.__dict__.get("arrays", {})
+        if name in arrays:
+            return arrays[name]
+        raise AttributeError(name)
+
+    def upload(self) -> None:
+        """The arrays' state to the device (dem_set_particles_async)."""
+        check(self._lib, self._lib.dem_set_particles_async(self._g.h, C.byref(self._in)),
+              "dem_set_particles_async")
+
+    def download(self) -> None:
+        """The device state into the arrays (dem_get_particles)."""
+        check(self._lib, self._lib.dem_get_particles(self._g.h, C.byref(self._out)),
+              "dem_get_particles")
+
+    def close(self) -> None:
+        if getattr(self, "_base", None):
+            if getattr(self._g, "h", None):
+                self._lib.dem_sync(self._g.h)  # no kernel may still read the arrays
+            self._lib.dem_host_free(self._base)
+            self._base = None
+            self.arrays = {}
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class GlobalData:
     """Device state of one scene (particles, broad phase, contacts)."""
 
@@ -187,6 +251,10 @@ class GlobalData:
         """Particle state; `out` may hold preallocated (e.g. pinned) arrays."""
         return read_particles(self.lib, lambda st: self.lib.dem_get_particles(self.h, st),
                               self.n, forces, "dem_get_particles", out)
+
+    def state_buffers(self, forces: bool = False) -> StateBuffers:
+        """Page-locked state arrays bound to this handle (see StateBuffers)."""
+        return StateBuffers(self, forces)
 
     def set_particles(self, pos=None, vel=None, omega=None, quat=None, wall_shear=None) -> None:
         n = self.n
