@@ -334,7 +334,7 @@ def main_served(args, lib, ws, rank) -> None:
     sizing = ArenaSizing.from_budget(args.hbm_budget_gb * 1e9)
     clocks = ClockSampler(torch.cuda.current_device())
     with Server(sizing, precision=args.precision or "fp32", chunk_steps=200, lib=lib,
-                keep_state=False) as srv:
+                keep_state=False, policy=args.policy, max_active=args.max_active) as srv:
         clocks.start()
         rep = srv.run(reqs, realtime=True)
         clk = clocks.stop()
@@ -358,6 +358,7 @@ def main_served(args, lib, ws, rank) -> None:
                        "latency_p99_s": pct.get("p99"), "makespan_s": rep.makespan_s,
                        "particle_steps": rep.particle_steps,
                        "admissions_deferred": rep.admissions_deferred,
+                       "policy": args.policy, "max_active": args.max_active,
                        "arena_slots": sizing.max_particles,
                        "plain_fp64_scene_by_scene": plain,
                        "speedup_vs_plain": rep.throughput / plain["particle_steps_per_s"],
@@ -494,6 +495,10 @@ def main() -> None:
     ap.add_argument("--scenes", type=int, default=256, help="c4: number of scenes")
     ap.add_argument("--requests", type=int, default=12, help="c5: number of requests")
     ap.add_argument("--hbm-budget-gb", type=float, default=160.0, help="c5: arena budget")
+    ap.add_argument("--policy", default="sjf", choices=["fifo", "sjf"],
+                    help="c5: admission policy (sjf: least work first, capped active particles)")
+    ap.add_argument("--max-active", type=int, default=500_000,
+                    help="c5 sjf: particles the live scenes may hold before admission waits")
     ap.add_argument("--no-batched", action="store_true",
                     help="default workload: skip the batched summary")
     ap.add_argument("--no-tune", action="store_true", help="c4: keep the default launch shape")

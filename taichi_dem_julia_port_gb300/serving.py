@@ -127,7 +127,18 @@ class Server:
     """Continuous-batching loop over one arena sized from an HBM budget."""
 
     def __init__(self, sizing: ArenaSizing, precision: str = "fp32", chunk_steps: int = 200,
-                 cell_factor: float = 0.0, keep_state: bool = True, lib=None):
+                 cell_factor: float = 0.0, keep_state: bool = True, lib=None,
+                 policy: str = "fifo", max_active: int = 0):
+        """policy "fifo": waiting requests are admitted in arrival order as
+        soon as they fit.  policy "sjf": the waiting request with the least
+        work (particles x steps) first, and only while the live scenes hold
+        fewer than `max_active` particles (a request is always admitted into
+        an empty arena): small requests then share their launches with fewer
+        particles and finish sooner, at some cost in throughput."""
+        if policy not in ("fifo", "sjf"):
+            raise ValueError("policy must be 'fifo' or 'sjf'")
+        self.policy = policy
+        self.max_active = int(max_active) if max_active else 0
         self.sizing = sizing
         self.arena = Arena(sizing.max_particles, max_scenes=sizing.max_scenes,
                            max_contacts=sizing.max_contacts, max_buckets=sizing.max_buckets,
@@ -181,12 +192,20 @@ class Server:
             now = clock()
             while pending and pending[0].arrival_s <= now:
                 queue.append(pending.pop(0))
-            # admission in arrival order, skipping over requests that do not fit yet
+            # admission in arrival order (fifo) or by least work (sjf), skipping
+            # over requests that do not fit yet
+            if self.policy == "sjf":
+                queue.sort(key=lambda r: (r.n_hint or 1) * r.steps)
+            active = sum(lv.scene.n for lv in live.values())
             still = []
             for req in queue:
-                if not self._try_admit(req, time.perf_counter() - t0, live):
+                over = (self.policy == "sjf" and self.max_active and live
+                        and active + (req.n_hint or 0) > self.max_active)
+                if over or not self._try_admit(req, time.perf_counter() - t0, live):
                     still.append(req)
                     deferred += 1
+                else:
+                    active += req.scene().n
             queue = still
             if not live:
                 if queue:

@@ -50,13 +50,15 @@ def alone_state(req, precision):
     return st, stats
 
 
-@pytest.mark.parametrize("precision", ["fp32", "fp64"])
-def test_served_results_equal_alone(gpu, precision):
+@pytest.mark.parametrize("precision,policy", [("fp32", "fifo"), ("fp64", "fifo"),
+                                              ("fp32", "sjf")])
+def test_served_results_equal_alone(gpu, precision, policy):
     reqs = small_requests()
     # room for about two scenes at a time: the rest wait for freed slots
     sizing = ArenaSizing(max_particles=1000, max_contacts=16000, max_buckets=16384,
                          max_scenes=4, max_coordinate_number=16, contacts_per_particle=16)
-    with Server(sizing, precision=precision, chunk_steps=16) as srv:
+    with Server(sizing, precision=precision, chunk_steps=16, policy=policy,
+                max_active=700) as srv:
         rep = srv.run(reqs, realtime=False)
     assert len(rep.results) == len(reqs)
     assert rep.admissions_deferred > 0, "the arena was meant to be too small for all at once"

@@ -143,3 +143,9 @@ def test_serving_sizing_and_requests():
     assert all(900 <= r.n_hint <= 1_000_000 for r in a)
     sc = a[1].scene()
     assert not sc.bonded and abs(sc.n - a[1].n_hint) == 0
+
+
+def test_server_policy_argument():
+    from taichi_dem_julia_port_gb300.serving import ArenaSizing, Server
+    with pytest.raises(ValueError):
+        Server(ArenaSizing(1000, 1000, 4096, 2, 16, 8), policy="lifo")
