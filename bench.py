@@ -75,12 +75,34 @@ INTEGRATE_BYTES_PER_PARTICLE = 13 * 8 * 2 + 4 * 8 + 6 * 8 + 3 * 8 * 2 + 8 + 4  #
 DETECT_BYTES_PER_PARTICLE = 1 + 8 + 4 + 16 + 8 + 4 * (4 + 16)
 # k_search (fused full search), k_vdetect (lists + rows), k_force, k_integrate
 KERNELS_PER_STEP = 4
-# FP64 force kernel: FP64 thread instructions per bond (ncu
-# sm__thread_inst_executed_pipe_fp64_pred_on.sum over 50,700 bonds, in
-# profiles/k_force_fp64_bonded_cube_17576.md); GB300's FP64 pipe width
-FP64_INST_PER_BOND = 118.0
+# FP64-pipe instructions per unit (ncu sm__thread_inst_executed_pipe_fp64_pred_on.sum
+# per launch over the units it processed; profiles/k_force_fp64_bonded_cube_17576.md
+# and profiles/k_integrate_batched_64_scenes.md): the force kernel per bond, the
+# integrator per particle, in the FP64 and the FP32 force mode; GB300's FP64
+# pipe width
+FP64_INST = {("force", "fp64"): 118.0, ("force", "fp32"): 15.0,
+             ("integrate", "fp64"): 88.7, ("integrate", "fp32"): 54.0}
 FP64_LANES_PER_SM = 2
 SM_COUNT = 152
+
+
+def fp64_roofline(kernel: str, precision: str, n_particles: int, n_bond: int, ms: float,
+                  sm_mhz) -> dict | None:
+    """The FP64-pipe roofline of the force kernel (per bond; bonded scenes) or
+    the integrator (per particle): FP64 instructions over the live per-phase
+    time against the pipe's peak at the sampled SM clock."""
+    per = FP64_INST.get((kernel, precision))
+    units = n_bond if kernel == "force" else n_particles
+    if per is None or not units or not ms:
+        return None
+    sm_mhz = sm_mhz or 2070.0
+    peak = FP64_LANES_PER_SM * SM_COUNT * sm_mhz * 1e6 / 1e9
+    ach = per * units / (ms * 1e-3) / 1e9
+    return {"unit": "G FP64 thread-instructions/s", "achieved": ach, "peak": peak,
+            "frac": ach / peak, "inst_per_unit": per,
+            "unit_counted": "bond" if kernel == "force" else "particle",
+            "peak_source": f"nominal: {FP64_LANES_PER_SM} FP64 lanes per SM per cycle x "
+                           f"{SM_COUNT} SMs at the sampled {sm_mhz:.0f} MHz"}
 L2_FLUSH_BYTES = 256 << 20
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
@@ -268,6 +290,10 @@ def run_batched(args, lib, quick: bool = False) -> dict:
     if dom in alg:
         ach = alg[dom] / (ph[dom] * 1e-3) / 1e9
         roof.update({"achieved": ach, "frac": ach / peaks["hbm_gbs"], "algorithmic_bytes": alg[dom]})
+    fr = fp64_roofline(dom, precision, n_total, bonded, ph.get(dom),
+                       clk.get("sm_mhz") or peaks.get("sm_max_mhz"))
+    if fr:
+        roof["fp64_pipe"] = fr
     return {"value": value, "ms_per_step": ms_per_step, "steps": steps, "desc": desc,
             "n_particles": n_total, "scenes": len(batch), "contacts": contacts,
             "contact_steps_per_s": contacts * steps / (ms * 1e-3), "precision": precision,
@@ -605,19 +631,12 @@ def main() -> None:
                          "algorithmic_bytes": dom_bytes})
     else:
         roofline.update({"achieved": None, "frac": None})
-    if precision == "fp64" and dom == "force" and n_bond > 0:
-        # the FP64 force kernel is bound by GB300's FP64 pipe (2 lanes per SM
-        # per cycle), not by HBM: its FP64 instructions per bond (ncu count)
-        # over its live per-phase time, against that pipe's peak at the
-        # sampled SM clock
-        sm_mhz = (clk.get("sm_mhz") or peaks.get("sm_max_mhz") or 2070.0)
-        peak = FP64_LANES_PER_SM * SM_COUNT * sm_mhz * 1e6 / 1e9
-        ach = FP64_INST_PER_BOND * n_bond / (ph[dom] * 1e-3) / 1e9
-        roofline["fp64_pipe"] = {
-            "unit": "G FP64 thread-instructions/s", "achieved": ach, "peak": peak,
-            "frac": ach / peak, "inst_per_bond": FP64_INST_PER_BOND,
-            "peak_source": f"nominal: {FP64_LANES_PER_SM} FP64 lanes per SM per cycle x "
-                           f"{SM_COUNT} SMs at the sampled {sm_mhz:.0f} MHz"}
+    # the force kernel and the integrator are bound by GB300's FP64 pipe
+    # (2 lanes per SM per cycle) rather than by HBM: their FP64 roofline
+    fr = fp64_roofline(dom, precision, sc.n, n_bond, ph.get(dom),
+                       clk.get("sm_mhz") or peaks.get("sm_max_mhz"))
+    if fr:
+        roofline["fp64_pipe"] = fr
 
     # e2e through the public API with host buffers: page-locked state arrays
     # bound to the handle (GlobalData.state_buffers), written to the device,
