@@ -237,6 +237,52 @@ def oracle_sample(scene_list, seconds: float) -> dict:
                       "on the CPU oracle"}
 
 
+def precision_errors(scene_list, steps: int, lib) -> dict:
+    """FP32 force mode against FP64 on the same scenes (each alone on a
+    single-scene handle; the FP64 path equals the CPU oracle within 1e-9 in
+    the parity tests): after `steps` steps from the same start, the kinetic
+    energy, broken-bond count and positions; then one step from an identical
+    state (the FP64 state copied into the FP32 handle), the particle forces."""
+    from taichi_dem_julia_port_gb300 import GlobalData
+    ke_err, pos_err, force_err, bond_diff, bonds = 0.0, 0.0, 0.0, 0, 0
+    for sc in scene_list:
+        hs = []
+        for prec in ("fp64", "fp32"):
+            g = GlobalData(sc.cfg, sc.particles, precision=prec, lib=lib)
+            if sc.bonded:
+                g.initialize()
+            g.simulate(steps)
+            hs.append(g)
+        g64, g32 = hs
+        m = np.asarray(sc.particles.mass, dtype=np.float64)
+        p64, p32 = g64.particles(), g32.particles()
+        ke = [0.5 * float(np.sum(m * np.sum(p["vel"] ** 2, axis=1))) for p in (p64, p32)]
+        if ke[0] > 0:
+            ke_err = max(ke_err, abs(ke[1] - ke[0]) / ke[0])
+        r = np.median(np.cbrt(3.0 * np.asarray(sc.particles.volume) / (4.0 * np.pi)))
+        pos_err = max(pos_err, float(np.max(np.abs(p32["pos"] - p64["pos"]))) / r)
+        s64, s32 = g64.stats(), g32.stats()
+        bond_diff = max(bond_diff, abs(s32["bonds_broken"] - s64["bonds_broken"]))
+        bonds += s64["bonded"]
+        # one step from an identical state
+        g32.set_particles(**{k: p64[k] for k in ("pos", "vel", "omega", "quat", "wall_shear")})
+        g32.set_contacts(g64.contacts())
+        g64.simulate(1)
+        g32.simulate(1)
+        f64, f32 = g64.particles()["force"], g32.particles()["force"]
+        scale = float(np.max(np.linalg.norm(f64, axis=1)))
+        if scale > 0:
+            force_err = max(force_err, float(np.max(np.linalg.norm(f32 - f64, axis=1))) / scale)
+        g64.close()
+        g32.close()
+    return {"scenes": len(scene_list), "steps": steps,
+            "kinetic_energy_rel_err_max": ke_err, "position_err_max_in_radii": pos_err,
+            "force_rel_err_max_one_step": force_err,
+            "broken_bond_count_diff_max": bond_diff, "bonds": bonds,
+            "note": "FP32 force mode vs the FP64 path, each scene alone; force error relative "
+                    "to the scene's largest particle force"}
+
+
 def run_batched(args, lib, quick: bool = False) -> dict:
     """The batched workload on one arena: returns the JSON fields."""
     import torch
@@ -294,7 +340,11 @@ def run_batched(args, lib, quick: bool = False) -> dict:
                        clk.get("sm_mhz") or peaks.get("sm_max_mhz"))
     if fr:
         roof["fp64_pipe"] = fr
+    perr = None
+    if precision == "fp32":
+        perr = precision_errors(batch[:8] if quick else batch[:16], 300, lib)
     return {"value": value, "ms_per_step": ms_per_step, "steps": steps, "desc": desc,
+            "fp32_error_vs_fp64": perr,
             "n_particles": n_total, "scenes": len(batch), "contacts": contacts,
             "contact_steps_per_s": contacts * steps / (ms * 1e-3), "precision": precision,
             "plain_fp64_scene_by_scene": plain,
@@ -344,6 +394,7 @@ def main_batched(args, lib, ws, rank) -> None:
                        "contact_steps_per_s": ws * r["contact_steps_per_s"],
                        "plain_fp64_scene_by_scene": r["plain_fp64_scene_by_scene"],
                        "speedup_vs_plain": r["speedup_vs_plain"], "autotune": r["tune"],
+                       "fp32_error_vs_fp64": r["fp32_error_vs_fp64"],
                        "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "one arena"},
             "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": e2e, "clocks": r["clocks"],
@@ -671,7 +722,8 @@ def main() -> None:
         r = run_batched(args, lib, quick=True)
         batched = {k: r[k] for k in ("desc", "value", "ms_per_step", "steps", "n_particles",
                                      "contact_steps_per_s", "plain_fp64_scene_by_scene",
-                                     "speedup_vs_plain", "precision", "tune")}
+                                     "speedup_vs_plain", "precision", "tune",
+                                     "fp32_error_vs_fp64")}
         batched["phase_ms"] = r["roofline"]["phase_ms"]
         batched["metric"] = "particle-steps/s"
     if rank == 0:
