@@ -11,9 +11,9 @@ Our arm: W untimed steps, then K steps each timed with CUDA events on the
 library's stream, with a 256 MiB write between steps to flush L2 (the scene
 itself fits in L2).  value = particle-steps/s over all ranks (max time over
 ranks).  `e2e` repeats the metric through the C ABI with host buffers: every
-step uploads the particle state from page-locked host arrays
-(dem_set_particles_async), steps, and reads it back into them
-(dem_get_particles), through GlobalData.state_buffers.  `roofline` reports the dominant kernel
+step uploads the particle state from page-locked host arrays, steps, and
+reads it back into them (one dem_step_exchange call per step, through
+GlobalData.state_buffers).  `roofline` reports the dominant kernel
 from per-phase CUDA events (dem_step_profiled).  `cpu_baseline` times the CPU
 oracle (OpenMP, all host threads) on a bounded sample of the same workload.
 
@@ -716,9 +716,7 @@ def main() -> None:
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        buf.upload()
-        g.simulate(1)
-        buf.download()
+        buf.step(1)  # upload, step, download (dem_step_exchange)
     e2e_s = time.perf_counter() - t0
     buf.close()
     e2e_s = max_over_ranks(e2e_s, dist)

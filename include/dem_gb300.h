@@ -268,6 +268,13 @@ int dem_set_particles(DemHandle* h, const DemParticleState* in);
  * host loop that writes the state, steps and reads it back every step. */
 int dem_set_particles_async(DemHandle* h, const DemParticleState* in);
 
+/* One call of a host loop that exchanges the state every step:
+ * dem_set_particles_async(in) (skipped for NULL), dem_step(nsteps), then
+ * dem_get_particles(out) (skipped for NULL; returns when `out` holds the
+ * state).  Single-scene handles. */
+int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
+                      DemParticleState* out);
+
 /* Page-locked host memory for state buffers (cudaMallocHost / cudaFreeHost),
  * for callers without a CUDA runtime of their own. */
 int dem_host_alloc(int64_t bytes, void** out);

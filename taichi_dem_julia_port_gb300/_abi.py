@@ -161,6 +161,8 @@ ENTRY_POINTS = {
     "dem_get_particles": (C.c_int, [_H, C.POINTER(DemParticleState)]),
     "dem_set_particles": (C.c_int, [_H, C.POINTER(DemParticleState)]),
     "dem_set_particles_async": (C.c_int, [_H, C.POINTER(DemParticleState)]),
+    "dem_step_exchange": (C.c_int, [_H, C.POINTER(DemParticleState), C.c_int64,
+                                     C.POINTER(DemParticleState)]),
     "dem_host_alloc": (C.c_int, [C.c_int64, C.POINTER(C.c_void_p)]),
     "dem_host_free": (C.c_int, [C.c_void_p]),
     "dem_get_static": (C.c_int, [_H, C.POINTER(DemParticleStatic)]),

@@ -1404,6 +1404,15 @@ int dem_set_particles_async(DemHandle* h, const DemParticleState* in) {
     return set_particles(h, in, false);
 }
 
+int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
+                      DemParticleState* out) {
+    if (!h || nsteps < 0 || h->multi) return DEM_ERR_INVALID;
+    if (in) TRY(set_particles(h, in, false));
+    TRY(dem_step(h, nsteps));
+    if (out) return dem_get_particles(h, out);
+    return DEM_OK;
+}
+
 int dem_host_alloc(int64_t bytes, void** out) {
     if (!out || bytes < 0) return DEM_ERR_INVALID;
     *out = nullptr;

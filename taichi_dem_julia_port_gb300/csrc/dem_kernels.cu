@@ -1400,6 +1400,127 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
 // 𝛉ₛ = 𝐑(𝛚ᵢ + 𝛚ⱼ)dt and 𝛉_d = 𝐑(𝛚ᵢ - 𝛚ⱼ)dt, the reference's increments
 // k₅𝛉ᵢ + k₆𝛉ⱼ and k₆𝛉ᵢ + k₅𝛉ⱼ are k₊𝛉ₛ ± k₋𝛉_d with k₊ = (k₅+k₆)/2 =
 // 3EI/L/(1+ϕ) and k₋ = (k₅-k₆)/2 = EI/L; dt is folded into the stiffnesses.
+// One contact, one thread: FP64 mode (T = double) or the FP32 force mode's
+// Hertz and bond paths (T = float, via force32).
+template <typename T>
+__device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& SP,
+                                            const ContactSoA& w, int c, uint32_t fl, int i, int j,
+                                            int sc, size_t cap) {
+    if constexpr (std::is_same<T, float>::value) {
+        force32(d, SP, w, c, fl, i, j, sc, cap);
+        return;
+    }
+    const double dt = SP.dt;
+    const Vec3<double> ki{d.px[i], d.py[i], d.pz[i]}, kj{d.px[j], d.py[j], d.pz[j]};
+    const double ri = d.r[i], rj = d.r[j];
+    const Vec3<double> vi{d.vx[i], d.vy[i], d.vz[i]}, vj{d.vx[j], d.vy[j], d.vz[j]};
+    const Vec3<double> wi{d.wx[i], d.wy[i], d.wz[i]}, wj{d.wx[j], d.wy[j], d.wz[j]};
+    const double dx = kj.x - ki.x, dy = kj.y - ki.y, dz = kj.z - ki.z;
+    const double L2 = dx * dx + dy * dy + dz * dz;
+    const double invL = rsqrt(L2);
+    const double L = L2 * invL;
+    const double ax = dx * invL, ay = dy * invL, az = dz * invL;
+    const Frame R = contact_frame(dx, dy, dz, ax, ay, az, SP);
+    Vec3<T> fig, mi, mj;
+    if (fl & kBonded) {
+        // EBPM (src/kernels.jl:170-239)
+        const Vec3<double> Dd = rot<double>(R, {vi.x - vj.x, vi.y - vj.y, vi.z - vj.z});
+        const Vec3<double> Ts = rot<double>(R, {wi.x + wj.x, wi.y + wj.y, wi.z + wj.z});
+        const Vec3<double> Td = rot<double>(R, {wi.x - wj.x, wi.y - wj.y, wi.z - wj.z});
+        const Vec3<T> D = from_d<T>(Dd), Sv = from_d<T>(Ts), Q = from_d<T>(Td);
+        const int small = ri <= rj ? i : j;  // rb = ρ·min(rᵢ, rⱼ)
+        const T tinvL = (T)invL, tdt = (T)dt;
+        const T phi = (T)d.b_phic[small] * tinvL * tinvL;
+        const T iphi = rcp_nr((T)1.0 + phi);  // 1/(1 + ϕ)
+        const T EILdt = (T)d.b_EI[small] * tinvL * tdt;  // EI/L·dt
+        const T k1 = (T)d.b_EA[small] * tinvL * tdt;
+        const T k3 = (T)6.0 * EILdt * tinvL * iphi;
+        const T k2 = (T)2.0 * k3 * tinvL;
+        const T k4 = EILdt * (T)SP.b_inv1pnu;
+        const T kp = (T)3.0 * EILdt * iphi;
+        const T km = EILdt;
+        const T dFx = k1 * D.x, dFy = k2 * D.y + k3 * Sv.z, dFz = k2 * D.z - k3 * Sv.y;
+        const T ay_ = -k3 * D.z + kp * Sv.y, az_ = k3 * D.y + kp * Sv.z;
+        const T dtix = k4 * Q.x, dtiy = ay_ + km * Q.y, dtiz = az_ + km * Q.z;
+        const T dtjx = -k4 * Q.x, dtjy = ay_ - km * Q.y, dtjz = az_ - km * Q.z;
+        Vec3<double> Fi = ld3(w.f, CF, c), ti = ld3(w.f, CTI, c), tj = ld3(w.f, CTJ, c);
+        Fi = {Fi.x + (double)dFx, Fi.y + (double)dFy, Fi.z + (double)dFz};
+        ti = {ti.x + (double)dtix, ti.y + (double)dtiy, ti.z + (double)dtiz};
+        tj = {tj.x + (double)dtjx, tj.y + (double)dtjy, tj.z + (double)dtjz};
+        // breakage test, FP64 (src/kernels.jl:208-222)
+        if (bond_breaks_fp64(Fi, ti, tj, d, small, SP)) {
+            w.fl[c] = 0u;  // contact_active and contact_bonded bits cleared
+            atomicAdd(&d.sctr[sc].broken, 1ull);
+            fig = {(T)0, (T)0, (T)0};
+            mi = fig;
+            mj = fig;
+        } else {
+            fig = from_d<T>(rot_t<double>(R, {-Fi.x, -Fi.y, -Fi.z}));
+            mi = from_d<T>(rot_t<double>(R, {-ti.x, -ti.y, -ti.z}));
+            mj = from_d<T>(rot_t<double>(R, {-tj.x, -tj.y, -tj.z}));
+            st3(w.f, CK, c, {(ki.x + kj.x) * 0.5, (ki.y + kj.y) * 0.5, (ki.z + kj.z) * 0.5});
+            st3(w.f, CF, c, Fi);
+            st3(w.f, CTI, c, ti);
+            st3(w.f, CTJ, c, tj);  // a bond's 𝐬 stays zero and is not stored
+        }
+    } else {
+        // Hertz-Mindlin (src/kernels.jl:240-313)
+        const double gap = L - ri - rj;
+        if (gap > 0) atomicAdd(&d.sctr[sc].warn_gap, 1ull);
+        const double ext = ri - fabs(gap);
+        st3(w.f, CK, c, {ki.x + ax * ext, ki.y + ay * ext, ki.z + az * ext});
+        const Vec3<T> kri{(T)(ax * ext), (T)(ay * ext), (T)(az * ext)};
+        const Vec3<T> krj{kri.x - (T)dx, kri.y - (T)dy, kri.z - (T)dz};
+        const Vec3<T> wci = cross3<T>(from_d<T>(wi), kri);
+        const Vec3<T> wcj = cross3<T>(from_d<T>(wj), krj);
+        const Vec3<T> dv{(T)(vj.x - vi.x) + (wcj.x - wci.x), (T)(vj.y - vi.y) + (wcj.y - wci.y),
+                         (T)(vj.z - vi.z) + (wcj.z - wci.z)};
+        const Vec3<T> vc = rot<T>(R, dv);
+        const T tri = (T)ri, trj = (T)rj, tmi = (T)d.m[i], tmj = (T)d.m[j];
+        const T Rs = tri * trj / (tri + trj);
+        const T ms = tmi * tmj / (tmi + tmj);
+        const T tgap = (T)gap;
+        const T sq = sqrt(Rs * (T)fabs(gap));
+        const T kn = (T)(4.0 / 3.0 * SP.pp_Ys) * sq;
+        const T kt = (T)(8.0 * SP.pp_Gs) * sq;
+        const T root = sqrt(ms * sq);
+        const T gn = (T)SP.pp_cgn * root;
+        const T gt = (T)SP.pp_cgt * root;
+        if (gn < (T)0 || gt < (T)0)
+            atomicAdd(&d.sctr[sc].warn_damp, (unsigned long long)((gn < (T)0) + (gt < (T)0)));
+        Vec3<double> s = ld3(w.f, CS, c);
+        s = {s.x + (double)vc.x * 0.0, s.y + (double)vc.y * dt, s.z + (double)vc.z * dt};
+        const T F1 = -kn * tgap - gn * vc.x;
+        const Vec3<T> Ft{-kt * (T)s.x, -kt * (T)s.y, -kt * (T)s.z};
+        const T nFt = sqrt(Ft.x * Ft.x + Ft.y * Ft.y + Ft.z * Ft.z);
+        const T muF1 = (T)SP.pp_mu * F1;
+        T F2, F3;
+        if (nFt >= muF1) {
+            const T ratio = muF1 / nFt;
+            F2 = ratio * Ft.y;
+            F3 = ratio * Ft.z;
+            s = {s.x, (double)(F2 / kt), (double)(F3 / kt)};
+        } else {
+            F2 = Ft.y - gt * vc.y;
+            F3 = Ft.z - gt * vc.z;
+        }
+        fig = rot_t<T>(R, {-F1, -F2, -F3});
+        mi = cross3<T>(kri, fig);
+        mj = cross3<T>(krj, {-fig.x, -fig.y, -fig.z});
+        st3(w.f, CF, c, {(double)F1, (double)F2, (double)F3});
+        st3(w.f, CS, c, s);
+    }
+    d.contrib[0 * cap + c] = (double)fig.x;
+    d.contrib[1 * cap + c] = (double)fig.y;
+    d.contrib[2 * cap + c] = (double)fig.z;
+    d.contrib[3 * cap + c] = (double)mi.x;
+    d.contrib[4 * cap + c] = (double)mi.y;
+    d.contrib[5 * cap + c] = (double)mi.z;
+    d.contrib[6 * cap + c] = (double)mj.x;
+    d.contrib[7 * cap + c] = (double)mj.y;
+    d.contrib[8 * cap + c] = (double)mj.z;
+}
+
 template <typename T, bool MULTI>
 __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, int nxt) {
     const int C = min((int)d.ctr->row_alloc[nxt], p.cap);
@@ -1411,120 +1532,7 @@ __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, 
         const int i = w.ci[c], j = w.cj[c];
         const int sc = slot_scene<MULTI>(d, i);
         if (MULTI && (sc < 0 || d.sp[sc].mode != kModeStep)) continue;
-        const SceneParams& SP = scene_rec<MULTI>(d, p, sc);
-        if constexpr (std::is_same<T, float>::value) {
-            force32(d, SP, w, c, fl, i, j, sc, cap);
-            continue;
-        }
-        const double dt = SP.dt;
-        const Vec3<double> ki{d.px[i], d.py[i], d.pz[i]}, kj{d.px[j], d.py[j], d.pz[j]};
-        const double ri = d.r[i], rj = d.r[j];
-        const Vec3<double> vi{d.vx[i], d.vy[i], d.vz[i]}, vj{d.vx[j], d.vy[j], d.vz[j]};
-        const Vec3<double> wi{d.wx[i], d.wy[i], d.wz[i]}, wj{d.wx[j], d.wy[j], d.wz[j]};
-        const double dx = kj.x - ki.x, dy = kj.y - ki.y, dz = kj.z - ki.z;
-        const double L2 = dx * dx + dy * dy + dz * dz;
-        const double invL = rsqrt(L2);
-        const double L = L2 * invL;
-        const double ax = dx * invL, ay = dy * invL, az = dz * invL;
-        const Frame R = contact_frame(dx, dy, dz, ax, ay, az, SP);
-        Vec3<T> fig, mi, mj;
-        if (fl & kBonded) {
-            // EBPM (src/kernels.jl:170-239)
-            const Vec3<double> Dd = rot<double>(R, {vi.x - vj.x, vi.y - vj.y, vi.z - vj.z});
-            const Vec3<double> Ts = rot<double>(R, {wi.x + wj.x, wi.y + wj.y, wi.z + wj.z});
-            const Vec3<double> Td = rot<double>(R, {wi.x - wj.x, wi.y - wj.y, wi.z - wj.z});
-            const Vec3<T> D = from_d<T>(Dd), Sv = from_d<T>(Ts), Q = from_d<T>(Td);
-            const int small = ri <= rj ? i : j;  // rb = ρ·min(rᵢ, rⱼ)
-            const T tinvL = (T)invL, tdt = (T)dt;
-            const T phi = (T)d.b_phic[small] * tinvL * tinvL;
-            const T iphi = rcp_nr((T)1.0 + phi);  // 1/(1 + ϕ)
-            const T EILdt = (T)d.b_EI[small] * tinvL * tdt;  // EI/L·dt
-            const T k1 = (T)d.b_EA[small] * tinvL * tdt;
-            const T k3 = (T)6.0 * EILdt * tinvL * iphi;
-            const T k2 = (T)2.0 * k3 * tinvL;
-            const T k4 = EILdt * (T)SP.b_inv1pnu;
-            const T kp = (T)3.0 * EILdt * iphi;
-            const T km = EILdt;
-            const T dFx = k1 * D.x, dFy = k2 * D.y + k3 * Sv.z, dFz = k2 * D.z - k3 * Sv.y;
-            const T ay_ = -k3 * D.z + kp * Sv.y, az_ = k3 * D.y + kp * Sv.z;
-            const T dtix = k4 * Q.x, dtiy = ay_ + km * Q.y, dtiz = az_ + km * Q.z;
-            const T dtjx = -k4 * Q.x, dtjy = ay_ - km * Q.y, dtjz = az_ - km * Q.z;
-            Vec3<double> Fi = ld3(w.f, CF, c), ti = ld3(w.f, CTI, c), tj = ld3(w.f, CTJ, c);
-            Fi = {Fi.x + (double)dFx, Fi.y + (double)dFy, Fi.z + (double)dFz};
-            ti = {ti.x + (double)dtix, ti.y + (double)dtiy, ti.z + (double)dtiz};
-            tj = {tj.x + (double)dtjx, tj.y + (double)dtjy, tj.z + (double)dtjz};
-            // breakage test, FP64 (src/kernels.jl:208-222)
-            if (bond_breaks_fp64(Fi, ti, tj, d, small, SP)) {
-                w.fl[c] = 0u;  // contact_active and contact_bonded bits cleared
-                atomicAdd(&d.sctr[sc].broken, 1ull);
-                fig = {(T)0, (T)0, (T)0};
-                mi = fig;
-                mj = fig;
-            } else {
-                fig = from_d<T>(rot_t<double>(R, {-Fi.x, -Fi.y, -Fi.z}));
-                mi = from_d<T>(rot_t<double>(R, {-ti.x, -ti.y, -ti.z}));
-                mj = from_d<T>(rot_t<double>(R, {-tj.x, -tj.y, -tj.z}));
-                st3(w.f, CK, c, {(ki.x + kj.x) * 0.5, (ki.y + kj.y) * 0.5, (ki.z + kj.z) * 0.5});
-                st3(w.f, CF, c, Fi);
-                st3(w.f, CTI, c, ti);
-                st3(w.f, CTJ, c, tj);  // a bond's 𝐬 stays zero and is not stored
-            }
-        } else {
-            // Hertz-Mindlin (src/kernels.jl:240-313)
-            const double gap = L - ri - rj;
-            if (gap > 0) atomicAdd(&d.sctr[sc].warn_gap, 1ull);
-            const double ext = ri - fabs(gap);
-            st3(w.f, CK, c, {ki.x + ax * ext, ki.y + ay * ext, ki.z + az * ext});
-            const Vec3<T> kri{(T)(ax * ext), (T)(ay * ext), (T)(az * ext)};
-            const Vec3<T> krj{kri.x - (T)dx, kri.y - (T)dy, kri.z - (T)dz};
-            const Vec3<T> wci = cross3<T>(from_d<T>(wi), kri);
-            const Vec3<T> wcj = cross3<T>(from_d<T>(wj), krj);
-            const Vec3<T> dv{(T)(vj.x - vi.x) + (wcj.x - wci.x), (T)(vj.y - vi.y) + (wcj.y - wci.y),
-                             (T)(vj.z - vi.z) + (wcj.z - wci.z)};
-            const Vec3<T> vc = rot<T>(R, dv);
-            const T tri = (T)ri, trj = (T)rj, tmi = (T)d.m[i], tmj = (T)d.m[j];
-            const T Rs = tri * trj / (tri + trj);
-            const T ms = tmi * tmj / (tmi + tmj);
-            const T tgap = (T)gap;
-            const T sq = sqrt(Rs * (T)fabs(gap));
-            const T kn = (T)(4.0 / 3.0 * SP.pp_Ys) * sq;
-            const T kt = (T)(8.0 * SP.pp_Gs) * sq;
-            const T root = sqrt(ms * sq);
-            const T gn = (T)SP.pp_cgn * root;
-            const T gt = (T)SP.pp_cgt * root;
-            if (gn < (T)0 || gt < (T)0)
-                atomicAdd(&d.sctr[sc].warn_damp, (unsigned long long)((gn < (T)0) + (gt < (T)0)));
-            Vec3<double> s = ld3(w.f, CS, c);
-            s = {s.x + (double)vc.x * 0.0, s.y + (double)vc.y * dt, s.z + (double)vc.z * dt};
-            const T F1 = -kn * tgap - gn * vc.x;
-            const Vec3<T> Ft{-kt * (T)s.x, -kt * (T)s.y, -kt * (T)s.z};
-            const T nFt = sqrt(Ft.x * Ft.x + Ft.y * Ft.y + Ft.z * Ft.z);
-            const T muF1 = (T)SP.pp_mu * F1;
-            T F2, F3;
-            if (nFt >= muF1) {
-                const T ratio = muF1 / nFt;
-                F2 = ratio * Ft.y;
-                F3 = ratio * Ft.z;
-                s = {s.x, (double)(F2 / kt), (double)(F3 / kt)};
-            } else {
-                F2 = Ft.y - gt * vc.y;
-                F3 = Ft.z - gt * vc.z;
-            }
-            fig = rot_t<T>(R, {-F1, -F2, -F3});
-            mi = cross3<T>(kri, fig);
-            mj = cross3<T>(krj, {-fig.x, -fig.y, -fig.z});
-            st3(w.f, CF, c, {(double)F1, (double)F2, (double)F3});
-            st3(w.f, CS, c, s);
-        }
-        d.contrib[0 * cap + c] = (double)fig.x;
-        d.contrib[1 * cap + c] = (double)fig.y;
-        d.contrib[2 * cap + c] = (double)fig.z;
-        d.contrib[3 * cap + c] = (double)mi.x;
-        d.contrib[4 * cap + c] = (double)mi.y;
-        d.contrib[5 * cap + c] = (double)mi.z;
-        d.contrib[6 * cap + c] = (double)mj.x;
-        d.contrib[7 * cap + c] = (double)mj.y;
-        d.contrib[8 * cap + c] = (double)mj.z;
+        contact_one<T>(d, scene_rec<MULTI>(d, p, sc), w, c, fl, i, j, sc, cap);
     }
 }
 

@@ -138,6 +138,11 @@ class StateBuffers:
         check(self._lib, self._lib.dem_set_particles_async(self._g.h, C.byref(self._in)),
               "dem_set_particles_async")
 
+    def step(self, nsteps: int = 1) -> None:
+        """upload(), nsteps steps and download() in one call (dem_step_exchange)."""
+        check(self._lib, self._lib.dem_step_exchange(self._g.h, C.byref(self._in), int(nsteps),
+                                                     C.byref(self._out)), "dem_step_exchange")
+
     def download(self) -> None:
         """The device state into the arrays (dem_get_particles)."""
         check(self._lib, self._lib.dem_get_particles(self._g.h, C.byref(self._out)),

@@ -344,10 +344,13 @@ def test_state_buffers_loop(gpu):
     ref.close()
     g = GlobalData(sc.cfg, sc.particles)
     buf = g.state_buffers()
-    for _ in range(steps):
-        buf.upload()
-        g.simulate(1)
-        buf.download()
+    for s_ in range(steps):
+        if s_ % 2:
+            buf.upload()
+            g.simulate(1)
+            buf.download()
+        else:
+            buf.step(1)
     for k in ("pos", "vel", "omega", "quat", "wall_shear"):
         np.testing.assert_array_equal(getattr(buf, k), want[k], err_msg=k)
     buf.vel[:] *= 0.25
