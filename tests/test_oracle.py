@@ -193,3 +193,28 @@ def test_capacity_error(oracle_lib):
     o = O.OracleScene(cfg, sc.particles)
     with pytest.raises(RuntimeError):
         o.initialize()
+
+
+def test_reference_scenes_fixture(oracle_lib):
+    """The packed reference scenes equal a fresh read of the reference's files
+    (when the reference checkout is present) and run on the oracle."""
+    from pathlib import Path as _P
+    from taichi_dem_julia_port_gb300 import DEMConfig, load_particles
+    from tests import reference_scenes as rs
+    ref = _P("/root/reference")
+    for name, cfg_rel in (("carom", "cfg/1.toml"), ("cube_911", "cfg/2.toml")):
+        cfg, p, src = rs.load(name)
+        assert src.startswith(cfg_rel)
+        if ref.exists():
+            cfg2 = DEMConfig.from_toml(ref / cfg_rel)
+            p2 = load_particles((ref / cfg_rel).parent / cfg2.init_particles)
+            assert cfg2.to_toml() == cfg.to_toml()
+            for k in ("id", "gid", "volume", "mass", "pos", "vel"):
+                np.testing.assert_array_equal(getattr(p2, k), getattr(p, k), err_msg=k)
+    cfg, p, _ = rs.load("cube_911")
+    o = O.OracleScene(cfg, p)
+    o.initialize()
+    st = o.stats()
+    assert st["bonded"] > 2000 and st["bonded"] == st["contacts"]
+    o.simulate(20)
+    assert o.stats()["error"] == 0
