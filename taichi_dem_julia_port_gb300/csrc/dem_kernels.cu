@@ -897,10 +897,25 @@ __global__ void __launch_bounds__(kThreads, MINB) k_vdetect(DemDev d, DemParams 
             frozen = (path >> 2) == kModeFrozen;
         }
         RowJob job{};
+        int e0 = 0, e1 = 0, nv = 0;
+        if (active) {
+            e0 = d.row_start[cur][i];
+            e1 = e0 + d.row_len[cur][i];
+            nv = frozen ? 0 : d.vl_len[i];
+            // no contact and no list partner: an empty next row, decided at once
+            if (e1 == e0 && nv == 0) {
+                job.i = i;
+                job.mode = frozen ? kModeFrozen : kModeStep;
+                job.e0 = job.e1 = e0;
+                active = false;
+                if (lane == 0) {
+                    d.row_start[cur ^ 1][i] = 0;
+                    d.row_len[cur ^ 1][i] = 0;
+                }
+            }
+        }
         if (active) {
             if (lane == 0) sh[g].nnew = 0;
-            const int e0 = d.row_start[cur][i];
-            const int e1 = e0 + d.row_len[cur][i];
             const bool cached = e1 - e0 <= kRowCache;
             int nkeep = 0, ended = 0;
             for (int e2 = e0 + lane; e2 < e1; e2 += kVLanes) {
@@ -930,7 +945,6 @@ __global__ void __launch_bounds__(kThreads, MINB) k_vdetect(DemDev d, DemParams 
             int32_t* stash = d.stash + (size_t)i * p.kstash;
             if (!frozen) {
                 const float4 Pi = d.pos32[i];
-                const int nv = d.vl_len[i];
                 const int32_t* vl = d.vl + (size_t)i * p.kvl;
                 for (int v = lane; v < nv; v += kVLanes) {
                     const int j = vl[v];
