@@ -1864,19 +1864,21 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     d.vx[i] = vx + ax * dt;
     d.vy[i] = vy + ay * dt;
     d.vz[i] = vz + az * dt;
-    const double dq0 = -0.5 * (qx * wx + qy * wy + qz * wz);
-    const double dq1 = 0.5 * (qw * wx + qy * wz - qz * wy);
-    const double dq2 = 0.5 * (qw * wy + qx * wz + qz * wx);
-    const double dq3 = 0.5 * (qw * wz + qx * wy - qy * wx);
-    const double nw = qw + dq0, nx = qx + dq1, ny = qy + dq2, nz = qz + dq3;
+    // 𝐪 + Δ𝐪 with Δ𝐪 = ½ 𝛚 ⊗ 𝐪 (no dt, as the reference), the ½ folded into 𝛚
+    const double hx = 0.5 * wx, hy = 0.5 * wy, hz = 0.5 * wz;
+    const double nw = qw - qx * hx - qy * hy - qz * hz;
+    const double nx = qx + qw * hx + qy * hz - qz * hy;
+    const double ny = qy + qw * hy + qx * hz + qz * hx;
+    const double nz = qz + qw * hz + qx * hy - qy * hx;
     const double inq = rsqrt(nw * nw + nx * nx + ny * ny + nz * nz);
     d.qw[i] = nw * inq;
     d.qx[i] = nx * inq;
     d.qy[i] = ny * inq;
     d.qz[i] = nz * inq;
-    d.wx[i] = wx + M[0] * ii * dt;
-    d.wy[i] = wy + M[1] * ii * dt;
-    d.wz[i] = wz + M[2] * ii * dt;
+    const double iidt = ii * dt;
+    d.wx[i] = wx + M[0] * iidt;
+    d.wy[i] = wy + M[1] * iidt;
+    d.wz[i] = wz + M[2] * iidt;
     d.fx[i] = F[0];
     d.fy[i] = F[1];
     d.fz[i] = F[2];
