@@ -480,7 +480,7 @@ __device__ __forceinline__ void emit_rows(const DemDev& d, const DemParams& p, i
     if (len > 0) finish_row<L>(d, p, cur, r, start, lane);
 }
 
-// Shared memory of one 8-lane group of k_detect.
+// Shared memory of one 8-lane group of the pair search (k_search's detect phase).
 struct DetectShared {
     int nnew;
     int nvl;                  // neighbour-list entries found
@@ -866,7 +866,7 @@ __device__ __noinline__ bool in_cp_list(const DemDev& d, const SceneParams& S, i
 // `update_contacts!` from the neighbour lists, for the particles of scenes
 // that do not run the full search this step (four lanes per particle,
 // grid-stride over slots).  Survival of the current row is decided as in
-// k_detect; new contacts are the touching list partners that are not in the
+// the full search; new contacts are the touching list partners that are not in the
 // row.
 constexpr int kVLanes = 4;
 struct ListShared {
