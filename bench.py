@@ -73,8 +73,8 @@ INTEGRATE_BYTES_PER_PARTICLE = 13 * 8 * 2 + 4 * 8 + 6 * 8 + 3 * 8 * 2 + 8 + 4  #
 # FP32 position, next row bounds written, 4 list partners (index + FP32
 # position); the row rebuild adds the compaction bytes per surviving contact
 DETECT_BYTES_PER_PARTICLE = 1 + 8 + 4 + 16 + 8 + 4 * (4 + 16)
-# k_search (fused full search), k_vdetect (lists + rows), k_force, k_integrate
-KERNELS_PER_STEP = 4
+# k_search (contact update: full search or lists, next rows), k_force, k_integrate
+KERNELS_PER_STEP = 3
 # FP64-pipe instructions per unit (ncu sm__thread_inst_executed_pipe_fp64_pred_on.sum
 # per launch over the units it processed; profiles/k_force_fp64_bonded_cube_17576.md
 # and profiles/k_integrate_batched_64_scenes.md): the force kernel per bond, the
@@ -328,9 +328,9 @@ def run_batched(args, lib, quick: bool = False, dist=None) -> dict:
     plain = n_total / (plain_ms * 1e-3) if plain_ms > 0 else None
     peaks = load_peaks()
     force_bytes = bonded * FORCE_BYTES_BOND + (contacts - bonded) * FORCE_BYTES_HERTZ
-    alg = {"force": force_bytes, "search": n_total * BROADPHASE_BYTES_PER_PARTICLE,
+    alg = {"force": force_bytes,
            "integrate": n_total * INTEGRATE_BYTES_PER_PARTICLE,
-           "lists": n_total * DETECT_BYTES_PER_PARTICLE
+           "contacts": n_total * DETECT_BYTES_PER_PARTICLE
            + bonded * COMPACT_BYTES_BOND + (contacts - bonded) * COMPACT_BYTES_HERTZ}
     dom = max(ph, key=ph.get)
     roof = {"bound": "hbm", "kernel": dom, "unit": "GB/s", "peak": peaks["hbm_gbs"],
@@ -685,9 +685,8 @@ def main() -> None:
     n_bond = st["bonded"]
     force_bytes = n_bond * FORCE_BYTES_BOND + (c_now - n_bond) * FORCE_BYTES_HERTZ
     alg = {"force": force_bytes,
-           "search": sc.n * BROADPHASE_BYTES_PER_PARTICLE,
            "integrate": sc.n * INTEGRATE_BYTES_PER_PARTICLE,
-           "lists": sc.n * DETECT_BYTES_PER_PARTICLE
+           "contacts": sc.n * DETECT_BYTES_PER_PARTICLE
            + n_bond * COMPACT_BYTES_BOND + (c_now - n_bond) * COMPACT_BYTES_HERTZ}
     dom = max(ph, key=ph.get)
     dom_bytes = alg.get(dom)

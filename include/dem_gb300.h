@@ -197,12 +197,12 @@ int dem_step(DemHandle* h, int64_t nsteps);
 int dem_step_timed(DemHandle* h, int64_t nsteps, float* ms);
 
 /* One step launched phase by phase (no graph) with CUDA events between the
- * phases on the handle's stream.  phase_ms[0..3] (nphase >= 4; further
- * entries are set to 0) receive the device time of: the full pair search
- * (hash, bucket scan, scatter, canonical order, cp_list enumeration with
- * update_contacts!, next rows; it ends at once when no scene searches), the
- * neighbour-list contact update (with next rows), contact forces,
- * integration.
+ * phases on the handle's stream.  phase_ms[0..2] (nphase >= 3; further
+ * entries are set to 0) receive the device time of: the contact update (the
+ * full pair search of the scenes whose neighbour lists went stale — hash,
+ * bucket scan, scatter, canonical order, cp_list enumeration with
+ * update_contacts! — and the neighbour-list update of the others, with the
+ * next contact rows), contact forces, integration.
  * No counterpart in the reference: per-kernel timing for roofline reports. */
 int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase);
 

@@ -552,7 +552,6 @@ int flag_search(DemHandle* h, int s) {
 void record_step(DemHandle* h, int cur) {
     const int nxt = cur ^ 1;
     launch_search(h->d, h->p, cur, false, h->multi, false, h->shape, h->stream);
-    launch_lists(h->d, h->p, cur, h->multi, h->shape, h->stream);
     launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
     launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
 }
@@ -1304,7 +1303,7 @@ int dem_step_timed(DemHandle* h, int64_t nsteps, float* ms) {
 }
 
 int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
-    if (!h || !phase_ms || nphase < 4) return DEM_ERR_INVALID;
+    if (!h || !phase_ms || nphase < 3) return DEM_ERR_INVALID;
     for (int k = 0; k < nphase; ++k) phase_ms[k] = 0.f;
     if (h->n_cap == 0) return DEM_OK;
     TRY(ensure_encoding(h));
@@ -1312,22 +1311,20 @@ int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
         TRY(build_graphs(h));
         TRY(launch_inits(h));
     }
-    cudaEvent_t ev[5];
-    for (int k = 0; k < 5; ++k) CU(cudaEventCreate(&ev[k]));
+    cudaEvent_t ev[4];
+    for (int k = 0; k < 4; ++k) CU(cudaEventCreate(&ev[k]));
     const int cur = h->cur, nxt = cur ^ 1;
     cudaEventRecord(ev[0], h->stream);
     launch_search(h->d, h->p, cur, false, h->multi, false, h->shape, h->stream);
     cudaEventRecord(ev[1], h->stream);
-    launch_lists(h->d, h->p, cur, h->multi, h->shape, h->stream);
-    cudaEventRecord(ev[2], h->stream);
     launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
-    cudaEventRecord(ev[3], h->stream);
+    cudaEventRecord(ev[2], h->stream);
     launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
-    cudaEventRecord(ev[4], h->stream);
-    cudaError_t e = cudaEventSynchronize(ev[4]);
-    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+    cudaEventRecord(ev[3], h->stream);
+    cudaError_t e = cudaEventSynchronize(ev[3]);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
         e = cudaEventElapsedTime(&phase_ms[k], ev[k], ev[k + 1]);
-    for (int k = 0; k < 5; ++k) cudaEventDestroy(ev[k]);
+    for (int k = 0; k < 4; ++k) cudaEventDestroy(ev[k]);
     CU(e);
     h->cur = nxt;
     h->steps += 1;

@@ -1,9 +1,9 @@
 // dem_kernels.cu — the DEM step as hand-written CUDA for sm_103a.
 //
 // One step (the reference's `simulate!`, src/executor.jl:162-172) is
-//   k_search     the full pair search, one cooperative launch whose phases
-//                are separated by grid barriers (and which ends at once when
-//                no scene searches this step):
+//   k_search     the contact update, one cooperative launch whose phases
+//                are separated by grid barriers (the search phases run only
+//                for scenes whose neighbour lists went stale):
 //                  hash     cell, Morton bucket, octant; warp-aggregated counts
 //                  scan     exclusive scan of the occupied bucket range
 //                  scatter  counting-sort scatter (the counts return to zero,
@@ -13,8 +13,9 @@
 //                  detect   cp_list enumeration fused with update_contacts!:
 //                           existing contacts decide survival, new touching
 //                           pairs are found, neighbour lists are rebuilt
-//   k_vdetect    update_contacts! from the neighbour lists (scenes that do
-//                not search this step)
+//                  lists    update_contacts! from the neighbour lists for
+//                           the scenes that do not search this step (a
+//                           single-scene handle runs only this phase then)
 //                Both write each particle's next row where its contacts are
 //                decided (the rolling-array rebuild: survivors + new contacts
 //                sorted by j, placed by warp-aggregated atomics) and the
@@ -22,9 +23,10 @@
 //   k_force      resolve_collision! per contact (EBPM or Hertz-Mindlin)
 //   k_integrate  per particle: contact force gather in a fixed order,
 //                resolve_wall!, apply_body_force!, update!
-// All of it is captured once in a CUDA graph per contact-buffer parity.  The
-// standalone broad-phase kernels (k_hash, k_scan_excl, k_scatter, k_canon)
-// serve the cp_list inspection entry point.
+// All of it is captured once in a CUDA graph per contact-buffer parity (three
+// launches per step).  The standalone broad-phase kernels (k_hash,
+// k_scan_excl, k_scatter, k_canon) serve the cp_list inspection entry point;
+// the standalone list kernel (k_vdetect) is not on the step path.
 #include <type_traits>
 
 #include "dem_device.cuh"
@@ -689,158 +691,6 @@ __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p
     job.len = nkeep + job.nnew;
 }
 
-// ---------------------------------------------------------------------------
-// The full pair search fused into one cooperative launch.  Its phases are the
-// broad phase kernels above (hash, bucket scan, counting sort, canonical
-// order) and the cp_list enumeration, separated by grid barriers; every block
-// of a cooperative launch is resident, so the barriers cannot wait on a block
-// that has not started.  A step in which no scene searches ends at the first
-// check: a single-scene handle reads its one flag; an arena hashes (which also
-// records each slot's path) and ends when nothing was hashed.
-
-// Grid barrier: arrival counter and generation word; a block waits for the
-// generation to move on, with a bounded wait that raises kErrTimeout.
-__device__ __forceinline__ void grid_sync(DevCounters* c) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned int* gen = &c->bar_gen;
-        const unsigned int g = *gen;
-        __threadfence();
-        if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1) {
-            atomicExch(&c->bar_count, 0u);
-            __threadfence();
-            atomicAdd(&c->bar_gen, 1u);
-        } else {
-            for (unsigned long long it = 0; *gen == g; ++it) {
-                if (it > kSpinLimit) {
-                    raise_error(c, kErrTimeout);
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-}
-
-// Block-wide sum of one value per thread (kThreads threads).
-__device__ __forceinline__ unsigned long long block_sum(unsigned long long v,
-                                                        unsigned long long* red) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane_id() == 0) red[threadIdx.x >> 5] = v;
-    __syncthreads();
-    unsigned long long t = 0;
-#pragma unroll
-    for (int w = 0; w < kThreads / 32; ++w) t += red[w];
-    __syncthreads();
-    return t;
-}
-
-// Exclusive scan of cell_count[0, count) into cell_start (count = the
-// buckets up to this step's largest, as the standalone scan), in tiles of
-// kScanTile: tile sums, a barrier, then each tile's prefix from the sums.
-// Ends with a barrier.
-constexpr int kFusedItems = kScanTile / kThreads;
-__device__ void scan_phase(const DemDev& d, const DemParams& p, unsigned long long* red) {
-    // (values written by other blocks earlier in this launch are read past L1)
-    const long long lim = (long long)__ldcg(&d.ctr->bmax) + 1;
-    const long long count = lim < (long long)p.T ? lim : (long long)p.T;
-    const int ntiles = (int)((count + kScanTile - 1) / kScanTile);
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const long long base = (long long)t * kScanTile + (long long)threadIdx.x * kFusedItems;
-        unsigned long long v = 0;
-#pragma unroll 8
-        for (int k = 0; k < kFusedItems; ++k)
-            if (base + k < count) v += d.cell_count[base + k];
-        const unsigned long long tot = block_sum(v, red);
-        if (threadIdx.x == 0) d.tile_sums[t] = (uint32_t)tot;
-    }
-    grid_sync(d.ctr);
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        unsigned long long pre = 0;
-        for (int u = threadIdx.x; u < t; u += kThreads) pre += __ldcg(&d.tile_sums[u]);
-        pre = block_sum(pre, red);
-        const long long base = (long long)t * kScanTile + (long long)threadIdx.x * kFusedItems;
-        unsigned long long mine = 0;
-#pragma unroll 8
-        for (int k = 0; k < kFusedItems; ++k)
-            if (base + k < count) mine += d.cell_count[base + k];
-        // exclusive prefix of `mine` across the block
-        unsigned long long x = mine;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane_id() >= (unsigned)o) x += y;
-        }
-        if (lane_id() == 31) red[threadIdx.x >> 5] = x;
-        __syncthreads();
-        unsigned long long wpre = 0;
-        for (int w = 0; w < (int)(threadIdx.x >> 5); ++w) wpre += red[w];
-        __syncthreads();
-        unsigned long long run = pre + wpre + x - mine;
-#pragma unroll 8
-        for (int k = 0; k < kFusedItems; ++k) {
-            if (base + k < count) {
-                d.cell_start[base + k] = (uint32_t)run;
-                run += d.cell_count[base + k];
-            }
-        }
-        if (t == ntiles - 1 && threadIdx.x == kThreads - 1) d.cell_start[count] = (uint32_t)run;
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) d.ctr->cell_limit = (unsigned int)count;
-    grid_sync(d.ctr);
-}
-
-template <bool INIT, bool MULTI, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB) k_search(DemDev d, DemParams p, int cur, int all) {
-    __shared__ DetectShared sh[kThreads / kLanes];
-    __shared__ unsigned long long red[kThreads / 32];
-    dep_begin();
-    if (!MULTI && !(all || INIT || d.sflags[cur][0] != 0u)) return;
-    const int stride = gridDim.x * kThreads;
-    const int wbase = blockIdx.x * kThreads + (int)(threadIdx.x & ~31u);
-    if (MULTI && blockIdx.x == 0 && threadIdx.x == 0) d.ctr->hashed[cur ^ 1] = 0u;
-    // hash (`cell`, `hashcode`, `neighbors`, `count_particles!`)
-    for (int i0 = wbase; i0 < p.n; i0 += stride) {
-        const int i = i0 + (int)lane_id();
-        bool act = false;
-        uint32_t b = 0;
-        if (i < p.n) hash_particle<MULTI>(d, p, cur, all, i, act, b);
-        hash_count(d, act, b, MULTI ? &d.ctr->hashed[cur] : nullptr);
-    }
-    grid_sync(d.ctr);
-    if (MULTI && *(volatile unsigned int*)&d.ctr->hashed[cur] == 0u) return;
-    // `accumulate!` of the bucket counts
-    scan_phase(d, p, red);
-    // `get_particle_id!`
-    for (int i0 = wbase; i0 < p.n; i0 += stride) scatter_warp(d, p, i0 + (int)lane_id());
-    grid_sync(d.ctr);
-    // canonical order; this step's bucket maximum is no longer read
-    const uint32_t lim = __ldcg(&d.ctr->cell_limit);
-    const int count = (int)__ldcg(&d.cell_start[lim]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) d.ctr->bmax = 0u;
-    for (int k = blockIdx.x * kThreads + (int)threadIdx.x; k < count; k += stride)
-        canon_slot<MULTI>(d, p, cur, k);
-    grid_sync(d.ctr);
-    // cp_list enumeration with update_contacts! / init_bonds!, then the next
-    // rows; a warp's four groups move together (the rows are placed per warp)
-    const int lane = threadIdx.x & (kLanes - 1);
-    const int g = threadIdx.x / kLanes;
-    const unsigned gmask = 0xffu << (lane_id() & ~7u);
-    const int gwarp = (int)(threadIdx.x >> 5) * (32 / kLanes);  // the warp's first group
-    for (int k0 = blockIdx.x * (kThreads / kLanes) + gwarp; k0 < count;
-         k0 += gridDim.x * (kThreads / kLanes)) {
-        const int k = k0 + (g - gwarp);
-        RowJob job{};
-        const bool active = k < count;
-        if (active) detect_group<INIT, MULTI>(d, p, cur, k, lane, gmask, lim, sh[g], job);
-        emit_rows<kLanes>(d, p, cur, active, job, lane);
-        __syncwarp();
-    }
-}
-
 // cp_list membership of the pair (i, j), i < j, from the current positions:
 // j's bucket among i's 8 octant buckets, in the reference's cells and table.
 template <bool MULTI>
@@ -873,16 +723,15 @@ struct ListShared {
     int nnew;
     int row[kRowCache];
 };
-template <bool MULTI, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB) k_vdetect(DemDev d, DemParams p, int cur) {
-    __shared__ ListShared sh[kThreads / kVLanes];
-    dep_begin(p.dep == 2);
+// The list update over slots [0, n), grid-stride (every thread of the launch
+// calls it; a warp's groups move together).
+template <bool MULTI>
+__device__ __forceinline__ void list_phase(const DemDev& d, const DemParams& p, int cur,
+                                           ListShared* sh) {
     const int lane = threadIdx.x & (kVLanes - 1);
     const int g = threadIdx.x / kVLanes;
     const unsigned gmask = 0xfu << (lane_id() & ~3u);
     const ContactSoA o = d.c[cur];
-    // a single-scene handle decides from its one flag
-    if (!MULTI && d.sflags[cur][0] != 0u) return;
     // a warp's eight groups move together (their rows are placed per warp)
     const int gwarp = (int)(threadIdx.x >> 5) * (32 / kVLanes);
     for (int i0 = blockIdx.x * (kThreads / kVLanes) + gwarp; i0 < p.n;
@@ -996,6 +845,176 @@ __global__ void __launch_bounds__(kThreads, MINB) k_vdetect(DemDev d, DemParams 
             job.len = nkeep + job.nnew;
         }
         emit_rows<kVLanes>(d, p, cur, active, job, lane);
+        __syncwarp();
+    }
+}
+
+template <bool MULTI, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_vdetect(DemDev d, DemParams p, int cur) {
+    __shared__ ListShared sh[kThreads / kVLanes];
+    dep_begin(p.dep == 2);
+    // a single-scene handle decides from its one flag
+    if (!MULTI && d.sflags[cur][0] != 0u) return;
+    list_phase<MULTI>(d, p, cur, sh);
+}
+
+// ---------------------------------------------------------------------------
+// The contact update of a step in one cooperative launch: the full pair
+// search (the broad phase kernels above: hash, bucket scan, counting sort,
+// canonical order; then the cp_list enumeration), separated by grid
+// barriers, and the neighbour-list update of the scenes that do not search.
+// Every block of a cooperative launch is resident, so the barriers cannot
+// wait on a block that has not started.  A single-scene handle whose lists
+// are valid runs the list update only; an arena hashes (which also records
+// each slot's path), runs the list update of its list scenes, and ends there
+// when nothing was hashed.
+
+// Grid barrier: arrival counter and generation word; a block waits for the
+// generation to move on, with a bounded wait that raises kErrTimeout.
+__device__ __forceinline__ void grid_sync(DevCounters* c) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* gen = &c->bar_gen;
+        const unsigned int g = *gen;
+        __threadfence();
+        if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1) {
+            atomicExch(&c->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&c->bar_gen, 1u);
+        } else {
+            for (unsigned long long it = 0; *gen == g; ++it) {
+                if (it > kSpinLimit) {
+                    raise_error(c, kErrTimeout);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// Block-wide sum of one value per thread (kThreads threads).
+__device__ __forceinline__ unsigned long long block_sum(unsigned long long v,
+                                                        unsigned long long* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane_id() == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    unsigned long long t = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+    __syncthreads();
+    return t;
+}
+
+// Exclusive scan of cell_count[0, count) into cell_start (count = the
+// buckets up to this step's largest, as the standalone scan), in tiles of
+// kScanTile: tile sums, a barrier, then each tile's prefix from the sums.
+// Ends with a barrier.
+constexpr int kFusedItems = kScanTile / kThreads;
+__device__ void scan_phase(const DemDev& d, const DemParams& p, unsigned long long* red) {
+    // (values written by other blocks earlier in this launch are read past L1)
+    const long long lim = (long long)__ldcg(&d.ctr->bmax) + 1;
+    const long long count = lim < (long long)p.T ? lim : (long long)p.T;
+    const int ntiles = (int)((count + kScanTile - 1) / kScanTile);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const long long base = (long long)t * kScanTile + (long long)threadIdx.x * kFusedItems;
+        unsigned long long v = 0;
+#pragma unroll 8
+        for (int k = 0; k < kFusedItems; ++k)
+            if (base + k < count) v += d.cell_count[base + k];
+        const unsigned long long tot = block_sum(v, red);
+        if (threadIdx.x == 0) d.tile_sums[t] = (uint32_t)tot;
+    }
+    grid_sync(d.ctr);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        unsigned long long pre = 0;
+        for (int u = threadIdx.x; u < t; u += kThreads) pre += __ldcg(&d.tile_sums[u]);
+        pre = block_sum(pre, red);
+        const long long base = (long long)t * kScanTile + (long long)threadIdx.x * kFusedItems;
+        unsigned long long mine = 0;
+#pragma unroll 8
+        for (int k = 0; k < kFusedItems; ++k)
+            if (base + k < count) mine += d.cell_count[base + k];
+        // exclusive prefix of `mine` across the block
+        unsigned long long x = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane_id() >= (unsigned)o) x += y;
+        }
+        if (lane_id() == 31) red[threadIdx.x >> 5] = x;
+        __syncthreads();
+        unsigned long long wpre = 0;
+        for (int w = 0; w < (int)(threadIdx.x >> 5); ++w) wpre += red[w];
+        __syncthreads();
+        unsigned long long run = pre + wpre + x - mine;
+#pragma unroll 8
+        for (int k = 0; k < kFusedItems; ++k) {
+            if (base + k < count) {
+                d.cell_start[base + k] = (uint32_t)run;
+                run += d.cell_count[base + k];
+            }
+        }
+        if (t == ntiles - 1 && threadIdx.x == kThreads - 1) d.cell_start[count] = (uint32_t)run;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.ctr->cell_limit = (unsigned int)count;
+    grid_sync(d.ctr);
+}
+
+template <bool INIT, bool MULTI, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_search(DemDev d, DemParams p, int cur, int all) {
+    __shared__ DetectShared sh[kThreads / kLanes];
+    __shared__ ListShared lsh[kThreads / kVLanes];
+    __shared__ unsigned long long red[kThreads / 32];
+    dep_begin();
+    if (!MULTI && !(all || INIT || d.sflags[cur][0] != 0u)) {
+        list_phase<false>(d, p, cur, lsh);  // the scene tests its neighbour lists
+        return;
+    }
+    const int stride = gridDim.x * kThreads;
+    const int wbase = blockIdx.x * kThreads + (int)(threadIdx.x & ~31u);
+    if (MULTI && blockIdx.x == 0 && threadIdx.x == 0) d.ctr->hashed[cur ^ 1] = 0u;
+    // hash (`cell`, `hashcode`, `neighbors`, `count_particles!`)
+    for (int i0 = wbase; i0 < p.n; i0 += stride) {
+        const int i = i0 + (int)lane_id();
+        bool act = false;
+        uint32_t b = 0;
+        if (i < p.n) hash_particle<MULTI>(d, p, cur, all, i, act, b);
+        hash_count(d, act, b, MULTI ? &d.ctr->hashed[cur] : nullptr);
+    }
+    grid_sync(d.ctr);
+    // the scenes that test their neighbour lists (path bytes written above):
+    // independent of the search below (other particles and rows)
+    if (MULTI && !INIT) list_phase<true>(d, p, cur, lsh);
+    if (MULTI && *(volatile unsigned int*)&d.ctr->hashed[cur] == 0u) return;
+    // `accumulate!` of the bucket counts
+    scan_phase(d, p, red);
+    // `get_particle_id!`
+    for (int i0 = wbase; i0 < p.n; i0 += stride) scatter_warp(d, p, i0 + (int)lane_id());
+    grid_sync(d.ctr);
+    // canonical order; this step's bucket maximum is no longer read
+    const uint32_t lim = __ldcg(&d.ctr->cell_limit);
+    const int count = (int)__ldcg(&d.cell_start[lim]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.ctr->bmax = 0u;
+    for (int k = blockIdx.x * kThreads + (int)threadIdx.x; k < count; k += stride)
+        canon_slot<MULTI>(d, p, cur, k);
+    grid_sync(d.ctr);
+    // cp_list enumeration with update_contacts! / init_bonds!, then the next
+    // rows; a warp's four groups move together (the rows are placed per warp)
+    const int lane = threadIdx.x & (kLanes - 1);
+    const int g = threadIdx.x / kLanes;
+    const unsigned gmask = 0xffu << (lane_id() & ~7u);
+    const int gwarp = (int)(threadIdx.x >> 5) * (32 / kLanes);  // the warp's first group
+    for (int k0 = blockIdx.x * (kThreads / kLanes) + gwarp; k0 < count;
+         k0 += gridDim.x * (kThreads / kLanes)) {
+        const int k = k0 + (g - gwarp);
+        RowJob job{};
+        const bool active = k < count;
+        if (active) detect_group<INIT, MULTI>(d, p, cur, k, lane, gmask, lim, sh[g], job);
+        emit_rows<kLanes>(d, p, cur, active, job, lane);
         __syncwarp();
     }
 }

@@ -240,7 +240,7 @@ class GlobalData:
               "dem_step_timed")
         return float(ms.value)
 
-    PHASES = ("search", "lists", "force", "integrate")
+    PHASES = ("contacts", "force", "integrate")
 
     def simulate_profiled(self) -> dict:
         """One step launched phase by phase; device milliseconds per phase."""
