@@ -114,6 +114,8 @@ NCU_TRAFFIC = {
     ("c2", "force"): (6.419456e6, 17576),          # k_force<double>
     ("c4", "force"): (145.409024e6, 431416),       # k_force<float>
     ("c4", "integrate"): (186.321408e6, 431416),   # k_integrate (FP32 gather)
+    ("c4", "contacts"): (150.255616e6, 431416),    # k_search, list step
+    ("c2", "contacts"): (6.824448e6, 17576),       # k_search, list step
 }
 
 
