@@ -422,6 +422,7 @@ int allocate(DemHandle* h) {
         TRY(dalloc(h, &d.c[b].ci, cap));
         TRY(dalloc(h, &d.c[b].cj, cap));
         TRY(dalloc(h, &d.c[b].fl, cap));
+        TRY(dalloc(h, &d.c[b].src, cap));
         for (int f = 0; f < 15; ++f) TRY(dalloc(h, &d.c[b].f[f], cap));
         TRY(dalloc(h, &d.row_start[b], n));
         TRY(dalloc(h, &d.row_len[b], n));

@@ -53,6 +53,7 @@ struct ContactSoA {
     int32_t* ci;
     int32_t* cj;
     uint32_t* fl;
+    int32_t* src;   // slot of the contact in the other buffer (its carried state), -1 new
     double* f[15];  // kx ky kz | Fx Fy Fz | tix tiy tiz | tjx tjy tjz | sx sy sz
 };
 enum ContactField { CK = 0, CF = 3, CTI = 6, CTJ = 9, CS = 12 };

@@ -411,48 +411,35 @@ __device__ __forceinline__ void add_incoming_entry(const DemDev& d, const DemPar
 
 // Writes the row of job `r` at [start, start + r.len) of buffer cur^1 (L
 // lanes share it) and records, for a stepping scene, each contact in its
-// partner's incoming list (the force gather's order).  A stepping contact
-// carries only the state the next force pass reads: a bond its accumulated
-// 𝐅, 𝛕ᵢ, 𝛕ⱼ, a Hertz contact its 𝐬 (the force pass rewrites 𝐤 and 𝐅; a
-// bond's 𝐬 and a Hertz contact's torques are zero, reported as such by the
-// host).  Contacts of scenes that do not step keep every field.
+// partner's incoming list (the force gather's order).  A stepping contact is
+// written as its ids, flags and `src`, its slot in buffer cur: the force pass
+// reads the carried state there (a bond's accumulated 𝐅, 𝛕ᵢ, 𝛕ⱼ, a Hertz
+// contact's 𝐬) and writes the new state here, so the state is not copied
+// (a bond's 𝐬 and a Hertz contact's torques are zero, reported as such by
+// the host).  Contacts of scenes that do not step keep every field.
 template <int L>
 __device__ __forceinline__ void finish_row(const DemDev& d, const DemParams& p, int cur,
                                            const RowJob& r, int start, int lane) {
     const ContactSoA o = d.c[cur];
     const ContactSoA w = d.c[cur ^ 1];
     const int32_t* st = d.stash + (size_t)r.i * p.kstash;
+    const bool stepping = r.mode == kModeStep;
     for (int e = r.e0 + lane; e < r.e1; e += L) {
         if (!d.keep[e]) continue;
         const int j = o.cj[e];
         const uint32_t fl = o.fl[e];
-        const int kind = r.mode != kModeStep ? 0 : ((fl & kBonded) ? 1 : 2);
-        // a stepping contact's carried state is loaded before its slot is
-        // computed (the loads overlap the rank loops)
-        double v[9];
-        if (kind == 1) {
-#pragma unroll
-            for (int f = 0; f < 9; ++f) v[f] = o.f[CF + f][e];
-        } else if (kind == 2) {
-#pragma unroll
-            for (int f = 0; f < 3; ++f) v[f] = o.f[CS + f][e];
-        }
         int pos = start;
         for (int q = r.e0; q < e; ++q) pos += d.keep[q];
         for (int u = 0; u < r.nnew; ++u) pos += st[u] < j ? 1 : 0;
         w.ci[pos] = r.i;
         w.cj[pos] = j;
         w.fl[pos] = fl;
-        if (kind == 0) {
+        w.src[pos] = stepping ? e : -1;
+        if (!stepping) {
             for (int f = 0; f < 15; ++f) w.f[f][pos] = o.f[f][e];
-        } else if (kind == 1) {
-#pragma unroll
-            for (int f = 0; f < 9; ++f) w.f[CF + f][pos] = v[f];
         } else {
-#pragma unroll
-            for (int f = 0; f < 3; ++f) w.f[CS + f][pos] = v[f];
+            add_incoming_entry(d, p, j, pos, r.i);
         }
-        if (r.mode == kModeStep) add_incoming_entry(d, p, j, pos, r.i);
     }
     for (int u = lane; u < r.nnew; u += L) {
         const int j = st[u];
@@ -461,9 +448,13 @@ __device__ __forceinline__ void finish_row(const DemDev& d, const DemParams& p, 
         w.ci[pos] = r.i;
         w.cj[pos] = j;
         w.fl[pos] = r.mode == kModeInit ? (kActive | kBonded) : kActive;
+        w.src[pos] = -1;  // a new contact: zero carried state
+        if (stepping) {
+            add_incoming_entry(d, p, j, pos, r.i);
+        } else {
 #pragma unroll
-        for (int f = 0; f < 15; ++f) w.f[f][pos] = 0.0;
-        if (r.mode == kModeStep) add_incoming_entry(d, p, j, pos, r.i);
+            for (int f = 0; f < 15; ++f) w.f[f][pos] = 0.0;
+        }
     }
 }
 
@@ -1284,8 +1275,8 @@ __device__ __forceinline__ Vec3<float> rot_t32(const Frame32& R, Vec3<float> v) 
 // (L² - (rᵢ+rⱼ)²)/(L + rᵢ + rⱼ) with the numerator in FP64, which keeps the
 // overlap's relative error at FP32 rounding even though L is FP32.
 __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
-                                        const ContactSoA& w, int c, uint32_t fl, int i, int j,
-                                        int sc, size_t cap) {
+                                        const ContactSoA& w, const ContactSoA& o, int sidx, int c,
+                                        uint32_t fl, int i, int j, int sc, size_t cap) {
     const double kix = d.px[i], kiy = d.py[i], kiz = d.pz[i];
     const double dxd = d.px[j] - kix, dyd = d.py[j] - kiy, dzd = d.pz[j] - kiz;
     const float dx = d2f(dxd), dy = d2f(dyd), dz = d2f(dzd);
@@ -1326,11 +1317,12 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
         float2 Fp[3], tip[3], tjp[3];
         const float dF[3] = {dFx, dFy, dFz}, dti[3] = {dtix, dtiy, dtiz};
         const float dtj[3] = {dtjx, dtjy, dtjz};
+        const float2 z2 = make_float2(0.0f, 0.0f);
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            Fp[q] = pair_add(pair_col(w, CF + q)[c], dF[q]);
-            tip[q] = pair_add(pair_col(w, CTI + q)[c], dti[q]);
-            tjp[q] = pair_add(pair_col(w, CTJ + q)[c], dtj[q]);
+        for (int q = 0; q < 3; ++q) {  // carried state from the other buffer
+            Fp[q] = pair_add(sidx >= 0 ? pair_col(o, CF + q)[sidx] : z2, dF[q]);
+            tip[q] = pair_add(sidx >= 0 ? pair_col(o, CTI + q)[sidx] : z2, dti[q]);
+            tjp[q] = pair_add(sidx >= 0 ? pair_col(o, CTJ + q)[sidx] : z2, dtj[q]);
         }
         const Vec3<float> Ff{Fp[0].x, Fp[1].x, Fp[2].x};
         const Vec3<float> tif{tip[0].x, tip[1].x, tip[2].x};
@@ -1386,7 +1378,7 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
         if (gn < 0.0f || gt < 0.0f)
             atomicAdd(&d.sctr[sc].warn_damp, (unsigned long long)((gn < 0.0f) + (gt < 0.0f)));
         // 𝐬 += (0, vc₂, vc₃)·dt in FP64 (the normal component stays)
-        Vec3<double> s = ld3(w.f, CS, c);
+        Vec3<double> s = sidx >= 0 ? ld3(o.f, CS, sidx) : Vec3<double>{0.0, 0.0, 0.0};
         s = {s.x, s.y + f2d(vc.y * SP.f_dt), s.z + f2d(vc.z * SP.f_dt)};
         const float F1 = -kn * gap - gn * vc.x;
         const Vec3<float> Ft{-kt * d2f(s.x), -kt * d2f(s.y), -kt * d2f(s.z)};
@@ -1437,10 +1429,11 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
 // Hertz and bond paths (T = float, via force32).
 template <typename T>
 __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& SP,
-                                            const ContactSoA& w, int c, uint32_t fl, int i, int j,
-                                            int sc, size_t cap) {
+                                            const ContactSoA& w, const ContactSoA& o, int c,
+                                            uint32_t fl, int i, int j, int sc, size_t cap) {
+    const int sidx = w.src[c];  // carried state in the other buffer (-1: new, zero)
     if constexpr (std::is_same<T, float>::value) {
-        force32(d, SP, w, c, fl, i, j, sc, cap);
+        force32(d, SP, w, o, sidx, c, fl, i, j, sc, cap);
         return;
     }
     const double dt = SP.dt;
@@ -1476,7 +1469,10 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
         const T ay_ = -k3 * D.z + kp * Sv.y, az_ = k3 * D.y + kp * Sv.z;
         const T dtix = k4 * Q.x, dtiy = ay_ + km * Q.y, dtiz = az_ + km * Q.z;
         const T dtjx = -k4 * Q.x, dtjy = ay_ - km * Q.y, dtjz = az_ - km * Q.z;
-        Vec3<double> Fi = ld3(w.f, CF, c), ti = ld3(w.f, CTI, c), tj = ld3(w.f, CTJ, c);
+        const Vec3<double> z3{0.0, 0.0, 0.0};
+        Vec3<double> Fi = sidx >= 0 ? ld3(o.f, CF, sidx) : z3;
+        Vec3<double> ti = sidx >= 0 ? ld3(o.f, CTI, sidx) : z3;
+        Vec3<double> tj = sidx >= 0 ? ld3(o.f, CTJ, sidx) : z3;
         Fi = {Fi.x + (double)dFx, Fi.y + (double)dFy, Fi.z + (double)dFz};
         ti = {ti.x + (double)dtix, ti.y + (double)dtiy, ti.z + (double)dtiz};
         tj = {tj.x + (double)dtjx, tj.y + (double)dtjy, tj.z + (double)dtjz};
@@ -1521,7 +1517,7 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
         const T gt = (T)SP.pp_cgt * root;
         if (gn < (T)0 || gt < (T)0)
             atomicAdd(&d.sctr[sc].warn_damp, (unsigned long long)((gn < (T)0) + (gt < (T)0)));
-        Vec3<double> s = ld3(w.f, CS, c);
+        Vec3<double> s = sidx >= 0 ? ld3(o.f, CS, sidx) : Vec3<double>{0.0, 0.0, 0.0};
         s = {s.x + (double)vc.x * 0.0, s.y + (double)vc.y * dt, s.z + (double)vc.z * dt};
         const T F1 = -kn * tgap - gn * vc.x;
         const Vec3<T> Ft{-kt * (T)s.x, -kt * (T)s.y, -kt * (T)s.z};
@@ -1558,6 +1554,7 @@ template <typename T, bool MULTI>
 __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, int nxt) {
     const int C = min((int)d.ctr->row_alloc[nxt], p.cap);
     const ContactSoA w = d.c[nxt];
+    const ContactSoA o = d.c[nxt ^ 1];
     const int stride = gridDim.x * blockDim.x;
     const size_t cap = (size_t)p.cap;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += stride) {
@@ -1565,7 +1562,7 @@ __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, 
         const int i = w.ci[c], j = w.cj[c];
         const int sc = slot_scene<MULTI>(d, i);
         if (MULTI && (sc < 0 || d.sp[sc].mode != kModeStep)) continue;
-        contact_one<T>(d, scene_rec<MULTI>(d, p, sc), w, c, fl, i, j, sc, cap);
+        contact_one<T>(d, scene_rec<MULTI>(d, p, sc), w, o, c, fl, i, j, sc, cap);
     }
 }
 
