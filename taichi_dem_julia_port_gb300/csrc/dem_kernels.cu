@@ -18,9 +18,10 @@
 //                           single-scene handle runs only this phase then)
 //                Both write each particle's next row where its contacts are
 //                decided (the rolling-array rebuild: survivors + new contacts
-//                sorted by j, placed by warp-aggregated atomics) and the
-//                incoming-contact lists for the force gather.
-//   k_force      resolve_collision! per contact (EBPM or Hertz-Mindlin)
+//                sorted by j, placed by warp-aggregated atomics).
+//   k_force      resolve_collision! per contact (EBPM or Hertz-Mindlin), and
+//                each contact's entry in its partner's incoming list (the
+//                integrator's gather)
 //   k_integrate  per particle: contact force gather in a fixed order,
 //                resolve_wall!, apply_body_force!, update!
 // All of it is captured once in a CUDA graph per contact-buffer parity (three
@@ -410,8 +411,7 @@ __device__ __forceinline__ void add_incoming_entry(const DemDev& d, const DemPar
 }
 
 // Writes the row of job `r` at [start, start + r.len) of buffer cur^1 (L
-// lanes share it) and records, for a stepping scene, each contact in its
-// partner's incoming list (the force gather's order).  A stepping contact is
+// lanes share it).  A stepping contact is
 // written as its ids, flags and `src`, its slot in buffer cur: the force pass
 // reads the carried state there (a bond's accumulated 𝐅, 𝛕ᵢ, 𝛕ⱼ, a Hertz
 // contact's 𝐬) and writes the new state here, so the state is not copied
@@ -435,11 +435,8 @@ __device__ __forceinline__ void finish_row(const DemDev& d, const DemParams& p, 
         w.cj[pos] = j;
         w.fl[pos] = fl;
         w.src[pos] = stepping ? e : -1;
-        if (!stepping) {
+        if (!stepping)
             for (int f = 0; f < 15; ++f) w.f[f][pos] = o.f[f][e];
-        } else {
-            add_incoming_entry(d, p, j, pos, r.i);
-        }
     }
     for (int u = lane; u < r.nnew; u += L) {
         const int j = st[u];
@@ -449,9 +446,7 @@ __device__ __forceinline__ void finish_row(const DemDev& d, const DemParams& p, 
         w.cj[pos] = j;
         w.fl[pos] = r.mode == kModeInit ? (kActive | kBonded) : kActive;
         w.src[pos] = -1;  // a new contact: zero carried state
-        if (stepping) {
-            add_incoming_entry(d, p, j, pos, r.i);
-        } else {
+        if (!stepping) {
 #pragma unroll
             for (int f = 0; f < 15; ++f) w.f[f][pos] = 0.0;
         }
@@ -788,7 +783,8 @@ __device__ __forceinline__ void list_phase(const DemDev& d, const DemParams& p, 
                 const int32_t* vl = d.vl + (size_t)i * p.kvl;
                 for (int v = lane; v < nv; v += kVLanes) {
                     const int j = vl[v];
-                    if (!maybe_touching32(Pi, d.pos32[j])) continue;
+                    // a partner already in the row (a bond, a Hertz contact)
+                    // needs no position: the row is checked first
                     bool found = false;
                     if (cached) {
                         for (int t = 0; t < e1 - e0 && !found; ++t) found = sh[g].row[t] == j;
@@ -797,6 +793,7 @@ __device__ __forceinline__ void list_phase(const DemDev& d, const DemParams& p, 
                             found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
                     }
                     if (found) continue;
+                    if (!maybe_touching32(Pi, d.pos32[j])) continue;
                     if (!touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j], d.pz[j], d.r[i],
                                      d.r[j]))
                         continue;
@@ -1562,6 +1559,9 @@ __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, 
         const int i = w.ci[c], j = w.cj[c];
         const int sc = slot_scene<MULTI>(d, i);
         if (MULTI && (sc < 0 || d.sp[sc].mode != kModeStep)) continue;
+        // the contact in its partner's incoming list (the integrator's gather
+        // sorts the list by owner, so the order of registration is free)
+        add_incoming_entry(d, p, j, c, i);
         contact_one<T>(d, scene_rec<MULTI>(d, p, sc), w, o, c, fl, i, j, sc, cap);
     }
 }
