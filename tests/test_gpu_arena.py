@@ -359,3 +359,26 @@ def test_state_buffers_loop(gpu):
     np.testing.assert_array_equal(g.particles()["vel"], expect)
     buf.close()
     g.close()
+
+
+@pytest.mark.slow
+def test_full_size_pour_properties(gpu):
+    """The 2,000,000-sphere pour at full size, FP32 force mode: two runs are
+    bit-identical, and the neighbour-list schedule gives the results of a
+    full pair search every step."""
+    sc = scenes.c3()
+    steps = 12
+    runs = []
+    for skin in (0.9, 0.9, 0.0):
+        g = GlobalData(sc.cfg, sc.particles, precision="fp32")
+        g.set_skin_factor(skin)
+        g.simulate(steps)
+        st = g.stats()
+        assert st["error"] == 0
+        runs.append((g.particles(forces=False), st))
+        g.close()
+    for k in ("pos", "vel", "omega", "quat"):
+        np.testing.assert_array_equal(runs[0][0][k], runs[1][0][k], err_msg=f"rerun {k}")
+        np.testing.assert_array_equal(runs[0][0][k], runs[2][0][k], err_msg=f"lists {k}")
+    assert runs[2][1]["full_searches"] == steps
+    assert runs[0][1]["full_searches"] < steps
