@@ -463,6 +463,30 @@ def main_served(args, lib, ws, rank, dist=None) -> None:
         print(json.dumps(line), flush=True)
 
 
+def host_link(nbytes: int, reps: int = 20) -> dict:
+    """Copy-engine bandwidth of one page-locked buffer of `nbytes` to and from
+    the device (CUDA events around `reps` copies): what an exchange of that
+    size can reach over this host link."""
+    import torch
+    n = max(nbytes // 8, 1)
+    h = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    d = torch.empty(n, dtype=torch.float64, device="cuda")
+    out = {}
+    for name, f in (("h2d_gbs", lambda: d.copy_(h, non_blocking=True)),
+                    ("d2h_gbs", lambda: h.copy_(d, non_blocking=True))):
+        for _ in range(3):
+            f()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            f()
+        e1.record()
+        torch.cuda.synchronize()
+        out[name] = 8 * n * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    return out
+
+
 def max_over_ranks(x: float, dist, device: str = "cuda") -> float:
     """The largest value of x over the ranks (one all-reduce); x itself with
     no process group."""
@@ -724,6 +748,11 @@ def main() -> None:
     e2e = {"value": ws * sc.n * args.e2e_steps / e2e_s, "unit": "particle-steps/s",
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
            "steps": args.e2e_steps, "ms_per_step": 1e3 * e2e_s / args.e2e_steps}
+    # the host link bounds the exchange: one step plus one copy each way
+    link = host_link(int(h2d))
+    e2e["host_link"] = link
+    e2e["bound_ms_per_step"] = ms_per_step + 1e3 * h2d * (1 / link["h2d_gbs"] +
+                                                          1 / link["d2h_gbs"]) / 1e9
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

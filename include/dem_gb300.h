@@ -276,7 +276,8 @@ int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
                       DemParticleState* out);
 
 /* Page-locked host memory for state buffers (cudaMallocHost / cudaFreeHost),
- * for callers without a CUDA runtime of their own. */
+ * for callers without a CUDA runtime of their own.  The library remembers
+ * these ranges, so exchanges with them skip the per-buffer pointer query. */
 int dem_host_alloc(int64_t bytes, void** out);
 int dem_host_free(void* p);
 

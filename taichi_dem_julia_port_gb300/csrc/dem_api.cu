@@ -8,6 +8,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <iterator>
+#include <map>
+#include <mutex>
 #include <numeric>
 #include <vector>
 
@@ -353,6 +356,7 @@ struct DemHandle {
     double* xfer = nullptr;    // device staging: particle records in the host's layout
     int64_t xfer_n = 0;        // doubles
     int* err_host = nullptr;   // page-locked copy of the device error word
+    int* err_dev = nullptr;    // its device address
 };
 
 #define CU(expr)                                                                            \
@@ -466,6 +470,7 @@ void free_all(DemHandle* h) {
     h->xfer = nullptr;
     if (h->err_host) cudaFreeHost(h->err_host);
     h->err_host = nullptr;
+    h->err_dev = nullptr;
 }
 
 // Default launch shape: blocks of at most 256 threads, small enough that a
@@ -747,9 +752,31 @@ int xfer_buffer(DemHandle* h, int64_t doubles, double** out) {
     return DEM_OK;
 }
 
+// Page-locked ranges from dem_host_alloc: host base -> (bytes, device base),
+// so that an exchange with them needs no pointer query.
+struct HostRanges {
+    std::mutex mu;
+    std::map<uintptr_t, std::pair<size_t, uintptr_t>> r;
+};
+HostRanges& host_ranges() {
+    static HostRanges* h = new HostRanges;  // never destroyed: used at exit by frees
+    return *h;
+}
+
 // The device address of a caller buffer the GPU can access in place
 // (page-locked host memory, or device memory), else nullptr.
 double* device_view(const void* p) {
+    {
+        HostRanges& H = host_ranges();
+        std::lock_guard<std::mutex> lk(H.mu);
+        const uintptr_t u = reinterpret_cast<uintptr_t>(p);
+        auto it = H.r.upper_bound(u);
+        if (it != H.r.begin()) {
+            --it;
+            if (u - it->first < it->second.first)
+                return reinterpret_cast<double*>(it->second.second + (u - it->first));
+        }
+    }
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
@@ -767,29 +794,27 @@ double* device_view(const void* p) {
 // library's staging copy with one cudaMemcpyAsync each.  Synchronises unless
 // `sync` is false (uploads only: a pageable buffer is free once its copy call
 // returns, a device-accessible one once the stream has passed the kernel);
-// with `error`, also returns the device error word as of the exchange.
+// with `error`, also returns the device error word as of the exchange (copied
+// by the kernel).  `posf` >= 0 (uploads to a single-scene handle): field posf
+// holds positions; the kernel also refreshes the FP32 positions and, with
+// `fb` 0 or 1, flags a full search when a particle left its skin.
 int exchange(DemHandle* h, int64_t p0, int64_t n, const int* k, double* const* host,
              double* const (*cols)[4], int nfields, bool to_cols, int* error = nullptr,
-             bool sync = true) {
-    if (error) {
-        if (!h->err_host) CU(cudaMallocHost(&h->err_host, 64));
-        CU(cudaMemcpyAsync(h->err_host, &h->d.ctr->error, sizeof(int), cudaMemcpyDeviceToHost,
-                           h->stream));
-    }
-    if (n <= 0) {
-        if (error) {
-            CU(cudaStreamSynchronize(h->stream));
-            *error = *h->err_host;
-        }
-        return DEM_OK;
+             bool sync = true, int posf = -1, int fb = -1) {
+    if (error && !h->err_host) {
+        CU(cudaMallocHost(&h->err_host, 64));
+        h->err_dev = reinterpret_cast<int*>(device_view(h->err_host));
     }
     XferSet x{};
     double* staged[kXferFields] = {};
     const double* src_host[kXferFields] = {};
     double* xf = nullptr;
     size_t off = 0;
-    for (int f = 0; f < nfields; ++f) {
+    int xpos = -1;
+    int ncol = 0;
+    for (int f = 0; f < nfields && n > 0; ++f) {
         if (!host[f]) continue;
+        if (k[f] < 1 || k[f] > 4 || (ncol += k[f]) > kXferCols) return DEM_ERR_INVALID;
         double* dv = device_view(host[f]);
         if (!dv) {
             if (!xf) TRY(xfer_buffer(h, 22 * n, &xf));
@@ -798,18 +823,31 @@ int exchange(DemHandle* h, int64_t p0, int64_t n, const int* k, double* const* h
             staged[x.nf] = dv;
             src_host[x.nf] = host[f];
         }
+        if (f == posf) xpos = x.nf;
         x.rec[x.nf] = dv;
         for (int c = 0; c < 4; ++c) x.col[x.nf][c] = cols[f][c];
         x.k[x.nf] = k[f];
         ++x.nf;
     }
-    if (to_cols)
-        for (int f = 0; f < x.nf; ++f)
-            if (staged[f])
-                CU(cudaMemcpyAsync(staged[f], src_host[f], sizeof(double) * x.k[f] * n,
-                                   cudaMemcpyHostToDevice, h->stream));
-    launch_xfer(x, (int)n, (int)p0, to_cols, h->stream);
-    CU(cudaGetLastError());
+    if (error) {
+        if (n > 0 && x.nf > 0 && h->err_dev) {
+            x.err_src = &h->d.ctr->error;
+            x.err_dst = h->err_dev;
+        } else {
+            CU(cudaMemcpyAsync(h->err_host, &h->d.ctr->error, sizeof(int),
+                               cudaMemcpyDeviceToHost, h->stream));
+        }
+    }
+    if (n > 0 && x.nf > 0) {
+        if (to_cols)
+            for (int f = 0; f < x.nf; ++f)
+                if (staged[f])
+                    CU(cudaMemcpyAsync(staged[f], src_host[f], sizeof(double) * x.k[f] * n,
+                                       cudaMemcpyHostToDevice, h->stream));
+        if (xpos >= 0) launch_xfer_pos(x, (int)n, h->d, h->p, xpos, fb, h->stream);
+        else launch_xfer(x, (int)n, (int)p0, to_cols, h->stream);
+        CU(cudaGetLastError());
+    }
     if (!to_cols)
         for (int f = 0; f < x.nf; ++f)
             if (staged[f])
@@ -1386,12 +1424,10 @@ int set_particles(DemHandle* h, const DemParticleState* in, bool sync) {
     double* const host[] = {in->pos, in->vel, in->omega, in->quat, in->wall_shear};
     double* const cols[][4] = {{d.px, d.py, d.pz}, {d.vx, d.vy, d.vz}, {d.wx, d.wy, d.wz},
                                {d.qw, d.qx, d.qy, d.qz}, {d.wsx, d.wsy, d.wsz}};
-    TRY(exchange(h, 0, n, k, host, cols, 5, true, nullptr, sync));
-    // new positions: the neighbour lists stay valid while every particle lies
-    // within skin/2 of where they were built, else the next step searches in full
-    launch_refresh_pos32(h->d, h->p, false, 0, (int)n, in->pos ? h->cur : -1, h->stream);
-    CU(cudaGetLastError());
-    return DEM_OK;
+    // new positions: the exchange kernel refreshes the FP32 positions; the
+    // neighbour lists stay valid while every particle lies within skin/2 of
+    // where they were built, else the next step searches in full
+    return exchange(h, 0, n, k, host, cols, 5, true, nullptr, sync, 0, h->cur);
 }
 
 int dem_set_particles(DemHandle* h, const DemParticleState* in) {
@@ -1414,12 +1450,25 @@ int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
 int dem_host_alloc(int64_t bytes, void** out) {
     if (!out || bytes < 0) return DEM_ERR_INVALID;
     *out = nullptr;
-    CU(cudaMallocHost(out, (size_t)std::max<int64_t>(bytes, 1)));
+    const size_t nb = (size_t)std::max<int64_t>(bytes, 1);
+    CU(cudaMallocHost(out, nb));
+    double* dv = device_view(*out);  // before registration: the driver's answer
+    if (dv) {
+        HostRanges& H = host_ranges();
+        std::lock_guard<std::mutex> lk(H.mu);
+        H.r[reinterpret_cast<uintptr_t>(*out)] = {nb, reinterpret_cast<uintptr_t>(dv)};
+    }
     return DEM_OK;
 }
 
 int dem_host_free(void* p) {
-    if (p) CU(cudaFreeHost(p));
+    if (!p) return DEM_OK;
+    {
+        HostRanges& H = host_ranges();
+        std::lock_guard<std::mutex> lk(H.mu);
+        H.r.erase(reinterpret_cast<uintptr_t>(p));
+    }
+    CU(cudaFreeHost(p));
     return DEM_OK;
 }
 

@@ -232,13 +232,21 @@ void launch_morton(const DemDev& d, const DemParams& p, uint32_t* morton, cudaSt
 // particle state exchange: per field, k-component records <-> k columns,
 // slots [p0, p0 + n); to_cols: records -> columns
 constexpr int kXferFields = 7;
+constexpr int kXferCols = 22;  // columns of all exchangeable fields (3+3+3+4+3+3+3)
 struct XferSet {
     double* rec[kXferFields];
     double* col[kXferFields][4];
     int k[kXferFields];
     int nf;
+    const int* err_src;  // with err_dst (device-accessible): the kernel copies
+    int* err_dst;        // the device error word (nullptr: no copy)
 };
 void launch_xfer(const XferSet& x, int n, int p0, bool to_cols, cudaStream_t s);
+// the upload of a single-scene handle whose field `posf` holds positions:
+// also refreshes the FP32 positions of the uploaded slots and, with fb 0 or
+// 1, flags a full search as launch_refresh_pos32 does
+void launch_xfer_pos(const XferSet& x, int n, const DemDev& d, const DemParams& p, int posf,
+                     int fb, cudaStream_t s);
 // FP32 positions (pos32) of slots [first, first + n) from the FP64 positions;
 // with fb 0 or 1, scenes with a particle beyond skin/2 of its list position
 // are flagged for a full search in sflags[fb] (no test for fb < 0)

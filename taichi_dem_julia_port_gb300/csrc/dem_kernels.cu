@@ -2199,35 +2199,90 @@ void launch_refresh_pos32(const DemDev& d, const DemParams& p, bool multi, int f
 // record per particle (the host's layout) <-> k columns of the structure of
 // arrays at slots [p0, p0 + n).  A record array is device-accessible caller
 // memory (page-locked host or device) or the library's staging copy.
-// A block moves kThreads particles: their k·kThreads record values are one
-// contiguous range, read or written linearly (whole 128-byte lines, which
-// matters most for page-locked host memory across the chip-to-chip link)
-// and transposed through shared memory.
-__global__ void __launch_bounds__(kThreads) k_xfer(XferSet x, int n, int p0, bool to_cols) {
-    __shared__ double tile[4 * kThreads];
-    const int base = blockIdx.x * kThreads;
-    const int m = min(kThreads, n - base);  // particles of this block
+// A block moves kXferBlock particles, all fields at once: per field their
+// k·kXferBlock record values are one contiguous range (whole 128-byte lines,
+// which matters most for page-locked host memory across the chip-to-chip
+// link), one value per thread, every field's loads issued before the first
+// store, then transposed through shared memory and written column by column.
+// Small blocks put a 17,576-particle scene on every SM.  REFRESH (an upload
+// to a single-scene handle, field `posf` the positions): the FP32 position
+// and the skin test of each slot, from the uploaded values, as
+// k_refresh_pos32 does.
+constexpr int kXferBlock = 64;
+static_assert(4 * kXferBlock <= kThreads, "one record value per thread and field");
+template <bool REFRESH>
+__global__ void __launch_bounds__(kThreads)
+    k_xfer(XferSet x, int n, int p0, bool to_cols, DemDev d, DemParams p, int posf, int fb) {
+    __shared__ double tile[kXferCols * kXferBlock];
+    __shared__ double* s_col[kXferCols];
+    __shared__ int s_off[kXferCols], s_k[kXferCols], s_foff[kXferFields], s_ncol;
+    const int base = blockIdx.x * kXferBlock;
+    const int m = min(kXferBlock, n - base);  // particles of this block
     const int t = threadIdx.x;
-    for (int f = 0; f < x.nf; ++f) {
-        const int k = x.k[f];
-        double* const rec = x.rec[f] + (size_t)k * base;
-        if (to_cols) {
-            for (int e = t; e < k * m; e += kThreads) tile[e] = rec[e];
-            __syncthreads();
-            if (t < m)
-                for (int c = 0; c < k; ++c) x.col[f][c][p0 + base + t] = tile[k * t + c];
-        } else {
-            if (t < m)
-                for (int c = 0; c < k; ++c) tile[k * t + c] = x.col[f][c][p0 + base + t];
-            __syncthreads();
-            for (int e = t; e < k * m; e += kThreads) rec[e] = tile[e];
+    if (t == 0) {
+        int cc = 0, off = 0;
+        for (int f = 0; f < x.nf; ++f) {
+            s_foff[f] = off;
+            for (int c = 0; c < x.k[f]; ++c, ++cc) {
+                s_col[cc] = x.col[f][c];
+                s_off[cc] = off + c;  // value c of particle q at off + k·q + c
+                s_k[cc] = x.k[f];
+            }
+            off += x.k[f] * kXferBlock;
         }
-        __syncthreads();  // the tile is reused by the next field
+        s_ncol = cc;
+        if (x.err_dst && blockIdx.x == 0) *x.err_dst = __ldcg(x.err_src);
+    }
+    if (to_cols) {
+        double v[kXferFields];
+#pragma unroll
+        for (int f = 0; f < kXferFields; ++f) {
+            v[f] = 0.0;
+            if (f < x.nf && t < x.k[f] * m) v[f] = x.rec[f][(size_t)x.k[f] * base + t];
+        }
+        __syncthreads();  // the column table
+#pragma unroll
+        for (int f = 0; f < kXferFields; ++f)
+            if (f < x.nf && t < x.k[f] * m) tile[s_foff[f] + t] = v[f];
+        __syncthreads();
+        for (int e = t; e < s_ncol * kXferBlock; e += kThreads) {
+            const int cc = e / kXferBlock, q = e % kXferBlock;
+            if (q < m) s_col[cc][p0 + base + q] = tile[s_off[cc] + s_k[cc] * q];
+        }
+        if (REFRESH && t < m) {
+            const int i = p0 + base + t;
+            const SceneParams& S = scene_rec<false>(d, p, 0);
+            const double* xp = tile + s_foff[posf] + 3 * t;
+            const float fx = d2f(xp[0] - S.dmin[0]), fy = d2f(xp[1] - S.dmin[1]),
+                        fz = d2f(xp[2] - S.dmin[2]);
+            d.pos32[i] = make_float4(fx, fy, fz, reach32(fx, fy, fz, d.rm32[i].z));
+            if (fb >= 0 && (!(S.f_half_skin > 0.0f) || left_skin(S, fx, fy, fz, d.xref[i])) &&
+                d.sflags[fb][0] == 0u)
+                atomicOr(&d.sflags[fb][0], 1u);
+        }
+    } else {
+        __syncthreads();  // the column table
+        for (int e = t; e < s_ncol * kXferBlock; e += kThreads) {
+            const int cc = e / kXferBlock, q = e % kXferBlock;
+            if (q < m) tile[s_off[cc] + s_k[cc] * q] = s_col[cc][p0 + base + q];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int f = 0; f < kXferFields; ++f)
+            if (f < x.nf && t < x.k[f] * m) x.rec[f][(size_t)x.k[f] * base + t] = tile[s_foff[f] + t];
     }
 }
 void launch_xfer(const XferSet& x, int n, int p0, bool to_cols, cudaStream_t s) {
     if (n <= 0 || x.nf <= 0) return;
-    k_xfer<<<blocks_for(n, kThreads), kThreads, 0, s>>>(x, n, p0, to_cols);
+    k_xfer<false><<<blocks_for(n, kXferBlock), kThreads, 0, s>>>(x, n, p0, to_cols, DemDev{},
+                                                                  DemParams{}, -1, -1);
+}
+void launch_xfer_pos(const XferSet& x, int n, const DemDev& d, const DemParams& p, int posf,
+                     int fb, cudaStream_t s) {
+    if (posf < 0 || posf >= x.nf || x.k[posf] != 3) return launch_xfer(x, n, 0, true, s);
+    if (n <= 0) return;
+    fb = fb == 0 || fb == 1 ? fb : -1;
+    k_xfer<true><<<blocks_for(n, kXferBlock), kThreads, 0, s>>>(x, n, 0, true, d, p, posf, fb);
 }
 
 void launch_recode(const DemDev& d, int buf, int n, bool to_pairs, cudaStream_t s) {
