@@ -111,7 +111,8 @@ L2_FLUSH_BYTES = 256 << 20
 # ran on the first 64 scenes of the batch (431,416 spheres); their traffic is
 # scaled to a launch by particles processed.
 NCU_TRAFFIC = {
-    ("c2", "force"): (6.419456e6, 17576),          # k_force<double>
+    ("c2", "force"): (6.98368e6, 17576),           # k_force<double>
+    ("c3", "integrate"): (724.541696e6, 2000000),  # k_integrate (FP32 mode, no contacts)
     ("c4", "force"): (145.409024e6, 431416),       # k_force<float>
     ("c4", "integrate"): (186.321408e6, 431416),   # k_integrate (FP32 gather)
     ("c4", "contacts"): (150.255616e6, 431416),    # k_search, list step
