@@ -80,7 +80,7 @@ KERNELS_PER_STEP = 3
 # and profiles/k_integrate_batched_64_scenes.md): the force kernel per bond, the
 # integrator per particle, in the FP64 and the FP32 force mode; GB300's FP64
 # pipe width
-FP64_INST = {("force", "fp64"): 118.0, ("force", "fp32"): 15.0,
+FP64_INST = {("force", "fp64"): 117.0, ("force", "fp32"): 15.0,
              ("integrate", "fp64"): 85.7, ("integrate", "fp32"): 51.0}
 FP64_LANES_PER_SM = 2
 SM_COUNT = 152
@@ -193,14 +193,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_scene(name: str):
+def make_scene(name: str, pour_n: int = 2_000_000):
     from taichi_dem_julia_port_gb300 import scenes
     if name == "c1":
         return scenes.c1(), "bonded cube 10^3 = 1,000 spheres, -10 m/s, FP64, dt 1e-6"
     if name == "c2":
         return scenes.c2(), "bonded cube 26^3 = 17,576 spheres, 20 m/s, FP64, dt 1e-6"
     if name == "c3":
-        return scenes.c3(), "unbonded pour 2,000,000 spheres, FP32 force, dt 2e-7"
+        return (scenes.c3(pour_n),
+                f"unbonded pour {pour_n:,} spheres in 0.4 x 0.4 x 1.2 m, FP32 force, dt 2e-7")
     raise ValueError(name)
 
 
@@ -536,7 +537,7 @@ def run_reference(args) -> None:
         }
         print(json.dumps(line), flush=True)
         return
-    sc, desc = make_scene(args.workload)
+    sc, desc = make_scene(args.workload, args.pour_n)
     threads = host_threads()
     o = OracleScene(sc.cfg, sc.particles, threads=threads)
     if sc.bonded:
@@ -630,6 +631,8 @@ def main() -> None:
     ap.add_argument("--no-plain", action="store_true",
                     help="c4: skip the scene-by-scene plain-path comparison")
     ap.add_argument("--precision", default=None, choices=["fp64", "fp32"])
+    ap.add_argument("--pour-n", type=int, default=2_000_000,
+                    help="c3: spheres in the pour (smaller pours for profiling captures)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--e2e-steps", type=int, default=500)
     ap.add_argument("--profile-steps", type=int, default=20)
@@ -665,7 +668,7 @@ def main() -> None:
         if dist:
             dist.destroy_process_group()
         return
-    sc, desc = make_scene(args.workload)
+    sc, desc = make_scene(args.workload, args.pour_n)
     precision = args.precision or ("fp32" if args.workload == "c3" else "fp64")
     g = GlobalData(sc.cfg, sc.particles, precision=precision)
     if sc.bonded:

@@ -1008,8 +1008,8 @@ int dem_selftest_conversions(int64_t n, uint64_t seed, int64_t* mismatches) {
     int dev = 0, sms = 0;
     TRY(check_device(&dev, &sms));
     unsigned long long* bad = nullptr;
-    CU(cudaMalloc(&bad, 3 * sizeof(unsigned long long)));
-    unsigned long long hb[3] = {0, 0, 0};
+    CU(cudaMalloc(&bad, 4 * sizeof(unsigned long long)));
+    unsigned long long hb[4] = {0, 0, 0, 0};
     cudaError_t e = cudaMemset(bad, 0, sizeof(hb));
     if (e == cudaSuccess) {
         launch_selftest_conv((long long)n, (unsigned long long)seed, bad, 0);
@@ -1021,6 +1021,7 @@ int dem_selftest_conversions(int64_t n, uint64_t seed, int64_t* mismatches) {
     mismatches[0] = (int64_t)hb[0];
     mismatches[1] = (int64_t)hb[1];
     mismatches[2] = (int64_t)hb[2];
+    mismatches[3] = (int64_t)hb[3];
     return DEM_OK;
 }
 

@@ -111,6 +111,19 @@ __device__ __forceinline__ double rcp_nr(double x) {
     return fma(y, e, y);
 }
 
+// x·0.5 exactly, without the FP64 pipe: a normal x whose exponent field is at
+// least 2 loses one from it, a zero is returned as it is; subnormal,
+// smallest-normal, infinite and NaN inputs take the FP64 multiply (out of
+// line).  Bit-identical to x * 0.5 (checked by dem_selftest_conversions).
+static __device__ __noinline__ double half_hw(double x) { return x * 0.5; }
+__device__ __forceinline__ double half_exact(double x) {
+    const long long b = __double_as_longlong(x);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    if (e - 2u < 0x7fdu) return __longlong_as_double(b - (1ll << 52));  // e in [2, 0x7fe]
+    if ((b & 0x7fffffffffffffffll) == 0) return x;
+    return half_hw(x);
+}
+
 // ---- Morton / bucket ---------------------------------------------------------
 // Morton.jl `cartesian3morton` for 1-based cells (x in bit 0): the interleave of
 // (ijk - 1) plus one.  Each coordinate keeps its low 10 bits.  The spreading

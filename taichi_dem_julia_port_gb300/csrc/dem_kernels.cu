@@ -1484,7 +1484,8 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
             fig = from_d<T>(rot_t<double>(R, {-Fi.x, -Fi.y, -Fi.z}));
             mi = from_d<T>(rot_t<double>(R, {-ti.x, -ti.y, -ti.z}));
             mj = from_d<T>(rot_t<double>(R, {-tj.x, -tj.y, -tj.z}));
-            st3(w.f, CK, c, {(ki.x + kj.x) * 0.5, (ki.y + kj.y) * 0.5, (ki.z + kj.z) * 0.5});
+            st3(w.f, CK, c, {half_exact(ki.x + kj.x), half_exact(ki.y + kj.y),
+                             half_exact(ki.z + kj.z)});
             st3(w.f, CF, c, Fi);
             st3(w.f, CTI, c, ti);
             st3(w.f, CTJ, c, tj);  // a bond's 𝐬 stays zero and is not stored
@@ -1881,7 +1882,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     d.vy[i] = vy + ay * dt;
     d.vz[i] = vz + az * dt;
     // 𝐪 + Δ𝐪 with Δ𝐪 = ½ 𝛚 ⊗ 𝐪 (no dt, as the reference), the ½ folded into 𝛚
-    const double hx = 0.5 * wx, hy = 0.5 * wy, hz = 0.5 * wz;
+    const double hx = half_exact(wx), hy = half_exact(wy), hz = half_exact(wz);
     const double nw = qw - qx * hx - qy * hy - qz * hz;
     const double nx = qx + qw * hx + qy * hz - qz * hy;
     const double ny = qy + qw * hy + qx * hz + qz * hx;
@@ -2158,6 +2159,19 @@ __global__ void k_selftest_conv(long long n, unsigned long long seed, unsigned l
     const long long u1 = __double_as_longlong(rcp_nr(xr)), u2 = __double_as_longlong(__drcp_rn(xr));
     const long long du = u1 > u2 ? u1 - u2 : u2 - u1;
     if (du > 2) atomicAdd(bad + 2, 1ull);
+    // half_exact on the values drawn for d2f (zeros, subnormals, normals) and
+    // on the FP32-widened ones: bit-identical to x * 0.5
+    if (__double_as_longlong(half_exact(x)) != __double_as_longlong(x * 0.5)) atomicAdd(bad + 3, 1ull);
+    const double xf = (double)f;
+    if (!isnan(xf) && __double_as_longlong(half_exact(xf)) != __double_as_longlong(xf * 0.5))
+        atomicAdd(bad + 3, 1ull);
+    // and on the exponent fields at the edges: 0 (subnormal), 1, 2, 0x7fe, 0x7ff (inf)
+    const unsigned long long edge[5] = {0ull, 1ull, 2ull, 0x7feull, 0x7ffull};
+    const unsigned long long xe_bits = ((r1 >> 63) << 63) | (edge[(r2 >> 32) % 5ull] << 52) |
+                                       ((t & 3) == 3 ? 0ull : (r2 & 0xfffffffffffffull));
+    const double xe = __longlong_as_double((long long)xe_bits);
+    if (!isnan(xe) && __double_as_longlong(half_exact(xe)) != __double_as_longlong(xe * 0.5))
+        atomicAdd(bad + 3, 1ull);
 }
 
 void launch_selftest_conv(long long n, unsigned long long seed, unsigned long long* bad,
