@@ -69,6 +69,9 @@ COMPACT_BYTES_HERTZ = 24 + 48 + 8
 # Algorithmic bytes of the other phases per particle / per contact
 BROADPHASE_BYTES_PER_PARTICLE = 24 + 16 + 4 + 4 + 4 + 8 + 24 + 8 + 32 + 16  # hash..canon
 INTEGRATE_BYTES_PER_PARTICLE = 13 * 8 * 2 + 4 * 8 + 6 * 8 + 3 * 8 * 2 + 8 + 4  # state r/w
+# the pour settles without contacts: every particle is torque-free, so the
+# integrator keeps its stored spin (no 24-byte spin write)
+INTEGRATE_BYTES_WORKLOAD = {"c3": INTEGRATE_BYTES_PER_PARTICLE - 3 * 8}
 # neighbour-list step per particle: path byte, current row bounds, list length,
 # FP32 position, next row bounds written, 4 list partners (index + FP32
 # position); the row rebuild adds the compaction bytes per surviving contact
@@ -82,16 +85,21 @@ KERNELS_PER_STEP = 3
 # pipe width
 FP64_INST = {("force", "fp64"): 117.0, ("force", "fp32"): 15.0,
              ("integrate", "fp64"): 85.7, ("integrate", "fp32"): 51.0}
+# The integrator skips the quaternion increment of a particle with exactly zero
+# spin and the spin update of one with exactly zero torque: in the pour's
+# settling phase (no contacts) that is every particle (ncu on a 400,000-sphere
+# pour: 14,000,000 FP64 thread instructions per launch)
+FP64_INST_WORKLOAD = {("c3", "integrate", "fp32"): 35.0}
 FP64_LANES_PER_SM = 2
 SM_COUNT = 152
 
 
 def fp64_roofline(kernel: str, precision: str, n_particles: int, n_bond: int, ms: float,
-                  sm_mhz) -> dict | None:
+                  sm_mhz, workload: str | None = None) -> dict | None:
     """The FP64-pipe roofline of the force kernel (per bond; bonded scenes) or
     the integrator (per particle): FP64 instructions over the live per-phase
     time against the pipe's peak at the sampled SM clock."""
-    per = FP64_INST.get((kernel, precision))
+    per = FP64_INST_WORKLOAD.get((workload, kernel, precision), FP64_INST.get((kernel, precision)))
     units = n_bond if kernel == "force" else n_particles
     if per is None or not units or not ms:
         return None
@@ -112,7 +120,7 @@ L2_FLUSH_BYTES = 256 << 20
 # scaled to a launch by particles processed.
 NCU_TRAFFIC = {
     ("c2", "force"): (6.98368e6, 17576),           # k_force<double>
-    ("c3", "integrate"): (724.541696e6, 2000000),  # k_integrate (FP32 mode, no contacts)
+    ("c3", "integrate"): (679.441664e6, 2000000),  # k_integrate (FP32 mode, no contacts)
     ("c4", "force"): (145.409024e6, 431416),       # k_force<float>
     ("c4", "integrate"): (186.321408e6, 431416),   # k_integrate (FP32 gather)
     ("c4", "contacts"): (150.255616e6, 431416),    # k_search, list step
@@ -715,7 +723,8 @@ def main() -> None:
     n_bond = st["bonded"]
     force_bytes = n_bond * FORCE_BYTES_BOND + (c_now - n_bond) * FORCE_BYTES_HERTZ
     alg = {"force": force_bytes,
-           "integrate": sc.n * INTEGRATE_BYTES_PER_PARTICLE,
+           "integrate": sc.n * INTEGRATE_BYTES_WORKLOAD.get(args.workload,
+                                                            INTEGRATE_BYTES_PER_PARTICLE),
            "contacts": sc.n * DETECT_BYTES_PER_PARTICLE
            + n_bond * COMPACT_BYTES_BOND + (c_now - n_bond) * COMPACT_BYTES_HERTZ}
     dom = max(ph, key=ph.get)
@@ -733,7 +742,7 @@ def main() -> None:
     # the force kernel and the integrator are bound by GB300's FP64 pipe
     # (2 lanes per SM per cycle) rather than by HBM: their FP64 roofline
     fr = fp64_roofline(dom, precision, sc.n, n_bond, ph.get(dom),
-                       clk.get("sm_mhz") or peaks.get("sm_max_mhz"))
+                       clk.get("sm_mhz") or peaks.get("sm_max_mhz"), args.workload)
     if fr:
         roofline["fp64_pipe"] = fr
 

@@ -415,11 +415,12 @@ const char* dem_strerror(int code);
 /* Self-test: compares the library's integer-pipe FP64->FP32 and FP32->FP64
  * conversions (used by the FP32 force mode and the neighbour lists) with the
  * hardware conversions, its Newton-Raphson FP64 reciprocal with the
- * correctly rounded one and its integer-pipe halving with x * 0.5, on n
+ * correctly rounded one, its integer-pipe halving with x * 0.5 and the
+ * identities behind the integrator's zero-spin and zero-torque skips, on n
  * seeded random values; mismatches[0] .. [3] (four entries) receive the
  * narrowing / widening mismatch counts, the reciprocals more than 2 ulp off
- * and the halvings that differ (all 0 when correct).  No counterpart in the
- * reference. */
+ * and the halvings or identities that fail (all 0 when correct).  No
+ * counterpart in the reference. */
 int dem_selftest_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
 
 /* Library version string, e.g. "dem_gb300 0.1.0 sm_103a". */

@@ -124,6 +124,23 @@ __device__ __forceinline__ double half_exact(double x) {
     return half_hw(x);
 }
 
+// Bit tests on the IEEE 754 binary64 layout (integer pipe): v is not -0; v
+// is finite and not -0; a·b cannot overflow (for positive finite a and b:
+// the sum of their exponent fields leaves the product's exponent below the
+// largest one).
+__device__ __forceinline__ bool not_negzero(double v) {
+    return __double_as_longlong(v) != (long long)0x8000000000000000ull;
+}
+__device__ __forceinline__ bool finite_not_negzero(double v) {
+    const long long b = __double_as_longlong(v);
+    return b != (long long)0x8000000000000000ull && ((b >> 52) & 0x7ff) != 0x7ff;
+}
+__device__ __forceinline__ bool product_finite(double a, double b) {
+    const int ea = (int)((__double_as_longlong(a) >> 52) & 0x7ff);
+    const int eb = (int)((__double_as_longlong(b) >> 52) & 0x7ff);
+    return ea != 0x7ff && eb != 0x7ff && ea + eb <= 0x7fd + 1023;
+}
+
 // ---- Morton / bucket ---------------------------------------------------------
 // Morton.jl `cartesian3morton` for 1-based cells (x in bit 0): the interleave of
 // (ijk - 1) plus one.  Each coordinate keeps its low 10 bits.  The spreading

@@ -1838,10 +1838,11 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
             d.wsz[i] = 0.0;
         }
     }
-    // apply_body_force!
-    F[0] += S.grav[0] * m;
-    F[1] += S.grav[1] * m;
-    F[2] += S.grav[2] * m;
+    // apply_body_force!  A zero gravity component adds nothing: the force sum
+    // starts at +0 and never becomes -0, so F + 0·m is F.
+    if (S.grav[0] != 0.0) F[0] += S.grav[0] * m;
+    if (S.grav[1] != 0.0) F[1] += S.grav[1] * m;
+    if (S.grav[2] != 0.0) F[2] += S.grav[2] * m;
     if (S.damping != 0.0) {
         const double v3[3] = {vx, vy, vz}, w3[3] = {wx, wy, wz};
         double dF[3], dM[3];
@@ -1881,21 +1882,38 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     d.vx[i] = vx + ax * dt;
     d.vy[i] = vy + ay * dt;
     d.vz[i] = vz + az * dt;
-    // 𝐪 + Δ𝐪 with Δ𝐪 = ½ 𝛚 ⊗ 𝐪 (no dt, as the reference), the ½ folded into 𝛚
-    const double hx = half_exact(wx), hy = half_exact(wy), hz = half_exact(wz);
-    const double nw = qw - qx * hx - qy * hy - qz * hz;
-    const double nx = qx + qw * hx + qy * hz - qz * hy;
-    const double ny = qy + qw * hy + qx * hz + qz * hx;
-    const double nz = qz + qw * hz + qx * hy - qy * hx;
+    // 𝐪 + Δ𝐪 with Δ𝐪 = ½ 𝛚 ⊗ 𝐪 (no dt, as the reference), the ½ folded into
+    // 𝛚, as explicit FMA chains.  With 𝛚 = (+0, +0, +0) each fma(a, +0, c)
+    // (a finite) returns c unless c is -0, so for a finite 𝐪 without a -0
+    // component the chains return 𝐪 itself: a particle that does not spin
+    // skips them, with identical results.  The normalisation always runs.
+    double nw = qw, nx = qx, ny = qy, nz = qz;
+    const bool spinless = (__double_as_longlong(wx) | __double_as_longlong(wy) |
+                           __double_as_longlong(wz)) == 0ll;
+    if (!(spinless && finite_not_negzero(qw) && finite_not_negzero(qx) &&
+          finite_not_negzero(qy) && finite_not_negzero(qz))) {
+        const double hx = half_exact(wx), hy = half_exact(wy), hz = half_exact(wz);
+        nw = __fma_rn(-qz, hz, __fma_rn(-qy, hy, __fma_rn(-qx, hx, qw)));
+        nx = __fma_rn(-qz, hy, __fma_rn(qy, hz, __fma_rn(qw, hx, qx)));
+        ny = __fma_rn(qz, hx, __fma_rn(qx, hz, __fma_rn(qw, hy, qy)));
+        nz = __fma_rn(-qy, hx, __fma_rn(qx, hy, __fma_rn(qw, hz, qz)));
+    }
     const double inq = rsqrt(nw * nw + nx * nx + ny * ny + nz * nz);
     d.qw[i] = nw * inq;
     d.qx[i] = nx * inq;
     d.qy[i] = ny * inq;
     d.qz[i] = nz * inq;
-    const double iidt = ii * dt;
-    d.wx[i] = wx + M[0] * iidt;
-    d.wy[i] = wy + M[1] * iidt;
-    d.wz[i] = wz + M[2] * iidt;
+    // 𝛚 + 𝐌·I⁻¹dt: with 𝐌 = (+0, +0, +0) and a finite I⁻¹dt, fma(+0, I⁻¹dt, w)
+    // is w unless w is -0, so a torque-free particle keeps its stored spin
+    const bool torque_free = (__double_as_longlong(M[0]) | __double_as_longlong(M[1]) |
+                              __double_as_longlong(M[2])) == 0ll;
+    if (!(torque_free && product_finite(ii, dt) && not_negzero(wx) && not_negzero(wy) &&
+          not_negzero(wz))) {
+        const double iidt = ii * dt;
+        d.wx[i] = __fma_rn(M[0], iidt, wx);
+        d.wy[i] = __fma_rn(M[1], iidt, wy);
+        d.wz[i] = __fma_rn(M[2], iidt, wz);
+    }
     d.fx[i] = F[0];
     d.fy[i] = F[1];
     d.fz[i] = F[2];
@@ -2171,6 +2189,28 @@ __global__ void k_selftest_conv(long long n, unsigned long long seed, unsigned l
                                        ((t & 3) == 3 ? 0ull : (r2 & 0xfffffffffffffull));
     const double xe = __longlong_as_double((long long)xe_bits);
     if (!isnan(xe) && __double_as_longlong(half_exact(xe)) != __double_as_longlong(xe * 0.5))
+        atomicAdd(bad + 3, 1ull);
+    // the integrator's zero-spin and zero-torque skips: where they apply, the
+    // quaternion chains with 𝛚 = +0 return 𝐪 and the spin update returns 𝛚
+    // (z is +0 at run time, so no rule of the compiler's folds the products)
+    const double z = (double)(t >> 62);
+    const double q0 = x, q1 = xf, q2 = xe, q3 = (t & 2) ? -xr : 0.0;
+    const unsigned long long bq[4] = {
+        (unsigned long long)__double_as_longlong(q0), (unsigned long long)__double_as_longlong(q1),
+        (unsigned long long)__double_as_longlong(q2), (unsigned long long)__double_as_longlong(q3)};
+    if (finite_not_negzero(q0) && finite_not_negzero(q1) && finite_not_negzero(q2) &&
+        finite_not_negzero(q3)) {
+        const double n[4] = {__fma_rn(-q3, z, __fma_rn(-q2, z, __fma_rn(-q1, z, q0))),
+                             __fma_rn(-q3, z, __fma_rn(q2, z, __fma_rn(q0, z, q1))),
+                             __fma_rn(q3, z, __fma_rn(q1, z, __fma_rn(q0, z, q2))),
+                             __fma_rn(-q2, z, __fma_rn(q1, z, __fma_rn(q0, z, q3)))};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if ((unsigned long long)__double_as_longlong(n[k]) != bq[k]) atomicAdd(bad + 3, 1ull);
+    }
+    const double ia = fabs(xf), ib = fabs(xe);
+    if (product_finite(ia, ib) && not_negzero(x) &&
+        __double_as_longlong(__fma_rn(z, ia * ib, x)) != __double_as_longlong(x))
         atomicAdd(bad + 3, 1ull);
 }
 

@@ -324,7 +324,10 @@ def test_integer_pipe_conversions_match_hardware(gpu):
     exactly as the hardware conversions (ties, range edges, subnormal and
     overflowing results included); the Newton-Raphson FP64 reciprocal is
     within 2 ulp of the correctly rounded one; the integer-pipe halving is
-    bit-identical to x * 0.5 (zeros, subnormals, exponent edges, infinities)."""
+    bit-identical to x * 0.5 (zeros, subnormals, exponent edges, infinities);
+    where the integrator skips the quaternion increment of a spinless
+    particle or the spin update of a torque-free one, the skipped FMA chains
+    would have returned their input bit for bit."""
     import ctypes
     bad = (ctypes.c_int64 * 4)()
     for seed in (1, 2, 3):
