@@ -120,9 +120,9 @@ L2_FLUSH_BYTES = 256 << 20
 # scaled to a launch by particles processed.
 NCU_TRAFFIC = {
     ("c2", "force"): (6.98368e6, 17576),           # k_force<double>
-    ("c3", "integrate"): (679.441664e6, 2000000),  # k_integrate (FP32 mode, no contacts)
+    ("c3", "integrate"): (688.167168e6, 2000000),  # k_integrate3 (FP32 mode, no contacts)
     ("c4", "force"): (145.409024e6, 431416),       # k_force<float>
-    ("c4", "integrate"): (186.321408e6, 431416),   # k_integrate (FP32 gather)
+    ("c4", "integrate"): (184.980224e6, 431416),   # k_integrate3 (FP32 gather)
     ("c4", "contacts"): (150.255616e6, 431416),    # k_search, list step
     ("c2", "contacts"): (6.824448e6, 17576),       # k_search, list step
 }

@@ -1726,8 +1726,7 @@ __device__ __forceinline__ bool left_skin(const SceneParams& S, float fx, float 
 }
 
 template <bool MULTI, bool F32>
-__global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, int cur) {
-    dep_begin(p.dep == 2);
+__device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams& p, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nxt = cur ^ 1;
     if (i == 0) d.ctr->row_alloc[cur] = 0u;  // the free buffer is next step's target
@@ -1920,6 +1919,21 @@ __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, i
     d.tx[i] = M[0];
     d.ty[i] = M[1];
     d.tz[i] = M[2];
+}
+
+// The integrator with the compiler's register choice (FP64 force mode), and
+// in the FP32 force mode with a budget for three 256-thread blocks per SM:
+// its FP64 work per particle is small enough that more resident warps hide
+// the state loads better than the extra registers would.
+template <bool MULTI, bool F32>
+__global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, int cur) {
+    dep_begin(p.dep == 2);
+    integrate_body<MULTI, F32>(d, p, cur);
+}
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads, 3) k_integrate3(DemDev d, DemParams p, int cur) {
+    dep_begin(p.dep == 2);
+    integrate_body<MULTI, true>(d, p, cur);
 }
 
 // ---- inspection kernels (dem_debug_broadphase) -------------------------------
@@ -2126,8 +2140,8 @@ void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
     const int block = clamp_block(sh.integrate_block);
     const int nb = blocks_for(p.n, block);
     if (p.precision == 1)
-        launch(p.dep != 0, multi ? k_integrate<true, true> : k_integrate<false, true>, nb, block, s,
-               d, p, cur);
+        launch(p.dep != 0, multi ? k_integrate3<true> : k_integrate3<false>, nb, block, s, d, p,
+               cur);
     else
         launch(p.dep != 0, multi ? k_integrate<true, false> : k_integrate<false, false>, nb, block,
                s, d, p, cur);
