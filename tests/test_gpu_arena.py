@@ -382,3 +382,60 @@ def test_full_size_pour_properties(gpu):
         np.testing.assert_array_equal(runs[0][0][k], runs[2][0][k], err_msg=f"lists {k}")
     assert runs[2][1]["full_searches"] == steps
     assert runs[0][1]["full_searches"] < steps
+
+
+def test_list_update_large_scenes(gpu):
+    """Scenes with more particles than one pass of the list update's 4-lane
+    groups: a sparse 64,000-sphere pour (fewer contacts than a quarter of its
+    particles: the wide pass, which reads 32 particles per warp and hands only
+    those with contacts or list partners to the groups) and a 64,000-sphere
+    bonded cube (dense: the per-group pass).  Their neighbour-list steps give
+    the results of a full pair search every step, bit for bit, while contacts
+    form and end (the pour) and an impact breaks bonds (the cube); the pour
+    gives the same results inside an arena with a small cube."""
+    pour = scenes.granular_pour(64_000, box=(0.14, 0.14, 0.19), seed=83, steps=0, rmin=0.8e-3,
+                                rmax=1.2e-3)
+    pour.cfg = pour.cfg.replace(dt=1e-6)
+    pv = pour.particles.copy()
+    pv.vel = np.random.default_rng(83).normal(0, 5.0, pv.vel.shape)
+    pour.particles = pv
+    cube = small_cube(40, speed=40.0, seed=81)
+    # weak in compression too: the impact face breaks before the wave returns
+    cube.cfg = cube.cfg.replace(bond_compressive_strength=3e5)
+    steps = 150
+
+    def run(sc, init, skin):
+        g = GlobalData(sc.cfg, sc.particles)
+        g.set_skin_factor(skin)
+        if init:
+            g.initialize()
+        g.simulate(steps)
+        out = (g.particles(), g.contacts(), g.stats())
+        g.close()
+        return out
+
+    fulls = []
+    for sc, init, name in ((pour, False, "pour"), (cube, True, "cube")):
+        full, lists = run(sc, init, 0.0), run(sc, init, 0.9)
+        for k in PARTICLE_KEYS:
+            np.testing.assert_array_equal(lists[0][k], full[0][k], err_msg=f"{name} lists {k}")
+        for k in CONTACT_KEYS:
+            np.testing.assert_array_equal(lists[1][k], full[1][k],
+                                          err_msg=f"{name} lists contacts {k}")
+        assert full[2]["full_searches"] == steps
+        assert 1 <= lists[2]["full_searches"] < steps, (name, lists[2]["full_searches"])
+        for k in ("bonds_broken", "contacts_created", "contacts_ended"):
+            assert lists[2][k] == full[2][k], (name, k)
+        fulls.append(full)
+    assert fulls[0][2]["contacts_created"] > 0 and fulls[0][2]["contacts_ended"] > 0
+    assert len(fulls[0][1]["i"]) * 4 < pour.n
+    assert fulls[1][2]["bonds_broken"] > 0
+    # an arena whose contacts stay sparse (the pour and a small cube) takes
+    # the wide pass too
+    small = small_cube(5, seed=84)
+    small_ref = alone(small, steps)
+    with Arena(pour.n + 4096, max_scenes=2) as a:
+        ids = [a.add(pour.cfg, pour.particles, init_bonds=False), a.add(small.cfg, small.particles)]
+        a.step(steps)
+        assert_same(a, ids[0], fulls[0], "arena pour")
+        assert_same(a, ids[1], small_ref, "arena small cube")
