@@ -12,7 +12,10 @@ The search is coordinate descent: cell factor first, then the force kernel's
 block and grid, then the integration block, the FP32
 force kernel's register budget, the launch mode (ordinary or programmatic
 dependent launches) and the pair search's register budget; each
-candidate is timed over `steps` steps after one untimed step.
+candidate is timed over `steps` steps after one untimed step.  The run moves
+on while candidates are timed, so the choice is confirmed at the end: the
+chosen and the starting settings are timed alternately (`confirm_rounds`
+times each) and the faster is kept.
 """
 from __future__ import annotations
 
@@ -49,11 +52,14 @@ def _time(target, steps: int) -> float:
 def autotune(target, sm_count: int = 152, steps: int = 10, cell_factors=CELL_FACTORS,
              blocks=BLOCKS, grids_per_sm=GRIDS_PER_SM,
              integrate_blocks=INTEGRATE_BLOCKS, detect_blocks=DETECT_BLOCKS,
-             force_blocks=FORCE_BLOCKS, dependent=DEPENDENT) -> TuneResult:
+             force_blocks=FORCE_BLOCKS, dependent=DEPENDENT,
+             confirm_rounds: int = 3) -> TuneResult:
     """Tunes `target` in place and returns the chosen settings."""
     trials = []
     is_arena = hasattr(target, "set_cell_factor")
     best_cf = None
+    start_cf = 1.0 if is_arena else None
+    start_shape = target.launch_shape()
     best = _time(target, steps)
     trials.append(({"baseline": True}, best))
     if is_arena:
@@ -102,5 +108,28 @@ def autotune(target, sm_count: int = 152, steps: int = 10, cell_factors=CELL_FAC
         trials.append((cand, t))
         if t < best:
             best, shape = t, cand
-    target.set_launch_shape(**shape)
+    # the run moves on while the candidates are timed (cubes reach their walls,
+    # contacts form), so the choice is confirmed against the starting settings
+    # on one stretch of the run, the two alternating
+    if confirm_rounds <= 0:
+        target.set_launch_shape(**shape)
+        return TuneResult(best_cf, shape, best, trials)
+    t_new = t_start = 0.0
+    for _ in range(confirm_rounds):
+        _apply(target, start_cf, start_shape, is_arena)
+        t_start += _time(target, steps)
+        _apply(target, best_cf, shape, is_arena)
+        t_new += _time(target, steps)
+    trials.append(({"confirm": True, "start": t_start, "chosen": t_new}, t_new / confirm_rounds))
+    if t_start < t_new:
+        best_cf, shape, best = start_cf, start_shape, t_start / confirm_rounds
+        _apply(target, best_cf, shape, is_arena)
+    else:
+        best = t_new / confirm_rounds
     return TuneResult(best_cf, shape, best, trials)
+
+
+def _apply(target, cell_factor, shape, is_arena) -> None:
+    if is_arena and cell_factor is not None:
+        target.set_cell_factor(cell_factor)
+    target.set_launch_shape(**shape)

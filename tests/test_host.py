@@ -149,3 +149,47 @@ def test_server_policy_argument():
     from taichi_dem_julia_port_gb300.serving import ArenaSizing, Server
     with pytest.raises(ValueError):
         Server(ArenaSizing(1000, 1000, 4096, 2, 16, 8), policy="lifo")
+
+
+class _DriftingHandle:
+    """A stand-in for a stepping handle whose step cost falls as the run goes
+    on (as when scenes settle), by more than the difference between shapes:
+    the default shape is truly the fastest, but a candidate timed late in
+    the descent looks faster than the baseline timed first."""
+
+    def __init__(self):
+        self.shape = {"force_block": 256, "force_grid": 152 * 16, "integrate_block": 256,
+                      "force_blocks_per_sm": 0, "dependent_launch": 0,
+                      "detect_blocks_per_sm": 4}
+        self.default = dict(self.shape)
+        self.t = 0
+
+    def launch_shape(self):
+        return dict(self.shape)
+
+    def set_launch_shape(self, **shape):
+        self.shape = dict(self.shape, **shape)
+
+    def step(self, n):
+        self.t += n
+
+    def step_timed(self, n):
+        cost = 1.0 if self.shape == self.default else 1.02
+        total = sum(cost * (1.0 - 0.004 * min(self.t + k, 150)) for k in range(n))
+        self.t += n
+        return total
+
+
+def test_autotune_confirms_its_choice():
+    """The descent picks a shape that only looked faster because the run
+    moved on; timing it against the starting shape on one stretch of the run
+    reverts to the starting shape."""
+    from taichi_dem_julia_port_gb300.autotune import autotune
+    unconfirmed = _DriftingHandle()
+    assert autotune(unconfirmed, steps=2, confirm_rounds=0).shape != unconfirmed.default
+    h = _DriftingHandle()
+    r = autotune(h, steps=2, confirm_rounds=2)
+    assert r.shape == h.default
+    assert h.shape == h.default
+    chosen = [c for c, _ in r.trials if not c.get("baseline") and not c.get("confirm")]
+    assert chosen, "the descent timed candidates"
