@@ -123,8 +123,9 @@ NCU_TRAFFIC = {
     ("c3", "integrate"): (688.167168e6, 2000000),  # k_integrate3 (FP32 mode, no contacts)
     ("c4", "force"): (145.409024e6, 431416),       # k_force<float>
     ("c4", "integrate"): (184.980224e6, 431416),   # k_integrate3 (FP32 gather)
-    ("c4", "contacts"): (150.255616e6, 431416),    # k_search, list step
-    ("c2", "contacts"): (6.824448e6, 17576),       # k_search, list step
+    ("c4", "contacts"): (35.102976e6, 431416),     # k_search, list step
+    ("c2", "contacts"): (2.096128e6, 17576),       # k_search, list step
+    ("c3", "contacts"): (43.205888e6, 2000000),    # k_search, list step (wide pass)
 }
 
 
