@@ -69,9 +69,10 @@ COMPACT_BYTES_HERTZ = 24 + 48 + 8
 # Algorithmic bytes of the other phases per particle / per contact
 BROADPHASE_BYTES_PER_PARTICLE = 24 + 16 + 4 + 4 + 4 + 8 + 24 + 8 + 32 + 16  # hash..canon
 INTEGRATE_BYTES_PER_PARTICLE = 13 * 8 * 2 + 4 * 8 + 6 * 8 + 3 * 8 * 2 + 8 + 4  # state r/w
-# the pour settles without contacts: every particle is torque-free, so the
-# integrator keeps its stored spin (no 24-byte spin write)
-INTEGRATE_BYTES_WORKLOAD = {"c3": INTEGRATE_BYTES_PER_PARTICLE - 3 * 8}
+# the pour settles without contacts: every particle is torque-free and keeps
+# the identity orientation, so the integrator writes neither its spin (24 B)
+# nor its quaternion (32 B)
+INTEGRATE_BYTES_WORKLOAD = {"c3": INTEGRATE_BYTES_PER_PARTICLE - 3 * 8 - 4 * 8}
 # neighbour-list step per particle: path byte, current row bounds, list length,
 # FP32 position, next row bounds written, 4 list partners (index + FP32
 # position); the row rebuild adds the compaction bytes per surviving contact
@@ -86,10 +87,11 @@ KERNELS_PER_STEP = 3
 FP64_INST = {("force", "fp64"): 117.0, ("force", "fp32"): 15.0,
              ("integrate", "fp64"): 85.7, ("integrate", "fp32"): 51.0}
 # The integrator skips the quaternion increment of a particle with exactly zero
-# spin and the spin update of one with exactly zero torque: in the pour's
-# settling phase (no contacts) that is every particle (ncu on a 400,000-sphere
-# pour: 14,000,000 FP64 thread instructions per launch)
-FP64_INST_WORKLOAD = {("c3", "integrate", "fp32"): 35.0}
+# spin, the normalisation of a spinless identity orientation and the spin
+# update of a particle with exactly zero torque: in the pour's settling phase
+# (no contacts) that is every particle (ncu on a 400,000-sphere pour:
+# 8,800,000 FP64 thread instructions per launch)
+FP64_INST_WORKLOAD = {("c3", "integrate", "fp32"): 22.0}
 FP64_LANES_PER_SM = 2
 SM_COUNT = 152
 

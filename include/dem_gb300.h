@@ -416,11 +416,11 @@ const char* dem_strerror(int code);
  * conversions (used by the FP32 force mode and the neighbour lists) with the
  * hardware conversions, its Newton-Raphson FP64 reciprocal with the
  * correctly rounded one, its integer-pipe halving with x * 0.5 and the
- * identities behind the integrator's zero-spin and zero-torque skips, on n
- * seeded random values; mismatches[0] .. [3] (four entries) receive the
- * narrowing / widening mismatch counts, the reciprocals more than 2 ulp off
- * and the halvings or identities that fail (all 0 when correct).  No
- * counterpart in the reference. */
+ * identities behind the integrator's zero-spin, zero-torque and
+ * identity-orientation skips, on n seeded random values; mismatches[0] ..
+ * [3] (four entries) receive the narrowing / widening mismatch counts, the
+ * reciprocals more than 2 ulp off and the halvings or identities that fail
+ * (all 0 when correct).  No counterpart in the reference. */
 int dem_selftest_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
 
 /* Library version string, e.g. "dem_gb300 0.1.0 sm_103a". */

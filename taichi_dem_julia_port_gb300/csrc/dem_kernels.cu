@@ -1953,22 +1953,30 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
     // (a finite) returns c unless c is -0, so for a finite 𝐪 without a -0
     // component the chains return 𝐪 itself: a particle that does not spin
     // skips them, with identical results.  The normalisation always runs.
+    // A spinless particle with the identity orientation (1, +0, +0, +0)
+    // keeps it: |𝐪|² = 1 exactly, rsqrt(1) = 1 (checked by
+    // dem_selftest_conversions) and 𝐪·1 = 𝐪, so nothing is computed or stored.
     double nw = qw, nx = qx, ny = qy, nz = qz;
     const bool spinless = (__double_as_longlong(wx) | __double_as_longlong(wy) |
                            __double_as_longlong(wz)) == 0ll;
-    if (!(spinless && finite_not_negzero(qw) && finite_not_negzero(qx) &&
-          finite_not_negzero(qy) && finite_not_negzero(qz))) {
-        const double hx = half_exact(wx), hy = half_exact(wy), hz = half_exact(wz);
-        nw = __fma_rn(-qz, hz, __fma_rn(-qy, hy, __fma_rn(-qx, hx, qw)));
-        nx = __fma_rn(-qz, hy, __fma_rn(qy, hz, __fma_rn(qw, hx, qx)));
-        ny = __fma_rn(qz, hx, __fma_rn(qx, hz, __fma_rn(qw, hy, qy)));
-        nz = __fma_rn(-qy, hx, __fma_rn(qx, hy, __fma_rn(qw, hz, qz)));
+    const bool identity = spinless && __double_as_longlong(qw) == 0x3ff0000000000000ll &&
+                          (__double_as_longlong(qx) | __double_as_longlong(qy) |
+                           __double_as_longlong(qz)) == 0ll;
+    if (!identity) {
+        if (!(spinless && finite_not_negzero(qw) && finite_not_negzero(qx) &&
+              finite_not_negzero(qy) && finite_not_negzero(qz))) {
+            const double hx = half_exact(wx), hy = half_exact(wy), hz = half_exact(wz);
+            nw = __fma_rn(-qz, hz, __fma_rn(-qy, hy, __fma_rn(-qx, hx, qw)));
+            nx = __fma_rn(-qz, hy, __fma_rn(qy, hz, __fma_rn(qw, hx, qx)));
+            ny = __fma_rn(qz, hx, __fma_rn(qx, hz, __fma_rn(qw, hy, qy)));
+            nz = __fma_rn(-qy, hx, __fma_rn(qx, hy, __fma_rn(qw, hz, qz)));
+        }
+        const double inq = rsqrt(__fma_rn(nz, nz, __fma_rn(ny, ny, __fma_rn(nx, nx, nw * nw))));
+        d.qw[i] = nw * inq;
+        d.qx[i] = nx * inq;
+        d.qy[i] = ny * inq;
+        d.qz[i] = nz * inq;
     }
-    const double inq = rsqrt(nw * nw + nx * nx + ny * ny + nz * nz);
-    d.qw[i] = nw * inq;
-    d.qx[i] = nx * inq;
-    d.qy[i] = ny * inq;
-    d.qz[i] = nz * inq;
     // 𝛚 + 𝐌·I⁻¹dt: with 𝐌 = (+0, +0, +0) and a finite I⁻¹dt, fma(+0, I⁻¹dt, w)
     // is w unless w is -0, so a torque-free particle keeps its stored spin
     const bool torque_free = (__double_as_longlong(M[0]) | __double_as_longlong(M[1]) |
@@ -2293,6 +2301,11 @@ __global__ void k_selftest_conv(long long n, unsigned long long seed, unsigned l
     if (product_finite(ia, ib) && not_negzero(x) &&
         __double_as_longlong(__fma_rn(z, ia * ib, x)) != __double_as_longlong(x))
         atomicAdd(bad + 3, 1ull);
+    // the identity orientation: |𝐪|² of (1, +0, +0, +0) as the integrator
+    // forms it is 1, and rsqrt(1) is exactly 1
+    const double one = 1.0 + z;
+    const double nq2 = __fma_rn(z, z, __fma_rn(z, z, __fma_rn(z, z, one * one)));
+    if (__double_as_longlong(rsqrt(nq2)) != 0x3ff0000000000000ll) atomicAdd(bad + 3, 1ull);
 }
 
 void launch_selftest_conv(long long n, unsigned long long seed, unsigned long long* bad,

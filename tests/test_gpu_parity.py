@@ -327,7 +327,8 @@ def test_integer_pipe_conversions_match_hardware(gpu):
     bit-identical to x * 0.5 (zeros, subnormals, exponent edges, infinities);
     where the integrator skips the quaternion increment of a spinless
     particle or the spin update of a torque-free one, the skipped FMA chains
-    would have returned their input bit for bit."""
+    would have returned their input bit for bit, and the identity
+    orientation normalises to itself (rsqrt(1) is exactly 1)."""
     import ctypes
     bad = (ctypes.c_int64 * 4)()
     for seed in (1, 2, 3):
