@@ -122,7 +122,7 @@ L2_FLUSH_BYTES = 256 << 20
 # scaled to a launch by particles processed.
 NCU_TRAFFIC = {
     ("c2", "force"): (6.98368e6, 17576),           # k_force<double>
-    ("c3", "integrate"): (688.167168e6, 2000000),  # k_integrate3 (FP32 mode, no contacts)
+    ("c3", "integrate"): (627.860224e6, 2000000),  # k_integrate3 (FP32 mode, no contacts)
     ("c4", "force"): (145.409024e6, 431416),       # k_force<float>
     ("c4", "integrate"): (184.980224e6, 431416),   # k_integrate3 (FP32 gather)
     ("c4", "contacts"): (35.102976e6, 431416),     # k_search, list step
