@@ -84,14 +84,14 @@ KERNELS_PER_STEP = 3
 # and profiles/k_integrate_batched_64_scenes.md): the force kernel per bond, the
 # integrator per particle, in the FP64 and the FP32 force mode; GB300's FP64
 # pipe width
-FP64_INST = {("force", "fp64"): 117.0, ("force", "fp32"): 15.0,
+FP64_INST = {("force", "fp64"): 114.2, ("force", "fp32"): 15.0,
              ("integrate", "fp64"): 85.7, ("integrate", "fp32"): 51.0}
 # The integrator skips the quaternion increment of a particle with exactly zero
 # spin, the normalisation of a spinless identity orientation and the spin
 # update of a particle with exactly zero torque: in the pour's settling phase
 # (no contacts) that is every particle (ncu on a 400,000-sphere pour:
-# 8,800,000 FP64 thread instructions per launch)
-FP64_INST_WORKLOAD = {("c3", "integrate", "fp32"): 22.0}
+# 7,200,000 FP64 thread instructions per launch)
+FP64_INST_WORKLOAD = {("c3", "integrate", "fp32"): 18.0}
 FP64_LANES_PER_SM = 2
 SM_COUNT = 152
 

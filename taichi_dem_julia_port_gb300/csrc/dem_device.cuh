@@ -135,6 +135,18 @@ __device__ __forceinline__ bool finite_not_negzero(double v) {
     const long long b = __double_as_longlong(v);
     return b != (long long)0x8000000000000000ull && ((b >> 52) & 0x7ff) != 0x7ff;
 }
+// a != 0 (either sign; NaN counts as nonzero), and a < b for a that is +0,
+// positive or NaN and a positive b, on the integer pipe: for binary64 values
+// with a clear sign bit the IEEE order is the order of their bit patterns,
+// and a NaN of either sign compares as an unsigned pattern above every
+// finite positive b, so it compares false as in IEEE.
+__device__ __forceinline__ bool nonzero_bits(double a) {
+    return (__double_as_longlong(a) & 0x7fffffffffffffffll) != 0;
+}
+__device__ __forceinline__ bool less_nonneg(double a, double b) {
+    return (unsigned long long)__double_as_longlong(a) <
+           (unsigned long long)__double_as_longlong(b);
+}
 __device__ __forceinline__ bool product_finite(double a, double b) {
     const int ea = (int)((__double_as_longlong(a) >> 52) & 0x7ff);
     const int eb = (int)((__double_as_longlong(b) >> 52) & 0x7ff);

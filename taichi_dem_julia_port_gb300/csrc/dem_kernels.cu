@@ -1151,8 +1151,10 @@ static __device__ __noinline__ Frame frame_exact_from(double dx, double dy, doub
 __device__ __forceinline__ Frame contact_frame(double dx, double dy, double dz, double ax,
                                                double ay, double az, const SceneParams& S) {
     const double s2 = ay * ay + az * az;
-    if (s2 < S.tol2_lo) return frame_degenerate(ax);
-    if (s2 < S.tol2_x4) return frame_exact_from(dx, dy, dz, S.tol);
+    // s² >= +0 (a sum of squares) and the tolerances are positive: compared
+    // as bit patterns, off the FP64 pipe
+    if (less_nonneg(s2, S.tol2_lo)) return frame_degenerate(ax);
+    if (less_nonneg(s2, S.tol2_x4)) return frame_exact_from(dx, dy, dz, S.tol);
     Frame F;
     F.a1 = ax;
     F.a2 = ay;
@@ -1518,7 +1520,7 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
         const Vec3<double> Ts = rot<double>(R, {wi.x + wj.x, wi.y + wj.y, wi.z + wj.z});
         const Vec3<double> Td = rot<double>(R, {wi.x - wj.x, wi.y - wj.y, wi.z - wj.z});
         const Vec3<T> D = from_d<T>(Dd), Sv = from_d<T>(Ts), Q = from_d<T>(Td);
-        const int small = ri <= rj ? i : j;  // rb = ρ·min(rᵢ, rⱼ)
+        const int small = !less_nonneg(rj, ri) ? i : j;  // rb = ρ·min(rᵢ, rⱼ); radii > 0
         const T tinvL = (T)invL, tdt = (T)dt;
         const T phi = (T)d.b_phic[small] * tinvL * tinvL;
         const T iphi = rcp_nr((T)1.0 + phi);  // 1/(1 + ϕ)
@@ -1906,10 +1908,10 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
     }
     // apply_body_force!  A zero gravity component adds nothing: the force sum
     // starts at +0 and never becomes -0, so F + 0·m is F.
-    if (S.grav[0] != 0.0) F[0] += S.grav[0] * m;
-    if (S.grav[1] != 0.0) F[1] += S.grav[1] * m;
-    if (S.grav[2] != 0.0) F[2] += S.grav[2] * m;
-    if (S.damping != 0.0) {
+    if (nonzero_bits(S.grav[0])) F[0] += S.grav[0] * m;
+    if (nonzero_bits(S.grav[1])) F[1] += S.grav[1] * m;
+    if (nonzero_bits(S.grav[2])) F[2] += S.grav[2] * m;
+    if (nonzero_bits(S.damping)) {
         const double v3[3] = {vx, vy, vz}, w3[3] = {wx, wy, wz};
         double dF[3], dM[3];
 #pragma unroll
