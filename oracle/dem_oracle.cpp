@@ -33,14 +33,24 @@
  * are applied sequentially, so a pair is appended at most once; the reference
  * races there (src/kernels.jl:104-117).
  *
- * Parity status: partially pinned.  The Morton code is pinned against the
- * reference's own morton3d32 (dem.py:758-777, executed from its source by
- * tests/golden/make_golden.py) and README.md:23; the quaternion-to-matrix
- * formula against dem.py:317-344.  Third-party arithmetic with no source in
- * the reference (Morton.jl outside [1,1024], Quaternionic.jl, StaticArrays'
- * norm/inv, Julia's ^ and log) is restated from the published algorithms and
- * is unpinned beyond rounding; the force model is checked by analytic
- * known-answer tests.
+ * Parity status: pinned against the reference's own code where it runs here.
+ *   - Morton code: dem.py's morton3d32 (dem.py:758-777) and README.md:23.
+ *   - Quaternion-to-matrix formula: dem.py:317-344.
+ *   - Contact physics: dem.py's DEMSolver.resolve (EBPM and Hertz-Mindlin,
+ *     dem.py:1357-1606), evaluate_wall/resolve_wall (dem.py:1609-1743),
+ *     apply_body_force (dem.py:1280-1305) and update (dem.py:1309-1354),
+ *     executed from the reference's source on golden cases
+ *     (tests/golden/make_physics_golden.py); the oracle agrees to 1e-12 of
+ *     each vector's magnitude and takes identical breakage and wall-contact
+ *     decisions.  dem.py states kernels.jl's formulas with a few sums
+ *     associated differently, which is why the bound is not zero.
+ * The broad phase and contact bookkeeping follow kernels.jl/executor.jl,
+ * which dem.py does differently (0-based floor cells, per-particle contact
+ * slots); those rows are checked against analytic properties (every touching
+ * pair in cp_list) and the reference's scenes.  Third-party arithmetic with
+ * no source in the reference (Morton.jl outside [1,1024], Quaternionic.jl,
+ * StaticArrays' norm/inv, Julia's ^ and log) is restated from the published
+ * algorithms.
  *
  * Modes: `threads` = 1 runs serially; > 1 runs the per-particle / per-pair /
  * per-contact loops with OpenMP and applies every order-dependent update
@@ -307,6 +317,8 @@ struct Scene {
 };
 
 // ---- setup (src/executor.jl:217-315) --------------------------------------
+void set_tables(Scene& S);
+
 void setup(Scene& S, const DemConfigC& cfg, const DemParticlesIn& p) {
     S.cfg = cfg;
     S.n = p.n;
@@ -342,6 +354,22 @@ void setup(Scene& S, const DemConfigC& cfg, const DemParticlesIn& p) {
     S.H = std::min<int64_t>(std::max<int64_t>(prod, 1 << 20), 1 << 22);
     S.total_steps = (int64_t)std::trunc(cfg.target_time / cfg.dt);
     S.save_per_steps = (int64_t)std::trunc(cfg.saving_interval_time / cfg.dt);
+    set_tables(S);
+    S.wall_contacts.assign(S.n, Contact{});
+    for (int64_t i = 0; i < S.n; ++i) S.wall_contacts[i].i = (int32_t)i;
+    S.forces.assign(3 * S.n, 0.0);
+    S.moments.assign(3 * S.n, 0.0);
+    S.contacts.clear();
+    S.contacts.reserve((size_t)std::max<int64_t>(S.n, 1) * 4);
+    S.ptr_total = S.ptr_inactive = 0;
+    S.active.init(S.n);
+    S.bonded.init(S.n);
+}
+
+// Material, surface and wall tables of src/executor.jl:282-315 (one particle
+// material, mid = 1; the wall material, mid = 2).
+void set_tables(Scene& S) {
+    const DemConfigC& cfg = S.cfg;
     S.mat[0] = {S.material_density, cfg.particle_elastic_modulus, cfg.particle_poisson_ratio};
     S.mat[1] = {cfg.wall_density, cfg.wall_elastic_modulus, cfg.wall_poisson_ratio};
     S.surf[0][0] = {cfg.pp_coefficient_friction, cfg.pp_coefficient_restitution,
@@ -353,15 +381,6 @@ void setup(Scene& S, const DemConfigC& cfg, const DemParticlesIn& p) {
                                    cfg.pw_coefficient_rolling_resistance, 0, 0, 0, 0, 0, 0};
     S.surf[1][1] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     S.wall = {{cfg.wall_normal[0], cfg.wall_normal[1], cfg.wall_normal[2]}, cfg.wall_distance, 1};
-    S.wall_contacts.assign(S.n, Contact{});
-    for (int64_t i = 0; i < S.n; ++i) S.wall_contacts[i].i = (int32_t)i;
-    S.forces.assign(3 * S.n, 0.0);
-    S.moments.assign(3 * S.n, 0.0);
-    S.contacts.clear();
-    S.contacts.reserve((size_t)std::max<int64_t>(S.n, 1) * 4);
-    S.ptr_total = S.ptr_inactive = 0;
-    S.active.init(S.n);
-    S.bonded.init(S.n);
 }
 
 // ---- broad phase (src/executor.jl:38-78, src/utils.jl:1-16, src/kernels.jl:7-58)
@@ -1012,5 +1031,114 @@ void oracle_frame_to_x(const double* a, double tol, double* R9) {
 }
 
 double oracle_jl_norm(const double* a) { return jl_norm(V3{a[0], a[1], a[2]}); }
+
+// Single-contact and single-particle evaluations through the oracle's own
+// resolve_one / resolve_wall / body_and_update, for the golden vectors that
+// tests/golden/make_physics_golden.py computes with the reference's dem.py
+// (DEMSolver.resolve dem.py:1357-1606, evaluate_wall/resolve_wall
+// dem.py:1609-1743, apply_body_force dem.py:1280-1305, update
+// dem.py:1309-1354).  A grain record is 16 doubles:
+//   r, m, k[3], v[3], w[3], q[4] (w,x,y,z), I (isotropic moment of inertia).
+// Material 0 is the particles', material 1 the wall's; the tables come from
+// `cfg` as in `solve` (the particle density does not enter any force).
+static void load_grain(Grain& G, const double* g) {
+    G.id = G.gid = G.mid = 0;
+    G.r = g[0];
+    G.m = g[1];
+    G.V = 0.0;
+    G.r0 = G.r;
+    G.k = {g[2], g[3], g[4]};
+    G.v = {g[5], g[6], g[7]};
+    G.a = {0, 0, 0};
+    G.w = {g[8], g[9], g[10]};
+    for (int c = 0; c < 4; ++c) G.q[c] = g[11 + c];
+    G.dw = {0, 0, 0};
+    G.I = M3{{{g[15], 0.0, 0.0}, {0.0, g[15], 0.0}, {0.0, 0.0, g[15]}}};
+}
+
+static double* put3(double* o, V3 v) {
+    o[0] = v.x; o[1] = v.y; o[2] = v.z;
+    return o + 3;
+}
+
+// One particle-particle contact (i = grain 0, j = grain 1).  `state` is the
+// contact's carried state F[3], ti[3], tj[3], s[3]; `bonded` selects EBPM.
+// out (28): kind (1 bond broken, 2 forces applied), fi, fj, mi, mj, then the
+// contact's new k, F, ti, tj, s.
+int oracle_eval_pair(const DemConfigC* cfg, const double* gi, const double* gj,
+                     const double* state, int bonded, double* out) {
+    Scene S;
+    S.cfg = *cfg;
+    S.n = 2;
+    S.g.resize(2);
+    load_grain(S.g[0], gi);
+    load_grain(S.g[1], gj);
+    set_tables(S);
+    Contact ct{};
+    ct.i = 0; ct.j = 1;
+    ct.F = {state[0], state[1], state[2]};
+    ct.ti = {state[3], state[4], state[5]};
+    ct.tj = {state[6], state[7], state[8]};
+    ct.s = {state[9], state[10], state[11]};
+    ContactResult r = resolve_one(S, ct, bonded != 0);
+    out[0] = r.kind;
+    double* o = out + 1;
+    o = put3(o, r.fi); o = put3(o, r.fj); o = put3(o, r.mi); o = put3(o, r.mj);
+    o = put3(o, r.c.k); o = put3(o, r.c.F); o = put3(o, r.c.ti); o = put3(o, r.c.tj);
+    put3(o, r.c.s);
+    return DEM_OK;
+}
+
+// One particle against the configured wall, with the wall contact's carried
+// shear displacement `s_in`.  out (16): touching, force, moment, then the wall
+// contact's k, F, s.
+int oracle_eval_wall(const DemConfigC* cfg, const double* g, const double* s_in, double* out) {
+    Scene S;
+    S.cfg = *cfg;
+    S.n = 1;
+    S.threads = 1;
+    S.g.resize(1);
+    load_grain(S.g[0], g);
+    set_tables(S);
+    S.wall_contacts.assign(1, Contact{});
+    S.wall_contacts[0].s = {s_in[0], s_in[1], s_in[2]};
+    S.forces.assign(3, 0.0);
+    S.moments.assign(3, 0.0);
+    resolve_wall(S);
+    const Contact& wc = S.wall_contacts[0];
+    out[0] = wc.j == -1 ? 1.0 : 0.0;
+    double* o = out + 1;
+    o = put3(o, {S.forces[0], S.forces[1], S.forces[2]});
+    o = put3(o, {S.moments[0], S.moments[1], S.moments[2]});
+    o = put3(o, wc.k); o = put3(o, wc.F);
+    put3(o, wc.s);
+    return DEM_OK;
+}
+
+// apply_body_force! + update! for n particles whose contact force and moment
+// sums are F, T (3n each).  out (19 per particle): k, v, q, w, then the force
+// and moment after gravity and damping.
+int oracle_eval_update(const DemConfigC* cfg, int64_t n, const double* g, const double* F,
+                       const double* T, double* out) {
+    Scene S;
+    S.cfg = *cfg;
+    S.n = n;
+    S.threads = 1;
+    S.g.resize(n);
+    for (int64_t i = 0; i < n; ++i) load_grain(S.g[i], g + 16 * i);
+    S.forces.assign(F, F + 3 * n);
+    S.moments.assign(T, T + 3 * n);
+    body_and_update(S);
+    for (int64_t i = 0; i < n; ++i) {
+        const Grain& G = S.g[i];
+        double* o = out + 19 * i;
+        o = put3(o, G.k); o = put3(o, G.v);
+        for (int c = 0; c < 4; ++c) *o++ = G.q[c];
+        o = put3(o, G.w);
+        o = put3(o, {S.forces[3 * i], S.forces[3 * i + 1], S.forces[3 * i + 2]});
+        put3(o, {S.moments[3 * i], S.moments[3 * i + 1], S.moments[3 * i + 2]});
+    }
+    return DEM_OK;
+}
 
 }  // extern "C"

@@ -55,6 +55,14 @@ def load() -> C.CDLL:
         "oracle_quat_to_matrix": (None, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "oracle_frame_to_x": (None, [C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_double)]),
         "oracle_jl_norm": (C.c_double, [C.POINTER(C.c_double)]),
+        "oracle_eval_pair": (C.c_int, [C.POINTER(_abi.DemConfigC), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
+                                       C.POINTER(C.c_double)]),
+        "oracle_eval_wall": (C.c_int, [C.POINTER(_abi.DemConfigC), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "oracle_eval_update": (C.c_int, [C.POINTER(_abi.DemConfigC), C.c_int64,
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -217,6 +225,52 @@ def frame_to_x(a, tol: float = 1e-12) -> np.ndarray:
 def jl_norm(a) -> float:
     a = np.ascontiguousarray(a, np.float64)
     return float(load().oracle_jl_norm(ptr(a, C.c_double)))
+
+
+def _d(a) -> np.ndarray:
+    return np.ascontiguousarray(a, np.float64)
+
+
+def grain_record(g: dict) -> np.ndarray:
+    """16-double grain record of the oracle_eval_* helpers: r, m, k, v, w, q, I."""
+    return _d([g["r"], g["m"], *g["k"], *g["v"], *g["w"], *g["q"], g["I"]])
+
+
+def eval_pair(cfg, gi: dict, gj: dict, state, bonded: bool) -> dict:
+    """One contact through the oracle's resolve_one (grain 0 = i, grain 1 = j)."""
+    c = cfg.to_c()
+    a, b, st = grain_record(gi), grain_record(gj), _d(state)
+    out = np.empty(28)
+    _chk(load().oracle_eval_pair(C.byref(c), ptr(a, C.c_double), ptr(b, C.c_double),
+                                 ptr(st, C.c_double), int(bool(bonded)), ptr(out, C.c_double)),
+         "oracle_eval_pair")
+    v = out[1:].reshape(9, 3)
+    return {"kind": int(out[0]), "fi": v[0], "fj": v[1], "mi": v[2], "mj": v[3], "k": v[4],
+            "F": v[5], "ti": v[6], "tj": v[7], "s": v[8]}
+
+
+def eval_wall(cfg, g: dict, s_in) -> dict:
+    """One particle against the configured wall through the oracle's resolve_wall."""
+    c = cfg.to_c()
+    a, s = grain_record(g), _d(s_in)
+    out = np.empty(16)
+    _chk(load().oracle_eval_wall(C.byref(c), ptr(a, C.c_double), ptr(s, C.c_double),
+                                 ptr(out, C.c_double)), "oracle_eval_wall")
+    v = out[1:].reshape(5, 3)
+    return {"touch": int(out[0]), "f": v[0], "m": v[1], "k": v[2], "F": v[3], "s": v[4]}
+
+
+def eval_update(cfg, grains: list, F, T) -> dict:
+    """apply_body_force! + update! for the given grains and contact sums."""
+    c = cfg.to_c()
+    n = len(grains)
+    g = _d(np.concatenate([grain_record(x) for x in grains]))
+    f, t = _d(F).reshape(-1), _d(T).reshape(-1)
+    out = np.empty((n, 19))
+    _chk(load().oracle_eval_update(C.byref(c), n, ptr(g, C.c_double), ptr(f, C.c_double),
+                                   ptr(t, C.c_double), ptr(out, C.c_double)), "oracle_eval_update")
+    return {"k": out[:, 0:3], "v": out[:, 3:6], "q": out[:, 6:10], "w": out[:, 10:13],
+            "F": out[:, 13:16], "T": out[:, 16:19]}
 
 
 def host_threads() -> int:

@@ -89,8 +89,15 @@ def oracle_vectors() -> dict:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None,
+                    help="reference checkout (default: $DEM_REFERENCE, else ../reference)")
     args = ap.parse_args()
+    if args.reference is None:
+        from tests.reference_scenes import reference_checkout
+        found = reference_checkout()
+        if found is None:
+            ap.error("no reference checkout: give --reference PATH or set DEM_REFERENCE")
+        args.reference = str(found)
     rng = np.random.default_rng(20231203)
     ns = reference_functions(Path(args.reference) / "dem.py")
     golden = {

@@ -29,9 +29,16 @@ SCENES = {"carom": "cfg/1.toml", "cube_911": "cfg/2.toml"}
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None,
+                    help="reference checkout (default: $DEM_REFERENCE, else ../reference)")
     ap.add_argument("--out", default=str(HERE / "reference_scenes.npz"))
     args = ap.parse_args()
+    if args.reference is None:
+        from tests.reference_scenes import reference_checkout
+        found = reference_checkout()
+        if found is None:
+            ap.error("no reference checkout: give --reference PATH or set DEM_REFERENCE")
+        args.reference = str(found)
     from taichi_dem_julia_port_gb300 import DEMConfig, load_particles
 
     ref = Path(args.reference)

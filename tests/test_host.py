@@ -12,7 +12,10 @@ from taichi_dem_julia_port_gb300 import _abi, p4io, scenes
 from taichi_dem_julia_port_gb300.config import DEMConfig
 
 ROOT = Path(__file__).resolve().parents[1]
-REF_CFG = Path("/root/reference/cfg")
+from tests.reference_scenes import reference_checkout  # noqa: E402
+
+_REF = reference_checkout()
+REF_CFG = _REF / "cfg" if _REF is not None else Path("reference-checkout-absent")
 
 
 def header_functions():

@@ -37,6 +37,127 @@ def test_quaternion_matrix_matches_reference(oracle_lib, ref_golden):
         np.testing.assert_allclose(R.ravel(), rec["R"], rtol=0, atol=1e-14)
 
 
+# ---- physics pinned to the reference's dem.py ----------------------------------
+# tests/golden/reference_physics.json holds the outputs of dem.py's own
+# DEMSolver.resolve (EBPM dem.py:1405-1528, Hertz-Mindlin dem.py:1529-1606),
+# resolve_wall/evaluate_wall (dem.py:1609-1743), apply_body_force
+# (dem.py:1280-1305) and update (dem.py:1309-1354), executed from the
+# reference's source (tests/golden/make_physics_golden.py).  dem.py and
+# src/kernels.jl state the same formulas; they differ only in the association
+# of a few sums (the Rodrigues term, the position update, the quaternion
+# increments), in normalize (v/|v| against inv(|v|)·v) and in the 3x3 inverse
+# (adjugate/determinant against column cross products), so the oracle, which
+# follows kernels.jl, agrees with them to rounding: measured at most 1.8e-14
+# of each vector's magnitude.  The stated bound is 1e-12.  Discrete outcomes
+# (bond broken or not, wall contact or not) must be identical, including
+# strengths placed a relative 1e-9 below and above the stress a case reaches.
+PHYS_RTOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def phys_golden():
+    return json.loads((GOLDEN / "reference_physics.json").read_text())
+
+
+def _cfg_of(p: dict) -> DEMConfig:
+    return DEMConfig(
+        particle_elastic_modulus=p["E"], particle_poisson_ratio=p["nu"],
+        wall_elastic_modulus=p["wall_E"], wall_poisson_ratio=p["wall_nu"],
+        pp_coefficient_friction=p["mu"], pp_coefficient_restitution=p["e"],
+        pw_coefficient_friction=p["pw_mu"], pw_coefficient_restitution=p["pw_e"],
+        bond_radius_ratio=p["bond_ratio"], bond_elastic_modulus=p["bond_E"],
+        bond_poisson_ratio=p["bond_nu"], bond_compressive_strength=p["sc"],
+        bond_tensile_strength=p["st"], bond_shear_strength=p["ss"], dt=p["dt"],
+        gravity=list(p["gravity"]), global_damping=p["global_damping"],
+        wall_normal=list(p["wall_n"]), wall_distance=p["wall_d"], tolerance=1e-12)
+
+
+def _close(got, want, what):
+    got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
+    scale = float(np.abs(want).max())
+    err = float(np.abs(got - want).max())
+    assert err <= PHYS_RTOL * scale, f"{what}: |d| {err:.3e} > {PHYS_RTOL:g}·{scale:.3e}"
+
+
+def test_bond_forces_match_reference_dem_py(oracle_lib, phys_golden):
+    """EBPM: increments k1..k6, accumulated force and moments, particle forces
+    and moments, for random frames and the degenerate ones (bond along ±x)."""
+    n_intact = 0
+    for c in phys_golden["bond"]:
+        if c["out"]["bonded"] == 0:
+            continue
+        o = O.eval_pair(_cfg_of(c["params"]), c["gi"], c["gj"], c["state"], True)
+        assert o["kind"] == 2
+        for k in ("fi", "fj", "mi", "mj", "k", "F", "ti", "tj"):
+            _close(o[k], c["out"][k], f"bond {k}")
+        n_intact += 1
+    assert n_intact >= 60
+
+
+def test_bond_breakage_decisions_match_reference_dem_py(oracle_lib, phys_golden):
+    """σc, σt, τ against strengths a relative 1e-9 below (breaks) and above
+    (holds) the stress each case reaches; a broken bond applies no force."""
+    modes = set()
+    for c in phys_golden["bond"]:
+        o = O.eval_pair(_cfg_of(c["params"]), c["gi"], c["gj"], c["state"], True)
+        broken = c["out"]["bonded"] == 0
+        assert (o["kind"] == 1) == broken, c.get("threshold")
+        assert c["out"]["active"] == (0 if broken else 1)
+        if broken:
+            assert not np.any(c["out"]["fi"]) and not np.any(o["fi"])
+        if "threshold" in c:
+            t = c["threshold"]
+            assert broken == (t["rel"] < 1.0)
+            modes.add(t["mode"])
+    assert modes == {"sc", "st", "ss"}
+
+
+def test_hertz_forces_match_reference_dem_py(oracle_lib, phys_golden):
+    """Hertz-Mindlin: new and carried shear histories, sliding and sticking,
+    spinning and spinless grains, degenerate and near-degenerate frames."""
+    sliding = 0
+    for c in phys_golden["hertz"]:
+        o = O.eval_pair(_cfg_of(c["params"]), c["gi"], c["gj"], c["state"], False)
+        assert o["kind"] == 2
+        for k in ("fi", "fj", "mi", "mj", "k", "F", "s"):
+            _close(o[k], c["out"][k], f"hertz {k}")
+        F = np.asarray(c["out"]["F"])
+        sliding += abs(np.hypot(F[1], F[2]) - c["params"]["mu"] * F[0]) <= 1e-9 * abs(F[0])
+    assert 20 <= sliding <= len(phys_golden["hertz"]) - 20
+
+
+def test_wall_forces_match_reference_dem_py(oracle_lib, phys_golden):
+    """Particle-wall Hertz-Mindlin on both sides of the plane, axis-aligned
+    and oblique normals, carried or new shear history, and non-touching cases."""
+    touching = 0
+    for c in phys_golden["wall"]:
+        o = O.eval_wall(_cfg_of(c["params"]), c["g"], c["s_in"])
+        assert o["touch"] == c["out"]["touch"]
+        if not o["touch"]:
+            assert not np.any(o["f"]) and not np.any(c["out"]["f"])
+            continue
+        touching += 1
+        for k in ("f", "m", "k", "F", "s"):
+            _close(o[k], c["out"][k], f"wall {k}")
+    assert touching >= 80
+
+
+def test_body_force_and_update_match_reference_dem_py(oracle_lib, phys_golden):
+    """Gravity, global damping (including sign(0) = 0 on zero velocity and
+    spin components) and the integrator: position, velocity, quaternion and
+    spin after one update."""
+    dampings = set()
+    for c in phys_golden["update"]:
+        o = O.eval_update(_cfg_of(c["params"]), c["grains"], c["F"], c["T"])
+        dampings.add(c["params"]["global_damping"])
+        for i, ref in enumerate(c["out"]):
+            np.testing.assert_array_equal(o["F"][i], ref["F"])
+            np.testing.assert_array_equal(o["T"][i], ref["T"])
+            for k in ("k", "v", "q", "w"):
+                _close(o[k][i], ref[k], f"update {k}")
+    assert len(dampings) >= 3 and 0.0 in dampings
+
+
 def test_frame_maps_normal_to_x(oracle_lib):
     rng = np.random.default_rng(0)
     for _ in range(100):
@@ -198,14 +319,13 @@ def test_capacity_error(oracle_lib):
 def test_reference_scenes_fixture(oracle_lib):
     """The packed reference scenes equal a fresh read of the reference's files
     (when the reference checkout is present) and run on the oracle."""
-    from pathlib import Path as _P
     from taichi_dem_julia_port_gb300 import DEMConfig, load_particles
     from tests import reference_scenes as rs
-    ref = _P("/root/reference")
+    ref = rs.reference_checkout()
     for name, cfg_rel in (("carom", "cfg/1.toml"), ("cube_911", "cfg/2.toml")):
         cfg, p, src = rs.load(name)
         assert src.startswith(cfg_rel)
-        if ref.exists():
+        if ref is not None:
             cfg2 = DEMConfig.from_toml(ref / cfg_rel)
             p2 = load_particles((ref / cfg_rel).parent / cfg2.init_particles)
             assert cfg2.to_toml() == cfg.to_toml()
