@@ -7,15 +7,31 @@ plane, FP64, dt = 1e-6 s.  One "step" is one DEM time step (`simulate!`).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-Our arm: W untimed steps, then K steps each timed with CUDA events on the
-library's stream, with a 256 MiB write between steps to flush L2 (the scene
-itself fits in L2).  value = particle-steps/s over all ranks (max time over
-ranks).  `e2e` repeats the metric through the C ABI with host buffers: every
-step uploads the particle state from page-locked host arrays, steps, and
-reads it back into them (one dem_step_exchange call per step, through
-GlobalData.state_buffers).  `roofline` reports the dominant kernel
-from per-phase CUDA events (dem_step_profiled).  `cpu_baseline` times the CPU
-oracle (OpenMP, all host threads) on a bounded sample of the same workload.
+Our arm: --advance untimed steps (default 4,000 for the 17,576-sphere cube:
+the cube meets the wall after about 50 steps and its stress wave has crossed
+it by about 3,000, so the timed window lies in the fragmentation, with wall
+contacts, Hertz contacts between fragments and bonds breaking), W untimed
+warm-up steps, then K steps each timed with CUDA
+events on the library's stream, with a 256 MiB write between steps to flush
+L2 (the scene itself fits in L2).  value = particle-steps/s over all ranks
+(max time over ranks); `config.timed_window` gives the window's first step,
+mean contact and bond counts, wall contacts, bonds broken and full pair
+searches.  `e2e` repeats the metric through the C ABI with host buffers on
+the same window (replayed from its first state until at least --e2e-steps
+steps are timed): every step uploads the particle state from page-locked host
+arrays, steps, and reads it back into them (one dem_step_exchange call per
+step, through GlobalData.state_buffers).  `roofline` reports the dominant
+kernel from per-phase CUDA events (dem_step_profiled) over the same window,
+against its algorithmic bytes (every field once per unit; re-reads from L2
+are `gather_bytes`).  `cpu_baseline` times the CPU oracle (OpenMP, all host
+threads) from the window's first state.  The clock sampler polls every 20 ms;
+a window shorter than five samples is followed by untimed steps of the same
+load until five are in (`clocks.padding_steps`).
+
+The default line also carries `batched` (below), `pour` (the 2,000,000-sphere
+pour settling, and pre-compacted into a bed with about one contact per sphere)
+and `served` (a 100-request Poisson stream with step counts scaled by 0.05,
+p50/p99 completion latency, against the plain FP64 path scene by scene).
 
 --workload c4 steps 256 independent scenes (500-20,000 spheres each, half
 bonded cubes, half pours, FP32 force / FP64 state) together in one arena,
@@ -54,36 +70,60 @@ sys.path.insert(0, str(ROOT))
 
 import numpy as np  # noqa: E402
 
-# Algorithmic bytes of the force kernel per contact, from its SoA field list
-# (k_force in dem_kernels.cu): contact ids + flags (12 B), particle gathers of
-# i and j (pos, vel, ω, r, m: 2 × 88 B), contact state read (bond: 𝐅, 𝛕ᵢ, 𝛕ⱼ 72 B;
-# Hertz: 𝐬 24 B), state write (bond: 𝐤, 𝐅, 𝛕ᵢ, 𝛕ⱼ, 𝐬 120 B; Hertz: 𝐤, 𝐅, 𝐬 72 B),
-# force contributions (9 × 8 B).
-FORCE_BYTES_BOND = 12 + 176 + 72 + 120 + 72
-FORCE_BYTES_HERTZ = 12 + 176 + 24 + 72 + 72
-# Compaction per surviving contact: ids + flags read and written (2 × 12 B),
-# the carried state read and written (bond 𝐅, 𝛕ᵢ, 𝛕ⱼ: 2 × 72 B; Hertz 𝐬:
-# 2 × 24 B) and the incoming-list entry (8 B).
-COMPACT_BYTES_BOND = 24 + 144 + 8
-COMPACT_BYTES_HERTZ = 24 + 48 + 8
-# Algorithmic bytes of the other phases per particle / per contact
-BROADPHASE_BYTES_PER_PARTICLE = 24 + 16 + 4 + 4 + 4 + 8 + 24 + 8 + 32 + 16  # hash..canon
-INTEGRATE_BYTES_PER_PARTICLE = 13 * 8 * 2 + 4 * 8 + 6 * 8 + 3 * 8 * 2 + 8 + 4  # state r/w
-# the pour settles without contacts: every particle is torque-free and keeps
+# Algorithmic bytes: every field a kernel must move, counted once per unit
+# (particle fields once per particle, contact columns once per contact), from
+# the kernels' SoA field lists in dem_kernels.cu.
+#
+# k_force, per contact: ids, flags and the carried-state slot read (16 B); the
+# entry in the partner's incoming list (counter read and written, entry
+# written: 16 B); the nine force contributions written (72 B); a bond reads
+# its carried F, tau_i, tau_j (72 B) and writes k, F, tau_i, tau_j (96 B); a
+# Hertz contact reads s (24 B) and writes k, F, s (72 B).  Per particle, once:
+# position, velocity, spin, radius, mass and the bond section constants
+# (112 B).  A particle gathered again by its second and later contacts is a
+# re-read served from L2: reported apart as `gather_bytes` (88 B per contact
+# end beyond the first), not counted as algorithmic.
+FORCE_BYTES_BOND = 16 + 16 + 72 + 72 + 96
+FORCE_BYTES_HERTZ = 16 + 16 + 72 + 24 + 72
+FORCE_BYTES_PER_PARTICLE = 112
+GATHER_BYTES_PER_CONTACT_END = 88
+# k_integrate, per particle: reads position, velocity, spin, quaternion, 1/m,
+# r, 1/I, wall shear, row bounds and incoming count (164 B); writes position,
+# velocity, spin, quaternion, wall shear, force and moment totals, the FP32
+# position and the incoming count (196 B).  Per contact: its nine
+# contributions and its incoming-list entry read (80 B).
+INTEGRATE_BYTES_PER_PARTICLE = 164 + 196
+INTEGRATE_BYTES_PER_CONTACT = 80
+# a pour settling without contacts: every particle is torque-free and keeps
 # the identity orientation, so the integrator writes neither its spin (24 B)
 # nor its quaternion (32 B)
-INTEGRATE_BYTES_WORKLOAD = {"c3": INTEGRATE_BYTES_PER_PARTICLE - 3 * 8 - 4 * 8}
-# neighbour-list step per particle: path byte, current row bounds, list length,
-# FP32 position, next row bounds written, 4 list partners (index + FP32
-# position); the row rebuild adds the compaction bytes per surviving contact
-DETECT_BYTES_PER_PARTICLE = 1 + 8 + 4 + 16 + 8 + 4 * (4 + 16)
+INTEGRATE_BYTES_SETTLING = INTEGRATE_BYTES_PER_PARTICLE - 3 * 8 - 4 * 8
+# k_search on a neighbour-list step, per particle: path byte, current row
+# bounds, list length, FP32 position, next row bounds written, four list
+# partner indices (53 B; the partners' FP32 positions are re-reads); per
+# surviving contact: partner and flags read, survival flag written and read,
+# the next row's ids, flags and carried-state slot written (26 B).
+DETECT_BYTES_PER_PARTICLE = 1 + 8 + 4 + 16 + 8 + 4 * 4
+ROW_BYTES_PER_CONTACT = 8 + 2 + 16
+
+
+def algorithmic_bytes(n: int, contacts: int, bonds: int, settling: bool = False) -> dict:
+    """Algorithmic bytes of one step's three kernels (see the constants)."""
+    hertz = contacts - bonds
+    integ = INTEGRATE_BYTES_SETTLING if settling and contacts == 0 else INTEGRATE_BYTES_PER_PARTICLE
+    return {"force": bonds * FORCE_BYTES_BOND + hertz * FORCE_BYTES_HERTZ
+            + (n * FORCE_BYTES_PER_PARTICLE if contacts else 0),
+            "integrate": n * integ + contacts * INTEGRATE_BYTES_PER_CONTACT,
+            "contacts": n * DETECT_BYTES_PER_PARTICLE + contacts * ROW_BYTES_PER_CONTACT}
+
+
 # k_search (contact update: full search or lists, next rows), k_force, k_integrate
 KERNELS_PER_STEP = 3
-# FP64-pipe instructions per unit (ncu sm__thread_inst_executed_pipe_fp64_pred_on.sum
-# per launch over the units it processed; profiles/k_force_fp64_bonded_cube_17576.md
-# and profiles/k_integrate_batched_64_scenes.md): the force kernel per bond, the
-# integrator per particle, in the FP64 and the FP32 force mode; GB300's FP64
-# pipe width
+# FP64-pipe instructions per unit, from ncu (sm__thread_inst_executed_pipe_fp64_pred_on.sum
+# of one launch over the units it processed): the force kernel per bond (the
+# 17,576-sphere cube before its impact, every contact a bond), the integrator
+# per particle (64 scenes of the batched workload), in the FP64 and the FP32
+# force mode; then GB300's FP64 pipe width
 FP64_INST = {("force", "fp64"): 114.2, ("force", "fp32"): 15.0,
              ("integrate", "fp64"): 85.7, ("integrate", "fp32"): 51.0}
 # The integrator skips the quaternion increment of a particle with exactly zero
@@ -97,36 +137,42 @@ SM_COUNT = 152
 
 
 def fp64_roofline(kernel: str, precision: str, n_particles: int, n_bond: int, ms: float,
-                  sm_mhz, workload: str | None = None) -> dict | None:
-    """The FP64-pipe roofline of the force kernel (per bond; bonded scenes) or
-    the integrator (per particle): FP64 instructions over the live per-phase
-    time against the pipe's peak at the sampled SM clock."""
+                  clk: dict, peaks: dict, workload: str | None = None) -> dict | None:
+    """The FP64-pipe roofline of the force kernel (per bond, on a scene whose
+    contacts are all bonds) or the integrator (per particle): FP64
+    instructions over the live per-phase time against the pipe's peak at the
+    SM clock sampled during the timed region (else the measured maximum
+    clock of MEASURED_PEAKS.json, else 2,070 MHz), saying which."""
     per = FP64_INST_WORKLOAD.get((workload, kernel, precision), FP64_INST.get((kernel, precision)))
     units = n_bond if kernel == "force" else n_particles
     if per is None or not units or not ms:
         return None
-    sm_mhz = sm_mhz or 2070.0
+    if clk.get("sm_mhz"):
+        sm_mhz, src = clk["sm_mhz"], "the median SM clock sampled during the timed region"
+    elif peaks.get("sm_max_mhz"):
+        sm_mhz, src = float(peaks["sm_max_mhz"]), "the maximum SM clock of MEASURED_PEAKS.json"
+    else:
+        sm_mhz, src = 2070.0, "the nominal maximum SM clock"
     peak = FP64_LANES_PER_SM * SM_COUNT * sm_mhz * 1e6 / 1e9
     ach = per * units / (ms * 1e-3) / 1e9
     return {"unit": "G FP64 thread-instructions/s", "achieved": ach, "peak": peak,
             "frac": ach / peak, "inst_per_unit": per,
             "unit_counted": "bond" if kernel == "force" else "particle",
-            "peak_source": f"nominal: {FP64_LANES_PER_SM} FP64 lanes per SM per cycle x "
-                           f"{SM_COUNT} SMs at the sampled {sm_mhz:.0f} MHz"}
+            "peak_source": f"{FP64_LANES_PER_SM} FP64 lanes per SM per cycle x {SM_COUNT} SMs "
+                           f"at {sm_mhz:.0f} MHz ({src})"}
 L2_FLUSH_BYTES = 256 << 20
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
-# of each dominant kernel, from one ncu capture each (the summaries under
-# profiles/), with the particles that launch processed.  The batched captures
-# ran on the first 64 scenes of the batch (431,416 spheres); their traffic is
-# scaled to a launch by particles processed.
+# of each dominant kernel, from one ncu capture each, with the particles that
+# launch processed.  The batched captures ran on the first 64 scenes of the
+# batch (431,416 spheres); their traffic is scaled to a launch by particles
+# processed.  Keys: workload and timed window ("c2" the cube in its impact
+# window, "c3" the pour settling, "c3bed" the compacted bed), kernel.
 NCU_TRAFFIC = {
-    ("c2", "force"): (6.98368e6, 17576),           # k_force<double>
     ("c3", "integrate"): (627.860224e6, 2000000),  # k_integrate3 (FP32 mode, no contacts)
     ("c4", "force"): (145.409024e6, 431416),       # k_force<float>
     ("c4", "integrate"): (184.980224e6, 431416),   # k_integrate3 (FP32 gather)
     ("c4", "contacts"): (35.102976e6, 431416),     # k_search, list step
-    ("c2", "contacts"): (2.096128e6, 17576),       # k_search, list step
     ("c3", "contacts"): (43.205888e6, 2000000),    # k_search, list step (wide pass)
 }
 
@@ -161,7 +207,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -176,6 +222,10 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def count(self) -> int:
+        """Samples taken since the timed region started."""
+        return len(self.lines) if self.proc else 1 << 30
 
     def stop(self) -> dict:
         if not self.proc:
@@ -342,11 +392,7 @@ def run_batched(args, lib, quick: bool = False, dist=None) -> dict:
         g.close()
     plain = n_total / (plain_ms * 1e-3) if plain_ms > 0 else None
     peaks = load_peaks()
-    force_bytes = bonded * FORCE_BYTES_BOND + (contacts - bonded) * FORCE_BYTES_HERTZ
-    alg = {"force": force_bytes,
-           "integrate": n_total * INTEGRATE_BYTES_PER_PARTICLE,
-           "contacts": n_total * DETECT_BYTES_PER_PARTICLE
-           + bonded * COMPACT_BYTES_BOND + (contacts - bonded) * COMPACT_BYTES_HERTZ}
+    alg = algorithmic_bytes(n_total, contacts, bonded)
     dom = max(ph, key=ph.get)
     roof = {"bound": "hbm", "kernel": dom, "unit": "GB/s", "peak": peaks["hbm_gbs"],
             "peak_source": peaks["source"], "traffic": ncu_traffic("c4", dom, n_total),
@@ -354,8 +400,8 @@ def run_batched(args, lib, quick: bool = False, dist=None) -> dict:
     if dom in alg:
         ach = alg[dom] / (ph[dom] * 1e-3) / 1e9
         roof.update({"achieved": ach, "frac": ach / peaks["hbm_gbs"], "algorithmic_bytes": alg[dom]})
-    fr = fp64_roofline(dom, precision, n_total, bonded, ph.get(dom),
-                       clk.get("sm_mhz") or peaks.get("sm_max_mhz"))
+    fr = None if dom == "force" and contacts != bonded else fp64_roofline(
+        dom, precision, n_total, bonded, ph.get(dom), clk, peaks)
     if fr:
         roof["fp64_pipe"] = fr
     perr = None
@@ -553,7 +599,7 @@ def run_reference(args) -> None:
     o = OracleScene(sc.cfg, sc.particles, threads=threads)
     if sc.bonded:
         o.initialize()
-    o.simulate(args.warmup)
+    o.simulate(args.advance + args.warmup)  # the same timed window as the GPU arm
     t0 = time.perf_counter()
     o.simulate(args.steps)
     dt_s = time.perf_counter() - t0
@@ -564,10 +610,14 @@ def run_reference(args) -> None:
         "warmup": args.warmup, "ms_per_step": 1e3 * dt_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded lattice)",
-        "config": {"workload": desc, "n_particles": sc.n, "parallelism": "cpu-openmp"},
+        "config": {"workload": desc, "n_particles": sc.n, "parallelism": "cpu-openmp",
+                   "timed_window": {"start_step": args.advance + args.warmup + 1,
+                                    "steps": args.steps}},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads,
                          "kind": "port",
-                         "sample": f"{args.steps} steps of the full workload after {args.warmup} warm-up steps"},
+                         "sample": f"steps {args.advance + args.warmup + 1}-"
+                                   f"{args.advance + args.warmup + args.steps} of the full "
+                                   "workload (the GPU arm's timed window)"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "note": "CPU restatement of the reference step (oracle/dem_oracle.cpp); the reference's "
@@ -576,18 +626,19 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def run_proxy(args, sc, flush) -> dict:
+def run_proxy(args, sc, flush, advance: int) -> dict:
     """The reference-structured GPU proxy (baseline/refproxy: the reference's
     kernel decomposition, AoS records, BitTables and three host reads per
-    step, in plain CUDA C++) on the same scene, timed the same way: after the
-    same warm-up, one step at a time between L2 flushes, CUDA events."""
+    step, in plain CUDA C++) on the same scene and window, timed the same way:
+    `advance` untimed steps and the same warm-up, then one step at a time
+    between L2 flushes, CUDA events."""
     import torch
     from baseline.refproxy import RefProxy
     p = RefProxy(sc.cfg, sc.particles)
     if sc.bonded:
         p.initialize()
     steps = min(args.steps, 500)
-    for _ in range(args.warmup):
+    for _ in range(advance + args.warmup):
         p.simulate(1)
     total = 0.0
     for _ in range(steps):
@@ -597,19 +648,33 @@ def run_proxy(args, sc, flush) -> dict:
     p.close()
     ms = total / steps
     return {"value": sc.n / (ms * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms,
-            "steps": steps, "warmup": args.warmup,
+            "steps": steps, "warmup": args.warmup, "start_step": advance + args.warmup,
             "kind": "reference-structured CUDA C++ proxy for the reference's CUDA.jl path "
                     "(AoS 272/136-byte records, BitTables, ~25 launches and 3 device-to-host "
                     "reads per step); the CUDA.jl path itself cannot run on this GPU"}
 
 
-def cpu_baseline(sc, seconds: float) -> dict:
+def snapshot(g) -> dict:
+    """A handle's particle and contact state (for restoring a window)."""
+    return {"particles": g.particles(forces=False), "contacts": g.contacts()}
+
+
+def restore(h, snap: dict) -> None:
+    """Puts a snapshot into a GPU handle or an oracle scene."""
+    p = snap["particles"]
+    h.set_particles(pos=p["pos"], vel=p["vel"], omega=p["omega"], quat=p["quat"],
+                    wall_shear=p["wall_shear"])
+    h.set_contacts(snap["contacts"])
+
+
+def cpu_baseline(sc, snap: dict, seconds: float, start_step: int) -> dict:
+    """The CPU oracle (all host threads) from the timed window's first state,
+    for about `seconds`."""
     from oracle.oracle import OracleScene, host_threads
     threads = host_threads()
     o = OracleScene(sc.cfg, sc.particles, threads=threads)
-    if sc.bonded:
-        o.initialize()
-    o.simulate(2)
+    restore(o, snap)
+    o.simulate(1)
     steps, t0 = 0, time.perf_counter()
     while True:
         o.simulate(1)
@@ -619,7 +684,193 @@ def cpu_baseline(sc, seconds: float) -> dict:
             break
     return {"value": sc.n * steps / el, "unit": "particle-steps/s", "cores": threads,
             "kind": "port",
-            "sample": f"{steps} steps ({el:.1f} s) of the same scene from t=0 on the CPU oracle"}
+            "sample": f"{steps} steps ({el:.1f} s) of the same scene from step {start_step + 1} "
+                      "(the timed window's state) on the CPU oracle"}
+
+
+def wall_contacts(snap: dict) -> int:
+    return int(np.count_nonzero(np.any(snap["particles"]["wall_shear"] != 0, axis=1)))
+
+
+def measure_scene(args, lib, sc, precision: str, steps: int, warmup: int, advance: int, flush,
+                  dist=None, ws: int = 1, settling: bool = False, e2e_min_steps: int = 0,
+                  profile_steps: int = 20, traffic_key: str = "") -> dict:
+    """One scene on a single-scene handle: `advance` untimed steps (past the
+    start-up transient, e.g. into a cube's wall impact), `warmup` flushed
+    steps, then `steps` timed steps, each after an L2 flush and bracketed by
+    CUDA events on the library's stream.  Returns the window's numbers; the
+    handle's state at the window's first step is kept (`snap`) so that the
+    per-phase profile, the end-to-end loop and the CPU baseline run the same
+    window."""
+    import torch
+    from taichi_dem_julia_port_gb300 import GlobalData
+    g = GlobalData(sc.cfg, sc.particles, precision=precision, lib=lib)
+    if sc.bonded:
+        g.initialize()
+    if advance:
+        g.simulate(advance)
+        g.sync()
+
+    def flushed_step() -> float:
+        flush.zero_()
+        torch.cuda.synchronize()
+        return g.simulate_timed(1)
+
+    for _ in range(warmup):
+        flushed_step()
+    snap = snapshot(g)
+    s0 = g.stats()
+    clocks = ClockSampler(torch.cuda.current_device())
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    total_ms, contacts, bonds = 0.0, [], []
+    s1 = s0
+    for _ in range(steps):
+        total_ms += flushed_step()
+        s1 = g.stats()
+        contacts.append(s1["contacts"])
+        bonds.append(s1["bonded"])
+    # the sampler polls every 20 ms: a short window keeps the same load on
+    # (untimed steps) until five samples are in
+    pad = 0
+    while clocks.count() < 5 and pad < 20000:
+        flushed_step()
+        pad += 1
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    clk["padding_steps"] = pad
+    if dist:
+        dist.barrier()
+        total_ms = max_over_ranks(total_ms, dist)
+    ms_per_step = total_ms / steps
+    window = {"start_step": s0["steps_done"] + 1, "steps": steps,
+              "contacts_mean": float(np.mean(contacts)), "bonds_mean": float(np.mean(bonds)),
+              "hertz_contacts_mean": float(np.mean(contacts) - np.mean(bonds)),
+              "wall_contacts_at_start": wall_contacts(snap),
+              "bonds_broken_in_window": s1["bonds_broken"] - s0["bonds_broken"],
+              "bonds_broken_total": s1["bonds_broken"],
+              "full_searches_in_window": s1["full_searches"] - s0["full_searches"]}
+    # per-phase device times over the same window (eager launches, L2 flushed)
+    restore(g, snap)
+    phases = []
+    for _ in range(profile_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        phases.append(g.simulate_profiled())
+    ph = {k: float(np.mean([q[k] for q in phases])) for k in phases[0]}
+    c_mean, b_mean = window["contacts_mean"], window["bonds_mean"]
+    alg = algorithmic_bytes(sc.n, int(round(c_mean)), int(round(b_mean)), settling)
+    dom = max(ph, key=ph.get)
+    peaks = load_peaks()
+    roof = {"bound": "hbm", "kernel": dom, "unit": "GB/s", "peak": peaks["hbm_gbs"],
+            "peak_source": peaks["source"], "phase_ms": ph, "algorithmic_bytes": alg[dom],
+            "achieved": alg[dom] / (ph[dom] * 1e-3) / 1e9,
+            "traffic": ncu_traffic(traffic_key, dom, sc.n)}
+    roof["frac"] = roof["achieved"] / peaks["hbm_gbs"]
+    if dom == "force":
+        # re-reads of particles gathered by more than one contact (L2 hits)
+        roof["gather_bytes"] = max(0, 2 * int(round(c_mean)) - sc.n) * GATHER_BYTES_PER_CONTACT_END
+    fr = None if dom == "force" and c_mean != b_mean else fp64_roofline(
+        dom, precision, sc.n, int(round(b_mean)), ph.get(dom), clk, peaks,
+        "c3" if settling else None)
+    if fr:
+        roof["fp64_pipe"] = fr
+    out = {"value": ws * sc.n * steps / (total_ms / 1e3), "ms_per_step": ms_per_step,
+           "contact_steps_per_s": ws * c_mean * steps / (total_ms / 1e3), "window": window,
+           "roofline": roof, "clocks": clk, "snap": snap, "n": sc.n}
+    if e2e_min_steps:
+        # end to end through the public API with host buffers, on the same
+        # window: page-locked state arrays bound to the handle
+        # (GlobalData.state_buffers) are uploaded, stepped and read back every
+        # step (one dem_step_exchange call); the window is replayed from its
+        # first state until at least e2e_min_steps steps are timed
+        buf = g.state_buffers()
+        h2d = sum(a.nbytes for a in buf.arrays.values())
+        reps = max(1, math.ceil(e2e_min_steps / steps))
+        e2e_s = 0.0
+        for _ in range(reps):
+            restore(g, snap)
+            buf.download()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                buf.step(1)  # upload, step, download (dem_step_exchange)
+            e2e_s += time.perf_counter() - t0
+        buf.close()
+        e2e_s = max_over_ranks(e2e_s, dist)
+        n_e2e = reps * steps
+        e2e = {"value": ws * sc.n * n_e2e / e2e_s, "unit": "particle-steps/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
+               "steps": n_e2e, "window_replays": reps, "ms_per_step": 1e3 * e2e_s / n_e2e}
+        link = host_link(int(h2d))
+        e2e["host_link"] = link
+        e2e["bound_ms_per_step"] = ms_per_step + 1e3 * h2d * (1 / link["h2d_gbs"] +
+                                                              1 / link["d2h_gbs"]) / 1e9
+        out["e2e"] = e2e
+    g.close()
+    return out
+
+
+def pour_summary(args, lib, flush) -> dict:
+    """The 2,000,000-sphere pour (FP32 force, dt 2e-7) in two phases: settling
+    (the seeded non-overlapping start, free fall: no contacts) and a
+    pre-compacted bed of the same spheres with about one contact per sphere
+    (scenes.granular_bed)."""
+    from taichi_dem_julia_port_gb300 import scenes
+    out = {"metric": "particle-steps/s", "precision": "fp32"}
+    steps = min(args.steps, args.pour_steps)
+    for name, sc, settling in (("settling", scenes.c3(args.pour_n), True),
+                               ("bed", scenes.granular_bed(args.pour_n), False)):
+        r = measure_scene(args, lib, sc, "fp32", steps, args.warmup, 0, flush,
+                          settling=settling, profile_steps=5,
+                          traffic_key="c3" if settling else "c3bed")
+        out[name] = {"value": r["value"], "ms_per_step": r["ms_per_step"], "steps": steps,
+                     "n_particles": sc.n, "contact_steps_per_s": r["contact_steps_per_s"],
+                     "window": r["window"], "roofline": r["roofline"]}
+    out["workload"] = (f"{args.pour_n:,} spheres, radii lognormal (median 1 mm, sigma 0.25, "
+                       "clipped to [0.5, 2] mm), 0.4 x 0.4 m floor, FP32 force / FP64 state, "
+                       "dt 2e-7 s; settling: non-overlapping seeded start in 0.4 x 0.4 x 1.2 m "
+                       "(no contacts in the window); bed: the same radii stacked in touching "
+                       "columns (about one Hertz contact per sphere)")
+    return out
+
+
+def served_summary(args, lib) -> dict:
+    """A shortened served stream for the default line: `served_requests`
+    Poisson requests (50/s, 1e3-1e6 spheres log-uniform, mixed bonded /
+    unbonded) with step counts scaled by `served_steps_scale`, against the
+    plain FP64 path scene by scene."""
+    import torch
+    from taichi_dem_julia_port_gb300.serving import (ArenaSizing, Server, poisson_requests,
+                                                     sequential_plain)
+    sc = args.served_steps_scale
+    reqs = poisson_requests(args.served_requests, rate=50.0, seed=5,
+                            smin=max(1, int(1_000 * sc)), smax=max(1, int(50_000 * sc)))
+    sizing = ArenaSizing.from_budget(args.hbm_budget_gb * 1e9)
+    clocks = ClockSampler(torch.cuda.current_device())
+    with Server(sizing, precision="fp32", chunk_steps=200, lib=lib, keep_state=False,
+                policy=args.policy, max_active=args.max_active) as srv:
+        clocks.start()
+        rep = srv.run(reqs, realtime=True)
+        clk = clocks.stop()
+    pct = rep.latency_percentiles()
+    plain = sequential_plain(reqs, lib=lib)
+    return {"metric": "particle-steps/s", "value": rep.throughput,
+            "latency_p50_s": pct.get("p50"), "latency_p99_s": pct.get("p99"),
+            "makespan_s": rep.makespan_s, "requests": len(reqs),
+            "particle_steps": rep.particle_steps, "launches": rep.launches,
+            "policy": args.policy, "max_active": args.max_active,
+            "plain_fp64_scene_by_scene": plain,
+            "speedup_vs_plain": rep.throughput / plain["particle_steps_per_s"],
+            "p99_vs_plain": pct.get("p99", 0.0) / plain["p99_s"] if plain["p99_s"] else None,
+            "clocks": clk,
+            "workload": (f"served: {len(reqs)} Poisson requests (50/s), 1e3-1e6 spheres "
+                         "log-uniform, alternately bonded cubes and unbonded pours, step counts "
+                         f"uniform in [{int(1_000 * sc)}, {int(50_000 * sc)}] (the served "
+                         f"workload's 1,000-50,000 scaled by {sc:g}), FP32 force, "
+                         f"{args.hbm_budget_gb:g} GB HBM budget, continuous batching")}
 
 
 def main() -> None:
@@ -629,6 +880,10 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--advance", type=int, default=None,
+                    help="untimed steps before the warm-up (default: 4,000 for the "
+                         "17,576-sphere cube and 2,000 for the 1,000-sphere cube, so the timed "
+                         "window lies in the fragmentation after the wall impact; 0 for the pour)")
     ap.add_argument("--scenes", type=int, default=256, help="c4: number of scenes")
     ap.add_argument("--requests", type=int, default=12, help="c5: number of requests")
     ap.add_argument("--hbm-budget-gb", type=float, default=160.0, help="c5: arena budget")
@@ -638,6 +893,12 @@ def main() -> None:
                     help="c5 sjf: particles the live scenes may hold before admission waits")
     ap.add_argument("--no-batched", action="store_true",
                     help="default workload: skip the batched summary")
+    ap.add_argument("--no-pour", action="store_true", help="default workload: skip the pour")
+    ap.add_argument("--no-served", action="store_true",
+                    help="default workload: skip the served summary")
+    ap.add_argument("--served-requests", type=int, default=100)
+    ap.add_argument("--served-steps-scale", type=float, default=0.05)
+    ap.add_argument("--pour-steps", type=int, default=50, help="pour summary: timed steps")
     ap.add_argument("--no-tune", action="store_true", help="c4: keep the default launch shape")
     ap.add_argument("--no-plain", action="store_true",
                     help="c4: skip the scene-by-scene plain-path comparison")
@@ -645,13 +906,16 @@ def main() -> None:
     ap.add_argument("--pour-n", type=int, default=2_000_000,
                     help="c3: spheres in the pour (smaller pours for profiling captures)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--e2e-steps", type=int, default=500)
+    ap.add_argument("--e2e-steps", type=int, default=500,
+                    help="least number of end-to-end steps (the window is replayed)")
     ap.add_argument("--profile-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-proxy", action="store_true",
                     help="skip the reference-structured GPU proxy (c1/c2)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.advance is None:
+        args.advance = {"c1": 2000, "c2": 4000}.get(args.workload, 0)
 
     if args.impl == "reference":
         run_reference(args)
@@ -665,7 +929,7 @@ def main() -> None:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    from taichi_dem_julia_port_gb300 import GlobalData, _abi
+    from taichi_dem_julia_port_gb300 import _abi
 
     lib = _abi.load_library()
     _abi.check(lib, lib.dem_set_device(local), "dem_set_device")
@@ -681,132 +945,52 @@ def main() -> None:
         return
     sc, desc = make_scene(args.workload, args.pour_n)
     precision = args.precision or ("fp32" if args.workload == "c3" else "fp64")
-    g = GlobalData(sc.cfg, sc.particles, precision=precision)
-    if sc.bonded:
-        g.initialize()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-
-    def flushed_step() -> float:
-        flush.zero_()
-        torch.cuda.synchronize()
-        return g.simulate_timed(1)
-
-    for _ in range(args.warmup):
-        flushed_step()
-    contacts = []
-    clocks = ClockSampler(local)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    total_ms = 0.0
-    for _ in range(args.steps):
-        total_ms += flushed_step()
-        contacts.append(g.stats()["contacts"])
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    if dist:
-        dist.barrier()
-        total_ms = max_over_ranks(total_ms, dist)
-    g.sync()
-    ms_per_step = total_ms / args.steps
-    value = ws * sc.n * args.steps / (total_ms / 1e3)
-    mean_c = float(np.mean(contacts))
-    stats = g.stats()
-
-    # per-phase device times (eager launches, L2 flushed before each step)
-    phases = []
-    for _ in range(args.profile_steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        phases.append(g.simulate_profiled())
-    ph = {k: float(np.mean([p[k] for p in phases])) for k in phases[0]}
-    st = g.stats()
-    c_now = st["contacts"]
-    n_bond = st["bonded"]
-    force_bytes = n_bond * FORCE_BYTES_BOND + (c_now - n_bond) * FORCE_BYTES_HERTZ
-    alg = {"force": force_bytes,
-           "integrate": sc.n * INTEGRATE_BYTES_WORKLOAD.get(args.workload,
-                                                            INTEGRATE_BYTES_PER_PARTICLE),
-           "contacts": sc.n * DETECT_BYTES_PER_PARTICLE
-           + n_bond * COMPACT_BYTES_BOND + (c_now - n_bond) * COMPACT_BYTES_HERTZ}
-    dom = max(ph, key=ph.get)
-    dom_bytes = alg.get(dom)
-    peaks = load_peaks()
-    roofline = {"bound": "hbm", "kernel": dom, "unit": "GB/s",
-                "peak": peaks["hbm_gbs"], "peak_source": peaks["source"],
-                "traffic": ncu_traffic(args.workload, dom, sc.n), "phase_ms": ph}
-    if dom_bytes is not None:
-        ach = dom_bytes / (ph[dom] * 1e-3) / 1e9
-        roofline.update({"achieved": ach, "frac": ach / peaks["hbm_gbs"],
-                         "algorithmic_bytes": dom_bytes})
-    else:
-        roofline.update({"achieved": None, "frac": None})
-    # the force kernel and the integrator are bound by GB300's FP64 pipe
-    # (2 lanes per SM per cycle) rather than by HBM: their FP64 roofline
-    fr = fp64_roofline(dom, precision, sc.n, n_bond, ph.get(dom),
-                       clk.get("sm_mhz") or peaks.get("sm_max_mhz"), args.workload)
-    if fr:
-        roofline["fp64_pipe"] = fr
-
-    # e2e through the public API with host buffers: page-locked state arrays
-    # bound to the handle (GlobalData.state_buffers), written to the device,
-    # stepped and read back every step
-    buf = g.state_buffers()
-    h2d = sum(a.nbytes for a in buf.arrays.values())
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        buf.step(1)  # upload, step, download (dem_step_exchange)
-    e2e_s = time.perf_counter() - t0
-    buf.close()
-    e2e_s = max_over_ranks(e2e_s, dist)
-    e2e = {"value": ws * sc.n * args.e2e_steps / e2e_s, "unit": "particle-steps/s",
-           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
-           "steps": args.e2e_steps, "ms_per_step": 1e3 * e2e_s / args.e2e_steps}
-    # the host link bounds the exchange: one step plus one copy each way
-    link = host_link(int(h2d))
-    e2e["host_link"] = link
-    e2e["bound_ms_per_step"] = ms_per_step + 1e3 * h2d * (1 / link["h2d_gbs"] +
-                                                          1 / link["d2h_gbs"]) / 1e9
-
+    r = measure_scene(args, lib, sc, precision, args.steps, args.warmup, args.advance, flush,
+                      dist=dist, ws=ws, settling=args.workload == "c3",
+                      e2e_min_steps=args.e2e_steps, profile_steps=args.profile_steps,
+                      traffic_key=args.workload)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(sc, args.cpu_seconds)
+        cpu = cpu_baseline(sc, r["snap"], args.cpu_seconds, r["window"]["start_step"] - 1)
     proxy = None
     if rank == 0 and args.workload in ("c1", "c2") and not args.no_proxy:
-        proxy = run_proxy(args, sc, flush)
-    batched = None
-    if args.workload == "c2" and not args.no_batched:
-        g.close()
-        r = run_batched(args, lib, quick=True)
-        batched = {k: r[k] for k in ("desc", "value", "ms_per_step", "steps", "n_particles",
-                                     "contact_steps_per_s", "plain_fp64_scene_by_scene",
-                                     "speedup_vs_plain", "precision", "tune",
-                                     "fp32_error_vs_fp64")}
-        batched["phase_ms"] = r["roofline"]["phase_ms"]
-        batched["metric"] = "particle-steps/s"
+        proxy = run_proxy(args, sc, flush, args.advance)
+    extra = {}
+    if args.workload == "c2" and rank == 0:
+        if not args.no_batched:
+            b = run_batched(args, lib, quick=True)
+            extra["batched"] = {k: b[k] for k in (
+                "desc", "value", "ms_per_step", "steps", "n_particles", "contact_steps_per_s",
+                "plain_fp64_scene_by_scene", "speedup_vs_plain", "precision", "tune",
+                "fp32_error_vs_fp64")}
+            extra["batched"]["phase_ms"] = b["roofline"]["phase_ms"]
+            extra["batched"]["metric"] = "particle-steps/s"
+        if not args.no_pour:
+            extra["pour"] = pour_summary(args, lib, flush)
+        if not args.no_served:
+            extra["served"] = served_summary(args, lib)
     if rank == 0:
         line = {
-            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+            "metric": "particle-steps/s", "value": r["value"], "unit": "particle-steps/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "f32-force/f64-state",
-            "data": "synthetic (seeded lattice)",
-            "config": {"workload": desc, "n_particles": sc.n, "contacts_mean": mean_c,
-                       "contact_steps_per_s": ws * mean_c * args.steps / (total_ms / 1e3),
-                       "bonds_broken": stats["bonds_broken"], "precision": precision,
+            "data": "synthetic (seeded lattice)" if sc.bonded else "synthetic (seeded pour)",
+            "config": {"workload": desc, "n_particles": sc.n, "precision": precision,
+                       "timed_window": r["window"],
+                       "contacts_mean": r["window"]["contacts_mean"],
+                       "contact_steps_per_s": r["contact_steps_per_s"],
+                       "advance_steps": args.advance,
                        "l2": "flushed between timed steps (256 MiB write)",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single scene"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": KERNELS_PER_STEP * args.steps,
+            "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r.get("e2e"),
+            "clocks": r["clocks"], "gpu_launches": KERNELS_PER_STEP * args.steps,
         }
         if proxy:
             line["reference_gpu_proxy"] = proxy
-        if batched:
-            line["batched"] = batched
+        line.update(extra)
         print(json.dumps(line), flush=True)
-    g.close()
     if dist:
         dist.destroy_process_group()
 

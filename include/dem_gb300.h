@@ -381,6 +381,18 @@ int dem_debug_broadphase(DemHandle* h, int32_t* cell, uint32_t* morton,
                          uint32_t* sorted, int32_t* cp, int64_t cp_cap,
                          int64_t* cp_n);
 
+/* Steps the scene once with the full pair search forced and returns what
+ * the step's own fused enumeration visited: *pairs = the candidate pairs
+ * (i, j > i) taken from the distinct buckets among i's 8 octant buckets,
+ * *checksum = the wrapping 64-bit sum of a mix of each pair, with
+ *   mix(i, j): z = i·2^32 + j; z ^= z >> 33; z *= 0xff51afd7ed558ccd;
+ *              z ^= z >> 33; z *= 0xc4ceb9fe1a85ec53; z ^= z >> 33.
+ * They equal the count and checksum of the distinct pairs of the
+ * reference's cp_list (src/kernels.jl:24-58, dem_debug_broadphase) when the
+ * step visits exactly those pairs.  Single-scene handles only; the step
+ * otherwise runs as dem_step does. */
+int dem_debug_step_enumeration(DemHandle* h, int64_t* pairs, uint64_t* checksum);
+
 /* Bucket sort of the reference broad phase (cell, hashcode, counting sort:
  * src/utils.jl:1-2, src/kernels.jl:7-22) that allocates nothing.  No
  * counterpart in the reference.
@@ -410,6 +422,10 @@ int dem_bucket_sort_noalloc(const double* px, const double* py, const double* pz
 
 /* ---- misc -------------------------------------------------------------- */
 
+/* Text for a status code.  For DEM_ERR_INVALID from dem_create,
+ * dem_arena_add or dem_set_particles it names the offending grain and field
+ * when an input value was the cause (the last such check on the calling
+ * thread); for DEM_ERR_CUDA it is the CUDA runtime's message. */
 const char* dem_strerror(int code);
 
 /* Self-test: compares the library's integer-pipe FP64->FP32 and FP32->FP64
@@ -422,6 +438,18 @@ const char* dem_strerror(int code);
  * reciprocals more than 2 ulp off and the halvings or identities that fail
  * (all 0 when correct).  No counterpart in the reference. */
 int dem_selftest_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
+
+/* Self-test of the device's bounded waits (the failure detection of the
+ * fused pair search): which = 0 runs a grid barrier of two blocks, 1 a scan
+ * look-back over two tiles, each with a wait limit of `spin_limit` polls
+ * (1 .. 2^20).  With `missing` = 1 one party never arrives (its block returns
+ * before the barrier / its tile never publishes), so the wait gives up and
+ * *status receives DEM_ERR_TIMEOUT; with `missing` = 0 everyone arrives and
+ * *status is DEM_OK.  Nothing hangs: every wait of the library is bounded in
+ * the same way (about a second at the default limit) and reports
+ * DEM_ERR_TIMEOUT through the handle's error word.  No counterpart in the
+ * reference (its kernels do not wait on one another). */
+int dem_selftest_wait_timeout(int which, int missing, int64_t spin_limit, int* status);
 
 /* Library version string, e.g. "dem_gb300 0.1.0 sm_103a". */
 const char* dem_version(void);

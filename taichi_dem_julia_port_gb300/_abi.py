@@ -187,6 +187,8 @@ ENTRY_POINTS = {
                                           C.POINTER(C.c_double), C.c_double, C.c_int64,
                                           C.c_void_p, C.c_void_p, C.c_void_p]),
     "dem_selftest_conversions": (C.c_int, [C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
+    "dem_selftest_wait_timeout": (C.c_int, [C.c_int, C.c_int, C.c_int64, C.POINTER(C.c_int)]),
+    "dem_debug_step_enumeration": (C.c_int, [_H, C.POINTER(C.c_int64), C.POINTER(C.c_uint64)]),
     "dem_strerror": (C.c_char_p, [C.c_int]),
     "dem_version": (C.c_char_p, []),
 }

@@ -103,6 +103,9 @@ Hertz hertz_constants(double Ei, double nui, double Ej, double nuj, double e) {
 }
 
 thread_local char g_msg[512];
+// what the last input check that returned DEM_ERR_INVALID on this thread found
+// (cleared by the entry points that check their input)
+thread_local char g_invalid[256];
 
 // First-fit allocator of [start, start + len) ranges inside [0, cap).
 struct FreeList {
@@ -189,6 +192,7 @@ uint32_t pow2_mask(uint32_t H) { return (H & (H - 1)) == 0 ? H - 1 : 0u; }
 // The grain set-up and derived values of `solve` (src/executor.jl:217-315).
 int prepare_scene(const DemConfigC* cfg, const DemParticlesIn* pin, double cell_factor,
                   SceneHost& S, SceneArrays& A) {
+    g_invalid[0] = 0;
     if (!cfg || !pin || pin->n < 0 || pin->n > 0x3fffffff) return DEM_ERR_INVALID;
     if (pin->n > 0 && (!pin->volume || !pin->mass || !pin->pos || !pin->vel)) return DEM_ERR_INVALID;
     if (!(cfg->dt > 0) || cfg->max_coordinate_number <= 0) return DEM_ERR_INVALID;
@@ -204,6 +208,17 @@ int prepare_scene(const DemConfigC* cfg, const DemParticlesIn* pin, double cell_
     double rmax_r = -INFINITY;
     for (int i = 0; i < n; ++i) {
         const double V = pin->volume[i], m = pin->mass[i];
+        // a grain needs a positive finite volume and mass and a finite position
+        // and velocity: anything else would make NaN cells and forces
+        bool ok = V > 0 && m > 0 && std::isfinite(V) && std::isfinite(m);
+        for (int c = 0; c < 3; ++c)
+            ok = ok && std::isfinite(pin->pos[3 * i + c]) && std::isfinite(pin->vel[3 * i + c]);
+        if (!ok) {
+            std::snprintf(g_invalid, sizeof(g_invalid),
+                          "grain %d: volume, mass, position and velocity must be finite "
+                          "(volume and mass > 0)", i);
+            return DEM_ERR_INVALID;
+        }
         A.m[i] = m;
         A.r[i] = std::cbrt(V / (4.0 / 3.0 * kPi));
         A.r0[i] = A.r[i] * cfg->particle_contact_radius_multiplier;
@@ -791,6 +806,16 @@ double* device_view(const void* p) {
     return nullptr;
 }
 
+// Can the host read the buffer (pageable or page-locked host memory)?
+bool host_readable(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return a.type == cudaMemoryTypeUnregistered || a.type == cudaMemoryTypeHost;
+}
+
 // One particle state exchange between caller buffers (`host[f]`, k[f] doubles
 // per particle, nullptr = field not exchanged) and the columns `cols[f]` at
 // slots [p0, p0 + n): one kernel over all fields, which reads or writes
@@ -992,7 +1017,7 @@ const char* dem_version(void) { return "dem_gb300 0.2.0 sm_103a"; }
 const char* dem_strerror(int code) {
     switch (code) {
         case DEM_OK: return "ok";
-        case DEM_ERR_INVALID: return "invalid argument or state";
+        case DEM_ERR_INVALID: return g_invalid[0] ? g_invalid : "invalid argument or state";
         case DEM_ERR_CUDA: return g_msg[0] ? g_msg : "CUDA runtime error";
         case DEM_ERR_CAPACITY:
             return "capacity exceeded (contacts per particle, arena slots, buckets or scenes)";
@@ -1427,6 +1452,19 @@ int set_particles(DemHandle* h, const DemParticleState* in, bool sync) {
     const DemDev& d = h->d;
     const int k[] = {3, 3, 3, 4, 3};
     double* const host[] = {in->pos, in->vel, in->omega, in->quat, in->wall_shear};
+    g_invalid[0] = 0;
+    if (sync) {  // the synchronous upload checks its values (the exchange path does not)
+        for (int f = 0; f < 5; ++f) {
+            if (!host[f] || !host_readable(host[f])) continue;
+            for (int64_t q = 0; q < k[f] * n; ++q)
+                if (!std::isfinite(host[f][q])) {
+                    std::snprintf(g_invalid, sizeof(g_invalid),
+                                  "dem_set_particles: non-finite value in field %d, grain %lld",
+                                  f, (long long)(q / k[f]));
+                    return DEM_ERR_INVALID;
+                }
+        }
+    }
     double* const cols[][4] = {{d.px, d.py, d.pz}, {d.vx, d.vy, d.vz}, {d.wx, d.wy, d.wz},
                                {d.qw, d.qx, d.qy, d.qz}, {d.wsx, d.wsy, d.wsz}};
     // new positions: the exchange kernel refreshes the FP32 positions; the
@@ -1628,6 +1666,62 @@ int dem_debug_broadphase(DemHandle* h, int32_t* cell, uint32_t* morton, uint32_t
             bucket_count[b] = b < ctr.cell_limit ? start[b + 1] - start[b] : 0u;
     int err = device_error(h);
     return err != DEM_OK ? err : rc;
+}
+
+int dem_debug_step_enumeration(DemHandle* h, int64_t* pairs, uint64_t* checksum) {
+    if (!h || !pairs || !checksum || h->multi) return DEM_ERR_INVALID;
+    *pairs = 0;
+    *checksum = 0;
+    if (h->n_cap == 0) return DEM_OK;
+    TRY(ensure_encoding(h));
+    TRY(flag_search(h, 0));
+    CU(cudaMemsetAsync(&h->d.ctr->enum_pairs, 0, 2 * sizeof(unsigned long long), h->stream));
+    DemParams p = h->p;  // the captured graphs keep debug_enum = 0
+    p.debug_enum = 1;
+    const int cur = h->cur;
+    launch_search(h->d, p, cur, false, false, false, h->shape, h->stream);
+    launch_force(h->d, p, cur ^ 1, false, h->shape, h->stream);
+    launch_integrate(h->d, p, cur, false, h->shape, h->stream);
+    CU(cudaGetLastError());
+    h->cur ^= 1;
+    h->steps += 1;
+    DevCounters c;
+    TRY(read_counters(h, &c));
+    *pairs = (int64_t)c.enum_pairs;
+    *checksum = (uint64_t)c.enum_hash;
+    return error_code(c.error);
+}
+
+int dem_selftest_wait_timeout(int which, int missing, int64_t spin_limit, int* status) {
+    if (!status || (which != 0 && which != 1) || spin_limit < 1 || spin_limit > (1 << 20))
+        return DEM_ERR_INVALID;
+    int dev = 0, sms = 0;
+    TRY(check_device(&dev, &sms));
+    DevCounters* c = nullptr;
+    unsigned long long* state = nullptr;
+    uint32_t* io = nullptr;
+    const size_t tile = 8192;  // values per scan tile
+    auto cleanup = [&]() {
+        cudaFree(c);
+        cudaFree(state);
+        cudaFree(io);
+    };
+    cudaError_t e = cudaMalloc(&c, sizeof(DevCounters));
+    if (e == cudaSuccess) e = cudaMalloc(&state, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&io, (4 * tile + 1) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(c, 0, sizeof(DevCounters));
+    if (e == cudaSuccess) e = cudaMemset(state, 0, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(io, 0, (4 * tile + 1) * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = launch_selftest_wait(which, missing ? 1 : 0, (unsigned long long)spin_limit, c, state,
+                                 io, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    DevCounters hc{};
+    if (e == cudaSuccess) e = cudaMemcpy(&hc, c, sizeof(hc), cudaMemcpyDeviceToHost);
+    cleanup();
+    CU(e);
+    *status = error_code(hc.error);
+    return DEM_OK;
 }
 
 }  // extern "C"

@@ -111,6 +111,9 @@ struct DevCounters {
     unsigned long long tickets[2];  // tile tickets of the scan sites (never reset)
     unsigned int bar_count, bar_gen;  // grid barrier of the fused search (arrivals, generation)
     unsigned int hashed[2];           // particles hashed by the step reading buffer cur
+    // inspection of the fused pair search (DemParams::debug_enum): candidate
+    // pairs (i, j > i) it visited and the wrapping sum of enum_mix(i, j)
+    unsigned long long enum_pairs, enum_hash;
 };
 
 // scan sites: each has its own ticket counter and tile-state array
@@ -184,6 +187,7 @@ struct DemParams {
     int sms;        // streaming multiprocessors (grid-stride launch sizes)
     int dep;        // a step's kernels: 0 ordinary launches, 1 programmatic dependent
                     // launches, 2 the same with the successor scheduled early
+    int debug_enum; // 1: the pair search counts its candidate pairs (never in a graph)
     SceneParams s0; // the scene of a single-scene handle
 };
 
@@ -262,6 +266,14 @@ void launch_scan_i32(const int32_t* in, int32_t* out, int64_t n, const DemDev& d
 // bad[1]: widening mismatches against the hardware)
 void launch_selftest_conv(long long n, unsigned long long seed, unsigned long long* bad,
                           cudaStream_t s);
+// self-test of the bounded device waits on the counters `c` (zeroed by the
+// caller): which = 0 a grid barrier of two blocks, 1 a scan look-back over two
+// tiles; `missing` = 1 leaves one party out (its block returns without
+// arriving / its tile never publishes), so the wait must give up after
+// `spin_limit` polls and raise kErrTimeout.
+cudaError_t launch_selftest_wait(int which, int missing, unsigned long long spin_limit,
+                                 DevCounters* c, unsigned long long* state, uint32_t* io,
+                                 cudaStream_t s);
 
 int scan_tiles(int64_t n);
 

@@ -88,7 +88,8 @@ __device__ __forceinline__ unsigned long long scan_word(unsigned long long epoch
 template <typename T, bool LIMITED>
 __global__ void __launch_bounds__(kScanBlock)
     k_scan_excl(const T* __restrict__ in, T* __restrict__ out, long long count, int ntiles,
-                unsigned long long* state, unsigned long long* tickets, DevCounters* ctr) {
+                unsigned long long* state, unsigned long long* tickets, DevCounters* ctr,
+                unsigned long long spin_limit) {
     __shared__ unsigned long long s_ticket;
     __shared__ unsigned long long s_warp[kScanBlock / 32];
     dep_begin();
@@ -152,7 +153,7 @@ __global__ void __launch_bounds__(kScanBlock)
                     st = pr.load(cuda::memory_order_acquire);
                     flag = (unsigned)(st >> 32) & 3u;
                     if ((st >> 34) == epoch && flag) break;
-                    if (it > kSpinLimit) {
+                    if (it > spin_limit) {
                         raise_error(ctr, kErrTimeout);
                         flag = 2u;
                         st = 0;
@@ -468,6 +469,17 @@ __device__ __forceinline__ void emit_rows(const DemDev& d, const DemParams& p, i
     if (len > 0) finish_row<L>(d, p, cur, r, start, lane);
 }
 
+// Checksum term of a candidate pair (i, j) for the inspection of the pair
+// search (a 64-bit finaliser of i·2^32 + j; summed with wrap-around).
+__device__ __forceinline__ unsigned long long enum_mix(int i, int j) {
+    unsigned long long z = ((unsigned long long)(unsigned)i << 32) | (unsigned)j;
+    z ^= z >> 33;
+    z *= 0xff51afd7ed558ccdull;
+    z ^= z >> 33;
+    z *= 0xc4ceb9fe1a85ec53ull;
+    return z ^ (z >> 33);
+}
+
 // Shared memory of one 8-lane group of the pair search (k_search's detect phase).
 struct DetectShared {
     int nnew;
@@ -590,6 +602,7 @@ __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p
     const bool build = !frozen;
     int32_t* vl = d.vl + (size_t)i * p.kvl;
     const float skin = S.f_skin;
+    unsigned long long en = 0, eh = 0;  // inspection: pairs visited, their checksum
     for (int c0 = 0; c0 < total; c0 += kLanes * kBatch) {
         int jj[kBatch], qi[kBatch];
         float4 qq[kBatch];
@@ -616,6 +629,10 @@ __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p
         for (int u = 0; u < kBatch; ++u) {
             const int j = jj[u];
             if (j <= i) continue;
+            if (p.debug_enum) {
+                ++en;
+                eh += enum_mix(i, j);
+            }
             // partners within rᵢ + rⱼ + skin join the neighbour list
             const bool near = maybe_touching32(P32, qq[u], skin);
             if (build && near) {
@@ -640,6 +657,15 @@ __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p
             if (!touching_rn(P.x, P.y, P.z, Q.x, Q.y, Q.z, ri, rj)) continue;
             const int slot = atomicAdd(&sh.nnew, 1);
             if (slot < p.kstash) stash[slot] = j;
+        }
+    }
+    if (p.debug_enum) {
+        en = __reduce_add_sync(gmask, (unsigned)en);
+#pragma unroll
+        for (int o2 = kLanes / 2; o2 > 0; o2 >>= 1) eh += __shfl_xor_sync(gmask, eh, o2, kLanes);
+        if (lane == 0) {
+            atomicAdd(&d.ctr->enum_pairs, en);
+            atomicAdd(&d.ctr->enum_hash, eh);
         }
     }
     __syncwarp(gmask);
@@ -926,7 +952,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_vdetect(DemDev d, DemParams 
 
 // Grid barrier: arrival counter and generation word; a block waits for the
 // generation to move on, with a bounded wait that raises kErrTimeout.
-__device__ __forceinline__ void grid_sync(DevCounters* c) {
+__device__ __forceinline__ void grid_sync(DevCounters* c,
+                                          unsigned long long spin_limit = kSpinLimit) {
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned int* gen = &c->bar_gen;
@@ -938,7 +965,7 @@ __device__ __forceinline__ void grid_sync(DevCounters* c) {
             atomicAdd(&c->bar_gen, 1u);
         } else {
             for (unsigned long long it = 0; *gen == g; ++it) {
-                if (it > kSpinLimit) {
+                if (it > spin_limit) {
                     raise_error(c, kErrTimeout);
                     break;
                 }
@@ -2116,7 +2143,7 @@ void launch_scan_i32(const int32_t* in, int32_t* out, int64_t n, const DemDev& d
         return;
     }
     k_scan_excl<int32_t, false><<<nt, kScanBlock, 0, s>>>(in, out, n, nt, d.scan_state[site],
-                                                          &d.ctr->tickets[site], d.ctr);
+                                                          &d.ctr->tickets[site], d.ctr, kSpinLimit);
 }
 
 void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi, bool all,
@@ -2127,7 +2154,7 @@ void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi,
     launch(dep, multi ? k_hash<true> : k_hash<false>, nb, kThreads, s, d, p, cur, all ? 1 : 0);
     launch(dep, k_scan_excl<uint32_t, true>, ntiles_cells, kScanBlock, s,
            (const uint32_t*)d.cell_count, d.cell_start, (long long)p.T, ntiles_cells,
-           d.scan_state[kScanCells], &d.ctr->tickets[kScanCells], d.ctr);
+           d.scan_state[kScanCells], &d.ctr->tickets[kScanCells], d.ctr, kSpinLimit);
     launch(dep, k_scatter, nb, kThreads, s, d, p);
     launch(dep, multi ? k_canon<true> : k_canon<false>, nb, kThreads, s, d, p, cur);
 }
@@ -2314,6 +2341,43 @@ void launch_selftest_conv(long long n, unsigned long long seed, unsigned long lo
                           cudaStream_t s) {
     if (n <= 0) return;
     k_selftest_conv<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, seed, bad);
+}
+
+// Bounded-wait self-test: two blocks meet at the grid barrier that the fused
+// pair search uses; with `missing`, block 1 returns before it arrives, so
+// block 0's wait must give up after `spin_limit` polls (kErrTimeout) and
+// return.  Launched cooperatively, so both blocks are resident.
+__global__ void k_selftest_barrier(DevCounters* c, int missing, unsigned long long spin_limit) {
+    if (missing && blockIdx.x == 1) return;
+    grid_sync(c, spin_limit);
+}
+
+cudaError_t launch_selftest_wait(int which, int missing, unsigned long long spin_limit,
+                                 DevCounters* c, unsigned long long* state, uint32_t* io,
+                                 cudaStream_t s) {
+    if (which == 0) {
+        void* args[] = {&c, &missing, &spin_limit};
+        return cudaLaunchCooperativeKernel((const void*)k_selftest_barrier, dim3(2), dim3(32),
+                                           args, 0, s);
+    }
+    // The scan of 2·kScanTile values in two tiles: every block draws a ticket
+    // (tile = ticket mod 2).  With `missing`, one block runs: it draws ticket
+    // 1 (the counter starts at 1), i.e. tile 1, whose look-back waits for
+    // tile 0, which never publishes.  io holds 2·kScanTile inputs followed by
+    // 2·kScanTile + 1 outputs.
+    const long long count = 2LL * kScanTile;
+    if (missing) {
+        cudaError_t e = cudaMemsetAsync(&c->tickets[0], 0, sizeof(unsigned long long), s);
+        if (e != cudaSuccess) return e;
+        const unsigned long long one = 1ull;
+        e = cudaMemcpyAsync(&c->tickets[0], &one, sizeof(one), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return e;
+        e = cudaStreamSynchronize(s);  // `one` lives on this stack frame
+        if (e != cudaSuccess) return e;
+    }
+    k_scan_excl<uint32_t, false><<<missing ? 1 : 2, kScanBlock, 0, s>>>(
+        io, io + count, count, 2, state, &c->tickets[0], c, spin_limit);
+    return cudaGetLastError();
 }
 
 

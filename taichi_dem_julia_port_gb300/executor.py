@@ -331,6 +331,29 @@ class GlobalData:
         out["cp_count"] = cnt.value
         return out
 
+    def debug_step_enumeration(self) -> tuple[int, int]:
+        """One step with the full pair search forced; returns the candidate
+        pairs its fused enumeration visited and their 64-bit checksum
+        (`dem_debug_step_enumeration`)."""
+        pairs, chk = C.c_int64(), C.c_uint64()
+        check(self.lib, self.lib.dem_debug_step_enumeration(self.h, C.byref(pairs), C.byref(chk)),
+              "dem_debug_step_enumeration")
+        return int(pairs.value), int(chk.value)
+
+
+def enumeration_checksum(pairs: np.ndarray) -> int:
+    """Wrapping 64-bit sum of the pair mix that dem_debug_step_enumeration
+    uses, over an (m, 2) array of pairs (i, j)."""
+    p = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+    z = (p[:, 0].astype(np.uint64) << np.uint64(32)) | p[:, 1].astype(np.uint64)
+    with np.errstate(over="ignore"):
+        z ^= z >> np.uint64(33)
+        z *= np.uint64(0xff51afd7ed558ccd)
+        z ^= z >> np.uint64(33)
+        z *= np.uint64(0xc4ceb9fe1a85ec53)
+        z ^= z >> np.uint64(33)
+        return int(np.sum(z, dtype=np.uint64))
+
 
 def initialize(g: GlobalData) -> None:
     """`initialize!(global_data, ...)` (src/executor.jl:155-160)."""
@@ -344,11 +367,40 @@ def simulate(g: GlobalData, nsteps: int = 1) -> None:
 
 def load_particles(p4p_path: str | Path) -> ParticleInput:
     """The grains of the first record of a p4p file, in file order
-    (src/executor.jl:217-243)."""
-    lines = Path(p4p_path).read_text().split("\n")
-    n = int(lines[1].split()[1])
-    rows = np.array([[float(x) for x in lines[3 + k].split()[:10]] for k in range(n)],
-                    dtype=np.float64).reshape(n, 10)
+    (src/executor.jl:217-243).
+
+    A malformed file raises ValueError naming the file and line: a first line
+    that is not the TIMESTEP header, a second line without an integer
+    particle count, fewer particle rows than that count, or a row with fewer
+    than ten numbers (ID GROUP VOLUME MASS PX PY PZ VX VY VZ) or a value that
+    does not parse."""
+    path = Path(p4p_path)
+    lines = path.read_text().split("\n")
+
+    def bad(line_no: int, what: str) -> ValueError:
+        return ValueError(f"{path}:{line_no}: {what}")
+
+    if not lines or not lines[0].startswith("TIMESTEP"):
+        raise bad(1, "expected the 'TIMESTEP PARTICLES' header")
+    head = lines[1].split() if len(lines) > 1 else []
+    try:
+        n = int(head[1])
+    except (IndexError, ValueError):
+        raise bad(2, "expected '<timestep> <particle count>'") from None
+    if n < 0:
+        raise bad(2, f"negative particle count {n}")
+    if len(lines) < 3 + n or any(not lines[3 + k].strip() for k in range(n)):
+        have = sum(1 for ln in lines[3:3 + n] if ln.strip())
+        raise bad(3 + have + 1, f"the header announces {n} particles, the file has {have} rows")
+    rows = np.empty((n, 10), dtype=np.float64)
+    for k in range(n):
+        f = lines[3 + k].split()
+        if len(f) < 10:
+            raise bad(4 + k, f"expected 10 columns, found {len(f)}")
+        try:
+            rows[k] = [float(x) for x in f[:10]]
+        except ValueError as e:
+            raise bad(4 + k, str(e)) from None
     return ParticleInput(id=rows[:, 0].astype(np.int32), gid=rows[:, 1].astype(np.int32),
                          volume=rows[:, 2].copy(), mass=rows[:, 3].copy(),
                          pos=rows[:, 4:7].copy(), vel=rows[:, 7:10].copy())

@@ -8,6 +8,7 @@ definitions:
   bonded_cube(10, ...)  1,000-sphere bonded cube impact (10x10x10 lattice)
   bonded_cube(26, ...)  17,576-sphere bonded cube impact (26x26x26 lattice)
   granular_pour(n)      unbonded polydisperse pour, lognormal radii
+  granular_bed(n)       the pour's spheres pre-compacted into touching columns
   mixed_batch(256)      256 independent scenes of 500-20,000 spheres, half
                         cubes and half pours, per-scene materials
 """
@@ -139,6 +140,62 @@ def granular_pour(n: int = 2_000_000, box=(0.4, 0.4, 1.2), seed: int = 3, median
         saving_interval_time=1000 * dt, gravity=[0.0, 0.0, -9.81],
     )
     return Scene(f"granular_pour_{n}", cfg, p, steps, False)
+
+
+def granular_bed(n: int = 2_000_000, box=(0.4, 0.4, 1.2), seed: int = 3, median: float = 1e-3,
+                 sigma: float = 0.25, rmin: float = 0.5e-3, rmax: float = 2e-3,
+                 overlap: float = 1e-3, density: float = 2500.0, E: float = 1e8,
+                 friction: float = 0.4, dt: float = 2e-7, steps: int = 5_000) -> Scene:
+    """The pour's spheres (lognormal radii, median 1 mm, σ 0.25, clipped to
+    [0.5, 2] mm) pre-compacted into a bed with contacts from the first step.
+
+    Columns on a square grid of pitch 2·rmax·1.001 over the box's floor; each
+    column is a stack in which every sphere rests on the one below with an
+    overlap of `overlap`·(rᵢ + rⱼ), its centre displaced sideways at random
+    within the column (so no sphere reaches a neighbouring column), and the
+    lowest sphere overlaps the floor plane by the same fraction of its radius.
+    Every sphere therefore starts with one or two contacts; gravity and the
+    sideways offsets then let the columns lean, creating and ending contacts.
+    The box's floor must hold enough columns for the stacks to stay below its
+    height."""
+    rng = np.random.default_rng(seed)
+    r = np.clip(median * np.exp(sigma * rng.standard_normal(n)), rmin, rmax)
+    h = 2.0 * rmax * 1.001
+    nx, ny = max(int(box[0] / h), 1), max(int(box[1] / h), 1)
+    ncol = nx * ny
+    col = np.arange(n) % ncol                     # round-robin: columns of equal count
+    lvl = np.arange(n) // ncol
+    off = rng.uniform(-1.0, 1.0, size=(n, 2)) * (rmax - r)[:, None] * 0.999
+    cx = (col % nx + 0.5) * h
+    cy = (col // nx + 0.5) * h
+    pos = np.empty((n, 3))
+    pos[:, 0] = cx + off[:, 0]
+    pos[:, 1] = cy + off[:, 1]
+    z = np.empty(n)
+    first = lvl == 0
+    z[first] = r[first] * (1.0 - overlap)
+    for k in range(1, int(lvl.max()) + 1 if n else 0):
+        cur = np.nonzero(lvl == k)[0]
+        below = cur - ncol
+        dxy2 = np.sum((pos[cur, :2] - pos[below, :2]) ** 2, axis=1)
+        d = (r[cur] + r[below]) * (1.0 - overlap)
+        z[cur] = z[below] + np.sqrt(np.maximum(d * d - dxy2, 0.0))
+    pos[:, 2] = z
+    if n and z.max() + rmax > box[2]:
+        raise ValueError(f"bed of {n} spheres is {z.max():.3f} m high, box {box[2]} m")
+    p = ParticleInput.from_arrays(r, pos, np.zeros((n, 3)), density)
+    lo = np.array([-0.05, -0.05, -0.05])
+    hi = np.asarray(box, dtype=np.float64) + 0.05
+    cfg = DEMConfig(
+        domain_min=lo.tolist(), domain_max=hi.tolist(), init_particles="<synthetic>",
+        particle_elastic_modulus=E, particle_poisson_ratio=0.3,
+        wall_normal=[0.0, 0.0, -1.0], wall_distance=0.0,
+        bond_elastic_modulus=1e8, bond_tensile_strength=1e6, bond_shear_strength=1e6,
+        pp_coefficient_friction=friction, pp_coefficient_restitution=0.9,
+        max_coordinate_number=16, dt=dt, target_time=steps * dt,
+        saving_interval_time=1000 * dt, gravity=[0.0, 0.0, -9.81],
+    )
+    return Scene(f"granular_bed_{n}", cfg, p, steps, False)
 
 
 def mixed_batch(count: int = 256, seed: int = 4, nmin: int = 500, nmax: int = 20_000,

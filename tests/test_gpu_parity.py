@@ -7,8 +7,9 @@ state, 1e-5 over a short horizon; FP32 force mode: 1e-3)."""
 import numpy as np
 import pytest
 
-from oracle.oracle import OracleScene
+from oracle.oracle import OracleScene, host_threads
 from taichi_dem_julia_port_gb300 import GlobalData, scenes
+from taichi_dem_julia_port_gb300.executor import enumeration_checksum
 from taichi_dem_julia_port_gb300._abi import DEM_ERR_CAPACITY, DemError
 from taichi_dem_julia_port_gb300.config import DEMConfig
 from taichi_dem_julia_port_gb300.scenes import ParticleInput
@@ -43,8 +44,16 @@ def random_cloud(n, box, rmin, rmax, seed, v=0.0, cfg_kw=None):
     return DEMConfig(**kw), ParticleInput.from_arrays(r, pos, vel, 2500.0)
 
 
-def both(cfg, p, precision="fp64"):
-    return GlobalData(cfg, p, precision=precision), OracleScene(cfg, p)
+def both(cfg, p, precision="fp64", threads=1):
+    return GlobalData(cfg, p, precision=precision), OracleScene(cfg, p, threads=threads)
+
+
+def copy_state(o, g):
+    """The oracle's particle and contact state onto the GPU handle."""
+    p, c = o.particles(), o.contacts()
+    g.set_particles(pos=p["pos"], vel=p["vel"], omega=p["omega"], quat=p["quat"],
+                    wall_shear=p["wall_shear"])
+    g.set_contacts(c)
 
 
 def compare_broadphase(g, o):
@@ -67,6 +76,8 @@ def compare_state(g, o, rtol, what=""):
     assert_rows_close(pg["vel"], po["vel"], rtol, f"{what} vel")
     assert_rows_close(pg["force"], po["force"], rtol, f"{what} force", atol_frac=rtol)
     assert_rows_close(pg["moment"], po["moment"], rtol, f"{what} moment", atol_frac=rtol)
+    assert_rows_close(pg["omega"], po["omega"], rtol, f"{what} omega", atol_frac=rtol)
+    assert_rows_close(pg["quat"], po["quat"], rtol, f"{what} quat")
     assert_rows_close(cg["force"], co["force"], rtol, f"{what} contact force", atol_frac=rtol)
     assert_rows_close(cg["shear"], co["shear"], rtol, f"{what} shear", atol_frac=rtol)
     assert_rows_close(cg["point"], co["point"], rtol, f"{what} point")
@@ -158,6 +169,117 @@ def test_one_step_from_identical_state_granular(gpu):
         o.simulate(10)
     s = o.stats()
     assert s["contacts_created"] > 0 and s["contacts_ended"] > 0
+
+
+def test_step_enumeration_visits_cp_list(gpu):
+    """The step's own fused pair enumeration (8 lanes per particle over its
+    octant buckets, repeated buckets skipped, entries above i by binary
+    search) visits exactly the distinct pairs of the reference's cp_list, on
+    a lattice, on a random cloud, and with colliding hash buckets."""
+    sc = scenes.bonded_cube(10, steps=0)
+    cloud = random_cloud(3000, (0.05, 0.05, 0.05), 0.0008, 0.0015, seed=5, v=0.5)
+    wide = random_cloud(4000, (3.9, 3.9, 3.9), 0.004, 0.006, seed=3,
+                        cfg_kw=dict(domain_max=[4.0, 4.0, 4.0]))
+    for cfg, p in ((sc.cfg, sc.particles), cloud, wide):
+        g = GlobalData(cfg, p)
+        g.simulate(3)
+        bp = g.debug_broadphase()
+        distinct = np.unique(bp["cp"], axis=0)
+        pairs, chk = g.debug_step_enumeration()
+        assert pairs == len(distinct), (pairs, len(distinct), bp["cp_count"])
+        assert chk == enumeration_checksum(distinct)
+        assert g.stats()["error"] == 0
+        g.close()
+
+
+def test_global_damping_one_step_and_horizon(gpu):
+    """apply_body_force!'s damping term -d·|F|·sign(v) (src/kernels.jl:436-441)
+    with a nonzero coefficient: one step from an identical state of a granular
+    cloud whose grains have velocity or spin components that are exactly zero
+    (sign(0) = 0) as well as moving and spinning ones; then a bonded cube's
+    impact with damping over a 200-step horizon.  (A horizon on the granular
+    cloud is not a parity test: sign(v) of a velocity component passing
+    through zero turns rounding differences into O(1) force differences, and
+    the dense cloud's collisions amplify them.)"""
+    cfg, p = random_cloud(3000, (0.05, 0.05, 0.05), 0.0008, 0.0015, seed=15, v=0.5,
+                          cfg_kw=dict(global_damping=0.3, pp_coefficient_friction=0.3))
+    rng = np.random.default_rng(15)
+    g, o = both(cfg, p)
+    o.simulate(5)
+    pp = o.particles()
+    vel, omega = pp["vel"].copy(), rng.normal(0, 50.0, (p.n, 3))
+    for k in range(0, p.n, 7):
+        vel[k, k % 3] = 0.0
+        omega[k, (k + 1) % 3] = 0.0
+    vel[::11] = 0.0
+    omega[::13] = 0.0
+    o.set_particles(vel=vel, omega=omega)
+    copy_state(o, g)
+    g.simulate(1)
+    o.simulate(1)
+    compare_state(g, o, RTOL_STEP, "damping one step")
+    g.close()
+    sc = scenes.bonded_cube(8, speed=10.0, steps=0, seed=4)
+    cfg = sc.cfg.replace(global_damping=0.2)
+    g, o = both(cfg, sc.particles)
+    g.initialize()
+    o.initialize()
+    for _ in range(4):
+        g.simulate(50)
+        o.simulate(50)
+        compare_state(g, o, RTOL_HORIZON, "damped cube horizon")
+    assert np.count_nonzero(np.any(o.particles()["wall_shear"] != 0, axis=1)) > 0
+
+
+def test_full_size_cube_mid_impact(gpu):
+    """The 17,576-sphere bonded cube at 20 m/s in its fragmentation (the GPU
+    runs the first 3,800 steps; the oracle joins from the GPU's state): one
+    step from that identical state — wall contacts, Hertz contacts between
+    fragments and bonds breaking — then a 200-step horizon."""
+    sc = scenes.c2()
+    g, o = both(sc.cfg, sc.particles, threads=host_threads())
+    g.initialize()
+    g.simulate(3800)
+    copy_state(g, o)
+    g.simulate(1)
+    o.simulate(1)
+    cg = compare_state(g, o, RTOL_STEP, "c2 one step")
+    pg = g.particles()
+    assert np.count_nonzero(np.any(pg["wall_shear"] != 0, axis=1)) > 100
+    assert np.count_nonzero(cg["bonded"] == 0) > 1000  # Hertz contacts between fragments
+    b0 = o.stats()["bonds_broken"]
+    for _ in range(4):
+        g.simulate(50)
+        o.simulate(50)
+        compare_state(g, o, RTOL_HORIZON, "c2 horizon")
+    assert o.stats()["bonds_broken"] > b0  # bonds broke inside the compared horizon
+    assert g.stats()["error"] == 0
+
+
+@pytest.mark.parametrize("precision,rtol", [("fp64", RTOL_STEP), ("fp32", RTOL_FP32)])
+def test_polydisperse_bed_one_step(gpu, precision, rtol):
+    """100,000 spheres with the 2,000,000-sphere pour's radii (lognormal,
+    median 1 mm, σ 0.25, clipped to [0.5, 2] mm) pre-compacted into touching
+    columns on the floor: one step from an identical state with about one
+    Hertz contact per sphere, FP64 (rtol 1e-9) and the FP32 force mode
+    (1e-3 against the FP64 oracle)."""
+    f = 2.0 * (100_000 / 2_000_000) ** (1.0 / 3.0)
+    sc = scenes.granular_bed(100_000, box=(0.4 * f, 0.4 * f, 1.2), seed=21)
+    g, o = both(sc.cfg, sc.particles, precision=precision, threads=host_threads())
+    o.simulate(20)
+    copy_state(o, g)
+    g.simulate(1)
+    o.simulate(1)
+    cg, co = g.contacts(), o.contacts()
+    assert len(co["i"]) > 80_000
+    if precision == "fp64":
+        compare_state(g, o, rtol, "bed one step")
+    else:
+        assert pair_set(cg) == pair_set(co)
+        assert_rows_close(cg["force"], co["force"], rtol, "bed fp32 contact force", atol_frac=rtol)
+        pg, po = g.particles(), o.particles()
+        assert_rows_close(pg["force"], po["force"], rtol, "bed fp32 force", atol_frac=rtol)
+        assert_rows_close(pg["pos"], po["pos"], 1e-9, "bed fp32 pos")
 
 
 def test_short_horizon_cube(gpu):

@@ -196,3 +196,30 @@ def test_autotune_confirms_its_choice():
     assert h.shape == h.default
     chosen = [c for c, _ in r.trials if not c.get("baseline") and not c.get("confirm")]
     assert chosen, "the descent timed candidates"
+
+
+def test_corrupt_p4p_is_rejected_with_its_line(tmp_path):
+    """Malformed p4p input raises ValueError naming the file and line, before
+    anything reaches the library."""
+    from taichi_dem_julia_port_gb300.executor import load_particles
+    good = ("TIMESTEP PARTICLES\n0.0 2\nID  GROUP  VOLUME  MASS  PX  PY  PZ  VX  VY  VZ\n"
+            "1 0 4.1e-6 0.01 0.0 0.0 0.0 0.0 0.0 0.0\n"
+            "2 0 4.1e-6 0.01 0.02 0.0 0.0 0.0 0.0 0.0\n")
+    f = tmp_path / "good.p4p"
+    f.write_text(good)
+    assert load_particles(f).n == 2
+    cases = {
+        "header": ("PARTICLES\n" + good.split("\n", 1)[1], ":1:"),
+        "count": (good.replace("0.0 2\n", "0.0 two\n"), ":2:"),
+        "truncated": ("".join(good.splitlines(True)[:4]),
+                      "announces 2 particles, the file has 1"),
+        "columns": (good.replace("2 0 4.1e-6 0.01 0.02 0.0 0.0 0.0 0.0 0.0",
+                                 "2 0 4.1e-6 0.01 0.02"), ":5: expected 10 columns"),
+        "value": (good.replace("0.02 0.0 0.0", "0.02 x 0.0"), ":5:"),
+    }
+    for name, (text, msg) in cases.items():
+        f = tmp_path / f"{name}.p4p"
+        f.write_text(text)
+        with pytest.raises(ValueError) as e:
+            load_particles(f)
+        assert msg in str(e.value), (name, str(e.value))
