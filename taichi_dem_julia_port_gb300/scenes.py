@@ -144,33 +144,36 @@ def granular_pour(n: int = 2_000_000, box=(0.4, 0.4, 1.2), seed: int = 3, median
 
 def granular_bed(n: int = 2_000_000, box=(0.4, 0.4, 1.2), seed: int = 3, median: float = 1e-3,
                  sigma: float = 0.25, rmin: float = 0.5e-3, rmax: float = 2e-3,
-                 overlap: float = 1e-3, density: float = 2500.0, E: float = 1e8,
-                 friction: float = 0.4, dt: float = 2e-7, steps: int = 5_000) -> Scene:
+                 overlap: float = 1e-3, tilt: float = 0.25, density: float = 2500.0,
+                 E: float = 1e8, friction: float = 0.4, dt: float = 2e-7,
+                 steps: int = 5_000) -> Scene:
     """The pour's spheres (lognormal radii, median 1 mm, σ 0.25, clipped to
     [0.5, 2] mm) pre-compacted into a bed with contacts from the first step.
 
-    Columns on a square grid of pitch 2·rmax·1.001 over the box's floor; each
-    column is a stack in which every sphere rests on the one below with an
-    overlap of `overlap`·(rᵢ + rⱼ), its centre displaced sideways at random
-    within the column (so no sphere reaches a neighbouring column), and the
-    lowest sphere overlaps the floor plane by the same fraction of its radius.
-    Every sphere therefore starts with one or two contacts; gravity and the
-    sideways offsets then let the columns lean, creating and ending contacts.
-    The box's floor must hold enough columns for the stacks to stay below its
-    height."""
+    Columns on a square grid over the box's floor; each column is a stack in
+    which every sphere rests on the one below with an overlap of
+    `overlap`·(rᵢ + rⱼ) and the lowest sphere overlaps the floor plane by the
+    same fraction of its radius.  Each sphere's centre is displaced sideways
+    by at most `tilt`·rmin from its column's axis, so consecutive spheres
+    meet nearly head-on (a sphere is higher than the one below by at least
+    0.94 of their radii's sum, so it touches no other sphere of its column),
+    and the grid pitch 2·rmax·1.001 + 2·tilt·rmin keeps neighbouring columns
+    apart.  Every sphere therefore starts with one or two contacts; gravity
+    and the sideways offsets then let the columns lean, creating and ending
+    contacts.  The box's floor must hold enough columns for the stacks to
+    stay below its height."""
     rng = np.random.default_rng(seed)
     r = np.clip(median * np.exp(sigma * rng.standard_normal(n)), rmin, rmax)
-    h = 2.0 * rmax * 1.001
+    off_max = tilt * rmin
+    h = 2.0 * rmax * 1.001 + 2.0 * off_max
     nx, ny = max(int(box[0] / h), 1), max(int(box[1] / h), 1)
     ncol = nx * ny
     col = np.arange(n) % ncol                     # round-robin: columns of equal count
     lvl = np.arange(n) // ncol
-    off = rng.uniform(-1.0, 1.0, size=(n, 2)) * (rmax - r)[:, None] * 0.999
-    cx = (col % nx + 0.5) * h
-    cy = (col // nx + 0.5) * h
+    off = rng.uniform(-1.0, 1.0, size=(n, 2)) * off_max
     pos = np.empty((n, 3))
-    pos[:, 0] = cx + off[:, 0]
-    pos[:, 1] = cy + off[:, 1]
+    pos[:, 0] = (col % nx + 0.5) * h + off[:, 0]
+    pos[:, 1] = (col // nx + 0.5) * h + off[:, 1]
     z = np.empty(n)
     first = lvl == 0
     z[first] = r[first] * (1.0 - overlap)
@@ -179,7 +182,7 @@ def granular_bed(n: int = 2_000_000, box=(0.4, 0.4, 1.2), seed: int = 3, median:
         below = cur - ncol
         dxy2 = np.sum((pos[cur, :2] - pos[below, :2]) ** 2, axis=1)
         d = (r[cur] + r[below]) * (1.0 - overlap)
-        z[cur] = z[below] + np.sqrt(np.maximum(d * d - dxy2, 0.0))
+        z[cur] = z[below] + np.sqrt(d * d - dxy2)
     pos[:, 2] = z
     if n and z.max() + rmax > box[2]:
         raise ValueError(f"bed of {n} spheres is {z.max():.3f} m high, box {box[2]} m")
