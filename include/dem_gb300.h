@@ -403,9 +403,14 @@ int dem_debug_step_enumeration(DemHandle* h, int64_t* pairs, uint64_t* checksum)
  * allocation is blocked.  The caller passes device pointers: positions
  * px/py/pz (n each), and the outputs bucket[n] (the reference's 1-based
  * hashcode) and sorted[n] (particle indices grouped by bucket, ascending
- * inside a bucket; the same as dem_debug_broadphase's `sorted`).  Work is
+ * inside a bucket; the same as dem_debug_broadphase's `sorted`).
+ * domain_min is a HOST pointer to 3 doubles (read during the call).  Work is
  * queued on `stream` (a cudaStream_t, NULL for the default stream); results
  * are ready when that stream is synchronised.
+ *
+ * The sort is a stable radix sort of the indices by bucket (one pass for
+ * hash_table_size <= 1,024, two above): its work is O(n + H) whatever the
+ * number of particles per bucket.
  *
  * The temporary memory is one 12.6 MB array inside the library, reserved on
  * every GPU that loads it until the process exits, so n and hash_table_size
@@ -414,7 +419,10 @@ int dem_debug_step_enumeration(DemHandle* h, int64_t* pairs, uint64_t* checksum)
  * array's device address; make that first call before any stream capture on
  * the device.  Every call reuses the same array: calls whose work overlaps on
  * the GPU (different streams or threads) race and must be serialised by the
- * caller. */
+ * caller.  DEM_ERR_CUDA is returned, with nothing queued, when a CUDA error
+ * is already pending on the calling thread (it is left in place for its
+ * owner), and when one of this call's launches fails (the call stops at the
+ * first failure). */
 int dem_bucket_sort_noalloc(const double* px, const double* py, const double* pz,
                             int64_t n, const double* domain_min, double cell_size,
                             int64_t hash_table_size, uint32_t* bucket,

@@ -9,8 +9,18 @@
 // in one file-scope device array below, reserved on every GPU that loads this
 // library until the process exits.
 //
+// The sort: cell + hashcode per particle (src/utils.jl:1-2), then a stable
+// least-significant-digit radix sort of the particle indices by bucket, 10
+// bits per pass (one pass for tables of up to 1,024 buckets, two above).
+// Stability keeps ascending index inside each bucket, which is the order the
+// library's regular broad phase gives (the reference leaves it free,
+// src/kernels.jl:15-22).  The work is O(n + H) whatever the bucket
+// occupancy: one bucket holding every particle costs the same as many small
+// ones.
+//
 // Limits: n <= 1,048,576 particles and hash_table_size <= 1,048,576 buckets;
-// the array is 12.6 MB (counts, starts, tile sums, unsorted order).
+// the array is 12.6 MB (the first pass's keys and indices, the per-block
+// digit counts, and the tile sums of their scan).
 #include <mutex>
 
 #include "dem_device.cuh"
@@ -20,20 +30,29 @@ namespace {
 
 constexpr long long kMaxN = 1 << 20;
 constexpr long long kMaxH = 1 << 20;
-constexpr int kTile = 2048;
 constexpr int kBlock = 256;
-constexpr int kMaxTiles = (int)((kMaxH + kTile - 1) / kTile);
-constexpr size_t kCountsOff = 0;
-constexpr size_t kStartsOff = kCountsOff + kMaxH;
-constexpr size_t kTilesOff = kStartsOff + kMaxH + 64;
-constexpr size_t kUnsortedOff = kTilesOff + kMaxTiles;
-constexpr size_t kWords = kUnsortedOff + kMaxN;
+constexpr int kItems = 4;
+constexpr int kChunk = kBlock * kItems;  // particles per block of a radix pass
+constexpr int kDigitBits = 10;
+constexpr int kBins = 1 << kDigitBits;
+constexpr long long kMaxBlocks = kMaxN / kChunk;
+constexpr long long kHistWords = kBins * kMaxBlocks;
+constexpr int kTile = 2048;  // counts per tile of the digit-count scan
+constexpr int kMaxTiles = (int)((kHistWords + kTile - 1) / kTile);
+constexpr size_t kKeysOff = 0;
+constexpr size_t kValsOff = kKeysOff + kMaxN;
+constexpr size_t kHistOff = kValsOff + kMaxN;
+constexpr size_t kTilesOff = kHistOff + kHistWords;
+constexpr size_t kWords = kTilesOff + kMaxTiles;
 constexpr int kMaxDevices = 64;
 
-// The scratch: bucket counts (zero at the start of every call), bucket starts,
-// per-tile sums of the counts, and the bucket-grouped order before the
-// within-bucket ordering.  Host code must not take this name as a device
-// address; it uses the address from cudaGetSymbolAddress (see scratch_on()).
+// The scratch: the first pass's output keys (0-based buckets) and particle
+// indices, the digit counts of every block (digit-major, scanned in place
+// into each block's first slot per digit) and the per-tile sums of that scan.
+// Every word a call reads is written earlier in the same call, so nothing
+// needs clearing between calls.  Host code must not take this name as a
+// device address; it uses the address from cudaGetSymbolAddress (see
+// scratch_on()).
 static __device__ __align__(256) uint32_t g_scratch[kWords];
 
 struct Geometry {
@@ -48,10 +67,9 @@ __device__ __forceinline__ uint32_t na_bucket(int x, int y, int z, const Geometr
     return g.mask ? (m & g.mask) : (m % g.H);
 }
 
-// cell + hashcode (src/utils.jl:1-2) and count_particles! (src/kernels.jl:7-13)
+// cell + hashcode (src/utils.jl:1-2): the reference's 1-based bucket
 __global__ void k_na_hash(const double* __restrict__ px, const double* __restrict__ py,
-                          const double* __restrict__ pz, int n, Geometry g, uint32_t* bucket_out,
-                          uint32_t* counts) {
+                          const double* __restrict__ pz, int n, Geometry g, uint32_t* bucket_out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double pos[3] = {px[i], py[i], pz[i]};
@@ -59,9 +77,24 @@ __global__ void k_na_hash(const double* __restrict__ px, const double* __restric
 #pragma unroll
     for (int c = 0; c < 3; ++c)
         ijk[c] = dem::ceil_i32(__ddiv_rn(__dsub_rn(pos[c], g.dmin[c]), g.cell));
-    const uint32_t b = na_bucket(ijk[0], ijk[1], ijk[2], g);
-    bucket_out[i] = b + 1u;  // the reference's 1-based hashcode
-    atomicAdd(&counts[b], 1u);
+    bucket_out[i] = na_bucket(ijk[0], ijk[1], ijk[2], g) + 1u;
+}
+
+// Digit counts of one block's kChunk keys (key = in[k] - bias), written
+// digit-major: hist[digit * nblk + block].
+__global__ void k_na_digit_count(const uint32_t* __restrict__ keys, uint32_t bias, int n,
+                                 int shift, int nblk, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[kBins];
+    for (int b = threadIdx.x; b < kBins; b += kBlock) h[b] = 0u;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * kChunk;
+#pragma unroll
+    for (int q = 0; q < kItems; ++q) {
+        const long long k = base + q * kBlock + threadIdx.x;
+        if (k < n) atomicAdd(&h[((keys[k] - bias) >> shift) & (kBins - 1)], 1u);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < kBins; b += kBlock) hist[(size_t)b * nblk + blockIdx.x] = h[b];
 }
 
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
@@ -91,13 +124,13 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total)
     return r;
 }
 
-// accumulate! of the counts (src/executor.jl:50) in three passes without
-// any inter-block waiting: tile sums, one-block scan of the sums, apply.
-__global__ void k_na_tile_sums(const uint32_t* counts, long long H, uint32_t* tiles) {
+// Exclusive scan of the digit counts, in place, in three passes without any
+// inter-block waiting: tile sums, one-block scan of the sums, apply.
+__global__ void k_na_tile_sums(const uint32_t* v, long long m, uint32_t* tiles) {
     const long long base = (long long)blockIdx.x * kTile + threadIdx.x * (kTile / kBlock);
     uint32_t s = 0;
     for (int k = 0; k < kTile / kBlock; ++k)
-        if (base + k < H) s += counts[base + k];
+        if (base + k < m) s += v[base + k];
     uint32_t total;
     block_excl_scan(s, &total);
     if (threadIdx.x == 0) tiles[blockIdx.x] = total;
@@ -115,46 +148,73 @@ __global__ void k_na_scan_tiles(uint32_t* tiles, int ntiles) {
     }
 }
 
-__global__ void k_na_apply(const uint32_t* counts, long long H, const uint32_t* tiles,
-                           uint32_t* starts) {
+__global__ void k_na_apply(uint32_t* v, long long m, const uint32_t* tiles) {
     const long long base = (long long)blockIdx.x * kTile + threadIdx.x * (kTile / kBlock);
-    uint32_t v[kTile / kBlock];
+    uint32_t x[kTile / kBlock];
     uint32_t s = 0;
     for (int k = 0; k < kTile / kBlock; ++k) {
-        v[k] = base + k < H ? counts[base + k] : 0u;
-        s += v[k];
+        x[k] = base + k < m ? v[base + k] : 0u;
+        s += x[k];
     }
     uint32_t total;
     uint32_t run = tiles[blockIdx.x] + block_excl_scan(s, &total);
     for (int k = 0; k < kTile / kBlock; ++k) {
-        if (base + k < H) starts[base + k] = run;
-        if (base + k == H - 1) starts[H] = run + v[k];
-        run += v[k];
+        if (base + k < m) v[base + k] = run;
+        run += x[k];
     }
 }
 
-// get_particle_id! (src/kernels.jl:15-22); the decrements return every count
-// to zero.
-__global__ void k_na_scatter(const uint32_t* bucket, int n, uint32_t* counts,
-                             const uint32_t* starts, uint32_t* unsorted) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t b = bucket[i] - 1u;
-    const uint32_t slot = atomicSub(&counts[b], 1u) - 1u;
-    unsorted[starts[b] + slot] = (uint32_t)i;
-}
-
-// ascending particle index inside each bucket
-__global__ void k_na_order(const uint32_t* bucket, const uint32_t* unsorted,
-                           const uint32_t* starts, int n, uint32_t* sorted) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const uint32_t i = unsorted[k];
-    const uint32_t b = bucket[i] - 1u;
-    const uint32_t s = starts[b], e = starts[b + 1];
-    uint32_t rank = 0;
-    for (uint32_t t = s; t < e; ++t) rank += unsorted[t] < i ? 1u : 0u;
-    sorted[s + rank] = i;
+// Stable scatter of one block's kChunk (key, index) pairs by the digit at
+// `shift`: an element's place is its block's first slot for that digit plus
+// the number of elements of the block before it with the same digit.  The
+// ranks are counted in element order by one warp, 32 elements per round
+// (__match_any_sync groups equal digits), so the order inside a digit is
+// the input order.  idx_in == nullptr: the indices are the positions.
+__global__ void k_na_digit_scatter(const uint32_t* __restrict__ keys, uint32_t bias,
+                                   const uint32_t* __restrict__ idx_in, int n, int shift, int nblk,
+                                   const uint32_t* __restrict__ first,
+                                   uint32_t* __restrict__ keys_out, uint32_t* __restrict__ idx_out) {
+    __shared__ uint32_t s_key[kChunk], s_idx[kChunk], s_rank[kChunk], s_cnt[kBins];
+    const long long base = (long long)blockIdx.x * kChunk;
+    const int m = (int)min((long long)kChunk, (long long)n - base);
+    for (int b = threadIdx.x; b < kBins; b += kBlock) s_cnt[b] = 0u;
+#pragma unroll
+    for (int q = 0; q < kItems; ++q) {
+        const int e = q * kBlock + threadIdx.x;
+        if (e < m) {
+            s_key[e] = keys[base + e] - bias;
+            s_idx[e] = idx_in ? idx_in[base + e] : (uint32_t)(base + e);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const unsigned lane = threadIdx.x;
+        for (int r = 0; r < kChunk / 32; ++r) {
+            const int e = r * 32 + (int)lane;
+            const bool valid = e < m;
+            const uint32_t d = valid ? (s_key[e] >> shift) & (kBins - 1) : (uint32_t)kBins;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            uint32_t before = 0;
+            if (valid) before = s_cnt[d];
+            __syncwarp();
+            if (valid) {
+                s_rank[e] = before + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+                if ((unsigned)(__ffs(peers) - 1) == lane) s_cnt[d] = before + (uint32_t)__popc(peers);
+            }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kItems; ++q) {
+        const int e = q * kBlock + threadIdx.x;
+        if (e < m) {
+            const uint32_t d = (s_key[e] >> shift) & (kBins - 1);
+            const uint32_t dst = first[(size_t)d * nblk + blockIdx.x] + s_rank[e];
+            idx_out[dst] = s_idx[e];
+            if (keys_out) keys_out[dst] = s_key[e];
+        }
+    }
 }
 
 std::mutex g_setup_mutex;
@@ -168,12 +228,19 @@ int scratch_on(int device, uint32_t** out) {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (!g_scratch_ptr[device]) {
         void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return DEM_ERR_CUDA;
+        if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) {
+            cudaGetLastError();  // this call's own failure
+            return DEM_ERR_CUDA;
+        }
         g_scratch_ptr[device] = static_cast<uint32_t*>(p);
     }
     *out = g_scratch_ptr[device];
     return DEM_OK;
 }
+
+// The launch just queued: its configuration error, if any (a launch error is
+// this call's own; the check at entry made sure none was pending before).
+inline bool launched() { return cudaGetLastError() == cudaSuccess; }
 
 }  // namespace
 
@@ -185,31 +252,50 @@ extern "C" int dem_bucket_sort_noalloc(const double* px, const double* py, const
     if (n > kMaxN || hash_table_size > kMaxH) return DEM_ERR_CAPACITY;
     if (n > 0 && (!px || !py || !pz || !bucket || !sorted)) return DEM_ERR_INVALID;
     if (n == 0) return DEM_OK;
+    // an error already pending on this thread belongs to someone else: it is
+    // reported (DEM_ERR_CUDA) and left in place, and no work is queued
+    if (cudaPeekAtLastError() != cudaSuccess) return DEM_ERR_CUDA;
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) return DEM_ERR_NO_DEVICE;
     uint32_t* scratch = nullptr;
     const int rc = scratch_on(device, &scratch);
     if (rc != DEM_OK) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    uint32_t* counts = scratch + kCountsOff;
-    uint32_t* starts = scratch + kStartsOff;
+    uint32_t* keys_tmp = scratch + kKeysOff;
+    uint32_t* idx_tmp = scratch + kValsOff;
+    uint32_t* hist = scratch + kHistOff;
     uint32_t* tiles = scratch + kTilesOff;
-    uint32_t* unsorted = scratch + kUnsortedOff;
     Geometry g;
-    for (int c = 0; c < 3; ++c) g.dmin[c] = domain_min[c];
+    for (int c = 0; c < 3; ++c) g.dmin[c] = domain_min[c];  // host memory
     g.cell = cell_size;
     g.H = (uint32_t)hash_table_size;
     g.mask = (g.H & (g.H - 1)) == 0 ? g.H - 1 : 0u;
     const int nn = (int)n;
-    const int nb = (nn + kBlock - 1) / kBlock;
-    const int ntiles = (int)((hash_table_size + kTile - 1) / kTile);
-    if (cudaMemsetAsync(counts, 0, sizeof(uint32_t) * (size_t)hash_table_size, s) != cudaSuccess)
-        return DEM_ERR_CUDA;
-    k_na_hash<<<nb, kBlock, 0, s>>>(px, py, pz, nn, g, bucket, counts);
-    k_na_tile_sums<<<ntiles, kBlock, 0, s>>>(counts, hash_table_size, tiles);
-    k_na_scan_tiles<<<1, kBlock, 0, s>>>(tiles, ntiles);
-    k_na_apply<<<ntiles, kBlock, 0, s>>>(counts, hash_table_size, tiles, starts);
-    k_na_scatter<<<nb, kBlock, 0, s>>>(bucket, nn, counts, starts, unsorted);
-    k_na_order<<<nb, kBlock, 0, s>>>(bucket, unsorted, starts, nn, sorted);
-    return cudaGetLastError() == cudaSuccess ? DEM_OK : DEM_ERR_CUDA;
+    k_na_hash<<<(nn + kBlock - 1) / kBlock, kBlock, 0, s>>>(px, py, pz, nn, g, bucket);
+    if (!launched()) return DEM_ERR_CUDA;
+    // buckets are 0 .. H-1 < 2^20: one 10-bit pass for H <= 1,024, else two
+    const int passes = hash_table_size <= kBins ? 1 : 2;
+    const int nblk = (nn + kChunk - 1) / kChunk;
+    const long long m = (long long)kBins * nblk;
+    const int ntiles = (int)((m + kTile - 1) / kTile);
+    for (int pass = 0; pass < passes; ++pass) {
+        const int shift = pass * kDigitBits;
+        const bool last = pass == passes - 1;
+        const uint32_t* kin = pass == 0 ? bucket : keys_tmp;
+        const uint32_t bias = pass == 0 ? 1u : 0u;  // the outputs' buckets are 1-based
+        const uint32_t* iin = pass == 0 ? nullptr : idx_tmp;
+        k_na_digit_count<<<nblk, kBlock, 0, s>>>(kin, bias, nn, shift, nblk, hist);
+        if (!launched()) return DEM_ERR_CUDA;
+        k_na_tile_sums<<<ntiles, kBlock, 0, s>>>(hist, m, tiles);
+        if (!launched()) return DEM_ERR_CUDA;
+        k_na_scan_tiles<<<1, kBlock, 0, s>>>(tiles, ntiles);
+        if (!launched()) return DEM_ERR_CUDA;
+        k_na_apply<<<ntiles, kBlock, 0, s>>>(hist, m, tiles);
+        if (!launched()) return DEM_ERR_CUDA;
+        k_na_digit_scatter<<<nblk, kBlock, 0, s>>>(kin, bias, iin, nn, shift, nblk, hist,
+                                                   last ? nullptr : keys_tmp,
+                                                   last ? sorted : idx_tmp);
+        if (!launched()) return DEM_ERR_CUDA;
+    }
+    return DEM_OK;
 }

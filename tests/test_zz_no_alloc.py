@@ -37,7 +37,7 @@ def _run_noalloc(lib, torch, p, derived, cfg):
     px, py, pz = (pos[:, k].contiguous() for k in range(3))
     bucket = torch.full((n,), -1, dtype=torch.int32, device="cuda")
     order = torch.full((n,), -1, dtype=torch.int32, device="cuda")
-    dmin = (C.c_double * 3)(*cfg.domain_min)
+    dmin = (C.c_double * 3)(*cfg.domain_min)  # a host array, as the entry point reads it
     torch.cuda.synchronize()
     rc = lib.dem_bucket_sort_noalloc(px.data_ptr(), py.data_ptr(), pz.data_ptr(), n, dmin,
                                      derived["cell_size"], derived["hash_table_size"],
@@ -73,3 +73,28 @@ def test_noalloc_rejects_sizes_beyond_its_array(gpu):
     rc = lib.dem_bucket_sort_noalloc(None, None, None, 10, dmin, 0.1, (1 << 20) + 1,
                                      None, None, None)
     assert rc == _abi.DEM_ERR_CAPACITY
+
+
+def _hashcode(pos, dmin, cell, H):
+    """src/utils.jl:1-2 restated: ceil((x - dmin) / cell) per axis, then the
+    1-based Morton code (x in bit 0) modulo H, plus 1."""
+    from oracle import oracle as O
+    ijk = np.ceil((pos - np.asarray(dmin)) / cell).astype(np.int64)
+    return np.array([O.morton1(int(x), int(y), int(z)) % H + 1 for x, y, z in ijk], np.uint32)
+
+
+@pytest.mark.parametrize("H,cell", [(3001, 0.013), (65537, 0.011), (1, 0.02), (1024, 0.5)])
+def test_noalloc_small_tables_and_crowded_buckets(gpu, H, cell):
+    """Tables the regular path never uses (any H from 1 up; non-powers of two
+    take the modulo path, H = 1 and a cell as large as the domain put every
+    particle in one bucket), against a restatement of hashcode and a stable
+    argsort by bucket, twice in a row."""
+    torch = pytest.importorskip("torch")
+    lib = _abi.load_library()
+    for seed in (7, 8):
+        cfg, p = _cloud(20000, seed=seed)
+        bucket, order = _run_noalloc(lib, torch, p, {"cell_size": cell, "hash_table_size": H},
+                                     cfg)
+        want = _hashcode(p.pos, cfg.domain_min, cell, H)
+        np.testing.assert_array_equal(bucket, want)
+        np.testing.assert_array_equal(order, np.argsort(want, kind="stable").astype(np.uint32))
