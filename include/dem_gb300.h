@@ -135,6 +135,17 @@ typedef struct DemContacts {
     double* shear;     /* 3 per contact, 𝐬                      */
 } DemContacts;
 
+/* One line of a p4c record, as `save_single` writes it (src/utils.jl:48-69):
+ * the contact's particles (0-based, i < j), whether it is a bond, its
+ * position 𝐤 and its force 𝐅ᵢ in the local frame.  64 bytes. */
+typedef struct DemIOContact {
+    int32_t i, j;
+    int32_t bonded;
+    int32_t pad;
+    double point[3];
+    double force[3];
+} DemIOContact;
+
 /* Values `solve` derives before the loop (src/executor.jl:244-267). */
 typedef struct DemDerived {
     double cell_size;        /* 4 rₘₐₓ                                  */
@@ -284,6 +295,16 @@ int dem_host_free(void* p);
 int dem_get_static(DemHandle* h, DemParticleStatic* out);
 
 int dem_get_derived(DemHandle* h, DemDerived* out);
+
+/* The active contacts as p4c records, sorted by (i, j): what `save_single`
+ * writes (src/utils.jl:48-69, which copies every contact and both BitTables
+ * to the host and filters there).  The active contacts are compacted on the
+ * device into DemIOContact records, and only those cross to the host.
+ * *n_out receives the count even when it exceeds cap (then DEM_ERR_CAPACITY
+ * is returned and nothing is written). */
+int dem_get_io_contacts(DemHandle* h, DemIOContact* out, int64_t cap, int64_t* n_out);
+int dem_scene_get_io_contacts(DemHandle* h, int32_t scene, DemIOContact* out, int64_t cap,
+                              int64_t* n_out);
 
 /* Active contacts, sorted by (i, j).  *n_out receives the count even when it
  * exceeds cap (then DEM_ERR_CAPACITY is returned and nothing is written). */

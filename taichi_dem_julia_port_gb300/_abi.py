@@ -168,6 +168,9 @@ ENTRY_POINTS = {
     "dem_get_static": (C.c_int, [_H, C.POINTER(DemParticleStatic)]),
     "dem_get_derived": (C.c_int, [_H, C.POINTER(DemDerived)]),
     "dem_get_contacts": (C.c_int, [_H, C.POINTER(DemContacts), C.c_int64, C.POINTER(C.c_int64)]),
+    "dem_get_io_contacts": (C.c_int, [_H, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "dem_scene_get_io_contacts": (C.c_int, [_H, C.c_int32, C.c_void_p, C.c_int64,
+                                            C.POINTER(C.c_int64)]),
     "dem_set_contacts": (C.c_int, [_H, C.POINTER(DemContacts), C.c_int64]),
     "dem_get_stats": (C.c_int, [_H, C.POINTER(DemStats)]),
     "dem_debug_broadphase": (C.c_int, [_H, _PI32, _PU32, _PU32, _PU32, _PU32, _PI32, C.c_int64,
@@ -192,6 +195,11 @@ ENTRY_POINTS = {
     "dem_strerror": (C.c_char_p, [C.c_int]),
     "dem_version": (C.c_char_p, []),
 }
+
+# DemIOContact: one p4c line (i, j 0-based; bonded; 𝐤; 𝐅ᵢ), 64 bytes
+IO_CONTACT_DTYPE = np.dtype([("i", "<i4"), ("j", "<i4"), ("bonded", "<i4"), ("pad", "<i4"),
+                             ("point", "<f8", (3,)), ("force", "<f8", (3,))])
+assert IO_CONTACT_DTYPE.itemsize == 64
 
 PKG_DIR = Path(__file__).resolve().parent
 LIB_PATH = PKG_DIR / "libdem_sm100a.so"

@@ -372,6 +372,10 @@ struct DemHandle {
     int64_t xfer_n = 0;        // doubles
     int* err_host = nullptr;   // page-locked copy of the device error word
     int* err_dev = nullptr;    // its device address
+    int32_t* io_idx = nullptr;  // p4c records: per-slot counts and their scan (2n + 1)
+    int64_t io_idx_n = 0;
+    void* io_rec = nullptr;     // p4c records (64 bytes each)
+    int64_t io_rec_n = 0;
 };
 
 #define CU(expr)                                                                            \
@@ -483,6 +487,10 @@ void free_all(DemHandle* h) {
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->xfer) cudaFree(h->xfer);
     h->xfer = nullptr;
+    if (h->io_idx) cudaFree(h->io_idx);
+    h->io_idx = nullptr;
+    if (h->io_rec) cudaFree(h->io_rec);
+    h->io_rec = nullptr;
     if (h->err_host) cudaFreeHost(h->err_host);
     h->err_host = nullptr;
     h->err_dev = nullptr;
@@ -979,6 +987,49 @@ int get_contacts_range(DemHandle* h, int64_t p0, int64_t n, DemContacts* out, in
             if (out->shear) out->shear[3 * t + q] = bonded ? 0.0 : f[CS + q][c];
         }
     }
+    return DEM_OK;
+}
+
+// The active contacts of slots [p0, p0 + n) as p4c records in (i, j) order,
+// compacted on the device: per-slot counts, their scan, then the records of
+// each row in row order (rows are sorted by j); only the records cross to
+// the host.
+int get_io_contacts_range(DemHandle* h, int64_t p0, int64_t n, DemIOContact* out, int64_t cap,
+                          int64_t* n_out) {
+    TRY(device_error(h));
+    *n_out = 0;
+    if (n == 0) return DEM_OK;
+    if (h->io_idx_n < 2 * n + 1) {
+        if (h->io_idx) cudaFree(h->io_idx);
+        h->io_idx = nullptr;
+        h->io_idx_n = 0;
+        CU(cudaMalloc(&h->io_idx, sizeof(int32_t) * (size_t)(2 * n + 1)));
+        h->io_idx_n = 2 * n + 1;
+    }
+    int32_t* cnt = h->io_idx;
+    int32_t* off = h->io_idx + n;
+    launch_io_count(h->d, h->cur, h->c_cap, (int)p0, (int)n, cnt, h->stream);
+    launch_scan_i32(cnt, off, n, h->d, kScanDebug, h->stream);
+    CU(cudaGetLastError());
+    int32_t total = 0;
+    CU(cudaMemcpyAsync(&total, off + n, sizeof(total), cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaStreamSynchronize(h->stream));
+    *n_out = total;
+    if (!out || total == 0) return DEM_OK;
+    if (total > cap) return DEM_ERR_CAPACITY;
+    if (h->io_rec_n < total) {
+        if (h->io_rec) cudaFree(h->io_rec);
+        h->io_rec = nullptr;
+        h->io_rec_n = 0;
+        CU(cudaMalloc(&h->io_rec, sizeof(DemIOContact) * (size_t)total));
+        h->io_rec_n = total;
+    }
+    launch_io_fill(h->d, h->cur, h->c_cap, (int)p0, (int)n, off, h->enc == DEM_FP32_FORCE,
+                   h->io_rec, h->stream);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(out, h->io_rec, sizeof(DemIOContact) * (size_t)total,
+                       cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaStreamSynchronize(h->stream));
     return DEM_OK;
 }
 
@@ -1524,6 +1575,17 @@ int dem_scene_get_contacts(DemHandle* h, int32_t s, DemContacts* out, int64_t ca
 
 int dem_get_contacts(DemHandle* h, DemContacts* out, int64_t cap, int64_t* n_out) {
     return dem_scene_get_contacts(h, 0, out, cap, n_out);
+}
+
+int dem_scene_get_io_contacts(DemHandle* h, int32_t s, DemIOContact* out, int64_t cap,
+                              int64_t* n_out) {
+    const SceneHost* S = scene_at(h, s);
+    if (!S || !n_out || cap < 0) return DEM_ERR_INVALID;
+    return get_io_contacts_range(h, S->sp.p0, S->sp.n, out, cap, n_out);
+}
+
+int dem_get_io_contacts(DemHandle* h, DemIOContact* out, int64_t cap, int64_t* n_out) {
+    return dem_scene_get_io_contacts(h, 0, out, cap, n_out);
 }
 
 int dem_set_contacts(DemHandle* h, const DemContacts* in, int64_t nc) {

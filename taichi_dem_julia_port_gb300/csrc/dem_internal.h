@@ -228,6 +228,16 @@ void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, cons
 void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
                       const LaunchShape& sh, cudaStream_t s);
 
+// save_single's contact records (src/utils.jl:48-69): per slot of
+// [p0, p0 + n) the number of active entries of its row in buffer `cur`
+// (cnt[n]); then, from their exclusive scan `off` (n + 1 entries), the
+// records themselves (64 bytes each: i, j, bonded, pad, 𝐤, 𝐅ᵢ; indices
+// relative to p0; 𝐅ᵢ decoded from FP32 hi/lo pairs when `pairs`)
+void launch_io_count(const DemDev& d, int cur, int cap, int p0, int n, int32_t* cnt,
+                     cudaStream_t s);
+void launch_io_fill(const DemDev& d, int cur, int cap, int p0, int n, const int32_t* off,
+                    bool pairs, void* out, cudaStream_t s);
+
 // debug: cp_list materialisation on the current bucket arrays (single scene)
 void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cudaStream_t s);
 void launch_cplist_fill(const DemDev& d, const DemParams& p, const int32_t* off, int32_t* cp,

@@ -2251,6 +2251,70 @@ void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
                s, d, p, cur);
 }
 
+// Active entries of a slot's row (its contacts (i, j), j > i, sorted by j).
+__device__ __forceinline__ void io_row(const DemDev& d, int cur, int cap, int i, int& e0,
+                                       int& e1) {
+    const int C = min((int)d.ctr->row_alloc[cur], cap);
+    e0 = max(d.row_start[cur][i], 0);
+    e1 = min(d.row_start[cur][i] + d.row_len[cur][i], C);
+}
+__global__ void k_io_count(DemDev d, int cur, int cap, int p0, int n, int32_t* cnt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int i = p0 + t;
+    int e0, e1, m = 0;
+    io_row(d, cur, cap, i, e0, e1);
+    const ContactSoA w = d.c[cur];
+    for (int e = e0; e < e1; ++e) m += ((w.fl[e] & kActive) && w.ci[e] == i) ? 1 : 0;
+    cnt[t] = m;
+}
+struct IORecord {
+    int32_t i, j, bonded, pad;
+    double k[3], F[3];
+};
+static_assert(sizeof(IORecord) == 64, "the DemIOContact layout");
+__global__ void k_io_fill(DemDev d, int cur, int cap, int p0, int n, const int32_t* off,
+                          int pairs, IORecord* out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int i = p0 + t;
+    int e0, e1;
+    io_row(d, cur, cap, i, e0, e1);
+    const ContactSoA w = d.c[cur];
+    int q = off[t];
+    for (int e = e0; e < e1; ++e) {
+        const uint32_t fl = w.fl[e];
+        if (!(fl & kActive) || w.ci[e] != i) continue;
+        IORecord r;
+        r.i = t;
+        r.j = w.cj[e] - p0;
+        r.bonded = (fl & kBonded) ? 1 : 0;
+        r.pad = 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            r.k[c] = w.f[CK + c][e];
+            if (pairs) {
+                const float2 v = reinterpret_cast<const float2*>(w.f[CF + c])[e];
+                r.F[c] = (double)v.x + (double)v.y;
+            } else {
+                r.F[c] = w.f[CF + c][e];
+            }
+        }
+        out[q++] = r;
+    }
+}
+void launch_io_count(const DemDev& d, int cur, int cap, int p0, int n, int32_t* cnt,
+                     cudaStream_t s) {
+    if (n <= 0) return;
+    k_io_count<<<blocks_for(n, kThreads), kThreads, 0, s>>>(d, cur, cap, p0, n, cnt);
+}
+void launch_io_fill(const DemDev& d, int cur, int cap, int p0, int n, const int32_t* off,
+                    bool pairs, void* out, cudaStream_t s) {
+    if (n <= 0) return;
+    k_io_fill<<<blocks_for(n, kThreads), kThreads, 0, s>>>(d, cur, cap, p0, n, off, pairs ? 1 : 0,
+                                                           static_cast<IORecord*>(out));
+}
+
 void launch_cplist_count(const DemDev& d, const DemParams& p, int32_t* cnt, cudaStream_t s) {
     if (p.n == 0) return;
     k_cp_count<<<blocks_for(p.n, kThreads), kThreads, 0, s>>>(d, p, cnt);

@@ -289,6 +289,19 @@ class GlobalData:
             self.lib, lambda cs, cap, cnt: self.lib.dem_get_contacts(self.h, cs, cap, cnt),
             "dem_get_contacts")
 
+    def io_contacts(self) -> np.ndarray:
+        """The active contacts as p4c records (a structured array of
+        _abi.IO_CONTACT_DTYPE: i, j 0-based, bonded, point, force), sorted by
+        (i, j), compacted on the device (dem_get_io_contacts)."""
+        cnt = C.c_int64()
+        check(self.lib, self.lib.dem_get_io_contacts(self.h, None, 0, C.byref(cnt)),
+              "dem_get_io_contacts")
+        out = np.empty(cnt.value, dtype=_abi.IO_CONTACT_DTYPE)
+        if cnt.value:
+            check(self.lib, self.lib.dem_get_io_contacts(self.h, out.ctypes.data, cnt.value,
+                                                         C.byref(cnt)), "dem_get_io_contacts")
+        return out
+
     def set_contacts(self, c: dict) -> None:
         m = len(c["i"])
         arr = {"i": np.ascontiguousarray(c["i"], np.int32),
@@ -408,12 +421,13 @@ def load_particles(p4p_path: str | Path) -> ParticleInput:
 
 def save_single(g: GlobalData, p4p, p4c, t: float) -> int:
     """`save_single` (src/utils.jl:30-78): appends one record to each file and
-    returns the number of active contacts written."""
+    returns the number of active contacts written.  The active contacts are
+    compacted into p4c records on the device (dem_get_io_contacts)."""
     st = g.particles(forces=False)
     write_p4p(p4p, t, g.ids, g.gid, g.volume, g.mass, st["pos"], st["vel"])
-    c = g.contacts()
+    c = g.io_contacts()
     write_p4c(p4c, t, c["i"], c["j"], c["point"], c["force"], c["bonded"])
-    return len(c["i"])
+    return len(c)
 
 
 def solve(cfg_filename: str | Path, no_bond: bool = False, save_snapshot: bool = False,
