@@ -135,6 +135,51 @@ typedef struct DemContacts {
     double* shear;     /* 3 per contact, 𝐬                      */
 } DemContacts;
 
+/* ---- material, surface and wall tables ---------------------------------
+ * The reference's GlobalData holds a table of materials, a square table of
+ * surfaces indexed by the two materials in contact, a list of walls and one
+ * material index per grain (src/types.jl:9-27, 58-62; src/executor.jl:1-29);
+ * its kernels read them per contact (src/kernels.jl:175-177, 255-263) and
+ * loop over the walls per particle (src/kernels.jl:317-426).  Its `solve`
+ * fills them with one particle material, one wall material and one wall
+ * (src/executor.jl:282-315), which is what dem_create does.  Indices here are
+ * 0-based (the reference's mid - 1). */
+#define DEM_MAX_MATERIALS 8
+#define DEM_MAX_WALLS 8
+
+typedef struct DemMaterial {   /* Material (src/types.jl:9-13) */
+    double density;            /* ρ (not used by any force)            */
+    double elastic_modulus;    /* E                                    */
+    double poisson_ratio;      /* ν                                    */
+} DemMaterial;
+
+typedef struct DemSurface {    /* Surface (src/types.jl:17-27) */
+    double friction;           /* μ                                    */
+    double restitution;        /* e                                    */
+    double rolling_resistance; /* μᵣ (declared, unused, as in the reference) */
+    double bond_radius_ratio;  /* ρ: bond radius = ρ·min(rᵢ, rⱼ)       */
+    double bond_elastic_modulus;
+    double bond_poisson_ratio;
+    double bond_compressive_strength;
+    double bond_tensile_strength;
+    double bond_shear_strength;
+} DemSurface;
+
+typedef struct DemWall {       /* Wall (src/types.jl:58-62) */
+    double normal[3];          /* 𝐧                                    */
+    double distance;           /* d: the plane 𝐧·𝐱 = d                 */
+    int64_t material;          /* index into the materials            */
+} DemWall;
+
+typedef struct DemTables {
+    int64_t n_materials;              /* 1 .. DEM_MAX_MATERIALS         */
+    const DemMaterial* materials;     /* n_materials                    */
+    const DemSurface* surfaces;       /* n_materials², [a * n_materials + b] = surfaces[a+1, b+1] */
+    int64_t n_walls;                  /* 0 .. DEM_MAX_WALLS             */
+    const DemWall* walls;             /* n_walls                        */
+    const int32_t* grain_material;    /* one per grain (Grain.mid - 1)  */
+} DemTables;
+
 /* One line of a p4c record, as `save_single` writes it (src/utils.jl:48-69):
  * the contact's particles (0-based, i < j), whether it is a bond, its
  * position 𝐤 and its force 𝐅ᵢ in the local frame.  64 bytes. */
@@ -195,6 +240,25 @@ int dem_destroy(DemHandle* h);
 
 /* `initialize!` (src/executor.jl:155-160): broad phase + `init_bonds!`
  * (src/kernels.jl:60-85). */
+/* dem_create with the scene's own material, surface and wall tables (the
+ * reference's GlobalData.materials / surfaces / walls and Grain.mid, which
+ * `initialize!` and `simulate!` read; src/executor.jl:155-172).  The config
+ * supplies everything else as for dem_create: domain, derived sizes (cell
+ * size from the largest radius and the config's bond strength and modulus,
+ * src/executor.jl:244-267), dt, gravity, damping, tolerance, contact
+ * capacity; its material, surface and wall keys are not used.  Returns
+ * DEM_ERR_INVALID for a table outside the limits above or an index out of
+ * range.  Such a handle computes in FP64: dem_set_precision(DEM_FP32_FORCE)
+ * returns DEM_ERR_INVALID for it. */
+int dem_create_tables(const DemConfigC* cfg, const DemParticlesIn* particles,
+                      const DemTables* tables, DemHandle** out);
+
+/* Shear history 𝐬 of wall `wall`'s contacts, wall_contacts[wall+1, :] of the
+ * reference (3n doubles, zero where the grain does not touch the wall).
+ * DemParticleState.wall_shear is wall 0's. */
+int dem_get_wall_shear(DemHandle* h, int32_t wall, double* shear);
+int dem_set_wall_shear(DemHandle* h, int32_t wall, const double* shear);
+
 int dem_init_bonds(DemHandle* h);
 
 /* `simulate!` × nsteps (src/executor.jl:162-172): clear_state!, contact!,

@@ -294,9 +294,12 @@ struct Scene {
     std::vector<Grain> g;
     double cell_size = 0, rmax = 0, material_density = 0;
     int64_t H = 0, total_steps = 0, save_per_steps = 0;
-    Material mat[2];
-    Surface surf[2][2];
-    Wall wall;
+    // materials, surfaces ([a * nmat + b] = surfaces[a+1, b+1]) and walls
+    // (src/types.jl:9-27, 58-62); wall_contacts[w * n + i] = wall_contacts[w+1, i+1]
+    int nmat = 0;
+    std::vector<Material> mat;
+    std::vector<Surface> surf;
+    std::vector<Wall> walls;
     std::vector<Contact> wall_contacts;  // nwall = 1
     std::vector<double> forces, moments;
     // broad phase
@@ -355,8 +358,7 @@ void setup(Scene& S, const DemConfigC& cfg, const DemParticlesIn& p) {
     S.total_steps = (int64_t)std::trunc(cfg.target_time / cfg.dt);
     S.save_per_steps = (int64_t)std::trunc(cfg.saving_interval_time / cfg.dt);
     set_tables(S);
-    S.wall_contacts.assign(S.n, Contact{});
-    for (int64_t i = 0; i < S.n; ++i) S.wall_contacts[i].i = (int32_t)i;
+    S.wall_contacts.assign(S.n * S.walls.size(), Contact{});
     S.forces.assign(3 * S.n, 0.0);
     S.moments.assign(3 * S.n, 0.0);
     S.contacts.clear();
@@ -370,17 +372,18 @@ void setup(Scene& S, const DemConfigC& cfg, const DemParticlesIn& p) {
 // material, mid = 1; the wall material, mid = 2).
 void set_tables(Scene& S) {
     const DemConfigC& cfg = S.cfg;
-    S.mat[0] = {S.material_density, cfg.particle_elastic_modulus, cfg.particle_poisson_ratio};
-    S.mat[1] = {cfg.wall_density, cfg.wall_elastic_modulus, cfg.wall_poisson_ratio};
-    S.surf[0][0] = {cfg.pp_coefficient_friction, cfg.pp_coefficient_restitution,
-                    cfg.pp_coefficient_rolling_resistance, cfg.bond_radius_ratio,
-                    cfg.bond_elastic_modulus, cfg.bond_poisson_ratio,
-                    cfg.bond_compressive_strength, cfg.bond_tensile_strength,
-                    cfg.bond_shear_strength};
-    S.surf[0][1] = S.surf[1][0] = {cfg.pw_coefficient_friction, cfg.pw_coefficient_restitution,
-                                   cfg.pw_coefficient_rolling_resistance, 0, 0, 0, 0, 0, 0};
-    S.surf[1][1] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    S.wall = {{cfg.wall_normal[0], cfg.wall_normal[1], cfg.wall_normal[2]}, cfg.wall_distance, 1};
+    S.nmat = 2;
+    S.mat = {{S.material_density, cfg.particle_elastic_modulus, cfg.particle_poisson_ratio},
+             {cfg.wall_density, cfg.wall_elastic_modulus, cfg.wall_poisson_ratio}};
+    const Surface pp{cfg.pp_coefficient_friction, cfg.pp_coefficient_restitution,
+                     cfg.pp_coefficient_rolling_resistance, cfg.bond_radius_ratio,
+                     cfg.bond_elastic_modulus, cfg.bond_poisson_ratio,
+                     cfg.bond_compressive_strength, cfg.bond_tensile_strength,
+                     cfg.bond_shear_strength};
+    const Surface pw{cfg.pw_coefficient_friction, cfg.pw_coefficient_restitution,
+                     cfg.pw_coefficient_rolling_resistance, 0, 0, 0, 0, 0, 0};
+    S.surf = {pp, pw, pw, Surface{0, 0, 0, 0, 0, 0, 0, 0, 0}};
+    S.walls = {Wall{{cfg.wall_normal[0], cfg.wall_normal[1], cfg.wall_normal[2]}, cfg.wall_distance, 1}};
 }
 
 // ---- broad phase (src/executor.jl:38-78, src/utils.jl:1-16, src/kernels.jl:7-58)
@@ -544,7 +547,7 @@ ContactResult resolve_one(const Scene& S, const Contact& ct, bool is_bonded) {
         V3 k = (gi.k + gj.k) * 0.5;
         V3 di = mv(R, gi.v) * dt, dj = mv(R, gj.v) * dt;
         V3 thi = mv(R, gi.w) * dt, thj = mv(R, gj.w) * dt;
-        const Surface& sf = S.surf[gi.mid][gj.mid];
+        const Surface& sf = S.surf[gi.mid * S.nmat + gj.mid];
         double rj = sf.rho * jl_min(gi.r, gj.r);
         double Lj = Li;
         double Ej = sf.E, nu = sf.nu;
@@ -598,7 +601,7 @@ ContactResult resolve_one(const Scene& S, const Contact& ct, bool is_bonded) {
     V3 vcj = cross(gj.w, kj) + gj.v;
     V3 vc = mv(R, vcj - vci);
     const Material &mi = S.mat[gi.mid], &mj = S.mat[gj.mid];
-    const Surface& sf = S.surf[gi.mid][gj.mid];
+    const Surface& sf = S.surf[gi.mid * S.nmat + gj.mid];
     double Ys = 1.0 / ((1.0 - mi.nu * mi.nu) / mi.E + (1.0 - mj.nu * mj.nu) / mj.E);
     double Gs = 1.0 / (2.0 * (2.0 - mi.nu) * (1.0 + mi.nu) / mi.E +
                        2.0 * (2.0 - mj.nu) * (1.0 + mj.nu) / mj.E);
@@ -679,15 +682,17 @@ void resolve_collision(Scene& S) {
     }
 }
 
-// resolve_wall! (src/kernels.jl:317-426), one wall
+// resolve_wall! (src/kernels.jl:317-426): every wall j in order, per particle
 void resolve_wall(Scene& S) {
     const double dt = S.cfg.dt, tol = S.cfg.tolerance;
-    const Wall& W = S.wall;
+    const int64_t nw = (int64_t)S.walls.size();
     int64_t warn = 0;
 #pragma omp parallel for num_threads(S.threads) schedule(static) reduction(+ : warn)
     for (int64_t i = 0; i < S.n; ++i) {
-        const Grain& G = S.g[i];
-        Contact& wc = S.wall_contacts[i];
+      const Grain& G = S.g[i];
+      for (int64_t w = 0; w < nw; ++w) {
+        const Wall& W = S.walls[w];
+        Contact& wc = S.wall_contacts[w * S.n + i];
         if (std::fabs(dot(G.k, W.n) - W.d) < G.r) {
             M3 R = frame_to_x(W.n, tol);
             double L = dot(G.k, W.n) - W.d;
@@ -700,7 +705,7 @@ void resolve_wall(Scene& S) {
             V3 vci = cross(G.w, ki) + G.v;
             V3 vc = mv(R, -vci);
             const Material &mi = S.mat[G.mid], &mj = S.mat[W.mid];
-            const Surface& sf = S.surf[G.mid][W.mid];
+            const Surface& sf = S.surf[G.mid * S.nmat + W.mid];
             double Ys = 1.0 / ((1.0 - mi.nu * mi.nu) / mi.E + (1.0 - mj.nu * mj.nu) / mj.E);
             double Gs = 1.0 / (2.0 * (2.0 - mi.nu) * (1.0 + mi.nu) / mi.E +
                                2.0 * (2.0 - mj.nu) * (1.0 + mj.nu) / mj.E);
@@ -745,6 +750,7 @@ void resolve_wall(Scene& S) {
         } else {
             wc = Contact{};
         }
+      }
     }
     S.warn_gamma += warn;
 }
@@ -835,7 +841,57 @@ void* oracle_create(const DemConfigC* cfg, const DemParticlesIn* p, int threads)
     return S;
 }
 
+// A scene with its own material, surface and wall tables (the reference's
+// GlobalData.materials / surfaces / walls and Grain.mid); indices 0-based.
+void* oracle_create_tables(const DemConfigC* cfg, const DemParticlesIn* p, const DemTables* t,
+                           int threads) {
+    if (!cfg || !p || p->n < 0 || !t || t->n_materials < 1) return nullptr;
+    Scene* S = new Scene();
+    S->threads = threads > 0 ? threads : 1;
+    setup(*S, *cfg, *p);
+    const int nm = (int)t->n_materials;
+    S->nmat = nm;
+    S->mat.clear();
+    for (int a = 0; a < nm; ++a) {
+        const DemMaterial& m = t->materials[a];
+        S->mat.push_back({m.density, m.elastic_modulus, m.poisson_ratio});
+    }
+    S->surf.clear();
+    for (int q = 0; q < nm * nm; ++q) {
+        const DemSurface& f = t->surfaces[q];
+        S->surf.push_back({f.friction, f.restitution, f.rolling_resistance, f.bond_radius_ratio,
+                           f.bond_elastic_modulus, f.bond_poisson_ratio,
+                           f.bond_compressive_strength, f.bond_tensile_strength,
+                           f.bond_shear_strength});
+    }
+    S->walls.clear();
+    for (int64_t w = 0; w < t->n_walls; ++w) {
+        const DemWall& W = t->walls[w];
+        S->walls.push_back({{W.normal[0], W.normal[1], W.normal[2]}, W.distance,
+                            (int32_t)W.material});
+    }
+    S->wall_contacts.assign((size_t)S->n * S->walls.size(), Contact{});
+    for (int64_t i = 0; i < S->n; ++i) S->g[i].mid = t->grain_material[i];
+    return S;
+}
+
 void oracle_destroy(void* h) { delete static_cast<Scene*>(h); }
+
+// wall_contacts[w+1, :].𝐬 (3n doubles)
+int oracle_get_wall_shear(void* h, int w, double* out) {
+    Scene& S = *static_cast<Scene*>(h);
+    if (w < 0 || w >= (int)S.walls.size()) return DEM_ERR_INVALID;
+    for (int64_t i = 0; i < S.n; ++i)
+        for (int c = 0; c < 3; ++c) out[3 * i + c] = at(S.wall_contacts[w * S.n + i].s, c);
+    return DEM_OK;
+}
+int oracle_set_wall_shear(void* h, int w, const double* in) {
+    Scene& S = *static_cast<Scene*>(h);
+    if (w < 0 || w >= (int)S.walls.size()) return DEM_ERR_INVALID;
+    for (int64_t i = 0; i < S.n; ++i)
+        S.wall_contacts[w * S.n + i].s = {in[3 * i], in[3 * i + 1], in[3 * i + 2]};
+    return DEM_OK;
+}
 
 void oracle_set_threads(void* h, int threads) {
     static_cast<Scene*>(h)->threads = threads > 0 ? threads : 1;
@@ -888,7 +944,8 @@ int oracle_get_particles(void* h, DemParticleState* out) {
             if (out->omega) out->omega[3 * i + c] = at(G.w, c);
             if (out->force) out->force[3 * i + c] = S.forces[3 * i + c];
             if (out->moment) out->moment[3 * i + c] = S.moments[3 * i + c];
-            if (out->wall_shear) out->wall_shear[3 * i + c] = at(S.wall_contacts[i].s, c);
+            if (out->wall_shear)
+                out->wall_shear[3 * i + c] = S.walls.empty() ? 0.0 : at(S.wall_contacts[i].s, c);
         }
         if (out->quat)
             for (int c = 0; c < 4; ++c) out->quat[4 * i + c] = G.q[c];
@@ -905,7 +962,7 @@ int oracle_set_particles(void* h, const DemParticleState* in) {
         if (in->omega) G.w = {in->omega[3 * i], in->omega[3 * i + 1], in->omega[3 * i + 2]};
         if (in->quat)
             for (int c = 0; c < 4; ++c) G.q[c] = in->quat[4 * i + c];
-        if (in->wall_shear)
+        if (in->wall_shear && !S.walls.empty())
             S.wall_contacts[i].s = {in->wall_shear[3 * i], in->wall_shear[3 * i + 1],
                                     in->wall_shear[3 * i + 2]};
     }

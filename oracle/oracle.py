@@ -35,6 +35,10 @@ def load() -> C.CDLL:
     sig = {
         "oracle_create": (H, [C.POINTER(_abi.DemConfigC), C.POINTER(_abi.DemParticlesIn), C.c_int]),
         "oracle_destroy": (None, [H]),
+        "oracle_create_tables": (H, [C.POINTER(_abi.DemConfigC), C.POINTER(_abi.DemParticlesIn),
+                                     C.POINTER(_abi.DemTables), C.c_int]),
+        "oracle_get_wall_shear": (C.c_int, [H, C.c_int, C.POINTER(C.c_double)]),
+        "oracle_set_wall_shear": (C.c_int, [H, C.c_int, C.POINTER(C.c_double)]),
         "oracle_set_threads": (None, [H, C.c_int]),
         "oracle_max_threads": (C.c_int, []),
         "oracle_init_bonds": (C.c_int, [H]),
@@ -80,7 +84,7 @@ def _chk(rc: int, where: str) -> None:
 class OracleScene:
     """One scene on the CPU oracle; `threads` = 1 is the serial mode."""
 
-    def __init__(self, cfg, particles, threads: int = 1):
+    def __init__(self, cfg, particles, threads: int = 1, tables=None):
         self.lib = load()
         self.n = particles.n
         self._cfg = cfg.to_c()
@@ -94,7 +98,12 @@ class OracleScene:
         pin = _abi.DemParticlesIn(self.n, ptr(ids, C.c_int32), ptr(gid, C.c_int32),
                                   ptr(vol, C.c_double), ptr(mass, C.c_double),
                                   ptr(pos, C.c_double), ptr(vel, C.c_double))
-        self.h = self.lib.oracle_create(C.byref(self._cfg), C.byref(pin), int(threads))
+        if tables is not None:
+            tc, self._tables_keep = tables.to_c()
+            self.h = self.lib.oracle_create_tables(C.byref(self._cfg), C.byref(pin), C.byref(tc),
+                                                   int(threads))
+        else:
+            self.h = self.lib.oracle_create(C.byref(self._cfg), C.byref(pin), int(threads))
         if not self.h:
             raise RuntimeError("oracle_create failed")
 
@@ -149,6 +158,17 @@ class OracleScene:
         arrs = [f(pos, 3), f(vel, 3), f(omega, 3), f(quat, 4), None, None, f(wall_shear, 3)]
         st = _abi.DemParticleState(n, *(None if a is None else a.ctypes.data for a in arrs))
         self.lib.oracle_set_particles(self.h, C.byref(st))
+
+    def wall_shear(self, wall: int) -> np.ndarray:
+        out = np.empty((self.n, 3))
+        _chk(self.lib.oracle_get_wall_shear(self.h, int(wall), ptr(out, C.c_double)),
+             "oracle_get_wall_shear")
+        return out
+
+    def set_wall_shear(self, wall: int, shear) -> None:
+        a = np.ascontiguousarray(shear, np.float64).reshape(self.n, 3)
+        _chk(self.lib.oracle_set_wall_shear(self.h, int(wall), ptr(a, C.c_double)),
+             "oracle_set_wall_shear")
 
     def contacts(self) -> dict:
         cnt = C.c_int64()

@@ -12,6 +12,7 @@ from .executor import (GlobalData, StateBuffers, initialize, load_particles, sav
                        solve)
 from .p4io import compare_p4c, compare_p4p, read_p4c, read_p4p
 from .scenes import ParticleInput, bonded_cube, granular_pour
+from .tables import Material, Surface, Tables, Wall
 
 DEMConfigDefault = DEMConfig
 
@@ -19,5 +20,5 @@ __all__ = [
     "Arena", "DEMConfig", "DEMConfigDefault", "GlobalData", "StateBuffers", "initialize",
     "simulate", "solve",
     "load_particles", "save_single", "read_p4p", "read_p4c", "compare_p4p", "compare_p4c",
-    "ParticleInput", "bonded_cube", "granular_pour",
+    "ParticleInput", "bonded_cube", "granular_pour", "Material", "Surface", "Wall", "Tables",
 ]

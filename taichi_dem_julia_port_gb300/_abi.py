@@ -98,6 +98,28 @@ class DemDerived(C.Structure):
                 ("material_density", C.c_double), ("contact_capacity", C.c_int64)]
 
 
+class DemMaterial(C.Structure):
+    _fields_ = [("density", C.c_double), ("elastic_modulus", C.c_double),
+                ("poisson_ratio", C.c_double)]
+
+
+class DemSurface(C.Structure):
+    _fields_ = [(k, C.c_double) for k in (
+        "friction", "restitution", "rolling_resistance", "bond_radius_ratio",
+        "bond_elastic_modulus", "bond_poisson_ratio", "bond_compressive_strength",
+        "bond_tensile_strength", "bond_shear_strength")]
+
+
+class DemWall(C.Structure):
+    _fields_ = [("normal", _D3), ("distance", C.c_double), ("material", C.c_int64)]
+
+
+class DemTables(C.Structure):
+    _fields_ = [("n_materials", C.c_int64), ("materials", C.POINTER(DemMaterial)),
+                ("surfaces", C.POINTER(DemSurface)), ("n_walls", C.c_int64),
+                ("walls", C.POINTER(DemWall)), ("grain_material", C.POINTER(C.c_int32))]
+
+
 class DemStats(C.Structure):
     _fields_ = [("n_particles", C.c_int64), ("steps_done", C.c_int64), ("contacts", C.c_int64),
                 ("bonded", C.c_int64), ("bonds_broken", C.c_int64), ("contacts_ended", C.c_int64),
@@ -148,6 +170,10 @@ _PH = C.POINTER(C.c_void_p)
 ENTRY_POINTS = {
     "dem_set_device": (C.c_int, [C.c_int]),
     "dem_create": (C.c_int, [C.POINTER(DemConfigC), C.POINTER(DemParticlesIn), _PH]),
+    "dem_create_tables": (C.c_int, [C.POINTER(DemConfigC), C.POINTER(DemParticlesIn),
+                                    C.POINTER(DemTables), _PH]),
+    "dem_get_wall_shear": (C.c_int, [_H, C.c_int32, C.c_void_p]),
+    "dem_set_wall_shear": (C.c_int, [_H, C.c_int32, C.c_void_p]),
     "dem_destroy": (C.c_int, [_H]),
     "dem_init_bonds": (C.c_int, [_H]),
     "dem_step": (C.c_int, [_H, C.c_int64]),

@@ -349,6 +349,8 @@ __global__ void k_fill_i32(int32_t* a, int64_t n, int32_t v) {
 
 struct DemHandle {
     bool multi = false;
+    bool tab = false;  // material / wall tables (dem_create_tables)
+    int nwall = 1;     // wall-shear columns per slot
     int device = 0;
     int sm_count = 0;
     int n_cap = 0, c_cap = 0, s_cap = 0;
@@ -428,8 +430,11 @@ int allocate(DemHandle* h) {
     double** dbl[] = {&d.px, &d.py, &d.pz, &d.vx, &d.vy, &d.vz, &d.wx, &d.wy, &d.wz,
                       &d.qw, &d.qx, &d.qy, &d.qz, &d.m, &d.inv_m, &d.r, &d.r0, &d.inv_inertia,
                       &d.b_invA, &d.b_rbI, &d.b_EA, &d.b_EI, &d.b_phic,
-                      &d.fx, &d.fy, &d.fz, &d.tx, &d.ty, &d.tz, &d.wsx, &d.wsy, &d.wsz};
+                      &d.fx, &d.fy, &d.fz, &d.tx, &d.ty, &d.tz};
     for (double** a : dbl) TRY(dalloc(h, a, n));
+    // wall shear: one column per wall, wall w of slot i at [w * n + i]
+    for (double** a : {&d.wsx, &d.wsy, &d.wsz}) TRY(dalloc(h, a, n * (size_t)std::max(h->nwall, 1)));
+    h->p.wstride = (int)n;
     TRY(dalloc(h, &d.cellinfo, n));
     TRY(dalloc(h, &d.scell, n));
     TRY(dalloc(h, &d.srow, n));
@@ -572,6 +577,110 @@ int upload_scene(DemHandle* h, const SceneArrays& A, int64_t p0) {
         CU(cudaMemsetAsync(z + p0, 0, n * sizeof(double), h->stream));
     // the host vectors above must outlive the copies
     CU(cudaStreamSynchronize(h->stream));
+    return DEM_OK;
+}
+
+// The device form of a scene's material, surface and wall tables
+// (dem_create_tables), checked: counts within the limits, every material
+// index in range, finite constants.
+int build_tables(const DemConfigC& cfg, const DemTables& t, int64_t n, MatTables& M,
+                 std::vector<uint8_t>& mid) {
+    g_invalid[0] = 0;
+    auto bad = [](const char* what) {
+        std::snprintf(g_invalid, sizeof(g_invalid), "tables: %s", what);
+        return DEM_ERR_INVALID;
+    };
+    if (t.n_materials < 1 || t.n_materials > kMaxMaterials) return bad("n_materials not in 1..8");
+    if (t.n_walls < 0 || t.n_walls > kMaxWalls) return bad("n_walls not in 0..8");
+    if (!t.materials || !t.surfaces || (t.n_walls && !t.walls) || (n && !t.grain_material))
+        return bad("missing array");
+    const int nm = (int)t.n_materials;
+    M.nmat = nm;
+    M.nwall = (int)t.n_walls;
+    for (int a = 0; a < nm; ++a) {
+        const DemMaterial& m = t.materials[a];
+        if (!(m.elastic_modulus > 0) || !std::isfinite(m.poisson_ratio)) return bad("material constants");
+    }
+    for (int a = 0; a < nm; ++a)
+        for (int b = 0; b < nm; ++b) {
+            const DemSurface& S = t.surfaces[a * nm + b];
+            const DemMaterial &ma = t.materials[a], &mb = t.materials[b];
+            const Hertz hc = hertz_constants(ma.elastic_modulus, ma.poisson_ratio,
+                                             mb.elastic_modulus, mb.poisson_ratio, S.restitution);
+            PairConst& P = M.pair[a * nm + b];
+            P.mu = S.friction;
+            P.Ys = hc.Ys;
+            P.Gs = hc.Gs;
+            P.cgn = hc.cgn;
+            P.cgt = hc.cgt;
+            P.ratio = S.bond_radius_ratio;
+            P.E = S.bond_elastic_modulus;
+            P.nu = S.bond_poisson_ratio;
+            P.inv1pnu = 1.0 / (1.0 + S.bond_poisson_ratio);
+            P.sc = S.bond_compressive_strength;
+            P.st = S.bond_tensile_strength;
+            P.ss = S.bond_shear_strength;
+        }
+    for (int w = 0; w < M.nwall; ++w) {
+        const DemWall& W = t.walls[w];
+        if (W.material < 0 || W.material >= nm) return bad("wall material out of range");
+        WallConst& C = M.wall[w];
+        double c0 = -W.distance;
+        for (int c = 0; c < 3; ++c) {
+            C.wn[c] = W.normal[c];
+            C.f_wn[c] = (float)W.normal[c];
+            c0 += W.normal[c] * cfg.domain_min[c];
+        }
+        C.wd = W.distance;
+        C.f_wc0 = (float)c0;
+        const M3 R = wall_frame(W.normal, cfg.tolerance);
+        const M3 Ri = inverse3(R);
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                C.wR[3 * r + c] = R.a[r][c];
+                C.wRinv[3 * r + c] = Ri.a[r][c];
+            }
+        const DemMaterial& mw = t.materials[W.material];
+        for (int a = 0; a < nm; ++a) {
+            const DemSurface& S = t.surfaces[a * nm + W.material];
+            const DemMaterial& ma = t.materials[a];
+            const Hertz hc = hertz_constants(ma.elastic_modulus, ma.poisson_ratio,
+                                             mw.elastic_modulus, mw.poisson_ratio, S.restitution);
+            C.mu[a] = S.friction;
+            C.Ys[a] = hc.Ys;
+            C.Gs[a] = hc.Gs;
+            C.cgn[a] = hc.cgn;
+            C.cgt[a] = hc.cgt;
+        }
+    }
+    mid.resize((size_t)n);
+    for (int64_t i = 0; i < n; ++i) {
+        const int32_t g = t.grain_material[i];
+        if (g < 0 || g >= nm) {
+            std::snprintf(g_invalid, sizeof(g_invalid), "tables: grain %lld material %d out of range",
+                          (long long)i, (int)g);
+            return DEM_ERR_INVALID;
+        }
+        mid[(size_t)i] = (uint8_t)g;
+    }
+    return DEM_OK;
+}
+
+int upload_tables(DemHandle* h, const MatTables& M, const std::vector<uint8_t>& mid) {
+    MatTables* dm = nullptr;
+    uint8_t* dmid = nullptr;
+    TRY(dalloc(h, &dm, 1));
+    TRY(dalloc(h, &dmid, std::max<size_t>(mid.size(), 1)));
+    CU(cudaMemcpyAsync(dm, &M, sizeof(MatTables), cudaMemcpyHostToDevice, h->stream));
+    if (!mid.empty())
+        CU(cudaMemcpyAsync(dmid, mid.data(), mid.size(), cudaMemcpyHostToDevice, h->stream));
+    h->d.mt = dm;
+    h->d.mid = dmid;
+    // every wall's shear history starts at zero
+    const size_t cols = (size_t)h->nwall * (size_t)h->n_cap;
+    for (double* z : {h->d.wsx, h->d.wsy, h->d.wsz})
+        CU(cudaMemsetAsync(z, 0, cols * sizeof(double), h->stream));
+    CU(cudaStreamSynchronize(h->stream));  // M and mid are the caller's stack and vector
     return DEM_OK;
 }
 
@@ -1109,16 +1218,23 @@ int dem_set_device(int device) {
     return DEM_OK;
 }
 
-int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out) {
+int create_single(const DemConfigC* cfg, const DemParticlesIn* pin, const DemTables* tables,
+                  DemHandle** out) {
     if (!out) return DEM_ERR_INVALID;
     *out = nullptr;
     SceneHost S;
     SceneArrays A;
     TRY(prepare_scene(cfg, pin, 1.0, S, A));
     if (S.der.contact_capacity > 0x7fffffff) return DEM_ERR_CAPACITY;
+    MatTables M{};
+    std::vector<uint8_t> mid;
+    if (tables) TRY(build_tables(*cfg, *tables, pin->n, M, mid));
     int dev = 0, sms = 0;
     TRY(check_device(&dev, &sms));
     DemHandle* h = new DemHandle();
+    h->tab = tables != nullptr;
+    h->nwall = tables ? std::max<int>(M.nwall, 1) : 1;
+    h->p.tab = h->tab ? 1 : 0;
     h->device = dev;
     h->sm_count = sms;
     h->multi = false;
@@ -1145,6 +1261,7 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
     h->scenes.push_back(S);
     int rc = init_handle(h);
     if (rc == DEM_OK) rc = upload_scene(h, A, 0);
+    if (rc == DEM_OK && h->tab) rc = upload_tables(h, M, mid);
     if (rc == DEM_OK) rc = flag_search(h, 0);
     if (rc == DEM_OK) {
         launch_refresh_pos32(h->d, h->p, false, 0, h->n_cap, -1, h->stream);
@@ -1157,6 +1274,16 @@ int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out
     }
     *out = h;
     return DEM_OK;
+}
+
+int dem_create(const DemConfigC* cfg, const DemParticlesIn* pin, DemHandle** out) {
+    return create_single(cfg, pin, nullptr, out);
+}
+
+int dem_create_tables(const DemConfigC* cfg, const DemParticlesIn* pin, const DemTables* tables,
+                      DemHandle** out) {
+    if (!tables) return DEM_ERR_INVALID;
+    return create_single(cfg, pin, tables, out);
 }
 
 int dem_arena_create(const DemArenaConfig* cfg, DemHandle** out) {
@@ -1376,6 +1503,11 @@ int dem_destroy(DemHandle* h) {
 
 int dem_set_precision(DemHandle* h, int mode) {
     if (!h || (mode != DEM_FP64 && mode != DEM_FP32_FORCE)) return DEM_ERR_INVALID;
+    if (h->tab && mode != DEM_FP64) {
+        std::snprintf(g_invalid, sizeof(g_invalid),
+                      "a handle with material and wall tables computes in FP64 only");
+        return DEM_ERR_INVALID;
+    }
     h->p.precision = mode;
     return DEM_OK;
 }
@@ -1575,6 +1707,26 @@ int dem_scene_get_contacts(DemHandle* h, int32_t s, DemContacts* out, int64_t ca
 
 int dem_get_contacts(DemHandle* h, DemContacts* out, int64_t cap, int64_t* n_out) {
     return dem_scene_get_contacts(h, 0, out, cap, n_out);
+}
+
+int dem_get_wall_shear(DemHandle* h, int32_t wall, double* shear) {
+    if (!h || h->multi || !shear || wall < 0 || wall >= h->nwall) return DEM_ERR_INVALID;
+    const size_t o = (size_t)wall * (size_t)h->n_cap;
+    const int k[] = {3};
+    double* const host[] = {shear};
+    double* const cols[][4] = {{h->d.wsx + o, h->d.wsy + o, h->d.wsz + o}};
+    int err = 0;
+    TRY(exchange(h, 0, h->n_cap, k, host, cols, 1, false, &err));
+    return error_code(err);
+}
+
+int dem_set_wall_shear(DemHandle* h, int32_t wall, const double* shear) {
+    if (!h || h->multi || !shear || wall < 0 || wall >= h->nwall) return DEM_ERR_INVALID;
+    const size_t o = (size_t)wall * (size_t)h->n_cap;
+    const int k[] = {3};
+    double* const host[] = {const_cast<double*>(shear)};
+    double* const cols[][4] = {{h->d.wsx + o, h->d.wsy + o, h->d.wsz + o}};
+    return exchange(h, 0, h->n_cap, k, host, cols, 1, true);
 }
 
 int dem_scene_get_io_contacts(DemHandle* h, int32_t s, DemIOContact* out, int64_t cap,

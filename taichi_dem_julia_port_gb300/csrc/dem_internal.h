@@ -97,6 +97,32 @@ struct SceneParams {
     float f_wn[3], f_wc0;   // FP32 wall normal and n·domain_min - wall_distance (wall screen)
 };
 
+// Material, surface and wall tables of a scene built with dem_create_tables
+// (the reference's GlobalData.materials / surfaces / walls, src/types.jl:9-27,
+// 58-62, which its `solve` fills with one particle material, one wall
+// material and one wall, src/executor.jl:282-315).  Indices are 0-based
+// (the reference's mid - 1).  Pair constants are surfaces[a, b] with
+// materials a and b; wall constants hold, per particle material a, the
+// particle-wall constants of surfaces[a, wall material].
+constexpr int kMaxMaterials = 8;
+constexpr int kMaxWalls = 8;
+struct PairConst {
+    double mu, Ys, Gs, cgn, cgt;              // Hertz-Mindlin: μ, Y*, G*, γ coefficients
+    double ratio, E, nu, inv1pnu, sc, st, ss;  // EBPM: ρ, E, ν, 1/(1+ν), σc, σt, σs
+};
+struct WallConst {
+    double wn[3], wd;
+    double wR[9], wRinv[9];  // contact frame of the wall and its inverse
+    float f_wn[3], f_wc0;    // FP32 normal and n·domain_min - distance (the wall screen)
+    double mu[kMaxMaterials], Ys[kMaxMaterials], Gs[kMaxMaterials];
+    double cgn[kMaxMaterials], cgt[kMaxMaterials];
+};
+struct MatTables {
+    int nmat, nwall;
+    PairConst pair[kMaxMaterials * kMaxMaterials];  // [a * nmat + b]
+    WallConst wall[kMaxWalls];
+};
+
 struct SceneCounters {
     unsigned long long broken, ended, created, warn_gap, warn_damp;
     unsigned long long searches;  // steps that ran the full pair search
@@ -131,7 +157,10 @@ struct DemDev {
     float4* bk32;                  // FP32 (b_phic, b_EI, b_EA, b_invA)
     float4* rm32;                  // FP32 (b_rbI, m, r, 0)
     double *fx, *fy, *fz, *tx, *ty, *tz;  // totals of the last step
-    double *wsx, *wsy, *wsz;              // wall shear history (one wall)
+    double *wsx, *wsy, *wsz;              // wall shear history: wall w of slot i at
+                                          // [w * DemParams::wstride + i]
+    const MatTables* mt;                  // tables of a dem_create_tables handle, else null
+    const uint8_t* mid;                   // its grains' material indices, else null
     int32_t* scene_of;                    // arena: scene of each slot (-1 free); null otherwise
     // neighbour lists: kvl partners per slot, their count, the position at the
     // last full search and the current position (FP32, relative to the
@@ -188,6 +217,8 @@ struct DemParams {
     int dep;        // a step's kernels: 0 ordinary launches, 1 programmatic dependent
                     // launches, 2 the same with the successor scheduled early
     int debug_enum; // 1: the pair search counts its candidate pairs (never in a graph)
+    int tab;        // 1: a single scene with material / wall tables (DemDev::mt, mid)
+    int wstride;    // slots per wall-shear column
     SceneParams s0; // the scene of a single-scene handle
 };
 

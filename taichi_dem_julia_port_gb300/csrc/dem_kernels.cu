@@ -40,6 +40,7 @@ constexpr int kScanBlock = 1024;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanBlock * kScanItems;
 constexpr unsigned long long kSpinLimit = 1ull << 24;
+constexpr double kPi = 3.141592653589793;  // Julia's π rounded to binary64
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
@@ -1229,20 +1230,31 @@ __device__ __forceinline__ Vec3<T> from_d(Vec3<double> v) {
 // A NaN operand makes a comparison false, as in the reference.
 __device__ __forceinline__ bool bond_breaks(const Vec3<double>& F, const Vec3<double>& ti,
                                             const Vec3<double>& tj, double invA, double rbI,
-                                            const SceneParams& p) {
+                                            double b_sc, double b_st, double b_ss) {
     const double ai = ti.y * ti.y + ti.z * ti.z, aj = tj.y * tj.y + tj.z * tj.z;
     const bool nan_a = isnan(ai) || isnan(aj);
     const double amax = fmax(ai, aj), amin = fmin(ai, aj);
     const double fa = F.x * invA, k2 = rbI * rbI;
-    const double Rc = p.b_sc - fa;     // σc >= σc₀  <=>  rbI·sqrt(amax) >= Rc
-    const double Rt = -(p.b_st + fa);  // σt >= σt₀  <=>  rbI·sqrt(amin) <= Rt
-    const double Rs = p.b_ss - fabs(ti.x) * (0.5 * rbI);  // σs >= σs₀ <=> 4/3·invA·sqrt(b) >= Rs
+    const double Rc = b_sc - fa;     // σc >= σc₀  <=>  rbI·sqrt(amax) >= Rc
+    const double Rt = -(b_st + fa);  // σt >= σt₀  <=>  rbI·sqrt(amin) <= Rt
+    const double Rs = b_ss - fabs(ti.x) * (0.5 * rbI);  // σs >= σs₀ <=> 4/3·invA·sqrt(b) >= Rs
     const double b = F.y * F.y + F.z * F.z;
     const double ks = (4.0 / 3.0) * invA;
     const bool comp = !nan_a && (Rc <= 0.0 || amax * k2 >= Rc * Rc);
     const bool tens = !nan_a && Rt >= 0.0 && amin * k2 <= Rt * Rt;
     const bool shear = !isnan(b) && !isnan(Rs) && (Rs <= 0.0 || b * (ks * ks) >= Rs * Rs);
     return comp || tens || shear;
+}
+__device__ __forceinline__ bool bond_breaks(const Vec3<double>& F, const Vec3<double>& ti,
+                                            const Vec3<double>& tj, double invA, double rbI,
+                                            const SceneParams& p) {
+    return bond_breaks(F, ti, tj, invA, rbI, p.b_sc, p.b_st, p.b_ss);
+}
+// The breakage test of a bond between grains of a table scene (no FP32 screen).
+static __device__ __noinline__ bool bond_breaks_tab(const Vec3<double>& F, const Vec3<double>& ti,
+                                                    const Vec3<double>& tj, double invA,
+                                                    double rbI, const PairConst& pc) {
+    return bond_breaks(F, ti, tj, invA, rbI, pc.sc, pc.st, pc.ss);
 }
 
 // Breakage decision of bond_breaks behind an FP32 screen.  The three stresses
@@ -1520,7 +1532,10 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
 // 3EI/L/(1+ϕ) and k₋ = (k₅-k₆)/2 = EI/L; dt is folded into the stiffnesses.
 // One contact, one thread: FP64 mode (T = double) or the FP32 force mode's
 // Hertz and bond paths (T = float, via force32).
-template <typename T>
+// TAB: a scene with material and wall tables (FP64 only): the pair's
+// constants come from surfaces[midᵢ, midⱼ] and materials midᵢ, midⱼ, and the
+// bond section of rb = ρ·min(rᵢ, rⱼ) is formed here from that surface.
+template <typename T, bool TAB = false>
 __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& SP,
                                             const ContactSoA& w, const ContactSoA& o, int c,
                                             uint32_t fl, int i, int j, int sc, size_t cap) {
@@ -1529,6 +1544,8 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
         force32(d, SP, w, o, sidx, c, fl, i, j, sc, cap);
         return;
     }
+    const PairConst* pc = nullptr;
+    if constexpr (TAB) pc = &d.mt->pair[d.mid[i] * d.mt->nmat + d.mid[j]];
     const double dt = SP.dt;
     const Vec3<double> ki{d.px[i], d.py[i], d.pz[i]}, kj{d.px[j], d.py[j], d.pz[j]};
     const double ri = d.r[i], rj = d.r[j];
@@ -1548,14 +1565,34 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
         const Vec3<double> Td = rot<double>(R, {wi.x - wj.x, wi.y - wj.y, wi.z - wj.z});
         const Vec3<T> D = from_d<T>(Dd), Sv = from_d<T>(Ts), Q = from_d<T>(Td);
         const int small = !less_nonneg(rj, ri) ? i : j;  // rb = ρ·min(rᵢ, rⱼ); radii > 0
+        // bond section (src/kernels.jl:178-184): per particle for the scene's
+        // one surface, per pair from the surface table
+        double b_phic, b_EI, b_EA, b_1pnu, b_invA = 0.0, b_rbI = 0.0;
+        if constexpr (TAB) {
+            const double rb = __dmul_rn(pc->ratio, d.r[small]);
+            const double rb2 = __dmul_rn(rb, rb);
+            const double Ab = __dmul_rn(rb2, kPi);
+            const double Ib = __dmul_rn(__dmul_rn(rb2, rb2), kPi / 4.0);
+            b_EA = __dmul_rn(pc->E, Ab);
+            b_EI = __dmul_rn(pc->E, Ib);
+            b_phic = __dmul_rn(__dmul_rn(20.0 / 3.0, __dadd_rn(1.0, pc->nu)), rb2);
+            b_1pnu = pc->inv1pnu;
+            b_invA = __ddiv_rn(1.0, Ab);
+            b_rbI = __ddiv_rn(rb, Ib);
+        } else {
+            b_phic = d.b_phic[small];
+            b_EI = d.b_EI[small];
+            b_EA = d.b_EA[small];
+            b_1pnu = SP.b_inv1pnu;
+        }
         const T tinvL = (T)invL, tdt = (T)dt;
-        const T phi = (T)d.b_phic[small] * tinvL * tinvL;
+        const T phi = (T)b_phic * tinvL * tinvL;
         const T iphi = rcp_nr((T)1.0 + phi);  // 1/(1 + ϕ)
-        const T EILdt = (T)d.b_EI[small] * tinvL * tdt;  // EI/L·dt
-        const T k1 = (T)d.b_EA[small] * tinvL * tdt;
+        const T EILdt = (T)b_EI * tinvL * tdt;  // EI/L·dt
+        const T k1 = (T)b_EA * tinvL * tdt;
         const T k3 = (T)6.0 * EILdt * tinvL * iphi;
         const T k2 = (T)2.0 * k3 * tinvL;
-        const T k4 = EILdt * (T)SP.b_inv1pnu;
+        const T k4 = EILdt * (T)b_1pnu;
         const T kp = (T)3.0 * EILdt * iphi;
         const T km = EILdt;
         const T dFx = k1 * D.x, dFy = k2 * D.y + k3 * Sv.z, dFz = k2 * D.z - k3 * Sv.y;
@@ -1570,7 +1607,10 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
         ti = {ti.x + (double)dtix, ti.y + (double)dtiy, ti.z + (double)dtiz};
         tj = {tj.x + (double)dtjx, tj.y + (double)dtjy, tj.z + (double)dtjz};
         // breakage test, FP64 (src/kernels.jl:208-222)
-        if (bond_breaks_fp64(Fi, ti, tj, d, small, SP)) {
+        bool broken;
+        if constexpr (TAB) broken = bond_breaks_tab(Fi, ti, tj, b_invA, b_rbI, *pc);
+        else broken = bond_breaks_fp64(Fi, ti, tj, d, small, SP);
+        if (broken) {
             w.fl[c] = 0u;  // contact_active and contact_bonded bits cleared
             atomicAdd(&d.sctr[sc].broken, 1ull);
             fig = {(T)0, (T)0, (T)0};
@@ -1604,11 +1644,14 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
         const T ms = tmi * tmj / (tmi + tmj);
         const T tgap = (T)gap;
         const T sq = sqrt(Rs * (T)fabs(gap));
-        const T kn = (T)(4.0 / 3.0 * SP.pp_Ys) * sq;
-        const T kt = (T)(8.0 * SP.pp_Gs) * sq;
+        const double pYs = TAB ? pc->Ys : SP.pp_Ys, pGs = TAB ? pc->Gs : SP.pp_Gs;
+        const double pcgn = TAB ? pc->cgn : SP.pp_cgn, pcgt = TAB ? pc->cgt : SP.pp_cgt;
+        const double pmu = TAB ? pc->mu : SP.pp_mu;
+        const T kn = (T)(4.0 / 3.0 * pYs) * sq;
+        const T kt = (T)(8.0 * pGs) * sq;
         const T root = sqrt(ms * sq);
-        const T gn = (T)SP.pp_cgn * root;
-        const T gt = (T)SP.pp_cgt * root;
+        const T gn = (T)pcgn * root;
+        const T gt = (T)pcgt * root;
         if (gn < (T)0 || gt < (T)0)
             atomicAdd(&d.sctr[sc].warn_damp, (unsigned long long)((gn < (T)0) + (gt < (T)0)));
         Vec3<double> s = sidx >= 0 ? ld3(o.f, CS, sidx) : Vec3<double>{0.0, 0.0, 0.0};
@@ -1616,7 +1659,7 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
         const T F1 = -kn * tgap - gn * vc.x;
         const Vec3<T> Ft{-kt * (T)s.x, -kt * (T)s.y, -kt * (T)s.z};
         const T nFt = sqrt(Ft.x * Ft.x + Ft.y * Ft.y + Ft.z * Ft.z);
-        const T muF1 = (T)SP.pp_mu * F1;
+        const T muF1 = (T)pmu * F1;
         T F2, F3;
         if (nFt >= muF1) {
             const T ratio = muF1 / nFt;
@@ -1644,7 +1687,7 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
     d.contrib[8 * cap + c] = (double)mj.z;
 }
 
-template <typename T, bool MULTI>
+template <typename T, bool MULTI, bool TAB = false>
 __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, int nxt) {
     const int C = min((int)d.ctr->row_alloc[nxt], p.cap);
     const ContactSoA w = d.c[nxt];
@@ -1659,7 +1702,7 @@ __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, 
         // the contact in its partner's incoming list (the integrator's gather
         // sorts the list by owner, so the order of registration is free)
         add_incoming_entry(d, p, j, c, i);
-        contact_one<T>(d, scene_rec<MULTI>(d, p, sc), w, o, c, fl, i, j, sc, cap);
+        contact_one<T, TAB>(d, scene_rec<MULTI>(d, p, sc), w, o, c, fl, i, j, sc, cap);
     }
 }
 
@@ -1674,6 +1717,11 @@ template <typename T, bool MULTI>
 __global__ void __launch_bounds__(kThreads, 4) k_force4(DemDev d, DemParams p, int nxt) {
     dep_begin(p.dep == 2);
     force_body<T, MULTI>(d, p, nxt);
+}
+// a single scene with material and wall tables (FP64)
+__global__ void __launch_bounds__(kThreads) k_force_tab(DemDev d, DemParams p, int nxt) {
+    dep_begin(p.dep == 2);
+    force_body<double, false, true>(d, p, nxt);
 }
 
 // ---------------------------------------------------------------------------
@@ -1821,7 +1869,99 @@ __device__ __forceinline__ bool left_skin(const SceneParams& S, float fx, float 
     return !(lim > 0.0f) || !(ex * ex + ey * ey + ez * ez <= lim * lim);
 }
 
-template <bool MULTI, bool F32>
+// One wall's constants as the wall contact reads them.
+struct WallK {
+    const double* wn;
+    double wd;
+    const double* wR;
+    const double* wRinv;
+    const float* f_wn;
+    float f_wc0;
+    double mu, Ys, Gs, cgn, cgt;
+};
+// resolve_wall! for one particle and one wall (src/kernels.jl:317-426): adds
+// the wall's force and moment to F, M and updates the wall contact's shear
+// history (*sx, *sy, *sz; zero when not touching).  An FP32 screen on the
+// step's starting position (pos32, within 2^-24 of the FP64 one per
+// coordinate) skips the exact test when |n·x - d| exceeds r by a margin that
+// covers its rounding.
+__device__ __forceinline__ void wall_contact(const DemDev& d, int sc, const WallK& W, double dt,
+                                             float4 p32, float r32, double x, double y, double z,
+                                             double vx, double vy, double vz, double wx, double wy,
+                                             double wz, double r, double m, double* wsx,
+                                             double* wsy, double* wsz, double F[3], double M[3]) {
+    bool wall_near;
+    {
+        const float4 q = p32;
+        const float Lf = q.x * W.f_wn[0] + q.y * W.f_wn[1] + q.z * W.f_wn[2] + W.f_wc0;
+        const float rf = r32;
+        const float mg = (fabsf(q.x) + fabsf(q.y) + fabsf(q.z) + fabsf(W.f_wc0) + rf) * 0x1p-20f;
+        wall_near = !(fabsf(Lf) > rf + mg);
+    }
+    if (!wall_near) {
+        *wsx = 0.0;
+        *wsy = 0.0;
+        *wsz = 0.0;
+        return;
+    }
+    const double dotkn = __dadd_rn(__dadd_rn(__dmul_rn(x, W.wn[0]), __dmul_rn(y, W.wn[1])),
+                                   __dmul_rn(z, W.wn[2]));
+    const double L = __dsub_rn(dotkn, W.wd);
+    if (fabs(L) < r) {
+        const double gap = fabs(L) - r;
+        const double dn = fabs(gap);
+        const double lsc = (fabs(L) + dn / 2.0) / fabs(L);
+        const double kix = -L * W.wn[0] * lsc, kiy = -L * W.wn[1] * lsc, kiz = -L * W.wn[2] * lsc;
+        const double vcix = wy * kiz - wz * kiy + vx, vciy = wz * kix - wx * kiz + vy,
+                     vciz = wx * kiy - wy * kix + vz;
+        const double* Rw = W.wR;
+        const double vcx = -(Rw[0] * vcix + Rw[1] * vciy + Rw[2] * vciz);
+        const double vcy = -(Rw[3] * vcix + Rw[4] * vciy + Rw[5] * vciz);
+        const double vcz = -(Rw[6] * vcix + Rw[7] * vciy + Rw[8] * vciz);
+        const double sq = sqrt(r * dn);
+        const double kn = 4.0 / 3.0 * W.Ys * sq;
+        const double kt = 8.0 * W.Gs * sq;
+        const double root = sqrt(m * sq);
+        const double gn = W.cgn * root;
+        const double gt = W.cgt * root;
+        if (gn < 0) atomicAdd(&d.sctr[sc].warn_damp, 1ull);
+        if (gt < 0) atomicAdd(&d.sctr[sc].warn_damp, 1ull);
+        double sx = *wsx + vcx * 0.0, sy = *wsy + vcy * dt, sz = *wsz + vcz * dt;
+        const double F1 = -kn * gap - gn * vcx;
+        const double Ftx = -kt * sx, Fty = -kt * sy, Ftz = -kt * sz;
+        const double nFt = sqrt(Ftx * Ftx + Fty * Fty + Ftz * Ftz);
+        double F2, F3;
+        if (nFt >= W.mu * F1) {
+            const double ratio = W.mu * F1 / nFt;
+            F2 = ratio * Fty;
+            F3 = ratio * Ftz;
+            sy = F2 / kt;
+            sz = F3 / kt;
+        } else {
+            F2 = Fty - gt * vcy;
+            F3 = Ftz - gt * vcz;
+        }
+        const double* Ri = W.wRinv;
+        const double gx = -(Ri[0] * F1 + Ri[1] * F2 + Ri[2] * F3);
+        const double gy = -(Ri[3] * F1 + Ri[4] * F2 + Ri[5] * F3);
+        const double gz = -(Ri[6] * F1 + Ri[7] * F2 + Ri[8] * F3);
+        F[0] += gx;
+        F[1] += gy;
+        F[2] += gz;
+        M[0] += kiy * gz - kiz * gy;
+        M[1] += kiz * gx - kix * gz;
+        M[2] += kix * gy - kiy * gx;
+        *wsx = sx;
+        *wsy = sy;
+        *wsz = sz;
+    } else {
+        *wsx = 0.0;
+        *wsy = 0.0;
+        *wsz = 0.0;
+    }
+}
+
+template <bool MULTI, bool F32, bool TAB = false>
 __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams& p, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nxt = cur ^ 1;
@@ -1861,77 +2001,25 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
     }
     d.in_cnt[i] = 0;
     const double dt = S.dt;
-    // resolve_wall!, one wall.  An FP32 screen on the step's starting position
-    // (pos32, within 2^-24 of the FP64 one per coordinate) skips the exact
-    // test when |n·x - d| exceeds r by a margin that covers its rounding.
-    bool wall_near = true;
-    if (S.has_wall) {
-        const float4 q = p32;
-        const float Lf = q.x * S.f_wn[0] + q.y * S.f_wn[1] + q.z * S.f_wn[2] + S.f_wc0;
-        const float rf = r32;
-        const float mg = (fabsf(q.x) + fabsf(q.y) + fabsf(q.z) + fabsf(S.f_wc0) + rf) * 0x1p-20f;
-        wall_near = !(fabsf(Lf) > rf + mg);
-    }
-    if (S.has_wall && !wall_near) {
-        d.wsx[i] = 0.0;
-        d.wsy[i] = 0.0;
-        d.wsz[i] = 0.0;
-    } else if (S.has_wall) {
-        const double dotkn = __dadd_rn(__dadd_rn(__dmul_rn(x, S.wn[0]), __dmul_rn(y, S.wn[1])),
-                                       __dmul_rn(z, S.wn[2]));
-        const double L = __dsub_rn(dotkn, S.wd);
-        if (fabs(L) < r) {
-            const double gap = fabs(L) - r;
-            const double dn = fabs(gap);
-            const double lsc = (fabs(L) + dn / 2.0) / fabs(L);
-            const double kix = -L * S.wn[0] * lsc, kiy = -L * S.wn[1] * lsc, kiz = -L * S.wn[2] * lsc;
-            const double vcix = wy * kiz - wz * kiy + vx, vciy = wz * kix - wx * kiz + vy,
-                         vciz = wx * kiy - wy * kix + vz;
-            const double* Rw = S.wR;
-            const double vcx = -(Rw[0] * vcix + Rw[1] * vciy + Rw[2] * vciz);
-            const double vcy = -(Rw[3] * vcix + Rw[4] * vciy + Rw[5] * vciz);
-            const double vcz = -(Rw[6] * vcix + Rw[7] * vciy + Rw[8] * vciz);
-            const double sq = sqrt(r * dn);
-            const double kn = 4.0 / 3.0 * S.pw_Ys * sq;
-            const double kt = 8.0 * S.pw_Gs * sq;
-            const double root = sqrt(m * sq);
-            const double gn = S.pw_cgn * root;
-            const double gt = S.pw_cgt * root;
-            if (gn < 0) atomicAdd(&d.sctr[sc].warn_damp, 1ull);
-            if (gt < 0) atomicAdd(&d.sctr[sc].warn_damp, 1ull);
-            double sx = d.wsx[i] + vcx * 0.0, sy = d.wsy[i] + vcy * dt, sz = d.wsz[i] + vcz * dt;
-            const double F1 = -kn * gap - gn * vcx;
-            const double Ftx = -kt * sx, Fty = -kt * sy, Ftz = -kt * sz;
-            const double nFt = sqrt(Ftx * Ftx + Fty * Fty + Ftz * Ftz);
-            double F2, F3;
-            if (nFt >= S.pw_mu * F1) {
-                const double ratio = S.pw_mu * F1 / nFt;
-                F2 = ratio * Fty;
-                F3 = ratio * Ftz;
-                sy = F2 / kt;
-                sz = F3 / kt;
-            } else {
-                F2 = Fty - gt * vcy;
-                F3 = Ftz - gt * vcz;
-            }
-            const double* Ri = S.wRinv;
-            const double gx = -(Ri[0] * F1 + Ri[1] * F2 + Ri[2] * F3);
-            const double gy = -(Ri[3] * F1 + Ri[4] * F2 + Ri[5] * F3);
-            const double gz = -(Ri[6] * F1 + Ri[7] * F2 + Ri[8] * F3);
-            F[0] += gx;
-            F[1] += gy;
-            F[2] += gz;
-            M[0] += kiy * gz - kiz * gy;
-            M[1] += kiz * gx - kix * gz;
-            M[2] += kix * gy - kiy * gx;
-            d.wsx[i] = sx;
-            d.wsy[i] = sy;
-            d.wsz[i] = sz;
-        } else {
-            d.wsx[i] = 0.0;
-            d.wsy[i] = 0.0;
-            d.wsz[i] = 0.0;
+    // resolve_wall! (src/kernels.jl:317-426): the scene's one wall, or every
+    // wall of a table scene in order (wall j's force and moment are added
+    // after wall j-1's, as the reference's per-particle loop over j does)
+    if constexpr (TAB) {
+        const MatTables& T = *d.mt;
+        const int a = d.mid[i];
+        for (int wl = 0; wl < T.nwall; ++wl) {
+            const WallConst& W = T.wall[wl];
+            const WallK K{W.wn, W.wd, W.wR, W.wRinv, W.f_wn, W.f_wc0, W.mu[a], W.Ys[a], W.Gs[a],
+                          W.cgn[a], W.cgt[a]};
+            const size_t o = (size_t)wl * p.wstride + i;
+            wall_contact(d, sc, K, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r, m, d.wsx + o,
+                         d.wsy + o, d.wsz + o, F, M);
         }
+    } else if (S.has_wall) {
+        const WallK K{S.wn, S.wd, S.wR, S.wRinv, S.f_wn, S.f_wc0, S.pw_mu, S.pw_Ys, S.pw_Gs,
+                      S.pw_cgn, S.pw_cgt};
+        wall_contact(d, sc, K, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r, m, d.wsx + i,
+                     d.wsy + i, d.wsz + i, F, M);
     }
     // apply_body_force!  A zero gravity component adds nothing: the force sum
     // starts at +0 and never becomes -0, so F + 0·m is F.
@@ -2033,6 +2121,10 @@ template <bool MULTI, bool F32>
 __global__ void __launch_bounds__(kThreads) k_integrate(DemDev d, DemParams p, int cur) {
     dep_begin(p.dep == 2);
     integrate_body<MULTI, F32>(d, p, cur);
+}
+__global__ void __launch_bounds__(kThreads) k_integrate_tab(DemDev d, DemParams p, int cur) {
+    dep_begin(p.dep == 2);
+    integrate_body<false, false, true>(d, p, cur);
 }
 template <bool MULTI>
 __global__ void __launch_bounds__(kThreads, 3) k_integrate3(DemDev d, DemParams p, int cur) {
@@ -2232,6 +2324,8 @@ void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, cons
         else
             launch(p.dep != 0, multi ? k_force<float, true> : k_force<float, false>, grid, block, s,
                    d, p, nxt);
+    } else if (p.tab) {
+        launch(p.dep != 0, k_force_tab, grid, block, s, d, p, nxt);
     } else {
         launch(p.dep != 0, multi ? k_force<double, true> : k_force<double, false>, grid, block, s,
                d, p, nxt);
@@ -2243,7 +2337,9 @@ void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
     if (p.n == 0) return;
     const int block = clamp_block(sh.integrate_block);
     const int nb = blocks_for(p.n, block);
-    if (p.precision == 1)
+    if (p.tab)
+        launch(p.dep != 0, k_integrate_tab, nb, block, s, d, p, cur);
+    else if (p.precision == 1)
         launch(p.dep != 0, multi ? k_integrate3<true> : k_integrate3<false>, nb, block, s, d, p,
                cur);
     else

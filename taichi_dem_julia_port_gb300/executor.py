@@ -167,7 +167,7 @@ class GlobalData:
     """Device state of one scene (particles, broad phase, contacts)."""
 
     def __init__(self, cfg: DEMConfig, particles: ParticleInput, precision: str = "fp64",
-                 lib=None):
+                 lib=None, tables=None):
         self.lib = lib or _abi.load_library()
         self.cfg = cfg
         self.n = particles.n
@@ -183,8 +183,15 @@ class GlobalData:
                                   ptr(vol, C.c_double), ptr(mass, C.c_double),
                                   ptr(pos, C.c_double), ptr(vel, C.c_double))
         h = C.c_void_p()
-        check(self.lib, self.lib.dem_create(C.byref(self._cfg_c), C.byref(pin), C.byref(h)),
-              "dem_create")
+        self.tables = tables
+        if tables is not None:  # the scene's own material, surface and wall tables
+            tc, self._tables_keep = tables.to_c()
+            check(self.lib, self.lib.dem_create_tables(C.byref(self._cfg_c), C.byref(pin),
+                                                       C.byref(tc), C.byref(h)),
+                  "dem_create_tables")
+        else:
+            check(self.lib, self.lib.dem_create(C.byref(self._cfg_c), C.byref(pin), C.byref(h)),
+                  "dem_create")
         self.h = h
         self.set_precision(precision)
 
@@ -288,6 +295,19 @@ class GlobalData:
         return read_contacts(
             self.lib, lambda cs, cap, cnt: self.lib.dem_get_contacts(self.h, cs, cap, cnt),
             "dem_get_contacts")
+
+    def wall_shear(self, wall: int) -> np.ndarray:
+        """Shear history of wall `wall`'s contacts, (n, 3) (zero where a grain
+        does not touch it); wall 0's is also particles()["wall_shear"]."""
+        out = np.empty((self.n, 3))
+        check(self.lib, self.lib.dem_get_wall_shear(self.h, int(wall), out.ctypes.data),
+              "dem_get_wall_shear")
+        return out
+
+    def set_wall_shear(self, wall: int, shear) -> None:
+        a = _f64(shear, (self.n, 3))
+        check(self.lib, self.lib.dem_set_wall_shear(self.h, int(wall), a.ctypes.data),
+              "dem_set_wall_shear")
 
     def io_contacts(self) -> np.ndarray:
         """The active contacts as p4c records (a structured array of
