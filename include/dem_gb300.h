@@ -306,6 +306,9 @@ typedef struct DemLaunchShape {
                                    * programmatic dependent launches (each may be
                                    * scheduled while its predecessor finishes); 2 the
                                    * same, successor scheduled once all blocks run  */
+    int32_t list_lanes;           /* neighbour-list update: lanes per particle, 1 or 4
+                                   * (0 = 1 when the particles outnumber half the
+                                   * launch's threads, else 4)                        */
 } DemLaunchShape;
 
 int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* shape);

@@ -517,7 +517,7 @@ LaunchShape default_shape(const DemHandle* h) {
     };
     const int64_t n = h->multi ? INT64_MAX / 16 : h->n_cap;
     const int ib = block_for(n, 4), fb = block_for(3 * n, 8), cb = block_for(4 * n, 4);
-    return LaunchShape{fb, h->sm_count * 16, cb, h->sm_count * 16, ib, 4, 0, 0};
+    return LaunchShape{fb, h->sm_count * 16, cb, h->sm_count * 16, ib, 4, 0, 0, 0};
 }
 
 int init_handle(DemHandle* h) {
@@ -528,6 +528,7 @@ int init_handle(DemHandle* h) {
     h->ntiles_cells = std::max(1, scan_tiles((int64_t)h->p.T));
     h->shape = default_shape(h);
     h->p.dep = h->shape.dependent_launch;
+    h->p.list_lanes = h->shape.list_lanes;
     return DEM_OK;
 }
 
@@ -1460,13 +1461,15 @@ int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* sh) {
         sh->compact_block < 32 || sh->compact_block > 256 || sh->compact_block % 32 ||
         sh->integrate_block < 32 || sh->integrate_block > 256 || sh->integrate_block % 32 ||
         sh->force_grid < 1 || sh->compact_grid < 1 ||
-        sh->dependent_launch < 0 || sh->dependent_launch > 2)
+        sh->dependent_launch < 0 || sh->dependent_launch > 2 ||
+        (sh->list_lanes != 0 && sh->list_lanes != 1 && sh->list_lanes != 4))
         return DEM_ERR_INVALID;
     h->shape = LaunchShape{sh->force_block, sh->force_grid, sh->compact_block, sh->compact_grid,
                            sh->integrate_block,
                            sh->detect_blocks_per_sm ? sh->detect_blocks_per_sm : 4,
-                           sh->force_blocks_per_sm, sh->dependent_launch};
+                           sh->force_blocks_per_sm, sh->dependent_launch, sh->list_lanes};
     h->p.dep = h->shape.dependent_launch;
+    h->p.list_lanes = h->shape.list_lanes;
     drop_graphs(h);
     return DEM_OK;
 }
@@ -1476,7 +1479,8 @@ int dem_get_launch_shape(DemHandle* h, DemLaunchShape* out) {
     *out = DemLaunchShape{h->shape.force_block,         h->shape.force_grid,
                           h->shape.compact_block,       h->shape.compact_grid,
                           h->shape.integrate_block,     h->shape.detect_blocks_per_sm,
-                          h->shape.force_blocks_per_sm, h->shape.dependent_launch};
+                          h->shape.force_blocks_per_sm, h->shape.dependent_launch,
+                          h->shape.list_lanes};
     return DEM_OK;
 }
 

@@ -218,6 +218,7 @@ struct DemParams {
                     // launches, 2 the same with the successor scheduled early
     int debug_enum; // 1: the pair search counts its candidate pairs (never in a graph)
     int tab;        // 1: a single scene with material / wall tables (DemDev::mt, mid)
+    int list_lanes; // neighbour-list update: 0 auto, 1 or 4 lanes per particle
     int wstride;    // slots per wall-shear column
     SceneParams s0; // the scene of a single-scene handle
 };
@@ -233,6 +234,7 @@ struct LaunchShape {
                                // 3 or 4 blocks per SM
     int force_blocks_per_sm;   // register budget of the FP32 force kernel: 0 (none) or 4
     int dependent_launch;      // 0 ordinary, 1 programmatic dependent, 2 with early trigger
+    int list_lanes;            // neighbour-list update: 0 auto, 1 or 4 lanes per particle
 };
 
 // ---- launchers (dem_kernels.cu) --------------------------------------------

@@ -831,6 +831,113 @@ __device__ __forceinline__ void list_particle(const DemDev& d, const DemParams& 
     job.len = nkeep + job.nnew;
 }
 
+// The list update of one particle by one lane (the narrow layout): the same
+// decisions as list_particle, with the row and the list walked by the lane
+// itself (no shared row cache: a row's few entries are re-read from L1).
+template <bool MULTI>
+__device__ __forceinline__ void list_particle1(const DemDev& d, const DemParams& p, int cur, int i,
+                                               int e0, int e1, int nv, bool frozen, RowJob& job) {
+    const ContactSoA o = d.c[cur];
+    int nkeep = 0, ended = 0;
+    for (int e = e0; e < e1; ++e) {
+        const uint32_t fl = o.fl[e];
+        int keep;
+        if (!(fl & kActive)) {
+            keep = 0;
+        } else if (frozen || (fl & kBonded)) {
+            keep = 1;
+        } else {
+            const int j = o.cj[e];
+            const bool valid = touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j],
+                                           d.pz[j], d.r[i], d.r[j]);
+            keep = (valid ||
+                    !in_cp_list<MULTI>(d, scene_rec<MULTI>(d, p, slot_scene<MULTI>(d, i)), i, j))
+                       ? 1
+                       : 0;
+            ended += 1 - keep;
+        }
+        d.keep[e] = (uint8_t)keep;
+        nkeep += keep;
+    }
+    int32_t* stash = d.stash + (size_t)i * p.kstash;
+    int nnew = 0;
+    if (!frozen) {
+        const float4 Pi = d.pos32[i];
+        const int32_t* vl = d.vl + (size_t)i * p.kvl;
+        for (int v = 0; v < nv; ++v) {
+            const int j = vl[v];
+            bool found = false;
+            for (int e = e0; e < e1 && !found; ++e)
+                found = (o.cj[e] == j) && (o.fl[e] & kActive);
+            if (found) continue;
+            if (!maybe_touching32(Pi, d.pos32[j])) continue;
+            if (!touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j], d.pz[j], d.r[i],
+                             d.r[j]))
+                continue;
+            if (nnew < p.kstash) stash[nnew] = j;
+            ++nnew;
+        }
+    }
+    if (nnew > p.kstash) {
+        raise_error(d.ctr, kErrCapacity);
+        nnew = p.kstash;
+    }
+    for (int a2 = 1; a2 < nnew; ++a2) {  // new partners ascending
+        const int v = stash[a2];
+        int b2 = a2 - 1;
+        while (b2 >= 0 && stash[b2] > v) {
+            stash[b2 + 1] = stash[b2];
+            --b2;
+        }
+        stash[b2 + 1] = v;
+    }
+    if (ended || nnew) {
+        const int sc = slot_scene<MULTI>(d, i);
+        if (ended) atomicAdd(&d.sctr[sc].ended, (unsigned long long)ended);
+        if (nnew) atomicAdd(&d.sctr[sc].created, (unsigned long long)nnew);
+    }
+    job.i = i;
+    job.mode = frozen ? kModeFrozen : kModeStep;
+    job.e0 = e0;
+    job.e1 = e1;
+    job.nnew = nnew;
+    job.len = nkeep + nnew;
+}
+
+// The neighbour-list update with one lane per particle: in large scenes with
+// few contacts and list partners per particle (a compacted bed, a pour) four
+// lanes per particle leave most lanes idle and too few particles in flight
+// to cover the chain of dependent loads; one lane per particle puts four
+// times as many particles in flight.  A warp's rows are placed together
+// (one atomic per warp).
+template <bool MULTI>
+__device__ __forceinline__ void list_phase_narrow(const DemDev& d, const DemParams& p, int cur) {
+    for (int i0 = blockIdx.x * kThreads + (int)(threadIdx.x & ~31u); i0 < p.n;
+         i0 += gridDim.x * kThreads) {
+        const int i = i0 + (int)lane_id();
+        bool act = i < p.n, frz = false;
+        if (MULTI && act) {
+            const uint8_t path = d.path[i];
+            act = (path & 3) == 2;
+            frz = (path >> 2) == kModeFrozen;
+        }
+        RowJob job{};
+        if (act) {
+            const int e0 = d.row_start[cur][i];
+            const int e1 = e0 + d.row_len[cur][i];
+            const int nv = frz ? 0 : d.vl_len[i];
+            if (e1 == e0 && nv == 0) {  // no contact and no list partner: an empty row
+                d.row_start[cur ^ 1][i] = 0;
+                d.row_len[cur ^ 1][i] = 0;
+                act = false;
+            } else {
+                list_particle1<MULTI>(d, p, cur, i, e0, e1, nv, frz, job);
+            }
+        }
+        emit_rows<1>(d, p, cur, act, job, 0);
+    }
+}
+
 // The neighbour-list update (a12, a13, a21 for scenes whose lists are valid):
 // 4 lanes per particle.  A particle with no contact and no list partner gets
 // an empty next row at once.  When the particles outnumber one pass of the
@@ -845,6 +952,13 @@ __device__ __forceinline__ void list_particle(const DemDev& d, const DemParams& 
 template <bool MULTI>
 __device__ __forceinline__ void list_phase(const DemDev& d, const DemParams& p, int cur,
                                            ListShared* sh) {
+    // one lane per particle when chosen, or by default when the particles
+    // outnumber half the launch's threads
+    if (p.list_lanes == 1 ||
+        (p.list_lanes == 0 && 2LL * p.n > (long long)gridDim.x * kThreads)) {
+        list_phase_narrow<MULTI>(d, p, cur);
+        return;
+    }
     const int lane = threadIdx.x & (kVLanes - 1);
     const int g = threadIdx.x / kVLanes;
     const unsigned gmask = 0xfu << (lane_id() & ~3u);

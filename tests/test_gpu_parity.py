@@ -282,6 +282,32 @@ def test_polydisperse_bed_one_step(gpu, precision, rtol):
         assert_rows_close(pg["pos"], po["pos"], 1e-9, "bed fp32 pos")
 
 
+def test_list_layouts_bit_identical(gpu):
+    """The neighbour-list update with one lane per particle and with four
+    give the same results bit for bit (a compacted polydisperse bed, where
+    contacts are created and ended every step, and a bonded cube impact)."""
+    f = 2.0 * (30_000 / 2_000_000) ** (1.0 / 3.0)
+    bed = scenes.granular_bed(30_000, box=(0.4 * f, 0.4 * f, 1.2), seed=23)
+    cube = scenes.bonded_cube(8, speed=30.0, steps=0, seed=2)
+    for sc, steps in ((bed, 200), (cube, 200)):
+        outs = []
+        for lanes in (1, 4):
+            g = GlobalData(sc.cfg, sc.particles)
+            g.set_launch_shape(list_lanes=lanes)
+            if sc.bonded:
+                g.initialize()
+            g.simulate(steps)
+            outs.append((g.particles(), g.contacts(), g.stats()))
+            g.close()
+        for k in outs[0][0]:
+            np.testing.assert_array_equal(outs[0][0][k], outs[1][0][k], err_msg=k)
+        for k in outs[0][1]:
+            np.testing.assert_array_equal(outs[0][1][k], outs[1][1][k], err_msg=k)
+        s1, s4 = outs[0][2], outs[1][2]
+        assert (s1["contacts_created"], s1["contacts_ended"]) == \
+            (s4["contacts_created"], s4["contacts_ended"])
+
+
 def test_short_horizon_cube(gpu):
     sc = scenes.bonded_cube(10, speed=10.0, steps=0, seed=1)
     g, o = both(sc.cfg, sc.particles)
