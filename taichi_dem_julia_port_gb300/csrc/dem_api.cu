@@ -459,8 +459,8 @@ int allocate(DemHandle* h) {
     TRY(dalloc(h, &d.keep, cap));
     TRY(dalloc(h, &d.in_cnt, n));
     TRY(dalloc(h, &d.in_list, n * (size_t)h->p.kin));
-    TRY(dalloc(h, &d.contrib, 12 * cap));   // one 96-byte record per contact
-    TRY(dalloc(h, &d.contrib32, 12 * cap)); // one 48-byte record per contact
+    TRY(dalloc(h, &d.contrib, 9 * cap));
+    TRY(dalloc(h, &d.contrib32, 9 * cap));
     TRY(dalloc(h, &d.bk32, n));
     TRY(dalloc(h, &d.rm32, n));
     TRY(dalloc(h, &d.scan_state[kScanCells], (size_t)scan_tiles((int64_t)T)));

@@ -15,7 +15,7 @@
 //    pair), each a structure of arrays of rows — row i holds the contacts
 //    (i, j) with j > i, sorted by j, at [row_start[i], row_start[i]+row_len[i]);
 //    rows are placed by an atomic allocator, so the buffers need no scan;
-//  * per-contact force contributions (one record of 𝐦ᵢ, 𝐅, 𝐦ⱼ) and a per-particle list
+//  * per-contact force contributions (9 FP64 values) and a per-particle list
 //    of incoming contacts (those where the particle is j) used to sum forces
 //    per particle in a fixed order, without floating-point atomics.
 #pragma once
@@ -196,8 +196,8 @@ struct DemDev {
     int2* in_list;        // n * kin: (contact slot, owner i) of contacts where the particle is j
     // Contact columns 𝐅ᵢ, 𝛕ᵢ, 𝛕ⱼ hold FP64 values in the FP64 force mode and
     // FP32 (hi, lo) pairs in the FP32 force mode.
-    double* contrib;      // 12 * cap: per contact 𝐦ᵢ, 𝐅, 𝐦ⱼ and 3 pad values (96 bytes)
-    float* contrib32;     // 12 * cap: the FP32 force mode's records (48 bytes)
+    double* contrib;      // 9 * cap, [field][contact]
+    float* contrib32;     // 9 * cap, the FP32 force mode's contributions
     // scan scratch: tile states of each scan site
     unsigned long long* scan_state[2];
     DevCounters* ctr;

@@ -1430,55 +1430,6 @@ __device__ __forceinline__ bool bond_breaks_fp64(const Vec3<double>& F, const Ve
     return bond_breaks_d(F, ti, tj, d.b_invA[small], d.b_rbI[small], p);
 }
 
-// Force contributions: one record of kContribStride values per contact, in
-// the order 𝐦ᵢ, 𝐅, 𝐦ⱼ (𝐅 the force on i in global coordinates, 𝐦ᵢ, 𝐦ⱼ the
-// moments on i and j) and three pad values: 96 bytes in FP64, 48 in FP32,
-// both 16-byte aligned.  The integrator reads its own row's (𝐦ᵢ, 𝐅) and its
-// incoming contacts' (𝐅, 𝐦ⱼ) as contiguous 48 / 24 bytes, instead of six
-// values from six separate arrays.
-constexpr int kContribStride = 12;
-__device__ __forceinline__ void put_contrib(double* cb, size_t c, const Vec3<double>& F,
-                                            const Vec3<double>& mi, const Vec3<double>& mj) {
-    double2* r = reinterpret_cast<double2*>(cb + c * kContribStride);
-    r[0] = make_double2(mi.x, mi.y);
-    r[1] = make_double2(mi.z, F.x);
-    r[2] = make_double2(F.y, F.z);
-    r[3] = make_double2(mj.x, mj.y);
-    r[4] = make_double2(mj.z, 0.0);
-}
-__device__ __forceinline__ void put_contrib(float* cb, size_t c, const Vec3<float>& F,
-                                            const Vec3<float>& mi, const Vec3<float>& mj) {
-    float4* r = reinterpret_cast<float4*>(cb + c * kContribStride);
-    r[0] = make_float4(mi.x, mi.y, mi.z, F.x);
-    r[1] = make_float4(F.y, F.z, mj.x, mj.y);
-    reinterpret_cast<float*>(r + 2)[0] = mj.z;
-}
-// (𝐅, 𝐦ᵢ) of contact c: v[0..2] = 𝐅, v[3..5] = 𝐦ᵢ
-__device__ __forceinline__ void get_own(const double* cb, size_t c, double (&v)[6]) {
-    const double2* r = reinterpret_cast<const double2*>(cb + c * kContribStride);
-    const double2 a = r[0], b = r[1], e = r[2];
-    v[0] = b.y; v[1] = e.x; v[2] = e.y; v[3] = a.x; v[4] = a.y; v[5] = b.x;
-}
-__device__ __forceinline__ void get_own(const float* cb, size_t c, float (&v)[6]) {
-    const float* base = cb + c * kContribStride;
-    const float4 a = *reinterpret_cast<const float4*>(base);
-    const float2 b = *reinterpret_cast<const float2*>(base + 4);
-    v[0] = a.w; v[1] = b.x; v[2] = b.y; v[3] = a.x; v[4] = a.y; v[5] = a.z;
-}
-// (𝐅, 𝐦ⱼ) of contact c: v[0..2] = 𝐅, v[3..5] = 𝐦ⱼ
-__device__ __forceinline__ void get_in(const double* cb, size_t c, double (&v)[6]) {
-    const double* base = cb + c * kContribStride;
-    const double f0 = base[3];
-    const double2 b = *reinterpret_cast<const double2*>(base + 4);
-    const double2 e = *reinterpret_cast<const double2*>(base + 6);
-    v[0] = f0; v[1] = b.x; v[2] = b.y; v[3] = e.x; v[4] = e.y; v[5] = base[8];
-}
-__device__ __forceinline__ void get_in(const float* cb, size_t c, float (&v)[6]) {
-    const float* base = cb + c * kContribStride;
-    const float4 b = *reinterpret_cast<const float4*>(base + 4);
-    v[0] = base[3]; v[1] = b.x; v[2] = b.y; v[3] = b.z; v[4] = b.w; v[5] = base[8];
-}
-
 // FP32 hi/lo pair accumulator (hi + lo carries about 48 bits): (hi, lo) + x
 // by Knuth's two-sum and a fast renormalisation, all in FP32.
 __device__ __forceinline__ float2 pair_add(float2 a, float x) {
@@ -1670,7 +1621,16 @@ __device__ __forceinline__ void force32(const DemDev& d, const SceneParams& SP,
         pair_col(w, CF + 2)[c] = make_float2(F3, 0.0f);
         st3(w.f, CS, c, s);
     }
-    put_contrib(d.contrib32, (size_t)c, fig, mi, mj);
+    float* cb = d.contrib32;
+    cb[0 * cap + c] = fig.x;
+    cb[1 * cap + c] = fig.y;
+    cb[2 * cap + c] = fig.z;
+    cb[3 * cap + c] = mi.x;
+    cb[4 * cap + c] = mi.y;
+    cb[5 * cap + c] = mi.z;
+    cb[6 * cap + c] = mj.x;
+    cb[7 * cap + c] = mj.y;
+    cb[8 * cap + c] = mj.z;
 }
 
 // `resolve_collision!` for one active contact (src/kernels.jl:136-313).  T is
@@ -1830,9 +1790,15 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
         st3(w.f, CF, c, {(double)F1, (double)F2, (double)F3});
         st3(w.f, CS, c, s);
     }
-    put_contrib(d.contrib, (size_t)c, Vec3<double>{(double)fig.x, (double)fig.y, (double)fig.z},
-                Vec3<double>{(double)mi.x, (double)mi.y, (double)mi.z},
-                Vec3<double>{(double)mj.x, (double)mj.y, (double)mj.z});
+    d.contrib[0 * cap + c] = (double)fig.x;
+    d.contrib[1 * cap + c] = (double)fig.y;
+    d.contrib[2 * cap + c] = (double)fig.z;
+    d.contrib[3 * cap + c] = (double)mi.x;
+    d.contrib[4 * cap + c] = (double)mi.y;
+    d.contrib[5 * cap + c] = (double)mi.z;
+    d.contrib[6 * cap + c] = (double)mj.x;
+    d.contrib[7 * cap + c] = (double)mj.y;
+    d.contrib[8 * cap + c] = (double)mj.z;
 }
 
 template <typename T, bool MULTI, bool TAB = false>
@@ -1910,8 +1876,16 @@ __device__ __forceinline__ void add_incoming(const DemDev& d, size_t cap, int2 (
     sort_by_owner<N>(v);
     T g[N][6];
 #pragma unroll
-    for (int u = 0; u < N; ++u)
-        if (u < nin) get_in(cb, (size_t)v[u].x, g[u]);
+    for (int u = 0; u < N; ++u) {
+        if (u < nin) {
+            const int c = v[u].x;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                g[u][q] = cb[q * cap + c];
+                g[u][3 + q] = cb[(6 + q) * cap + c];
+            }
+        }
+    }
 #pragma unroll
     for (int u = 0; u < N; ++u) {
         if (u < nin) {
@@ -1945,8 +1919,11 @@ __device__ __forceinline__ void gather(const DemDev& d, const DemParams& p, int 
     int c = c0;
     for (; c + 1 < c1; c += 2) {
         T a[6], b[6];
-        get_own(cb, (size_t)c, a);
-        get_own(cb, (size_t)c + 1, b);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            a[q] = cb[q * cap + c];
+            b[q] = cb[q * cap + c + 1];
+        }
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             F[q] += a[q];
@@ -1959,12 +1936,10 @@ __device__ __forceinline__ void gather(const DemDev& d, const DemParams& p, int 
         }
     }
     if (c < c1) {
-        T a[6];
-        get_own(cb, (size_t)c, a);
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            F[q] += a[q];
-            M[q] += a[3 + q];
+            F[q] += cb[q * cap + c];
+            M[q] += cb[(3 + q) * cap + c];
         }
     }
     if (nin <= 4) {
@@ -1986,12 +1961,11 @@ __device__ __forceinline__ void gather(const DemDev& d, const DemParams& p, int 
             inc[b + 1] = v;
         }
         for (int u = 0; u < nin; ++u) {
-            T g[6];
-            get_in(cb, (size_t)inc[u].x, g);
+            const int cc = inc[u].x;
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
-                F[q] += -g[q];
-                M[q] += g[3 + q];
+                F[q] += -cb[q * cap + cc];
+                M[q] += cb[(6 + q) * cap + cc];
             }
         }
     }

@@ -29,7 +29,7 @@ from .scenes import Scene, bonded_cube, granular_pour
 # device bytes per arena unit (the buffers dem_arena_create allocates)
 SLOT_BYTES_BASE = 516          # particle SoA, broad phase, neighbour lists, bookkeeping
 SLOT_BYTES_PER_PARTNER = 12    # new-partner stash (4 B) + incoming list (8 B), per partner
-CONTACT_BYTES = 381            # two contact buffers, force contributions, survival flag
+CONTACT_BYTES = 345            # two contact buffers, force contributions, survival flag
 BUCKET_BYTES = 8               # count + start
 
 
