@@ -263,6 +263,11 @@ def make_scene(name: str, pour_n: int = 2_000_000):
     if name == "c3":
         return (scenes.c3(pour_n),
                 f"unbonded pour {pour_n:,} spheres in 0.4 x 0.4 x 1.2 m, FP32 force, dt 2e-7")
+    if name == "c3bed":
+        f = (pour_n / 2_000_000) ** 0.5  # the same column height on a smaller floor
+        return (scenes.granular_bed(pour_n, box=(0.4 * f, 0.4 * f, 1.2)),
+                f"the pour's {pour_n:,} spheres pre-compacted into a bed of touching columns "
+                "(about one Hertz contact per sphere), FP32 force, dt 2e-7")
     raise ValueError(name)
 
 
@@ -884,7 +889,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c3bed", "c4", "c5"])
     ap.add_argument("--advance", type=int, default=None,
                     help="untimed steps before the warm-up (default: 4,000 for the "
                          "17,576-sphere cube and 2,000 for the 1,000-sphere cube, so the timed "
@@ -952,7 +957,7 @@ def main() -> None:
             dist.destroy_process_group()
         return
     sc, desc = make_scene(args.workload, args.pour_n)
-    precision = args.precision or ("fp32" if args.workload == "c3" else "fp64")
+    precision = args.precision or ("fp32" if args.workload in ("c3", "c3bed") else "fp64")
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     r = measure_scene(args, lib, sc, precision, args.steps, args.warmup, args.advance, flush,
                       dist=dist, ws=ws, settling=args.workload == "c3",

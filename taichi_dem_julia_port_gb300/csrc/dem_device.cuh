@@ -62,6 +62,23 @@ __device__ __forceinline__ bool maybe_touching32(float4 a, float4 b, float extra
     return !(s * (1.0f - 0x1p-17f) > B * B);
 }
 
+// Conservative FP32 acceptance, the mirror of maybe_touching32: returns true
+// only when the FP64 test touching_rn is certain to succeed.  a, b are the
+// particles' FP32 positions (as for maybe_touching32), ra, rb their FP32
+// radii; each inner reach r'(1 - 2^-19) - M·2^-19 and the factor 1 + 2^-17 on
+// the squared distance take the same error bounds the other way (the FP64
+// evaluation's own rounding, ~2^-52 relative, is far inside the margins).
+__device__ __forceinline__ float inner_reach32(float4 a, float r) {
+    const float M = fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fabsf(a.z));
+    return (r * (1.0f - 0x1p-19f) - M * 0x1p-19f) * (1.0f - 0x1p-21f);
+}
+__device__ __forceinline__ bool surely_touching32(float4 a, float ra, float4 b, float rb) {
+    const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    const float s = dx * dx + dy * dy + dz * dz;
+    const float B = inner_reach32(a, ra) + inner_reach32(b, rb);
+    return B > 0.0f && s * (1.0f + 0x1p-17f) < B * B;
+}
+
 // ---- FP64 <-> FP32 conversions on the integer pipe -----------------------------
 // GB300 runs conversions involving FP64 on its narrow FP64 pipe.  These do the
 // same conversions with integer instructions, from the IEEE 754 binary64 and

@@ -761,8 +761,12 @@ __device__ __forceinline__ void list_particle(const DemDev& d, const DemParams& 
         } else if (frozen || (fl & kBonded)) {
             keep = 1;
         } else {
-            const bool valid = touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j],
-                                           d.pz[j], d.r[i], d.r[j]);
+            // an FP32 screen accepts the clearly touching pairs; the FP64
+            // test decides the rest
+            const bool valid =
+                surely_touching32(d.pos32[i], d.rm32[i].z, d.pos32[j], d.rm32[j].z) ||
+                touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j], d.pz[j], d.r[i],
+                            d.r[j]);
             keep = (valid ||
                     !in_cp_list<MULTI>(d, scene_rec<MULTI>(d, p, slot_scene<MULTI>(d, i)), i, j))
                        ? 1
@@ -791,8 +795,10 @@ __device__ __forceinline__ void list_particle(const DemDev& d, const DemParams& 
                     found = (o.cj[e2] == j) && (o.fl[e2] & kActive);
             }
             if (found) continue;
-            if (!maybe_touching32(Pi, d.pos32[j])) continue;
-            if (!touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j], d.pz[j], d.r[i],
+            const float4 Pj = d.pos32[j];
+            if (!maybe_touching32(Pi, Pj)) continue;
+            if (!surely_touching32(Pi, d.rm32[i].z, Pj, d.rm32[j].z) &&
+                !touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j], d.pz[j], d.r[i],
                              d.r[j]))
                 continue;
             const int slot = atomicAdd(&sh[g].nnew, 1);
@@ -848,8 +854,10 @@ __device__ __forceinline__ void list_particle1(const DemDev& d, const DemParams&
             keep = 1;
         } else {
             const int j = o.cj[e];
-            const bool valid = touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j],
-                                           d.pz[j], d.r[i], d.r[j]);
+            const bool valid =
+                surely_touching32(d.pos32[i], d.rm32[i].z, d.pos32[j], d.rm32[j].z) ||
+                touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j], d.pz[j], d.r[i],
+                            d.r[j]);
             keep = (valid ||
                     !in_cp_list<MULTI>(d, scene_rec<MULTI>(d, p, slot_scene<MULTI>(d, i)), i, j))
                        ? 1
@@ -870,8 +878,10 @@ __device__ __forceinline__ void list_particle1(const DemDev& d, const DemParams&
             for (int e = e0; e < e1 && !found; ++e)
                 found = (o.cj[e] == j) && (o.fl[e] & kActive);
             if (found) continue;
-            if (!maybe_touching32(Pi, d.pos32[j])) continue;
-            if (!touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j], d.pz[j], d.r[i],
+            const float4 Pj = d.pos32[j];
+            if (!maybe_touching32(Pi, Pj)) continue;
+            if (!surely_touching32(Pi, d.rm32[i].z, Pj, d.rm32[j].z) &&
+                !touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j], d.pz[j], d.r[i],
                              d.r[j]))
                 continue;
             if (nnew < p.kstash) stash[nnew] = j;
@@ -910,10 +920,15 @@ __device__ __forceinline__ void list_particle1(const DemDev& d, const DemParams&
 // to cover the chain of dependent loads; one lane per particle puts four
 // times as many particles in flight.  A warp's rows are placed together
 // (one atomic per warp).
+// Warps take 32 consecutive particles in turn across the blocks (warp w of
+// block b is the grid's warp w·gridDim + b): a cooperative launch places
+// consecutive blocks on the same SM, so chunks by block would leave SMs idle
+// whenever the particles do not fill the grid.
 template <bool MULTI>
 __device__ __forceinline__ void list_phase_narrow(const DemDev& d, const DemParams& p, int cur) {
-    for (int i0 = blockIdx.x * kThreads + (int)(threadIdx.x & ~31u); i0 < p.n;
-         i0 += gridDim.x * kThreads) {
+    const int wslot = (int)(threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x;
+    for (long long t0 = 0; t0 < p.n; t0 += (long long)gridDim.x * kThreads) {
+        const int i0 = (int)(t0 + 32LL * wslot);
         const int i = i0 + (int)lane_id();
         bool act = i < p.n, frz = false;
         if (MULTI && act) {
@@ -1010,9 +1025,11 @@ __device__ __forceinline__ void list_phase(const DemDev& d, const DemParams& p, 
         }
         return;
     }
-    for (int i0 = blockIdx.x * (kThreads / kVLanes) + gwarp; i0 < p.n;
-         i0 += gridDim.x * (kThreads / kVLanes)) {
-        const int i = i0 + (g - gwarp);
+    // group g of block b takes the grid's group g·gridDim + b in turn (see
+    // list_phase_narrow: every block gets particles, whatever their number)
+    const int gslot = g * (int)gridDim.x + (int)blockIdx.x;
+    for (long long t0 = 0; t0 < p.n; t0 += (long long)gridDim.x * (kThreads / kVLanes)) {
+        const int i = (int)(t0 + gslot);
         // which particles test their lists: the path byte the search wrote (arena)
         bool active = i < p.n;
         bool frozen = false;

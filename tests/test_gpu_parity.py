@@ -282,6 +282,61 @@ def test_polydisperse_bed_one_step(gpu, precision, rtol):
         assert_rows_close(pg["pos"], po["pos"], 1e-9, "bed fp32 pos")
 
 
+def _boundary_pairs(npair, seed):
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(0.004, 0.006, 2 * npair)
+    side = int(np.ceil(npair ** (1.0 / 3.0)))
+    ijk = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)[:npair]
+    centres = (ijk + 0.5) * 0.05
+    dirs = rng.standard_normal((npair, 3))
+    dirs /= np.linalg.norm(dirs, axis=1)[:, None]
+    return r, centres, dirs
+
+
+def _place(r, centres, dirs, rel):
+    """Pair k's spheres at separation (r_a + r_b)(1 + rel[k]) along dirs[k]."""
+    sep = (r[0::2] + r[1::2]) * (1.0 + rel)
+    pos = np.empty((2 * len(centres), 3))
+    pos[0::2] = centres - dirs * (sep / 2)[:, None]
+    pos[1::2] = centres + dirs * (sep / 2)[:, None]
+    return pos
+
+
+def test_touching_decisions_at_the_boundary(gpu):
+    """Pairs placed at separations (rᵢ + rⱼ)(1 + δ), δ from -1e-6 to +1e-6
+    down to a few ulps either side of touching: the contacts the neighbour-list
+    step creates, and then keeps or ends, equal the oracle's (the FP32 screens
+    decide only pairs whose outcome they can prove)."""
+    npair = 512
+    r, centres, dirs = _boundary_pairs(npair, seed=5)
+    deltas = np.array([-1e-6, -1e-8, -1e-10, -1e-12, -1e-14, -4e-16, -2e-16, 0.0, 2e-16, 4e-16,
+                       1e-14, 1e-12, 1e-10, 1e-8, 1e-6, 3e-3])
+    cfg = DEMConfig(domain_min=[-0.05] * 3, domain_max=[0.5] * 3, max_coordinate_number=8,
+                    wall_distance=10.0, gravity=[0.0, 0.0, 0.0], dt=1e-9,
+                    particle_elastic_modulus=1e8)
+    pos0 = _place(r, centres, dirs, np.full(npair, 2e-3))  # apart, on the neighbour lists
+    p = ParticleInput.from_arrays(r, pos0, np.zeros_like(pos0), 2500.0)
+    for lanes in (4, 1):  # both layouts of the list step
+        g, o = both(cfg, p)
+        g.set_launch_shape(list_lanes=lanes)
+        g.simulate(2)  # a full search, then a list step
+        created = 0
+        for shift in range(3):
+            rel = deltas[(np.arange(npair) + 5 * shift) % len(deltas)]
+            copy_state(g, o)
+            pos = _place(r, centres, dirs, rel)
+            g.set_particles(pos=pos)
+            o.set_particles(pos=pos)
+            g.simulate(1)
+            o.simulate(1)
+            assert g.stats()["full_searches"] == 1, "the steps under test are list steps"
+            cg, co = g.contacts(), o.contacts()
+            assert pair_set(cg) == pair_set(co), f"lanes {lanes} shift {shift}"
+            created += len(co["i"])
+        assert 0 < created < 3 * npair
+        g.close()
+
+
 def test_list_layouts_bit_identical(gpu):
     """The neighbour-list update with one lane per particle and with four
     give the same results bit for bit (a compacted polydisperse bed, where
