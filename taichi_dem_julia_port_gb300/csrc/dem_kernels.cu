@@ -1025,13 +1025,18 @@ __device__ __forceinline__ void list_phase(const DemDev& d, const DemParams& p, 
         }
         return;
     }
-    // group g of block b takes the grid's group g·gridDim + b in turn (see
-    // list_phase_narrow: every block gets particles, whatever their number)
-    const int gslot = g * (int)gridDim.x + (int)blockIdx.x;
-    for (long long t0 = 0; t0 < p.n; t0 += (long long)gridDim.x * (kThreads / kVLanes)) {
-        const int i = (int)(t0 + gslot);
+    // each pass gives every block a chunk of consecutive particles, at most
+    // one per group, the chunk sized so that the particles spread over all
+    // blocks (a cooperative launch places consecutive blocks on the same SM:
+    // full chunks for the first blocks would leave SMs idle), while a warp's
+    // groups keep neighbouring particles (their rows are placed together)
+    const int per_block = kThreads / kVLanes;
+    const int chunk = (int)min((long long)per_block,
+                               ((long long)p.n + gridDim.x - 1) / (long long)gridDim.x);
+    for (long long t0 = 0; t0 < p.n; t0 += (long long)gridDim.x * chunk) {
+        const int i = (int)(t0 + (long long)blockIdx.x * chunk + g);
         // which particles test their lists: the path byte the search wrote (arena)
-        bool active = i < p.n;
+        bool active = g < chunk && i < p.n;
         bool frozen = false;
         if (MULTI && active) {
             const uint8_t path = d.path[i];
