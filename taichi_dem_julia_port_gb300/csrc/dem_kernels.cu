@@ -1025,18 +1025,17 @@ __device__ __forceinline__ void list_phase(const DemDev& d, const DemParams& p, 
         }
         return;
     }
-    // each pass gives every block a chunk of consecutive particles, at most
-    // one per group, the chunk sized so that the particles spread over all
-    // blocks (a cooperative launch places consecutive blocks on the same SM:
-    // full chunks for the first blocks would leave SMs idle), while a warp's
-    // groups keep neighbouring particles (their rows are placed together)
-    const int per_block = kThreads / kVLanes;
-    const int chunk = (int)min((long long)per_block,
-                               ((long long)p.n + gridDim.x - 1) / (long long)gridDim.x);
-    for (long long t0 = 0; t0 < p.n; t0 += (long long)gridDim.x * chunk) {
-        const int i = (int)(t0 + (long long)blockIdx.x * chunk + g);
+    // blocks take 64 consecutive particles each in turn.  (Spreading a small
+    // scene's particles over every block of the grid, contiguous per block or
+    // interleaved, left this phase as fast and made the force pass slower:
+    // rows then enter the next buffer in a less particle-ordered sequence and
+    // the force pass's gathers lose locality; measured on the 17,576-sphere
+    // cube, force 27 -> 30 us.)
+    for (int i0 = blockIdx.x * (kThreads / kVLanes) + gwarp; i0 < p.n;
+         i0 += gridDim.x * (kThreads / kVLanes)) {
+        const int i = i0 + (g - gwarp);
         // which particles test their lists: the path byte the search wrote (arena)
-        bool active = g < chunk && i < p.n;
+        bool active = i < p.n;
         bool frozen = false;
         if (MULTI && active) {
             const uint8_t path = d.path[i];
