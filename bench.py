@@ -120,12 +120,17 @@ def algorithmic_bytes(n: int, contacts: int, bonds: int, settling: bool = False)
 # k_search (contact update: full search or lists, next rows), k_force, k_integrate
 KERNELS_PER_STEP = 3
 # FP64-pipe instructions per unit, from ncu (sm__thread_inst_executed_pipe_fp64_pred_on.sum
-# of one launch over the units it processed): the force kernel per bond (the
-# 17,576-sphere cube before its impact, every contact a bond), the integrator
-# per particle (64 scenes of the batched workload), in the FP64 and the FP32
-# force mode; then GB300's FP64 pipe width
-FP64_INST = {("force", "fp64"): 114.2, ("force", "fp32"): 15.0,
-             ("integrate", "fp64"): 85.7, ("integrate", "fp32"): 51.0}
+# of one launch over the units it processed).  Force kernel, FP64 mode: per
+# Hertz contact 151.0 (a 100,000-sphere compacted bed, every contact a Hertz
+# contact: 1.503e7 per launch), per bond 116.1 (the 17,576-sphere cube in its
+# fragmentation, 41,427 bonds and 6,670 Hertz contacts: 5.817e6 per launch,
+# less the Hertz share); FP32 mode per bond 15.0 (the same cube before its
+# impact).  Integrator per particle: 84.1 in FP64 mode (the cube in its
+# fragmentation), 51.0 in the FP32 mode (64 scenes of the batched workload).
+# Then GB300's FP64 pipe width.
+FP64_INST = {("force", "fp64", "bond"): 116.1, ("force", "fp64", "hertz"): 151.0,
+             ("force", "fp32", "bond"): 15.0,
+             ("integrate", "fp64"): 84.1, ("integrate", "fp32"): 51.0}
 # The integrator skips the quaternion increment of a particle with exactly zero
 # spin, the normalisation of a spinless identity orientation and the spin
 # update of a particle with exactly zero torque: in the pour's settling phase
@@ -137,14 +142,25 @@ SM_COUNT = 152
 
 
 def fp64_roofline(kernel: str, precision: str, n_particles: int, n_bond: int, ms: float,
-                  clk: dict, peaks: dict, workload: str | None = None) -> dict | None:
-    """The FP64-pipe roofline of the force kernel (per bond, on a scene whose
-    contacts are all bonds) or the integrator (per particle): FP64
-    instructions over the live per-phase time against the pipe's peak at the
-    SM clock sampled during the timed region (else the measured maximum
-    clock of MEASURED_PEAKS.json, else 2,070 MHz), saying which."""
-    per = FP64_INST_WORKLOAD.get((workload, kernel, precision), FP64_INST.get((kernel, precision)))
-    units = n_bond if kernel == "force" else n_particles
+                  clk: dict, peaks: dict, workload: str | None = None,
+                  n_hertz: int = 0) -> dict | None:
+    """The FP64-pipe roofline of the force kernel (per bond and per Hertz
+    contact) or the integrator (per particle): FP64 instructions over the live
+    per-phase time against the pipe's peak at the SM clock sampled during the
+    timed region (else the measured maximum clock of MEASURED_PEAKS.json, else
+    2,070 MHz), saying which.  None when a count per unit is not known."""
+    if kernel == "force":
+        pb = FP64_INST.get(("force", precision, "bond"))
+        ph = FP64_INST.get(("force", precision, "hertz"))
+        if (n_bond and pb is None) or (n_hertz and ph is None) or not (n_bond or n_hertz):
+            return None
+        inst = (pb or 0.0) * n_bond + (ph or 0.0) * n_hertz
+        units = n_bond + n_hertz
+        per = inst / units
+    else:
+        per = FP64_INST_WORKLOAD.get((workload, kernel, precision),
+                                     FP64_INST.get((kernel, precision)))
+        units = n_particles
     if per is None or not units or not ms:
         return None
     if clk.get("sm_mhz"):
@@ -157,7 +173,7 @@ def fp64_roofline(kernel: str, precision: str, n_particles: int, n_bond: int, ms
     ach = per * units / (ms * 1e-3) / 1e9
     return {"unit": "G FP64 thread-instructions/s", "achieved": ach, "peak": peak,
             "frac": ach / peak, "inst_per_unit": per,
-            "unit_counted": "bond" if kernel == "force" else "particle",
+            "unit_counted": "contact" if kernel == "force" else "particle",
             "peak_source": f"{FP64_LANES_PER_SM} FP64 lanes per SM per cycle x {SM_COUNT} SMs "
                            f"at {sm_mhz:.0f} MHz ({src})"}
 L2_FLUSH_BYTES = 256 << 20
@@ -169,6 +185,12 @@ L2_FLUSH_BYTES = 256 << 20
 # processed.  Keys: workload and timed window ("c2" the cube in its impact
 # window, "c3" the pour settling, "c3bed" the compacted bed), kernel.
 NCU_TRAFFIC = {
+    ("c2", "force"): (7.155200e6, 17576),          # k_force<double>, step 4,006
+    ("c2", "contacts"): (2.317056e6, 17576),       # k_search, list step, step 4,006
+    ("c2", "integrate"): (9.232896e6, 17576),      # k_integrate, step 4,006
+    ("c3bed", "force"): (93.960960e6, 400000),     # k_force<float>, 400,000-sphere bed
+    ("c3bed", "contacts"): (53.395712e6, 400000),  # k_search, list step (one lane per particle)
+    ("c3bed", "integrate"): (181.155840e6, 400000),  # k_integrate3 (FP32 gather)
     ("c3", "integrate"): (627.860224e6, 2000000),  # k_integrate3 (FP32 mode, no contacts)
     ("c4", "force"): (145.409024e6, 431416),       # k_force<float>
     ("c4", "integrate"): (184.980224e6, 431416),   # k_integrate3 (FP32 gather)
@@ -405,8 +427,8 @@ def run_batched(args, lib, quick: bool = False, dist=None) -> dict:
     if dom in alg:
         ach = alg[dom] / (ph[dom] * 1e-3) / 1e9
         roof.update({"achieved": ach, "frac": ach / peaks["hbm_gbs"], "algorithmic_bytes": alg[dom]})
-    fr = None if dom == "force" and contacts != bonded else fp64_roofline(
-        dom, precision, n_total, bonded, ph.get(dom), clk, peaks)
+    fr = fp64_roofline(dom, precision, n_total, bonded, ph.get(dom), clk, peaks,
+                       n_hertz=contacts - bonded)
     if fr:
         roof["fp64_pipe"] = fr
     perr = None
@@ -782,9 +804,8 @@ def measure_scene(args, lib, sc, precision: str, steps: int, warmup: int, advanc
     if dom == "force":
         # re-reads of particles gathered by more than one contact (L2 hits)
         roof["gather_bytes"] = max(0, 2 * int(round(c_mean)) - sc.n) * GATHER_BYTES_PER_CONTACT_END
-    fr = None if dom == "force" and c_mean != b_mean else fp64_roofline(
-        dom, precision, sc.n, int(round(b_mean)), ph.get(dom), clk, peaks,
-        "c3" if settling else None)
+    fr = fp64_roofline(dom, precision, sc.n, int(round(b_mean)), ph.get(dom), clk, peaks,
+                       "c3" if settling else None, n_hertz=int(round(c_mean - b_mean)))
     if fr:
         roof["fp64_pipe"] = fr
     out = {"value": ws * sc.n * steps / (total_ms / 1e3), "ms_per_step": ms_per_step,
