@@ -309,6 +309,9 @@ typedef struct DemLaunchShape {
     int32_t list_lanes;           /* neighbour-list update: lanes per particle, 1 or 4
                                    * (0 = 1 when the particles outnumber half the
                                    * launch's threads, else 4)                        */
+    int32_t integrate_lanes;      /* integrator: lanes per particle, 1 or 4 (0 = 4
+                                   * while the particles number at most 32 per SM,
+                                   * else 1)                                          */
 } DemLaunchShape;
 
 int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* shape);

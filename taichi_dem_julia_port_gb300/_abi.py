@@ -136,7 +136,7 @@ class DemLaunchShape(C.Structure):
                 ("compact_block", C.c_int32), ("compact_grid", C.c_int32),
                 ("integrate_block", C.c_int32), ("detect_blocks_per_sm", C.c_int32),
                 ("force_blocks_per_sm", C.c_int32), ("dependent_launch", C.c_int32),
-                ("list_lanes", C.c_int32)]
+                ("list_lanes", C.c_int32), ("integrate_lanes", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

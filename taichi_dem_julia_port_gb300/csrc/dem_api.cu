@@ -457,6 +457,7 @@ int allocate(DemHandle* h) {
     }
     TRY(dalloc(h, &d.stash, n * (size_t)h->p.kstash));
     TRY(dalloc(h, &d.keep, cap));
+    TRY(dalloc(h, &d.tlist, cap));
     TRY(dalloc(h, &d.in_cnt, n));
     TRY(dalloc(h, &d.in_list, n * (size_t)h->p.kin));
     TRY(dalloc(h, &d.contrib, 9 * cap));
@@ -517,7 +518,7 @@ LaunchShape default_shape(const DemHandle* h) {
     };
     const int64_t n = h->multi ? INT64_MAX / 16 : h->n_cap;
     const int ib = block_for(n, 4), fb = block_for(3 * n, 8), cb = block_for(4 * n, 4);
-    return LaunchShape{fb, h->sm_count * 16, cb, h->sm_count * 16, ib, 4, 0, 0, 0};
+    return LaunchShape{fb, h->sm_count * 16, cb, h->sm_count * 16, ib, 4, 0, 0, 0, 0};
 }
 
 int init_handle(DemHandle* h) {
@@ -777,7 +778,7 @@ int device_error(DemHandle* h) {
 
 int contact_count(DemHandle* h, int buf, int32_t* total) {
     unsigned int v = 0;
-    CU(cudaMemcpyAsync(&v, &h->d.ctr->row_alloc[buf], sizeof(v), cudaMemcpyDeviceToHost,
+    CU(cudaMemcpyAsync(&v, &h->d.ctr->alloc[buf].rows, sizeof(v), cudaMemcpyDeviceToHost,
                        h->stream));
     CU(cudaStreamSynchronize(h->stream));
     *total = (int32_t)std::min<int64_t>((int64_t)v, (int64_t)h->c_cap);
@@ -1462,12 +1463,14 @@ int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* sh) {
         sh->integrate_block < 32 || sh->integrate_block > 256 || sh->integrate_block % 32 ||
         sh->force_grid < 1 || sh->compact_grid < 1 ||
         sh->dependent_launch < 0 || sh->dependent_launch > 2 ||
-        (sh->list_lanes != 0 && sh->list_lanes != 1 && sh->list_lanes != 4))
+        (sh->list_lanes != 0 && sh->list_lanes != 1 && sh->list_lanes != 4) ||
+        (sh->integrate_lanes != 0 && sh->integrate_lanes != 1 && sh->integrate_lanes != 4))
         return DEM_ERR_INVALID;
     h->shape = LaunchShape{sh->force_block, sh->force_grid, sh->compact_block, sh->compact_grid,
                            sh->integrate_block,
                            sh->detect_blocks_per_sm ? sh->detect_blocks_per_sm : 4,
-                           sh->force_blocks_per_sm, sh->dependent_launch, sh->list_lanes};
+                           sh->force_blocks_per_sm, sh->dependent_launch, sh->list_lanes,
+                           sh->integrate_lanes};
     h->p.dep = h->shape.dependent_launch;
     h->p.list_lanes = h->shape.list_lanes;
     drop_graphs(h);
@@ -1480,7 +1483,7 @@ int dem_get_launch_shape(DemHandle* h, DemLaunchShape* out) {
                           h->shape.compact_block,       h->shape.compact_grid,
                           h->shape.integrate_block,     h->shape.detect_blocks_per_sm,
                           h->shape.force_blocks_per_sm, h->shape.dependent_launch,
-                          h->shape.list_lanes};
+                          h->shape.list_lanes,          h->shape.integrate_lanes};
     return DEM_OK;
 }
 
@@ -1523,7 +1526,7 @@ int dem_init_bonds(DemHandle* h) {
     const int cur = h->cur, nxt = cur ^ 1;
     launch_search(h->d, h->p, cur, true, false, true, h->shape, h->stream);
     // the old buffer becomes the next step's target: its allocator starts at 0
-    CU(cudaMemsetAsync(&h->d.ctr->row_alloc[cur], 0, sizeof(unsigned int), h->stream));
+    CU(cudaMemsetAsync(&h->d.ctr->alloc[cur], 0, sizeof(RowCounter), h->stream));
     CU(cudaGetLastError());
     h->cur = nxt;
     return device_error(h);
@@ -1790,8 +1793,11 @@ int dem_set_contacts(DemHandle* h, const DemContacts* in, int64_t nc) {
         CU(cudaMemcpyAsync(h->d.row_len[h->cur], rl.data(), (size_t)n * 4,
                            cudaMemcpyHostToDevice, h->stream));
     }
-    const unsigned int alloc[2] = {h->cur == 0 ? (unsigned)nc : 0u, h->cur == 1 ? (unsigned)nc : 0u};
-    CU(cudaMemcpyAsync(h->d.ctr->row_alloc, alloc, sizeof(alloc), cudaMemcpyHostToDevice,
+    // the uploaded buffer's bond count is not kept: the force pass reads the
+    // type-ordered list of the buffer a step's rows are placed in
+    RowCounter alloc[2] = {{0u, 0u}, {0u, 0u}};
+    alloc[h->cur].rows = (unsigned)nc;
+    CU(cudaMemcpyAsync(h->d.ctr->alloc, alloc, sizeof(alloc), cudaMemcpyHostToDevice,
                        h->stream));
     CU(cudaStreamSynchronize(h->stream));
     return DEM_OK;

@@ -128,12 +128,19 @@ struct SceneCounters {
     unsigned long long searches;  // steps that ran the full pair search
 };
 
+// Contacts placed in one contact buffer: all of them (rows) and, of them,
+// the bonds.  One 64-bit word, so that a warp places its rows and its entries
+// of the force pass's type-ordered list (DemDev::tlist) with one atomic.
+struct alignas(8) RowCounter {
+    unsigned int rows, bonds;
+};
+
 struct DevCounters {
     int error;
     unsigned int bmax;        // largest bucket id of this step (k_hash), reset by k_canon
     unsigned int cell_limit;  // buckets [0, cell_limit) have valid starts this step
     unsigned int pad;
-    unsigned int row_alloc[2];      // contacts allocated in each contact buffer
+    RowCounter alloc[2];            // contacts placed in each contact buffer
     unsigned long long tickets[2];  // tile tickets of the scan sites (never reset)
     unsigned int bar_count, bar_gen;  // grid barrier of the fused search (arrivals, generation)
     unsigned int hashed[2];           // particles hashed by the step reading buffer cur
@@ -192,6 +199,9 @@ struct DemDev {
     int32_t* row_len[2];    // entries in the row
     int32_t* stash;       // n * kstash new partners of this step
     uint8_t* keep;        // cap, survival flags of the current buffer
+    int32_t* tlist;       // cap, the next buffer's contacts by type for the force pass:
+                          // bonds at [0, bonds), the others at cap-1-k, k in
+                          // [0, rows - bonds)
     int32_t* in_cnt;      // zero between steps
     int2* in_list;        // n * kin: (contact slot, owner i) of contacts where the particle is j
     // Contact columns 𝐅ᵢ, 𝛕ᵢ, 𝛕ⱼ hold FP64 values in the FP64 force mode and
@@ -235,6 +245,7 @@ struct LaunchShape {
     int force_blocks_per_sm;   // register budget of the FP32 force kernel: 0 (none) or 4
     int dependent_launch;      // 0 ordinary, 1 programmatic dependent, 2 with early trigger
     int list_lanes;            // neighbour-list update: 0 auto, 1 or 4 lanes per particle
+    int integrate_lanes;       // integrator: 0 auto, 1 or 4 lanes per particle
 };
 
 // ---- launchers (dem_kernels.cu) --------------------------------------------

@@ -377,26 +377,45 @@ struct RowJob {
     int e0, e1;   // current row entries [e0, e1)
     int nnew;     // new partners (sorted, in the particle's stash)
     int len;      // next row length (survivors + new), 0 for no row
+    int nb;       // bonds among them
 };
 
 // Places the rows of a warp's groups (L lanes each) in buffer nxt: every lane
-// of the warp calls it with its group's (group-uniform) `len`; returns the
-// group's row start.  A row that would cross the capacity raises
-// kErrCapacity and gets length 0.
+// of the warp calls it with its group's (group-uniform) `len` and bond count
+// `nb`; returns the group's row start and, in *bstart, the start of its bonds
+// in the type-ordered list (its other contacts start at start - *bstart: the
+// bonds placed before a row never outnumber the contacts placed before it,
+// so both ranges lie inside [0, start + len)).  A row that would cross the
+// capacity raises kErrCapacity and gets length 0.
 template <int L>
-__device__ __forceinline__ int place_rows(const DemDev& d, const DemParams& p, int nxt, int& len) {
+__device__ __forceinline__ int place_rows(const DemDev& d, const DemParams& p, int nxt, int& len,
+                                          int nb, int* bstart) {
     const unsigned lane = lane_id();
-    const int v = (lane % L == 0) ? len : 0;
-    int incl = v;
+    const bool lead = lane % L == 0;
+    const unsigned v = lead ? (unsigned)len : 0u, vb = lead ? (unsigned)nb : 0u;
+    unsigned incl = v, inclb = vb;
 #pragma unroll
     for (int o2 = 1; o2 < 32; o2 <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, o2);
-        if (lane >= (unsigned)o2) incl += y;
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o2);
+        const unsigned yb = __shfl_up_sync(0xffffffffu, inclb, o2);
+        if (lane >= (unsigned)o2) {
+            incl += y;
+            inclb += yb;
+        }
     }
-    int base = 0;
-    if (lane == 31 && incl) base = (int)atomicAdd(&d.ctr->row_alloc[nxt], (unsigned)incl);
+    // rows in the low word, bonds in the high word: the rows placed in a
+    // step number at most the capacity plus kstash per particle, far below
+    // 2^32, so the low word never carries
+    unsigned long long base = 0ull;
+    if (lane == 31 && incl)
+        base = atomicAdd(reinterpret_cast<unsigned long long*>(&d.ctr->alloc[nxt]),
+                         (unsigned long long)incl | ((unsigned long long)inclb << 32));
     base = __shfl_sync(0xffffffffu, base, 31);
-    int start = __shfl_sync(0xffffffffu, base + incl - v, (int)(lane & ~(unsigned)(L - 1)));
+    const int src = (int)(lane & ~(unsigned)(L - 1));
+    const unsigned excl = __shfl_sync(0xffffffffu, incl - v, src);
+    const unsigned exclb = __shfl_sync(0xffffffffu, inclb - vb, src);
+    int start = (int)((unsigned)base + excl);
+    *bstart = (int)((unsigned)(base >> 32) + exclb);
     if (len > 0 && (long long)start + len > (long long)p.cap) {
         if (lane % L == 0) raise_error(d.ctr, kErrCapacity);
         start = 0;
@@ -421,37 +440,60 @@ __device__ __forceinline__ void add_incoming_entry(const DemDev& d, const DemPar
 // the host).  Contacts of scenes that do not step keep every field.
 template <int L>
 __device__ __forceinline__ void finish_row(const DemDev& d, const DemParams& p, int cur,
-                                           const RowJob& r, int start, int lane) {
+                                           const RowJob& r, int start, int bstart, int lane) {
     const ContactSoA o = d.c[cur];
     const ContactSoA w = d.c[cur ^ 1];
     const int32_t* st = d.stash + (size_t)r.i * p.kstash;
     const bool stepping = r.mode == kModeStep;
+    const bool init = r.mode == kModeInit;  // new contacts are bonds
+    const int hstart = start - bstart;
+    const long long last = (long long)p.cap - 1;
+    // the contact at row position pos, with nbb bonds before it in the row,
+    // in the type-ordered list
+    auto list_entry = [&](int pos, int nbb, bool bonded) {
+        const long long k = bonded ? (long long)bstart + nbb
+                                   : (long long)last - (hstart + (pos - start) - nbb);
+        if (k >= 0 && k < (long long)p.cap) d.tlist[k] = pos;
+    };
     for (int e = r.e0 + lane; e < r.e1; e += L) {
         if (!d.keep[e]) continue;
         const int j = o.cj[e];
         const uint32_t fl = o.fl[e];
-        int pos = start;
-        for (int q = r.e0; q < e; ++q) pos += d.keep[q];
-        for (int u = 0; u < r.nnew; ++u) pos += st[u] < j ? 1 : 0;
+        int pos = start, nbb = 0;
+        for (int q = r.e0; q < e; ++q) {
+            pos += d.keep[q];
+            nbb += (d.keep[q] && (o.fl[q] & kBonded)) ? 1 : 0;
+        }
+        for (int u = 0; u < r.nnew; ++u) {
+            const int before = st[u] < j ? 1 : 0;
+            pos += before;
+            if (init) nbb += before;
+        }
         w.ci[pos] = r.i;
         w.cj[pos] = j;
         w.fl[pos] = fl;
         w.src[pos] = stepping ? e : -1;
         if (!stepping)
             for (int f = 0; f < 15; ++f) w.f[f][pos] = o.f[f][e];
+        list_entry(pos, nbb, (fl & kBonded) != 0u);
     }
     for (int u = lane; u < r.nnew; u += L) {
         const int j = st[u];
-        int pos = start + u;
-        for (int q = r.e0; q < r.e1; ++q) pos += (d.keep[q] && o.cj[q] < j) ? 1 : 0;
+        int pos = start + u, nbb = init ? u : 0;
+        for (int q = r.e0; q < r.e1; ++q) {
+            const bool before = d.keep[q] && o.cj[q] < j;
+            pos += before ? 1 : 0;
+            nbb += (before && (o.fl[q] & kBonded)) ? 1 : 0;
+        }
         w.ci[pos] = r.i;
         w.cj[pos] = j;
-        w.fl[pos] = r.mode == kModeInit ? (kActive | kBonded) : kActive;
+        w.fl[pos] = init ? (kActive | kBonded) : kActive;
         w.src[pos] = -1;  // a new contact: zero carried state
         if (!stepping) {
 #pragma unroll
             for (int f = 0; f < 15; ++f) w.f[f][pos] = 0.0;
         }
+        list_entry(pos, nbb, init);
     }
 }
 
@@ -460,14 +502,14 @@ __device__ __forceinline__ void finish_row(const DemDev& d, const DemParams& p, 
 template <int L>
 __device__ __forceinline__ void emit_rows(const DemDev& d, const DemParams& p, int cur, bool active,
                                           const RowJob& r, int lane) {
-    int len = active ? r.len : 0;
-    const int start = place_rows<L>(d, p, cur ^ 1, len);
+    int len = active ? r.len : 0, bstart = 0;
+    const int start = place_rows<L>(d, p, cur ^ 1, len, active ? r.nb : 0, &bstart);
     if (!active) return;
     if (lane == 0) {
         d.row_start[cur ^ 1][r.i] = start;
         d.row_len[cur ^ 1][r.i] = len;
     }
-    if (len > 0) finish_row<L>(d, p, cur, r, start, lane);
+    if (len > 0) finish_row<L>(d, p, cur, r, start, bstart, lane);
 }
 
 // Checksum term of a candidate pair (i, j) for the inspection of the pair
@@ -560,7 +602,7 @@ __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p
     const int e0 = row.x;
     const int e1 = e0 + row.y;
     const bool cached = e1 - e0 <= kRowCache;
-    int nkeep = 0, ended = 0;
+    int nkeep = 0, ended = 0, nbond = 0;
     for (int e2 = e0 + lane; e2 < e1; e2 += kLanes) {
         const uint32_t fl = o.fl[e2];
         const int j = o.cj[e2];
@@ -589,8 +631,10 @@ __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p
         }
         d.keep[e2] = (uint8_t)keep;
         nkeep += keep;
+        nbond += (keep && (fl & kBonded)) ? 1 : 0;
     }
     nkeep = __reduce_add_sync(gmask, nkeep);
+    nbond = __reduce_add_sync(gmask, nbond);
     ended = __reduce_add_sync(gmask, ended);
     __syncwarp(gmask);
 
@@ -702,6 +746,7 @@ __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p
     job.e1 = e1;
     job.nnew = sh.nnew;
     job.len = nkeep + job.nnew;
+    job.nb = nbond + (init ? job.nnew : 0);  // init_bonds!: every new contact is a bond
 }
 
 // cp_list membership of the pair (i, j), i < j, from the current positions:
@@ -750,7 +795,7 @@ __device__ __forceinline__ void list_particle(const DemDev& d, const DemParams& 
     const ContactSoA o = d.c[cur];
     if (lane == 0) sh[g].nnew = 0;
     const bool cached = e1 - e0 <= kRowCache;
-    int nkeep = 0, ended = 0;
+    int nkeep = 0, ended = 0, nbond = 0;
     for (int e2 = e0 + lane; e2 < e1; e2 += kVLanes) {
         const uint32_t fl = o.fl[e2];
         const int j = o.cj[e2];
@@ -773,8 +818,10 @@ __device__ __forceinline__ void list_particle(const DemDev& d, const DemParams& 
         }
         d.keep[e2] = (uint8_t)keep;
         nkeep += keep;
+        nbond += (keep && (fl & kBonded)) ? 1 : 0;
     }
     nkeep = __reduce_add_sync(gmask, nkeep);
+    nbond = __reduce_add_sync(gmask, nbond);
     ended = __reduce_add_sync(gmask, ended);
     __syncwarp(gmask);
     int32_t* stash = d.stash + (size_t)i * p.kstash;
@@ -832,6 +879,7 @@ __device__ __forceinline__ void list_particle(const DemDev& d, const DemParams& 
     job.e1 = e1;
     job.nnew = sh[g].nnew;
     job.len = nkeep + job.nnew;
+    job.nb = nbond;
 }
 
 // The list update of one particle by one lane (the narrow layout): the same
@@ -846,7 +894,7 @@ template <bool MULTI>
 __device__ __forceinline__ void list_particle1(const DemDev& d, const DemParams& p, int cur, int i,
                                                int e0, int e1, int nv, bool frozen, RowJob& job) {
     const ContactSoA o = d.c[cur];
-    int nkeep = 0, ended = 0;
+    int nkeep = 0, ended = 0, nbond = 0;
     for (int e = e0; e < e1; ++e) {
         const uint32_t fl = o.fl[e];
         int keep;
@@ -868,6 +916,7 @@ __device__ __forceinline__ void list_particle1(const DemDev& d, const DemParams&
         }
         d.keep[e] = (uint8_t)keep;
         nkeep += keep;
+        nbond += (keep && (fl & kBonded)) ? 1 : 0;
     }
     int32_t* stash = d.stash + (size_t)i * p.kstash;
     int nnew = 0;
@@ -914,6 +963,7 @@ __device__ __forceinline__ void list_particle1(const DemDev& d, const DemParams&
     job.e1 = e1;
     job.nnew = nnew;
     job.len = nkeep + nnew;
+    job.nb = nbond;
 }
 
 // The neighbour-list update with one lane per particle: in large scenes with
@@ -983,7 +1033,7 @@ __device__ __forceinline__ void list_phase(const DemDev& d, const DemParams& p, 
     const int gwarp = (int)(threadIdx.x >> 5) * (32 / kVLanes);
     // contacts in the current buffer: fixed while this kernel runs (rows are
     // placed in the other buffer), so every thread takes the same branch
-    const long long ncur = (long long)__ldcg(&d.ctr->row_alloc[cur]);
+    const long long ncur = (long long)__ldcg(&d.ctr->alloc[cur].rows);
     if (p.n > gridDim.x * (kThreads / kVLanes) && 4 * ncur < (long long)p.n) {
         const int gw = g - gwarp;  // the group within the warp, 0..7
         for (int base = blockIdx.x * kThreads + (int)(threadIdx.x & ~31u); base < p.n;
@@ -1824,14 +1874,25 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
     d.contrib[8 * cap + c] = (double)mj.z;
 }
 
+// Threads take the contacts in the order of the type-ordered list that the
+// rows' placement wrote (bonds first, then the others, the second part
+// starting on a warp boundary), so that a warp runs one of the two force
+// laws: a warp with both would run both in turn on the FP64 pipe.
 template <typename T, bool MULTI, bool TAB = false>
 __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, int nxt) {
-    const int C = min((int)d.ctr->row_alloc[nxt], p.cap);
+    const RowCounter a = d.ctr->alloc[nxt];
+    const int C = min((int)a.rows, p.cap);
+    const int NB = min((int)a.bonds, C);
+    const int NBw = (NB + 31) & ~31;
+    const int total = NBw + (C - NB);
     const ContactSoA w = d.c[nxt];
     const ContactSoA o = d.c[nxt ^ 1];
     const int stride = gridDim.x * blockDim.x;
     const size_t cap = (size_t)p.cap;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += stride) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        if (t >= NB && t < NBw) continue;
+        const int c = t < NB ? d.tlist[t] : d.tlist[cap - 1 - (size_t)(t - NBw)];
+        if ((unsigned)c >= (unsigned)C) continue;  // only after a capacity overflow
         const uint32_t fl = w.fl[c];
         const int i = w.ci[c], j = w.cj[c];
         const int sc = slot_scene<MULTI>(d, i);
@@ -2018,7 +2079,8 @@ struct WallK {
 };
 // resolve_wall! for one particle and one wall (src/kernels.jl:317-426): adds
 // the wall's force and moment to F, M and updates the wall contact's shear
-// history (*sx, *sy, *sz; zero when not touching).  An FP32 screen on the
+// history (*sx, *sy, *sz; zero when not touching); `count`: this thread adds
+// to the scene's warning counters.  An FP32 screen on the
 // step's starting position (pos32, within 2^-24 of the FP64 one per
 // coordinate) skips the exact test when |n·x - d| exceeds r by a margin that
 // covers its rounding.
@@ -2026,7 +2088,8 @@ __device__ __forceinline__ void wall_contact(const DemDev& d, int sc, const Wall
                                              float4 p32, float r32, double x, double y, double z,
                                              double vx, double vy, double vz, double wx, double wy,
                                              double wz, double r, double m, double* wsx,
-                                             double* wsy, double* wsz, double F[3], double M[3]) {
+                                             double* wsy, double* wsz, double F[3], double M[3],
+                                             bool count = true) {
     bool wall_near;
     {
         const float4 q = p32;
@@ -2061,8 +2124,8 @@ __device__ __forceinline__ void wall_contact(const DemDev& d, int sc, const Wall
         const double root = sqrt(m * sq);
         const double gn = W.cgn * root;
         const double gt = W.cgt * root;
-        if (gn < 0) atomicAdd(&d.sctr[sc].warn_damp, 1ull);
-        if (gt < 0) atomicAdd(&d.sctr[sc].warn_damp, 1ull);
+        if (count && gn < 0) atomicAdd(&d.sctr[sc].warn_damp, 1ull);
+        if (count && gt < 0) atomicAdd(&d.sctr[sc].warn_damp, 1ull);
         double sx = *wsx + vcx * 0.0, sy = *wsy + vcy * dt, sz = *wsz + vcz * dt;
         const double F1 = -kn * gap - gn * vcx;
         const double Ftx = -kt * sx, Fty = -kt * sy, Ftz = -kt * sz;
@@ -2102,7 +2165,7 @@ template <bool MULTI, bool F32, bool TAB = false>
 __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams& p, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nxt = cur ^ 1;
-    if (i == 0) d.ctr->row_alloc[cur] = 0u;  // the free buffer is next step's target
+    if (i == 0) d.ctr->alloc[cur] = RowCounter{0u, 0u};  // the free buffer is next step's target
     // the end-of-step rebuild-flag work of every scene (see scene_flags_one):
     // it only ORs into the next flags, as the particles' skin test does
     for (int s = i; s < p.ns; s += gridDim.x * blockDim.x) scene_flags_one<MULTI>(d, p, cur, s);
@@ -2250,6 +2313,228 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
     d.tz[i] = M[2];
 }
 
+// ---------------------------------------------------------------------------
+// The same integration with four lanes per particle, for scenes that leave
+// most of the GPU idle at one thread per particle (there the dependent gather
+// loads and FP64 chains of each thread set the time).  Lane q = 0, 1, 2 owns
+// component q of the force and moment sums and of the position, velocity and
+// spin updates; lane 3 repeats lane 2's component work without storing it and
+// owns the quaternion's real part.  Each component goes through the same
+// operations in the same order as in integrate_body, so the results are
+// bit-identical to it; the four lanes exchange components by shuffles.
+
+template <typename P>
+__device__ __forceinline__ P pick3(int q, P a, P b, P c) {
+    return q == 0 ? a : (q == 1 ? b : c);
+}
+template <typename T, int N>
+__device__ __forceinline__ void add_incoming_component(const T* cf, const T* cmj, int2 (&v)[N],
+                                                       int nin, T& F, T& M) {
+    sort_by_owner<N>(v);
+    T gf[N], gm[N];
+#pragma unroll
+    for (int u = 0; u < N; ++u) {
+        if (u < nin) {
+            gf[u] = cf[v[u].x];
+            gm[u] = cmj[v[u].x];
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < N; ++u) {
+        if (u < nin) {
+            F += -gf[u];
+            M += gm[u];
+        }
+    }
+}
+// component qc of gather(): the particle's own row, then its incoming
+// contacts ordered by owner index
+template <typename T>
+__device__ __forceinline__ void gather_component(const DemDev& d, const DemParams& p, int i,
+                                                 int c0, int len, int nin, int qc, T& F, T& M) {
+    const size_t cap = (size_t)p.cap;
+    const T* cb = contrib_of<T>(d);
+    const T* cf = cb + (size_t)qc * cap;         // force on the owner
+    const T* cmi = cb + (size_t)(3 + qc) * cap;  // the owner's moment
+    const T* cmj = cb + (size_t)(6 + qc) * cap;  // the partner's moment
+    nin = nin < p.kin ? nin : p.kin;
+    nin = nin < kMaxIncoming ? nin : kMaxIncoming;
+    const int2* il = d.in_list + (size_t)i * p.kin;
+    int2 v4[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v4[u] = u < nin ? il[u] : make_int2(0, 0x7fffffff);
+    const int c1 = min(c0 + len, p.cap);
+    int c = c0;
+    for (; c + 1 < c1; c += 2) {
+        const T a0 = cf[c], a1 = cmi[c], b0 = cf[c + 1], b1 = cmi[c + 1];
+        F += a0;
+        M += a1;
+        F += b0;
+        M += b1;
+    }
+    if (c < c1) {
+        F += cf[c];
+        M += cmi[c];
+    }
+    if (nin <= 4) {
+        add_incoming_component<T, 4>(cf, cmj, v4, nin, F, M);
+    } else if (nin <= 8) {
+        int2 v8[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v8[u] = u < 4 ? v4[u] : (u < nin ? il[u] : make_int2(0, 0x7fffffff));
+        add_incoming_component<T, 8>(cf, cmj, v8, nin, F, M);
+    } else {
+        int2 inc[kMaxIncoming];
+        for (int u = 0; u < nin; ++u) {
+            const int2 v = il[u];
+            int b = u - 1;
+            while (b >= 0 && inc[b].y > v.y) {
+                inc[b + 1] = inc[b];
+                --b;
+            }
+            inc[b + 1] = v;
+        }
+        for (int u = 0; u < nin; ++u) {
+            const int cc = inc[u].x;
+            F += -cf[cc];
+            M += cmj[cc];
+        }
+    }
+}
+
+template <bool MULTI, bool F32, bool TAB = false>
+__device__ __forceinline__ void integrate_lanes(const DemDev& d, const DemParams& p, int cur) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t >> 2, q = t & 3, qc = q < 3 ? q : 2;
+    const int nxt = cur ^ 1;
+    if (t == 0) d.ctr->alloc[cur] = RowCounter{0u, 0u};
+    for (int s = t; s < p.ns; s += gridDim.x * blockDim.x) scene_flags_one<MULTI>(d, p, cur, s);
+    if (i >= p.n) return;  // the four lanes of a particle leave together
+    const unsigned gmask = 0xFu << (lane_id() & 28u);
+    const int sc = slot_scene<MULTI>(d, i);
+    if (MULTI && (sc < 0 || d.sp[sc].mode != kModeStep)) {
+        if (q == 0) d.in_cnt[i] = 0;
+        return;
+    }
+    const SceneParams& S = scene_rec<MULTI>(d, p, sc);
+    // every lane loads the whole particle state (the four lanes read the same
+    // words); nothing is stored before the __syncwarp below
+    const int row0 = d.row_start[nxt][i], rlen = d.row_len[nxt][i], nin = d.in_cnt[i];
+    const double x = d.px[i], y = d.py[i], z = d.pz[i];
+    const double vx = d.vx[i], vy = d.vy[i], vz = d.vz[i];
+    const double wx = d.wx[i], wy = d.wy[i], wz = d.wz[i];
+    const double r = d.r[i], m = d.m[i];
+    const double invm = d.inv_m[i], ii = d.inv_inertia[i];
+    const double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
+    const float4 p32 = d.pos32[i], xr = d.xref[i];
+    const float r32 = d.rm32[i].z;
+    const double xq = pick3(qc, x, y, z), vq = pick3(qc, vx, vy, vz), wq = pick3(qc, wx, wy, wz);
+    double Fq = 0.0, Mq = 0.0;
+    if constexpr (F32) {
+        float Ff = 0.0f, Mf = 0.0f;
+        gather_component<float>(d, p, i, row0, rlen, nin, qc, Ff, Mf);
+        Fq = f2d(Ff);
+        Mq = f2d(Mf);
+    } else {
+        gather_component<double>(d, p, i, row0, rlen, nin, qc, Fq, Mq);
+    }
+    __syncwarp(gmask);  // the group's loads are done before lane 0 stores
+    if (q == 0) d.in_cnt[i] = 0;
+    const double dt = S.dt;
+    // resolve_wall!: every lane evaluates the wall contact (the same values)
+    // and keeps its component; lane 0 counts warnings and stores the shear
+    auto wall = [&](const WallK& K, double* gsx, double* gsy, double* gsz) {
+        double sx = *gsx, sy = *gsy, sz = *gsz;
+        double F3[3] = {qc == 0 ? Fq : 0.0, qc == 1 ? Fq : 0.0, qc == 2 ? Fq : 0.0};
+        double M3[3] = {qc == 0 ? Mq : 0.0, qc == 1 ? Mq : 0.0, qc == 2 ? Mq : 0.0};
+        wall_contact(d, sc, K, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r, m, &sx, &sy, &sz,
+                     F3, M3, q == 0);
+        Fq = pick3(qc, F3[0], F3[1], F3[2]);
+        Mq = pick3(qc, M3[0], M3[1], M3[2]);
+        __syncwarp(gmask);  // every lane has read the old shear
+        if (q == 0) {
+            *gsx = sx;
+            *gsy = sy;
+            *gsz = sz;
+        }
+    };
+    if constexpr (TAB) {
+        const MatTables& T = *d.mt;
+        const int a = d.mid[i];
+        for (int wl = 0; wl < T.nwall; ++wl) {
+            const WallConst& W = T.wall[wl];
+            const WallK K{W.wn, W.wd, W.wR, W.wRinv, W.f_wn, W.f_wc0, W.mu[a], W.Ys[a], W.Gs[a],
+                          W.cgn[a], W.cgt[a]};
+            const size_t o = (size_t)wl * p.wstride + i;
+            wall(K, d.wsx + o, d.wsy + o, d.wsz + o);
+        }
+    } else if (S.has_wall) {
+        const WallK K{S.wn, S.wd, S.wR, S.wRinv, S.f_wn, S.f_wc0, S.pw_mu, S.pw_Ys, S.pw_Gs,
+                      S.pw_cgn, S.pw_cgt};
+        wall(K, d.wsx + i, d.wsy + i, d.wsz + i);
+    }
+    // apply_body_force!
+    if (nonzero_bits(S.grav[qc])) Fq += S.grav[qc] * m;
+    if (nonzero_bits(S.damping)) {
+        const double dF = -S.damping * fabs(Fq) * jl_sign(vq);
+        const double dM = -S.damping * fabs(Mq) * jl_sign(wq);
+        Fq += dF;
+        Mq += dM;
+    }
+    // update!
+    const double aq = Fq * invm;
+    const double hdt2 = S.hdt2;
+    const double pq1 = xq + vq * dt + aq * hdt2;
+    if (q < 3) pick3(qc, d.px, d.py, d.pz)[i] = pq1;
+    {
+        const float fq = d2f(pq1 - S.dmin[qc]);
+        const float fx = __shfl_sync(gmask, fq, 0, 4), fy = __shfl_sync(gmask, fq, 1, 4),
+                    fz = __shfl_sync(gmask, fq, 2, 4);
+        if (q == 0) d.pos32[i] = make_float4(fx, fy, fz, reach32(fx, fy, fz, r32));
+        const bool moved = S.f_half_skin > 0.0f && left_skin(S, fx, fy, fz, xr);
+        const unsigned am = __activemask();
+        const unsigned peers = __match_any_sync(am, moved ? sc : -1);
+        if (moved && lane_id() == (unsigned)(__ffs(peers) - 1) && d.sflags[nxt][sc] == 0u)
+            atomicOr(&d.sflags[nxt][sc], 1u);
+    }
+    if (q < 3) pick3(qc, d.vx, d.vy, d.vz)[i] = vq + aq * dt;
+    // the quaternion: lanes 0, 1, 2 own x, y, z and lane 3 owns w
+    const bool spinless = (__double_as_longlong(wx) | __double_as_longlong(wy) |
+                           __double_as_longlong(wz)) == 0ll;
+    const bool identity = spinless && __double_as_longlong(qw) == 0x3ff0000000000000ll &&
+                          (__double_as_longlong(qx) | __double_as_longlong(qy) |
+                           __double_as_longlong(qz)) == 0ll;
+    if (!identity) {
+        double nc = q == 3 ? qw : pick3(q, qx, qy, qz);
+        if (!(spinless && finite_not_negzero(qw) && finite_not_negzero(qx) &&
+              finite_not_negzero(qy) && finite_not_negzero(qz))) {
+            const double hx = half_exact(wx), hy = half_exact(wy), hz = half_exact(wz);
+            // integrate_body's four FMA chains, operands chosen per lane
+            const double a1 = q == 3 ? -qx : qw;
+            const double b1 = q == 3 ? hx : pick3(q, hx, hy, hz);
+            const double a2 = q == 3 ? -qy : (q == 0 ? qy : qx);
+            const double b2 = q == 3 ? hy : pick3(q, hz, hz, hy);
+            const double a3 = q == 3 ? -qz : pick3(q, -qz, qz, -qy);
+            const double b3 = q == 3 ? hz : pick3(q, hy, hx, hx);
+            nc = __fma_rn(a3, b3, __fma_rn(a2, b2, __fma_rn(a1, b1, nc)));
+        }
+        const double nx = __shfl_sync(gmask, nc, 0, 4), ny = __shfl_sync(gmask, nc, 1, 4),
+                     nz = __shfl_sync(gmask, nc, 2, 4), nw = __shfl_sync(gmask, nc, 3, 4);
+        const double inq = rsqrt(__fma_rn(nz, nz, __fma_rn(ny, ny, __fma_rn(nx, nx, nw * nw))));
+        (q == 3 ? d.qw : pick3(q, d.qx, d.qy, d.qz))[i] = nc * inq;
+    }
+    const bool torque_free = __all_sync(gmask, __double_as_longlong(Mq) == 0ll);
+    if (!(torque_free && product_finite(ii, dt) && not_negzero(wx) && not_negzero(wy) &&
+          not_negzero(wz))) {
+        const double iidt = ii * dt;
+        if (q < 3) pick3(qc, d.wx, d.wy, d.wz)[i] = __fma_rn(Mq, iidt, wq);
+    }
+    if (q < 3) {
+        pick3(qc, d.fx, d.fy, d.fz)[i] = Fq;
+        pick3(qc, d.tx, d.ty, d.tz)[i] = Mq;
+    }
+}
+
 // The integrator with the compiler's register choice (FP64 force mode), and
 // in the FP32 force mode with a budget for three 256-thread blocks per SM:
 // its FP64 work per particle is small enough that more resident warps hide
@@ -2267,6 +2552,16 @@ template <bool MULTI>
 __global__ void __launch_bounds__(kThreads, 3) k_integrate3(DemDev d, DemParams p, int cur) {
     dep_begin(p.dep == 2);
     integrate_body<MULTI, true>(d, p, cur);
+}
+// four lanes per particle (integrate_lanes)
+template <bool MULTI, bool F32>
+__global__ void __launch_bounds__(kThreads) k_integrate_v(DemDev d, DemParams p, int cur) {
+    dep_begin(p.dep == 2);
+    integrate_lanes<MULTI, F32>(d, p, cur);
+}
+__global__ void __launch_bounds__(kThreads) k_integrate_tab_v(DemDev d, DemParams p, int cur) {
+    dep_begin(p.dep == 2);
+    integrate_lanes<false, false, true>(d, p, cur);
 }
 
 // ---- inspection kernels (dem_debug_broadphase) -------------------------------
@@ -2473,6 +2768,22 @@ void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
                       const LaunchShape& sh, cudaStream_t s) {
     if (p.n == 0) return;
     const int block = clamp_block(sh.integrate_block);
+    // four lanes per particle while one thread per particle would give the
+    // SMs at most one warp each
+    const bool lanes = sh.integrate_lanes == 4 ||
+                       (sh.integrate_lanes == 0 && (long long)p.n <= (long long)p.sms * 32);
+    if (lanes) {
+        const int nb = blocks_for(4LL * p.n, block);
+        if (p.tab)
+            launch(p.dep != 0, k_integrate_tab_v, nb, block, s, d, p, cur);
+        else if (p.precision == 1)
+            launch(p.dep != 0, multi ? k_integrate_v<true, true> : k_integrate_v<false, true>, nb,
+                   block, s, d, p, cur);
+        else
+            launch(p.dep != 0, multi ? k_integrate_v<true, false> : k_integrate_v<false, false>,
+                   nb, block, s, d, p, cur);
+        return;
+    }
     const int nb = blocks_for(p.n, block);
     if (p.tab)
         launch(p.dep != 0, k_integrate_tab, nb, block, s, d, p, cur);
@@ -2487,7 +2798,7 @@ void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
 // Active entries of a slot's row (its contacts (i, j), j > i, sorted by j).
 __device__ __forceinline__ void io_row(const DemDev& d, int cur, int cap, int i, int& e0,
                                        int& e1) {
-    const int C = min((int)d.ctr->row_alloc[cur], cap);
+    const int C = min((int)d.ctr->alloc[cur].rows, cap);
     e0 = max(d.row_start[cur][i], 0);
     e1 = min(d.row_start[cur][i] + d.row_len[cur][i], C);
 }

@@ -185,12 +185,13 @@ def test_tuning_knobs_keep_results(gpu):
         ids = [a.add(cube.cfg, cube.particles), a.add(pour.cfg, pour.particles, init_bonds=False)]
         a.step(15)
         a.set_launch_shape(force_block=128, force_grid=152 * 4, compact_block=64,
-                           compact_grid=152 * 2, integrate_block=128, list_lanes=1)
+                           compact_grid=152 * 2, integrate_block=128, list_lanes=1,
+                           integrate_lanes=1)
         a.set_cell_factor(0.4)
         a.step(15)
         a.set_cell_factor(0.7, scene=ids[0])
         a.set_launch_shape(force_block=256, force_grid=152 * 32, integrate_block=256,
-                           dependent_launch=2, list_lanes=4)
+                           dependent_launch=2, list_lanes=4, integrate_lanes=4)
         a.step(10)
         for sid, ref, name in zip(ids, refs, ("cube", "pour")):
             assert_same(a, sid, ref, f"retuned {name}")
@@ -200,7 +201,7 @@ def test_tuning_knobs_keep_results(gpu):
     g.set_launch_shape(force_block=96, force_grid=100, compact_grid=50, integrate_block=64,
                        dependent_launch=1)
     g.simulate(10)
-    g.set_launch_shape(dependent_launch=2, list_lanes=1)
+    g.set_launch_shape(dependent_launch=2, list_lanes=1, integrate_lanes=1)
     g.simulate(10)
     p, c = g.particles(), g.contacts()
     for k in PARTICLE_KEYS:

@@ -369,6 +369,59 @@ def test_list_layouts_bit_identical(gpu):
             (s4["contacts_created"], s4["contacts_ended"])
 
 
+def run_layouts(cfg, p, steps, bonded, knob, values=(1, 4), precision="fp64", tables=None):
+    """Runs the scene once per value of a launch-shape knob; returns each run's
+    particles, contacts and stats."""
+    outs = []
+    for v in values:
+        g = GlobalData(cfg, p, precision=precision, tables=tables)
+        g.set_launch_shape(**{knob: v})
+        if bonded:
+            g.initialize()
+        g.simulate(steps)
+        outs.append((g.particles(), g.contacts(), g.stats()))
+        g.close()
+    return outs
+
+
+def assert_runs_identical(outs, what):
+    (p0, c0, s0), rest = outs[0], outs[1:]
+    for p1, c1, s1 in rest:
+        for k in p0:
+            np.testing.assert_array_equal(p0[k], p1[k], err_msg=f"{what} {k}")
+        for k in c0:
+            np.testing.assert_array_equal(c0[k], c1[k], err_msg=f"{what} contacts {k}")
+        for k in ("bonds_broken", "contacts_created", "contacts_ended", "warn_gap",
+                  "warn_damping", "error"):
+            assert s0.get(k) == s1.get(k), (what, k)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_integrate_layouts_bit_identical(gpu, precision):
+    """The integrator with one lane per particle and with four (one per
+    vector component) gives the same results bit for bit: a bonded cube's
+    wall impact (wall contacts, spin, bonds breaking), a damped cube, and a
+    polydisperse cloud under gravity with damping thrown at the floor."""
+    cube = scenes.bonded_cube(8, speed=30.0, steps=0, seed=2)
+    outs = run_layouts(cube.cfg, cube.particles, 1000, True, "integrate_lanes",
+                       precision=precision)  # bonds start to break near step 900
+    assert_runs_identical(outs, f"cube {precision}")
+    assert outs[0][2]["bonds_broken"] > 0
+    assert np.count_nonzero(np.any(outs[0][0]["wall_shear"] != 0, axis=1)) > 0
+    damped = cube.cfg.replace(global_damping=0.2)
+    assert_runs_identical(run_layouts(damped, cube.particles, 150, True, "integrate_lanes",
+                                      precision=precision), f"damped cube {precision}")
+    # a wall restitution above 1 gives negative wall damping, which is
+    # counted once per wall contact and step, whatever the layout
+    cfg, p = random_cloud(3000, (0.05, 0.05, 0.05), 0.0008, 0.0015, seed=15, v=0.5,
+                          cfg_kw=dict(global_damping=0.3, pp_coefficient_friction=0.3,
+                                      pw_coefficient_restitution=1.2))
+    p.vel[:, 2] -= 1.0
+    outs = run_layouts(cfg, p, 150, False, "integrate_lanes", precision=precision)
+    assert_runs_identical(outs, f"cloud {precision}")
+    assert outs[0][2]["warn_damping"] > 0
+
+
 def test_short_horizon_cube(gpu):
     sc = scenes.bonded_cube(10, speed=10.0, steps=0, seed=1)
     g, o = both(sc.cfg, sc.particles)

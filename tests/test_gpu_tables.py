@@ -9,8 +9,9 @@ from oracle.oracle import OracleScene
 from taichi_dem_julia_port_gb300 import GlobalData, Material, Surface, Tables, Wall, scenes
 from taichi_dem_julia_port_gb300._abi import DEM_ERR_INVALID, DemError
 from tests.conftest import assert_rows_close
-from tests.test_gpu_parity import (RTOL_HORIZON, RTOL_STEP, bonded_set, compare_state,
-                                   copy_state, pair_set, random_cloud)
+from tests.test_gpu_parity import (RTOL_HORIZON, RTOL_STEP, assert_runs_identical, bonded_set,
+                                   compare_state, copy_state, pair_set, random_cloud,
+                                   run_layouts)
 
 pytestmark = pytest.mark.gpu
 
@@ -115,6 +116,21 @@ def test_two_materials_bonded_cube_two_walls(gpu):
     assert so["bonds_broken"] > 0 and sg["bonds_broken"] == so["bonds_broken"]
     assert pair_set(g.contacts()) == pair_set(o.contacts())
     g.close()
+
+
+def test_tables_integrate_layouts_bit_identical(gpu):
+    """A two-material cube against two walls: the integrator with one lane
+    per particle and with four give the same results bit for bit."""
+    sc = scenes.bonded_cube(8, speed=30.0, steps=0, seed=12)
+    cfg = sc.cfg
+    z = sc.particles.pos[:, 2]
+    gm = np.round((z - z.min()) / 0.02).astype(int) % 2
+    nrm = np.array([-1.0, 0.0, -1.0]) / np.sqrt(2.0)
+    t = two_material_tables(gm, [Wall(list(cfg.wall_normal), cfg.wall_distance, 2),
+                                 Wall(nrm.tolist(), 0.0105, 2)])
+    outs = run_layouts(cfg, sc.particles, 300, True, "integrate_lanes", tables=t)
+    assert_runs_identical(outs, "two-material cube")
+    assert outs[0][2]["bonds_broken"] > 0
 
 
 def test_tables_reject_fp32_and_bad_indices(gpu):
