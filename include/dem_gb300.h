@@ -301,7 +301,9 @@ typedef struct DemLaunchShape {
     int32_t integrate_block;
     int32_t detect_blocks_per_sm; /* register budget of the pair search and the
                                    * neighbour-list update: 3 or 4 (0 = 4)          */
-    int32_t force_blocks_per_sm;  /* FP32 force kernel: 0 (compiler's choice) or 4     */
+    int32_t force_blocks_per_sm;  /* FP32 force kernel: 0 (compiler's choice) or 4
+                                   * (register budget for four 256-thread blocks per
+                                   * SM); default 4 for a single scene, 0 for an arena */
     int32_t dependent_launch;     /* a step's kernels: 0 ordinary launches; 1
                                    * programmatic dependent launches (each may be
                                    * scheduled while its predecessor finishes); 2 the
@@ -309,9 +311,11 @@ typedef struct DemLaunchShape {
     int32_t list_lanes;           /* neighbour-list update: lanes per particle, 1 or 4
                                    * (0 = 1 when the particles outnumber half the
                                    * launch's threads, else 4)                        */
-    int32_t integrate_lanes;      /* integrator: lanes per particle, 1 or 4 (0 = 4
-                                   * while the particles number at most 32 per SM,
-                                   * else 1)                                          */
+    int32_t integrate_lanes;      /* integrator: threads per particle, 1 or 4 (one
+                                   * per force component and one for the walls and
+                                   * the quaternion, in four warps per 32 particles);
+                                   * 0 = 4 while the particles number at most 256 per
+                                   * SM, else 1.  Results do not change.              */
 } DemLaunchShape;
 
 int dem_set_launch_shape(DemHandle* h, const DemLaunchShape* shape);

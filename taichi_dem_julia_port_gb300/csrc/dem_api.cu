@@ -518,7 +518,13 @@ LaunchShape default_shape(const DemHandle* h) {
     };
     const int64_t n = h->multi ? INT64_MAX / 16 : h->n_cap;
     const int ib = block_for(n, 4), fb = block_for(3 * n, 8), cb = block_for(4 * n, 4);
-    return LaunchShape{fb, h->sm_count * 16, cb, h->sm_count * 16, ib, 4, 0, 0, 0, 0};
+    // a single scene's FP32 force kernel with the register budget for four
+    // 256-thread blocks per SM (64 registers, a few bytes of spills): with
+    // the compiler's choice (74 registers, three blocks) the 2,000,000-sphere
+    // bed's force pass measured 215 us instead of 171 us.  The arena's keeps
+    // the compiler's choice (the autotuner tries both).
+    return LaunchShape{fb, h->sm_count * 16, cb, h->sm_count * 16, ib, 4, h->multi ? 0 : 4,
+                       0, 0, 0};
 }
 
 int init_handle(DemHandle* h) {

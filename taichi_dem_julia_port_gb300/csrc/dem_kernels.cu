@@ -1874,25 +1874,33 @@ __device__ __forceinline__ void contact_one(const DemDev& d, const SceneParams& 
     d.contrib[8 * cap + c] = (double)mj.z;
 }
 
-// Threads take the contacts in the order of the type-ordered list that the
-// rows' placement wrote (bonds first, then the others, the second part
-// starting on a warp boundary), so that a warp runs one of the two force
-// laws: a warp with both would run both in turn on the FP64 pipe.
+// With bonds and other contacts both present, threads take the contacts in
+// the order of the type-ordered list that the rows' placement wrote (bonds
+// first, then the others, the second part starting on a warp boundary), so
+// that a warp runs one of the two force laws: a warp with both runs both in
+// turn on the FP64 pipe, which spends the same time on a warp instruction
+// whatever the number of active lanes.  With one type only, thread t takes
+// contact t (no list read).  The list entry of a thread's next contact is
+// read one iteration ahead, so that its latency overlaps the current one.
 template <typename T, bool MULTI, bool TAB = false>
 __device__ __forceinline__ void force_body(const DemDev& d, const DemParams& p, int nxt) {
     const RowCounter a = d.ctr->alloc[nxt];
     const int C = min((int)a.rows, p.cap);
     const int NB = min((int)a.bonds, C);
-    const int NBw = (NB + 31) & ~31;
-    const int total = NBw + (C - NB);
+    const bool mixed = NB > 0 && NB < C;
+    const int NBw = mixed ? (NB + 31) & ~31 : NB;
+    const int total = mixed ? NBw + (C - NB) : C;
     const ContactSoA w = d.c[nxt];
     const ContactSoA o = d.c[nxt ^ 1];
     const int stride = gridDim.x * blockDim.x;
     const size_t cap = (size_t)p.cap;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-        if (t >= NB && t < NBw) continue;
-        const int c = t < NB ? d.tlist[t] : d.tlist[cap - 1 - (size_t)(t - NBw)];
-        if ((unsigned)c >= (unsigned)C) continue;  // only after a capacity overflow
+        int c = t;
+        if (mixed) {
+            if (t >= NB && t < NBw) continue;  // padding up to the warp boundary
+            c = t < NB ? d.tlist[t] : d.tlist[cap - 1 - (size_t)(t - NBw)];
+            if ((unsigned)c >= (unsigned)C) continue;  // only after a capacity overflow
+        }
         const uint32_t fl = w.fl[c];
         const int i = w.ci[c], j = w.cj[c];
         const int sc = slot_scene<MULTI>(d, i);
@@ -2077,19 +2085,19 @@ struct WallK {
     float f_wc0;
     double mu, Ys, Gs, cgn, cgt;
 };
-// resolve_wall! for one particle and one wall (src/kernels.jl:317-426): adds
-// the wall's force and moment to F, M and updates the wall contact's shear
-// history (*sx, *sy, *sz; zero when not touching); `count`: this thread adds
-// to the scene's warning counters.  An FP32 screen on the
+// resolve_wall! for one particle and one wall (src/kernels.jl:317-426):
+// whether the wall touches the particle and, if so, the wall's force g and
+// moment mw on it; updates the wall contact's shear history (*wsx, *wsy,
+// *wsz; zero when not touching); `count`: this thread adds to the scene's
+// warning counters.  An FP32 screen on the
 // step's starting position (pos32, within 2^-24 of the FP64 one per
 // coordinate) skips the exact test when |n·x - d| exceeds r by a margin that
 // covers its rounding.
-__device__ __forceinline__ void wall_contact(const DemDev& d, int sc, const WallK& W, double dt,
-                                             float4 p32, float r32, double x, double y, double z,
-                                             double vx, double vy, double vz, double wx, double wy,
-                                             double wz, double r, double m, double* wsx,
-                                             double* wsy, double* wsz, double F[3], double M[3],
-                                             bool count = true) {
+__device__ __forceinline__ bool wall_force(const DemDev& d, int sc, const WallK& W, double dt,
+                                           float4 p32, float r32, double x, double y, double z,
+                                           double vx, double vy, double vz, double wx, double wy,
+                                           double wz, double r, double m, double* wsx, double* wsy,
+                                           double* wsz, double g[3], double mw[3], bool count) {
     bool wall_near;
     {
         const float4 q = p32;
@@ -2102,7 +2110,7 @@ __device__ __forceinline__ void wall_contact(const DemDev& d, int sc, const Wall
         *wsx = 0.0;
         *wsy = 0.0;
         *wsz = 0.0;
-        return;
+        return false;
     }
     const double dotkn = __dadd_rn(__dadd_rn(__dmul_rn(x, W.wn[0]), __dmul_rn(y, W.wn[1])),
                                    __dmul_rn(z, W.wn[2]));
@@ -2145,19 +2153,37 @@ __device__ __forceinline__ void wall_contact(const DemDev& d, int sc, const Wall
         const double gx = -(Ri[0] * F1 + Ri[1] * F2 + Ri[2] * F3);
         const double gy = -(Ri[3] * F1 + Ri[4] * F2 + Ri[5] * F3);
         const double gz = -(Ri[6] * F1 + Ri[7] * F2 + Ri[8] * F3);
-        F[0] += gx;
-        F[1] += gy;
-        F[2] += gz;
-        M[0] += kiy * gz - kiz * gy;
-        M[1] += kiz * gx - kix * gz;
-        M[2] += kix * gy - kiy * gx;
+        g[0] = gx;
+        g[1] = gy;
+        g[2] = gz;
+        mw[0] = kiy * gz - kiz * gy;
+        mw[1] = kiz * gx - kix * gz;
+        mw[2] = kix * gy - kiy * gx;
         *wsx = sx;
         *wsy = sy;
         *wsz = sz;
-    } else {
-        *wsx = 0.0;
-        *wsy = 0.0;
-        *wsz = 0.0;
+        return true;
+    }
+    *wsx = 0.0;
+    *wsy = 0.0;
+    *wsz = 0.0;
+    return false;
+}
+// resolve_wall! adding the wall's force and moment to F, M
+__device__ __forceinline__ void wall_contact(const DemDev& d, int sc, const WallK& W, double dt,
+                                             float4 p32, float r32, double x, double y, double z,
+                                             double vx, double vy, double vz, double wx, double wy,
+                                             double wz, double r, double m, double* wsx,
+                                             double* wsy, double* wsz, double F[3], double M[3]) {
+    double g[3], mw[3];
+    if (wall_force(d, sc, W, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r, m, wsx, wsy, wsz, g,
+                   mw, true)) {
+        F[0] += g[0];
+        F[1] += g[1];
+        F[2] += g[2];
+        M[0] += mw[0];
+        M[1] += mw[1];
+        M[2] += mw[2];
     }
 }
 
@@ -2187,6 +2213,58 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
     const double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
     const float4 p32 = d.pos32[i], xr = d.xref[i];
     const float r32 = d.rm32[i].z;
+    // The wall contact of a single-wall scene and the quaternion depend only
+    // on the step's starting state: a single scene evaluates the wall before
+    // the gather, so that its FP64 work overlaps the gather's dependent loads
+    // (the sums are unchanged: the wall's force and moment are added after
+    // the gather)
+    bool wall_touch = false;
+    double wall_g[3], wall_m[3];
+    if constexpr (!TAB && !MULTI) {
+        if (S.has_wall) {
+            const WallK K{S.wn, S.wd, S.wR, S.wRinv, S.f_wn, S.f_wc0, S.pw_mu, S.pw_Ys, S.pw_Gs,
+                          S.pw_cgn, S.pw_cgt};
+            wall_touch = wall_force(d, sc, K, S.dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r,
+                                    m, d.wsx + i, d.wsy + i, d.wsz + i, wall_g, wall_m, true);
+        }
+    }
+    // 𝐪 + Δ𝐪 with Δ𝐪 = ½ 𝛚 ⊗ 𝐪 (no dt, as the reference), the ½ folded into
+    // 𝛚, as explicit FMA chains.  With 𝛚 = (+0, +0, +0) each fma(a, +0, c)
+    // (a finite) returns c unless c is -0, so for a finite 𝐪 without a -0
+    // component the chains return 𝐪 itself: a particle that does not spin
+    // skips them, with identical results.  The normalisation always runs.
+    // A spinless particle with the identity orientation (1, +0, +0, +0)
+    // keeps it: |𝐪|² = 1 exactly, rsqrt(1) = 1 (checked by
+    // dem_selftest_conversions) and 𝐪·1 = 𝐪, so nothing is computed or stored.
+    auto update_quaternion = [&]() {
+        double nw = qw, nx = qx, ny = qy, nz = qz;
+        const bool spinless = (__double_as_longlong(wx) | __double_as_longlong(wy) |
+                               __double_as_longlong(wz)) == 0ll;
+        const bool identity = spinless && __double_as_longlong(qw) == 0x3ff0000000000000ll &&
+                              (__double_as_longlong(qx) | __double_as_longlong(qy) |
+                               __double_as_longlong(qz)) == 0ll;
+        if (!identity) {
+            if (!(spinless && finite_not_negzero(qw) && finite_not_negzero(qx) &&
+                  finite_not_negzero(qy) && finite_not_negzero(qz))) {
+                const double hx = half_exact(wx), hy = half_exact(wy), hz = half_exact(wz);
+                nw = __fma_rn(-qz, hz, __fma_rn(-qy, hy, __fma_rn(-qx, hx, qw)));
+                nx = __fma_rn(-qz, hy, __fma_rn(qy, hz, __fma_rn(qw, hx, qx)));
+                ny = __fma_rn(qz, hx, __fma_rn(qx, hz, __fma_rn(qw, hy, qy)));
+                nz = __fma_rn(-qy, hx, __fma_rn(qx, hy, __fma_rn(qw, hz, qz)));
+            }
+            const double inq = rsqrt(__fma_rn(nz, nz, __fma_rn(ny, ny, __fma_rn(nx, nx, nw * nw))));
+            d.qw[i] = nw * inq;
+            d.qx[i] = nx * inq;
+            d.qy[i] = ny * inq;
+            d.qz[i] = nz * inq;
+        }
+    };
+    // a single scene evaluates it before the gather, so that its FP64 work
+    // overlaps the gather's loads (measured on the 2,000,000-sphere bed:
+    // integrate 238 -> 231 us); the arena keeps it after the update (there
+    // the early placement measured slower: 131 -> 142 us on the 256-scene
+    // batch)
+    if constexpr (!MULTI) update_quaternion();
     double F[3] = {0.0, 0.0, 0.0}, M[3] = {0.0, 0.0, 0.0};
     if constexpr (F32) {
         float Ff[3] = {0.0f, 0.0f, 0.0f}, Mf[3] = {0.0f, 0.0f, 0.0f};
@@ -2215,11 +2293,18 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
             wall_contact(d, sc, K, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r, m, d.wsx + o,
                          d.wsy + o, d.wsz + o, F, M);
         }
-    } else if (S.has_wall) {
-        const WallK K{S.wn, S.wd, S.wR, S.wRinv, S.f_wn, S.f_wc0, S.pw_mu, S.pw_Ys, S.pw_Gs,
-                      S.pw_cgn, S.pw_cgt};
-        wall_contact(d, sc, K, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r, m, d.wsx + i,
-                     d.wsy + i, d.wsz + i, F, M);
+    } else if constexpr (MULTI) {
+        if (S.has_wall) {
+            const WallK K{S.wn, S.wd, S.wR, S.wRinv, S.f_wn, S.f_wc0, S.pw_mu, S.pw_Ys, S.pw_Gs,
+                          S.pw_cgn, S.pw_cgt};
+            wall_contact(d, sc, K, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r, m,
+                         d.wsx + i, d.wsy + i, d.wsz + i, F, M);
+        }
+    } else if (wall_touch) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) F[q] += wall_g[q];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) M[q] += wall_m[q];
     }
     // apply_body_force!  A zero gravity component adds nothing: the force sum
     // starts at +0 and never becomes -0, so F + 0·m is F.
@@ -2265,35 +2350,7 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
     d.vx[i] = vx + ax * dt;
     d.vy[i] = vy + ay * dt;
     d.vz[i] = vz + az * dt;
-    // 𝐪 + Δ𝐪 with Δ𝐪 = ½ 𝛚 ⊗ 𝐪 (no dt, as the reference), the ½ folded into
-    // 𝛚, as explicit FMA chains.  With 𝛚 = (+0, +0, +0) each fma(a, +0, c)
-    // (a finite) returns c unless c is -0, so for a finite 𝐪 without a -0
-    // component the chains return 𝐪 itself: a particle that does not spin
-    // skips them, with identical results.  The normalisation always runs.
-    // A spinless particle with the identity orientation (1, +0, +0, +0)
-    // keeps it: |𝐪|² = 1 exactly, rsqrt(1) = 1 (checked by
-    // dem_selftest_conversions) and 𝐪·1 = 𝐪, so nothing is computed or stored.
-    double nw = qw, nx = qx, ny = qy, nz = qz;
-    const bool spinless = (__double_as_longlong(wx) | __double_as_longlong(wy) |
-                           __double_as_longlong(wz)) == 0ll;
-    const bool identity = spinless && __double_as_longlong(qw) == 0x3ff0000000000000ll &&
-                          (__double_as_longlong(qx) | __double_as_longlong(qy) |
-                           __double_as_longlong(qz)) == 0ll;
-    if (!identity) {
-        if (!(spinless && finite_not_negzero(qw) && finite_not_negzero(qx) &&
-              finite_not_negzero(qy) && finite_not_negzero(qz))) {
-            const double hx = half_exact(wx), hy = half_exact(wy), hz = half_exact(wz);
-            nw = __fma_rn(-qz, hz, __fma_rn(-qy, hy, __fma_rn(-qx, hx, qw)));
-            nx = __fma_rn(-qz, hy, __fma_rn(qy, hz, __fma_rn(qw, hx, qx)));
-            ny = __fma_rn(qz, hx, __fma_rn(qx, hz, __fma_rn(qw, hy, qy)));
-            nz = __fma_rn(-qy, hx, __fma_rn(qx, hy, __fma_rn(qw, hz, qz)));
-        }
-        const double inq = rsqrt(__fma_rn(nz, nz, __fma_rn(ny, ny, __fma_rn(nx, nx, nw * nw))));
-        d.qw[i] = nw * inq;
-        d.qx[i] = nx * inq;
-        d.qy[i] = ny * inq;
-        d.qz[i] = nz * inq;
-    }
+    if constexpr (MULTI) update_quaternion();
     // 𝛚 + 𝐌·I⁻¹dt: with 𝐌 = (+0, +0, +0) and a finite I⁻¹dt, fma(+0, I⁻¹dt, w)
     // is w unless w is -0, so a torque-free particle keeps its stored spin
     const bool torque_free = (__double_as_longlong(M[0]) | __double_as_longlong(M[1]) |
@@ -2314,14 +2371,19 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
 }
 
 // ---------------------------------------------------------------------------
-// The same integration with four lanes per particle, for scenes that leave
-// most of the GPU idle at one thread per particle (there the dependent gather
-// loads and FP64 chains of each thread set the time).  Lane q = 0, 1, 2 owns
-// component q of the force and moment sums and of the position, velocity and
-// spin updates; lane 3 repeats lane 2's component work without storing it and
-// owns the quaternion's real part.  Each component goes through the same
-// operations in the same order as in integrate_body, so the results are
-// bit-identical to it; the four lanes exchange components by shuffles.
+// The same integration split over four warps per 32 particles, for scenes
+// that leave most SM sub-partitions with at most one warp at one thread per
+// particle.  An SM sub-partition retires one FP64 warp-instruction per ~64
+// cycles whatever the number of active lanes, so a lone warp's FP64
+// instructions, not its memory loads, set the pace there; the split divides
+// them over four warps (on different sub-partitions) without repeating any:
+// warps 0, 1, 2 own component q of the force and moment sums and of the
+// position, velocity and spin updates of the block's 32 particles; warp 3
+// evaluates the walls, updates the quaternion and, once the new position
+// components are in shared memory, writes the FP32 position and runs the
+// skin test.  Each component goes through the same operations in the same
+// order as in integrate_body, so the results are bit-identical to it.
+constexpr int kSplitThreads = 128;
 
 template <typename P>
 __device__ __forceinline__ P pick3(int q, P a, P b, P c) {
@@ -2403,135 +2465,149 @@ __device__ __forceinline__ void gather_component(const DemDev& d, const DemParam
 }
 
 template <bool MULTI, bool F32, bool TAB = false>
-__device__ __forceinline__ void integrate_lanes(const DemDev& d, const DemParams& p, int cur) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = t >> 2, q = t & 3, qc = q < 3 ? q : 2;
+__device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams& p, int cur) {
+    constexpr int NW = TAB ? kMaxWalls : 1;
+    __shared__ double s_wall[NW][6][32];  // each wall's force and moment on each particle
+    __shared__ uint8_t s_touch[NW][32];
+    __shared__ float s_pos[3][32];        // the new FP32 position components
+    const int q = (int)(threadIdx.x >> 5);  // 0, 1, 2: component; 3: walls and quaternion
+    const int l = (int)lane_id();
+    const int i = blockIdx.x * 32 + l;
     const int nxt = cur ^ 1;
-    if (t == 0) d.ctr->alloc[cur] = RowCounter{0u, 0u};
-    for (int s = t; s < p.ns; s += gridDim.x * blockDim.x) scene_flags_one<MULTI>(d, p, cur, s);
-    if (i >= p.n) return;  // the four lanes of a particle leave together
-    const unsigned gmask = 0xFu << (lane_id() & 28u);
-    const int sc = slot_scene<MULTI>(d, i);
-    if (MULTI && (sc < 0 || d.sp[sc].mode != kModeStep)) {
-        if (q == 0) d.in_cnt[i] = 0;
-        return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) d.ctr->alloc[cur] = RowCounter{0u, 0u};  // the free buffer is next step's target
+    for (int s2 = t; s2 < p.ns; s2 += gridDim.x * blockDim.x) scene_flags_one<MULTI>(d, p, cur, s2);
+    // every thread reaches both barriers; `live`: a particle of a stepping scene
+    const bool exists = i < p.n;
+    int sc = 0;
+    bool live = exists;
+    if (live) {
+        sc = slot_scene<MULTI>(d, i);
+        if (MULTI && (sc < 0 || d.sp[sc].mode != kModeStep)) live = false;
     }
-    const SceneParams& S = scene_rec<MULTI>(d, p, sc);
-    // every lane loads the whole particle state (the four lanes read the same
-    // words); nothing is stored before the __syncwarp below
-    const int row0 = d.row_start[nxt][i], rlen = d.row_len[nxt][i], nin = d.in_cnt[i];
-    const double x = d.px[i], y = d.py[i], z = d.pz[i];
-    const double vx = d.vx[i], vy = d.vy[i], vz = d.vz[i];
-    const double wx = d.wx[i], wy = d.wy[i], wz = d.wz[i];
-    const double r = d.r[i], m = d.m[i];
-    const double invm = d.inv_m[i], ii = d.inv_inertia[i];
-    const double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
-    const float4 p32 = d.pos32[i], xr = d.xref[i];
-    const float r32 = d.rm32[i].z;
-    const double xq = pick3(qc, x, y, z), vq = pick3(qc, vx, vy, vz), wq = pick3(qc, wx, wy, wz);
-    double Fq = 0.0, Mq = 0.0;
-    if constexpr (F32) {
-        float Ff = 0.0f, Mf = 0.0f;
-        gather_component<float>(d, p, i, row0, rlen, nin, qc, Ff, Mf);
-        Fq = f2d(Ff);
-        Mq = f2d(Mf);
-    } else {
-        gather_component<double>(d, p, i, row0, rlen, nin, qc, Fq, Mq);
-    }
-    __syncwarp(gmask);  // the group's loads are done before lane 0 stores
-    if (q == 0) d.in_cnt[i] = 0;
-    const double dt = S.dt;
-    // resolve_wall!: every lane evaluates the wall contact (the same values)
-    // and keeps its component; lane 0 counts warnings and stores the shear
-    auto wall = [&](const WallK& K, double* gsx, double* gsy, double* gsz) {
-        double sx = *gsx, sy = *gsy, sz = *gsz;
-        double F3[3] = {qc == 0 ? Fq : 0.0, qc == 1 ? Fq : 0.0, qc == 2 ? Fq : 0.0};
-        double M3[3] = {qc == 0 ? Mq : 0.0, qc == 1 ? Mq : 0.0, qc == 2 ? Mq : 0.0};
-        wall_contact(d, sc, K, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r, m, &sx, &sy, &sz,
-                     F3, M3, q == 0);
-        Fq = pick3(qc, F3[0], F3[1], F3[2]);
-        Mq = pick3(qc, M3[0], M3[1], M3[2]);
-        __syncwarp(gmask);  // every lane has read the old shear
-        if (q == 0) {
-            *gsx = sx;
-            *gsy = sy;
-            *gsz = sz;
+    const SceneParams& S = scene_rec<MULTI>(d, p, live ? sc : 0);
+    const int nwall = TAB ? d.mt->nwall : (live && S.has_wall ? 1 : 0);
+    double Fq = 0.0, Mq = 0.0, xq = 0.0, vq = 0.0, wq = 0.0, invm = 0.0, ii = 0.0, m = 0.0;
+    if (q < 3) {
+        if (live) {
+            const int row0 = d.row_start[nxt][i], rlen = d.row_len[nxt][i], nin = d.in_cnt[i];
+            xq = pick3(q, d.px, d.py, d.pz)[i];
+            vq = pick3(q, d.vx, d.vy, d.vz)[i];
+            wq = pick3(q, d.wx, d.wy, d.wz)[i];
+            m = d.m[i];
+            invm = d.inv_m[i];
+            ii = d.inv_inertia[i];
+            if constexpr (F32) {
+                float Ff = 0.0f, Mf = 0.0f;
+                gather_component<float>(d, p, i, row0, rlen, nin, q, Ff, Mf);
+                Fq = f2d(Ff);
+                Mq = f2d(Mf);
+            } else {
+                gather_component<double>(d, p, i, row0, rlen, nin, q, Fq, Mq);
+            }
         }
-    };
-    if constexpr (TAB) {
-        const MatTables& T = *d.mt;
-        const int a = d.mid[i];
-        for (int wl = 0; wl < T.nwall; ++wl) {
-            const WallConst& W = T.wall[wl];
-            const WallK K{W.wn, W.wd, W.wR, W.wRinv, W.f_wn, W.f_wc0, W.mu[a], W.Ys[a], W.Gs[a],
+    } else if (live) {
+        const double x = d.px[i], y = d.py[i], z = d.pz[i];
+        const double vx = d.vx[i], vy = d.vy[i], vz = d.vz[i];
+        const double wx = d.wx[i], wy = d.wy[i], wz = d.wz[i];
+        const double r = d.r[i];
+        const float4 p32 = d.pos32[i];
+        const float r32 = d.rm32[i].z;
+        const double dt = S.dt;
+        // resolve_wall!: each wall's force and moment, added by the component
+        // warps in wall order
+        for (int wl = 0; wl < nwall; ++wl) {
+            size_t o = i;
+            WallK K;
+            if constexpr (TAB) {
+                const MatTables& T = *d.mt;
+                const int a = d.mid[i];
+                const WallConst& W = T.wall[wl];
+                K = WallK{W.wn, W.wd, W.wR, W.wRinv, W.f_wn, W.f_wc0, W.mu[a], W.Ys[a], W.Gs[a],
                           W.cgn[a], W.cgt[a]};
-            const size_t o = (size_t)wl * p.wstride + i;
-            wall(K, d.wsx + o, d.wsy + o, d.wsz + o);
+                o = (size_t)wl * p.wstride + i;
+            } else {
+                K = WallK{S.wn, S.wd, S.wR, S.wRinv, S.f_wn, S.f_wc0, S.pw_mu, S.pw_Ys, S.pw_Gs,
+                          S.pw_cgn, S.pw_cgt};
+            }
+            double g[3], mw[3];
+            const bool touch = wall_force(d, sc, K, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz,
+                                          r, d.m[i], d.wsx + o, d.wsy + o, d.wsz + o, g, mw, true);
+            s_touch[wl][l] = touch ? 1 : 0;
+            if (touch) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    s_wall[wl][c][l] = g[c];
+                    s_wall[wl][3 + c][l] = mw[c];
+                }
+            }
         }
-    } else if (S.has_wall) {
-        const WallK K{S.wn, S.wd, S.wR, S.wRinv, S.f_wn, S.f_wc0, S.pw_mu, S.pw_Ys, S.pw_Gs,
-                      S.pw_cgn, S.pw_cgt};
-        wall(K, d.wsx + i, d.wsy + i, d.wsz + i);
+        // the quaternion, from the step's starting spin (integrate_body)
+        const double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
+        const bool spinless = (__double_as_longlong(wx) | __double_as_longlong(wy) |
+                               __double_as_longlong(wz)) == 0ll;
+        const bool identity = spinless && __double_as_longlong(qw) == 0x3ff0000000000000ll &&
+                              (__double_as_longlong(qx) | __double_as_longlong(qy) |
+                               __double_as_longlong(qz)) == 0ll;
+        if (!identity) {
+            double nw = qw, nx = qx, ny = qy, nz = qz;
+            if (!(spinless && finite_not_negzero(qw) && finite_not_negzero(qx) &&
+                  finite_not_negzero(qy) && finite_not_negzero(qz))) {
+                const double hx = half_exact(wx), hy = half_exact(wy), hz = half_exact(wz);
+                nw = __fma_rn(-qz, hz, __fma_rn(-qy, hy, __fma_rn(-qx, hx, qw)));
+                nx = __fma_rn(-qz, hy, __fma_rn(qy, hz, __fma_rn(qw, hx, qx)));
+                ny = __fma_rn(qz, hx, __fma_rn(qx, hz, __fma_rn(qw, hy, qy)));
+                nz = __fma_rn(-qy, hx, __fma_rn(qx, hy, __fma_rn(qw, hz, qz)));
+            }
+            const double inq =
+                rsqrt(__fma_rn(nz, nz, __fma_rn(ny, ny, __fma_rn(nx, nx, nw * nw))));
+            d.qw[i] = nw * inq;
+            d.qx[i] = nx * inq;
+            d.qy[i] = ny * inq;
+            d.qz[i] = nz * inq;
+        }
     }
-    // apply_body_force!
-    if (nonzero_bits(S.grav[qc])) Fq += S.grav[qc] * m;
-    if (nonzero_bits(S.damping)) {
-        const double dF = -S.damping * fabs(Fq) * jl_sign(vq);
-        const double dM = -S.damping * fabs(Mq) * jl_sign(wq);
-        Fq += dF;
-        Mq += dM;
+    __syncthreads();  // walls in shared memory; every component thread has read in_cnt
+    if (q == 3 && exists) d.in_cnt[i] = 0;
+    if (q < 3 && live) {
+        const double dt = S.dt;
+        for (int wl = 0; wl < nwall; ++wl) {
+            if (s_touch[wl][l]) {
+                Fq += s_wall[wl][q][l];
+                Mq += s_wall[wl][3 + q][l];
+            }
+        }
+        // apply_body_force!
+        if (nonzero_bits(S.grav[q])) Fq += S.grav[q] * m;
+        if (nonzero_bits(S.damping)) {
+            const double dF = -S.damping * fabs(Fq) * jl_sign(vq);
+            const double dM = -S.damping * fabs(Mq) * jl_sign(wq);
+            Fq += dF;
+            Mq += dM;
+        }
+        // update!
+        const double aq = Fq * invm;
+        const double hdt2 = S.hdt2;
+        const double pq1 = xq + vq * dt + aq * hdt2;
+        pick3(q, d.px, d.py, d.pz)[i] = pq1;
+        s_pos[q][l] = d2f(pq1 - S.dmin[q]);
+        pick3(q, d.vx, d.vy, d.vz)[i] = vq + aq * dt;
+        // 𝛚 + 𝐌·I⁻¹dt; with Mq = +0, a finite I⁻¹dt and wq not -0 the sum
+        // is wq and the stored spin stays
+        if (!(__double_as_longlong(Mq) == 0ll && product_finite(ii, dt) && not_negzero(wq)))
+            pick3(q, d.wx, d.wy, d.wz)[i] = __fma_rn(Mq, ii * dt, wq);
+        pick3(q, d.fx, d.fy, d.fz)[i] = Fq;
+        pick3(q, d.tx, d.ty, d.tz)[i] = Mq;
     }
-    // update!
-    const double aq = Fq * invm;
-    const double hdt2 = S.hdt2;
-    const double pq1 = xq + vq * dt + aq * hdt2;
-    if (q < 3) pick3(qc, d.px, d.py, d.pz)[i] = pq1;
-    {
-        const float fq = d2f(pq1 - S.dmin[qc]);
-        const float fx = __shfl_sync(gmask, fq, 0, 4), fy = __shfl_sync(gmask, fq, 1, 4),
-                    fz = __shfl_sync(gmask, fq, 2, 4);
-        if (q == 0) d.pos32[i] = make_float4(fx, fy, fz, reach32(fx, fy, fz, r32));
-        const bool moved = S.f_half_skin > 0.0f && left_skin(S, fx, fy, fz, xr);
+    __syncthreads();  // the new position components in shared memory
+    if (q == 3 && live) {
+        const float fx = s_pos[0][l], fy = s_pos[1][l], fz = s_pos[2][l];
+        d.pos32[i] = make_float4(fx, fy, fz, reach32(fx, fy, fz, d.rm32[i].z));
+        const bool moved = S.f_half_skin > 0.0f && left_skin(S, fx, fy, fz, d.xref[i]);
         const unsigned am = __activemask();
         const unsigned peers = __match_any_sync(am, moved ? sc : -1);
         if (moved && lane_id() == (unsigned)(__ffs(peers) - 1) && d.sflags[nxt][sc] == 0u)
             atomicOr(&d.sflags[nxt][sc], 1u);
-    }
-    if (q < 3) pick3(qc, d.vx, d.vy, d.vz)[i] = vq + aq * dt;
-    // the quaternion: lanes 0, 1, 2 own x, y, z and lane 3 owns w
-    const bool spinless = (__double_as_longlong(wx) | __double_as_longlong(wy) |
-                           __double_as_longlong(wz)) == 0ll;
-    const bool identity = spinless && __double_as_longlong(qw) == 0x3ff0000000000000ll &&
-                          (__double_as_longlong(qx) | __double_as_longlong(qy) |
-                           __double_as_longlong(qz)) == 0ll;
-    if (!identity) {
-        double nc = q == 3 ? qw : pick3(q, qx, qy, qz);
-        if (!(spinless && finite_not_negzero(qw) && finite_not_negzero(qx) &&
-              finite_not_negzero(qy) && finite_not_negzero(qz))) {
-            const double hx = half_exact(wx), hy = half_exact(wy), hz = half_exact(wz);
-            // integrate_body's four FMA chains, operands chosen per lane
-            const double a1 = q == 3 ? -qx : qw;
-            const double b1 = q == 3 ? hx : pick3(q, hx, hy, hz);
-            const double a2 = q == 3 ? -qy : (q == 0 ? qy : qx);
-            const double b2 = q == 3 ? hy : pick3(q, hz, hz, hy);
-            const double a3 = q == 3 ? -qz : pick3(q, -qz, qz, -qy);
-            const double b3 = q == 3 ? hz : pick3(q, hy, hx, hx);
-            nc = __fma_rn(a3, b3, __fma_rn(a2, b2, __fma_rn(a1, b1, nc)));
-        }
-        const double nx = __shfl_sync(gmask, nc, 0, 4), ny = __shfl_sync(gmask, nc, 1, 4),
-                     nz = __shfl_sync(gmask, nc, 2, 4), nw = __shfl_sync(gmask, nc, 3, 4);
-        const double inq = rsqrt(__fma_rn(nz, nz, __fma_rn(ny, ny, __fma_rn(nx, nx, nw * nw))));
-        (q == 3 ? d.qw : pick3(q, d.qx, d.qy, d.qz))[i] = nc * inq;
-    }
-    const bool torque_free = __all_sync(gmask, __double_as_longlong(Mq) == 0ll);
-    if (!(torque_free && product_finite(ii, dt) && not_negzero(wx) && not_negzero(wy) &&
-          not_negzero(wz))) {
-        const double iidt = ii * dt;
-        if (q < 3) pick3(qc, d.wx, d.wy, d.wz)[i] = __fma_rn(Mq, iidt, wq);
-    }
-    if (q < 3) {
-        pick3(qc, d.fx, d.fy, d.fz)[i] = Fq;
-        pick3(qc, d.tx, d.ty, d.tz)[i] = Mq;
     }
 }
 
@@ -2553,15 +2629,16 @@ __global__ void __launch_bounds__(kThreads, 3) k_integrate3(DemDev d, DemParams 
     dep_begin(p.dep == 2);
     integrate_body<MULTI, true>(d, p, cur);
 }
-// four lanes per particle (integrate_lanes)
+// four warps per 32 particles (integrate_split)
 template <bool MULTI, bool F32>
-__global__ void __launch_bounds__(kThreads) k_integrate_v(DemDev d, DemParams p, int cur) {
+__global__ void __launch_bounds__(kSplitThreads) k_integrate_split(DemDev d, DemParams p, int cur) {
     dep_begin(p.dep == 2);
-    integrate_lanes<MULTI, F32>(d, p, cur);
+    integrate_split<MULTI, F32>(d, p, cur);
 }
-__global__ void __launch_bounds__(kThreads) k_integrate_tab_v(DemDev d, DemParams p, int cur) {
+__global__ void __launch_bounds__(kSplitThreads) k_integrate_split_tab(DemDev d, DemParams p,
+                                                                       int cur) {
     dep_begin(p.dep == 2);
-    integrate_lanes<false, false, true>(d, p, cur);
+    integrate_split<false, false, true>(d, p, cur);
 }
 
 // ---- inspection kernels (dem_debug_broadphase) -------------------------------
@@ -2768,20 +2845,21 @@ void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
                       const LaunchShape& sh, cudaStream_t s) {
     if (p.n == 0) return;
     const int block = clamp_block(sh.integrate_block);
-    // four lanes per particle while one thread per particle would give the
-    // SMs at most one warp each
-    const bool lanes = sh.integrate_lanes == 4 ||
-                       (sh.integrate_lanes == 0 && (long long)p.n <= (long long)p.sms * 32);
-    if (lanes) {
-        const int nb = blocks_for(4LL * p.n, block);
+    // the split integrator while one thread per particle would leave the SM
+    // sub-partitions with at most two warps each
+    const bool split = sh.integrate_lanes == 4 ||
+                       (sh.integrate_lanes == 0 && (long long)p.n <= (long long)p.sms * 256);
+    if (split) {
+        const int nb = blocks_for(p.n, 32);
         if (p.tab)
-            launch(p.dep != 0, k_integrate_tab_v, nb, block, s, d, p, cur);
+            launch(p.dep != 0, k_integrate_split_tab, nb, kSplitThreads, s, d, p, cur);
         else if (p.precision == 1)
-            launch(p.dep != 0, multi ? k_integrate_v<true, true> : k_integrate_v<false, true>, nb,
-                   block, s, d, p, cur);
+            launch(p.dep != 0, multi ? k_integrate_split<true, true> : k_integrate_split<false, true>,
+                   nb, kSplitThreads, s, d, p, cur);
         else
-            launch(p.dep != 0, multi ? k_integrate_v<true, false> : k_integrate_v<false, false>,
-                   nb, block, s, d, p, cur);
+            launch(p.dep != 0,
+                   multi ? k_integrate_split<true, false> : k_integrate_split<false, false>, nb,
+                   kSplitThreads, s, d, p, cur);
         return;
     }
     const int nb = blocks_for(p.n, block);

@@ -398,9 +398,10 @@ def assert_runs_identical(outs, what):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_integrate_layouts_bit_identical(gpu, precision):
-    """The integrator with one lane per particle and with four (one per
-    vector component) gives the same results bit for bit: a bonded cube's
-    wall impact (wall contacts, spin, bonds breaking), a damped cube, and a
+    """The integrator with one thread per particle and split over four warps
+    per 32 particles (one per force component, one for the walls and the
+    quaternion) gives the same results bit for bit: a bonded cube's wall
+    impact (wall contacts, spin, bonds breaking), a damped cube, and a
     polydisperse cloud under gravity with damping thrown at the floor."""
     cube = scenes.bonded_cube(8, speed=30.0, steps=0, seed=2)
     outs = run_layouts(cube.cfg, cube.particles, 1000, True, "integrate_lanes",

@@ -119,8 +119,9 @@ def test_two_materials_bonded_cube_two_walls(gpu):
 
 
 def test_tables_integrate_layouts_bit_identical(gpu):
-    """A two-material cube against two walls: the integrator with one lane
-    per particle and with four give the same results bit for bit."""
+    """A two-material cube against two walls: the integrator with one thread
+    per particle and split over four warps give the same results bit for
+    bit."""
     sc = scenes.bonded_cube(8, speed=30.0, steps=0, seed=12)
     cfg = sc.cfg
     z = sc.particles.pos[:, 2]
