@@ -1077,17 +1077,18 @@ __device__ __forceinline__ void list_phase(const DemDev& d, const DemParams& p, 
         }
         return;
     }
-    // blocks take 64 consecutive particles each in turn.  (Spreading a small
-    // scene's particles over every block of the grid, contiguous per block or
-    // interleaved, left this phase as fast and made the force pass slower:
-    // rows then enter the next buffer in a less particle-ordered sequence and
-    // the force pass's gathers lose locality; measured on the 17,576-sphere
-    // cube, force 27 -> 30 us.)
-    for (int i0 = blockIdx.x * (kThreads / kVLanes) + gwarp; i0 < p.n;
-         i0 += gridDim.x * (kThreads / kVLanes)) {
+    // each block takes a contiguous share of the particles, a multiple of a
+    // warp's 8 groups, so that every block of the cooperative grid (which
+    // places consecutive blocks on the same SM) has work: on the
+    // 17,576-sphere cube, 64 consecutive particles per block left half of
+    // the SMs idle (54.5 -> 52.8 us per step with the even shares)
+    const int per = (int)((((long long)p.n + gridDim.x - 1) / gridDim.x + 7) & ~7LL);
+    const int lo = blockIdx.x * per;
+    const int hi = min(lo + per, p.n);
+    for (int i0 = lo + gwarp; i0 < hi; i0 += kThreads / kVLanes) {
         const int i = i0 + (g - gwarp);
         // which particles test their lists: the path byte the search wrote (arena)
-        bool active = i < p.n;
+        bool active = i < hi;
         bool frozen = false;
         if (MULTI && active) {
             const uint8_t path = d.path[i];
@@ -2213,21 +2214,6 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
     const double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
     const float4 p32 = d.pos32[i], xr = d.xref[i];
     const float r32 = d.rm32[i].z;
-    // The wall contact of a single-wall scene and the quaternion depend only
-    // on the step's starting state: a single scene evaluates the wall before
-    // the gather, so that its FP64 work overlaps the gather's dependent loads
-    // (the sums are unchanged: the wall's force and moment are added after
-    // the gather)
-    bool wall_touch = false;
-    double wall_g[3], wall_m[3];
-    if constexpr (!TAB && !MULTI) {
-        if (S.has_wall) {
-            const WallK K{S.wn, S.wd, S.wR, S.wRinv, S.f_wn, S.f_wc0, S.pw_mu, S.pw_Ys, S.pw_Gs,
-                          S.pw_cgn, S.pw_cgt};
-            wall_touch = wall_force(d, sc, K, S.dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r,
-                                    m, d.wsx + i, d.wsy + i, d.wsz + i, wall_g, wall_m, true);
-        }
-    }
     // 𝐪 + Δ𝐪 with Δ𝐪 = ½ 𝛚 ⊗ 𝐪 (no dt, as the reference), the ½ folded into
     // 𝛚, as explicit FMA chains.  With 𝛚 = (+0, +0, +0) each fma(a, +0, c)
     // (a finite) returns c unless c is -0, so for a finite 𝐪 without a -0
@@ -2259,12 +2245,6 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
             d.qz[i] = nz * inq;
         }
     };
-    // a single scene evaluates it before the gather, so that its FP64 work
-    // overlaps the gather's loads (measured on the 2,000,000-sphere bed:
-    // integrate 238 -> 231 us); the arena keeps it after the update (there
-    // the early placement measured slower: 131 -> 142 us on the 256-scene
-    // batch)
-    if constexpr (!MULTI) update_quaternion();
     double F[3] = {0.0, 0.0, 0.0}, M[3] = {0.0, 0.0, 0.0};
     if constexpr (F32) {
         float Ff[3] = {0.0f, 0.0f, 0.0f}, Mf[3] = {0.0f, 0.0f, 0.0f};
@@ -2293,18 +2273,11 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
             wall_contact(d, sc, K, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r, m, d.wsx + o,
                          d.wsy + o, d.wsz + o, F, M);
         }
-    } else if constexpr (MULTI) {
-        if (S.has_wall) {
-            const WallK K{S.wn, S.wd, S.wR, S.wRinv, S.f_wn, S.f_wc0, S.pw_mu, S.pw_Ys, S.pw_Gs,
-                          S.pw_cgn, S.pw_cgt};
-            wall_contact(d, sc, K, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r, m,
-                         d.wsx + i, d.wsy + i, d.wsz + i, F, M);
-        }
-    } else if (wall_touch) {
-#pragma unroll
-        for (int q = 0; q < 3; ++q) F[q] += wall_g[q];
-#pragma unroll
-        for (int q = 0; q < 3; ++q) M[q] += wall_m[q];
+    } else if (S.has_wall) {
+        const WallK K{S.wn, S.wd, S.wR, S.wRinv, S.f_wn, S.f_wc0, S.pw_mu, S.pw_Ys, S.pw_Gs,
+                      S.pw_cgn, S.pw_cgt};
+        wall_contact(d, sc, K, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz, r, m, d.wsx + i,
+                     d.wsy + i, d.wsz + i, F, M);
     }
     // apply_body_force!  A zero gravity component adds nothing: the force sum
     // starts at +0 and never becomes -0, so F + 0·m is F.
@@ -2350,7 +2323,7 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
     d.vx[i] = vx + ax * dt;
     d.vy[i] = vy + ay * dt;
     d.vz[i] = vz + az * dt;
-    if constexpr (MULTI) update_quaternion();
+    update_quaternion();
     // 𝛚 + 𝐌·I⁻¹dt: with 𝐌 = (+0, +0, +0) and a finite I⁻¹dt, fma(+0, I⁻¹dt, w)
     // is w unless w is -0, so a torque-free particle keeps its stored spin
     const bool torque_free = (__double_as_longlong(M[0]) | __double_as_longlong(M[1]) |

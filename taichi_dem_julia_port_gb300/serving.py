@@ -128,13 +128,20 @@ class Server:
 
     def __init__(self, sizing: ArenaSizing, precision: str = "fp32", chunk_steps: int = 200,
                  cell_factor: float = 0.0, keep_state: bool = True, lib=None,
-                 policy: str = "fifo", max_active: int = 0):
+                 policy: str = "fifo", max_active: int = 0, min_chunk: int = 1,
+                 build_ahead: int = 4):
         """policy "fifo": waiting requests are admitted in arrival order as
         soon as they fit.  policy "sjf": the waiting request with the least
         work (particles x steps) first, and only while the live scenes hold
         fewer than `max_active` particles (a request is always admitted into
         an empty arena): small requests then share their launches with fewer
-        particles and finish sooner, at some cost in throughput."""
+        particles and finish sooner, at some cost in throughput.
+
+        A chunk runs `chunk_steps` steps, or fewer when a live scene needs
+        fewer to finish (so that its slots are freed promptly), but at least
+        `min_chunk` (scenes freeze on the device at their step count, so a
+        longer chunk never oversteps one).  While a chunk runs, the scenes of
+        up to `build_ahead` waiting requests are built on the host."""
         if policy not in ("fifo", "sjf"):
             raise ValueError("policy must be 'fifo' or 'sjf'")
         self.policy = policy
@@ -145,6 +152,8 @@ class Server:
                            max_coordinate_number=sizing.max_coordinate_number,
                            precision=precision, cell_factor=cell_factor, lib=lib)
         self.chunk_steps = int(chunk_steps)
+        self.min_chunk = max(1, min(int(min_chunk), self.chunk_steps))
+        self.build_ahead = max(0, int(build_ahead))
         self.keep_state = keep_state
         self._reserved = 0
 
@@ -186,6 +195,9 @@ class Server:
         launches = 0
         deferred = 0
         work = 0
+        # where the wall-clock time goes: admission (scene build, upload),
+        # waiting for the device, collection of finished scenes
+        spent = {"admit_s": 0.0, "device_wait_s": 0.0, "collect_s": 0.0, "chunks": 0}
         t0 = time.perf_counter()
         clock = (lambda: time.perf_counter() - t0) if realtime else (lambda: math.inf)
         while pending or queue or live:
@@ -197,6 +209,7 @@ class Server:
             if self.policy == "sjf":
                 queue.sort(key=lambda r: (r.n_hint or 1) * r.steps)
             active = sum(lv.scene.n for lv in live.values())
+            ta = time.perf_counter()
             still = []
             for req in queue:
                 over = (self.policy == "sjf" and self.max_active and live
@@ -207,6 +220,7 @@ class Server:
                 else:
                     active += req.scene().n
             queue = still
+            spent["admit_s"] += time.perf_counter() - ta
             if not live:
                 if queue:
                     raise RuntimeError(f"request {queue[0].rid} can never fit the arena")
@@ -217,11 +231,24 @@ class Server:
             # so a finishing scene frees its slots promptly
             need = min(lv.req.steps - self.arena.info(sid)["steps_done"]
                        for sid, lv in live.items())
-            k = max(1, min(self.chunk_steps, need))
-            self.arena.step(k)
+            k = max(self.min_chunk, min(self.chunk_steps, need))
+            self.arena.step(k)  # asynchronous
             launches += k
+            # host work that overlaps the chunk: arrivals join the queue and the
+            # next requests' scenes are built
+            now = clock()
+            while pending and pending[0].arrival_s <= now:
+                queue.append(pending.pop(0))
+            if self.policy == "sjf":
+                queue.sort(key=lambda r: (r.n_hint or 1) * r.steps)
+            for req in queue[:self.build_ahead]:
+                req.scene()
+            tw = time.perf_counter()
             self.arena.sync()
+            spent["device_wait_s"] += time.perf_counter() - tw
+            spent["chunks"] += 1
             done_t = time.perf_counter() - t0
+            tc = time.perf_counter()
             for sid in list(live):
                 lv = live[sid]
                 info = self.arena.info(sid)
@@ -239,9 +266,10 @@ class Server:
                 self._reserved -= lv.reserve
                 lv.req._scene = None  # host copy no longer needed
                 del live[sid]
+            spent["collect_s"] += time.perf_counter() - tc
         makespan = time.perf_counter() - t0
         results.sort(key=lambda r: r.rid)
-        return ServeReport(results, makespan, work, launches, deferred)
+        return ServeReport(results, makespan, work, launches, deferred, extra=spent)
 
 
 def log_uniform_int(rng, lo: float, hi: float) -> int:
