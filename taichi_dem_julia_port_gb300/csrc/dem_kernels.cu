@@ -2443,7 +2443,11 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
     __shared__ double s_wall[NW][6][32];  // each wall's force and moment on each particle
     __shared__ uint8_t s_touch[NW][32];
     __shared__ float s_pos[3][32];        // the new FP32 position components
-    const int q = (int)(threadIdx.x >> 5);  // 0, 1, 2: component; 3: walls and quaternion
+    // 0, 1, 2: component; 3: walls and quaternion.  The roles rotate with
+    // the block: warp w of an SM runs on sub-partition w mod 4, so a fixed
+    // role would put every block's wall and quaternion warp, the one with
+    // the most FP64 instructions, on the same sub-partition's FP64 unit
+    const int q = ((int)(threadIdx.x >> 5) - (int)(blockIdx.x & 3u) - 1) & 3;
     const int l = (int)lane_id();
     const int i = blockIdx.x * 32 + l;
     const int nxt = cur ^ 1;
