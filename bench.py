@@ -123,14 +123,15 @@ KERNELS_PER_STEP = 3
 # of one launch over the units it processed).  Force kernel, FP64 mode: per
 # Hertz contact 151.0 (a 100,000-sphere compacted bed, every contact a Hertz
 # contact: 1.503e7 per launch), per bond 116.1 (the 17,576-sphere cube in its
-# fragmentation, 41,427 bonds and 6,670 Hertz contacts: 5.817e6 per launch,
+# fragmentation, 41,427 bonds and 6,670 Hertz contacts: 5.818e6 per launch,
 # less the Hertz share); FP32 mode per bond 15.0 (the same cube before its
-# impact).  Integrator per particle: 84.1 in FP64 mode (the cube in its
-# fragmentation), 51.0 in the FP32 mode (64 scenes of the batched workload).
-# Then GB300's FP64 pipe width.
+# impact).  Integrator per particle: 91.9 in FP64 mode (the cube in its
+# fragmentation, split over four warps per 32 particles: 1.616e6 per launch;
+# the one-thread form measured 84.1), 51.0 in the FP32 mode (64 scenes of the
+# batched workload).  Then GB300's FP64 pipe width.
 FP64_INST = {("force", "fp64", "bond"): 116.1, ("force", "fp64", "hertz"): 151.0,
              ("force", "fp32", "bond"): 15.0,
-             ("integrate", "fp64"): 84.1, ("integrate", "fp32"): 51.0}
+             ("integrate", "fp64"): 91.9, ("integrate", "fp32"): 51.0}
 # The integrator skips the quaternion increment of a particle with exactly zero
 # spin, the normalisation of a spinless identity orientation and the spin
 # update of a particle with exactly zero torque: in the pour's settling phase
@@ -185,17 +186,17 @@ L2_FLUSH_BYTES = 256 << 20
 # processed.  Keys: workload and timed window ("c2" the cube in its impact
 # window, "c3" the pour settling, "c3bed" the compacted bed), kernel.
 NCU_TRAFFIC = {
-    ("c2", "force"): (7.155200e6, 17576),          # k_force<double>, step 4,006
-    ("c2", "contacts"): (2.317056e6, 17576),       # k_search, list step, step 4,006
-    ("c2", "integrate"): (9.232896e6, 17576),      # k_integrate, step 4,006
-    ("c3bed", "force"): (93.960960e6, 400000),     # k_force<float>, 400,000-sphere bed
-    ("c3bed", "contacts"): (53.395712e6, 400000),  # k_search, list step (one lane per particle)
-    ("c3bed", "integrate"): (181.155840e6, 400000),  # k_integrate3 (FP32 gather)
-    ("c3", "integrate"): (627.860224e6, 2000000),  # k_integrate3 (FP32 mode, no contacts)
-    ("c4", "force"): (145.409024e6, 431416),       # k_force<float>
-    ("c4", "integrate"): (184.980224e6, 431416),   # k_integrate3 (FP32 gather)
-    ("c4", "contacts"): (35.102976e6, 431416),     # k_search, list step
-    ("c3", "contacts"): (43.205888e6, 2000000),    # k_search, list step (wide pass)
+    ("c2", "force"): (7.368064e6, 17576),          # k_force<double>, step 4,006
+    ("c2", "contacts"): (2.330368e6, 17576),       # k_search, list step, step 4,006
+    ("c2", "integrate"): (9.095936e6, 17576),      # k_integrate_split, step 4,006
+    ("c3bed", "force"): (93.908480e6, 400000),     # k_force4<float>, 400,000-sphere bed
+    ("c3bed", "contacts"): (51.669504e6, 400000),  # k_search, list step (one lane per particle)
+    ("c3bed", "integrate"): (181.207040e6, 400000),  # k_integrate3 (FP32 gather)
+    ("c3", "integrate"): (628.354048e6, 2000000),  # k_integrate3 (FP32 mode, no contacts)
+    ("c3", "contacts"): (43.727872e6, 2000000),    # k_search, list step (wide pass)
+    ("c4", "force"): (185.573376e6, 431416),       # k_force<float, 1>
+    ("c4", "integrate"): (175.813632e6, 431416),   # k_integrate3<1> (FP32 gather)
+    ("c4", "contacts"): (35.996672e6, 431416),     # k_search<0, 1>, list step
 }
 
 
@@ -810,6 +811,20 @@ def measure_scene(args, lib, sc, precision: str, steps: int, warmup: int, advanc
                        "c3" if settling else None, n_hertz=int(round(c_mean - b_mean)))
     if fr:
         roof["fp64_pipe"] = fr
+    # every phase's figures (the phases of a step are close in length, so the
+    # dominant one alone does not describe the step)
+    roof["phases"] = {}
+    for k, ms_k in ph.items():
+        e = {"ms": ms_k, "algorithmic_bytes": alg.get(k),
+             "traffic": ncu_traffic(traffic_key, k, sc.n)}
+        if alg.get(k) and ms_k:
+            e["achieved_gbs"] = alg[k] / (ms_k * 1e-3) / 1e9
+            e["frac_hbm"] = e["achieved_gbs"] / peaks["hbm_gbs"]
+        f64 = fp64_roofline(k, precision, sc.n, int(round(b_mean)), ms_k, clk, peaks,
+                            "c3" if settling else None, n_hertz=int(round(c_mean - b_mean)))
+        if f64:
+            e["fp64_frac"] = f64["frac"]
+        roof["phases"][k] = e
     out = {"value": ws * sc.n * steps / (total_ms / 1e3), "ms_per_step": ms_per_step,
            "contact_steps_per_s": ws * c_mean * steps / (total_ms / 1e3), "window": window,
            "roofline": roof, "clocks": clk, "snap": snap, "n": sc.n}

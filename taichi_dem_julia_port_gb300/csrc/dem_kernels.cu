@@ -751,8 +751,12 @@ __device__ __forceinline__ void detect_group(const DemDev& d, const DemParams& p
 
 // cp_list membership of the pair (i, j), i < j, from the current positions:
 // j's bucket among i's 8 octant buckets, in the reference's cells and table.
+// Inlined: as a call it made the list kernels save and restore live registers
+// around it (twice the spill traffic), and a warp whose particle had a contact
+// to end waited about 16,000 cycles longer in its row loop (the 17,576-sphere
+// cube: 53.8 -> 53.2 us per step; the 2,000,000-sphere bed 506 -> 497 us).
 template <bool MULTI>
-__device__ __noinline__ bool in_cp_list(const DemDev& d, const SceneParams& S, int i, int j) {
+__device__ __forceinline__ bool in_cp_list(const DemDev& d, const SceneParams& S, int i, int j) {
     const double pi[3] = {d.px[i], d.py[i], d.pz[i]}, pj[3] = {d.px[j], d.py[j], d.pz[j]};
     const int4 ci = cell_of_screened(pi, S.dmin, S.cell_ref, S.inv_cell_ref, S.f_inv_cell_ref,
                                      S.f_dmin_cells_ref);
