@@ -203,6 +203,27 @@ __device__ __forceinline__ int32_t cell_index(double num, double cell, double in
 // m = 2^-20·(|q'| + |dmin|/cell + 1) from 0, 1/2 and 1, the exact ceiling and
 // the exact octant side follow from q' alone; otherwise (and for NaN or huge
 // values, which fail the test) the exact FP64 computation decides.
+// One coordinate: the cell index and, with want_side, whether the coordinate
+// lies above the cell's centre (*above; not computed otherwise).
+__device__ __forceinline__ int cell_component(double x, double dmin, double cell,
+                                              double inv_cell, float inv_cell32, float dmin_cells,
+                                              bool want_side, bool* above) {
+    const double num = __dsub_rn(x, dmin);
+    const float q = d2f(num) * inv_cell32;
+    const float fl = floorf(q);
+    const float frac = q - fl;
+    const float m = (fabsf(q) + dmin_cells + 1.0f) * 0x1p-20f;
+    if (frac > m && frac < 1.0f - m && fabsf(frac - 0.5f) > m) {
+        if (want_side) *above = frac > 0.5f;
+        return (int)fl + 1;
+    }
+    const int ijk = cell_index(num, cell, inv_cell);
+    if (want_side) {
+        const double ctr = __dadd_rn(dmin, __dmul_rn(__dsub_rn((double)ijk, 0.5), cell));
+        *above = x > ctr;
+    }
+    return ijk;
+}
 __device__ __forceinline__ int4 cell_of_screened(const double pos[3], const double dmin[3],
                                                  double cell, double inv_cell, float inv_cell32,
                                                  float dmin_cells) {
@@ -210,19 +231,10 @@ __device__ __forceinline__ int4 cell_of_screened(const double pos[3], const doub
     int oct = 0;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const double num = __dsub_rn(pos[c], dmin[c]);
-        const float q = d2f(num) * inv_cell32;
-        const float fl = floorf(q);
-        const float frac = q - fl;
-        const float m = (fabsf(q) + dmin_cells + 1.0f) * 0x1p-20f;
-        if (frac > m && frac < 1.0f - m && fabsf(frac - 0.5f) > m) {
-            ijk[c] = (int)fl + 1;
-            if (frac > 0.5f) oct |= 1 << c;
-        } else {
-            ijk[c] = cell_index(num, cell, inv_cell);
-            const double ctr = __dadd_rn(dmin[c], __dmul_rn(__dsub_rn((double)ijk[c], 0.5), cell));
-            if (pos[c] > ctr) oct |= 1 << c;
-        }
+        bool above = false;
+        ijk[c] = cell_component(pos[c], dmin[c], cell, inv_cell, inv_cell32, dmin_cells, true,
+                                &above);
+        if (above) oct |= 1 << c;
     }
     return make_int4(ijk[0], ijk[1], ijk[2], oct);
 }
@@ -775,6 +787,42 @@ __device__ __forceinline__ bool in_cp_list(const DemDev& d, const SceneParams& S
     return in;
 }
 
+// The same test with a particle's four lanes sharing it (every lane of the
+// group calls it with the same i, j): lanes 0, 1, 2 compute one axis each of
+// i's cell and side and of j's cell (j's side is not needed), so that the
+// exact FP64 fallbacks of lattice-aligned coordinates run side by side
+// instead of one after another on one lane.  The cells and sides are
+// exchanged by shuffles and every lane returns the result.
+__device__ __forceinline__ bool in_cp_list_group(const DemDev& d, const SceneParams& S, int i,
+                                                 int j, int lane, unsigned gmask) {
+    const int c = lane < 3 ? lane : 2;
+    const double* P = c == 0 ? d.px : (c == 1 ? d.py : d.pz);
+    bool above = false;
+    const int ci = cell_component(P[i], S.dmin[c], S.cell_ref, S.inv_cell_ref, S.f_inv_cell_ref,
+                                  S.f_dmin_cells_ref, true, &above);
+    const int cj = cell_component(P[j], S.dmin[c], S.cell_ref, S.inv_cell_ref, S.f_inv_cell_ref,
+                                  S.f_dmin_cells_ref, false, nullptr);
+    const int base = (int)(lane_id() & ~3u);
+    int CI[3], CJ[3], oct = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        CI[k] = __shfl_sync(gmask, ci, base + k);
+        CJ[k] = __shfl_sync(gmask, cj, base + k);
+        oct |= (__shfl_sync(gmask, above ? 1 : 0, base + k)) << k;
+    }
+    const uint32_t bj = ref_bucket_of(CJ[0], CJ[1], CJ[2], S);
+    const int dx = (oct & 1) ? 1 : -1, dy = (oct & 2) ? 1 : -1, dz = (oct & 4) ? 1 : -1;
+    bool in = false;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int ox = (t == 1 || t == 4 || t == 5 || t == 7) ? dx : 0;
+        const int oy = (t == 2 || t == 4 || t == 6 || t == 7) ? dy : 0;
+        const int oz = (t == 3 || t == 5 || t == 6 || t == 7) ? dz : 0;
+        in |= ref_bucket_of(CI[0] + ox, CI[1] + oy, CI[2] + oz, S) == bj;
+    }
+    return in;
+}
+
 // `update_contacts!` from the neighbour lists, for the particles of scenes
 // that do not run the full search this step (four lanes per particle,
 // grid-stride over slots).  Survival of the current row is decided as in
@@ -800,7 +848,12 @@ __device__ __forceinline__ void list_particle(const DemDev& d, const DemParams& 
     if (lane == 0) sh[g].nnew = 0;
     const bool cached = e1 - e0 <= kRowCache;
     int nkeep = 0, ended = 0, nbond = 0;
-    for (int e2 = e0 + lane; e2 < e1; e2 += kVLanes) {
+    // a Hertz contact that no longer touches ends iff the pair is in the
+    // cp_list: those entries wait (one bit per loop iteration of this lane)
+    // for the group's shared membership test below
+    unsigned pend = 0u;
+    int it = 0;
+    for (int e2 = e0 + lane; e2 < e1; e2 += kVLanes, ++it) {
         const uint32_t fl = o.fl[e2];
         const int j = o.cj[e2];
         if (cached) sh[g].row[e2 - e0] = (fl & kActive) ? j : -1;
@@ -810,19 +863,38 @@ __device__ __forceinline__ void list_particle(const DemDev& d, const DemParams& 
         } else if (frozen || (fl & kBonded)) {
             keep = 1;
         } else {
-            // an FP32 screen accepts the clearly touching pairs; the FP64
-            // test decides the rest
             const bool valid = touching_rn(d.px[i], d.py[i], d.pz[i], d.px[j], d.py[j],
                                            d.pz[j], d.r[i], d.r[j]);
-            keep = (valid ||
-                    !in_cp_list<MULTI>(d, scene_rec<MULTI>(d, p, slot_scene<MULTI>(d, i)), i, j))
-                       ? 1
-                       : 0;
-            ended += 1 - keep;
+            if (valid) {
+                keep = 1;
+            } else if (it < 32) {
+                pend |= 1u << it;
+                continue;
+            } else {
+                keep = in_cp_list<MULTI>(d, scene_rec<MULTI>(d, p, slot_scene<MULTI>(d, i)), i, j)
+                           ? 0
+                           : 1;
+                ended += 1 - keep;
+            }
         }
         d.keep[e2] = (uint8_t)keep;
         nkeep += keep;
         nbond += (keep && (fl & kBonded)) ? 1 : 0;
+    }
+    for (unsigned any = __ballot_sync(gmask, pend != 0u) & gmask; any;
+         any = __ballot_sync(gmask, pend != 0u) & gmask) {
+        const int src = __ffs(any) - 1;  // a lane of this group with a waiting entry
+        const int sit = __ffs(__shfl_sync(gmask, pend, src)) - 1;
+        const int e2 = e0 + (src & (kVLanes - 1)) + sit * kVLanes;
+        const bool in = in_cp_list_group(d, scene_rec<MULTI>(d, p, slot_scene<MULTI>(d, i)), i,
+                                         o.cj[e2], lane, gmask);
+        if (lane == (src & (kVLanes - 1))) {
+            pend &= ~(1u << sit);
+            const int keep = in ? 0 : 1;
+            d.keep[e2] = (uint8_t)keep;
+            nkeep += keep;
+            ended += 1 - keep;
+        }
     }
     nkeep = __reduce_add_sync(gmask, nkeep);
     nbond = __reduce_add_sync(gmask, nbond);
