@@ -2428,9 +2428,9 @@ __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams&
 // them over four warps (on different sub-partitions) without repeating any:
 // warps 0, 1, 2 own component q of the force and moment sums and of the
 // position, velocity and spin updates of the block's 32 particles; warp 3
-// evaluates the walls, updates the quaternion and, once the new position
-// components are in shared memory, writes the FP32 position and runs the
-// skin test.  Each component goes through the same operations in the same
+// evaluates the walls, then updates the quaternion while the others update
+// the particles and, once the new position components are in shared memory,
+// writes the FP32 position and runs the skin test.  Each component goes through the same operations in the same
 // order as in integrate_body, so the results are bit-identical to it.
 constexpr int kSplitThreads = 128;
 
@@ -2559,10 +2559,16 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
                 gather_component<double>(d, p, i, row0, rlen, nin, q, Fq, Mq);
             }
         }
-    } else if (live) {
+    }
+    // warp 3: the step's starting spin, for the walls now and the quaternion
+    // after the first barrier (the component warps store the new spin after it)
+    double wx = 0.0, wy = 0.0, wz = 0.0;
+    if (q == 3 && live) {
+        wx = d.wx[i];
+        wy = d.wy[i];
+        wz = d.wz[i];
         const double x = d.px[i], y = d.py[i], z = d.pz[i];
         const double vx = d.vx[i], vy = d.vy[i], vz = d.vz[i];
-        const double wx = d.wx[i], wy = d.wy[i], wz = d.wz[i];
         const double r = d.r[i];
         const float4 p32 = d.pos32[i];
         const float r32 = d.rm32[i].z;
@@ -2595,7 +2601,12 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
                 }
             }
         }
-        // the quaternion, from the step's starting spin (integrate_body)
+    }
+    __syncthreads();  // walls in shared memory; every component thread has read in_cnt
+    if (q == 3 && exists) d.in_cnt[i] = 0;
+    // the quaternion (integrate_body's update, from the starting spin) runs
+    // while the component warps update the position, velocity and spin
+    if (q == 3 && live) {
         const double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
         const bool spinless = (__double_as_longlong(wx) | __double_as_longlong(wy) |
                                __double_as_longlong(wz)) == 0ll;
@@ -2620,8 +2631,6 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
             d.qz[i] = nz * inq;
         }
     }
-    __syncthreads();  // walls in shared memory; every component thread has read in_cnt
-    if (q == 3 && exists) d.in_cnt[i] = 0;
     if (q < 3 && live) {
         const double dt = S.dt;
         for (int wl = 0; wl < nwall; ++wl) {
