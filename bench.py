@@ -186,17 +186,17 @@ L2_FLUSH_BYTES = 256 << 20
 # processed.  Keys: workload and timed window ("c2" the cube in its impact
 # window, "c3" the pour settling, "c3bed" the compacted bed), kernel.
 NCU_TRAFFIC = {
-    ("c2", "force"): (7.368064e6, 17576),          # k_force<double>, step 4,006
-    ("c2", "contacts"): (2.330368e6, 17576),       # k_search, list step, step 4,006
-    ("c2", "integrate"): (9.095936e6, 17576),      # k_integrate_split, step 4,006
-    ("c3bed", "force"): (93.908480e6, 400000),     # k_force4<float>, 400,000-sphere bed
-    ("c3bed", "contacts"): (51.669504e6, 400000),  # k_search, list step (one lane per particle)
-    ("c3bed", "integrate"): (181.207040e6, 400000),  # k_integrate3 (FP32 gather)
-    ("c3", "integrate"): (628.354048e6, 2000000),  # k_integrate3 (FP32 mode, no contacts)
-    ("c3", "contacts"): (43.727872e6, 2000000),    # k_search, list step (wide pass)
-    ("c4", "force"): (185.573376e6, 431416),       # k_force<float, 1>
-    ("c4", "integrate"): (175.813632e6, 431416),   # k_integrate3<1> (FP32 gather)
-    ("c4", "contacts"): (35.996672e6, 431416),     # k_search<0, 1>, list step
+    ("c2", "force"): (7.470848e6, 17576),          # k_force<double>, step 4,006
+    ("c2", "contacts"): (2.336768e6, 17576),       # k_search, list step, step 4,006
+    ("c2", "integrate"): (9.095680e6, 17576),      # k_integrate_split, step 4,006
+    ("c3bed", "force"): (94.237e6, 400000),        # k_force4<float>, 400,000-sphere bed
+    ("c3bed", "contacts"): (51.041e6, 400000),     # k_search, list step (one lane per particle)
+    ("c3bed", "integrate"): (181.203e6, 400000),   # k_integrate3 (FP32 gather)
+    ("c3", "integrate"): (628.523e6, 2000000),     # k_integrate3 (FP32 mode, no contacts)
+    ("c3", "contacts"): (43.036e6, 2000000),       # k_search, list step (wide pass)
+    ("c4", "force"): (186.237e6, 431416),          # k_force<float, 1>
+    ("c4", "integrate"): (176.134e6, 431416),      # k_integrate3<1> (FP32 gather)
+    ("c4", "contacts"): (35.621e6, 431416),        # k_search<0, 1>, list step
 }
 
 
