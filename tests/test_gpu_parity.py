@@ -4,6 +4,8 @@ Bit-exact: cell ijk, Morton codes, buckets, bucket counts, sorted order, the
 cp_list multiset, contact sets and bond sets.  Within tolerance: forces,
 positions and velocities (FP64: rtol 1e-9 for one step from an identical
 state, 1e-5 over a short horizon; FP32 force mode: 1e-3)."""
+from types import SimpleNamespace
+
 import numpy as np
 import pytest
 
@@ -345,12 +347,18 @@ def test_touching_decisions_at_the_boundary(gpu):
 
 def test_list_layouts_bit_identical(gpu):
     """The neighbour-list update with one lane per particle and with four
-    give the same results bit for bit (a compacted polydisperse bed, where
-    contacts are created and ended every step, and a bonded cube impact)."""
+    give the same results bit for bit: a compacted polydisperse bed, a dense
+    granular cloud whose contacts form and end every step, and a bonded cube
+    that fragments at the wall (its lattice coordinates take the exact FP64
+    fallbacks of the cell tests when a Hertz contact between fragments ends;
+    the four-lane path shares that cp_list test between a particle's lanes,
+    the one-lane path runs it alone)."""
     f = 2.0 * (30_000 / 2_000_000) ** (1.0 / 3.0)
     bed = scenes.granular_bed(30_000, box=(0.4 * f, 0.4 * f, 1.2), seed=23)
+    ccfg, cp = random_cloud(3000, (0.05, 0.05, 0.05), 0.0008, 0.0015, seed=15, v=0.5)
+    cloud = SimpleNamespace(cfg=ccfg, particles=cp, bonded=False)
     cube = scenes.bonded_cube(8, speed=30.0, steps=0, seed=2)
-    for sc, steps in ((bed, 200), (cube, 200)):
+    for name, sc, steps in (("bed", bed, 200), ("cloud", cloud, 200), ("cube", cube, 2000)):
         outs = []
         for lanes in (1, 4):
             g = GlobalData(sc.cfg, sc.particles)
@@ -367,6 +375,10 @@ def test_list_layouts_bit_identical(gpu):
         s1, s4 = outs[0][2], outs[1][2]
         assert (s1["contacts_created"], s1["contacts_ended"]) == \
             (s4["contacts_created"], s4["contacts_ended"])
+        if name != "bed":
+            # contacts ended: the four-lane path's shared cp_list membership
+            # test ran and matched the one-lane path's own
+            assert s4["contacts_ended"] > 0, name
 
 
 def run_layouts(cfg, p, steps, bonded, knob, values=(1, 4), precision="fp64", tables=None):
