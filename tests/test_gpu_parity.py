@@ -20,7 +20,7 @@ from tests.conftest import assert_rows_close
 pytestmark = pytest.mark.gpu
 
 RTOL_STEP = 1e-9      # one step from an identical state (FP64)
-RTOL_HORIZON = 1e-5   # short horizon (FP64), the spec force bound
+RTOL_HORIZON = 1e-5   # short horizon (FP64): the stated force bound of the FP64 path
 RTOL_FP32 = 1e-3      # FP32 force mode vs the FP64 oracle
 
 
