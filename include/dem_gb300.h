@@ -77,7 +77,11 @@ typedef struct DemConfigC {
     double pw_coefficient_friction;
     double pw_coefficient_restitution;
     double pw_coefficient_rolling_resistance; /* declared, unused (as in the reference) */
-    int64_t max_coordinate_number;
+    int64_t max_coordinate_number;     /* contacts per particle (the contact capacity is
+                                        * n · this); also new partners and incoming
+                                        * contacts per particle and step (at most 64)
+                                        * and neighbour-list partners per particle
+                                        * (at least 16, at most 256)                */
     int64_t collision_pair_init_capacity_factor;
     double tolerance;
     int64_t max_particle_count;
@@ -408,7 +412,9 @@ typedef struct DemArenaConfig {
     int64_t max_buckets;     /* bucket-table entries shared by all scenes    */
     int32_t max_scenes;
     int32_t max_coordinate_number; /* new partners / incoming contacts per
-                                      particle and step (at most 64)         */
+                                      particle and step (at most 64) and
+                                      neighbour-list partners per particle
+                                      (at least 16, at most 256)             */
     int32_t precision;       /* DEM_FP64 or DEM_FP32_FORCE                   */
     int32_t pad;
     double cell_factor;      /* search cell = cell_factor · 4 rₘₐₓ; 0 = 1.  Values

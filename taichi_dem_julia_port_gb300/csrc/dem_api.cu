@@ -22,7 +22,16 @@ using namespace dem;
 namespace {
 
 constexpr double kPi = 3.141592653589793;
-constexpr int kListCapacity = 16;  // neighbour-list partners per particle
+// Neighbour-list partners (j > i within reach) per particle: the scene's
+// max_coordinate_number, at least 16 and at most 256.  A list that overflows
+// makes its scene run the full pair search at the next step, so a dense
+// polydisperse packing, whose large spheres have many small neighbours, needs
+// room for them (measured: 100,000 spheres of radii 0.5-2 mm at solid
+// fraction 0.45 overflowed 16-entry lists on every step).
+constexpr int kListMin = 16, kListMax = 256;
+inline int list_capacity(int64_t max_coordinate_number) {
+    return (int)std::min<int64_t>(std::max<int64_t>(max_coordinate_number, kListMin), kListMax);
+}
 
 struct M3 {
     double a[3][3];
@@ -1254,7 +1263,7 @@ int create_single(const DemConfigC* cfg, const DemParticlesIn* pin, const DemTab
     h->p.cap = h->c_cap;
     h->p.kstash = (int)std::min<int64_t>(cfg->max_coordinate_number, 64);
     h->p.kin = h->p.kstash;
-    h->p.kvl = kListCapacity;
+    h->p.kvl = list_capacity(cfg->max_coordinate_number);
     h->p.ns = 1;
     h->p.sms = sms;
     h->p.T = h->t_cap;
@@ -1317,7 +1326,7 @@ int dem_arena_create(const DemArenaConfig* cfg, DemHandle** out) {
     h->p.cap = h->c_cap;
     h->p.kstash = std::min(cfg->max_coordinate_number, 64);
     h->p.kin = h->p.kstash;
-    h->p.kvl = kListCapacity;
+    h->p.kvl = list_capacity(cfg->max_coordinate_number);
     h->p.ns = h->s_cap;
     h->p.sms = sms;
     h->p.T = h->t_cap;

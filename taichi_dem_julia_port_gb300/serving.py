@@ -27,8 +27,14 @@ from .arena import Arena, buckets_for
 from .scenes import Scene, bonded_cube, granular_pour
 
 # device bytes per arena unit (the buffers dem_arena_create allocates)
-SLOT_BYTES_BASE = 516          # particle SoA, broad phase, neighbour lists, bookkeeping
+SLOT_BYTES_BASE = 452          # particle SoA, broad phase, bookkeeping
 SLOT_BYTES_PER_PARTNER = 12    # new-partner stash (4 B) + incoming list (8 B), per partner
+SLOT_BYTES_PER_LIST_ENTRY = 4  # neighbour-list partner
+
+
+def list_capacity(max_coordinate_number: int) -> int:
+    """Neighbour-list partners per particle (dem_arena_create's rule)."""
+    return min(max(int(max_coordinate_number), 16), 256)
 CONTACT_BYTES = 345            # two contact buffers, force contributions, survival flag
 BUCKET_BYTES = 8               # count + start
 
@@ -45,7 +51,9 @@ class ArenaSizing:
     @property
     def bytes(self) -> int:
         return (self.max_particles * (SLOT_BYTES_BASE + SLOT_BYTES_PER_PARTNER *
-                                      self.max_coordinate_number)
+                                      self.max_coordinate_number
+                                      + SLOT_BYTES_PER_LIST_ENTRY *
+                                      list_capacity(self.max_coordinate_number))
                 + self.max_contacts * CONTACT_BYTES + self.max_buckets * BUCKET_BYTES)
 
     @classmethod
@@ -55,6 +63,7 @@ class ArenaSizing:
         `contacts_per_particle` per slot and two bucket entries per slot plus
         1,024 per scene record."""
         per_slot = (SLOT_BYTES_BASE + SLOT_BYTES_PER_PARTNER * max_coordinate_number
+                    + SLOT_BYTES_PER_LIST_ENTRY * list_capacity(max_coordinate_number)
                     + contacts_per_particle * CONTACT_BYTES + 2 * BUCKET_BYTES)
         fixed = 1024 * max_scenes * BUCKET_BYTES
         n = int(max(hbm_bytes - fixed, 0) // per_slot)
