@@ -2520,10 +2520,14 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
     __shared__ uint8_t s_touch[NW][32];
     __shared__ float s_pos[3][32];        // the new FP32 position components
     // 0, 1, 2: component; 3: walls and quaternion.  The roles rotate with
-    // the block: warp w of an SM runs on sub-partition w mod 4, so a fixed
-    // role would put every block's wall and quaternion warp, the one with
-    // the most FP64 instructions, on the same sub-partition's FP64 unit
-    const int q = ((int)(threadIdx.x >> 5) - (int)(blockIdx.x & 3u) - 1) & 3;
+    // the block's round over the SMs: warp w of a block runs on SM
+    // sub-partition w, and blocks are placed one per SM in turn (blocks b,
+    // b + sms, b + 2·sms, ... share an SM), so rotating by b / sms gives the
+    // blocks on one SM different sub-partitions for their wall and
+    // quaternion warp, the one with the most FP64 instructions (a rotation by
+    // b mod 4 would not: the SM count, 152, is a multiple of 4)
+    const int q = ((int)(threadIdx.x >> 5) - (int)((blockIdx.x / (unsigned)max(p.sms, 1)) & 3u) -
+                   1) & 3;
     const int l = (int)lane_id();
     const int i = blockIdx.x * 32 + l;
     const int nxt = cur ^ 1;
@@ -2562,11 +2566,15 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
     }
     // warp 3: the step's starting spin, for the walls now and the quaternion
     // after the first barrier (the component warps store the new spin after it)
-    double wx = 0.0, wy = 0.0, wz = 0.0;
+    double wx = 0.0, wy = 0.0, wz = 0.0, qw = 1.0, qx = 0.0, qy = 0.0, qz = 0.0;
     if (q == 3 && live) {
         wx = d.wx[i];
         wy = d.wy[i];
         wz = d.wz[i];
+        qw = d.qw[i];  // loaded here: their latency hides behind the walls
+        qx = d.qx[i];
+        qy = d.qy[i];
+        qz = d.qz[i];
         const double x = d.px[i], y = d.py[i], z = d.pz[i];
         const double vx = d.vx[i], vy = d.vy[i], vz = d.vz[i];
         const double r = d.r[i];
@@ -2607,7 +2615,6 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
     // the quaternion (integrate_body's update, from the starting spin) runs
     // while the component warps update the position, velocity and spin
     if (q == 3 && live) {
-        const double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
         const bool spinless = (__double_as_longlong(wx) | __double_as_longlong(wy) |
                                __double_as_longlong(wz)) == 0ll;
         const bool identity = spinless && __double_as_longlong(qw) == 0x3ff0000000000000ll &&
@@ -2623,8 +2630,7 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
                 ny = __fma_rn(qz, hx, __fma_rn(qx, hz, __fma_rn(qw, hy, qy)));
                 nz = __fma_rn(-qy, hx, __fma_rn(qx, hy, __fma_rn(qw, hz, qz)));
             }
-            const double inq =
-                rsqrt(__fma_rn(nz, nz, __fma_rn(ny, ny, __fma_rn(nx, nx, nw * nw))));
+            const double inq = rsqrt(__fma_rn(nz, nz, __fma_rn(ny, ny, __fma_rn(nx, nx, nw * nw))));
             d.qw[i] = nw * inq;
             d.qx[i] = nx * inq;
             d.qy[i] = ny * inq;
