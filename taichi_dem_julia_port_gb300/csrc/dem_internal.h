@@ -263,10 +263,6 @@ void launch_broadphase(const DemDev& d, const DemParams& p, int cur, bool multi,
 // particle searches (bond initialisation).
 void launch_search(const DemDev& d, const DemParams& p, int cur, bool init, bool multi, bool all,
                    const LaunchShape& sh, cudaStream_t s);
-// update_contacts! from the neighbour lists (scenes that do not search this
-// step), with their next rows
-void launch_lists(const DemDev& d, const DemParams& p, int cur, bool multi, const LaunchShape& sh,
-                  cudaStream_t s);
 void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, const LaunchShape& sh,
                   cudaStream_t s);
 void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,

@@ -26,8 +26,7 @@
 //                resolve_wall!, apply_body_force!, update!
 // All of it is captured once in a CUDA graph per contact-buffer parity (three
 // launches per step).  The standalone broad-phase kernels (k_hash,
-// k_scan_excl, k_scatter, k_canon) serve the cp_list inspection entry point;
-// the standalone list kernel (k_vdetect) is not on the step path.
+// k_scan_excl, k_scatter, k_canon) serve the cp_list inspection entry point.
 #include <type_traits>
 
 #include "dem_device.cuh"
@@ -1193,15 +1192,6 @@ __device__ __forceinline__ void list_phase(const DemDev& d, const DemParams& p, 
         emit_rows<kVLanes>(d, p, cur, active, job, lane);
         __syncwarp();
     }
-}
-
-template <bool MULTI, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB) k_vdetect(DemDev d, DemParams p, int cur) {
-    __shared__ ListShared sh[kThreads / kVLanes];
-    dep_begin(p.dep == 2);
-    // a single-scene handle decides from its one flag
-    if (!MULTI && d.sflags[cur][0] != 0u) return;
-    list_phase<MULTI>(d, p, cur, sh);
 }
 
 // ---------------------------------------------------------------------------
@@ -2874,18 +2864,6 @@ void launch_search(const DemDev& d, const DemParams& p, int cur, bool init, bool
     if (p.n == 0) return;
     if (sh.detect_blocks_per_sm == 3) launch_search_b<3>(d, p, cur, init, multi, all, s);
     else launch_search_b<4>(d, p, cur, init, multi, all, s);
-}
-
-void launch_lists(const DemDev& d, const DemParams& p, int cur, bool multi, const LaunchShape& sh,
-                  cudaStream_t s) {
-    if (p.n == 0) return;
-    const int nv = max(1, min(blocks_for((long long)p.n * kVLanes, kThreads), p.sms * 8));
-    if (sh.detect_blocks_per_sm == 3)
-        launch(p.dep != 0, multi ? k_vdetect<true, 3> : k_vdetect<false, 3>, nv, kThreads, s, d, p,
-               cur);
-    else
-        launch(p.dep != 0, multi ? k_vdetect<true, 4> : k_vdetect<false, 4>, nv, kThreads, s, d, p,
-               cur);
 }
 
 void launch_force(const DemDev& d, const DemParams& p, int nxt, bool multi, const LaunchShape& sh,
