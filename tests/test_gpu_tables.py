@@ -58,6 +58,39 @@ def test_standard_tables_equal_dem_create(gpu):
     b.close()
 
 
+def test_rolling_resistance_declared_not_applied(gpu):
+    """The reference declares the rolling-resistance coefficients
+    (src/config.jl:26, 30; Surface.μᵣ, src/types.jl:20) and applies them in no
+    force law (src/kernels.jl:170-426): results do not depend on them, whether
+    they come through the config (dem_create) or the surface table
+    (dem_create_tables), for bonds, Hertz contacts and wall contacts alike."""
+    sc = scenes.bonded_cube(8, speed=10.0, steps=0, seed=4)
+    cl_cfg, cl = random_cloud(1500, (0.03, 0.03, 0.03), 0.0008, 0.0015, seed=7, v=0.5)
+    for cfg, p, steps, bond in ((sc.cfg, sc.particles, 250, True), (cl_cfg, cl, 100, False)):
+        rr = cfg.replace(pp_coefficient_rolling_resistance=0.5,
+                         pw_coefficient_rolling_resistance=0.3)
+        t = Tables.standard(cfg, p)
+        for row in t.surfaces:
+            for s in row:
+                s.rolling_resistance = 0.7
+        runs = [GlobalData(cfg, p), GlobalData(rr, p), GlobalData(cfg, p, tables=t)]
+        outs = []
+        for g in runs:
+            if bond:
+                g.initialize()
+            g.simulate(steps)
+            outs.append((g.particles(), g.contacts()))
+            g.close()
+        for pa, ca in outs[1:]:
+            for k in pa:
+                np.testing.assert_array_equal(pa[k], outs[0][0][k], err_msg=k)
+            for k in ca:
+                np.testing.assert_array_equal(ca[k], outs[0][1][k], err_msg=k)
+        c0 = outs[0][1]
+        assert len(c0["i"]) > 0 and np.abs(outs[0][0]["wall_shear"]).sum() > 0
+        assert c0["bonded"].all() if bond else not c0["bonded"].any()
+
+
 def test_two_materials_two_walls_granular(gpu):
     """A polydisperse cloud of two materials thrown into the corner of two
     walls of a third material: Hertz-Mindlin per material pair and per wall,
