@@ -220,6 +220,10 @@ typedef struct DemStats {
     int32_t precision;       /* DEM_FP64 or DEM_FP32_FORCE              */
     int64_t full_searches;   /* steps that ran the full pair search (the
                                 others tested the neighbour lists)      */
+    int64_t exchanges_direct;/* dem_step_exchange calls whose last step's
+                                integrator wrote the state into the
+                                caller's buffers while it ran (the others
+                                read it after the step)                 */
 } DemStats;
 
 typedef struct DemHandle DemHandle;

@@ -125,7 +125,7 @@ class DemStats(C.Structure):
                 ("bonded", C.c_int64), ("bonds_broken", C.c_int64), ("contacts_ended", C.c_int64),
                 ("contacts_created", C.c_int64), ("warn_gap", C.c_int64),
                 ("warn_damping", C.c_int64), ("error", C.c_int32), ("precision", C.c_int32),
-                ("full_searches", C.c_int64)]
+                ("full_searches", C.c_int64), ("exchanges_direct", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -5,6 +5,7 @@
 // (`simulate!`, src/executor.jl:162-172), host<->device state exchange, and the
 // arena of independent scenes (slot and bucket-range allocation, scene modes).
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -371,6 +372,7 @@ struct DemHandle {
     FreeList pfree, tfree;
     int cur = 0;  // contact buffer holding the current state
     int64_t steps = 0;
+    int64_t exchanges_direct = 0;  // fused downloads of dem_step_exchange
     int ntiles_cells = 0;
     LaunchShape shape{};
     cudaStream_t stream = nullptr;
@@ -963,7 +965,7 @@ bool host_readable(const void* p) {
 // `fb` 0 or 1, flags a full search when a particle left its skin.
 int exchange(DemHandle* h, int64_t p0, int64_t n, const int* k, double* const* host,
              double* const (*cols)[4], int nfields, bool to_cols, int* error = nullptr,
-             bool sync = true, int posf = -1, int fb = -1) {
+             bool sync = true, int posf = -1, int fb = -1, const HostOut* arm = nullptr) {
     if (error && !h->err_host) {
         CU(cudaMallocHost(&h->err_host, 64));
         h->err_dev = reinterpret_cast<int*>(device_view(h->err_host));
@@ -1007,6 +1009,10 @@ int exchange(DemHandle* h, int64_t p0, int64_t n, const int* k, double* const* h
                 if (staged[f])
                     CU(cudaMemcpyAsync(staged[f], src_host[f], sizeof(double) * x.k[f] * n,
                                        cudaMemcpyHostToDevice, h->stream));
+        if (arm && xpos >= 0) {
+            x.arm = 1;
+            x.hout = *arm;
+        }
         if (xpos >= 0) launch_xfer_pos(x, (int)n, h->d, h->p, xpos, fb, h->stream);
         else launch_xfer(x, (int)n, (int)p0, to_cols, h->stream);
         CU(cudaGetLastError());
@@ -1180,6 +1186,7 @@ int stats_of(DemHandle* h, int32_t s, const SceneHost& S, DemStats* out) {
     out->warn_gap = (int64_t)sc.warn_gap;
     out->warn_damping = (int64_t)sc.warn_damp;
     out->full_searches = (int64_t)sc.searches;
+    out->exchanges_direct = h->multi ? 0 : h->exchanges_direct;
     out->error = error_code(c.error);
     out->precision = h->p.precision;
     return DEM_OK;
@@ -1649,7 +1656,8 @@ int dem_get_particles(DemHandle* h, DemParticleState* out) {
     return dem_scene_get_particles(h, 0, out);
 }
 
-int set_particles(DemHandle* h, const DemParticleState* in, bool sync) {
+int set_particles(DemHandle* h, const DemParticleState* in, bool sync,
+                  const HostOut* arm = nullptr) {
     const SceneHost* S = scene_at(h, 0);
     if (!S || !in || h->multi) return DEM_ERR_INVALID;
     const int64_t n = S->sp.n;
@@ -1675,7 +1683,7 @@ int set_particles(DemHandle* h, const DemParticleState* in, bool sync) {
     // new positions: the exchange kernel refreshes the FP32 positions; the
     // neighbour lists stay valid while every particle lies within skin/2 of
     // where they were built, else the next step searches in full
-    return exchange(h, 0, n, k, host, cols, 5, true, nullptr, sync, 0, h->cur);
+    return exchange(h, 0, n, k, host, cols, 5, true, nullptr, sync, 0, h->cur, arm);
 }
 
 int dem_set_particles(DemHandle* h, const DemParticleState* in) {
@@ -1686,9 +1694,66 @@ int dem_set_particles_async(DemHandle* h, const DemParticleState* in) {
     return set_particles(h, in, false);
 }
 
+// The fused download of an exchanged step: the device addresses of the
+// caller's output records (every non-null field must be device-accessible:
+// page-locked host or device memory) and of the page-locked error word.
+constexpr int kNoHostOut = INT_MIN;  // the error word's sentinel: no fused download ran
+bool fused_download(DemHandle* h, const DemParticleState* out, HostOut* ho) {
+    double* const f[kHostOutFields] = {out->pos,   out->vel,    out->omega,     out->quat,
+                                       out->force, out->moment, out->wall_shear};
+    for (int q = 0; q < kHostOutFields; ++q) {
+        ho->rec[q] = nullptr;
+        if (f[q] && !(ho->rec[q] = device_view(f[q]))) return false;
+    }
+    if (!h->err_host) {
+        if (cudaMallocHost(&h->err_host, 64) != cudaSuccess) {
+            cudaGetLastError();
+            h->err_host = nullptr;
+            return false;
+        }
+        h->err_dev = reinterpret_cast<int*>(device_view(h->err_host));
+    }
+    ho->err = h->err_dev;
+    ho->done = 0u;
+    return h->err_dev != nullptr;
+}
+
 int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
                       DemParticleState* out) {
     if (!h || nsteps < 0 || h->multi) return DEM_ERR_INVALID;
+    HostOut ho{};
+    const SceneHost* S = scene_at(h, 0);
+    if (in && in->pos && out && nsteps > 0 && nsteps <= INT_MAX && S && S->sp.n > 0 &&
+        fused_download(h, out, &ho)) {
+        // the upload arms the fused exchange: the last step's integrator
+        // writes the state into `out` while it runs, instead of a separate
+        // read after the step; the split integrator also reads the
+        // orientations and the first wall's shear history from `in` itself
+        // (the upload before the step carries positions, velocities, spins)
+        *reinterpret_cast<volatile int*>(h->err_host) = kNoHostOut;
+        ho.steps_left = ho.steps_total = (int)nsteps;
+        ho.qin = ho.wsin = nullptr;
+        DemParticleState up = *in;
+        if (split_integrator(h->shape, h->p.n, h->p.sms)) {  // the step graph's layout
+            if (in->quat && (ho.qin = device_view(in->quat))) up.quat = nullptr;
+            if (in->wall_shear && (ho.wsin = device_view(in->wall_shear))) up.wall_shear = nullptr;
+        }
+        TRY(set_particles(h, &up, false, &ho));
+        const int rc = dem_step(h, nsteps);
+        if (rc != DEM_OK) {  // disarm before any later step can see it
+            cudaMemsetAsync(&h->d.ctr->hout, 0, sizeof(HostOut), h->stream);
+            cudaStreamSynchronize(h->stream);
+            return rc;
+        }
+        CU(cudaStreamSynchronize(h->stream));
+        const int err = *reinterpret_cast<volatile int*>(h->err_host);
+        if (err != kNoHostOut) {
+            ++h->exchanges_direct;
+            return error_code(err);
+        }
+        // an integrator with one thread per particle ran: the usual read
+        return dem_get_particles(h, out);
+    }
     if (in) TRY(set_particles(h, in, false));
     TRY(dem_step(h, nsteps));
     if (out) return dem_get_particles(h, out);

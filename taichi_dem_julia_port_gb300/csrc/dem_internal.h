@@ -135,6 +135,30 @@ struct alignas(8) RowCounter {
     unsigned int rows, bonds;
 };
 
+// The fused exchange of dem_step_exchange: the upload arms it, and the
+// integrator of the last of `steps_left` steps writes the particle state
+// straight into the caller's device-accessible page-locked records (the
+// DemParticleState fields in their order: pos, vel, omega, quat, force,
+// moment, wall_shear; nullptr: not written) and then the device error word
+// into `err`.  With `qin` / `wsin` set, the upload left the orientations /
+// the first wall's shear history out and the integrator of the first step
+// (steps_left == steps_total) reads them from these records instead.  Every
+// integrator launch of an armed handle counts its blocks in `done`; the last
+// block out decrements `steps_left`, so the arming lasts exactly steps_total
+// launches.  An integrator that cannot use the records (one thread per
+// particle: the host then uploads every field) only counts, and `err` keeps
+// the host's sentinel, so the host reads the state the usual way.
+constexpr int kHostOutFields = 7;
+constexpr int kHostOutRows = 22;  // 3+3+3+4+3+3+3 values per particle
+struct HostOut {
+    double* rec[kHostOutFields];
+    const double* qin;   // orientations (4n), or nullptr: uploaded
+    const double* wsin;  // first wall's shear history (3n), or nullptr: uploaded
+    int* err;
+    int steps_left, steps_total;
+    unsigned int done;
+};
+
 struct DevCounters {
     int error;
     unsigned int bmax;        // largest bucket id of this step (k_hash), reset by k_canon
@@ -147,6 +171,7 @@ struct DevCounters {
     // inspection of the fused pair search (DemParams::debug_enum): candidate
     // pairs (i, j > i) it visited and the wrapping sum of enum_mix(i, j)
     unsigned long long enum_pairs, enum_hash;
+    HostOut hout;  // the fused download (zero: not armed)
 };
 
 // scan sites: each has its own ticket counter and tile-state array
@@ -248,6 +273,13 @@ struct LaunchShape {
     int integrate_lanes;       // integrator: 0 auto, 1 or 4 lanes per particle
 };
 
+// The integrator layout: split over four warps per 32 particles
+// (k_integrate_split) where one thread per particle would leave the SM
+// sub-partitions with at most two warps each, or as the shape asks.
+inline bool split_integrator(const LaunchShape& sh, long long n, int sms) {
+    return sh.integrate_lanes == 4 || (sh.integrate_lanes == 0 && n <= (long long)sms * 256);
+}
+
 // ---- launchers (dem_kernels.cu) --------------------------------------------
 // All launches go to `s`.  `cur` selects the contact buffer that holds the
 // state at the start of the step; the step writes buffer cur^1.  `multi`
@@ -294,6 +326,8 @@ struct XferSet {
     int nf;
     const int* err_src;  // with err_dst (device-accessible): the kernel copies
     int* err_dst;        // the device error word (nullptr: no copy)
+    int arm;             // an upload with positions: also arms the fused download
+    HostOut hout;
 };
 void launch_xfer(const XferSet& x, int n, int p0, bool to_cols, cudaStream_t s);
 // the upload of a single-scene handle whose field `posf` holds positions:

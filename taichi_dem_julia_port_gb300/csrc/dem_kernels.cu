@@ -2254,11 +2254,40 @@ __device__ __forceinline__ void wall_contact(const DemDev& d, int sc, const Wall
     }
 }
 
+// The fused download of an exchanged step (HostOut): the armed step count
+// as this launch sees it (0 for arena kernels and unarmed handles; every
+// block of a launch reads the same value, since it changes only after all
+// of them have counted themselves out).
+template <bool MULTI>
+__device__ __forceinline__ int host_out_left(const DemDev& d) {
+    if constexpr (MULTI) return 0;
+    else return __ldcg(&d.ctr->hout.steps_left);
+}
+// One thread per block, after the block's records are written (`wrote`) or
+// at any point (an integrator that writes none): the last block of the
+// launch disarms one step and, after the last armed step's records, copies
+// the device error word (no integrator raises one) to the host.
+__device__ __forceinline__ void host_out_count(const DemDev& d, int left, bool wrote) {
+    HostOut& H = d.ctr->hout;
+    __threadfence();
+    if (atomicAdd(&H.done, 1u) != gridDim.x - 1) return;
+    __threadfence();
+    if (left == 1 && wrote) *H.err = __ldcg(&d.ctr->error);
+    H.done = 0u;
+    H.steps_left = left - 1;
+}
+
 template <bool MULTI, bool F32, bool TAB = false>
 __device__ __forceinline__ void integrate_body(const DemDev& d, const DemParams& p, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nxt = cur ^ 1;
     if (i == 0) d.ctr->alloc[cur] = RowCounter{0u, 0u};  // the free buffer is next step's target
+    // an armed handle's step: this layout writes no records (the host reads
+    // the state the usual way), it only counts the launch
+    if (!MULTI && threadIdx.x == 0) {
+        const int left = host_out_left<MULTI>(d);
+        if (left > 0) host_out_count(d, left, false);
+    }
     // the end-of-step rebuild-flag work of every scene (see scene_flags_one):
     // it only ORs into the next flags, as the particles' skin test does
     for (int s = i; s < p.ns; s += gridDim.x * blockDim.x) scene_flags_one<MULTI>(d, p, cur, s);
@@ -2509,6 +2538,11 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
     __shared__ double s_wall[NW][6][32];  // each wall's force and moment on each particle
     __shared__ uint8_t s_touch[NW][32];
     __shared__ float s_pos[3][32];        // the new FP32 position components
+    // an armed single-scene step: the new state of the block's particles, as
+    // rows of the output records (HostOut), and the first armed step's
+    // orientations and first-wall shear histories read from the caller's
+    __shared__ double s_out[MULTI ? 1 : kHostOutRows][32];
+    __shared__ double s_in[MULTI ? 1 : 7][32];
     // 0, 1, 2: component; 3: walls and quaternion.  The roles rotate with
     // the block's round over the SMs: warp w of a block runs on SM
     // sub-partition w, and blocks are placed one per SM in turn (blocks b,
@@ -2522,6 +2556,14 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
     const int i = blockIdx.x * 32 + l;
     const int nxt = cur ^ 1;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int left = host_out_left<MULTI>(d);
+    const bool out = !MULTI && left == 1;  // this launch writes the caller's records
+    const double* qin = nullptr;           // this launch reads these from the caller's
+    const double* wsin = nullptr;
+    if (!MULTI && left > 0 && left == __ldcg(&d.ctr->hout.steps_total)) {
+        qin = d.ctr->hout.qin;
+        wsin = d.ctr->hout.wsin;
+    }
     if (t == 0) d.ctr->alloc[cur] = RowCounter{0u, 0u};  // the free buffer is next step's target
     for (int s2 = t; s2 < p.ns; s2 += gridDim.x * blockDim.x) scene_flags_one<MULTI>(d, p, cur, s2);
     // every thread reaches both barriers; `live`: a particle of a stepping scene
@@ -2554,6 +2596,21 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
             }
         }
     }
+    if constexpr (!MULTI) {
+        if (q == 3 && (qin || wsin)) {
+            // the block's 32 particles are one contiguous range of each
+            // record array: consecutive lanes read it, then each lane its own
+            const int i0 = blockIdx.x * 32, m = min(32, p.n - i0);
+            if (qin)
+                for (int e = l; e < 4 * m; e += 32) s_in[e & 3][e >> 2] = qin[(size_t)4 * i0 + e];
+            if (wsin)
+                for (int e = l; e < 3 * m; e += 32) {
+                    const int pq = e / 3;
+                    s_in[4 + e - 3 * pq][pq] = wsin[(size_t)3 * i0 + e];
+                }
+            __syncwarp();
+        }
+    }
     // warp 3: the step's starting spin, for the walls now and the quaternion
     // after the first barrier (the component warps store the new spin after it)
     double wx = 0.0, wy = 0.0, wz = 0.0, qw = 1.0, qx = 0.0, qy = 0.0, qz = 0.0;
@@ -2561,10 +2618,27 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
         wx = d.wx[i];
         wy = d.wy[i];
         wz = d.wz[i];
-        qw = d.qw[i];  // loaded here: their latency hides behind the walls
-        qx = d.qx[i];
-        qy = d.qy[i];
-        qz = d.qz[i];
+        bool qhost = false;
+        if constexpr (!MULTI) {
+            if (qin) {
+                qw = s_in[0][l];
+                qx = s_in[1][l];
+                qy = s_in[2][l];
+                qz = s_in[3][l];
+                qhost = true;
+            }
+            if (wsin) {  // the first wall's shear history, for wall_force below
+                d.wsx[i] = s_in[4][l];
+                d.wsy[i] = s_in[5][l];
+                d.wsz[i] = s_in[6][l];
+            }
+        }
+        if (!qhost) {
+            qw = d.qw[i];  // loaded here: their latency hides behind the walls
+            qx = d.qx[i];
+            qy = d.qy[i];
+            qz = d.qz[i];
+        }
         const double x = d.px[i], y = d.py[i], z = d.pz[i];
         const double vx = d.vx[i], vy = d.vy[i], vz = d.vz[i];
         const double r = d.r[i];
@@ -2599,6 +2673,11 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
                 }
             }
         }
+        if (out) {  // the first wall's shear history as this thread left it
+            s_out[19][l] = d.wsx[i];
+            s_out[20][l] = d.wsy[i];
+            s_out[21][l] = d.wsz[i];
+        }
     }
     __syncthreads();  // walls in shared memory; every component thread has read in_cnt
     if (q == 3 && exists) d.in_cnt[i] = 0;
@@ -2610,6 +2689,7 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
         const bool identity = spinless && __double_as_longlong(qw) == 0x3ff0000000000000ll &&
                               (__double_as_longlong(qx) | __double_as_longlong(qy) |
                                __double_as_longlong(qz)) == 0ll;
+        double ow = qw, ox = qx, oy = qy, oz = qz;
         if (!identity) {
             double nw = qw, nx = qx, ny = qy, nz = qz;
             if (!(spinless && finite_not_negzero(qw) && finite_not_negzero(qx) &&
@@ -2621,10 +2701,25 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
                 nz = __fma_rn(-qy, hx, __fma_rn(qx, hy, __fma_rn(qw, hz, qz)));
             }
             const double inq = rsqrt(__fma_rn(nz, nz, __fma_rn(ny, ny, __fma_rn(nx, nx, nw * nw))));
-            d.qw[i] = nw * inq;
-            d.qx[i] = nx * inq;
-            d.qy[i] = ny * inq;
-            d.qz[i] = nz * inq;
+            ow = nw * inq;
+            ox = nx * inq;
+            oy = ny * inq;
+            oz = nz * inq;
+            d.qw[i] = ow;
+            d.qx[i] = ox;
+            d.qy[i] = oy;
+            d.qz[i] = oz;
+        } else if (qin) {  // read from the caller's: the columns still hold the old ones
+            d.qw[i] = ow;
+            d.qx[i] = ox;
+            d.qy[i] = oy;
+            d.qz[i] = oz;
+        }
+        if (out) {
+            s_out[9][l] = ow;
+            s_out[10][l] = ox;
+            s_out[11][l] = oy;
+            s_out[12][l] = oz;
         }
     }
     if (q < 3 && live) {
@@ -2649,15 +2744,26 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
         const double pq1 = xq + vq * dt + aq * hdt2;
         pick3(q, d.px, d.py, d.pz)[i] = pq1;
         s_pos[q][l] = d2f(pq1 - S.dmin[q]);
-        pick3(q, d.vx, d.vy, d.vz)[i] = vq + aq * dt;
+        const double vq1 = vq + aq * dt;
+        pick3(q, d.vx, d.vy, d.vz)[i] = vq1;
         // 𝛚 + 𝐌·I⁻¹dt; with Mq = +0, a finite I⁻¹dt and wq not -0 the sum
         // is wq and the stored spin stays
-        if (!(__double_as_longlong(Mq) == 0ll && product_finite(ii, dt) && not_negzero(wq)))
-            pick3(q, d.wx, d.wy, d.wz)[i] = __fma_rn(Mq, ii * dt, wq);
+        double wq1 = wq;
+        if (!(__double_as_longlong(Mq) == 0ll && product_finite(ii, dt) && not_negzero(wq))) {
+            wq1 = __fma_rn(Mq, ii * dt, wq);
+            pick3(q, d.wx, d.wy, d.wz)[i] = wq1;
+        }
         pick3(q, d.fx, d.fy, d.fz)[i] = Fq;
         pick3(q, d.tx, d.ty, d.tz)[i] = Mq;
+        if (out) {
+            s_out[q][l] = pq1;
+            s_out[3 + q][l] = vq1;
+            s_out[6 + q][l] = wq1;
+            s_out[13 + q][l] = Fq;
+            s_out[16 + q][l] = Mq;
+        }
     }
-    __syncthreads();  // the new position components in shared memory
+    __syncthreads();  // the new position components (and an armed step's rows) in shared memory
     if (q == 3 && live) {
         const float fx = s_pos[0][l], fy = s_pos[1][l], fz = s_pos[2][l];
         d.pos32[i] = make_float4(fx, fy, fz, reach32(fx, fy, fz, d.rm32[i].z));
@@ -2666,6 +2772,30 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
         const unsigned peers = __match_any_sync(am, moved ? sc : -1);
         if (moved && lane_id() == (unsigned)(__ffs(peers) - 1) && d.sflags[nxt][sc] == 0u)
             atomicOr(&d.sflags[nxt][sc], 1u);
+    }
+    if constexpr (!MULTI) {
+        if (left > 0) {
+            if (out) {
+                // the block's 32 particles are one contiguous range of each
+                // record array: k·32 values, written by consecutive threads
+                const int i0 = blockIdx.x * 32, m = min(32, p.n - i0);
+                int row = 0;
+#pragma unroll
+                for (int f = 0; f < kHostOutFields; ++f) {
+                    const int k = f == 3 ? 4 : 3;
+                    double* rec = d.ctr->hout.rec[f];
+                    if (rec) {
+                        for (int e = threadIdx.x; e < k * 32; e += kSplitThreads) {
+                            const int pq = e / k;
+                            if (pq < m) rec[(size_t)k * i0 + e] = s_out[row + e - pq * k][pq];
+                        }
+                    }
+                    row += k;
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) host_out_count(d, left, out);
+        }
     }
 }
 
@@ -2891,11 +3021,7 @@ void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
                       const LaunchShape& sh, cudaStream_t s) {
     if (p.n == 0) return;
     const int block = clamp_block(sh.integrate_block);
-    // the split integrator while one thread per particle would leave the SM
-    // sub-partitions with at most two warps each
-    const bool split = sh.integrate_lanes == 4 ||
-                       (sh.integrate_lanes == 0 && (long long)p.n <= (long long)p.sms * 256);
-    if (split) {
+    if (split_integrator(sh, p.n, p.sms)) {
         const int nb = blocks_for(p.n, 32);
         if (p.tab)
             launch(p.dep != 0, k_integrate_split_tab, nb, kSplitThreads, s, d, p, cur);
@@ -3153,7 +3279,8 @@ void launch_refresh_pos32(const DemDev& d, const DemParams& p, bool multi, int f
 // Small blocks put a 17,576-particle scene on every SM.  REFRESH (an upload
 // to a single-scene handle, field `posf` the positions): the FP32 position
 // and the skin test of each slot, from the uploaded values, as
-// k_refresh_pos32 does.
+// k_refresh_pos32 does; with x.arm, it also arms the fused download
+// (HostOut) of the exchanged step that follows.
 constexpr int kXferBlock = 64;
 static_assert(4 * kXferBlock <= kThreads, "one record value per thread and field");
 template <bool REFRESH>
@@ -3178,6 +3305,8 @@ __global__ void __launch_bounds__(kThreads)
         }
         s_ncol = cc;
         if (x.err_dst && blockIdx.x == 0) *x.err_dst = __ldcg(x.err_src);
+        // the step's integrators run after this kernel (stream order)
+        if (REFRESH && x.arm && blockIdx.x == 0) d.ctr->hout = x.hout;
     }
     if (to_cols) {
         double v[kXferFields];
