@@ -385,6 +385,19 @@ struct DemHandle {
     int64_t xfer_n = 0;        // doubles
     int* err_host = nullptr;   // page-locked copy of the device error word
     int* err_dev = nullptr;    // its device address
+    // the exchanged step of dem_step_exchange as one graph per contact-buffer
+    // parity, for one set of caller buffers (key: their device addresses):
+    // the position upload, then the contact update while a second stream
+    // uploads velocities and spins, then forces and the integration (which
+    // reads orientations and wall shear from the caller and writes the state
+    // back into the caller's buffers)
+    static constexpr int kXKey = 13;
+    struct XGraph {
+        cudaGraphExec_t exec = nullptr;
+        const void* key[kXKey] = {};
+    } xg[2];
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     int32_t* io_idx = nullptr;  // p4c records: per-slot counts and their scan (2n + 1)
     int64_t io_idx_n = 0;
     void* io_rec = nullptr;     // p4c records (64 bytes each)
@@ -494,9 +507,15 @@ int allocate(DemHandle* h) {
     return DEM_OK;
 }
 
+void drop_graphs(DemHandle* h);
+
 void free_all(DemHandle* h) {
-    for (int b = 0; b < 2; ++b)
-        if (h->exec[b]) cudaGraphExecDestroy(h->exec[b]);
+    drop_graphs(h);
+    if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+    if (h->join_ev) cudaEventDestroy(h->join_ev);
+    if (h->side) cudaStreamDestroy(h->side);
+    h->fork_ev = h->join_ev = nullptr;
+    h->side = nullptr;
     for (void* p : h->allocs) cudaFree(p);
     h->allocs.clear();
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -721,6 +740,8 @@ void drop_graphs(DemHandle* h) {
     for (int b = 0; b < 2; ++b) {
         if (h->exec[b]) cudaGraphExecDestroy(h->exec[b]);
         h->exec[b] = nullptr;
+        if (h->xg[b].exec) cudaGraphExecDestroy(h->xg[b].exec);
+        h->xg[b].exec = nullptr;
     }
 }
 
@@ -757,6 +778,7 @@ int update_bounds(DemHandle* h) {
 
 int build_graphs(DemHandle* h) {
     if (h->graph_precision == h->p.precision && h->exec[0]) return DEM_OK;
+    drop_graphs(h);
     for (int b = 0; b < 2; ++b) {
         if (h->exec[b]) {
             cudaGraphExecDestroy(h->exec[b]);
@@ -1694,11 +1716,71 @@ int dem_set_particles_async(DemHandle* h, const DemParticleState* in) {
     return set_particles(h, in, false);
 }
 
-// The fused download of an exchanged step: the device addresses of the
-// caller's output records (every non-null field must be device-accessible:
-// page-locked host or device memory) and of the page-locked error word.
-constexpr int kNoHostOut = INT_MIN;  // the error word's sentinel: no fused download ran
-bool fused_download(DemHandle* h, const DemParticleState* out, HostOut* ho) {
+// One exchanged step as a graph (DemHandle::XGraph): captured once per
+// contact-buffer parity and set of caller buffers, replayed afterwards.
+static int capture_exchange(DemHandle* h, int cur, double* pv, double* vv, double* ov,
+                     const HostOut& ho, cudaGraphExec_t* exec) {
+    if (!h->side) {
+        CU(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+        CU(cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
+        CU(cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming));
+    }
+    const DemDev& d = h->d;
+    const int n = h->p.n;
+    XferSet xp{};  // positions: FP32 copies, skin test, arming
+    xp.rec[0] = pv;
+    xp.col[0][0] = d.px;
+    xp.col[0][1] = d.py;
+    xp.col[0][2] = d.pz;
+    xp.k[0] = 3;
+    xp.nf = 1;
+    xp.arm = 1;
+    xp.hout = ho;
+    XferSet xr{};  // velocities and spins, beside the contact update (which reads neither)
+    double* const rv[2] = {vv, ov};
+    double* const cv[2][3] = {{d.vx, d.vy, d.vz}, {d.wx, d.wy, d.wz}};
+    for (int f = 0; f < 2; ++f) {
+        if (!rv[f]) continue;
+        xr.rec[xr.nf] = rv[f];
+        for (int c = 0; c < 3; ++c) xr.col[xr.nf][c] = cv[f][c];
+        xr.k[xr.nf] = 3;
+        ++xr.nf;
+    }
+    CU(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    auto ok = [&](cudaError_t r) {
+        if (e == cudaSuccess) e = r;
+        return e == cudaSuccess;
+    };
+    if (xr.nf && ok(cudaEventRecord(h->fork_ev, h->stream)) &&
+        ok(cudaStreamWaitEvent(h->side, h->fork_ev, 0))) {
+        launch_xfer(xr, n, 0, true, h->side);
+        if (ok(cudaGetLastError())) ok(cudaEventRecord(h->join_ev, h->side));
+    }
+    if (e == cudaSuccess) {
+        launch_xfer_pos(xp, n, d, h->p, 0, cur, h->stream);
+        launch_search(d, h->p, cur, false, false, false, h->shape, h->stream);
+        if (ok(cudaGetLastError()) && xr.nf) ok(cudaStreamWaitEvent(h->stream, h->join_ev, 0));
+        if (e == cudaSuccess) {
+            launch_force(d, h->p, cur ^ 1, false, h->shape, h->stream);
+            launch_integrate(d, h->p, cur, false, h->shape, h->stream);
+            ok(cudaGetLastError());
+        }
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+    if (e == cudaSuccess) e = ec;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    CU(e);
+    return DEM_OK;
+}
+
+// The fused exchange: the device addresses of the caller's output records
+// (every non-null field must be device-accessible: page-locked host or
+// device memory) and of the page-locked error word.
+constexpr int kNoHostOut = INT_MIN;  // the error word's sentinel: no fused exchange ran
+static bool fused_download(DemHandle* h, const DemParticleState* out, HostOut* ho) {
     double* const f[kHostOutFields] = {out->pos,   out->vel,    out->omega,     out->quat,
                                        out->force, out->moment, out->wall_shear};
     for (int q = 0; q < kHostOutFields; ++q) {
@@ -1723,23 +1805,48 @@ int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
     if (!h || nsteps < 0 || h->multi) return DEM_ERR_INVALID;
     HostOut ho{};
     const SceneHost* S = scene_at(h, 0);
+    // the split integrator (the step graph's layout for this scene) reads
+    // orientations and the first wall's shear history from `in` and writes
+    // the state into `out` while it runs, instead of a separate read after
+    // the step; the upload before the step carries positions (and, in the
+    // graph of a single step, beside the contact update, velocities and spins)
     if (in && in->pos && out && nsteps > 0 && nsteps <= INT_MAX && S && S->sp.n > 0 &&
-        fused_download(h, out, &ho)) {
-        // the upload arms the fused exchange: the last step's integrator
-        // writes the state into `out` while it runs, instead of a separate
-        // read after the step; the split integrator also reads the
-        // orientations and the first wall's shear history from `in` itself
-        // (the upload before the step carries positions, velocities, spins)
+        split_integrator(h->shape, h->p.n, h->p.sms) && fused_download(h, out, &ho)) {
         *reinterpret_cast<volatile int*>(h->err_host) = kNoHostOut;
         ho.steps_left = ho.steps_total = (int)nsteps;
-        ho.qin = ho.wsin = nullptr;
-        DemParticleState up = *in;
-        if (split_integrator(h->shape, h->p.n, h->p.sms)) {  // the step graph's layout
-            if (in->quat && (ho.qin = device_view(in->quat))) up.quat = nullptr;
-            if (in->wall_shear && (ho.wsin = device_view(in->wall_shear))) up.wall_shear = nullptr;
+        ho.qin = in->quat ? device_view(in->quat) : nullptr;
+        ho.wsin = in->wall_shear ? device_view(in->wall_shear) : nullptr;
+        double* const pv = device_view(in->pos);
+        double* const vv = in->vel ? device_view(in->vel) : nullptr;
+        double* const ov = in->omega ? device_view(in->omega) : nullptr;
+        int rc = DEM_OK;
+        if (nsteps == 1 && pv && (!in->vel || vv) && (!in->omega || ov)) {
+            rc = ensure_encoding(h);
+            if (rc == DEM_OK) rc = build_graphs(h);
+            const void* key[DemHandle::kXKey] = {pv, vv, ov, ho.qin, ho.wsin, ho.err};
+            for (int q = 0; q < kHostOutFields; ++q) key[6 + q] = ho.rec[q];
+            DemHandle::XGraph& X = h->xg[h->cur];
+            if (rc == DEM_OK && (!X.exec || std::memcmp(X.key, key, sizeof(key)) != 0)) {
+                if (X.exec) cudaGraphExecDestroy(X.exec);
+                X.exec = nullptr;
+                rc = capture_exchange(h, h->cur, pv, vv, ov, ho, &X.exec);
+                if (rc == DEM_OK) std::memcpy(X.key, key, sizeof(key));
+            }
+            if (rc == DEM_OK) {
+                if (cudaGraphLaunch(X.exec, h->stream) == cudaSuccess) {
+                    h->cur ^= 1;
+                    h->steps += 1;
+                } else {
+                    rc = DEM_ERR_CUDA;
+                }
+            }
+        } else {
+            DemParticleState up = *in;
+            if (ho.qin) up.quat = nullptr;
+            if (ho.wsin) up.wall_shear = nullptr;
+            rc = set_particles(h, &up, false, &ho);
+            if (rc == DEM_OK) rc = dem_step(h, nsteps);
         }
-        TRY(set_particles(h, &up, false, &ho));
-        const int rc = dem_step(h, nsteps);
         if (rc != DEM_OK) {  // disarm before any later step can see it
             cudaMemsetAsync(&h->d.ctr->hout, 0, sizeof(HostOut), h->stream);
             cudaStreamSynchronize(h->stream);
@@ -1751,7 +1858,7 @@ int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
             ++h->exchanges_direct;
             return error_code(err);
         }
-        // an integrator with one thread per particle ran: the usual read
+        // not expected (the split layout writes the records): the usual read
         return dem_get_particles(h, out);
     }
     if (in) TRY(set_particles(h, in, false));
