@@ -787,7 +787,7 @@ def measure_scene(args, lib, sc, precision: str, steps: int, warmup: int, advanc
               "bonds_broken_in_window": s1["bonds_broken"] - s0["bonds_broken"],
               "bonds_broken_total": s1["bonds_broken"],
               "full_searches_in_window": s1["full_searches"] - s0["full_searches"]}
-    # per-phase device times over the same window (eager launches, L2 flushed)
+    # per-phase device times over the same window (events between the step's kernels, L2 flushed)
     restore(g, snap)
     phases = []
     for _ in range(profile_steps):

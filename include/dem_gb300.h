@@ -279,8 +279,9 @@ int dem_step(DemHandle* h, int64_t nsteps);
  * the device time of the nsteps (synchronises). */
 int dem_step_timed(DemHandle* h, int64_t nsteps, float* ms);
 
-/* One step launched phase by phase (no graph) with CUDA events between the
- * phases on the handle's stream.  phase_ms[0..2] (nphase >= 3; further
+/* One step as the step graph runs it, with CUDA events before, between and
+ * after its three kernels (one captured graph per contact-buffer parity, so
+ * no host launch latency falls inside a phase).  phase_ms[0..2] (nphase >= 3; further
  * entries are set to 0) receive the device time of: the contact update (the
  * full pair search of the scenes whose neighbour lists went stale — hash,
  * bucket scan, scatter, canonical order, cp_list enumeration with

@@ -152,7 +152,7 @@ class Arena:
         return float(ms.value)
 
     def step_profiled(self) -> dict:
-        """One step launched phase by phase; device milliseconds per phase."""
+        """One step with CUDA events between its kernels; device milliseconds per phase."""
         from .executor import GlobalData
         ms = (C.c_float * len(GlobalData.PHASES))()
         check(self.lib, self.lib.dem_step_profiled(self.h, ms, len(ms)), "dem_step_profiled")

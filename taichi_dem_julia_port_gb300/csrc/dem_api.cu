@@ -398,6 +398,10 @@ struct DemHandle {
     } xg[2];
     cudaStream_t side = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    // dem_step_profiled: the step's graph with an event before, between and
+    // after its three kernels, per contact-buffer parity
+    cudaGraphExec_t pg[2] = {nullptr, nullptr};
+    cudaEvent_t pev[4] = {nullptr, nullptr, nullptr, nullptr};
     int32_t* io_idx = nullptr;  // p4c records: per-slot counts and their scan (2n + 1)
     int64_t io_idx_n = 0;
     void* io_rec = nullptr;     // p4c records (64 bytes each)
@@ -513,6 +517,10 @@ void free_all(DemHandle* h) {
     drop_graphs(h);
     if (h->fork_ev) cudaEventDestroy(h->fork_ev);
     if (h->join_ev) cudaEventDestroy(h->join_ev);
+    for (cudaEvent_t& e : h->pev) {
+        if (e) cudaEventDestroy(e);
+        e = nullptr;
+    }
     if (h->side) cudaStreamDestroy(h->side);
     h->fork_ev = h->join_ev = nullptr;
     h->side = nullptr;
@@ -742,6 +750,8 @@ void drop_graphs(DemHandle* h) {
         h->exec[b] = nullptr;
         if (h->xg[b].exec) cudaGraphExecDestroy(h->xg[b].exec);
         h->xg[b].exec = nullptr;
+        if (h->pg[b]) cudaGraphExecDestroy(h->pg[b]);
+        h->pg[b] = nullptr;
     }
 }
 
@@ -1610,24 +1620,41 @@ int dem_step_profiled(DemHandle* h, float* phase_ms, int nphase) {
     for (int k = 0; k < nphase; ++k) phase_ms[k] = 0.f;
     if (h->n_cap == 0) return DEM_OK;
     TRY(ensure_encoding(h));
-    if (h->multi) {
-        TRY(build_graphs(h));
-        TRY(launch_inits(h));
-    }
-    cudaEvent_t ev[4];
-    for (int k = 0; k < 4; ++k) CU(cudaEventCreate(&ev[k]));
+    TRY(build_graphs(h));  // drops the profiled graphs too when the step graphs change
+    if (h->multi) TRY(launch_inits(h));
+    // the three kernels as the step graph runs them, with an event node
+    // before, between and after them (one graph launch: no host launch
+    // latency inside the timed phases)
+    for (cudaEvent_t& e : h->pev)
+        if (!e) CU(cudaEventCreate(&e));
     const int cur = h->cur, nxt = cur ^ 1;
-    cudaEventRecord(ev[0], h->stream);
-    launch_search(h->d, h->p, cur, false, h->multi, false, h->shape, h->stream);
-    cudaEventRecord(ev[1], h->stream);
-    launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
-    cudaEventRecord(ev[2], h->stream);
-    launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
-    cudaEventRecord(ev[3], h->stream);
-    cudaError_t e = cudaEventSynchronize(ev[3]);
+    if (!h->pg[cur]) {
+        CU(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaEventRecordWithFlags(h->pev[0], h->stream, cudaEventRecordExternal);
+        if (e == cudaSuccess) {
+            launch_search(h->d, h->p, cur, false, h->multi, false, h->shape, h->stream);
+            e = cudaEventRecordWithFlags(h->pev[1], h->stream, cudaEventRecordExternal);
+        }
+        if (e == cudaSuccess) {
+            launch_force(h->d, h->p, nxt, h->multi, h->shape, h->stream);
+            e = cudaEventRecordWithFlags(h->pev[2], h->stream, cudaEventRecordExternal);
+        }
+        if (e == cudaSuccess) {
+            launch_integrate(h->d, h->p, cur, h->multi, h->shape, h->stream);
+            e = cudaEventRecordWithFlags(h->pev[3], h->stream, cudaEventRecordExternal);
+        }
+        if (e == cudaSuccess) e = cudaGetLastError();
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+        if (e == cudaSuccess) e = ec;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&h->pg[cur], g, 0);
+        if (g) cudaGraphDestroy(g);
+        CU(e);
+    }
+    CU(cudaGraphLaunch(h->pg[cur], h->stream));
+    cudaError_t e = cudaEventSynchronize(h->pev[3]);
     for (int k = 0; k < 3 && e == cudaSuccess; ++k)
-        e = cudaEventElapsedTime(&phase_ms[k], ev[k], ev[k + 1]);
-    for (int k = 0; k < 4; ++k) cudaEventDestroy(ev[k]);
+        e = cudaEventElapsedTime(&phase_ms[k], h->pev[k], h->pev[k + 1]);
     CU(e);
     h->cur = nxt;
     h->steps += 1;

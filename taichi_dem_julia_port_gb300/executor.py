@@ -250,7 +250,7 @@ class GlobalData:
     PHASES = ("contacts", "force", "integrate")
 
     def simulate_profiled(self) -> dict:
-        """One step launched phase by phase; device milliseconds per phase."""
+        """One step with CUDA events between its kernels; device milliseconds per phase."""
         ms = (C.c_float * len(self.PHASES))()
         check(self.lib, self.lib.dem_step_profiled(self.h, ms, len(ms)), "dem_step_profiled")
         return dict(zip(self.PHASES, [float(x) for x in ms]))

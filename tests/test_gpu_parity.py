@@ -408,6 +408,31 @@ def assert_runs_identical(outs, what):
             assert s0.get(k) == s1.get(k), (what, k)
 
 
+def test_profiled_steps_equal_graph_steps(gpu):
+    """dem_step_profiled (the step's kernels with CUDA events between them)
+    steps exactly as dem_step does, on both contact buffers, and reports a
+    positive device time for each phase."""
+    sc = scenes.bonded_cube(8, speed=30.0, steps=0, seed=2)
+    a, b = GlobalData(sc.cfg, sc.particles), GlobalData(sc.cfg, sc.particles)
+    for g in (a, b):
+        g.initialize()
+    a.simulate(60)
+    for s in range(60):
+        if s % 3 == 0:  # both parities of the contact buffers
+            ph = b.simulate_profiled()
+            assert set(ph) == {"contacts", "force", "integrate"}
+            assert all(v > 0 for v in ph.values()), ph
+        else:
+            b.simulate(1)
+    pa, pb = a.particles(), b.particles()
+    for k in pa:
+        np.testing.assert_array_equal(pa[k], pb[k], err_msg=k)
+    assert pair_set(a.contacts()) == pair_set(b.contacts())
+    assert a.stats()["steps_done"] == b.stats()["steps_done"] == 60
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_integrate_layouts_bit_identical(gpu, precision):
     """The integrator with one thread per particle and split over four warps
