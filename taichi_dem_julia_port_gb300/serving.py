@@ -132,13 +132,17 @@ class ServeReport:
         return {f"p{q}": float(np.percentile(lat, q)) for q in qs} if lat.size else {}
 
 
+# launch-shape update of a served arena (see Server)
+SERVED_SHAPE = {"force_blocks_per_sm": 4}
+
+
 class Server:
     """Continuous-batching loop over one arena sized from an HBM budget."""
 
     def __init__(self, sizing: ArenaSizing, precision: str = "fp32", chunk_steps: int = 200,
                  cell_factor: float = 0.0, keep_state: bool = True, lib=None,
                  policy: str = "fifo", max_active: int = 0, min_chunk: int = 1,
-                 build_ahead: int = 4):
+                 build_ahead: int = 4, launch_shape: dict | None = None):
         """policy "fifo": waiting requests are admitted in arrival order as
         soon as they fit.  policy "sjf": the waiting request with the least
         work (particles x steps) first, and only while the live scenes hold
@@ -150,7 +154,14 @@ class Server:
         fewer to finish (so that its slots are freed promptly), but at least
         `min_chunk` (scenes freeze on the device at their step count, so a
         longer chunk never oversteps one).  While a chunk runs, the scenes of
-        up to `build_ahead` waiting requests are built on the host."""
+        up to `build_ahead` waiting requests are built on the host.
+
+        `launch_shape` updates the arena's launch shape (results do not
+        change).  By default the FP32 force kernel gets the register budget
+        for four blocks per SM: served scenes of up to 1e6 spheres put most
+        particles in large scenes, where it shortened the device time of the
+        100-request stream by 4-10 % (the many-small-scene batch prefers the
+        compiler's choice, which the arena keeps otherwise)."""
         if policy not in ("fifo", "sjf"):
             raise ValueError("policy must be 'fifo' or 'sjf'")
         self.policy = policy
@@ -160,6 +171,7 @@ class Server:
                            max_contacts=sizing.max_contacts, max_buckets=sizing.max_buckets,
                            max_coordinate_number=sizing.max_coordinate_number,
                            precision=precision, cell_factor=cell_factor, lib=lib)
+        self.arena.set_launch_shape(**(SERVED_SHAPE if launch_shape is None else launch_shape))
         self.chunk_steps = int(chunk_steps)
         self.min_chunk = max(1, min(int(min_chunk), self.chunk_steps))
         self.build_ahead = max(0, int(build_ahead))
