@@ -125,13 +125,13 @@ KERNELS_PER_STEP = 3
 # contact: 1.503e7 per launch), per bond 116.1 (the 17,576-sphere cube in its
 # fragmentation, 41,427 bonds and 6,670 Hertz contacts: 5.818e6 per launch,
 # less the Hertz share); FP32 mode per bond 15.0 (the same cube before its
-# impact).  Integrator per particle: 91.9 in FP64 mode (the cube in its
+# impact).  Integrator per particle: 92.0 in FP64 mode (the cube in its
 # fragmentation, split over four warps per 32 particles: 1.616e6 per launch;
 # the one-thread form measured 84.1), 51.0 in the FP32 mode (64 scenes of the
 # batched workload).  Then GB300's FP64 pipe width.
 FP64_INST = {("force", "fp64", "bond"): 116.1, ("force", "fp64", "hertz"): 151.0,
              ("force", "fp32", "bond"): 15.0,
-             ("integrate", "fp64"): 91.9, ("integrate", "fp32"): 51.0}
+             ("integrate", "fp64"): 92.0, ("integrate", "fp32"): 51.0}
 # The integrator skips the quaternion increment of a particle with exactly zero
 # spin, the normalisation of a spinless identity orientation and the spin
 # update of a particle with exactly zero torque: in the pour's settling phase

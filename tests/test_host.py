@@ -223,3 +223,15 @@ def test_corrupt_p4p_is_rejected_with_its_line(tmp_path):
         with pytest.raises(ValueError) as e:
             load_particles(f)
         assert msg in str(e.value), (name, str(e.value))
+
+
+def test_bench_byte_model_for_the_cube_window():
+    """bench.py's algorithmic bytes per kernel (every field once per unit)
+    for the 17,576-sphere cube's timed window (48,096 contacts, 41,427 of
+    them bonds): the figures its roofline divides by the phase times."""
+    import bench
+    alg = bench.algorithmic_bytes(17576, 48096, 41427)
+    assert alg == {"force": 14570456, "integrate": 10175040, "contacts": 2182024}
+    # a settling pour without contacts writes neither spin nor quaternion
+    assert bench.algorithmic_bytes(1000, 0, 0, settling=True)["integrate"] == 1000 * (360 - 56)
+    assert bench.algorithmic_bytes(1000, 0, 0)["force"] == 0
