@@ -1899,7 +1899,7 @@ int dem_host_alloc(int64_t bytes, void** out) {
     *out = nullptr;
     const size_t nb = (size_t)std::max<int64_t>(bytes, 1);
     CU(cudaMallocHost(out, nb));
-    double* dv = device_view(*out);  // before registration: the driver's answer
+    double* dv = device_view(*out);  // before registration: the CUDA driver's answer
     if (dv) {
         HostRanges& H = host_ranges();
         std::lock_guard<std::mutex> lk(H.mu);
