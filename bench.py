@@ -838,14 +838,19 @@ def measure_scene(args, lib, sc, precision: str, steps: int, warmup: int, advanc
         h2d = sum(a.nbytes for a in buf.arrays.values())
         reps = max(1, math.ceil(e2e_min_steps / steps))
         e2e_s = 0.0
-        for _ in range(reps):
+        for rep_ in range(reps):
             restore(g, snap)
             buf.download()
             torch.cuda.synchronize()
+            marked = rep_ == 0 and getattr(args, "profile_e2e", False)
+            if marked:
+                torch.cuda.cudart().cudaProfilerStart()
             t0 = time.perf_counter()
             for _ in range(steps):
                 buf.step(1)  # upload, step, download (dem_step_exchange)
             e2e_s += time.perf_counter() - t0
+            if marked:
+                torch.cuda.cudart().cudaProfilerStop()
         buf.close()
         e2e_s = max_over_ranks(e2e_s, dist)
         n_e2e = reps * steps
@@ -970,6 +975,9 @@ def main() -> None:
     ap.add_argument("--profiler-window", action="store_true",
                     help="mark the timed window with cudaProfilerStart/Stop (for ncu "
                          "--profile-from-start off); the work done is unchanged")
+    ap.add_argument("--profile-e2e", action="store_true",
+                    help="mark the first pass of the end-to-end loop instead (its "
+                         "exchanged steps)")
     ap.add_argument("--no-proxy", action="store_true",
                     help="skip the reference-structured GPU proxy (c1/c2)")
     args = ap.parse_args()

@@ -368,12 +368,14 @@ int dem_set_particles_async(DemHandle* h, const DemParticleState* in);
  * state).  Single-scene handles.  With `in` and `out` in page-locked host (or
  * device) memory and the integrator split over four warps per 32 particles
  * (scenes of up to 256 particles per SM), the host-link traffic overlaps the
- * step: the positions are uploaded first and the velocities and spins beside
- * the contact update (a one-step call replays one captured graph per set of
- * buffers), the first step's integrator reads the orientations and the first
- * wall's shear history from `in`, and the last step's integrator writes the
- * state into `out` block by block as it finishes (DemStats.exchanges_direct
- * counts these calls).  `in` and `out` may be the same buffers. */
+ * step: the positions are uploaded first, the other fields beside the
+ * contact update (a one-step call replays one captured graph per set of
+ * buffers; in a call of several steps the velocities and spins go with the
+ * positions and the first step's integrator reads the orientations and the
+ * first wall's shear history from `in`), and the last step's integrator
+ * writes the state into `out` block by block as it finishes
+ * (DemStats.exchanges_direct counts these calls).  `in` and `out` may be the
+ * same buffers. */
 int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
                       DemParticleState* out);
 

@@ -1745,8 +1745,8 @@ int dem_set_particles_async(DemHandle* h, const DemParticleState* in) {
 
 // One exchanged step as a graph (DemHandle::XGraph): captured once per
 // contact-buffer parity and set of caller buffers, replayed afterwards.
-static int capture_exchange(DemHandle* h, int cur, double* pv, double* vv, double* ov,
-                     const HostOut& ho, cudaGraphExec_t* exec) {
+static int capture_exchange(DemHandle* h, int cur, double* pv, double* vv, double* ov, double* qv,
+                            double* wv, const HostOut& ho, cudaGraphExec_t* exec) {
     if (!h->side) {
         CU(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
         CU(cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
@@ -1763,14 +1763,18 @@ static int capture_exchange(DemHandle* h, int cur, double* pv, double* vv, doubl
     xp.nf = 1;
     xp.arm = 1;
     xp.hout = ho;
-    XferSet xr{};  // velocities and spins, beside the contact update (which reads neither)
-    double* const rv[2] = {vv, ov};
-    double* const cv[2][3] = {{d.vx, d.vy, d.vz}, {d.wx, d.wy, d.wz}};
-    for (int f = 0; f < 2; ++f) {
+    // velocities, spins, orientations and the first wall's shear history,
+    // beside the contact update (which reads none of them)
+    XferSet xr{};
+    double* const rv[4] = {vv, ov, qv, wv};
+    double* const cv[4][4] = {{d.vx, d.vy, d.vz}, {d.wx, d.wy, d.wz}, {d.qw, d.qx, d.qy, d.qz},
+                              {d.wsx, d.wsy, d.wsz}};
+    const int kv[4] = {3, 3, 4, 3};
+    for (int f = 0; f < 4; ++f) {
         if (!rv[f]) continue;
         xr.rec[xr.nf] = rv[f];
-        for (int c = 0; c < 3; ++c) xr.col[xr.nf][c] = cv[f][c];
-        xr.k[xr.nf] = 3;
+        for (int c = 0; c < kv[f]; ++c) xr.col[xr.nf][c] = cv[f][c];
+        xr.k[xr.nf] = kv[f];
         ++xr.nf;
     }
     CU(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -1832,11 +1836,13 @@ int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
     if (!h || nsteps < 0 || h->multi) return DEM_ERR_INVALID;
     HostOut ho{};
     const SceneHost* S = scene_at(h, 0);
-    // the split integrator (the step graph's layout for this scene) reads
-    // orientations and the first wall's shear history from `in` and writes
+    // the split integrator (the step graph's layout for this scene) writes
     // the state into `out` while it runs, instead of a separate read after
-    // the step; the upload before the step carries positions (and, in the
-    // graph of a single step, beside the contact update, velocities and spins)
+    // the step.  The upload before the step carries only the positions: in
+    // the graph of a single step the other fields are uploaded on a second
+    // stream beside the contact update; otherwise velocities and spins go
+    // with the positions, and the integrator of the first step reads the
+    // orientations and the first wall's shear history from `in` itself.
     if (in && in->pos && out && nsteps > 0 && nsteps <= INT_MAX && S && S->sp.n > 0 &&
         split_integrator(h->shape, h->p.n, h->p.sms) && fused_download(h, out, &ho)) {
         *reinterpret_cast<volatile int*>(h->err_host) = kNoHostOut;
@@ -1846,17 +1852,21 @@ int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
         double* const pv = device_view(in->pos);
         double* const vv = in->vel ? device_view(in->vel) : nullptr;
         double* const ov = in->omega ? device_view(in->omega) : nullptr;
+        double* const qv = in->quat ? device_view(in->quat) : nullptr;
+        double* const wv = in->wall_shear ? device_view(in->wall_shear) : nullptr;
         int rc = DEM_OK;
-        if (nsteps == 1 && pv && (!in->vel || vv) && (!in->omega || ov)) {
+        if (nsteps == 1 && pv && (!in->vel || vv) && (!in->omega || ov) && (!in->quat || qv) &&
+            (!in->wall_shear || wv)) {
+            ho.qin = ho.wsin = nullptr;  // uploaded beside the contact update
             rc = ensure_encoding(h);
             if (rc == DEM_OK) rc = build_graphs(h);
-            const void* key[DemHandle::kXKey] = {pv, vv, ov, ho.qin, ho.wsin, ho.err};
+            const void* key[DemHandle::kXKey] = {pv, vv, ov, qv, wv, ho.err};
             for (int q = 0; q < kHostOutFields; ++q) key[6 + q] = ho.rec[q];
             DemHandle::XGraph& X = h->xg[h->cur];
             if (rc == DEM_OK && (!X.exec || std::memcmp(X.key, key, sizeof(key)) != 0)) {
                 if (X.exec) cudaGraphExecDestroy(X.exec);
                 X.exec = nullptr;
-                rc = capture_exchange(h, h->cur, pv, vv, ov, ho, &X.exec);
+                rc = capture_exchange(h, h->cur, pv, vv, ov, qv, wv, ho, &X.exec);
                 if (rc == DEM_OK) std::memcpy(X.key, key, sizeof(key));
             }
             if (rc == DEM_OK) {
