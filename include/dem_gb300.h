@@ -375,7 +375,8 @@ int dem_set_particles_async(DemHandle* h, const DemParticleState* in);
  * first wall's shear history from `in`), and the last step's integrator
  * writes the state into `out` block by block as it finishes
  * (DemStats.exchanges_direct counts these calls).  `in` and `out` may be the
- * same buffers. */
+ * same buffers; a one-step exchange in place then leaves out the values the
+ * step did not change (bit for bit), which the buffers hold already. */
 int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
                       DemParticleState* out);
 

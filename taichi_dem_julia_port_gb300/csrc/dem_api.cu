@@ -391,7 +391,7 @@ struct DemHandle {
     // uploads velocities and spins, then forces and the integration (which
     // reads orientations and wall shear from the caller and writes the state
     // back into the caller's buffers)
-    static constexpr int kXKey = 13;
+    static constexpr int kXKey = 14;
     struct XGraph {
         cudaGraphExec_t exec = nullptr;
         const void* key[kXKey] = {};
@@ -1847,6 +1847,14 @@ int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
         split_integrator(h->shape, h->p.n, h->p.sms) && fused_download(h, out, &ho)) {
         *reinterpret_cast<volatile int*>(h->err_host) = kNoHostOut;
         ho.steps_left = ho.steps_total = (int)nsteps;
+        // a one-step exchange in place: values the step leaves unchanged are
+        // in `out` already (the step's input of that field came from there)
+        const double* const inrec[kHostOutFields] = {in->pos, in->vel, in->omega, in->quat,
+                                                     nullptr, nullptr, in->wall_shear};
+        ho.same = 0u;
+        if (nsteps == 1)
+            for (int q = 0; q < kHostOutFields; ++q)
+                if (inrec[q] && ho.rec[q] && device_view(inrec[q]) == ho.rec[q]) ho.same |= 1u << q;
         ho.qin = in->quat ? device_view(in->quat) : nullptr;
         ho.wsin = in->wall_shear ? device_view(in->wall_shear) : nullptr;
         double* const pv = device_view(in->pos);
@@ -1860,8 +1868,9 @@ int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
             ho.qin = ho.wsin = nullptr;  // uploaded beside the contact update
             rc = ensure_encoding(h);
             if (rc == DEM_OK) rc = build_graphs(h);
-            const void* key[DemHandle::kXKey] = {pv, vv, ov, qv, wv, ho.err};
-            for (int q = 0; q < kHostOutFields; ++q) key[6 + q] = ho.rec[q];
+            const void* key[DemHandle::kXKey] = {pv, vv, ov, qv, wv, ho.err,
+                                                 reinterpret_cast<const void*>((uintptr_t)ho.same)};
+            for (int q = 0; q < kHostOutFields; ++q) key[7 + q] = ho.rec[q];
             DemHandle::XGraph& X = h->xg[h->cur];
             if (rc == DEM_OK && (!X.exec || std::memcmp(X.key, key, sizeof(key)) != 0)) {
                 if (X.exec) cudaGraphExecDestroy(X.exec);

@@ -157,6 +157,10 @@ struct HostOut {
     int* err;
     int steps_left, steps_total;
     unsigned int done;
+    // bit f: record f is the same memory as the step's input of that field
+    // (a one-step exchange in place), so values the step left bit for bit
+    // unchanged are already there and are not written again
+    unsigned int same;
 };
 
 struct DevCounters {

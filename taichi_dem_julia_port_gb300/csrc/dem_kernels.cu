@@ -2542,6 +2542,7 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
     // rows of the output records (HostOut), and the first armed step's
     // orientations and first-wall shear histories read from the caller's
     __shared__ double s_out[MULTI ? 1 : kHostOutRows][32];
+    __shared__ uint8_t s_chg[MULTI ? 1 : kHostOutRows][32];  // value differs from the input
     __shared__ double s_in[MULTI ? 1 : 7][32];
     // 0, 1, 2: component; 3: walls and quaternion.  The roles rotate with
     // the block's round over the SMs: warp w of a block runs on SM
@@ -2662,6 +2663,11 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
                           S.pw_cgn, S.pw_cgt};
             }
             double g[3], mw[3];
+            if (out && wl == 0) {  // the first wall's shear history before the step
+                s_out[19][l] = d.wsx[o];
+                s_out[20][l] = d.wsy[o];
+                s_out[21][l] = d.wsz[o];
+            }
             const bool touch = wall_force(d, sc, K, dt, p32, r32, x, y, z, vx, vy, vz, wx, wy, wz,
                                           r, d.m[i], d.wsx + o, d.wsy + o, d.wsz + o, g, mw, true);
             s_touch[wl][l] = touch ? 1 : 0;
@@ -2674,9 +2680,16 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
             }
         }
         if (out) {  // the first wall's shear history as this thread left it
-            s_out[19][l] = d.wsx[i];
-            s_out[20][l] = d.wsy[i];
-            s_out[21][l] = d.wsz[i];
+            const double* ws[3] = {d.wsx, d.wsy, d.wsz};
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const double v = ws[c][i];
+                // without walls nothing changed it (the value before the
+                // step is not staged then)
+                s_chg[19 + c][l] = nwall > 0 && __double_as_longlong(v) !=
+                                                    __double_as_longlong(s_out[19 + c][l]);
+                s_out[19 + c][l] = v;
+            }
         }
     }
     __syncthreads();  // walls in shared memory; every component thread has read in_cnt
@@ -2720,6 +2733,10 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
             s_out[10][l] = ox;
             s_out[11][l] = oy;
             s_out[12][l] = oz;
+            s_chg[9][l] = __double_as_longlong(ow) != __double_as_longlong(qw);
+            s_chg[10][l] = __double_as_longlong(ox) != __double_as_longlong(qx);
+            s_chg[11][l] = __double_as_longlong(oy) != __double_as_longlong(qy);
+            s_chg[12][l] = __double_as_longlong(oz) != __double_as_longlong(qz);
         }
     }
     if (q < 3 && live) {
@@ -2761,6 +2778,9 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
             s_out[6 + q][l] = wq1;
             s_out[13 + q][l] = Fq;
             s_out[16 + q][l] = Mq;
+            s_chg[q][l] = __double_as_longlong(pq1) != __double_as_longlong(xq);
+            s_chg[3 + q][l] = __double_as_longlong(vq1) != __double_as_longlong(vq);
+            s_chg[6 + q][l] = __double_as_longlong(wq1) != __double_as_longlong(wq);
         }
     }
     __syncthreads();  // the new position components (and an armed step's rows) in shared memory
@@ -2779,15 +2799,17 @@ __device__ __forceinline__ void integrate_split(const DemDev& d, const DemParams
                 // the block's 32 particles are one contiguous range of each
                 // record array: k·32 values, written by consecutive threads
                 const int i0 = blockIdx.x * 32, m = min(32, p.n - i0);
+                const unsigned same = d.ctr->hout.same;
                 int row = 0;
 #pragma unroll
                 for (int f = 0; f < kHostOutFields; ++f) {
                     const int k = f == 3 ? 4 : 3;
                     double* rec = d.ctr->hout.rec[f];
+                    const bool keep = (same >> f) & 1u;  // unchanged values are there already
                     if (rec) {
                         for (int e = threadIdx.x; e < k * 32; e += kSplitThreads) {
-                            const int pq = e / k;
-                            if (pq < m) rec[(size_t)k * i0 + e] = s_out[row + e - pq * k][pq];
+                            const int pq = e / k, r = row + e - pq * k;
+                            if (pq < m && (!keep || s_chg[r][pq])) rec[(size_t)k * i0 + e] = s_out[r][pq];
                         }
                     }
                     row += k;

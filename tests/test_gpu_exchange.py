@@ -120,6 +120,31 @@ def test_exchange_takes_the_callers_changes(gpu, per_call):
         np.testing.assert_array_equal(runs[1][k], runs[0][k], err_msg=k)
 
 
+def test_exchange_into_other_buffers(gpu):
+    """Input and output in different page-locked buffers: the output receives
+    every value (an exchange in place leaves out the values the step did not
+    change, which the buffer holds already), and the input is not written."""
+    import ctypes as C
+    sc = scenes.bonded_cube(8, speed=30.0, steps=0, seed=2)
+    want, _ = plain_run(sc.cfg, sc.particles, 400)
+    g = GlobalData(sc.cfg, sc.particles)
+    g.initialize()
+    g.simulate(399)
+    src, dst = g.state_buffers(forces=True), g.state_buffers(forces=True)
+    before = {k: getattr(src, k).copy() for k in FIELDS}
+    for k in FIELDS:  # stale values everywhere in the output buffer
+        getattr(dst, k)[:] = -7.0
+    rc = g.lib.dem_step_exchange(g.h, C.byref(src._in), 1, C.byref(dst._out))
+    assert rc == 0
+    for k in FIELDS:
+        np.testing.assert_array_equal(getattr(dst, k), want[k], err_msg=k)
+        np.testing.assert_array_equal(getattr(src, k), before[k], err_msg=k)
+    assert g.stats()["exchanges_direct"] == 1
+    src.close()
+    dst.close()
+    g.close()
+
+
 def test_exchange_reports_a_device_error(gpu):
     """A contact-capacity overflow in the exchanged step reaches the caller
     through the error word that the integrator copies with the state."""
