@@ -1847,21 +1847,20 @@ int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
         split_integrator(h->shape, h->p.n, h->p.sms) && fused_download(h, out, &ho)) {
         *reinterpret_cast<volatile int*>(h->err_host) = kNoHostOut;
         ho.steps_left = ho.steps_total = (int)nsteps;
-        // a one-step exchange in place: values the step leaves unchanged are
-        // in `out` already (the step's input of that field came from there)
-        const double* const inrec[kHostOutFields] = {in->pos, in->vel, in->omega, in->quat,
-                                                     nullptr, nullptr, in->wall_shear};
-        ho.same = 0u;
-        if (nsteps == 1)
-            for (int q = 0; q < kHostOutFields; ++q)
-                if (inrec[q] && ho.rec[q] && device_view(inrec[q]) == ho.rec[q]) ho.same |= 1u << q;
-        ho.qin = in->quat ? device_view(in->quat) : nullptr;
-        ho.wsin = in->wall_shear ? device_view(in->wall_shear) : nullptr;
         double* const pv = device_view(in->pos);
         double* const vv = in->vel ? device_view(in->vel) : nullptr;
         double* const ov = in->omega ? device_view(in->omega) : nullptr;
         double* const qv = in->quat ? device_view(in->quat) : nullptr;
         double* const wv = in->wall_shear ? device_view(in->wall_shear) : nullptr;
+        // a one-step exchange in place: values the step leaves unchanged are
+        // in `out` already (the step's input of that field came from there)
+        const double* const inv[kHostOutFields] = {pv, vv, ov, qv, nullptr, nullptr, wv};
+        ho.same = 0u;
+        if (nsteps == 1)
+            for (int q = 0; q < kHostOutFields; ++q)
+                if (inv[q] && inv[q] == ho.rec[q]) ho.same |= 1u << q;
+        ho.qin = qv;
+        ho.wsin = wv;
         int rc = DEM_OK;
         if (nsteps == 1 && pv && (!in->vel || vv) && (!in->omega || ov) && (!in->quat || qv) &&
             (!in->wall_shear || wv)) {
