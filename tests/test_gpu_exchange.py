@@ -145,6 +145,36 @@ def test_exchange_into_other_buffers(gpu):
     g.close()
 
 
+def test_exchange_alternating_buffers(gpu):
+    """Two buffer sets used in turn (each captured exchange graph belongs to
+    one set), with a launch-shape change and a skin change in between that
+    drop the captured graphs: the state stays that of uninterrupted stepping."""
+    sc = scenes.bonded_cube(8, speed=30.0, steps=0, seed=2)
+    steps = 240
+    want, _ = plain_run(sc.cfg, sc.particles, steps)
+    g = GlobalData(sc.cfg, sc.particles)
+    g.initialize()
+    bufs = [g.state_buffers(forces=True), g.state_buffers(forces=True)]
+    cur = bufs[0]
+    for s in range(steps):
+        nxt = bufs[s % 2]
+        if nxt is not cur:
+            for k in FIELDS:
+                getattr(nxt, k)[:] = getattr(cur, k)
+            cur = nxt
+        if s == 80:
+            g.set_launch_shape(force_block=64)
+        if s == 160:
+            g.set_skin_factor(0.5)
+        cur.step(1)
+    for k in FIELDS:
+        np.testing.assert_array_equal(getattr(cur, k), want[k], err_msg=k)
+    assert g.stats()["exchanges_direct"] == steps
+    for b in bufs:
+        b.close()
+    g.close()
+
+
 def test_exchange_reports_a_device_error(gpu):
     """A contact-capacity overflow in the exchanged step reaches the caller
     through the error word that the integrator copies with the state."""
