@@ -402,6 +402,7 @@ struct DemHandle {
     // after its three kernels, per contact-buffer parity
     cudaGraphExec_t pg[2] = {nullptr, nullptr};
     cudaEvent_t pev[4] = {nullptr, nullptr, nullptr, nullptr};
+    unsigned long long* counts = nullptr;  // dem_get_stats: a scene's active contacts, bonds
     int32_t* io_idx = nullptr;  // p4c records: per-slot counts and their scan (2n + 1)
     int64_t io_idx_n = 0;
     void* io_rec = nullptr;     // p4c records (64 bytes each)
@@ -533,6 +534,8 @@ void free_all(DemHandle* h) {
     h->xfer = nullptr;
     if (h->io_idx) cudaFree(h->io_idx);
     h->io_idx = nullptr;
+    if (h->counts) cudaFree(h->counts);
+    h->counts = nullptr;
     if (h->io_rec) cudaFree(h->io_rec);
     h->io_rec = nullptr;
     if (h->err_host) cudaFreeHost(h->err_host);
@@ -1202,11 +1205,15 @@ int stats_of(DemHandle* h, int32_t s, const SceneHost& S, DemStats* out) {
     TRY(read_counters(h, &c));
     SceneCounters sc{};
     CU(cudaMemcpy(&sc, h->d.sctr + s, sizeof(sc), cudaMemcpyDeviceToHost));
-    RangeContacts R;
-    TRY(range_contacts(h, S.sp.p0, S.sp.n, R));
-    const int64_t act = (int64_t)R.act.size();
-    int64_t bnd = 0;
-    for (int32_t k : R.act) bnd += (R.fl[k] & kBonded) ? 1 : 0;
+    // the scene's active contacts and bonds, counted on the device
+    if (!h->counts) CU(cudaMalloc(&h->counts, 2 * sizeof(unsigned long long)));
+    unsigned long long cnt[2] = {0ull, 0ull};
+    CU(cudaMemsetAsync(h->counts, 0, sizeof(cnt), h->stream));
+    launch_range_counts(h->d, h->cur, h->c_cap, (int)S.sp.p0, (int)S.sp.n, h->counts, h->stream);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(cnt, h->counts, sizeof(cnt), cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaStreamSynchronize(h->stream));
+    const int64_t act = (int64_t)cnt[0], bnd = (int64_t)cnt[1];
     std::memset(out, 0, sizeof(*out));
     out->n_particles = S.sp.n;
     out->steps_done = h->multi ? S.steps : h->steps;

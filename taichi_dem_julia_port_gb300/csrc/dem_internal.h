@@ -311,6 +311,9 @@ void launch_integrate(const DemDev& d, const DemParams& p, int cur, bool multi,
 // relative to p0; 𝐅ᵢ decoded from FP32 hi/lo pairs when `pairs`)
 void launch_io_count(const DemDev& d, int cur, int cap, int p0, int n, int32_t* cnt,
                      cudaStream_t s);
+// active contacts and bonds owned by slots [p0, p0 + n), added into tot[0..1]
+void launch_range_counts(const DemDev& d, int cur, int cap, int p0, int n,
+                         unsigned long long* tot, cudaStream_t s);
 void launch_io_fill(const DemDev& d, int cur, int cap, int p0, int n, const int32_t* off,
                     bool pairs, void* out, cudaStream_t s);
 

@@ -3119,6 +3119,40 @@ __global__ void k_io_fill(DemDev d, int cur, int cap, int p0, int n, const int32
         out[q++] = r;
     }
 }
+// Active contacts and active bonds owned by slots [p0, p0 + n) (the scene
+// counters of dem_get_stats), added into tot[0] and tot[1].
+__global__ void k_range_counts(DemDev d, int cur, int cap, int p0, int n,
+                               unsigned long long* tot) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned act = 0, bnd = 0;
+    if (t < n) {
+        const int i = p0 + t;
+        int e0, e1;
+        io_row(d, cur, cap, i, e0, e1);
+        const ContactSoA w = d.c[cur];
+        for (int e = e0; e < e1; ++e) {
+            const uint32_t fl = w.fl[e];
+            if ((fl & kActive) && w.ci[e] == i) {
+                ++act;
+                bnd += (fl & kBonded) ? 1u : 0u;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        act += __shfl_down_sync(0xffffffffu, act, o);
+        bnd += __shfl_down_sync(0xffffffffu, bnd, o);
+    }
+    if (lane_id() == 0 && (act | bnd)) {
+        atomicAdd(&tot[0], (unsigned long long)act);
+        atomicAdd(&tot[1], (unsigned long long)bnd);
+    }
+}
+void launch_range_counts(const DemDev& d, int cur, int cap, int p0, int n,
+                         unsigned long long* tot, cudaStream_t s) {
+    if (n <= 0) return;
+    k_range_counts<<<blocks_for(n, kThreads), kThreads, 0, s>>>(d, cur, cap, p0, n, tot);
+}
 void launch_io_count(const DemDev& d, int cur, int cap, int p0, int n, int32_t* cnt,
                      cudaStream_t s) {
     if (n <= 0) return;

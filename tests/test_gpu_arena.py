@@ -440,3 +440,29 @@ def test_list_update_large_scenes(gpu):
         a.step(steps)
         assert_same(a, ids[0], fulls[0], "arena pour")
         assert_same(a, ids[1], small_ref, "arena small cube")
+
+
+def test_stats_counts_equal_the_contact_read(gpu):
+    """dem_get_stats counts a scene's active contacts and bonds on the device:
+    they equal the counts of the full contact read, for a single scene and for
+    each scene of an arena (bonds broken, Hertz contacts, scenes side by side)."""
+    cube = scenes.bonded_cube(8, speed=30.0, steps=0, seed=2)
+    g = GlobalData(cube.cfg, cube.particles)
+    g.initialize()
+    g.simulate(1000)  # bonds start to break near step 900
+    st, c = g.stats(), g.contacts()
+    assert st["bonds_broken"] > 0 and np.count_nonzero(c["bonded"] == 0) > 0
+    assert st["contacts"] == len(c["i"]) and st["bonded"] == int(np.count_nonzero(c["bonded"]))
+    g.close()
+    with Arena(20000, max_scenes=4) as a:
+        ids = [a.add(small_cube().cfg, small_cube().particles),
+               a.add(cube.cfg, cube.particles),
+               a.add(small_pour(800, seed=74).cfg, small_pour(800, seed=74).particles,
+                     init_bonds=False)]
+        a.step(1000)
+        for s in ids:
+            st, c = a.stats(s), a.contacts(s)
+            assert st["contacts"] == len(c["i"]), s
+            assert st["bonded"] == int(np.count_nonzero(c["bonded"])), s
+        assert a.stats(ids[1])["bonds_broken"] > 0
+        assert a.stats(ids[2])["contacts"] > 0
