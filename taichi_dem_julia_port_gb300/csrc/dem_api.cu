@@ -13,6 +13,7 @@
 #include <map>
 #include <mutex>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "dem_gb300.h"
@@ -200,6 +201,31 @@ struct SceneArrays {
 uint32_t pow2_mask(uint32_t H) { return (H & (H - 1)) == 0 ? H - 1 : 0u; }
 
 // The grain set-up and derived values of `solve` (src/executor.jl:217-315).
+// The per-grain constants of `solve` (src/executor.jl:223-242) for grain i,
+// and the largest radius so far.
+static void grain_constants(const DemConfigC* cfg, const DemParticlesIn* pin, SceneArrays& A,
+                            int i, double& rmax_r) {
+    const double V = pin->volume[i], m = pin->mass[i];
+    A.m[i] = m;
+    A.r[i] = std::cbrt(V / (4.0 / 3.0 * kPi));
+    A.r0[i] = A.r[i] * cfg->particle_contact_radius_multiplier;
+    A.inv_inertia[i] = 1.0 / (2.0 / 5.0 * m * (A.r[i] * A.r[i]));
+    A.inv_m[i] = 1.0 / m;
+    // bond section of src/kernels.jl:178-184 for rb = ρ·rᵢ
+    const double rb = cfg->bond_radius_ratio * A.r[i];
+    const double Ab = rb * rb * kPi, Ib = rb * rb * (rb * rb) * (kPi / 4.0);
+    A.b_invA[i] = 1.0 / Ab;
+    A.b_rbI[i] = rb / Ib;
+    A.b_EA[i] = cfg->bond_elastic_modulus * Ab;
+    A.b_EI[i] = cfg->bond_elastic_modulus * Ib;
+    A.b_phic[i] = 20.0 / 3.0 * (1.0 + cfg->bond_poisson_ratio) * (rb * rb);
+    rmax_r = std::max(rmax_r, A.r[i]);
+    for (int c = 0; c < 3; ++c) {
+        A.pos[c][i] = pin->pos[3 * i + c];
+        A.vel[c][i] = pin->vel[3 * i + c];
+    }
+}
+
 int prepare_scene(const DemConfigC* cfg, const DemParticlesIn* pin, double cell_factor,
                   SceneHost& S, SceneArrays& A) {
     g_invalid[0] = 0;
@@ -215,39 +241,51 @@ int prepare_scene(const DemConfigC* cfg, const DemParticlesIn* pin, double cell_
         A.pos[c].resize(n);
         A.vel[c].resize(n);
     }
-    double rmax_r = -INFINITY;
-    for (int i = 0; i < n; ++i) {
-        const double V = pin->volume[i], m = pin->mass[i];
-        // a grain needs a positive finite volume and mass and a finite position
-        // and velocity: anything else would make NaN cells and forces
-        bool ok = V > 0 && m > 0 && std::isfinite(V) && std::isfinite(m);
-        for (int c = 0; c < 3; ++c)
-            ok = ok && std::isfinite(pin->pos[3 * i + c]) && std::isfinite(pin->vel[3 * i + c]);
-        if (!ok) {
+    // per grain, independently: split over host threads for large scenes
+    // (the results do not depend on the split)
+    auto grains = [&](int i0, int i1, double& rmax, int& bad) {
+        for (int i = i0; i < i1; ++i) {
+            const double V = pin->volume[i], m = pin->mass[i];
+            // a grain needs a positive finite volume and mass and a finite
+            // position and velocity: anything else would make NaN cells and forces
+            bool ok = V > 0 && m > 0 && std::isfinite(V) && std::isfinite(m);
+            for (int c = 0; c < 3; ++c)
+                ok = ok && std::isfinite(pin->pos[3 * i + c]) && std::isfinite(pin->vel[3 * i + c]);
+            if (!ok) {
+                bad = i;  // the first in this range
+                return;
+            }
+            grain_constants(cfg, pin, A, i, rmax);
+        }
+    };
+    const int nth = n < (1 << 16) ? 1
+                                  : (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<double> rmaxs(nth, -INFINITY);
+    std::vector<int> bads(nth, -1);
+    {
+        std::vector<std::thread> pool;
+        const int64_t per = ((int64_t)n + nth - 1) / nth;
+        for (int t = 1; t < nth; ++t) {
+            const int i0 = (int)std::min<int64_t>(n, t * per);
+            const int i1 = (int)std::min<int64_t>(n, (t + 1) * per);
+            try {
+                pool.emplace_back(grains, i0, i1, std::ref(rmaxs[t]), std::ref(bads[t]));
+            } catch (...) {  // no thread to be had: this one does the range
+                grains(i0, i1, rmaxs[t], bads[t]);
+            }
+        }
+        grains(0, (int)std::min<int64_t>(n, per), rmaxs[0], bads[0]);
+        for (auto& th : pool) th.join();
+    }
+    for (int t = 0; t < nth; ++t)
+        if (bads[t] >= 0) {
             std::snprintf(g_invalid, sizeof(g_invalid),
                           "grain %d: volume, mass, position and velocity must be finite "
-                          "(volume and mass > 0)", i);
+                          "(volume and mass > 0)", bads[t]);
             return DEM_ERR_INVALID;
         }
-        A.m[i] = m;
-        A.r[i] = std::cbrt(V / (4.0 / 3.0 * kPi));
-        A.r0[i] = A.r[i] * cfg->particle_contact_radius_multiplier;
-        A.inv_inertia[i] = 1.0 / (2.0 / 5.0 * m * (A.r[i] * A.r[i]));
-        A.inv_m[i] = 1.0 / m;
-        // bond section of src/kernels.jl:178-184 for rb = ρ·rᵢ
-        const double rb = cfg->bond_radius_ratio * A.r[i];
-        const double Ab = rb * rb * kPi, Ib = rb * rb * (rb * rb) * (kPi / 4.0);
-        A.b_invA[i] = 1.0 / Ab;
-        A.b_rbI[i] = rb / Ib;
-        A.b_EA[i] = cfg->bond_elastic_modulus * Ab;
-        A.b_EI[i] = cfg->bond_elastic_modulus * Ib;
-        A.b_phic[i] = 20.0 / 3.0 * (1.0 + cfg->bond_poisson_ratio) * (rb * rb);
-        rmax_r = std::max(rmax_r, A.r[i]);
-        for (int c = 0; c < 3; ++c) {
-            A.pos[c][i] = pin->pos[3 * i + c];
-            A.vel[c][i] = pin->vel[3 * i + c];
-        }
-    }
+    double rmax_r = -INFINITY;
+    for (double v : rmaxs) rmax_r = std::max(rmax_r, v);
     // derived sizes (src/executor.jl:244-267)
     DemDerived& D = S.der;
     D.material_density = n ? pin->mass[n - 1] / pin->volume[n - 1] : 0.0;

@@ -235,3 +235,27 @@ def test_bench_byte_model_for_the_cube_window():
     # a settling pour without contacts writes neither spin nor quaternion
     assert bench.algorithmic_bytes(1000, 0, 0, settling=True)["integrate"] == 1000 * (360 - 56)
     assert bench.algorithmic_bytes(1000, 0, 0)["force"] == 0
+
+
+def test_first_bad_grain_named_in_a_large_scene(dem_lib_path):
+    """Scene set-up checks every grain on the host before any device call,
+    over several threads for large scenes (200,000 grains here), and names the
+    first bad grain whichever thread finds it."""
+    from taichi_dem_julia_port_gb300 import GlobalData
+    from taichi_dem_julia_port_gb300.scenes import ParticleInput
+    n = 200_000
+    rng = np.random.default_rng(3)
+    r = np.full(n, 1e-3)
+    pos = rng.uniform(0.0, 0.2, (n, 3))
+    cfg = DEMConfig(domain_min=[-0.01] * 3, domain_max=[0.21] * 3)
+    for bad in ([150_001, 190_000], [7, 150_001], [199_999]):
+        p = ParticleInput.from_arrays(r, pos.copy(), np.zeros((n, 3)), 2500.0)
+        for k, i in enumerate(bad):
+            if k % 2:
+                p.volume[i] = -1.0
+            else:
+                p.pos[i, 2] = np.nan
+        with pytest.raises(_abi.DemError) as e:
+            GlobalData(cfg, p, lib=_abi.load_library(dem_lib_path))
+        assert e.value.code == _abi.DEM_ERR_INVALID
+        assert f"grain {bad[0]}:" in str(e.value), str(e.value)
