@@ -392,6 +392,20 @@ __global__ void k_fill_i32(int32_t* a, int64_t n, int32_t v) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] = v;
 }
+// A new scene's slots [p0, p0 + n) after its FP64 columns are uploaded: the
+// identity orientation's w and the FP32 copies of the bond-section constants
+// and of (rb/I, m, r) for the FP32 force mode, rounded to nearest as a host
+// cast would round them.
+__global__ void k_scene_columns(DemDev d, int64_t p0, int64_t n) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int64_t i = p0 + t;
+    d.qw[i] = 1.0;
+    d.bk32[i] = make_float4(__double2float_rn(d.b_phic[i]), __double2float_rn(d.b_EI[i]),
+                            __double2float_rn(d.b_EA[i]), __double2float_rn(d.b_invA[i]));
+    d.rm32[i] = make_float4(__double2float_rn(d.b_rbI[i]), __double2float_rn(d.m[i]),
+                            __double2float_rn(d.r[i]), 0.0f);
+}
 
 }  // namespace
 
@@ -646,19 +660,8 @@ int upload_scene(DemHandle* h, const SceneArrays& A, int64_t p0) {
         {d.b_EI, &A.b_EI},
         {d.b_phic, &A.b_phic}};
     for (const auto& c : cols) CU(up(c.first, *c.second));
-    std::vector<double> one(n, 1.0);
-    CU(up(d.qw, one));
-    std::vector<float4> bk(n);
-    std::vector<float4> rm(n);
-    for (size_t i = 0; i < n; ++i) {
-        bk[i] = make_float4((float)A.b_phic[i], (float)A.b_EI[i], (float)A.b_EA[i],
-                            (float)A.b_invA[i]);
-        rm[i] = make_float4((float)A.b_rbI[i], (float)A.m[i], (float)A.r[i], 0.0f);
-    }
-    CU(cudaMemcpyAsync(d.bk32 + p0, bk.data(), n * sizeof(float4), cudaMemcpyHostToDevice,
-                       h->stream));
-    CU(cudaMemcpyAsync(d.rm32 + p0, rm.data(), n * sizeof(float4), cudaMemcpyHostToDevice,
-                       h->stream));
+    k_scene_columns<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(d, p0, (int64_t)n);
+    CU(cudaGetLastError());
     for (double* z : {d.wx, d.wy, d.wz, d.qx, d.qy, d.qz, d.wsx, d.wsy, d.wsz, d.fx, d.fy, d.fz,
                       d.tx, d.ty, d.tz})
         CU(cudaMemsetAsync(z + p0, 0, n * sizeof(double), h->stream));
