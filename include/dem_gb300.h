@@ -376,13 +376,16 @@ int dem_set_particles_async(DemHandle* h, const DemParticleState* in);
  * writes the state into `out` block by block as it finishes
  * (DemStats.exchanges_direct counts these calls).  `in` and `out` may be the
  * same buffers; a one-step exchange in place then leaves out the values the
- * step did not change (bit for bit), which the buffers hold already. */
+ * step did not change (bit for bit), which the buffers hold already.
+ * Replaces `simulate!` (src/executor.jl:162-172) with the host copy of the
+ * grains around it (`Array(grains)`, src/utils.jl:40) done every step. */
 int dem_step_exchange(DemHandle* h, const DemParticleState* in, int64_t nsteps,
                       DemParticleState* out);
 
 /* Page-locked host memory for state buffers (cudaMallocHost / cudaFreeHost),
  * for callers without a CUDA runtime of their own.  The library remembers
- * these ranges, so exchanges with them skip the per-buffer pointer query. */
+ * these ranges, so exchanges with them skip the per-buffer pointer query.
+ * No counterpart in the reference (CUDA.jl owns its host copies). */
 int dem_host_alloc(int64_t bytes, void** out);
 int dem_host_free(void* p);
 
