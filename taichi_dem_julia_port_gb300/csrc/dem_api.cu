@@ -1831,13 +1831,16 @@ static int capture_exchange(DemHandle* h, int cur, double* pv, double* vv, doubl
         if (e == cudaSuccess) e = r;
         return e == cudaSuccess;
     };
-    if (xr.nf && ok(cudaEventRecord(h->fork_ev, h->stream)) &&
+    // the positions first, with the host link to themselves (the contact
+    // update waits for them); the rest from then on, beside the contact update
+    launch_xfer_pos(xp, n, d, h->p, 0, cur, h->stream);
+    ok(cudaGetLastError());
+    if (e == cudaSuccess && xr.nf && ok(cudaEventRecord(h->fork_ev, h->stream)) &&
         ok(cudaStreamWaitEvent(h->side, h->fork_ev, 0))) {
         launch_xfer(xr, n, 0, true, h->side);
         if (ok(cudaGetLastError())) ok(cudaEventRecord(h->join_ev, h->side));
     }
     if (e == cudaSuccess) {
-        launch_xfer_pos(xp, n, d, h->p, 0, cur, h->stream);
         launch_search(d, h->p, cur, false, false, false, h->shape, h->stream);
         if (ok(cudaGetLastError()) && xr.nf) ok(cudaStreamWaitEvent(h->stream, h->join_ev, 0));
         if (e == cudaSuccess) {
