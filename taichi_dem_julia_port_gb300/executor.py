@@ -99,10 +99,11 @@ class StateBuffers:
     that writes the state, steps and reads it back every step.  The arrays
     (`pos`, `vel`, `omega`, `quat`, `wall_shear`, and with forces=True
     `force`, `moment`) are numpy views of page-locked memory that the
-    library's exchange kernel reads and writes in place; `upload()` is
-    asynchronous (the arrays must stay unchanged until the next `download()`
-    or other synchronising call), `download()` returns when the arrays hold
-    the device state."""
+    library's kernels read and write in place; `upload()` is asynchronous
+    (the arrays must stay unchanged until the next `download()` or other
+    synchronising call), `download()` returns when the arrays hold the device
+    state.  `step(1)` does both around a step and moves most of the state
+    while the step runs (dem_step_exchange)."""
 
     def __init__(self, g: "GlobalData", forces: bool = False):
         self._g = g
