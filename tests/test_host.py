@@ -42,6 +42,30 @@ def test_config_struct_matches_header():
     assert len(fields) == 32  # + init_particles = the 33 keys of DEMConfig
 
 
+@pytest.mark.parametrize("name", ["DemStats", "DemLaunchShape", "DemParticleState"])
+def test_result_structs_match_header(name, tmp_path):
+    """The ctypes mirrors of the header's result structs: same fields in the
+    same order, and the same size as the C compiler gives them."""
+    import shutil
+    import subprocess
+    src = (ROOT / "include" / "dem_gb300.h").read_text()
+    body = src[src.index(f"typedef struct {name} {{"):src.index(f"}} {name};")]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = re.findall(r"(?:double|int64_t|int32_t|int)\s*\*?\s*(\w+)\s*[;,\[]", body)
+    mirror = getattr(_abi, name)
+    assert fields == [f for f, _ in mirror._fields_]
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    prog = tmp_path / "size.c"
+    prog.write_text(f'#include "dem_gb300.h"\n#include <stdio.h>\n'
+                    f'int main(void) {{ printf("%zu", sizeof({name})); return 0; }}\n')
+    exe = tmp_path / "size"
+    subprocess.run([cc, "-I", str(ROOT / "include"), str(prog), "-o", str(exe)], check=True)
+    assert int(subprocess.run([str(exe)], capture_output=True, text=True).stdout) == \
+        ctypes.sizeof(mirror)
+
+
 def test_config_defaults_and_roundtrip(tmp_path):
     c = DEMConfig()
     assert c.dt == 2.63e-5 and c.max_coordinate_number == 64 and c.tolerance == 1e-12
